@@ -1,0 +1,147 @@
+"""Host-side wrapper of one GPU context of the C ABI."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+class GpuContext:
+    """One libaxia_gpu context: setup (symbolic) -> assemble (numeric) -> solve."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        st = C.c_int32(0)
+        self.h = self.lib.axia_gpu_create(device, C.byref(st))
+        if not self.h:
+            raise L.AxiaError(st.value, f"cannot create a context on CUDA device {device}")
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.axia_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, code, what=""):
+        if code != L.OK:
+            msg = self.lib.axia_gpu_last_error(self.h)
+            raise L.AxiaError(code, f"{what}: {msg.decode() if msg else ''}")
+
+    # -- element_ke ---------------------------------------------------------
+    def element_ke(self, xyz, e, nu, reduced=False):
+        """Batched element stiffness: xyz (n_elem, nn, 3), e (n_elem,) -> ke (n_elem, 3nn, 3nn), vol."""
+        xyz = _c(xyz, np.float64)
+        if xyz.ndim == 2:
+            xyz = xyz[None]
+        n_elem, nn = xyz.shape[0], xyz.shape[1]
+        e = _c(np.broadcast_to(np.asarray(e, np.float64), (n_elem,)), np.float64)
+        ke = np.zeros((n_elem, 3 * nn, 3 * nn))
+        vol = np.zeros(n_elem)
+        bad = C.c_int64(-1)
+        code = self.lib.axia_gpu_element_ke(self.h, nn, int(reduced), n_elem, L.ptr(xyz), L.ptr(e), float(nu),
+                                            L.ptr(ke), L.ptr(vol), C.byref(bad))
+        if code != L.OK:
+            err = L.AxiaError(code, self.lib.axia_gpu_last_error(self.h).decode())
+            err.bad_index = bad.value
+            raise err
+        return ke, vol
+
+    # -- model --------------------------------------------------------------
+    def setup(self, model):
+        self.model = model
+        self._coords = _c(model.coords, np.float64)
+        self._conn = _c(model.conn, np.int32)
+        self._e = _c(model.e_elem, np.float64)
+        self._bc_dof = _c(model.bc_dof, np.int64)
+        self._bc_val = _c(model.bc_val, np.float64)
+        m = L.Mesh(model.n_nodes, L.ptr(self._coords), model.n_elem, model.nn, int(model.reduced),
+                   L.ptr(self._conn), L.ptr(self._e), 0.0, float(model.nu))
+        self._check(self.lib.axia_gpu_setup(self.h, C.byref(m), self._bc_dof.shape[0], L.ptr(self._bc_dof),
+                                            L.ptr(self._bc_val)), "setup")
+        n, nnz = C.c_int64(), C.c_int64()
+        self.lib.axia_gpu_system_size(self.h, C.byref(n), C.byref(nnz))
+        self.n_free, self.nnz = n.value, nnz.value
+        return self
+
+    def assemble(self, precision=L.PREC_FP64):
+        self._check(self.lib.axia_gpu_assemble(self.h, int(precision)), "assemble")
+        return self
+
+    def load_vector(self, model=None):
+        """CLOAD vector plus the DLOAD face pressures (host, library routine)."""
+        model = model or self.model
+        f = np.array(model.cload, dtype=np.float64, copy=True)
+        if model.dload_elem.shape[0]:
+            bad = C.c_int64(-1)
+            el, fc, pp = _c(model.dload_elem, np.int64), _c(model.dload_face, np.int32), _c(model.dload_p, np.float64)
+            code = self.lib.axia_face_loads(model.nn, model.n_nodes, L.ptr(_c(model.coords, np.float64)),
+                                            L.ptr(_c(model.conn, np.int32)), el.shape[0], L.ptr(el), L.ptr(fc),
+                                            L.ptr(pp), L.ptr(f), C.byref(bad))
+            if code != L.OK:
+                raise L.AxiaError(code, f"face load {bad.value}")
+        return f
+
+    @staticmethod
+    def opts(rtol=1e-8, max_iter=0, precision=L.PREC_FP64, refine_mode=L.REFINE_RESTART, inner_rtol=1e-3,
+             max_outer=50, spmv_lanes=0):
+        return L.SolveOpts(rtol, max_iter, precision, refine_mode, inner_rtol, max_outer, spmv_lanes)
+
+    def set_stream(self, stream_handle: int | None):
+        """Issue the context's work on a caller's cudaStream_t (None: own stream)."""
+        self._check(self.lib.axia_gpu_set_stream(self.h, C.c_void_p(stream_handle or 0)), "set_stream")
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.axia_gpu_kernel_launches(self.h))
+
+    def spmv_device(self, precision, x_dev_ptr, y_dev_ptr, lanes=0):
+        self._check(self.lib.axia_gpu_spmv_device(self.h, int(precision), C.c_void_p(x_dev_ptr),
+                                                  C.c_void_p(y_dev_ptr), int(lanes)), "spmv")
+
+    def solve(self, f_full, **kw):
+        f = _c(f_full, np.float64)
+        u = np.zeros_like(f)
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        self._check(self.lib.axia_gpu_solve(self.h, L.ptr(f), L.ptr(u), C.byref(o), C.byref(info)), "solve")
+        return u, info
+
+    def solve_device(self, f_dev_ptr, u_dev_ptr, **kw):
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        self._check(self.lib.axia_gpu_solve_device(self.h, C.c_void_p(f_dev_ptr), C.c_void_p(u_dev_ptr), C.byref(o),
+                                                   C.byref(info)), "solve_device")
+        return info
+
+    def export_system(self):
+        """K_ff as (rowptr, col, val), the Jacobi diagonal and K_fp u0."""
+        rp = np.zeros(self.n_free + 1, np.int32)
+        col = np.zeros(self.nnz, np.int32)
+        val = np.zeros(self.nnz)
+        dg = np.zeros(self.n_free)
+        kf = np.zeros(self.n_free)
+        self._check(self.lib.axia_gpu_export_system(self.h, L.ptr(rp), L.ptr(col), L.ptr(val), L.ptr(dg), L.ptr(kf)),
+                    "export_system")
+        return rp, col, val, dg, kf
+
+    def export_dofmap(self):
+        out = np.zeros(3 * self.model.n_nodes, np.int32)
+        self._check(self.lib.axia_gpu_export_dofmap(self.h, L.ptr(out)), "export_dofmap")
+        return out

@@ -1,0 +1,380 @@
+// api.cu -- the extern "C" entry points declared in include/axia_gpu.h.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "element.cuh"
+
+int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0);
+int numeric_assemble(axia_ctx* ctx, bool want32);
+int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args);
+struct PcgOut;
+int pcg_solve(axia_ctx* ctx, const axia_solve_opts* opts, axia_solve_info* info);
+int ensure_pcg_state(axia_ctx* ctx);
+int build_rhs(axia_ctx* ctx, const double* d_f);
+int reconstruct(axia_ctx* ctx, double* d_u);
+int true_residual(axia_ctx* ctx, double* out);
+int spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req);
+
+namespace {
+
+struct EventTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaStream_t s;
+  explicit EventTimer(cudaStream_t st) : s(st) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+  }
+  double stop_ms() {
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+  ~EventTimer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+void free_mesh_state(axia_ctx* ctx) {
+  dev_free(ctx->d_coords);
+  dev_free(ctx->d_conn);
+  dev_free(ctx->d_e);
+  dev_free(ctx->d_ind_of);
+  dev_free(ctx->d_u0);
+  dev_free(ctx->d_ne_ptr);
+  dev_free(ctx->d_ne);
+  dev_free(ctx->d_adj_ptr);
+  dev_free(ctx->d_adj);
+  dev_free(ctx->d_adj_off);
+  dev_free(ctx->d_node_rowlen);
+  dev_free(ctx->d_rowptr);
+  dev_free(ctx->d_col);
+  dev_free(ctx->d_val);
+  dev_free(ctx->d_val32);
+  dev_free(ctx->d_diag);
+  dev_free(ctx->d_dinv);
+  dev_free(ctx->d_dinv32);
+  dev_free(ctx->d_kfu0);
+  dev_free(ctx->d_ke);
+  ctx->ke_elems = 0;
+  dev_free(ctx->d_f);
+  dev_free(ctx->d_u);
+  dev_free(ctx->d_b);
+  dev_free(ctx->d_x);
+  dev_free(ctx->d_r);
+  dev_free(ctx->d_p);
+  dev_free(ctx->d_q);
+  dev_free(ctx->d_b32);
+  dev_free(ctx->d_x32);
+  dev_free(ctx->d_r32);
+  dev_free(ctx->d_p32);
+  dev_free(ctx->d_q32);
+  ctx->vec_capacity = 0;
+  ctx->assembled = ctx->have32 = false;
+  ctx->n_free = ctx->nnz = 0;
+}
+
+int use_device(axia_ctx* ctx) {
+  AXIA_CUDA(ctx, cudaSetDevice(ctx->device));
+  ctx->last_error.clear();
+  return AXIA_OK;
+}
+
+void fill_info_sizes(const axia_ctx* ctx, axia_solve_info* info) {
+  info->n_free = ctx->n_free;
+  info->nnz = ctx->nnz;
+  info->ms_setup = ctx->ms_setup;
+  info->ms_assemble = ctx->ms_assemble;
+  info->bad_index = ctx->last_bad;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t axia_gpu_abi_version(void) { return AXIA_GPU_ABI_VERSION; }
+
+axia_ctx* axia_gpu_create(int32_t device, int32_t* status) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    if (status) *status = AXIA_ERR_CUDA;
+    return nullptr;
+  }
+  axia_ctx* ctx = new axia_ctx;
+  ctx->device = device;
+  int st = AXIA_OK;
+  do {
+    if (cudaSetDevice(device) != cudaSuccess) { st = AXIA_ERR_CUDA; break; }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) { st = AXIA_ERR_CUDA; break; }
+    if (!prop.cooperativeLaunch) { st = AXIA_ERR_CUDA; break; }
+    ctx->sm_count = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) { st = AXIA_ERR_CUDA; break; }
+    ctx->stream = ctx->own_stream;
+    if (dev_alloc(ctx, &ctx->d_status, 1) != AXIA_OK) { st = AXIA_ERR_OOM; break; }
+    if (ensure_pcg_state(ctx) != AXIA_OK) { st = AXIA_ERR_OOM; break; }
+    if (reset_dev_status(ctx) != AXIA_OK) { st = AXIA_ERR_CUDA; break; }
+  } while (0);
+  if (st != AXIA_OK) {
+    axia_gpu_destroy(ctx);
+    if (status) *status = st;
+    return nullptr;
+  }
+  if (status) *status = AXIA_OK;
+  return ctx;
+}
+
+void axia_gpu_destroy(axia_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  free_mesh_state(ctx);
+  dev_free(ctx->d_partials);
+  dev_free(ctx->d_bar);
+  dev_free(ctx->d_status);
+  if (ctx->d_out) cudaFree(ctx->d_out);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+const char* axia_gpu_last_error(const axia_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
+
+int32_t axia_gpu_element_ke(axia_ctx* ctx, int32_t nn, int32_t reduced, int64_t n_elem, const double* xyz,
+                            const double* e, double nu, double* ke, double* vol, int64_t* bad_elem) {
+  if (!ctx) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (bad_elem) *bad_elem = -1;
+  if ((nn != 8 && nn != 20) || n_elem < 0 || (n_elem > 0 && (!xyz || !e || !ke)))
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "element_ke: nn must be 8 or 20 and buffers non-null");
+  if (nu >= 0.5 || nu <= -1.0 || !std::isfinite(nu))  // d_iso_3d, elem.rs:42-44
+    return set_error(ctx, AXIA_ERR_MATERIAL, "invalid Poisson ratio nu=" + std::to_string(nu));
+  if (n_elem == 0) return AXIA_OK;
+  const int64_t kesz = 9LL * nn * nn;
+  double *d_xyz = nullptr, *d_e = nullptr, *d_ke = nullptr, *d_vol = nullptr;
+  int st = AXIA_OK;
+  do {
+    if ((st = dev_alloc(ctx, &d_xyz, (size_t)(n_elem * 3 * nn)))) break;
+    if ((st = dev_alloc(ctx, &d_e, (size_t)n_elem))) break;
+    if ((st = dev_alloc(ctx, &d_ke, (size_t)(n_elem * kesz)))) break;
+    if ((st = dev_alloc(ctx, &d_vol, (size_t)n_elem))) break;
+    cudaMemcpyAsync(d_xyz, xyz, n_elem * 3 * nn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(d_e, e, n_elem * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    if ((st = reset_dev_status(ctx))) break;
+    ElemArgs a{};
+    a.n_elem = n_elem;
+    a.conn = nullptr;
+    a.coords = nullptr;
+    a.xyz = d_xyz;
+    a.e_elem = d_e;
+    a.c_lam = nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    a.c_mu = 1.0 / (2.0 * (1.0 + nu));
+    a.ke_out = d_ke;
+    a.vol_out = d_vol;
+    a.status = ctx->d_status;
+    if ((st = run_element_ke(ctx, nn, reduced, a))) break;
+    if (cudaMemcpyAsync(ke, d_ke, n_elem * kesz * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess) {
+      st = set_error(ctx, AXIA_ERR_CUDA, "copy of Ke");
+      break;
+    }
+    if (vol) cudaMemcpyAsync(vol, d_vol, n_elem * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+      st = set_error(ctx, AXIA_ERR_CUDA, std::string("element_ke: ") + cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    DevStatus hs;
+    if ((st = read_dev_status(ctx, &hs))) break;
+    if (hs.first_error != ~0ull) {
+      int code = (int)(hs.first_error & 0xff);
+      if (bad_elem) *bad_elem = (int64_t)(hs.first_error >> 8);
+      st = set_error(ctx, code, "element " + std::to_string(hs.first_error >> 8) + ": element_ke failed (code " +
+                                    std::to_string(code) + ")");
+    }
+  } while (0);
+  dev_free(d_xyz);
+  dev_free(d_e);
+  dev_free(d_ke);
+  dev_free(d_vol);
+  return st;
+}
+
+int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const int64_t* bc_dof,
+                       const double* bc_val) {
+  if (!ctx || !mesh) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  auto t0 = std::chrono::steady_clock::now();
+  if ((mesh->nn != 8 && mesh->nn != 20) || mesh->n_nodes <= 0 || mesh->n_elem < 0 || !mesh->coords ||
+      (mesh->n_elem > 0 && !mesh->conn) || n_bc < 0 || (n_bc > 0 && (!bc_dof || !bc_val)))
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "setup: bad mesh description");
+  if (mesh->n_elem >= (1LL << 26)) return set_error(ctx, AXIA_ERR_TOO_LARGE, "setup: more than 2^26 elements");
+  if (3 * mesh->n_nodes >= (int64_t)INT32_MAX) return set_error(ctx, AXIA_ERR_TOO_LARGE, "setup: too many nodes");
+  if (mesh->nu >= 0.5 || mesh->nu <= -1.0 || !std::isfinite(mesh->nu))
+    return set_error(ctx, AXIA_ERR_MATERIAL, "invalid Poisson ratio nu=" + std::to_string(mesh->nu));
+  if (!mesh->e_elem && !(mesh->e > 0.0))
+    return set_error(ctx, AXIA_ERR_MATERIAL, "invalid Young's modulus E=" + std::to_string(mesh->e));
+  free_mesh_state(ctx);
+  ctx->nn = mesh->nn;
+  ctx->reduced = mesh->nn == 20 && mesh->reduced ? 1 : 0;
+  ctx->ngp = (mesh->nn == 8 || ctx->reduced) ? 8 : 27;
+  ctx->n_nodes = mesh->n_nodes;
+  ctx->n_elem = mesh->n_elem;
+  ctx->nu = mesh->nu;
+  ctx->ndof = 3 * mesh->n_nodes;
+  ctx->last_bad = -1;
+  const int64_t ndof = ctx->ndof;
+  // prescribed DOFs, last BC wins (analysis.rs:556-565)
+  std::vector<uint8_t> presc(ndof, 0);
+  std::vector<double> u0(ndof, 0.0);
+  for (int64_t k = 0; k < n_bc; ++k) {
+    const int64_t d = bc_dof[k];
+    if (d < 0 || d >= ndof) return set_error(ctx, AXIA_ERR_INVALID_ARG, "BC " + std::to_string(k) + " names DOF out of range");
+    if (!std::isfinite(bc_val[k])) return set_error(ctx, AXIA_ERR_NONFINITE, "BC " + std::to_string(k) + " value not finite");
+    presc[d] = 1;
+    u0[d] = bc_val[k];
+  }
+  ctx->any_u0 = false;
+  for (int64_t d = 0; d < ndof; ++d) ctx->any_u0 |= (u0[d] != 0.0);
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_coords, (size_t)(3 * mesh->n_nodes)));
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_conn, (size_t)(mesh->n_elem * mesh->nn)));
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_e, (size_t)std::max<int64_t>(mesh->n_elem, 1)));
+  AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_coords, mesh->coords, 3 * mesh->n_nodes * sizeof(double),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+  if (mesh->n_elem > 0)
+    AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_conn, mesh->conn, mesh->n_elem * mesh->nn * sizeof(int32_t),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+  if (mesh->e_elem) {
+    AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_e, mesh->e_elem, mesh->n_elem * sizeof(double), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+  } else {
+    std::vector<double> ev(std::max<int64_t>(mesh->n_elem, 1), mesh->e);
+    AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_e, ev.data(), ev.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  AXIA_TRY(reset_dev_status(ctx));
+  int st = symbolic_setup(ctx, presc.data(), u0.data());
+  if (st != AXIA_OK) return st;
+  if (ctx->n_free == 0 && n_bc == 0)  // constraint.rs:111-113
+    return set_error(ctx, AXIA_ERR_NO_FREE_DOF, "model without free degrees of freedom");
+  ctx->ms_setup = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return AXIA_OK;
+}
+
+int32_t axia_gpu_assemble(axia_ctx* ctx, int32_t precision) {
+  if (!ctx) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->d_rowptr) return set_error(ctx, AXIA_ERR_STATE, "assemble before setup");
+  EventTimer t(ctx->stream);
+  int st = numeric_assemble(ctx, precision == AXIA_PREC_MIXED);
+  ctx->ms_assemble = t.stop_ms();
+  return st;
+}
+
+static int32_t solve_common(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_opts* opts,
+                            axia_solve_info* info) {
+  axia_solve_info local{};
+  if (!info) info = &local;
+  std::memset(info, 0, sizeof(*info));
+  info->bad_index = -1;
+  axia_solve_opts o{};
+  if (opts) {
+    o = *opts;
+  } else {
+    o.rtol = 1e-8;
+    o.precision = AXIA_PREC_FP64;
+  }
+  if (!(o.rtol > 0.0)) o.rtol = 1e-8;
+  EventTimer t(ctx->stream);
+  int st = AXIA_OK;
+  if (ctx->n_free > 0) {
+    st = build_rhs(ctx, d_f);
+    if (st == AXIA_OK) st = pcg_solve(ctx, &o, info);
+    if (st == AXIA_OK) st = reconstruct(ctx, d_u);
+  } else {
+    cudaMemcpyAsync(d_u, ctx->d_u0, ctx->ndof * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+  }
+  info->ms_solve = t.stop_ms();
+  if (st == AXIA_OK && ctx->n_free > 0) true_residual(ctx, &info->true_residual);
+  fill_info_sizes(ctx, info);
+  info->status = st;
+  return st;
+}
+
+int32_t axia_gpu_solve_device(axia_ctx* ctx, const double* f_full_dev, double* u_full_dev,
+                              const axia_solve_opts* opts, axia_solve_info* info) {
+  if (!ctx || !f_full_dev || !u_full_dev) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "solve before assemble");
+  return solve_common(ctx, f_full_dev, u_full_dev, opts, info);
+}
+
+int32_t axia_gpu_solve(axia_ctx* ctx, const double* f_full, double* u_full, const axia_solve_opts* opts,
+                       axia_solve_info* info) {
+  if (!ctx || !f_full || !u_full) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "solve before assemble");
+  for (int64_t d = 0; d < ctx->ndof; ++d)
+    if (!std::isfinite(f_full[d])) return set_error(ctx, AXIA_ERR_NONFINITE, "load vector entry " + std::to_string(d) + " not finite");
+  if (!ctx->d_f) AXIA_TRY(dev_alloc(ctx, &ctx->d_f, (size_t)ctx->ndof));
+  if (!ctx->d_u) AXIA_TRY(dev_alloc(ctx, &ctx->d_u, (size_t)ctx->ndof));
+  AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_f, f_full, ctx->ndof * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  int st = solve_common(ctx, ctx->d_f, ctx->d_u, opts, info);
+  if (st != AXIA_OK) return st;
+  AXIA_CUDA(ctx, cudaMemcpyAsync(u_full, ctx->d_u, ctx->ndof * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXIA_OK;
+}
+
+int32_t axia_gpu_set_stream(axia_ctx* ctx, void* stream) {
+  if (!ctx) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return AXIA_OK;
+}
+
+int64_t axia_gpu_kernel_launches(const axia_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int32_t axia_gpu_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev, int32_t lanes) {
+  if (!ctx || !x_dev || !y_dev) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "spmv before assemble");
+  const bool fp32 = precision == AXIA_PREC_MIXED;
+  if (fp32 && !ctx->have32) return set_error(ctx, AXIA_ERR_STATE, "FP32 spmv needs axia_gpu_assemble(AXIA_PREC_MIXED)");
+  return spmv_device(ctx, fp32, x_dev, y_dev, lanes);
+}
+
+int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz) {
+  if (!ctx) return AXIA_ERR_INVALID_ARG;
+  if (n_free) *n_free = ctx->n_free;
+  if (nnz) *nnz = ctx->nnz;
+  return AXIA_OK;
+}
+
+int32_t axia_gpu_export_system(const axia_ctx* ctx_c, int32_t* rowptr, int32_t* col, double* val, double* diag,
+                               double* kfu0) {
+  axia_ctx* ctx = const_cast<axia_ctx*>(ctx_c);
+  if (!ctx) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->d_rowptr) return set_error(ctx, AXIA_ERR_STATE, "export before setup");
+  const int64_t n = ctx->n_free, nnz = ctx->nnz;
+  if (rowptr) AXIA_CUDA(ctx, cudaMemcpy(rowptr, ctx->d_rowptr, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (col) AXIA_CUDA(ctx, cudaMemcpy(col, ctx->d_col, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if ((val || diag || kfu0) && !ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "export of values before assemble");
+  if (val) AXIA_CUDA(ctx, cudaMemcpy(val, ctx->d_val, nnz * sizeof(double), cudaMemcpyDeviceToHost));
+  if (diag) AXIA_CUDA(ctx, cudaMemcpy(diag, ctx->d_diag, n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (kfu0) AXIA_CUDA(ctx, cudaMemcpy(kfu0, ctx->d_kfu0, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return AXIA_OK;
+}
+
+int32_t axia_gpu_export_dofmap(const axia_ctx* ctx, int32_t* ind_of) {
+  if (!ctx || !ind_of) return AXIA_ERR_INVALID_ARG;
+  if (ctx->h_ind_of.empty()) return AXIA_ERR_STATE;
+  std::memcpy(ind_of, ctx->h_ind_of.data(), ctx->h_ind_of.size() * sizeof(int32_t));
+  return AXIA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,688 @@
+// assemble.cu -- symbolic phase (node incidence, node adjacency, DOF map,
+// CSR pattern of K_ff) and numeric phase (element stiffness, deterministic
+// gather into K_ff with Dirichlet elimination).
+//
+// The reference builds K by pushing every nonzero Ke entry as a triplet in
+// element order (solver/src/analysis.rs:651-668), maps the triplets to the
+// independent DOFs (DofMap::reduce, solver/src/constraint.rs:138-172) and sums
+// duplicates after a stable (row, col) sort (csr_from_triplets,
+// solver/src/linalg.rs:10-38).  Here every row of K_ff is owned by one warp,
+// which sums the contributions of the node's incident elements in ascending
+// element order -- the same order the reference's stable sort keeps -- and
+// writes the row once.  No atomics touch K, so the result is bitwise
+// reproducible run to run.
+//
+// CSR pattern: all couplings of nodes that share an element (full symmetric
+// storage like the reference); a block whose reference triplets are all exact
+// zeros is kept as an explicit zero.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "element.cuh"
+
+// ---------------------------------------------------------------------------
+// Element tables: dN/dxi at the Gauss points (hex8_shape elem.rs:158-171,
+// hex20_shape quadratic.rs:36-73, hex_gauss quadratic.rs:100-120) and the
+// entry/block tables of the upper triangle.
+// ---------------------------------------------------------------------------
+namespace {
+
+const double kG2 = 0.5773502691896257;
+const double kG3[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};
+const double kW3[3] = {0.5555555555555556, 0.8888888888888888, 0.5555555555555556};
+const int kXi20[20][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, 1},
+                          {1, -1, 1},   {1, 1, 1},   {-1, 1, 1}, {0, -1, -1}, {1, 0, -1},
+                          {0, 1, -1},   {-1, 0, -1}, {0, -1, 1}, {1, 0, 1},   {0, 1, 1},
+                          {-1, 0, 1},   {-1, -1, 0}, {1, -1, 0}, {1, 1, 0},   {-1, 1, 0}};
+
+void dshape_hex8(double xi, double eta, double zeta, double* dn) {
+  for (int i = 0; i < 8; ++i) {
+    double x = kXi20[i][0], e = kXi20[i][1], z = kXi20[i][2];
+    dn[3 * i + 0] = 0.125 * x * (1.0 + e * eta) * (1.0 + z * zeta);
+    dn[3 * i + 1] = 0.125 * e * (1.0 + x * xi) * (1.0 + z * zeta);
+    dn[3 * i + 2] = 0.125 * z * (1.0 + x * xi) * (1.0 + e * eta);
+  }
+}
+
+void dshape_hex20(double xi, double eta, double zeta, double* dn) {
+  for (int i = 0; i < 8; ++i) {
+    double x = kXi20[i][0], e = kXi20[i][1], z = kXi20[i][2];
+    double a = 1.0 + x * xi, b = 1.0 + e * eta, c = 1.0 + z * zeta;
+    dn[3 * i + 0] = 0.125 * x * b * c * (2.0 * x * xi + e * eta + z * zeta - 1.0);
+    dn[3 * i + 1] = 0.125 * e * a * c * (x * xi + 2.0 * e * eta + z * zeta - 1.0);
+    dn[3 * i + 2] = 0.125 * z * a * b * (x * xi + e * eta + 2.0 * z * zeta - 1.0);
+  }
+  for (int i = 8; i < 20; ++i) {
+    double x = kXi20[i][0], e = kXi20[i][1], z = kXi20[i][2];
+    if (x == 0) {
+      dn[3 * i + 0] = 0.25 * (-2.0 * xi) * (1.0 + e * eta) * (1.0 + z * zeta);
+      dn[3 * i + 1] = 0.25 * (1.0 - xi * xi) * e * (1.0 + z * zeta);
+      dn[3 * i + 2] = 0.25 * (1.0 - xi * xi) * (1.0 + e * eta) * z;
+    } else if (e == 0) {
+      dn[3 * i + 0] = 0.25 * (1.0 - eta * eta) * x * (1.0 + z * zeta);
+      dn[3 * i + 1] = 0.25 * (-2.0 * eta) * (1.0 + x * xi) * (1.0 + z * zeta);
+      dn[3 * i + 2] = 0.25 * (1.0 - eta * eta) * (1.0 + x * xi) * z;
+    } else {
+      dn[3 * i + 0] = 0.25 * (1.0 - zeta * zeta) * x * (1.0 + e * eta);
+      dn[3 * i + 1] = 0.25 * (1.0 - zeta * zeta) * (1.0 + x * xi) * e;
+      dn[3 * i + 2] = 0.25 * (-2.0 * zeta) * (1.0 + x * xi) * (1.0 + e * eta);
+    }
+  }
+}
+
+struct HostTables {
+  std::vector<double> dn, w;
+  std::vector<int> e0, e1, blk;
+};
+
+HostTables make_tables(int nn, int ng) {
+  HostTables t;
+  std::vector<double> pts;  // xi, eta, zeta, w
+  if (ng == 8) {
+    const double g[2] = {-kG2, kG2};
+    for (double a : g)
+      for (double b : g)
+        for (double c : g) pts.insert(pts.end(), {a, b, c, 1.0});
+  } else {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) pts.insert(pts.end(), {kG3[i], kG3[j], kG3[k], kW3[i] * kW3[j] * kW3[k]});
+  }
+  t.dn.resize((size_t)ng * nn * 3);
+  t.w.resize(ng);
+  for (int g = 0; g < ng; ++g) {
+    if (nn == 8)
+      dshape_hex8(pts[4 * g], pts[4 * g + 1], pts[4 * g + 2], &t.dn[(size_t)g * nn * 3]);
+    else
+      dshape_hex20(pts[4 * g], pts[4 * g + 1], pts[4 * g + 2], &t.dn[(size_t)g * nn * 3]);
+    t.w[g] = pts[4 * g + 3];
+  }
+  // entries of blocks a <= b; diagonal blocks keep i <= j
+  int k = 0, blk = 0;
+  for (int a = 0; a < nn; ++a)
+    for (int b = a; b < nn; ++b, ++blk) {
+      int base = k;
+      bool dg = a == b;
+      t.blk.push_back(base | (dg ? 1 << 16 : 0));
+      for (int i = 0; i < 3; ++i)
+        for (int j = dg ? i : 0; j < 3; ++j, ++k) {
+          int hi = 3 * a + i, ci = 3 * b + j;
+          t.e0.push_back(hi | (ci << 8) | (i == j ? 1 << 16 : 0));
+          int kT;
+          if (dg) {
+            kT = k;  // symmetric block
+          } else {
+            kT = base + 3 * j + i;
+          }
+          t.e1.push_back(kT | (blk << 16));
+        }
+    }
+  return t;
+}
+
+struct DevTables {
+  double* dn = nullptr;
+  double* w = nullptr;
+  int* e0 = nullptr;
+  int* e1 = nullptr;
+  int* blk = nullptr;
+};
+
+DevTables g_tab[3];  // hex8, hex20 (27 gp), hex20r (8 gp) -- per process, device 0..n share by device id
+int g_tab_device[3] = {-1, -1, -1};
+
+int table_index(int nn, int ng) { return nn == 8 ? 0 : (ng == 27 ? 1 : 2); }
+
+int ensure_tables(axia_ctx* ctx, int nn, int ng, ElemTables* out) {
+  int ti = table_index(nn, ng);
+  if (g_tab_device[ti] != ctx->device) {
+    HostTables h = make_tables(nn, ng);
+    DevTables& d = g_tab[ti];
+    AXIA_CUDA(ctx, cudaMalloc(&d.dn, h.dn.size() * sizeof(double)));
+    AXIA_CUDA(ctx, cudaMalloc(&d.w, h.w.size() * sizeof(double)));
+    AXIA_CUDA(ctx, cudaMalloc(&d.e0, h.e0.size() * sizeof(int)));
+    AXIA_CUDA(ctx, cudaMalloc(&d.e1, h.e1.size() * sizeof(int)));
+    AXIA_CUDA(ctx, cudaMalloc(&d.blk, h.blk.size() * sizeof(int)));
+    AXIA_CUDA(ctx, cudaMemcpy(d.dn, h.dn.data(), h.dn.size() * sizeof(double), cudaMemcpyHostToDevice));
+    AXIA_CUDA(ctx, cudaMemcpy(d.w, h.w.data(), h.w.size() * sizeof(double), cudaMemcpyHostToDevice));
+    AXIA_CUDA(ctx, cudaMemcpy(d.e0, h.e0.data(), h.e0.size() * sizeof(int), cudaMemcpyHostToDevice));
+    AXIA_CUDA(ctx, cudaMemcpy(d.e1, h.e1.data(), h.e1.size() * sizeof(int), cudaMemcpyHostToDevice));
+    AXIA_CUDA(ctx, cudaMemcpy(d.blk, h.blk.data(), h.blk.size() * sizeof(int), cudaMemcpyHostToDevice));
+    g_tab_device[ti] = ctx->device;
+  }
+  const DevTables& d = g_tab[ti];
+  out->dn = d.dn;
+  out->w = d.w;
+  out->e0 = d.e0;
+  out->e1 = d.e1;
+  out->blk = d.blk;
+  return AXIA_OK;
+}
+
+template <int NN, int NG, int WARPS>
+int launch_element_ke(axia_ctx* ctx, const ElemArgs& args) {
+  ElemTables tab;
+  AXIA_TRY(ensure_tables(ctx, NN, NG, &tab));
+  size_t smem = element_smem_bytes<NN, NG>(WARPS);
+  auto kern = element_ke_kernel<NN, NG, WARPS>;
+  AXIA_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARPS * 32, smem));
+  if (per_sm < 1) return set_error(ctx, AXIA_ERR_CUDA, "element kernel does not fit on an SM");
+  int64_t need = (args.n_elem + WARPS - 1) / WARPS;
+  int64_t grid = std::min<int64_t>(need, (int64_t)per_sm * ctx->sm_count);
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, WARPS * 32, smem, ctx->stream>>>(args, tab);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  return AXIA_OK;
+}
+
+}  // namespace
+
+// Runs the element kernel for nn / reduced on args (device pointers).
+int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args) {
+  if (args.n_elem == 0) return AXIA_OK;
+  if (nn == 8) return launch_element_ke<8, 8, 8>(ctx, args);
+  if (nn == 20 && !reduced) return launch_element_ke<20, 27, 4>(ctx, args);
+  if (nn == 20 && reduced) return launch_element_ke<20, 8, 4>(ctx, args);
+  return set_error(ctx, AXIA_ERR_INVALID_ARG, "nn must be 8 or 20");
+}
+
+// ---------------------------------------------------------------------------
+// Symbolic kernels
+// ---------------------------------------------------------------------------
+__global__ void k_count_incidence(int64_t n_items, int nn, const int32_t* conn, int64_t n_nodes,
+                                  int64_t* cnt, DevStatus* st) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_items;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int node = conn[t];
+    if (node < 0 || node >= n_nodes) {
+      record_error(st, t / nn, AXIA_ERR_INVALID_ARG);
+      continue;
+    }
+    atomicAdd((unsigned long long*)&cnt[node], 1ull);
+  }
+}
+
+__global__ void k_fill_incidence(int64_t n_items, int nn, const int32_t* conn, const int64_t* ptr,
+                                 int32_t* fill, int32_t* ne) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_items;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int node = conn[t];
+    int pos = atomicAdd(&fill[node], 1);
+    int64_t e = t / nn;
+    int la = (int)(t % nn);
+    ne[ptr[node] + pos] = (int32_t)(e * 32 + la);
+  }
+}
+
+// insertion sort of every node's incidence list: ascending element, then local index
+__global__ void k_sort_incidence(int64_t n_nodes, const int64_t* ptr, int32_t* ne) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n_nodes;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = ptr[a], e = ptr[a + 1];
+    for (int64_t i = b + 1; i < e; ++i) {
+      int32_t v = ne[i];
+      int64_t j = i - 1;
+      while (j >= b && ne[j] > v) {
+        ne[j + 1] = ne[j];
+        --j;
+      }
+      ne[j + 1] = v;
+    }
+  }
+}
+
+// Adjacency of node a: sorted unique nodes of its incident elements.
+// mode 0 counts (cnt[a]), mode 1 writes adj[ptr[a] ...].  One warp per node;
+// candidates staged in shared memory (cap per warp = cap).
+__global__ void k_adjacency(int64_t n_nodes, int nn, const int32_t* conn, const int64_t* ne_ptr,
+                            const int32_t* ne, int cap, int mode, int64_t* cnt, const int64_t* adj_ptr,
+                            int32_t* adj, DevStatus* st) {
+  extern __shared__ int32_t s_cand[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  int32_t* cand = s_cand + (size_t)warp * 2 * cap;
+  int32_t* first = cand + cap;
+  for (int64_t a = (int64_t)blockIdx.x * wpb + warp; a < n_nodes; a += (int64_t)gridDim.x * wpb) {
+    int64_t b0 = ne_ptr[a], b1 = ne_ptr[a + 1];
+    int m = (int)(b1 - b0) * nn;
+    if (m > cap) {
+      if (lane == 0) record_error(st, a, AXIA_ERR_TOO_LARGE);
+      continue;
+    }
+    for (int t = lane; t < m; t += 32) {
+      int32_t code = ne[b0 + t / nn];
+      cand[t] = conn[(int64_t)(code >> 5) * nn + (t % nn)];
+    }
+    __syncwarp();
+    for (int i = lane; i < m; i += 32) {
+      int v = cand[i], f = 1;
+      for (int j = 0; j < i; ++j)
+        if (cand[j] == v) {
+          f = 0;
+          break;
+        }
+      first[i] = f;
+    }
+    __syncwarp();
+    int my_count = 0;
+    for (int i = lane; i < m; i += 32) {
+      if (!first[i]) continue;
+      ++my_count;
+      if (mode == 1) {
+        int v = cand[i], pos = 0;
+        for (int j = 0; j < m; ++j) pos += (first[j] && cand[j] < v) ? 1 : 0;
+        adj[adj_ptr[a] + pos] = v;
+      }
+    }
+    my_count = warp_sum(my_count);
+    if (mode == 0 && lane == 0) cnt[a] = my_count;
+    __syncwarp();
+  }
+}
+
+// free[d] = !prescribed[d] && node attached (analysis.rs:2283-2330 pins isolated nodes)
+__global__ void k_free_flags(int64_t ndof, const uint8_t* presc, const int64_t* inc_cnt, int64_t* flag) {
+  for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < ndof;
+       d += (int64_t)gridDim.x * blockDim.x)
+    flag[d] = (!presc[d] && inc_cnt[d / 3] > 0) ? 1 : 0;
+}
+
+__global__ void k_ind_of(int64_t ndof, const int64_t* flag, const int64_t* scan, int32_t* ind_of) {
+  for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < ndof;
+       d += (int64_t)gridDim.x * blockDim.x)
+    ind_of[d] = flag[d] ? (int32_t)scan[d] : -1;
+}
+
+// per node: free-column offset of every adjacency block and the row length
+__global__ void k_row_layout(int64_t n_nodes, const int64_t* adj_ptr, const int32_t* adj,
+                             const int32_t* ind_of, int32_t* adj_off, int32_t* rowlen) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n_nodes;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    int run = 0;
+    for (int64_t s = adj_ptr[a]; s < adj_ptr[a + 1]; ++s) {
+      int b = adj[s];
+      adj_off[s] = run;
+      run += (ind_of[3 * (int64_t)b] >= 0) + (ind_of[3 * (int64_t)b + 1] >= 0) + (ind_of[3 * (int64_t)b + 2] >= 0);
+    }
+    rowlen[a] = run;
+  }
+}
+
+__global__ void k_row_counts(int64_t ndof, const int32_t* ind_of, const int32_t* rowlen, int64_t* cnt) {
+  for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < ndof;
+       d += (int64_t)gridDim.x * blockDim.x) {
+    int r = ind_of[d];
+    if (r >= 0) cnt[r] = rowlen[d / 3];
+  }
+}
+
+__global__ void k_to_i32(int64_t n, const int64_t* in, int32_t* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (int32_t)in[i];
+}
+
+// first free index of node b (free DOFs of a node are consecutive)
+__device__ __forceinline__ int first_free(const int32_t* ind_of, int b) {
+  int c = ind_of[3 * b];
+  if (c < 0) c = ind_of[3 * b + 1];
+  if (c < 0) c = ind_of[3 * b + 2];
+  return c;
+}
+
+// column indices of every free row, warp per node
+__global__ void k_fill_columns(int64_t n_nodes, const int64_t* adj_ptr, const int32_t* adj,
+                               const int32_t* adj_off, const int32_t* ind_of, const int32_t* rowptr,
+                               int32_t* col) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  for (int64_t a = (int64_t)blockIdx.x * wpb + warp; a < n_nodes; a += (int64_t)gridDim.x * wpb) {
+    int64_t s0 = adj_ptr[a];
+    int nadj = (int)(adj_ptr[a + 1] - s0);
+    for (int i = 0; i < 3; ++i) {
+      int r = ind_of[3 * a + i];
+      if (r < 0) continue;
+      int64_t rs = rowptr[r];
+      for (int t = lane; t < 3 * nadj; t += 32) {
+        int s = t / 3, j = t % 3;
+        int b = adj[s0 + s];
+        int c = ind_of[3 * (int64_t)b + j];
+        if (c >= 0) col[rs + adj_off[s0 + s] + (c - first_free(ind_of, b))] = c;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Numeric gather: warp per node, contributions of incident elements summed in
+// ascending element order into a shared-memory block row, then written as up
+// to three CSR rows of K_ff (free columns) and K_fp u0 (prescribed columns).
+// ---------------------------------------------------------------------------
+struct GatherArgs {
+  int64_t n_nodes;
+  int nn;
+  const int32_t* conn;
+  const int64_t* ne_ptr;
+  const int32_t* ne;
+  const int64_t* adj_ptr;
+  const int32_t* adj;
+  const int32_t* adj_off;
+  const int32_t* ind_of;
+  const int32_t* rowptr;
+  const double* ke;
+  const double* u0;
+  int any_u0;
+  int max_adj;
+  int warp_stride;   // bytes of shared memory per warp
+  double* val;
+  float* val32;
+  double* diag;
+  double* dinv;
+  float* dinv32;
+  double* kfu0;
+};
+
+__global__ void k_gather(GatherArgs g) {
+  extern __shared__ __align__(16) unsigned char s_gather[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  const int nn = g.nn, ndof_e = 3 * nn, ke_size = ndof_e * ndof_e;
+  unsigned char* base = s_gather + (size_t)warp * g.warp_stride;
+  double* acc = (double*)base;                                   // [max_adj][9]
+  int32_t* s_adj = (int32_t*)(base + (size_t)g.max_adj * 72);    // [max_adj]
+  int32_t* s_slot = s_adj + g.max_adj;                           // [nn]
+  for (int64_t a = (int64_t)blockIdx.x * wpb + warp; a < g.n_nodes; a += (int64_t)gridDim.x * wpb) {
+    const int64_t s0 = g.adj_ptr[a];
+    const int nadj = (int)(g.adj_ptr[a + 1] - s0);
+    for (int t = lane; t < nadj; t += 32) s_adj[t] = g.adj[s0 + t];
+    for (int t = lane; t < nadj * 9; t += 32) acc[t] = 0.0;
+    __syncwarp();
+    for (int64_t k = g.ne_ptr[a]; k < g.ne_ptr[a + 1]; ++k) {
+      const int32_t code = g.ne[k];
+      const int64_t e = code >> 5;
+      const int la = code & 31;
+      if (lane < nn) {
+        int b = g.conn[e * nn + lane];
+        int lo = 0, hi = nadj - 1;
+        while (lo < hi) {
+          int mid = (lo + hi) >> 1;
+          if (s_adj[mid] < b) lo = mid + 1; else hi = mid;
+        }
+        s_slot[lane] = lo;
+      }
+      __syncwarp();
+      const double* rowblk = g.ke + e * (int64_t)ke_size + (int64_t)(3 * la) * ndof_e;
+      for (int t = lane; t < 3 * ndof_e; t += 32) {
+        double v = __ldcs(rowblk + t);
+        int i = t / ndof_e, c = t % ndof_e;
+        acc[s_slot[c / 3] * 9 + i * 3 + (c % 3)] += v;
+      }
+      __syncwarp();
+    }
+    for (int i = 0; i < 3; ++i) {
+      const int r = g.ind_of[3 * a + i];
+      if (r < 0) continue;
+      const int64_t rs = g.rowptr[r];
+      double kf = 0.0;
+      for (int t = lane; t < 3 * nadj; t += 32) {
+        const int s = t / 3, j = t % 3;
+        const int b = s_adj[s];
+        const double v = acc[s * 9 + i * 3 + j];
+        const int c = g.ind_of[3 * (int64_t)b + j];
+        if (c >= 0) {
+          const int64_t pos = rs + g.adj_off[s0 + s] + (c - first_free(g.ind_of, b));
+          g.val[pos] = v;
+          if (g.val32) g.val32[pos] = (float)v;
+          if (c == r) {
+            g.diag[r] = v;
+            const double di = fabs(v) > 1e-30 ? 1.0 / v : 1.0;  // linalg.rs:218-219 guard
+            g.dinv[r] = di;
+            if (g.dinv32) g.dinv32[r] = (float)di;
+          }
+        } else if (g.any_u0) {
+          const double u0 = g.u0[3 * (int64_t)b + j];
+          if (u0 != 0.0) kf = fma(v, u0, kf);
+        }
+      }
+      if (g.any_u0) {
+        kf = warp_sum(kf);
+        if (lane == 0) g.kfu0[r] = kf;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+int run_gather(axia_ctx* ctx, GatherArgs args) {
+  size_t per_warp = (size_t)args.max_adj * 9 * sizeof(double) + (size_t)(args.max_adj + args.nn) * 4;
+  per_warp = (per_warp + 15) & ~(size_t)15;
+  if (per_warp > 200 * 1024) return set_error(ctx, AXIA_ERR_TOO_LARGE, "node adjacency too large for the gather");
+  int warps = 8;
+  while (warps > 1 && per_warp * warps > 200 * 1024) warps /= 2;
+  args.warp_stride = (int)per_warp;
+  size_t stride = per_warp;
+  size_t smem = stride * warps;
+  AXIA_CUDA(ctx, cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather, warps * 32, smem));
+  if (per_sm < 1) per_sm = 1;
+  int64_t need = (args.n_nodes + warps - 1) / warps;
+  int64_t grid = std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)per_sm * ctx->sm_count));
+  k_gather<<<(unsigned)grid, warps * 32, smem, ctx->stream>>>(args);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  return AXIA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host drivers
+// ---------------------------------------------------------------------------
+static unsigned grid_for(int64_t n, int threads, int sm_count) {
+  int64_t g = (n + threads - 1) / threads;
+  g = std::min<int64_t>(g, (int64_t)sm_count * 32);
+  return (unsigned)std::max<int64_t>(g, 1);
+}
+
+int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0) {
+  const int64_t n_nodes = ctx->n_nodes, n_elem = ctx->n_elem, nn = ctx->nn, ndof = ctx->ndof;
+  const int64_t n_items = n_elem * nn;
+  cudaStream_t s = ctx->stream;
+  int64_t *d_cnt = nullptr, *d_ne_ptr = nullptr;
+  int32_t* d_fill = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_cnt, n_nodes + 1));
+  AXIA_TRY(dev_alloc(ctx, &d_ne_ptr, n_nodes + 1));
+  AXIA_TRY(dev_alloc(ctx, &d_fill, n_nodes));
+  AXIA_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, (n_nodes + 1) * sizeof(int64_t), s));
+  AXIA_CUDA(ctx, cudaMemsetAsync(d_fill, 0, n_nodes * sizeof(int32_t), s));
+  k_count_incidence<<<grid_for(n_items, 256, ctx->sm_count), 256, 0, s>>>(n_items, (int)nn, ctx->d_conn,
+                                                                           n_nodes, d_cnt, ctx->d_status);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  DevStatus hs;
+  AXIA_TRY(read_dev_status(ctx, &hs));
+  if (hs.first_error != ~0ull)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG,
+                     "element " + std::to_string(hs.first_error >> 8) + " names a node outside 0..n_nodes-1");
+  int64_t total = 0;
+  AXIA_TRY(device_exclusive_scan(ctx, d_cnt, d_ne_ptr, n_nodes + 1, &total));
+  // per-node incidence maximum (for the adjacency candidate cap)
+  std::vector<int64_t> h_ptr(n_nodes + 1);
+  AXIA_CUDA(ctx, cudaMemcpyAsync(h_ptr.data(), d_ne_ptr, (n_nodes + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(s));
+  int max_inc = 0;
+  for (int64_t a = 0; a < n_nodes; ++a) max_inc = std::max<int>(max_inc, (int)(h_ptr[a + 1] - h_ptr[a]));
+  ctx->max_inc = max_inc;
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_ne, n_items));
+  k_fill_incidence<<<grid_for(n_items, 256, ctx->sm_count), 256, 0, s>>>(n_items, (int)nn, ctx->d_conn, d_ne_ptr,
+                                                                          d_fill, ctx->d_ne);
+  ctx->launches++;
+  k_sort_incidence<<<grid_for(n_nodes, 128, ctx->sm_count), 128, 0, s>>>(n_nodes, d_ne_ptr, ctx->d_ne);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  // adjacency
+  const int cap = std::max<int>(32, max_inc * (int)nn);
+  if (cap > 4096) return set_error(ctx, AXIA_ERR_TOO_LARGE, "a node touches too many elements");
+  int64_t *d_adj_cnt = nullptr, *d_adj_ptr = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_adj_cnt, n_nodes + 1));
+  AXIA_TRY(dev_alloc(ctx, &d_adj_ptr, n_nodes + 1));
+  AXIA_CUDA(ctx, cudaMemsetAsync(d_adj_cnt, 0, (n_nodes + 1) * sizeof(int64_t), s));
+  int wpb = 4;
+  size_t smem_adj = (size_t)wpb * 2 * cap * sizeof(int32_t);
+  AXIA_CUDA(ctx, cudaFuncSetAttribute(k_adjacency, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_adj));
+  unsigned g_adj = grid_for(n_nodes, wpb, ctx->sm_count);
+  k_adjacency<<<g_adj, wpb * 32, smem_adj, s>>>(n_nodes, (int)nn, ctx->d_conn, d_ne_ptr, ctx->d_ne, cap, 0, d_adj_cnt,
+                                                nullptr, nullptr, ctx->d_status);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  int64_t n_adj = 0;
+  AXIA_TRY(device_exclusive_scan(ctx, d_adj_cnt, d_adj_ptr, n_nodes + 1, &n_adj));
+  ctx->n_adj = n_adj;
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_adj, n_adj));
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_adj_off, n_adj));
+  k_adjacency<<<g_adj, wpb * 32, smem_adj, s>>>(n_nodes, (int)nn, ctx->d_conn, d_ne_ptr, ctx->d_ne, cap, 1, nullptr,
+                                                d_adj_ptr, ctx->d_adj, ctx->d_status);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  {
+    std::vector<int64_t> hp(n_nodes + 1);
+    AXIA_CUDA(ctx, cudaMemcpyAsync(hp.data(), d_adj_ptr, (n_nodes + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(s));
+    int mx = 0;
+    for (int64_t a = 0; a < n_nodes; ++a) mx = std::max<int>(mx, (int)(hp[a + 1] - hp[a]));
+    ctx->max_adj = mx;
+  }
+  // DOF map
+  uint8_t* d_presc = nullptr;
+  int64_t *d_flag = nullptr, *d_scan = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_presc, ndof));
+  AXIA_TRY(dev_alloc(ctx, &d_flag, ndof + 1));
+  AXIA_TRY(dev_alloc(ctx, &d_scan, ndof + 1));
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_u0, ndof));
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_ind_of, ndof));
+  AXIA_CUDA(ctx, cudaMemcpyAsync(d_presc, h_presc, ndof, cudaMemcpyHostToDevice, s));
+  AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_u0, h_u0, ndof * sizeof(double), cudaMemcpyHostToDevice, s));
+  AXIA_CUDA(ctx, cudaMemsetAsync(d_flag + ndof, 0, sizeof(int64_t), s));
+  k_free_flags<<<grid_for(ndof, 256, ctx->sm_count), 256, 0, s>>>(ndof, d_presc, d_cnt, d_flag);
+  ctx->launches++;
+  int64_t n_free = 0;
+  AXIA_TRY(device_exclusive_scan(ctx, d_flag, d_scan, ndof + 1, &n_free));
+  k_ind_of<<<grid_for(ndof, 256, ctx->sm_count), 256, 0, s>>>(ndof, d_flag, d_scan, ctx->d_ind_of);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  ctx->n_free = n_free;
+  // row layout
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_node_rowlen, n_nodes));
+  k_row_layout<<<grid_for(n_nodes, 128, ctx->sm_count), 128, 0, s>>>(n_nodes, d_adj_ptr, ctx->d_adj, ctx->d_ind_of,
+                                                                     ctx->d_adj_off, ctx->d_node_rowlen);
+  ctx->launches++;
+  int64_t *d_rcnt = nullptr, *d_rptr = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_rcnt, n_free + 1));
+  AXIA_TRY(dev_alloc(ctx, &d_rptr, n_free + 1));
+  AXIA_CUDA(ctx, cudaMemsetAsync(d_rcnt, 0, (n_free + 1) * sizeof(int64_t), s));
+  k_row_counts<<<grid_for(ndof, 256, ctx->sm_count), 256, 0, s>>>(ndof, ctx->d_ind_of, ctx->d_node_rowlen, d_rcnt);
+  ctx->launches++;
+  int64_t nnz = 0;
+  AXIA_TRY(device_exclusive_scan(ctx, d_rcnt, d_rptr, n_free + 1, &nnz));
+  if (nnz >= (int64_t)INT32_MAX)
+    return set_error(ctx, AXIA_ERR_TOO_LARGE, "nnz(K_ff) = " + std::to_string(nnz) + " exceeds 2^31-1");
+  ctx->nnz = nnz;
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_rowptr, n_free + 1));
+  k_to_i32<<<grid_for(n_free + 1, 256, ctx->sm_count), 256, 0, s>>>(n_free + 1, d_rptr, ctx->d_rowptr);
+  ctx->launches++;
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_col, nnz));
+  k_fill_columns<<<grid_for(n_nodes, 8, ctx->sm_count), 256, 0, s>>>(n_nodes, d_adj_ptr, ctx->d_adj, ctx->d_adj_off,
+                                                                     ctx->d_ind_of, ctx->d_rowptr, ctx->d_col);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  AXIA_CUDA(ctx, cudaStreamSynchronize(s));
+  AXIA_TRY(read_dev_status(ctx, &hs));
+  if (hs.first_error != ~0ull)
+    return set_error(ctx, AXIA_ERR_TOO_LARGE, "node " + std::to_string(hs.first_error >> 8) +
+                                                  ": adjacency candidate list above the cap");
+  // keep the 64-bit pointers for the gather
+  dev_free(ctx->d_ne_ptr);
+  dev_free(ctx->d_adj_ptr);
+  ctx->d_ne_ptr = d_ne_ptr;
+  ctx->d_adj_ptr = d_adj_ptr;
+  dev_free(d_cnt);
+  dev_free(d_fill);
+  dev_free(d_adj_cnt);
+  dev_free(d_presc);
+  dev_free(d_flag);
+  dev_free(d_scan);
+  dev_free(d_rcnt);
+  dev_free(d_rptr);
+  ctx->h_ind_of.resize(ndof);
+  AXIA_CUDA(ctx, cudaMemcpy(ctx->h_ind_of.data(), ctx->d_ind_of, ndof * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return AXIA_OK;
+}
+
+int numeric_assemble(axia_ctx* ctx, bool want32) {
+  cudaStream_t s = ctx->stream;
+  const int64_t kesz = (int64_t)9 * ctx->nn * ctx->nn;
+  if (ctx->ke_elems < (size_t)(ctx->n_elem * kesz)) {
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_ke, (size_t)(ctx->n_elem * kesz)));
+    ctx->ke_elems = (size_t)(ctx->n_elem * kesz);
+  }
+  AXIA_TRY(reset_dev_status(ctx));
+  ElemArgs ea{};
+  ea.n_elem = ctx->n_elem;
+  ea.conn = ctx->d_conn;
+  ea.coords = ctx->d_coords;
+  ea.xyz = nullptr;
+  ea.e_elem = ctx->d_e;
+  ea.e_const = 0.0;
+  ea.c_lam = ctx->nu / ((1.0 + ctx->nu) * (1.0 - 2.0 * ctx->nu));
+  ea.c_mu = 1.0 / (2.0 * (1.0 + ctx->nu));
+  ea.ke_out = ctx->d_ke;
+  ea.vol_out = nullptr;
+  ea.status = ctx->d_status;
+  AXIA_TRY(run_element_ke(ctx, ctx->nn, ctx->reduced, ea));
+  if (!ctx->d_val) AXIA_TRY(dev_alloc(ctx, &ctx->d_val, ctx->nnz));
+  if (want32 && !ctx->d_val32) AXIA_TRY(dev_alloc(ctx, &ctx->d_val32, ctx->nnz));
+  if (!ctx->d_diag) AXIA_TRY(dev_alloc(ctx, &ctx->d_diag, ctx->n_free));
+  if (!ctx->d_dinv) AXIA_TRY(dev_alloc(ctx, &ctx->d_dinv, ctx->n_free));
+  if (want32 && !ctx->d_dinv32) AXIA_TRY(dev_alloc(ctx, &ctx->d_dinv32, ctx->n_free));
+  if (!ctx->d_kfu0) AXIA_TRY(dev_alloc(ctx, &ctx->d_kfu0, ctx->n_free));
+  AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_kfu0, 0, ctx->n_free * sizeof(double), s));
+  GatherArgs g{};
+  g.n_nodes = ctx->n_nodes;
+  g.nn = ctx->nn;
+  g.conn = ctx->d_conn;
+  g.ne_ptr = ctx->d_ne_ptr;
+  g.ne = ctx->d_ne;
+  g.adj_ptr = ctx->d_adj_ptr;
+  g.adj = ctx->d_adj;
+  g.adj_off = ctx->d_adj_off;
+  g.ind_of = ctx->d_ind_of;
+  g.rowptr = ctx->d_rowptr;
+  g.ke = ctx->d_ke;
+  g.u0 = ctx->d_u0;
+  g.any_u0 = ctx->any_u0 ? 1 : 0;
+  g.max_adj = std::max(ctx->max_adj, 1);
+  g.val = ctx->d_val;
+  g.val32 = want32 ? ctx->d_val32 : nullptr;
+  g.diag = ctx->d_diag;
+  g.dinv = ctx->d_dinv;
+  g.dinv32 = want32 ? ctx->d_dinv32 : nullptr;
+  g.kfu0 = ctx->d_kfu0;
+  AXIA_TRY(run_gather(ctx, g));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(s));
+  DevStatus hs;
+  AXIA_TRY(read_dev_status(ctx, &hs));
+  if (hs.first_error != ~0ull) {
+    int code = (int)(hs.first_error & 0xff);
+    long long idx = (long long)(hs.first_error >> 8);
+    static const char* names[] = {"", "invalid argument", "singular Jacobian (degenerate element)",
+                                  "negative Jacobian determinant", "invalid material (E <= 0)"};
+    std::string what = code < 5 ? names[code] : (code == AXIA_ERR_NONFINITE ? "non-finite value" : "error");
+    ctx->last_bad = idx;
+    return set_error(ctx, code, "element " + std::to_string(idx) + ": " + what);
+  }
+  ctx->have32 = want32;
+  ctx->assembled = true;
+  return AXIA_OK;
+}

@@ -1,0 +1,226 @@
+// common.cuh -- context, error plumbing and device utilities shared by the
+// kernels of libaxia_gpu.so (GB300, sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/axia_gpu.h"
+
+// ---------------------------------------------------------------------------
+// Device-side status word.  Kernels never trap: they record the first error
+// (lowest element / row index wins) and return.
+// code in the low 8 bits, index in the upper 56 bits, so atomicMin picks the
+// lowest index, as the reference's sequential element loop reports the first
+// failing element (solver/src/analysis.rs:574-628).
+// ---------------------------------------------------------------------------
+struct DevStatus {
+  unsigned long long first_error;  // (index << 8) | code, ~0ull when clean
+  int timeout;                     // set by a wait that ran past its limit
+  int pad;
+};
+
+__device__ __forceinline__ void record_error(DevStatus* st, long long index, int code) {
+  unsigned long long key = ((unsigned long long)index << 8) | (unsigned long long)(code & 0xff);
+  atomicMin(&st->first_error, key);
+}
+
+// Nanosecond clock used to bound every spin-wait.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier for a cooperative (co-resident) launch.  The wait is
+// bounded: after `limit_ns` the block records a timeout and returns false;
+// every caller then leaves its loop, so a stuck barrier ends all blocks.
+struct GridBarrier {
+  unsigned count;
+  unsigned gen;
+};
+
+__device__ __forceinline__ bool grid_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned g = ld_acquire_gpu(&bar->gen);
+    __threadfence();
+    unsigned arrived = atomicAdd(&bar->count, 1u);
+    if (arrived == gridDim.x - 1) {
+      bar->count = 0;
+      __threadfence();
+      st_release_gpu(&bar->gen, g + 1);
+    } else {
+      unsigned long long t0 = global_ns();
+      unsigned spins = 0;
+      while (ld_acquire_gpu(&bar->gen) == g) {
+        if ((++spins & 63u) == 0 && global_ns() - t0 > limit_ns) {
+          atomicExch(&st->timeout, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*(volatile int*)&st->timeout) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Streaming (evict-first) loads for matrix data that is read once per sweep,
+// so the vectors keep their L2 lines.
+__device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
+__device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct axia_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;      // stream all work is issued on
+  cudaStream_t own_stream = nullptr;  // the context's own stream
+  int64_t launches = 0;               // kernels launched so far
+  std::string last_error;
+  int sm_count = 0;
+
+  // mesh
+  int nn = 0, reduced = 0, ngp = 0;
+  int64_t n_nodes = 0, n_elem = 0;
+  double nu = 0.0;
+  double* d_coords = nullptr;   // [n_nodes*3]
+  int32_t* d_conn = nullptr;    // [n_elem*nn]
+  double* d_e = nullptr;        // [n_elem]
+
+  // DOF map
+  int64_t ndof = 0, n_free = 0;
+  int32_t* d_ind_of = nullptr;  // [ndof], -1 prescribed
+  double* d_u0 = nullptr;       // [ndof]
+  bool any_u0 = false;
+  std::vector<int32_t> h_ind_of;
+
+  // node incidence and adjacency
+  int64_t* d_ne_ptr = nullptr;  // [n_nodes+1]
+  int32_t* d_ne = nullptr;      // [n_elem*nn] packed element*32 + local node
+  int64_t* d_adj_ptr = nullptr; // [n_nodes+1]
+  int32_t* d_adj = nullptr;     // [n_adj]
+  int32_t* d_adj_off = nullptr; // [n_adj] free-column offset of the block inside a row
+  int32_t* d_node_rowlen = nullptr;  // [n_nodes]
+  int64_t n_adj = 0;
+  int max_adj = 0, max_inc = 0;
+
+  // K_ff in CSR
+  int64_t nnz = 0;
+  int32_t* d_rowptr = nullptr;  // [n_free+1]
+  int32_t* d_col = nullptr;     // [nnz]
+  double* d_val = nullptr;      // [nnz]
+  float* d_val32 = nullptr;     // [nnz] (mixed)
+  double* d_diag = nullptr;     // [n_free]
+  double* d_dinv = nullptr;     // [n_free]
+  float* d_dinv32 = nullptr;    // [n_free]
+  double* d_kfu0 = nullptr;     // [n_free]
+  bool assembled = false, have32 = false;
+
+  // element stiffness scratch
+  double* d_ke = nullptr;
+  size_t ke_elems = 0;
+
+  // solver vectors
+  double* d_f = nullptr;        // [ndof]
+  double* d_u = nullptr;        // [ndof]
+  double* d_b = nullptr;        // [n_free]
+  double* d_x = nullptr;
+  double* d_r = nullptr;
+  double* d_p = nullptr;
+  double* d_q = nullptr;
+  float* d_b32 = nullptr;
+  float* d_x32 = nullptr;
+  float* d_r32 = nullptr;
+  float* d_p32 = nullptr;
+  float* d_q32 = nullptr;
+  double* d_partials = nullptr;
+  size_t partial_slots = 0;
+  GridBarrier* d_bar = nullptr;
+  DevStatus* d_status = nullptr;
+  void* d_out = nullptr;        // PcgOut
+  size_t vec_capacity = 0;
+
+  double ms_setup = 0.0, ms_assemble = 0.0;
+  int64_t last_bad = -1;
+};
+
+// set ctx->last_error and return code
+int set_error(axia_ctx* ctx, int code, const std::string& msg);
+
+#define AXIA_CUDA(ctx, call)                                                              \
+  do {                                                                                    \
+    cudaError_t _e = (call);                                                              \
+    if (_e != cudaSuccess) {                                                              \
+      return set_error((ctx), _e == cudaErrorMemoryAllocation ? AXIA_ERR_OOM : AXIA_ERR_CUDA, \
+                       std::string(#call) + ": " + cudaGetErrorString(_e));              \
+    }                                                                                     \
+  } while (0)
+
+#define AXIA_TRY(expr)      \
+  do {                      \
+    int _s = (expr);        \
+    if (_s != AXIA_OK) return _s; \
+  } while (0)
+
+template <typename T>
+int dev_alloc(axia_ctx* ctx, T** p, size_t count) {
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return set_error(ctx, AXIA_ERR_OOM, std::string("cudaMalloc ") + std::to_string(count * sizeof(T)) +
+                                            " bytes: " + cudaGetErrorString(e));
+  }
+  return AXIA_OK;
+}
+
+template <typename T>
+void dev_free(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+// exclusive scan of n int64 counts on the device (in place allowed), returns total
+int device_exclusive_scan(axia_ctx* ctx, const int64_t* d_in, int64_t* d_out, int64_t n, int64_t* total);
+
+// status word helpers
+int read_dev_status(axia_ctx* ctx, DevStatus* st_host);
+int reset_dev_status(axia_ctx* ctx);

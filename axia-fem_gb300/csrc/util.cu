@@ -1,0 +1,112 @@
+// util.cu -- device exclusive scan, status word, error strings.
+#include <algorithm>
+
+#include "common.cuh"
+
+int set_error(axia_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return code;
+}
+
+int read_dev_status(axia_ctx* ctx, DevStatus* st_host) {
+  AXIA_CUDA(ctx, cudaMemcpyAsync(st_host, ctx->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXIA_OK;
+}
+
+int reset_dev_status(axia_ctx* ctx) {
+  DevStatus clean;
+  clean.first_error = ~0ull;
+  clean.timeout = 0;
+  clean.pad = 0;
+  AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_status, &clean, sizeof(DevStatus), cudaMemcpyHostToDevice, ctx->stream));
+  return AXIA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of int64 counts: block-local scan of SCAN_ITEMS per block,
+// scan of the block totals (recursively), then add the block offsets.
+// ---------------------------------------------------------------------------
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_PER_THREAD = 8;
+constexpr int SCAN_ITEMS = SCAN_THREADS * SCAN_PER_THREAD;
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+k_scan_block(const int64_t* in, int64_t* out, int64_t n, int64_t* block_tot) {
+  __shared__ int64_t s_warp[SCAN_THREADS / 32];
+  const int64_t base = (int64_t)blockIdx.x * SCAN_ITEMS + (int64_t)threadIdx.x * SCAN_PER_THREAD;
+  int64_t v[SCAN_PER_THREAD];
+  int64_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+    int64_t i = base + k;
+    v[k] = i < n ? in[i] : 0;
+    sum += v[k];
+  }
+  // inclusive scan of per-thread sums within the warp
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t inc = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int64_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) s_warp[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    int64_t w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0;
+    int64_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int64_t t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
+    if (lane == SCAN_THREADS / 32 - 1 && block_tot) block_tot[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  int64_t run = s_warp[warp] + inc - sum;
+#pragma unroll
+  for (int k = 0; k < SCAN_PER_THREAD; ++k) {
+    int64_t i = base + k;
+    int64_t x = v[k];
+    if (i < n) out[i] = run;
+    run += x;
+  }
+}
+
+__global__ void k_scan_add(int64_t* out, int64_t n, const int64_t* offs) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += offs[i / SCAN_ITEMS];
+}
+
+int device_exclusive_scan(axia_ctx* ctx, const int64_t* d_in, int64_t* d_out, int64_t n, int64_t* total) {
+  if (n <= 0) {
+    *total = 0;
+    return AXIA_OK;
+  }
+  const int64_t nb = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
+  int64_t* d_tot = nullptr;
+  int64_t* d_tot_scan = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_tot, nb));
+  AXIA_TRY(dev_alloc(ctx, &d_tot_scan, nb));
+  // last input element (for the total), read before an in-place scan overwrites it
+  int64_t last_in = 0;
+  AXIA_CUDA(ctx, cudaMemcpyAsync(&last_in, d_in + (n - 1), sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  k_scan_block<<<(unsigned)nb, SCAN_THREADS, 0, ctx->stream>>>(d_in, d_out, n, d_tot);
+  AXIA_CUDA(ctx, cudaGetLastError());
+  if (nb > 1) {
+    int64_t t2 = 0;
+    AXIA_TRY(device_exclusive_scan(ctx, d_tot, d_tot_scan, nb, &t2));
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(d_out, n, d_tot_scan);
+    AXIA_CUDA(ctx, cudaGetLastError());
+  }
+  int64_t last_out = 0;
+  AXIA_CUDA(ctx, cudaMemcpyAsync(&last_out, d_out + (n - 1), sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *total = last_out + last_in;
+  dev_free(d_tot);
+  dev_free(d_tot_scan);
+  return AXIA_OK;
+}

@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Static-solve throughput of the GB300 backend (one JSON line on rank 0).
+
+Workload (default): C3D8 block of 100^3 unit elements (1,030,301 nodes), x=0
+clamped, uniform 1 MPa pressure on x=L, interior nodes perturbed by up to
++-0.15 h (seeded), E=210000, nu=0.3 -> 3,060,300 free DOFs, 242,991,882
+entries of K_ff.  The matrix (2.9 GB FP64) is far larger than the 129 MB L2,
+so no flush is needed between steps.
+
+A step = numeric assembly (element stiffness + gather into K_ff + Dirichlet
+elimination) + PCG solve to ||r|| <= 1e-10 ||b|| + reconstruct, on inputs
+already resident in HBM (the symbolic setup is done once, before timing).
+  value : MDOF/s of the mixed-precision path (FP32 inner PCG, FP64 residual
+          refinement), n_free / step time
+  fp64  : the plain FP64 Jacobi-PCG path timed the same way
+  e2e   : the same metric through the C ABI with host buffers: setup (mesh
+          upload + symbolic) + assemble + solve(host f -> host u) per step
+--impl reference times the CPU restatement of the reference's path on the
+host cores instead (see cpu_baseline).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "axia-fem_gb300"))
+
+METRIC = "MDOF/s static solve, mixed vs FP64 PCG at rel err ≤1e-8; SpMV HBM GB/s"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+CPU_SAMPLE_N = 30          # edge count of the CPU-baseline sample block
+RTOL = 1e-10
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def spmv_bytes(nnz, n, vbytes):
+    """Algorithmic bytes of y = K x in CSR with int32 indices: values, columns,
+    row pointers, x once, y once."""
+    return vbytes * nnz + 4 * nnz + 4 * (n + 1) + 2 * vbytes * n
+
+
+def pcg_iter_bytes(nnz, n, vbytes):
+    """Algorithmic bytes of one PCG iteration of the persistent kernel:
+    SpMV (values, columns, row pointers, p once, q written) + x/r update
+    (x r+w, p r, r r+w, q r, dinv r) + p update (r r, dinv r, p r+w)."""
+    return (vbytes + 4) * nnz + 4 * (n + 1) + 2 * vbytes * n + 7 * vbytes * n + 4 * vbytes * n
+
+
+def cpu_baseline(n=CPU_SAMPLE_N, threads=1):
+    """The CPU restatement of the reference's *STATIC path (oracle/) on a
+    bounded sample: the same block, loads and BCs at n^3, full path
+    (element loop -> triplets -> reduce -> CSR -> PCG to rtol 1e-10)."""
+    from axia_gpu import meshgen
+    from oracle import oracle as O
+    m = meshgen.block_c3d8_pressure(n=n)
+    f = O.load_vector(m)
+    t0 = time.perf_counter()
+    r = O.solve_static(m, solver=O.SOLVER_PCG, tol=RTOL, nthreads=threads, f=f)
+    dt = time.perf_counter() - t0
+    return {"value": r.n_free / dt / 1e6, "unit": "MDOF/s", "cores": threads, "kind": "port",
+            "sample": f"C3D8 {n}^3 block, same loads/BCs, full path to rtol {RTOL:g} "
+                      f"({r.n_free} free DOFs, {r.iters} PCG iterations, {dt:.2f} s)",
+            "seconds": dt, "iters": r.iters}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    vals = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        b = cpu_baseline(CPU_SAMPLE_N, threads)
+        if k >= args.warmup:
+            vals.append(b["value"])
+            info = b
+    v = statistics.median(vals)
+    out = {"metric": METRIC, "value": v, "unit": "MDOF/s", "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": info["seconds"] * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded structured C3D8 block)",
+           "config": {"workload": f"C3D8 block {CPU_SAMPLE_N}^3 sample of the 100^3 pressure block",
+                      "rtol": RTOL, "threads": threads},
+           "cpu_baseline": {"value": v, "unit": "MDOF/s", "cores": threads, "kind": "port",
+                            "sample": info["sample"]},
+           "e2e": {"value": v, "unit": "MDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=100, help="edge count of the C3D8 block")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--lanes64", type=int, default=0)
+    ap.add_argument("--lanes32", type=int, default=0)
+    ap.add_argument("--inner", type=float, default=1e-3)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from axia_gpu import GpuContext, _lib as L, meshgen
+
+    model = meshgen.block_c3d8_pressure(n=args.n)
+    ctx = GpuContext(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    f_host = ctx.load_vector(model)
+    t0 = time.perf_counter()
+    ctx.setup(model)
+    setup_s = time.perf_counter() - t0
+    n, nnz = ctx.n_free, ctx.nnz
+    f_dev = torch.from_numpy(f_host).to(f"cuda:{local}")
+    u64 = torch.empty_like(f_dev)
+    umx = torch.empty_like(f_dev)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def timed(prec, u_dev, lanes):
+        infos = []
+        times = []
+        for k in range(args.warmup + args.steps):
+            if k == args.warmup:
+                barrier()
+                l0 = ctx.kernel_launches()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                a.record(stream)
+                ctx.assemble(prec)
+                info = ctx.solve_device(f_dev.data_ptr(), u_dev.data_ptr(), rtol=RTOL, precision=prec,
+                                        inner_rtol=args.inner, spmv_lanes=lanes)
+                b.record(stream)
+            b.synchronize()
+            if k >= args.warmup:
+                times.append(a.elapsed_time(b))
+                infos.append(info.as_dict())
+        barrier()
+        launches = ctx.kernel_launches() - l0
+        ms = sum(times) / len(times)
+        if dist is not None:
+            t = torch.tensor([ms], device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, infos, launches
+
+    with ClockSampler(local) as clk:
+        ms64, inf64, la64 = timed(L.PREC_FP64, u64, args.lanes64)
+        msmx, infmx, lamx = timed(L.PREC_MIXED, umx, args.lanes32)
+    clocks = clk.summary()
+
+    # standalone SpMV bandwidth (FP64 and FP32), x in HBM, y written
+    x64 = torch.rand(n, dtype=torch.float64, device=f"cuda:{local}")
+    y64 = torch.empty_like(x64)
+    x32 = x64.float()
+    y32 = torch.empty_like(x32)
+    spmv = {}
+    for name, prec, x, y, vb, lanes in (("fp64", L.PREC_FP64, x64, y64, 8, args.lanes64),
+                                         ("fp32", L.PREC_MIXED, x32, y32, 4, args.lanes32)):
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                ctx.spmv_device(prec, x.data_ptr(), y.data_ptr(), lanes)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            reps = 20
+            a.record(stream)
+            for _ in range(reps):
+                ctx.spmv_device(prec, x.data_ptr(), y.data_ptr(), lanes)
+            b.record(stream)
+        b.synchronize()
+        ms = a.elapsed_time(b) / reps
+        gbs = spmv_bytes(nnz, n, vb) / (ms * 1e-3) / 1e9
+        spmv[name] = {"ms": ms, "gbs": gbs}
+
+    pk, pk_kind = peaks()
+    hbm = pk["hbm_gbs"]
+    for v in spmv.values():
+        v["frac_of_hbm"] = v["gbs"] / hbm
+
+    # accuracy: mixed vs FP64 solution, both with true FP64 residual <= 1e-10 ||b||
+    u64h = u64.cpu().numpy()
+    umxh = umx.cpu().numpy()
+    rel_mx = float(np.linalg.norm(umxh - u64h) / np.linalg.norm(u64h))
+
+    last64, lastmx = inf64[-1], infmx[-1]
+    mdofs = n / (msmx * 1e-3) / 1e6 * world
+    mdofs64 = n / (ms64 * 1e-3) / 1e6 * world
+
+    # roofline of the dominant kernel: the persistent FP32 PCG kernel of the mixed step
+    it32 = statistics.mean(i["iters"] for i in infmx)
+    k32_ms = statistics.mean(i["ms_pcg_kernel"] for i in infmx)
+    launches32 = statistics.mean(i["pcg_launches"] for i in infmx)
+    bytes32 = pcg_iter_bytes(nnz, n, 4) * it32 / launches32
+    ach32 = bytes32 / (k32_ms / launches32 * 1e-3) / 1e9
+    it64 = statistics.mean(i["iters"] for i in inf64)
+    k64_ms = statistics.mean(i["ms_pcg_kernel"] for i in inf64)
+    bytes64 = pcg_iter_bytes(nnz, n, 8) * it64
+    ach64 = bytes64 / (k64_ms * 1e-3) / 1e9
+
+    e2e = None
+    if not args.no_e2e:
+        # through the C ABI with host buffers: setup (mesh upload) + assemble + solve (host f -> host u)
+        h2d = (model.coords.nbytes + model.conn.astype(np.int32).nbytes + model.e_elem.nbytes +
+               model.bc_dof.nbytes + model.bc_val.nbytes + f_host.nbytes)
+        d2h = f_host.nbytes
+        ctx.set_stream(None)
+        ts = []
+        for k in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx.setup(model)
+            ctx.assemble(L.PREC_MIXED)
+            u, info = ctx.solve(f_host, rtol=RTOL, precision=L.PREC_MIXED, inner_rtol=args.inner,
+                                spmv_lanes=args.lanes32)
+            dt = time.perf_counter() - t0
+            if k >= args.warmup:
+                ts.append(dt)
+        e2e_s = sum(ts) / len(ts)
+        if dist is not None:
+            t = torch.tensor([e2e_s], device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": n / e2e_s / 1e6 * world, "unit": "MDOF/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(CPU_SAMPLE_N, 1)
+        cpu.pop("seconds", None)
+        cpu.pop("iters", None)
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    out = {
+        "metric": METRIC, "value": mdofs, "unit": "MDOF/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": msmx, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded perturbed structured C3D8 block)",
+        "config": {"workload": f"C3D8 block {args.n}^3 unit elements, x=0 clamped, p=1 MPa on x=L, "
+                               f"interior nodes perturbed +-0.15h", "n_free": n, "nnz_kff": nnz,
+                   "rtol": RTOL, "step": "assemble + solve (symbolic setup once)",
+                   "l2": "inputs (2.9 GB matrix) larger than L2, no flush", "parallelism": f"replicas x{world}"},
+        "fp64": {"value": mdofs64, "ms_per_step": ms64, "iters": last64["iters"],
+                 "ms_assemble": last64["ms_assemble"], "ms_solve": last64["ms_solve"],
+                 "true_rel_residual": last64["true_residual"] / last64["bnorm"]},
+        "mixed": {"value": mdofs, "ms_per_step": msmx, "inner_iters": lastmx["iters"],
+                  "outer_iters": lastmx["outer_iters"], "ms_assemble": lastmx["ms_assemble"],
+                  "ms_solve": lastmx["ms_solve"], "true_rel_residual": lastmx["true_residual"] / lastmx["bnorm"],
+                  "rel_err_vs_fp64": rel_mx},
+        "speedup_mixed_vs_fp64": ms64 / msmx,
+        "speedup_mixed_vs_fp64_solve": last64["ms_solve"] / lastmx["ms_solve"],
+        "setup_ms": setup_s * 1e3,
+        "spmv": spmv,
+        "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
+                     "traffic": None, "kernel": "pcg_kernel<float> (FP32 inner PCG, persistent)",
+                     "peak_source": f"{pk_kind} hbm_gbs", "bytes_per_launch": bytes32,
+                     "ms_per_launch": k32_ms / launches32},
+        "roofline_fp64_pcg": {"bound": "hbm", "achieved": ach64, "peak": hbm, "unit": "GB/s", "frac": ach64 / hbm,
+                              "ms_per_launch": k64_ms, "bytes_per_launch": bytes64},
+        "gpu_launches": int(la64 + lamx),
+        "clocks": clocks,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

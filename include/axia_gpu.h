@@ -1,0 +1,198 @@
+/*
+ * axia_gpu.h -- C ABI of the GB300 (sm_103a) linear-static backend for Axia.
+ *
+ * The library replaces, for C3D8 / C3D20(R) continuum models with isotropic
+ * material and single-point constraints, the *STATIC hot path of the
+ * reference solver crate (larsmei/axia-fem, crate axia-fem 1.31.10):
+ *
+ *   element_ke            solver/src/elem.rs:344-375 (Hex8 arm),
+ *                         solver/src/elem.rs:487-495 (Hex20/Hex20R arm)
+ *   element loop + triplet push   solver/src/analysis.rs:574-668
+ *   DofMap::build/reduce  solver/src/constraint.rs:26-172 (prescribed subset)
+ *   solve_kff             solver/src/linalg.rs:311-404 (csr_from_triplets
+ *                         linalg.rs:10-38, pcg linalg.rs:199-259)
+ *   DofMap::reconstruct   solver/src/constraint.rs:207-217
+ *
+ * All pointers are host pointers unless the function name ends in _device.
+ * The caller owns every buffer; the library copies what it needs into device
+ * memory held by the context.  Every call is synchronous: it returns after
+ * the device work has finished.  Errors are status codes, never aborts; the
+ * message of the last error is available from axia_gpu_last_error().
+ *
+ * Threading: a context belongs to one host thread at a time (the reference
+ * selects its backend per process or per thread, solver/src/backend.rs:49-89).
+ */
+#ifndef AXIA_GPU_H
+#define AXIA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AXIA_GPU_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define AXIA_API __attribute__((visibility("default")))
+#else
+#define AXIA_API
+#endif
+
+/* Status codes.  The reference returns Result<_, FemError(String)>
+ * (solver/src/error.rs:1-18); each code names the reference error it stands for. */
+typedef enum axia_status {
+  AXIA_OK = 0,
+  AXIA_ERR_INVALID_ARG = 1,        /* bad size, index or pointer */
+  AXIA_ERR_SINGULAR_JACOBIAN = 2,  /* |det J| < 1e-18, elem.rs:14-16 */
+  AXIA_ERR_NEG_JACOBIAN = 3,       /* det J <= 0, elem.rs:208-210, quadratic.rs:137-139 */
+  AXIA_ERR_MATERIAL = 4,           /* nu >= 0.5, nu <= -1 or E <= 0, elem.rs:42-47 */
+  AXIA_ERR_NOT_CONVERGED = 5,      /* final ||r|| > 10 tol ||b||, linalg.rs:253-257 */
+  AXIA_ERR_ZERO_PIVOT = 6,         /* |p.Ap| < 1e-30, linalg.rs:231-232 */
+  AXIA_ERR_NO_FREE_DOF = 9,        /* constraint.rs:111-113 */
+  AXIA_ERR_NONFINITE = 10,         /* NaN / Inf in coordinates, loads or iterates */
+  AXIA_ERR_CUDA = 11,              /* a CUDA runtime call failed */
+  AXIA_ERR_OOM = 12,               /* device allocation failed */
+  AXIA_ERR_TIMEOUT = 13,           /* a device-side wait ran past its limit */
+  AXIA_ERR_STATE = 14,             /* call order: e.g. solve before setup */
+  AXIA_ERR_TOO_LARGE = 15          /* a size above a documented limit */
+} axia_status;
+
+typedef enum axia_precision {
+  AXIA_PREC_FP64 = 0,   /* K in FP64 CSR, FP64 Jacobi-PCG */
+  AXIA_PREC_MIXED = 1   /* K in FP32 CSR for an FP32 inner PCG, FP64 residual and update */
+} axia_precision;
+
+typedef enum axia_refine_mode {
+  AXIA_REFINE_RESTART = 0,   /* classic iterative refinement: each inner solve restarts from 0 */
+  AXIA_REFINE_RELIABLE = 1   /* one FP32 Krylov sequence, FP64 residual replaced at each update */
+} axia_refine_mode;
+
+/* A C3D8 / C3D20 mesh.  Node d of node a has full DOF index 3*a + d
+ * (solver/src/analysis.rs:152-154 with ndn = 3, model.rs:1220-1232). */
+typedef struct axia_mesh {
+  int64_t n_nodes;
+  const double* coords;    /* [n_nodes][3] */
+  int64_t n_elem;
+  int32_t nn;              /* nodes per element: 8 (C3D8) or 20 (C3D20) */
+  int32_t reduced;         /* 1: C3D20R, 2x2x2 Gauss points (quadratic.rs:100-120) */
+  const int32_t* conn;     /* [n_elem][nn], 0-based node indices, CalculiX node order */
+  const double* e_elem;    /* [n_elem] Young's modulus per element, or NULL */
+  double e;                /* Young's modulus when e_elem == NULL */
+  double nu;               /* Poisson's ratio */
+} axia_mesh;
+
+typedef struct axia_solve_opts {
+  double rtol;             /* stop when ||r||_2 <= rtol ||b||_2 (reference: 1e-8, linalg.rs:363) */
+  int64_t max_iter;        /* <= 0: max(4 n, 200) as linalg.rs:376 */
+  int32_t precision;       /* axia_precision */
+  int32_t refine_mode;     /* axia_refine_mode (mixed only) */
+  double inner_rtol;       /* mixed: residual reduction per refinement step (e.g. 1e-3) */
+  int32_t max_outer;       /* mixed: refinement steps allowed */
+  int32_t spmv_lanes;      /* lanes per CSR row in the SpMV: 0 = automatic, else 4, 8, 16 or 32 */
+} axia_solve_opts;
+
+typedef struct axia_solve_info {
+  int64_t n_free;          /* independent DOFs (DofMap n_ind) */
+  int64_t nnz;             /* stored entries of K_ff */
+  int64_t iters;           /* PCG iterations (FP32 inner iterations for mixed) */
+  int64_t outer_iters;     /* refinement steps (mixed), 1 for FP64 */
+  double residual;         /* final ||b - K_ff x||_2 as the solver tracks it */
+  double bnorm;            /* ||b||_2 of the reduced right-hand side */
+  double true_residual;    /* ||b - K_ff x||_2 recomputed in FP64 after the solve */
+  double ms_setup;         /* symbolic phase (pattern, DOF map) */
+  double ms_assemble;      /* element integration + gather into K_ff */
+  double ms_solve;         /* PCG (+ refinement) */
+  double ms_pcg_kernel;    /* device time of the persistent PCG kernel launches (CUDA events) */
+  int64_t pcg_launches;    /* persistent PCG kernel launches of this solve */
+  int64_t bad_index;       /* element / load index of an element error, else -1 */
+  int32_t status;          /* axia_status of the call */
+  int32_t reserved;
+} axia_solve_info;
+
+typedef struct axia_ctx axia_ctx;
+
+/* Library ABI version (AXIA_GPU_ABI_VERSION). */
+AXIA_API int32_t axia_gpu_abi_version(void);
+
+/* Creates a context on CUDA device `device`.  Returns NULL and sets *status
+ * on failure (no device, CUDA error). */
+AXIA_API axia_ctx* axia_gpu_create(int32_t device, int32_t* status);
+AXIA_API void axia_gpu_destroy(axia_ctx* ctx);
+/* Message of the last failed call on ctx ("" when none). */
+AXIA_API const char* axia_gpu_last_error(const axia_ctx* ctx);
+
+/* Batched element_ke (solver/src/elem.rs:344-375 Hex8 arm, :487-495 Hex20
+ * arm, hex8_stiffness elem.rs:194-219, hex20_stiffness quadratic.rs:122-146):
+ * for n_elem elements with nn nodes each, xyz[n_elem][nn][3] -> ke[n_elem]
+ * [3nn][3nn] row-major (DOF order node-major, x y z) and vol[n_elem].
+ * e[n_elem] per element.  On an element error *bad_elem holds its index. */
+AXIA_API int32_t axia_gpu_element_ke(axia_ctx* ctx, int32_t nn, int32_t reduced, int64_t n_elem,
+                            const double* xyz, const double* e, double nu, double* ke,
+                            double* vol, int64_t* bad_elem);
+
+/* Consistent nodal forces of face pressures added into f_full[3*n_nodes], in
+ * list order, on the host (apply_pressure solver/src/analysis.rs:1365-1396 ->
+ * hex8_face_pressure elem.rs:891-950 / hex20_face_pressure quadratic.rs:275-315).
+ * face is 1..6 (P1..P6); positive pressure compresses. */
+AXIA_API int32_t axia_face_loads(int32_t nn, int64_t n_nodes, const double* coords, const int32_t* conn,
+                        int64_t n_loads, const int64_t* elem, const int32_t* face,
+                        const double* p, double* f_full, int64_t* bad_load);
+
+/* Symbolic phase for a mesh and its single-point constraints: uploads the
+ * mesh, builds node incidence and adjacency, the independent-DOF numbering
+ * (ascending full-DOF order, constraint.rs:103-110) and the CSR pattern of
+ * K_ff.  bc_dof/bc_val are full DOF indices and values; a later entry for the
+ * same DOF wins (analysis.rs:556-565).  Nodes no element touches are pinned
+ * (analysis.rs:2283-2330).  Limits: nn*3 <= 60, nnz(K_ff) < 2^31. */
+AXIA_API int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const int64_t* bc_dof,
+                       const double* bc_val);
+
+/* Numeric phase: element stiffness on the device and deterministic gather
+ * into K_ff (values in the reference's element order), the Jacobi diagonal
+ * and K_fp u0 (the prescribed-value part of constraint.rs:161-165).
+ * precision AXIA_PREC_MIXED also stores an FP32 copy of K_ff. */
+AXIA_API int32_t axia_gpu_assemble(axia_ctx* ctx, int32_t precision);
+
+/* Static solve: rhs = f_free - K_fp u0, PCG on K_ff, u_full = u0 + T x
+ * (reconstruct).  f_full[3*n_nodes] in, u_full[3*n_nodes] out (host). */
+AXIA_API int32_t axia_gpu_solve(axia_ctx* ctx, const double* f_full, double* u_full,
+                       const axia_solve_opts* opts, axia_solve_info* info);
+
+/* Same with f_full and u_full in device memory (for callers that keep the
+ * load and displacement vectors resident on the GPU). */
+AXIA_API int32_t axia_gpu_solve_device(axia_ctx* ctx, const double* f_full_dev, double* u_full_dev,
+                              const axia_solve_opts* opts, axia_solve_info* info);
+
+/* Runs the context's work on `stream` (a cudaStream_t; NULL restores the
+ * context's own stream), so a caller can order it with its own work and time
+ * it with events on that stream. */
+AXIA_API int32_t axia_gpu_set_stream(axia_ctx* ctx, void* stream);
+
+/* Number of kernels the context has launched so far. */
+AXIA_API int64_t axia_gpu_kernel_launches(const axia_ctx* ctx);
+
+/* y = K_ff x on device vectors of n_free entries: FP64 (double x, y) with
+ * precision AXIA_PREC_FP64, FP32 (float x, y, the FP32 copy of K_ff) with
+ * AXIA_PREC_MIXED.  lanes: CSR lanes per row (0 = automatic).  The matrix
+ * product of Csr::matvec (solver/src/linalg.rs:41-50). */
+AXIA_API int32_t axia_gpu_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev,
+                                      int32_t lanes);
+
+/* Sizes of the assembled system: n_free and nnz. */
+AXIA_API int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz);
+
+/* Copies K_ff (CSR, int32 indices, FP64 values), the Jacobi diagonal and
+ * K_fp u0 to host buffers of n_free+1, nnz, nnz, n_free, n_free entries.
+ * Any pointer may be NULL. */
+AXIA_API int32_t axia_gpu_export_system(const axia_ctx* ctx, int32_t* rowptr, int32_t* col, double* val,
+                               double* diag, double* kfu0);
+
+/* Independent-DOF index of every full DOF (-1 = prescribed), n_full entries. */
+AXIA_API int32_t axia_gpu_export_dofmap(const axia_ctx* ctx, int32_t* ind_of);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AXIA_GPU_H */

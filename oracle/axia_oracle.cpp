@@ -1,0 +1,871 @@
+// axia_oracle.cpp -- CPU restatement of the Axia linear-static path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the
+// smoke check and the CPU-baseline leg of bench.py call it as the checker.
+// The product library (libaxia_gpu.so) never links, loads or calls it.
+//
+// It restates, in plain C++17 / FP64 and in the reference's loop order, the
+// Rust functions of larsmei/axia-fem (crate axia-fem 1.31.10) on the *STATIC
+// path for C3D8 / C3D20:
+//   solver/src/elem.rs        invert3 (10-29), d_iso_3d (41-59),
+//                             gemm_bt_d_b (90-112), fill_b3 (114-132),
+//                             HEX_XI / hex8_shape / hex8_dndx (147-192),
+//                             hex8_stiffness(_d) (194-219),
+//                             hex8_face_pressure (891-950)
+//   solver/src/quadratic.rs   G3/W3 (10-11), HEX20_XI (13-34),
+//                             hex20_shape / hex20_dndx (36-98),
+//                             hex_gauss (100-120), hex20_stiffness (122-146),
+//                             HEX20_FACE / hex20_face_pressure (265-315),
+//                             quad8_shape (328-353)
+//   solver/src/analysis.rs    prescribed "last BC wins" (556-565),
+//                             pin_unused_dofs isolated nodes (2283-2330),
+//                             element loop + triplet push (574-668),
+//                             autospc_null_diag (2164-2228),
+//                             reduce / solve_kff / reconstruct (1018-1025)
+//   solver/src/constraint.rs  DofMap::build (26-136, prescribed subset),
+//                             DofMap::reduce (138-172), reconstruct (207-217)
+//   solver/src/linalg.rs      csr_from_triplets (10-38), matvec (41-50),
+//                             diag (52-63), chol_solve (78-117), pcg (199-259),
+//                             residual_of (268-278)
+//   solver/src/sparse_native.rs residual_ok (1572-1578)
+// The compliance-gradient routine at the end has no reference counterpart:
+// the reference has no adjoint code.  It restates dC/drho_e =
+// -p rho_e^(p-1) E0 u_e^T K_e(E=1) u_e on top of the restated hex8 stiffness.
+//
+// Build: oracle/build_oracle.sh (g++ -O2 -ffp-contract=off, so that products
+// and sums round separately, as rustc emits them).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+enum Status : int {
+  OK = 0,
+  ERR_INVALID_ARG = 1,
+  ERR_SINGULAR_JACOBIAN = 2,
+  ERR_NEG_JACOBIAN = 3,
+  ERR_MATERIAL = 4,
+  ERR_NOT_CONVERGED = 5,
+  ERR_ZERO_PIVOT = 6,
+  ERR_INDEFINITE = 7,
+  ERR_SINGULAR = 8,
+  ERR_NO_FREE_DOF = 9,
+};
+
+const double G2 = 0.5773502691896257;  // elem.rs:8
+const double G3[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};  // quadratic.rs:10
+const double W3[3] = {0.5555555555555556, 0.8888888888888888, 0.5555555555555556};  // quadratic.rs:11
+
+const double HEX_XI[8][3] = {  // elem.rs:147-156
+    {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+    {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+
+const double HEX20_XI[20][3] = {  // quadratic.rs:13-34
+    {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, 1},
+    {1, -1, 1},   {1, 1, 1},   {-1, 1, 1}, {0, -1, -1}, {1, 0, -1},
+    {0, 1, -1},   {-1, 0, -1}, {0, -1, 1}, {1, 0, 1},   {0, 1, 1},
+    {-1, 0, 1},   {-1, -1, 0}, {1, -1, 0}, {1, 1, 0},   {-1, 1, 0}};
+
+const int HEX8_FACE[6][4] = {  // elem.rs:894-901
+    {0, 1, 2, 3}, {4, 7, 6, 5}, {0, 4, 5, 1}, {1, 5, 6, 2}, {2, 6, 7, 3}, {3, 7, 4, 0}};
+
+const int HEX20_FACE[6][8] = {  // quadratic.rs:266-273
+    {0, 1, 2, 3, 8, 9, 10, 11},     {4, 7, 6, 5, 15, 14, 13, 12},
+    {0, 4, 5, 1, 16, 12, 17, 8},    {1, 5, 6, 2, 17, 13, 18, 9},
+    {2, 6, 7, 3, 18, 14, 19, 10},   {3, 7, 4, 0, 19, 15, 16, 11}};
+
+const double QUAD_XI[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};  // elem.rs:250
+const double QUAD8_XI[8][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1},
+                               {0, -1},  {1, 0},  {0, 1}, {-1, 0}};  // quadratic.rs:316-325
+
+// elem.rs:10-29
+int invert3(const double a[3][3], double b[3][3], double* det_out) {
+  double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) -
+               a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+               a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+  if (std::fabs(det) < 1e-18) return ERR_SINGULAR_JACOBIAN;
+  double inv_det = 1.0 / det;
+  b[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) * inv_det;
+  b[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * inv_det;
+  b[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) * inv_det;
+  b[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) * inv_det;
+  b[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) * inv_det;
+  b[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * inv_det;
+  b[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) * inv_det;
+  b[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * inv_det;
+  b[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) * inv_det;
+  *det_out = det;
+  return OK;
+}
+
+// elem.rs:41-59
+int d_iso_3d(double e, double nu, double d[36]) {
+  if (nu >= 0.5 || nu <= -1.0) return ERR_MATERIAL;
+  if (e <= 0.0) return ERR_MATERIAL;
+  double lam = e * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  double mu = e / (2.0 * (1.0 + nu));
+  for (int i = 0; i < 36; ++i) d[i] = 0.0;
+  double diag = lam + 2.0 * mu;
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) d[i * 6 + j] = (i == j) ? diag : lam;
+    d[(i + 3) * 6 + (i + 3)] = mu;
+  }
+  return OK;
+}
+
+// elem.rs:90-112 -- tmp = D*B, ke += w * B^T * tmp (dense, as written)
+void gemm_bt_d_b(double* ke, int n, const double* b, int nrow, const double* d, double w,
+                 std::vector<double>& tmp) {
+  tmp.assign((size_t)nrow * n, 0.0);
+  for (int i = 0; i < nrow; ++i)
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < nrow; ++k) s += d[i * nrow + k] * b[k * n + j];
+      tmp[(size_t)i * n + j] = s;
+    }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < nrow; ++k) s += b[k * n + i] * tmp[(size_t)k * n + j];
+      ke[(size_t)i * n + j] += w * s;
+    }
+}
+
+// elem.rs:114-132
+void fill_b3(double* b, int nnode, const double (*dndx)[3]) {
+  int n = 3 * nnode;
+  for (int i = 0; i < nnode; ++i) {
+    int c = 3 * i;
+    double dx = dndx[i][0], dy = dndx[i][1], dz = dndx[i][2];
+    b[0 * n + c] = dx;
+    b[1 * n + c + 1] = dy;
+    b[2 * n + c + 2] = dz;
+    b[3 * n + c] = dy;
+    b[3 * n + c + 1] = dx;
+    b[4 * n + c + 1] = dz;
+    b[4 * n + c + 2] = dy;
+    b[5 * n + c] = dz;
+    b[5 * n + c + 2] = dx;
+  }
+}
+
+// elem.rs:158-171
+void hex8_shape(double xi, double eta, double zeta, double n[8], double dn[8][3]) {
+  for (int i = 0; i < 8; ++i) {
+    double x = HEX_XI[i][0], e = HEX_XI[i][1], z = HEX_XI[i][2];
+    n[i] = 0.125 * (1.0 + x * xi) * (1.0 + e * eta) * (1.0 + z * zeta);
+    dn[i][0] = 0.125 * x * (1.0 + e * eta) * (1.0 + z * zeta);
+    dn[i][1] = 0.125 * e * (1.0 + x * xi) * (1.0 + z * zeta);
+    dn[i][2] = 0.125 * z * (1.0 + x * xi) * (1.0 + e * eta);
+  }
+}
+
+// quadratic.rs:36-73
+void hex20_shape(double xi, double eta, double zeta, double n[20], double dn[20][3]) {
+  for (int i = 0; i < 8; ++i) {
+    double x = HEX20_XI[i][0], e = HEX20_XI[i][1], z = HEX20_XI[i][2];
+    double a = 1.0 + x * xi, b = 1.0 + e * eta, c = 1.0 + z * zeta;
+    n[i] = 0.125 * a * b * c * (x * xi + e * eta + z * zeta - 2.0);
+    dn[i][0] = 0.125 * x * b * c * (2.0 * x * xi + e * eta + z * zeta - 1.0);
+    dn[i][1] = 0.125 * e * a * c * (x * xi + 2.0 * e * eta + z * zeta - 1.0);
+    dn[i][2] = 0.125 * z * a * b * (x * xi + e * eta + 2.0 * z * zeta - 1.0);
+  }
+  for (int i = 8; i < 20; ++i) {
+    double x = HEX20_XI[i][0], e = HEX20_XI[i][1], z = HEX20_XI[i][2];
+    if (std::fabs(x) < 0.5) {
+      n[i] = 0.25 * (1.0 - xi * xi) * (1.0 + e * eta) * (1.0 + z * zeta);
+      dn[i][0] = 0.25 * (-2.0 * xi) * (1.0 + e * eta) * (1.0 + z * zeta);
+      dn[i][1] = 0.25 * (1.0 - xi * xi) * e * (1.0 + z * zeta);
+      dn[i][2] = 0.25 * (1.0 - xi * xi) * (1.0 + e * eta) * z;
+    } else if (std::fabs(e) < 0.5) {
+      n[i] = 0.25 * (1.0 - eta * eta) * (1.0 + x * xi) * (1.0 + z * zeta);
+      dn[i][0] = 0.25 * (1.0 - eta * eta) * x * (1.0 + z * zeta);
+      dn[i][1] = 0.25 * (-2.0 * eta) * (1.0 + x * xi) * (1.0 + z * zeta);
+      dn[i][2] = 0.25 * (1.0 - eta * eta) * (1.0 + x * xi) * z;
+    } else {
+      n[i] = 0.25 * (1.0 - zeta * zeta) * (1.0 + x * xi) * (1.0 + e * eta);
+      dn[i][0] = 0.25 * (1.0 - zeta * zeta) * x * (1.0 + e * eta);
+      dn[i][1] = 0.25 * (1.0 - zeta * zeta) * (1.0 + x * xi) * e;
+      dn[i][2] = 0.25 * (-2.0 * zeta) * (1.0 + x * xi) * (1.0 + e * eta);
+    }
+  }
+}
+
+// elem.rs:173-192 / quadratic.rs:75-98: J[q][p] = sum_a dN_a/dxi_p x_a,q;
+// dN/dx = J^-T dN/dxi.
+template <int NN>
+int hex_dndx(const double* xyz, const double dn[NN][3], double dndx[NN][3], double* det) {
+  double j[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int a = 0; a < NN; ++a)
+    for (int p = 0; p < 3; ++p)
+      for (int q = 0; q < 3; ++q) j[q][p] += dn[a][p] * xyz[3 * a + q];
+  double inv[3][3];
+  int st = invert3(j, inv, det);
+  if (st) return st;
+  for (int a = 0; a < NN; ++a)
+    for (int i = 0; i < 3; ++i)
+      dndx[a][i] = inv[0][i] * dn[a][0] + inv[1][i] * dn[a][1] + inv[2][i] * dn[a][2];
+  return OK;
+}
+
+// elem.rs:199-219
+int hex8_stiffness_d(const double* xyz, const double d[36], double* ke, double* vol_out) {
+  const int n = 24;
+  std::fill(ke, ke + n * n, 0.0);
+  double vol = 0.0;
+  const double pts[2] = {-G2, G2};
+  std::vector<double> b(6 * n), tmp;
+  for (double xi : pts)
+    for (double eta : pts)
+      for (double zeta : pts) {
+        double N[8], dn[8][3], dndx[8][3], det;
+        hex8_shape(xi, eta, zeta, N, dn);
+        int st = hex_dndx<8>(xyz, dn, dndx, &det);
+        if (st) return st;
+        if (det <= 0.0) return ERR_NEG_JACOBIAN;
+        std::fill(b.begin(), b.end(), 0.0);
+        fill_b3(b.data(), 8, dndx);
+        gemm_bt_d_b(ke, n, b.data(), 6, d, det, tmp);
+        vol += det;
+      }
+  *vol_out = vol;
+  return OK;
+}
+
+// quadratic.rs:100-120
+void hex_gauss(bool reduced, std::vector<double>& pts /* xi,eta,zeta,w */) {
+  pts.clear();
+  if (reduced) {
+    const double g[2] = {-G2, G2};
+    for (double xi : g)
+      for (double eta : g)
+        for (double zeta : g) pts.insert(pts.end(), {xi, eta, zeta, 1.0});
+  } else {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) pts.insert(pts.end(), {G3[i], G3[j], G3[k], W3[i] * W3[j] * W3[k]});
+  }
+}
+
+// quadratic.rs:122-146
+int hex20_stiffness(const double* xyz, double e, double nu, bool reduced, double* ke, double* vol_out) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const int n = 60;
+  std::fill(ke, ke + n * n, 0.0);
+  double vol = 0.0;
+  std::vector<double> gp, b(6 * n), tmp;
+  hex_gauss(reduced, gp);
+  for (size_t g = 0; g < gp.size(); g += 4) {
+    double N[20], dn[20][3], dndx[20][3], det;
+    hex20_shape(gp[g], gp[g + 1], gp[g + 2], N, dn);
+    st = hex_dndx<20>(xyz, dn, dndx, &det);
+    if (st) return st;
+    if (det <= 0.0) return ERR_NEG_JACOBIAN;
+    std::fill(b.begin(), b.end(), 0.0);
+    fill_b3(b.data(), 20, dndx);
+    gemm_bt_d_b(ke, n, b.data(), 6, d, gp[g + 3] * det, tmp);
+    vol += gp[g + 3] * det;
+  }
+  *vol_out = vol;
+  return OK;
+}
+
+// elem.rs:891-950
+int hex8_face_pressure(const double* xyz, int face, double p, double fe[24]) {
+  if (face < 1 || face > 6) return ERR_INVALID_ARG;
+  int fi = face - 1;
+  for (int i = 0; i < 24; ++i) fe[i] = 0.0;
+  const double pts[2] = {-G2, G2};
+  for (double xi : pts)
+    for (double eta : pts) {
+      double n[4], dnxi[4], dneta[4];
+      for (int i = 0; i < 4; ++i) {
+        double x = QUAD_XI[i][0], e = QUAD_XI[i][1];
+        n[i] = 0.25 * (1.0 + x * xi) * (1.0 + e * eta);
+        dnxi[i] = 0.25 * x * (1.0 + e * eta);
+        dneta[i] = 0.25 * e * (1.0 + x * xi);
+      }
+      double rxi[3] = {0, 0, 0}, reta[3] = {0, 0, 0};
+      for (int a = 0; a < 4; ++a) {
+        const double* q = xyz + 3 * HEX8_FACE[fi][a];
+        for (int k = 0; k < 3; ++k) {
+          rxi[k] += dnxi[a] * q[k];
+          reta[k] += dneta[a] * q[k];
+        }
+      }
+      double nx = rxi[1] * reta[2] - rxi[2] * reta[1];
+      double ny = rxi[2] * reta[0] - rxi[0] * reta[2];
+      double nz = rxi[0] * reta[1] - rxi[1] * reta[0];
+      double tx = p * nx, ty = p * ny, tz = p * nz;
+      for (int a = 0; a < 4; ++a) {
+        int gd = 3 * HEX8_FACE[fi][a];
+        fe[gd] += n[a] * tx;
+        fe[gd + 1] += n[a] * ty;
+        fe[gd + 2] += n[a] * tz;
+      }
+    }
+  return OK;
+}
+
+// quadratic.rs:328-353
+void quad8_shape(double xi, double eta, double n[8], double dn[8][2]) {
+  for (int i = 0; i < 4; ++i) {
+    double x = QUAD8_XI[i][0], e = QUAD8_XI[i][1];
+    double a = 1.0 + x * xi, b = 1.0 + e * eta;
+    n[i] = 0.25 * a * b * (x * xi + e * eta - 1.0);
+    dn[i][0] = 0.25 * x * b * (2.0 * x * xi + e * eta);
+    dn[i][1] = 0.25 * e * a * (x * xi + 2.0 * e * eta);
+  }
+  for (int i = 4; i < 8; ++i) {
+    double x = QUAD8_XI[i][0], e = QUAD8_XI[i][1];
+    if (std::fabs(x) < 0.5) {
+      n[i] = 0.5 * (1.0 - xi * xi) * (1.0 + e * eta);
+      dn[i][0] = -xi * (1.0 + e * eta);
+      dn[i][1] = 0.5 * (1.0 - xi * xi) * e;
+    } else {
+      n[i] = 0.5 * (1.0 - eta * eta) * (1.0 + x * xi);
+      dn[i][0] = 0.5 * (1.0 - eta * eta) * x;
+      dn[i][1] = -eta * (1.0 + x * xi);
+    }
+  }
+}
+
+// quadratic.rs:275-315
+int hex20_face_pressure(const double* xyz, int face, double p, double fe[60]) {
+  if (face < 1 || face > 6) return ERR_INVALID_ARG;
+  int fi = face - 1;
+  for (int i = 0; i < 60; ++i) fe[i] = 0.0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double xi = G3[i], eta = G3[j], w = W3[i] * W3[j];
+      double nshp[8], dn[8][2];
+      quad8_shape(xi, eta, nshp, dn);
+      double rxi[3] = {0, 0, 0}, reta[3] = {0, 0, 0};
+      for (int a = 0; a < 8; ++a) {
+        const double* q = xyz + 3 * HEX20_FACE[fi][a];
+        for (int k = 0; k < 3; ++k) {
+          rxi[k] += dn[a][0] * q[k];
+          reta[k] += dn[a][1] * q[k];
+        }
+      }
+      double nx = rxi[1] * reta[2] - rxi[2] * reta[1];
+      double ny = rxi[2] * reta[0] - rxi[0] * reta[2];
+      double nz = rxi[0] * reta[1] - rxi[1] * reta[0];
+      double tx = p * nx * w, ty = p * ny * w, tz = p * nz * w;
+      for (int a = 0; a < 8; ++a) {
+        int gd = 3 * HEX20_FACE[fi][a];
+        fe[gd] += nshp[a] * tx;
+        fe[gd + 1] += nshp[a] * ty;
+        fe[gd + 2] += nshp[a] * tz;
+      }
+    }
+  return OK;
+}
+
+int element_ke(int nn, const double* xyz, double e, double nu, int reduced, double* ke, double* vol) {
+  if (nn == 8) {
+    double d[36];
+    int st = d_iso_3d(e, nu, d);
+    if (st) return st;
+    return hex8_stiffness_d(xyz, d, ke, vol);
+  }
+  if (nn == 20) return hex20_stiffness(xyz, e, nu, reduced != 0, ke, vol);
+  return ERR_INVALID_ARG;
+}
+
+// A triplet as the reference stores it: (usize, usize, f64).
+struct Trip {
+  uint64_t i, j;
+  double v;
+};
+
+// linalg.rs:3-8
+struct Csr {
+  size_t n = 0;
+  std::vector<uint64_t> indptr, indices;
+  std::vector<double> data;
+};
+
+// linalg.rs:10-38: drop out-of-range and zero entries, stable sort by (i,j),
+// sum duplicates in input order (explicit zero sums are kept).
+void csr_from_triplets(size_t n, std::vector<Trip>& trips, Csr& out) {
+  trips.erase(std::remove_if(trips.begin(), trips.end(),
+                             [n](const Trip& t) { return !(t.i < n && t.j < n && std::fabs(t.v) > 0.0); }),
+              trips.end());
+  std::stable_sort(trips.begin(), trips.end(), [](const Trip& a, const Trip& b) {
+    return a.i != b.i ? a.i < b.i : a.j < b.j;
+  });
+  out.n = n;
+  out.indptr.assign(n + 1, 0);
+  out.indices.clear();
+  out.data.clear();
+  out.indices.reserve(trips.size());
+  out.data.reserve(trips.size());
+  size_t k = 0;
+  while (k < trips.size()) {
+    uint64_t i = trips[k].i, j = trips[k].j;
+    double v = 0.0;
+    while (k < trips.size() && trips[k].i == i && trips[k].j == j) {
+      v += trips[k].v;
+      ++k;
+    }
+    out.indices.push_back(j);
+    out.data.push_back(v);
+    out.indptr[i + 1] += 1;
+  }
+  for (size_t i = 0; i < n; ++i) out.indptr[i + 1] += out.indptr[i];
+}
+
+// linalg.rs:41-50 (serial as written; nthreads > 1 splits rows over OpenMP,
+// each row is still summed in column order so the result is unchanged).
+void matvec(const Csr& a, const double* x, double* y, int nthreads) {
+  const int64_t n = (int64_t)a.n;
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+  for (int64_t i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (uint64_t k = a.indptr[i]; k < a.indptr[i + 1]; ++k) s += a.data[k] * x[a.indices[k]];
+    y[i] = s;
+  }
+}
+
+// linalg.rs:52-63
+std::vector<double> csr_diag(const Csr& a) {
+  std::vector<double> d(a.n, 0.0);
+  for (size_t i = 0; i < a.n; ++i)
+    for (uint64_t k = a.indptr[i]; k < a.indptr[i + 1]; ++k)
+      if (a.indices[k] == i) {
+        d[i] = a.data[k];
+        break;
+      }
+  return d;
+}
+
+double dotp(const double* a, const double* b, int64_t n, int nthreads) {
+  if (nthreads <= 1) {
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+  }
+  double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static) num_threads(nthreads)
+  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+// linalg.rs:199-259.  nthreads == 1 reproduces the serial reference order.
+int pcg(const Csr& a, const double* b, double tol, size_t max_iter, int nthreads, double* x,
+        size_t* iters_out, double* residual_out) {
+  const int64_t n = (int64_t)a.n;
+  std::fill(x, x + n, 0.0);
+  std::vector<double> r(b, b + n);
+  double bnorm = 0.0;
+  for (int64_t i = 0; i < n; ++i) bnorm += b[i] * b[i];
+  bnorm = std::sqrt(bnorm);
+  if (bnorm < 1e-30) {
+    *iters_out = 0;
+    *residual_out = 0.0;
+    return OK;
+  }
+  std::vector<double> diag = csr_diag(a);
+  std::vector<double> z(n), p, ap(n);
+  for (int64_t i = 0; i < n; ++i) z[i] = r[i] / (std::fabs(diag[i]) > 1e-30 ? diag[i] : 1.0);
+  p = z;
+  double rz = dotp(r.data(), z.data(), n, nthreads);
+  size_t iters = 0;
+  double residual = bnorm;
+  for (size_t it = 0; it < max_iter; ++it) {
+    iters = it + 1;
+    matvec(a, p.data(), ap.data(), nthreads);
+    double pap = dotp(p.data(), ap.data(), n, nthreads);
+    if (std::fabs(pap) < 1e-30) {
+      *iters_out = iters;
+      *residual_out = residual;
+      return ERR_ZERO_PIVOT;
+    }
+    double alpha = rz / pap;
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+    for (int64_t i = 0; i < n; ++i) {
+      x[i] += alpha * p[i];
+      r[i] -= alpha * ap[i];
+    }
+    residual = std::sqrt(dotp(r.data(), r.data(), n, nthreads));
+    if (residual <= tol * bnorm) break;
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+    for (int64_t i = 0; i < n; ++i) z[i] = r[i] / (std::fabs(diag[i]) > 1e-30 ? diag[i] : 1.0);
+    double rz_new = dotp(r.data(), z.data(), n, nthreads);
+    double beta = rz_new / rz;
+#pragma omp parallel for schedule(static) num_threads(nthreads) if (nthreads > 1)
+    for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    rz = rz_new;
+  }
+  *iters_out = iters;
+  *residual_out = residual;
+  if (residual > tol * bnorm * 10.0) return ERR_NOT_CONVERGED;
+  return OK;
+}
+
+// linalg.rs:78-117
+int chol_solve(double* a, size_t n, const double* b, double* x) {
+  for (size_t i = 0; i < n; ++i)
+    for (size_t j = 0; j <= i; ++j) {
+      double s = a[i * n + j];
+      for (size_t k = 0; k < j; ++k) s -= a[i * n + k] * a[j * n + k];
+      if (i == j) {
+        if (s < 0.0) return ERR_INDEFINITE;
+        if (s <= 1e-30) return ERR_SINGULAR;
+        a[i * n + i] = std::sqrt(s);
+      } else {
+        a[i * n + j] = s / a[j * n + j];
+      }
+    }
+  std::vector<double> y(n);
+  for (size_t i = 0; i < n; ++i) {
+    double s = b[i];
+    for (size_t k = 0; k < i; ++k) s -= a[i * n + k] * y[k];
+    y[i] = s / a[i * n + i];
+  }
+  for (size_t ii = n; ii-- > 0;) {
+    double s = y[ii];
+    for (size_t k = ii + 1; k < n; ++k) s -= a[k * n + ii] * x[k];
+    x[ii] = s / a[ii * n + ii];
+  }
+  return OK;
+}
+
+// linalg.rs:268-278
+double residual_of(const Csr& a, const double* x, const double* b) {
+  std::vector<double> ax(a.n);
+  matvec(a, x, ax.data(), 1);
+  double s = 0.0;
+  for (size_t i = 0; i < a.n; ++i) {
+    double d = ax[i] - b[i];
+    s += d * d;
+  }
+  return std::sqrt(s);
+}
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+extern "C" {
+
+int or_version() { return 1; }
+
+void or_hex8_shape(double xi, double eta, double zeta, double* n, double* dn) {
+  hex8_shape(xi, eta, zeta, n, reinterpret_cast<double(*)[3]>(dn));
+}
+void or_hex20_shape(double xi, double eta, double zeta, double* n, double* dn) {
+  hex20_shape(xi, eta, zeta, n, reinterpret_cast<double(*)[3]>(dn));
+}
+void or_quad8_shape(double xi, double eta, double* n, double* dn) {
+  quad8_shape(xi, eta, n, reinterpret_cast<double(*)[2]>(dn));
+}
+int or_invert3(const double* a9, double* inv9, double* det) {
+  double a[3][3], b[3][3];
+  std::memcpy(a, a9, sizeof(a));
+  int st = invert3(a, b, det);
+  if (st == OK) std::memcpy(inv9, b, sizeof(b));
+  return st;
+}
+int or_d_iso_3d(double e, double nu, double* d36) { return d_iso_3d(e, nu, d36); }
+
+// element_ke (elem.rs:344-375 Hex8 arm, elem.rs:487-495 Hex20 arm) for one element.
+int or_element_ke(int nn, const double* xyz, double e, double nu, int reduced, double* ke, double* vol) {
+  return element_ke(nn, xyz, e, nu, reduced, ke, vol);
+}
+
+int or_face_pressure(int nn, const double* xyz, int face, double p, double* fe) {
+  if (nn == 8) return hex8_face_pressure(xyz, face, p, fe);
+  if (nn == 20) return hex20_face_pressure(xyz, face, p, fe);
+  return ERR_INVALID_ARG;
+}
+
+// Consistent nodal forces of a list of face pressures, scattered into f_full
+// in list order (analysis.rs:723-755 -> apply_pressure 1365-1396 -> scatter_fe
+// 1546-1553).  Returns the index of the first failing load in *bad.
+int or_face_loads(int64_t n_nodes, const double* coords, int nn, const int32_t* conn, int64_t n_loads,
+                  const int64_t* elem, const int32_t* face, const double* p, double* f_full, int64_t* bad) {
+  double xyz[60], fe[60];
+  for (int64_t k = 0; k < n_loads; ++k) {
+    const int32_t* c = conn + elem[k] * nn;
+    for (int a = 0; a < nn; ++a)
+      for (int q = 0; q < 3; ++q) xyz[3 * a + q] = coords[3 * (int64_t)c[a] + q];
+    int st = or_face_pressure(nn, xyz, face[k], p[k], fe);
+    if (st) {
+      *bad = k;
+      return st;
+    }
+    for (int a = 0; a < nn; ++a)
+      for (int d = 0; d < 3; ++d) f_full[3 * (int64_t)c[a] + d] += fe[3 * a + d];
+  }
+  (void)n_nodes;
+  return OK;
+}
+
+// Sparse-matrix handle held by the Python wrapper.
+struct OrCsr {
+  Csr csr;
+};
+
+// solve_linear (analysis.rs:548-1035) for a pure C3D8 / C3D20 isotropic model
+// with single-point constraints, restricted to the linear *STATIC step:
+//   prescribed = BCs in input order, last wins            (analysis.rs:556-565)
+//   isolated nodes pinned                                  (analysis.rs:2283-2330)
+//   element loop -> element_ke -> push nonzero triplets    (analysis.rs:574-668)
+//   AUTOSPC null-diagonal pin                              (analysis.rs:2164-2228)
+//   DofMap::build / reduce                                 (constraint.rs:26-172)
+//   solve_kff: csr_from_triplets, then dense Cholesky (solver=1) or PCG
+//   (solver=2) with tol, max_iter max(4n,200) when max_iter <= 0 (linalg.rs:311-404)
+//   reconstruct                                            (constraint.rs:207-217)
+// The reactions K u - f over the raw triplets (analysis.rs:1027-1035) go to rf_full.
+// info[0..12] = n_free, nnz(K_ff CSR), iters, residual, t_assembly, t_reduce,
+//               t_csr, t_solve, t_total, n_triplets, bnorm, first bad element
+int or_solve_static(int64_t n_nodes, const double* coords, int nn, int reduced, int64_t n_elem,
+                    const int32_t* conn, const double* e_elem, double nu, int64_t n_bc,
+                    const int64_t* bc_dof, const double* bc_val, const double* f_in, int solver,
+                    double tol, int64_t max_iter, int nthreads, int autospc, double* u_full,
+                    double* rf_full, double* info, OrCsr** csr_out, double* rhs_out) {
+  const double t0 = now_s();
+  const int64_t ndof = 3 * n_nodes;
+  for (int i = 0; i < 12; ++i) info[i] = 0.0;
+  info[11] = -1;
+  if (ndof == 0) return ERR_INVALID_ARG;
+  // prescribed map: last BC wins; keep insertion semantics of a HashMap
+  std::vector<char> is_presc(ndof, 0);
+  std::vector<double> presc_val(ndof, 0.0);
+  for (int64_t k = 0; k < n_bc; ++k) {
+    int64_t d = bc_dof[k];
+    if (d < 0 || d >= ndof) return ERR_INVALID_ARG;
+    is_presc[d] = 1;
+    presc_val[d] = bc_val[k];
+  }
+  if (autospc) {  // isolated nodes: all dofs pinned (or_insert: keeps an existing BC)
+    std::vector<char> attached(n_nodes, 0);
+    for (int64_t e = 0; e < n_elem; ++e)
+      for (int a = 0; a < nn; ++a) attached[conn[e * nn + a]] = 1;
+    for (int64_t ni = 0; ni < n_nodes; ++ni)
+      if (!attached[ni])
+        for (int d = 0; d < 3; ++d)
+          if (!is_presc[3 * ni + d]) {
+            is_presc[3 * ni + d] = 1;
+            presc_val[3 * ni + d] = 0.0;
+          }
+  }
+  // element loop
+  std::vector<Trip> trips;
+  trips.reserve((size_t)n_elem * (size_t)(9 * nn * nn));
+  const int m = 3 * nn;
+  std::vector<double> ke((size_t)m * m);
+  double xyz[60], vol;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    const int32_t* c = conn + e * nn;
+    for (int a = 0; a < nn; ++a)
+      for (int q = 0; q < 3; ++q) xyz[3 * a + q] = coords[3 * (int64_t)c[a] + q];
+    int st = element_ke(nn, xyz, e_elem[e], nu, reduced, ke.data(), &vol);
+    if (st) {
+      info[11] = (double)e;
+      return st;
+    }
+    for (int i = 0; i < m; ++i) {
+      uint64_t gi = 3 * (uint64_t)c[i / 3] + (uint64_t)(i % 3);
+      for (int j = 0; j < m; ++j) {
+        double v = ke[(size_t)i * m + j];
+        if (std::fabs(v) > 0.0) trips.push_back({gi, 3 * (uint64_t)c[j / 3] + (uint64_t)(j % 3), v});
+      }
+    }
+  }
+  const double t1 = now_s();
+  std::vector<double> f_full(f_in, f_in + ndof);
+  if (autospc) {  // analysis.rs:2208-2227
+    std::vector<double> dg(ndof, 0.0);
+    for (const Trip& t : trips)
+      if (t.i == t.j) dg[t.i] += t.v;
+    double max_d = 0.0;
+    for (double v : dg) max_d = std::max(max_d, std::fabs(v));
+    if (max_d >= 1e-30) {
+      double tl = max_d * 1e-14;
+      for (int64_t i = 0; i < ndof; ++i)
+        if (!is_presc[i] && std::fabs(dg[i]) <= tl) {
+          is_presc[i] = 1;
+          presc_val[i] = 0.0;
+        }
+    }
+  }
+  // DofMap::build, prescribed subset (constraint.rs:26-136)
+  std::vector<int64_t> ind_of(ndof, -1);
+  int64_t n_ind = 0;
+  for (int64_t d = 0; d < ndof; ++d)
+    if (!is_presc[d]) ind_of[d] = n_ind++;
+  bool any_presc = false;
+  for (int64_t d = 0; d < ndof; ++d) any_presc |= is_presc[d] != 0;
+  if (n_ind == 0 && !any_presc) return ERR_NO_FREE_DOF;
+  std::vector<double> u0(ndof, 0.0);
+  for (int64_t d = 0; d < ndof; ++d)
+    if (is_presc[d]) u0[d] = presc_val[d];
+  // DofMap::reduce (constraint.rs:138-172): t_row[d] = [(ind_of[d], 1.0)] for free d.
+  std::vector<double> rhs(n_ind, 0.0);
+  for (int64_t i = 0; i < ndof; ++i) {
+    double fi = f_full[i];
+    if (std::fabs(fi) == 0.0) continue;
+    if (ind_of[i] >= 0) rhs[ind_of[i]] += 1.0 * fi;
+  }
+  std::vector<Trip> ff;
+  ff.reserve(trips.size());
+  for (const Trip& t : trips) {
+    if (t.i >= (uint64_t)ndof || t.j >= (uint64_t)ndof || std::fabs(t.v) == 0.0) continue;
+    double u0j = u0[t.j];
+    int64_t a = ind_of[t.i];
+    if (a < 0) continue;
+    if (std::fabs(u0j) > 0.0) rhs[a] -= t.v * 1.0 * u0j;
+    int64_t b = ind_of[t.j];
+    if (b >= 0) ff.push_back({(uint64_t)a, (uint64_t)b, t.v * 1.0 * 1.0});
+  }
+  const double t2 = now_s();
+  info[0] = (double)n_ind;
+  info[9] = (double)ff.size();
+  std::vector<double> u(ndof);
+  if (n_ind == 0) {
+    u = u0;
+  } else {
+    Csr csr;
+    csr_from_triplets((size_t)n_ind, ff, csr);
+    std::vector<Trip>().swap(ff);
+    const double t3 = now_s();
+    info[1] = (double)csr.data.size();
+    std::vector<double> x(n_ind, 0.0);
+    double bn = 0.0;
+    for (double v : rhs) bn += v * v;
+    info[10] = std::sqrt(bn);
+    int st = OK;
+    if (solver == 1) {
+      if ((double)n_ind * (double)n_ind > 4.0e8) return ERR_INVALID_ARG;
+      std::vector<double> dense((size_t)n_ind * n_ind, 0.0);
+      for (int64_t i = 0; i < n_ind; ++i)
+        for (uint64_t k = csr.indptr[i]; k < csr.indptr[i + 1]; ++k)
+          dense[(size_t)i * n_ind + csr.indices[k]] = csr.data[k];
+      st = chol_solve(dense.data(), (size_t)n_ind, rhs.data(), x.data());
+      info[2] = 1;
+      info[3] = st == OK ? residual_of(csr, x.data(), rhs.data()) : 0.0;
+    } else {
+      size_t mi = max_iter > 0 ? (size_t)max_iter : std::max<size_t>(4 * (size_t)n_ind, 200);
+      size_t iters = 0;
+      double res = 0.0;
+      st = pcg(csr, rhs.data(), tol, mi, nthreads, x.data(), &iters, &res);
+      info[2] = (double)iters;
+      info[3] = res;
+    }
+    const double t4 = now_s();
+    info[6] = t3 - t2;
+    info[7] = t4 - t3;
+    if (st) return st;
+    for (int64_t d = 0; d < ndof; ++d) u[d] = u0[d] + (ind_of[d] >= 0 ? 1.0 * x[ind_of[d]] : 0.0);
+    if (csr_out) {
+      OrCsr* h = new OrCsr;
+      h->csr = std::move(csr);
+      *csr_out = h;
+    }
+    if (rhs_out) std::copy(rhs.begin(), rhs.end(), rhs_out);
+  }
+  for (int64_t d = 0; d < ndof; ++d) u_full[d] = u[d];
+  if (rf_full) {  // analysis.rs:1027-1035
+    std::vector<double> ku(ndof, 0.0);
+    for (const Trip& t : trips) ku[t.i] += t.v * u[t.j];
+    for (int64_t d = 0; d < ndof; ++d) rf_full[d] = ku[d] - f_full[d];
+  }
+  info[4] = t1 - t0;
+  info[5] = t2 - t1;
+  info[8] = now_s() - t0;
+  return OK;
+}
+
+int64_t or_csr_n(const OrCsr* h) { return (int64_t)h->csr.n; }
+int64_t or_csr_nnz(const OrCsr* h) { return (int64_t)h->csr.data.size(); }
+void or_csr_export(const OrCsr* h, int64_t* indptr, int64_t* indices, double* data) {
+  for (size_t i = 0; i <= h->csr.n; ++i) indptr[i] = (int64_t)h->csr.indptr[i];
+  for (size_t k = 0; k < h->csr.data.size(); ++k) {
+    indices[k] = (int64_t)h->csr.indices[k];
+    data[k] = h->csr.data[k];
+  }
+}
+void or_csr_free(OrCsr* h) { delete h; }
+
+// solve_kff's CSR + backend part (linalg.rs:311-404) on caller triplets:
+// csr_from_triplets, then dense Cholesky (solver=1) or PCG (solver=2).
+// info = {iters, residual}.
+int or_solve_kff(int64_t n, int64_t nt, const int64_t* ti, const int64_t* tj, const double* tv,
+                 const double* rhs, int solver, double tol, int64_t max_iter, int nthreads, double* x,
+                 double* info) {
+  std::vector<Trip> trips(nt);
+  for (int64_t k = 0; k < nt; ++k) trips[k] = {(uint64_t)ti[k], (uint64_t)tj[k], tv[k]};
+  Csr csr;
+  csr_from_triplets((size_t)n, trips, csr);
+  if (solver == 1) {
+    std::vector<double> dense((size_t)n * n, 0.0);
+    for (int64_t i = 0; i < n; ++i)
+      for (uint64_t k = csr.indptr[i]; k < csr.indptr[i + 1]; ++k)
+        dense[(size_t)i * n + csr.indices[k]] = csr.data[k];
+    int st = chol_solve(dense.data(), (size_t)n, rhs, x);
+    info[0] = 1;
+    info[1] = st == OK ? residual_of(csr, x, rhs) : 0.0;
+    return st;
+  }
+  size_t mi = max_iter > 0 ? (size_t)max_iter : std::max<size_t>(4 * (size_t)n, 200);
+  size_t iters = 0;
+  double res = 0.0;
+  int st = pcg(csr, rhs, tol, mi, nthreads, x, &iters, &res);
+  info[0] = (double)iters;
+  info[1] = res;
+  return st;
+}
+
+// ||K x - b|| <= 1e-8 max(||b||, 1) + 1e-10 (sparse_native.rs:1572-1578)
+int or_residual_ok(double residual, double bnorm) {
+  return std::isfinite(residual) && residual <= 1e-8 * std::max(bnorm, 1.0) + 1e-10;
+}
+
+// Compliance gradient, no reference counterpart: for every element,
+// g_e = -p rho_e^(p-1) E0 u_e^T K_e(E=1, nu) u_e with K_e from the restated
+// hex8 / hex20 stiffness.  Returns the first failing element in *bad.
+int or_compliance_grad(int64_t n_nodes, const double* coords, int nn, int reduced, int64_t n_elem,
+                       const int32_t* conn, const double* rho, double pexp, double e0, double nu,
+                       const double* u_full, double* grad, int64_t* bad) {
+  const int m = 3 * nn;
+  std::vector<double> ke((size_t)m * m);
+  double xyz[60], ue[60], vol;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    const int32_t* c = conn + e * nn;
+    for (int a = 0; a < nn; ++a)
+      for (int q = 0; q < 3; ++q) {
+        xyz[3 * a + q] = coords[3 * (int64_t)c[a] + q];
+        ue[3 * a + q] = u_full[3 * (int64_t)c[a] + q];
+      }
+    int st = element_ke(nn, xyz, 1.0, nu, reduced, ke.data(), &vol);
+    if (st) {
+      *bad = e;
+      return st;
+    }
+    double s = 0.0;
+    for (int i = 0; i < m; ++i) {
+      double row = 0.0;
+      for (int j = 0; j < m; ++j) row += ke[(size_t)i * m + j] * ue[j];
+      s += ue[i] * row;
+    }
+    grad[e] = -pexp * std::pow(rho[e], pexp - 1.0) * e0 * s;
+  }
+  (void)n_nodes;
+  return OK;
+}
+
+}  // extern "C"

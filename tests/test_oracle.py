@@ -1,0 +1,130 @@
+"""The CPU oracle against the reference's own known answers (CPU only)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from axia_gpu import meshgen
+from oracle import oracle as O
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
+PINS = GOLD["pins"]
+VEC = GOLD["vectors"]
+
+
+def _mean_ux(u, nodes_1based):
+    return float(np.mean([u[3 * (n - 1)] for n in nodes_1based]))
+
+
+@pytest.mark.parametrize("solver", [O.SOLVER_CHOLESKY, O.SOLVER_PCG])
+def test_patch_c3d8(solver):
+    pin = PINS["patch_c3d8_mean_ux"]
+    r = O.solve_static(meshgen.patch_c3d8(), solver=solver)
+    assert abs(_mean_ux(r.u, pin["nodes_1based"]) - pin["value"]) < pin["tol"]
+
+
+def test_patch_c3d20():
+    pin = PINS["patch_c3d20_mean_ux"]
+    r = O.solve_static(meshgen.patch_c3d20(), solver=O.SOLVER_CHOLESKY)
+    assert abs(_mean_ux(r.u, pin["nodes_1based"]) - pin["value"]) < pin["tol"]
+
+
+def test_partition_of_unity():
+    n, _ = O.hex20_shape(0.0, 0.0, 0.0)
+    assert abs(n.sum() - 1.0) < PINS["hex20_partition_of_unity"]["tol"]
+    n, _ = O.quad8_shape(0.0, 0.0)
+    assert abs(n.sum() - 1.0) < PINS["quad8_partition_of_unity"]["tol"]
+    rng = np.random.default_rng(1)
+    for xi, eta, zeta in rng.uniform(-1, 1, (10, 3)):
+        n8, dn8 = O.hex8_shape(xi, eta, zeta)
+        n20, dn20 = O.hex20_shape(xi, eta, zeta)
+        assert abs(n8.sum() - 1) < 1e-14 and abs(n20.sum() - 1) < 1e-14
+        assert np.abs(dn8.sum(0)).max() < 1e-14 and np.abs(dn20.sum(0)).max() < 1e-13
+
+
+def test_element_ke_properties():
+    for key, nn in (("hex8_distorted", 8), ("hex20_distorted", 20)):
+        g = VEC[key]
+        xyz = np.array(g["xyz"])
+        ke, vol = O.element_ke(xyz, g["e"], g["nu"])
+        # matches the committed regression vector
+        assert np.allclose(ke.ravel(), g["ke"], rtol=0, atol=1e-9 * np.abs(ke).max())
+        assert abs(vol - g["vol"]) < 1e-12
+        # symmetric, rigid-body modes in the null space
+        assert np.abs(ke - ke.T).max() < 1e-9 * np.abs(ke).max()
+        for d in range(3):
+            t = np.zeros(3 * nn)
+            t[d::3] = 1.0
+            assert np.abs(ke @ t).max() < 1e-8 * np.abs(ke).max()
+        rot = np.zeros(3 * nn)
+        rot[0::3], rot[1::3] = -xyz[:, 1], xyz[:, 0]
+        assert np.abs(ke @ rot).max() < 1e-8 * np.abs(ke).max() * np.abs(xyz).max()
+
+
+def test_element_errors():
+    xyz = np.array(VEC["hex8_distorted"]["xyz"])
+    inverted = xyz[[4, 5, 6, 7, 0, 1, 2, 3]]
+    with pytest.raises(O.OracleError) as e:
+        O.element_ke(inverted, 1.0, 0.3)
+    assert e.value.code == 3  # negative Jacobian, elem.rs:208-210
+    with pytest.raises(O.OracleError) as e:
+        O.element_ke(xyz, 1.0, 0.5)
+    assert e.value.code == 4  # nu >= 0.5, elem.rs:42-44
+    flat = xyz.copy()
+    flat[:, 2] = 0.0
+    with pytest.raises(O.OracleError) as e:
+        O.element_ke(flat, 1.0, 0.3)
+    assert e.value.code == 2  # singular Jacobian, elem.rs:14-16
+
+
+def test_face_pressure_resultant():
+    # a uniform pressure on a planar face: resultant = p * area along the inward normal
+    xyz = np.array(VEC["hex8_distorted"]["xyz"])
+    fe = np.array(VEC["hex8_face_p4"]["fe"])
+    assert np.allclose(O.face_pressure(xyz, 4, 1.0), fe, atol=1e-14)
+    cube = (meshgen.HEX20_XI.astype(float) + 1) / 2
+    for face, axis, sign in ((2, 2, -1), (4, 0, -1), (1, 2, 1), (6, 0, 1)):
+        f = O.face_pressure(cube, face, 3.0).reshape(20, 3)
+        assert abs(f[:, axis].sum() - sign * 3.0) < 1e-12
+        f8 = O.face_pressure(cube[:8], face, 3.0).reshape(8, 3)
+        assert abs(f8[:, axis].sum() - sign * 3.0) < 1e-12
+
+
+def test_cantilever_pcg_vs_cholesky_vs_superlu():
+    m = meshgen.cantilever_c3d8()
+    g = VEC["cantilever_20x4x4"]
+    ch = O.solve_static(m, solver=O.SOLVER_CHOLESKY, keep_csr=True)
+    assert ch.n_free == g["n_free"] == 1500
+    assert ch.nnz == g["nnz_kff"] == 88218
+    assert np.abs(ch.u - np.array(g["u"])).max() < 1e-12 * np.abs(ch.u).max()
+    pc = O.solve_static(m, solver=O.SOLVER_PCG, tol=1e-12)
+    assert np.linalg.norm(pc.u - ch.u) / np.linalg.norm(ch.u) < 1e-9
+    x = O.direct_solve(ch.indptr, ch.indices, ch.data, ch.rhs)
+    free = m.free_mask()
+    assert np.linalg.norm(x - ch.u[free]) / np.linalg.norm(x) < 1e-12
+    assert O.residual_ok(ch.residual, ch.bnorm)
+
+
+def test_pcg_failure_modes():
+    m = meshgen.cantilever_c3d8(nx=6, ny=2, nz=2)
+    with pytest.raises(O.OracleError) as e:
+        O.solve_static(m, solver=O.SOLVER_PCG, tol=1e-12, max_iter=3)
+    assert e.value.code == 5  # linalg.rs:253-257
+    # zero load: x = 0 with zero iterations (linalg.rs:208-216)
+    m.cload[:] = 0
+    r = O.solve_static(m, solver=O.SOLVER_PCG)
+    assert r.iters == 0 and np.all(r.u == 0)
+
+
+def test_prescribed_nonzero_and_last_bc_wins():
+    m = meshgen.cantilever_c3d8(nx=4, ny=2, nz=2)
+    tip = np.nonzero(np.isclose(m.coords[:, 0], 4.0))[0]
+    # a prescribed tip displacement; the first entry is overridden by the second
+    m.bc_dof = np.concatenate([m.bc_dof, 3 * tip, 3 * tip])
+    m.bc_val = np.concatenate([m.bc_val, np.full(tip.shape[0], 5.0), np.full(tip.shape[0], 0.01)])
+    m.cload[:] = 0
+    r = O.solve_static(m, solver=O.SOLVER_CHOLESKY, reactions=True)
+    assert np.allclose(r.u[3 * tip], 0.01)
+    # reactions at the clamp balance the reactions at the driven face
+    assert abs(r.rf[0::3].sum()) < 1e-8 * np.abs(r.rf).max()
