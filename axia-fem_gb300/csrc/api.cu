@@ -15,6 +15,7 @@ int ensure_pcg_state(axia_ctx* ctx);
 int build_rhs(axia_ctx* ctx, const double* d_f);
 int reconstruct(axia_ctx* ctx, double* d_u);
 int true_residual(axia_ctx* ctx, double* out);
+int prepare_solve(axia_ctx* ctx, bool mixed);
 int spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req);
 
 namespace {
@@ -290,7 +291,8 @@ static int32_t solve_common(axia_ctx* ctx, const double* d_f, double* d_u, const
   EventTimer t(ctx->stream);
   int st = AXIA_OK;
   if (ctx->n_free > 0) {
-    st = build_rhs(ctx, d_f);
+    st = prepare_solve(ctx, o.precision == AXIA_PREC_MIXED);
+    if (st == AXIA_OK) st = build_rhs(ctx, d_f);
     if (st == AXIA_OK) st = pcg_solve(ctx, &o, info);
     if (st == AXIA_OK) st = reconstruct(ctx, d_u);
   } else {

@@ -491,7 +491,11 @@ int true_residual(axia_ctx* ctx, double* out) {
   return AXIA_OK;
 }
 
+int prepare_solve(axia_ctx* ctx, bool mixed) { return ensure_solver_buffers(ctx, mixed); }
+
 int build_rhs(axia_ctx* ctx, const double* d_f) {
+  if (!ctx->d_b || !ctx->d_kfu0 || !ctx->d_ind_of || !d_f)
+    return set_error(ctx, AXIA_ERR_STATE, "right-hand side buffers not allocated");
   k_build_rhs<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(ctx->ndof, ctx->d_ind_of, d_f, ctx->d_kfu0, ctx->d_b);
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());
@@ -499,6 +503,7 @@ int build_rhs(axia_ctx* ctx, const double* d_f) {
 }
 
 int reconstruct(axia_ctx* ctx, double* d_u) {
+  if (!ctx->d_x || !ctx->d_u0 || !d_u) return set_error(ctx, AXIA_ERR_STATE, "solution buffers not allocated");
   k_reconstruct<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(ctx->ndof, ctx->d_ind_of, ctx->d_u0, ctx->d_x, d_u);
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());
