@@ -39,6 +39,12 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 REFINE_RESTART = 0
 REFINE_RELIABLE = 1
+ASM_CSR64 = 1
+ASM_CSR32 = 2
+ASM_BSR64 = 4
+ASM_BSR32 = 8
+FORMAT_CSR = 0
+FORMAT_BSR3 = 1
 
 
 class Mesh(C.Structure):
@@ -50,7 +56,7 @@ class Mesh(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iter", C.c_int64), ("precision", C.c_int32),
                 ("refine_mode", C.c_int32), ("inner_rtol", C.c_double), ("max_outer", C.c_int32),
-                ("spmv_lanes", C.c_int32)]
+                ("spmv_lanes", C.c_int32), ("matrix_format", C.c_int32), ("reserved", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -75,11 +81,18 @@ SIGNATURES = [
     ("axia_face_loads", C.c_int32, [C.c_int32, C.c_int64, _P, _P, C.c_int64, _P, _P, _P, _P, C.POINTER(C.c_int64)]),
     ("axia_gpu_setup", C.c_int32, [_P, C.POINTER(Mesh), C.c_int64, _P, _P]),
     ("axia_gpu_assemble", C.c_int32, [_P, C.c_int32]),
+    ("axia_gpu_assemble_ex", C.c_int32, [_P, C.c_int32]),
     ("axia_gpu_solve", C.c_int32, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
     ("axia_gpu_solve_device", C.c_int32, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
     ("axia_gpu_set_stream", C.c_int32, [_P, _P]),
     ("axia_gpu_kernel_launches", C.c_int64, [_P]),
     ("axia_gpu_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32]),
+    ("axia_gpu_bsr_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32]),
+    ("axia_gpu_node_blocks", C.c_int64, [_P]),
+    ("axia_gpu_element_energy", C.c_int32, [_P, _P, _P, _P]),
+    ("axia_gpu_compliance_forward", C.c_int32, [_P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_double),
+                                                C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
+    ("axia_gpu_compliance_backward", C.c_int32, [_P, _P]),
     ("axia_gpu_system_size", C.c_int32, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("axia_gpu_export_system", C.c_int32, [_P, _P, _P, _P, _P, _P]),
     ("axia_gpu_export_dofmap", C.c_int32, [_P, _P]),

@@ -85,6 +85,11 @@ class GpuContext:
         self._check(self.lib.axia_gpu_assemble(self.h, int(precision)), "assemble")
         return self
 
+    def assemble_ex(self, flags):
+        """Build the matrix forms named by ASM_* flags (CSR / node-block, FP64 / FP32)."""
+        self._check(self.lib.axia_gpu_assemble_ex(self.h, int(flags)), "assemble_ex")
+        return self
+
     def load_vector(self, model=None):
         """CLOAD vector plus the DLOAD face pressures (host, library routine)."""
         model = model or self.model
@@ -101,12 +106,17 @@ class GpuContext:
 
     @staticmethod
     def opts(rtol=1e-8, max_iter=0, precision=L.PREC_FP64, refine_mode=L.REFINE_RESTART, inner_rtol=1e-3,
-             max_outer=50, spmv_lanes=0):
-        return L.SolveOpts(rtol, max_iter, precision, refine_mode, inner_rtol, max_outer, spmv_lanes)
+             max_outer=50, spmv_lanes=0, matrix_format=L.FORMAT_CSR):
+        return L.SolveOpts(rtol, max_iter, precision, refine_mode, inner_rtol, max_outer, spmv_lanes,
+                           matrix_format, 0)
 
     def set_stream(self, stream_handle: int | None):
         """Issue the context's work on a caller's cudaStream_t (None: own stream)."""
         self._check(self.lib.axia_gpu_set_stream(self.h, C.c_void_p(stream_handle or 0)), "set_stream")
+
+    def n_blocks(self) -> int:
+        """3x3 node blocks of the node-block form."""
+        return int(self.lib.axia_gpu_node_blocks(self.h))
 
     def kernel_launches(self) -> int:
         return int(self.lib.axia_gpu_kernel_launches(self.h))
@@ -114,6 +124,10 @@ class GpuContext:
     def spmv_device(self, precision, x_dev_ptr, y_dev_ptr, lanes=0):
         self._check(self.lib.axia_gpu_spmv_device(self.h, int(precision), C.c_void_p(x_dev_ptr),
                                                   C.c_void_p(y_dev_ptr), int(lanes)), "spmv")
+
+    def bsr_spmv_device(self, precision, x_dev_ptr, y_dev_ptr, lanes=0):
+        self._check(self.lib.axia_gpu_bsr_spmv_device(self.h, int(precision), C.c_void_p(x_dev_ptr),
+                                                      C.c_void_p(y_dev_ptr), int(lanes)), "bsr_spmv")
 
     def solve(self, f_full, **kw):
         f = _c(f_full, np.float64)
@@ -129,6 +143,32 @@ class GpuContext:
         self._check(self.lib.axia_gpu_solve_device(self.h, C.c_void_p(f_dev_ptr), C.c_void_p(u_dev_ptr), C.byref(o),
                                                    C.byref(info)), "solve_device")
         return info
+
+    def element_energy(self, u_full, v_full=None):
+        """s_e = u_e^T K_e(E=1) v_e for every element (v defaults to u)."""
+        u = _c(u_full, np.float64)
+        v = u if v_full is None else _c(v_full, np.float64)
+        s = np.zeros(self.model.n_elem)
+        self._check(self.lib.axia_gpu_element_energy(self.h, L.ptr(u), L.ptr(v), L.ptr(s)), "element_energy")
+        return s
+
+    def compliance_forward(self, rho, penal, e0, f_full, **kw):
+        """SIMP forward: E = e0 rho^penal, solve, return (u, C, info)."""
+        r = _c(rho, np.float64)
+        f = _c(f_full, np.float64)
+        u = np.zeros_like(f)
+        c = C.c_double(0.0)
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        self._check(self.lib.axia_gpu_compliance_forward(self.h, L.ptr(r), float(penal), float(e0), L.ptr(f), L.ptr(u),
+                                                         C.byref(c), C.byref(o), C.byref(info)), "compliance_forward")
+        return u, c.value, info
+
+    def compliance_backward(self):
+        """dC/drho_e for every element from the last forward call."""
+        g = np.zeros(self.model.n_elem)
+        self._check(self.lib.axia_gpu_compliance_backward(self.h, L.ptr(g)), "compliance_backward")
+        return g
 
     def export_system(self):
         """K_ff as (rowptr, col, val), the Jacobi diagonal and K_fp u0."""

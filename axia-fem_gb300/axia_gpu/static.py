@@ -31,9 +31,13 @@ class StaticResult:
 
 
 def solve_linear(model, backend: SparseBackend | None = None, rtol: float = 1e-8, max_iter: int = 0,
-                 ctx: GpuContext | None = None, inner_rtol: float = 1e-3,
-                 refine_mode: int = L.REFINE_RESTART) -> StaticResult:
-    """Solve the linear-static model on the GPU backend (Gpu or GpuMixed)."""
+                 ctx: GpuContext | None = None, inner_rtol: float | None = None,
+                 refine_mode: int = L.REFINE_RELIABLE, matrix_format: int | None = None) -> StaticResult:
+    """Solve the linear-static model on the GPU backend.
+
+    Gpu: FP64 Jacobi-PCG on K_ff in CSR (the reference's method).
+    GpuMixed: FP32 inner CG with FP64 refinement (reliable updates by default)
+    on the node-block form unless matrix_format says CSR."""
     apply_env_solver()
     b = backend if backend is not None else sparse_backend()
     if b == SparseBackend.Auto:
@@ -44,12 +48,20 @@ def solve_linear(model, backend: SparseBackend | None = None, rtol: float = 1e-8
     own = ctx is None
     ctx = ctx or GpuContext(0)
     try:
+        if matrix_format is None:
+            matrix_format = L.FORMAT_BSR3 if mixed else L.FORMAT_CSR
+        if inner_rtol is None:
+            inner_rtol = 0.1 if refine_mode == L.REFINE_RELIABLE else 1e-3
         ctx.setup(model)
-        ctx.assemble(L.PREC_MIXED if mixed else L.PREC_FP64)
+        if matrix_format == L.FORMAT_BSR3:
+            ctx.assemble_ex(L.ASM_BSR64 | (L.ASM_BSR32 if mixed else 0))
+        else:
+            ctx.assemble(L.PREC_MIXED if mixed else L.PREC_FP64)
         f = ctx.load_vector(model)
         u, info = ctx.solve(f, rtol=rtol, max_iter=max_iter, precision=L.PREC_MIXED if mixed else L.PREC_FP64,
-                            inner_rtol=inner_rtol, refine_mode=refine_mode)
-        name = "GPU PCG (FP32 inner, FP64 refinement)" if mixed else "GPU PCG (FP64)"
+                            inner_rtol=inner_rtol, refine_mode=refine_mode, matrix_format=matrix_format)
+        fmt = "node-block" if matrix_format == L.FORMAT_BSR3 else "CSR"
+        name = f"GPU PCG (FP32 inner, FP64 refinement, {fmt})" if mixed else f"GPU PCG (FP64, {fmt})"
         return StaticResult(u, name, int(info.iters), float(info.residual), info.as_dict())
     finally:
         if own:

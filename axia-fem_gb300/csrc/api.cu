@@ -7,7 +7,13 @@
 #include "element.cuh"
 
 int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0);
-int numeric_assemble(axia_ctx* ctx, bool want32);
+int numeric_assemble(axia_ctx* ctx, int flags);
+int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_opts* opts, axia_solve_info* info);
+int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req);
+int element_energy(axia_ctx* ctx, const double* d_u, const double* d_v, double* d_s);
+int simp_modulus(axia_ctx* ctx, const double* d_rho, double pexp, double e0);
+int simp_gradient(axia_ctx* ctx, const double* d_rho, const double* d_s, double pexp, double e0, double* d_g);
+int device_dot(axia_ctx* ctx, const double* a, const double* b, int64_t n, double* out);
 int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args);
 struct PcgOut;
 int pcg_solve(axia_ctx* ctx, const axia_solve_opts* opts, axia_solve_info* info);
@@ -75,8 +81,27 @@ void free_mesh_state(axia_ctx* ctx) {
   dev_free(ctx->d_r32);
   dev_free(ctx->d_p32);
   dev_free(ctx->d_q32);
+  dev_free(ctx->d_adj_ptr32);
+  dev_free(ctx->d_bval64);
+  dev_free(ctx->d_bval32);
+  dev_free(ctx->d_bdinv64);
+  dev_free(ctx->d_bdinv32);
+  dev_free(ctx->d_bf);
+  dev_free(ctx->d_xf);
+  dev_free(ctx->d_rf);
+  dev_free(ctx->d_pf);
+  dev_free(ctx->d_qf);
+  dev_free(ctx->d_xf32);
+  dev_free(ctx->d_rf32);
+  dev_free(ctx->d_pf32);
+  dev_free(ctx->d_qf32);
+  ctx->full_capacity = 0;
+  dev_free(ctx->d_rho);
+  dev_free(ctx->d_energy);
+  dev_free(ctx->d_grad);
+  ctx->have_forward = false;
   ctx->vec_capacity = 0;
-  ctx->assembled = ctx->have32 = false;
+  ctx->assembled = ctx->have32 = ctx->have_csr64 = ctx->have_bsr64 = ctx->have_bsr32 = false;
   ctx->n_free = ctx->nnz = 0;
 }
 
@@ -136,6 +161,7 @@ void axia_gpu_destroy(axia_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_mesh_state(ctx);
   dev_free(ctx->d_partials);
+  dev_free(ctx->d_totals);
   dev_free(ctx->d_bar);
   dev_free(ctx->d_status);
   if (ctx->d_out) cudaFree(ctx->d_out);
@@ -264,14 +290,19 @@ int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const
   return AXIA_OK;
 }
 
-int32_t axia_gpu_assemble(axia_ctx* ctx, int32_t precision) {
+int32_t axia_gpu_assemble_ex(axia_ctx* ctx, int32_t flags) {
   if (!ctx) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   if (!ctx->d_rowptr) return set_error(ctx, AXIA_ERR_STATE, "assemble before setup");
+  if (flags <= 0 || flags > 15) return set_error(ctx, AXIA_ERR_INVALID_ARG, "assemble: unknown matrix forms");
   EventTimer t(ctx->stream);
-  int st = numeric_assemble(ctx, precision == AXIA_PREC_MIXED);
+  int st = numeric_assemble(ctx, flags);
   ctx->ms_assemble = t.stop_ms();
   return st;
+}
+
+int32_t axia_gpu_assemble(axia_ctx* ctx, int32_t precision) {
+  return axia_gpu_assemble_ex(ctx, precision == AXIA_PREC_MIXED ? (AXIA_ASM_CSR64 | AXIA_ASM_CSR32) : AXIA_ASM_CSR64);
 }
 
 static int32_t solve_common(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_opts* opts,
@@ -290,7 +321,15 @@ static int32_t solve_common(axia_ctx* ctx, const double* d_f, double* d_u, const
   if (!(o.rtol > 0.0)) o.rtol = 1e-8;
   EventTimer t(ctx->stream);
   int st = AXIA_OK;
-  if (ctx->n_free > 0) {
+  if (ctx->n_free > 0 && o.matrix_format == AXIA_FORMAT_BSR3) {
+    st = bsr_solve(ctx, d_f, d_u, &o, info);
+    info->ms_solve = t.stop_ms();
+    fill_info_sizes(ctx, info);
+    info->status = st;
+    return st;
+  }
+  if (ctx->n_free > 0 && !ctx->have_csr64) st = set_error(ctx, AXIA_ERR_STATE, "CSR solve needs AXIA_ASM_CSR64");
+  if (ctx->n_free > 0 && st == AXIA_OK) {
     st = prepare_solve(ctx, o.precision == AXIA_PREC_MIXED);
     if (st == AXIA_OK) st = build_rhs(ctx, d_f);
     if (st == AXIA_OK) st = pcg_solve(ctx, &o, info);
@@ -346,7 +385,79 @@ int32_t axia_gpu_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev
   if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "spmv before assemble");
   const bool fp32 = precision == AXIA_PREC_MIXED;
   if (fp32 && !ctx->have32) return set_error(ctx, AXIA_ERR_STATE, "FP32 spmv needs axia_gpu_assemble(AXIA_PREC_MIXED)");
+  if (!fp32 && !ctx->have_csr64) return set_error(ctx, AXIA_ERR_STATE, "FP64 spmv needs AXIA_ASM_CSR64");
   return spmv_device(ctx, fp32, x_dev, y_dev, lanes);
+}
+
+int32_t axia_gpu_bsr_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev, int32_t lanes) {
+  if (!ctx || !x_dev || !y_dev) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "spmv before assemble");
+  return bsr_spmv_device(ctx, precision == AXIA_PREC_MIXED, x_dev, y_dev, lanes);
+}
+
+int64_t axia_gpu_node_blocks(const axia_ctx* ctx) { return ctx ? ctx->n_adj : -1; }
+
+int32_t axia_gpu_element_energy(axia_ctx* ctx, const double* u_full, const double* v_full, double* s) {
+  if (!ctx || !u_full || !v_full || !s) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->d_conn) return set_error(ctx, AXIA_ERR_STATE, "element energy before setup");
+  double *du = nullptr, *dv = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &du, (size_t)ctx->ndof));
+  int st = dev_alloc(ctx, &dv, (size_t)ctx->ndof);
+  if (st == AXIA_OK && !ctx->d_energy) st = dev_alloc(ctx, &ctx->d_energy, (size_t)std::max<int64_t>(ctx->n_elem, 1));
+  if (st == AXIA_OK) {
+    cudaMemcpyAsync(du, u_full, ctx->ndof * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(dv, v_full, ctx->ndof * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    st = element_energy(ctx, du, dv, ctx->d_energy);
+  }
+  if (st == AXIA_OK && cudaMemcpy(s, ctx->d_energy, ctx->n_elem * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    st = set_error(ctx, AXIA_ERR_CUDA, "copy of element energies");
+  dev_free(du);
+  dev_free(dv);
+  return st;
+}
+
+int32_t axia_gpu_compliance_forward(axia_ctx* ctx, const double* rho, double penal, double e0, const double* f_full,
+                                    double* u_full, double* compliance, const axia_solve_opts* opts,
+                                    axia_solve_info* info) {
+  if (!ctx || !rho || !f_full || !u_full || !compliance) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->d_rowptr) return set_error(ctx, AXIA_ERR_STATE, "compliance before setup");
+  if (!(e0 > 0.0) || !std::isfinite(penal)) return set_error(ctx, AXIA_ERR_MATERIAL, "SIMP needs E0 > 0 and a finite p");
+  ctx->have_forward = false;
+  if (!ctx->d_rho) AXIA_TRY(dev_alloc(ctx, &ctx->d_rho, (size_t)std::max<int64_t>(ctx->n_elem, 1)));
+  AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_rho, rho, ctx->n_elem * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  AXIA_TRY(simp_modulus(ctx, ctx->d_rho, penal, e0));
+  axia_solve_opts o{};
+  if (opts) {
+    o = *opts;
+  } else {
+    o.rtol = 1e-10;
+  }
+  const bool mixed = o.precision == AXIA_PREC_MIXED;
+  int flags = o.matrix_format == AXIA_FORMAT_BSR3 ? (AXIA_ASM_BSR64 | (mixed ? AXIA_ASM_BSR32 : 0))
+                                                  : (AXIA_ASM_CSR64 | (mixed ? AXIA_ASM_CSR32 : 0));
+  AXIA_TRY(axia_gpu_assemble_ex(ctx, flags));
+  AXIA_TRY(axia_gpu_solve(ctx, f_full, u_full, &o, info));
+  AXIA_TRY(device_dot(ctx, ctx->d_f, ctx->d_u, ctx->ndof, compliance));
+  ctx->simp_p = penal;
+  ctx->simp_e0 = e0;
+  ctx->have_forward = true;
+  return AXIA_OK;
+}
+
+int32_t axia_gpu_compliance_backward(axia_ctx* ctx, double* grad) {
+  if (!ctx || !grad) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->have_forward) return set_error(ctx, AXIA_ERR_STATE, "compliance backward before forward");
+  if (!ctx->d_energy) AXIA_TRY(dev_alloc(ctx, &ctx->d_energy, (size_t)std::max<int64_t>(ctx->n_elem, 1)));
+  if (!ctx->d_grad) AXIA_TRY(dev_alloc(ctx, &ctx->d_grad, (size_t)std::max<int64_t>(ctx->n_elem, 1)));
+  AXIA_TRY(element_energy(ctx, ctx->d_u, ctx->d_u, ctx->d_energy));
+  AXIA_TRY(simp_gradient(ctx, ctx->d_rho, ctx->d_energy, ctx->simp_p, ctx->simp_e0, ctx->d_grad));
+  AXIA_CUDA(ctx, cudaMemcpyAsync(grad, ctx->d_grad, ctx->n_elem * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXIA_OK;
 }
 
 int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz) {
@@ -366,6 +477,7 @@ int32_t axia_gpu_export_system(const axia_ctx* ctx_c, int32_t* rowptr, int32_t* 
   if (rowptr) AXIA_CUDA(ctx, cudaMemcpy(rowptr, ctx->d_rowptr, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost));
   if (col) AXIA_CUDA(ctx, cudaMemcpy(col, ctx->d_col, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
   if ((val || diag || kfu0) && !ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "export of values before assemble");
+  if (val && !ctx->have_csr64) return set_error(ctx, AXIA_ERR_STATE, "export of CSR values needs AXIA_ASM_CSR64");
   if (val) AXIA_CUDA(ctx, cudaMemcpy(val, ctx->d_val, nnz * sizeof(double), cudaMemcpyDeviceToHost));
   if (diag) AXIA_CUDA(ctx, cudaMemcpy(diag, ctx->d_diag, n * sizeof(double), cudaMemcpyDeviceToHost));
   if (kfu0) AXIA_CUDA(ctx, cudaMemcpy(kfu0, ctx->d_kfu0, n * sizeof(double), cudaMemcpyDeviceToHost));

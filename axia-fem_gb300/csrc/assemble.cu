@@ -181,6 +181,15 @@ int launch_element_ke(axia_ctx* ctx, const ElemArgs& args) {
 
 }  // namespace
 
+// dN/dxi and weights of the Gauss points of (nn, ng) in device memory
+int element_tables_for(axia_ctx* ctx, int nn, int ng, const double** dn, const double** w) {
+  ElemTables t;
+  AXIA_TRY(ensure_tables(ctx, nn, ng, &t));
+  *dn = t.dn;
+  *w = t.w;
+  return AXIA_OK;
+}
+
 // Runs the element kernel for nn / reduced on args (device pointers).
 int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args) {
   if (args.n_elem == 0) return AXIA_OK;
@@ -377,12 +386,17 @@ struct GatherArgs {
   int any_u0;
   int max_adj;
   int warp_stride;   // bytes of shared memory per warp
-  double* val;
-  float* val32;
+  double* val;        // CSR FP64 values (null: not assembled)
+  float* val32;       // CSR FP32 values (null: not assembled)
   double* diag;
   double* dinv;
   float* dinv32;
   double* kfu0;
+  double* bval64;     // node-block values [9][nb] (null: not assembled)
+  float* bval32;
+  double* bdinv64;    // full-DOF 1/diag, 1 on prescribed DOFs
+  float* bdinv32;
+  int64_t nb;
 };
 
 __global__ void k_gather(GatherArgs g) {
@@ -434,7 +448,7 @@ __global__ void k_gather(GatherArgs g) {
         const int c = g.ind_of[3 * (int64_t)b + j];
         if (c >= 0) {
           const int64_t pos = rs + g.adj_off[s0 + s] + (c - first_free(g.ind_of, b));
-          g.val[pos] = v;
+          if (g.val) g.val[pos] = v;
           if (g.val32) g.val32[pos] = (float)v;
           if (c == r) {
             g.diag[r] = v;
@@ -450,6 +464,25 @@ __global__ void k_gather(GatherArgs g) {
       if (g.any_u0) {
         kf = warp_sum(kf);
         if (lane == 0) g.kfu0[r] = kf;
+      }
+    }
+    if (g.bval64 || g.bval32) {
+      // node-block form: free-free entries of K, a unit diagonal on prescribed DOFs
+      for (int t = lane; t < 9 * nadj; t += 32) {
+        const int ij = t / nadj, s = t - ij * nadj;
+        const int i = ij / 3, j = ij % 3;
+        const int b = s_adj[s];
+        const bool fi = g.ind_of[3 * a + i] >= 0, fj = g.ind_of[3 * (int64_t)b + j] >= 0;
+        const bool dg = (b == a) && (i == j);
+        const double v = (fi && fj) ? acc[s * 9 + ij] : (dg ? 1.0 : 0.0);
+        const int64_t pos = (int64_t)ij * g.nb + s0 + s;
+        if (g.bval64) g.bval64[pos] = v;
+        if (g.bval32) g.bval32[pos] = (float)v;
+        if (dg) {
+          const double di = fi ? (fabs(v) > 1e-30 ? 1.0 / v : 1.0) : 1.0;
+          if (g.bdinv64) g.bdinv64[3 * a + i] = di;
+          if (g.bdinv32) g.bdinv32[3 * a + i] = (float)di;
+        }
       }
     }
     __syncwarp();
@@ -602,6 +635,10 @@ int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0) {
   if (hs.first_error != ~0ull)
     return set_error(ctx, AXIA_ERR_TOO_LARGE, "node " + std::to_string(hs.first_error >> 8) +
                                                   ": adjacency candidate list above the cap");
+  // int32 copy of the block-row pointers for the node-block kernels
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_adj_ptr32, n_nodes + 1));
+  k_to_i32<<<grid_for(n_nodes + 1, 256, ctx->sm_count), 256, 0, s>>>(n_nodes + 1, d_adj_ptr, ctx->d_adj_ptr32);
+  ctx->launches++;
   // keep the 64-bit pointers for the gather
   dev_free(ctx->d_ne_ptr);
   dev_free(ctx->d_adj_ptr);
@@ -620,8 +657,10 @@ int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0) {
   return AXIA_OK;
 }
 
-int numeric_assemble(axia_ctx* ctx, bool want32) {
+int numeric_assemble(axia_ctx* ctx, int flags) {
   cudaStream_t s = ctx->stream;
+  const bool csr64 = flags & AXIA_ASM_CSR64, csr32 = flags & AXIA_ASM_CSR32;
+  const bool bsr64 = flags & AXIA_ASM_BSR64, bsr32 = flags & AXIA_ASM_BSR32;
   const int64_t kesz = (int64_t)9 * ctx->nn * ctx->nn;
   if (ctx->ke_elems < (size_t)(ctx->n_elem * kesz)) {
     AXIA_TRY(dev_alloc(ctx, &ctx->d_ke, (size_t)(ctx->n_elem * kesz)));
@@ -641,12 +680,16 @@ int numeric_assemble(axia_ctx* ctx, bool want32) {
   ea.vol_out = nullptr;
   ea.status = ctx->d_status;
   AXIA_TRY(run_element_ke(ctx, ctx->nn, ctx->reduced, ea));
-  if (!ctx->d_val) AXIA_TRY(dev_alloc(ctx, &ctx->d_val, ctx->nnz));
-  if (want32 && !ctx->d_val32) AXIA_TRY(dev_alloc(ctx, &ctx->d_val32, ctx->nnz));
+  if (csr64 && !ctx->d_val) AXIA_TRY(dev_alloc(ctx, &ctx->d_val, ctx->nnz));
+  if (csr32 && !ctx->d_val32) AXIA_TRY(dev_alloc(ctx, &ctx->d_val32, ctx->nnz));
   if (!ctx->d_diag) AXIA_TRY(dev_alloc(ctx, &ctx->d_diag, ctx->n_free));
   if (!ctx->d_dinv) AXIA_TRY(dev_alloc(ctx, &ctx->d_dinv, ctx->n_free));
-  if (want32 && !ctx->d_dinv32) AXIA_TRY(dev_alloc(ctx, &ctx->d_dinv32, ctx->n_free));
+  if (csr32 && !ctx->d_dinv32) AXIA_TRY(dev_alloc(ctx, &ctx->d_dinv32, ctx->n_free));
   if (!ctx->d_kfu0) AXIA_TRY(dev_alloc(ctx, &ctx->d_kfu0, ctx->n_free));
+  if (bsr64 && !ctx->d_bval64) AXIA_TRY(dev_alloc(ctx, &ctx->d_bval64, (size_t)(9 * ctx->n_adj)));
+  if (bsr32 && !ctx->d_bval32) AXIA_TRY(dev_alloc(ctx, &ctx->d_bval32, (size_t)(9 * ctx->n_adj)));
+  if ((bsr64 || bsr32) && !ctx->d_bdinv64) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv64, (size_t)ctx->ndof));
+  if (bsr32 && !ctx->d_bdinv32) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv32, (size_t)ctx->ndof));
   AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_kfu0, 0, ctx->n_free * sizeof(double), s));
   GatherArgs g{};
   g.n_nodes = ctx->n_nodes;
@@ -663,16 +706,23 @@ int numeric_assemble(axia_ctx* ctx, bool want32) {
   g.u0 = ctx->d_u0;
   g.any_u0 = ctx->any_u0 ? 1 : 0;
   g.max_adj = std::max(ctx->max_adj, 1);
-  g.val = ctx->d_val;
-  g.val32 = want32 ? ctx->d_val32 : nullptr;
+  g.val = csr64 ? ctx->d_val : nullptr;
+  g.val32 = csr32 ? ctx->d_val32 : nullptr;
   g.diag = ctx->d_diag;
   g.dinv = ctx->d_dinv;
-  g.dinv32 = want32 ? ctx->d_dinv32 : nullptr;
+  g.dinv32 = csr32 ? ctx->d_dinv32 : nullptr;
   g.kfu0 = ctx->d_kfu0;
+  g.bval64 = bsr64 ? ctx->d_bval64 : nullptr;
+  g.bval32 = bsr32 ? ctx->d_bval32 : nullptr;
+  g.bdinv64 = (bsr64 || bsr32) ? ctx->d_bdinv64 : nullptr;
+  g.bdinv32 = bsr32 ? ctx->d_bdinv32 : nullptr;
+  g.nb = ctx->n_adj;
   AXIA_TRY(run_gather(ctx, g));
   AXIA_CUDA(ctx, cudaStreamSynchronize(s));
   DevStatus hs;
   AXIA_TRY(read_dev_status(ctx, &hs));
+  ctx->have_csr64 = ctx->have32 = ctx->have_bsr64 = ctx->have_bsr32 = false;
+  ctx->assembled = false;
   if (hs.first_error != ~0ull) {
     int code = (int)(hs.first_error & 0xff);
     long long idx = (long long)(hs.first_error >> 8);
@@ -682,7 +732,10 @@ int numeric_assemble(axia_ctx* ctx, bool want32) {
     ctx->last_bad = idx;
     return set_error(ctx, code, "element " + std::to_string(idx) + ": " + what);
   }
-  ctx->have32 = want32;
+  ctx->have_csr64 = csr64;
+  ctx->have32 = csr32;
+  ctx->have_bsr64 = bsr64;
+  ctx->have_bsr32 = bsr32;
   ctx->assembled = true;
   return AXIA_OK;
 }

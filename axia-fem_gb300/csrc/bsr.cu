@@ -1,0 +1,529 @@
+// bsr.cu -- the node-block (3x3 BSR) form of the static system and the
+// persistent Krylov kernels on it.
+//
+// Layout: one block row per node a, one 3x3 block per adjacent node b (the
+// node adjacency of the symbolic phase, sorted), values stored as nine
+// structure-of-arrays planes val[k][s] (k = 3 i + j) so lanes that walk
+// consecutive blocks of a row load consecutive addresses.  Index traffic is
+// one int32 per 9 values: 4.44 bytes per nonzero in FP32 (CSR: 8) and 8.44 in
+// FP64 (CSR: 12).
+//
+// The system is the full-DOF form of K_ff: rows and columns of prescribed
+// DOFs are zero except a unit diagonal, their right-hand side is zero.  CG on
+// it produces the same iterates as CG on K_ff (the prescribed components of
+// r, z, p, q, x stay exactly zero) with vectors of 3 n_nodes entries, so the
+// DOF map never enters the inner loop.
+//
+// Kernels: bsr_spmv_kernel (y = K x), pcg_bsr_kernel (Jacobi PCG as in
+// solver/src/linalg.rs:199-259, FP64 or FP32) and pcg_bsr_reliable_kernel
+// (FP32 inner CG with FP64 reliable updates, the mixed form).
+#include <algorithm>
+#include <cmath>
+
+#include "solver.cuh"
+
+template <typename V>
+struct BsrMat {
+  int n_nodes;
+  const int* adj_ptr;  // [n_nodes+1]
+  const int* adj;      // [nb]
+  const V* val;        // [9][nb]
+  long long nb;
+};
+
+// Block row a with L lanes: (y0, y1, y2) = sum_s K_as x_adj[s]
+template <typename V, typename A, int L>
+__device__ __forceinline__ void bsr_row(int a, int sl, const BsrMat<V>& M, const V* x, A& y0, A& y1, A& y2) {
+  y0 = y1 = y2 = A(0);
+  if (a < M.n_nodes) {
+    const int beg = __ldg(M.adj_ptr + a), end = __ldg(M.adj_ptr + a + 1);
+    const long long nb = M.nb;
+#pragma unroll 2
+    for (int s = beg + sl; s < end; s += L) {
+      const int b = ld_stream(M.adj + s);
+      const A x0 = (A)x[3 * b], x1 = (A)x[3 * b + 1], x2 = (A)x[3 * b + 2];
+      const V* v = M.val + s;
+      y0 = fma((A)ld_stream(v), x0, y0);
+      y0 = fma((A)ld_stream(v + nb), x1, y0);
+      y0 = fma((A)ld_stream(v + 2 * nb), x2, y0);
+      y1 = fma((A)ld_stream(v + 3 * nb), x0, y1);
+      y1 = fma((A)ld_stream(v + 4 * nb), x1, y1);
+      y1 = fma((A)ld_stream(v + 5 * nb), x2, y1);
+      y2 = fma((A)ld_stream(v + 6 * nb), x0, y2);
+      y2 = fma((A)ld_stream(v + 7 * nb), x1, y2);
+      y2 = fma((A)ld_stream(v + 8 * nb), x2, y2);
+    }
+  }
+  y0 = group_sum<L>(y0);
+  y1 = group_sum<L>(y1);
+  y2 = group_sum<L>(y2);
+}
+
+template <typename V, int L>
+__global__ void __launch_bounds__(PCG_THREADS) bsr_spmv_kernel(BsrMat<V> M, const V* x, V* y) {
+  constexpr int RPW = 32 / L;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  const int gwarp = tid >> 5, nwarps = nth >> 5;
+  const int lane = threadIdx.x & 31, sl = lane % L, grp = lane / L;
+  for (int base = gwarp * RPW; base < M.n_nodes; base += nwarps * RPW) {
+    const int a = base + grp;
+    V y0, y1, y2;
+    bsr_row<V, V, L>(a, sl, M, x, y0, y1, y2);
+    if (a < M.n_nodes && sl == 0) {
+      y[3 * a] = y0;
+      y[3 * a + 1] = y1;
+      y[3 * a + 2] = y2;
+    }
+  }
+}
+
+template <typename V>
+struct BsrPcgArgs {
+  BsrMat<V> M;
+  int nd;            // 3 n_nodes
+  const V* dinv;     // [nd]
+  const V* b;
+  V* x;
+  V* r;
+  V* p;
+  V* q;
+  double* partials;
+  double* totals;
+  GridBarrier* bar;
+  DevStatus* st;
+  PcgOut* out;
+  double tol;
+  long long max_iter;
+  unsigned long long limit_ns;
+};
+
+// Jacobi PCG on the node-block form (same recurrence as pcg_kernel).
+template <typename V, int L>
+__global__ void __launch_bounds__(PCG_THREADS) pcg_bsr_kernel(BsrPcgArgs<V> P) {
+  using A = V;
+  const int nd = P.nd, n_nodes = P.M.n_nodes;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  constexpr int RPW = 32 / L;
+  const int gwarp = tid >> 5, nwarps = nth >> 5;
+  const int lane = threadIdx.x & 31, sl = lane % L, grp = lane / L;
+  A rz_p = 0, bb_p = 0;
+  for (int i = tid; i < nd; i += nth) {
+    const V bi = P.b[i];
+    P.x[i] = V(0);
+    P.r[i] = bi;
+    const V z = bi * P.dinv[i];
+    P.p[i] = z;
+    rz_p = fma(bi, z, rz_p);
+    bb_p = fma(bi, bi, bb_p);
+  }
+  block_partials<A>(bb_p, rz_p, 2, P.partials, S_RR, S_RZ);
+  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+  A rz = (A)total(P.totals, S_RZ);
+  const double bnorm = sqrt(total(P.totals, S_RR));
+  long long iters = 0;
+  double residual = bnorm;
+  int status = AXIA_OK;
+  if (bnorm >= 1e-30) {
+    for (long long it = 0; it < P.max_iter; ++it) {
+      iters = it + 1;
+      A pq_p = 0;
+      for (int base = gwarp * RPW; base < n_nodes; base += nwarps * RPW) {
+        const int a = base + grp;
+        A y0, y1, y2;
+        bsr_row<V, A, L>(a, sl, P.M, P.p, y0, y1, y2);
+        if (a < n_nodes && sl == 0) {
+          P.q[3 * a] = (V)y0;
+          P.q[3 * a + 1] = (V)y1;
+          P.q[3 * a + 2] = (V)y2;
+          pq_p = fma((A)P.p[3 * a], y0, pq_p);
+          pq_p = fma((A)P.p[3 * a + 1], y1, pq_p);
+          pq_p = fma((A)P.p[3 * a + 2], y2, pq_p);
+        }
+      }
+      block_partials<A>(pq_p, A(0), 1, P.partials, S_PQ, S_PQ);
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1)) return;
+      const A pq = (A)total(P.totals, S_PQ);
+      if (!(fabs((double)pq) >= 1e-30)) {
+        status = AXIA_ERR_ZERO_PIVOT;
+        break;
+      }
+      const A alpha = rz / pq;
+      A rr_p = 0, rzn_p = 0;
+      for (int i = tid; i < nd; i += nth) {
+        P.x[i] = fma(alpha, P.p[i], P.x[i]);
+        const V ri = fma(-alpha, P.q[i], P.r[i]);
+        P.r[i] = ri;
+        rr_p = fma(ri, ri, rr_p);
+        rzn_p = fma(ri, ri * P.dinv[i], rzn_p);
+      }
+      block_partials<A>(rr_p, rzn_p, 2, P.partials, S_RR, S_RZ);
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+      const A rzn = (A)total(P.totals, S_RZ);
+      residual = sqrt(total(P.totals, S_RR));
+      if (!isfinite(residual)) {
+        status = AXIA_ERR_NONFINITE;
+        break;
+      }
+      if (residual <= P.tol * bnorm) break;
+      const A beta = rzn / rz;
+      rz = rzn;
+      for (int i = tid; i < nd; i += nth) P.p[i] = fma(beta, P.p[i], P.r[i] * P.dinv[i]);
+      if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+    }
+    if (status == AXIA_OK && residual > P.tol * bnorm * 10.0) status = AXIA_ERR_NOT_CONVERGED;
+  } else {
+    residual = 0.0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.out->iters = iters;
+    P.out->residual = residual;
+    P.out->bnorm = bnorm;
+    P.out->status = status;
+    P.out->updates = 0;
+  }
+}
+
+struct BsrReliableArgs {
+  BsrMat<float> M32;
+  BsrMat<double> M64;
+  int nd;
+  const float* dinv32;
+  const double* b;
+  double* x;
+  float* x32;
+  float* r32;
+  float* p32;
+  float* q32;
+  double* partials;
+  double* totals;
+  GridBarrier* bar;
+  DevStatus* st;
+  PcgOut* out;
+  double tol;
+  double delta;
+  long long max_iter;
+  unsigned long long limit_ns;
+};
+
+// FP32 CG on the FP32 node-block matrix with FP64 reliable updates
+// (the recurrence of pcg_reliable_kernel in pcg.cu on the node-block form).
+template <int L32, int L64>
+__global__ void __launch_bounds__(PCG_THREADS, 4) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
+  const int nd = P.nd, n_nodes = P.M32.n_nodes;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  const int gwarp = tid >> 5, nwarps = nth >> 5;
+  const int lane = threadIdx.x & 31;
+  float rz_p = 0.f;
+  double bb_p = 0.0;
+  for (int i = tid; i < nd; i += nth) {
+    const double bi = P.b[i];
+    P.x[i] = 0.0;
+    const float ri = (float)bi;
+    P.r32[i] = ri;
+    P.x32[i] = 0.f;
+    const float z = ri * P.dinv32[i];
+    P.p32[i] = z;
+    rz_p = fmaf(ri, z, rz_p);
+    bb_p = fma(bi, bi, bb_p);
+  }
+  block_partials<double>(bb_p, (double)rz_p, 2, P.partials, S_RR, S_RZ);
+  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+  float rz = (float)total(P.totals, S_RZ);
+  const double bnorm = sqrt(total(P.totals, S_RR));
+  double rmax = bnorm, residual = bnorm;
+  long long iters = 0;
+  int updates = 0, status = AXIA_OK;
+  bool converged = bnorm < 1e-30;
+  if (converged) residual = 0.0;
+  for (long long it = 0; !converged && it < P.max_iter; ++it) {
+    iters = it + 1;
+    float pq_p = 0.f;
+    {
+      constexpr int RPW = 32 / L32;
+      const int sl = lane % L32, grp = lane / L32;
+      for (int base = gwarp * RPW; base < n_nodes; base += nwarps * RPW) {
+        const int a = base + grp;
+        float y0, y1, y2;
+        bsr_row<float, float, L32>(a, sl, P.M32, P.p32, y0, y1, y2);
+        if (a < n_nodes && sl == 0) {
+          P.q32[3 * a] = y0;
+          P.q32[3 * a + 1] = y1;
+          P.q32[3 * a + 2] = y2;
+          pq_p = fmaf(P.p32[3 * a], y0, pq_p);
+          pq_p = fmaf(P.p32[3 * a + 1], y1, pq_p);
+          pq_p = fmaf(P.p32[3 * a + 2], y2, pq_p);
+        }
+      }
+    }
+    block_partials<float>(pq_p, 0.f, 1, P.partials, S_PQ, S_PQ);
+    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1)) return;
+    const float pq = (float)total(P.totals, S_PQ);
+    if (!(fabsf(pq) >= 1e-30f) || !isfinite(pq)) {
+      status = isfinite(pq) ? AXIA_ERR_ZERO_PIVOT : AXIA_ERR_NONFINITE;
+      break;
+    }
+    const float alpha = rz / pq;
+    float rr_p = 0.f, rzn_p = 0.f;
+    for (int i = tid; i < nd; i += nth) {
+      P.x32[i] = fmaf(alpha, P.p32[i], P.x32[i]);
+      const float ri = fmaf(-alpha, P.q32[i], P.r32[i]);
+      P.r32[i] = ri;
+      rr_p = fmaf(ri, ri, rr_p);
+      rzn_p = fmaf(ri, ri * P.dinv32[i], rzn_p);
+    }
+    block_partials<float>(rr_p, rzn_p, 2, P.partials, S_RR, S_RZ);
+    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+    float rzn = (float)total(P.totals, S_RZ);
+    const double rnorm32 = sqrt(total(P.totals, S_RR));
+    if (!isfinite(rnorm32)) {
+      status = AXIA_ERR_NONFINITE;
+      break;
+    }
+    if (rnorm32 <= P.delta * rmax || rnorm32 <= P.tol * bnorm) {
+      for (int i = tid; i < nd; i += nth) {
+        P.x[i] += (double)P.x32[i];
+        P.x32[i] = 0.f;
+      }
+      if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+      double rr64_p = 0.0;
+      float rz_new_p = 0.f;
+      {
+        constexpr int RPW = 32 / L64;
+        const int sl = lane % L64, grp = lane / L64;
+        for (int base = gwarp * RPW; base < n_nodes; base += nwarps * RPW) {
+          const int a = base + grp;
+          double y[3];
+          bsr_row<double, double, L64>(a, sl, P.M64, P.x, y[0], y[1], y[2]);
+          if (a < n_nodes && sl == 0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const int i = 3 * a + c;
+              const double ri = P.b[i] - y[c];
+              rr64_p = fma(ri, ri, rr64_p);
+              const float r32 = (float)ri;
+              P.r32[i] = r32;
+              rz_new_p = fmaf(r32, r32 * P.dinv32[i], rz_new_p);
+            }
+          }
+        }
+      }
+      block_partials<double>(rr64_p, (double)rz_new_p, 2, P.partials, S_RR, S_RZ);
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+      ++updates;
+      residual = sqrt(total(P.totals, S_RR));
+      rzn = (float)total(P.totals, S_RZ);
+      rmax = residual;
+      if (!isfinite(residual)) {
+        status = AXIA_ERR_NONFINITE;
+        break;
+      }
+      if (residual <= P.tol * bnorm) {
+        converged = true;
+        break;
+      }
+    }
+    const float beta = rzn / rz;
+    rz = rzn;
+    for (int i = tid; i < nd; i += nth) P.p32[i] = fmaf(beta, P.p32[i], P.r32[i] * P.dinv32[i]);
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+  }
+  if (status == AXIA_OK && residual > P.tol * bnorm * 10.0) status = AXIA_ERR_NOT_CONVERGED;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.out->iters = iters;
+    P.out->residual = residual;
+    P.out->bnorm = bnorm;
+    P.out->status = status;
+    P.out->updates = updates;
+  }
+}
+
+// b[d] = f[d] - K_fp u0 for free d, 0 for prescribed d
+__global__ void k_build_rhs_full(int64_t nd, const int32_t* ind_of, const double* f, const double* kfu0, double* b) {
+  for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
+    const int r = ind_of[d];
+    b[d] = r >= 0 ? f[d] - kfu0[r] : 0.0;
+  }
+}
+// u = u0 + x on free DOFs (reconstruct, constraint.rs:207-217)
+__global__ void k_reconstruct_full(int64_t nd, const int32_t* ind_of, const double* u0, const double* x, double* u) {
+  for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x)
+    u[d] = ind_of[d] >= 0 ? u0[d] + x[d] : u0[d];
+}
+// ||b - K x|| partials (FP64), full-DOF form
+template <int L>
+__global__ void __launch_bounds__(PCG_THREADS) bsr_residual_kernel(BsrMat<double> M, const double* b, const double* x,
+                                                                   double* partials) {
+  constexpr int RPW = 32 / L;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  const int gwarp = tid >> 5, nwarps = nth >> 5;
+  const int lane = threadIdx.x & 31, sl = lane % L, grp = lane / L;
+  double rr = 0.0;
+  for (int base = gwarp * RPW; base < M.n_nodes; base += nwarps * RPW) {
+    const int a = base + grp;
+    double y0, y1, y2;
+    bsr_row<double, double, L>(a, sl, M, x, y0, y1, y2);
+    if (a < M.n_nodes && sl == 0) {
+      const double r0 = b[3 * a] - y0, r1 = b[3 * a + 1] - y1, r2 = b[3 * a + 2] - y2;
+      rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, rr)));
+    }
+  }
+  block_partials<double>(rr, 0.0, 1, partials, 0, 0);
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+// Lanes per block row: about one block per lane (C3D8 interior rows have 27
+// blocks, C3D20 corner rows 81); measured on GB300 at 100^3 C3D8, 16 lanes
+// beat 8 by 1.3x for FP32.
+static int bsr_lanes(const axia_ctx* ctx, int requested) {
+  if (requested == 2 || requested == 4 || requested == 8 || requested == 16) return requested;
+  double avg = ctx->n_nodes ? (double)ctx->n_adj / (double)ctx->n_nodes : 1.0;  // blocks per block row
+  return avg <= 6 ? 4 : (avg <= 12 ? 8 : 16);
+}
+
+template <typename V>
+static BsrMat<V> bsr_mat(const axia_ctx* ctx, const V* val) {
+  return BsrMat<V>{(int)ctx->n_nodes, ctx->d_adj_ptr32, ctx->d_adj, val, (long long)ctx->n_adj};
+}
+
+static int ensure_full_buffers(axia_ctx* ctx, bool mixed) {
+  const size_t nd = (size_t)ctx->ndof;
+  if (ctx->full_capacity < nd || (mixed && !ctx->d_xf32)) {
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_bf, nd));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_xf, nd));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_rf, nd));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_pf, nd));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_qf, nd));
+    if (mixed) {
+      AXIA_TRY(dev_alloc(ctx, &ctx->d_xf32, nd));
+      AXIA_TRY(dev_alloc(ctx, &ctx->d_rf32, nd));
+      AXIA_TRY(dev_alloc(ctx, &ctx->d_pf32, nd));
+      AXIA_TRY(dev_alloc(ctx, &ctx->d_qf32, nd));
+    }
+    ctx->full_capacity = nd;
+  }
+  return AXIA_OK;
+}
+
+template <typename V, int L>
+static int launch_bsr_pcg_t(axia_ctx* ctx, BsrPcgArgs<V>& P) {
+  auto kern = pcg_bsr_kernel<V, L>;
+  int grid = 0;
+  AXIA_TRY(coop_grid(ctx, (const void*)kern, P.nd, &grid));
+  void* params[] = {&P};
+  AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params, 0, ctx->stream));
+  ctx->launches++;
+  return AXIA_OK;
+}
+
+template <typename V>
+static int launch_bsr_pcg(axia_ctx* ctx, BsrPcgArgs<V>& P, int lanes) {
+  switch (lanes) {
+    case 2: return launch_bsr_pcg_t<V, 2>(ctx, P);
+    case 4: return launch_bsr_pcg_t<V, 4>(ctx, P);
+    case 16: return launch_bsr_pcg_t<V, 16>(ctx, P);
+    default: return launch_bsr_pcg_t<V, 8>(ctx, P);
+  }
+}
+
+template <int L32, int L64>
+static int launch_bsr_rel_t(axia_ctx* ctx, BsrReliableArgs& P) {
+  auto kern = pcg_bsr_reliable_kernel<L32, L64>;
+  int grid = 0;
+  AXIA_TRY(coop_grid(ctx, (const void*)kern, P.nd, &grid));
+  void* params[] = {&P};
+  AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params, 0, ctx->stream));
+  ctx->launches++;
+  return AXIA_OK;
+}
+
+static int launch_bsr_rel(axia_ctx* ctx, BsrReliableArgs& P, int l32) {
+  switch (l32) {
+    case 2: return launch_bsr_rel_t<2, 8>(ctx, P);
+    case 4: return launch_bsr_rel_t<4, 8>(ctx, P);
+    case 16: return launch_bsr_rel_t<16, 8>(ctx, P);
+    default: return launch_bsr_rel_t<8, 8>(ctx, P);
+  }
+}
+
+static double bsr_residual(axia_ctx* ctx, const double* b, const double* x) {
+  const int grid = ctx->sm_count * 4;
+  bsr_residual_kernel<4><<<grid, PCG_THREADS, 0, ctx->stream>>>(bsr_mat<double>(ctx, ctx->d_bval64), b, x,
+                                                                ctx->d_partials);
+  ctx->launches++;
+  std::vector<double> h(grid);
+  cudaMemcpyAsync(h.data(), ctx->d_partials, grid * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  double s = 0.0;
+  for (double v : h) s += v;
+  return std::sqrt(s);
+}
+
+// Solve on the node-block form: rhs from d_f (full), solution into d_u (full).
+int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_opts* opts, axia_solve_info* info) {
+  const bool mixed = opts->precision == AXIA_PREC_MIXED;
+  if (!ctx->have_bsr64 || (mixed && !ctx->have_bsr32))
+    return set_error(ctx, AXIA_ERR_STATE, "node-block solve needs axia_gpu_assemble_ex with the BSR flags");
+  AXIA_TRY(ensure_full_buffers(ctx, mixed));
+  AXIA_TRY(reset_dev_status(ctx));
+  const int64_t nd = ctx->ndof;
+  k_build_rhs_full<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(nd, ctx->d_ind_of, d_f, ctx->d_kfu0, ctx->d_bf);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  const long long max_iter = opts->max_iter > 0 ? opts->max_iter : std::max<long long>(4LL * ctx->n_free, 200);
+  const unsigned long long limit_ns = 2000000000ull;
+  const int lanes = bsr_lanes(ctx, opts->spmv_lanes);
+  AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
+  PcgOut o{};
+  if (!mixed) {
+    BsrPcgArgs<double> P{bsr_mat<double>(ctx, ctx->d_bval64), (int)nd, ctx->d_bdinv64, ctx->d_bf, ctx->d_xf,
+                         ctx->d_rf, ctx->d_pf, ctx->d_qf, ctx->d_partials, ctx->d_totals, ctx->d_bar,
+                         ctx->d_status, (PcgOut*)ctx->d_out, opts->rtol, max_iter, limit_ns};
+    AXIA_TRY(timed_launch(ctx, info, [&] { return launch_bsr_pcg<double>(ctx, P, lanes); }));
+  } else {
+    const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.1;
+    BsrReliableArgs P{bsr_mat<float>(ctx, ctx->d_bval32), bsr_mat<double>(ctx, ctx->d_bval64), (int)nd,
+                      ctx->d_bdinv32, ctx->d_bf, ctx->d_xf, ctx->d_xf32, ctx->d_rf32, ctx->d_pf32, ctx->d_qf32,
+                      ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out, opts->rtol,
+                      delta, max_iter, limit_ns};
+    AXIA_TRY(timed_launch(ctx, info, [&] { return launch_bsr_rel(ctx, P, lanes); }));
+  }
+  AXIA_TRY(read_out(ctx, &o));
+  info->iters = o.iters;
+  info->outer_iters = mixed ? o.updates : 1;
+  info->residual = o.residual;
+  info->bnorm = o.bnorm;
+  if (o.status != AXIA_OK) return status_error(ctx, o);
+  k_reconstruct_full<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(nd, ctx->d_ind_of, ctx->d_u0, ctx->d_xf, d_u);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  info->true_residual = bsr_residual(ctx, ctx->d_bf, ctx->d_xf);
+  return AXIA_OK;
+}
+
+int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req) {
+  if (fp32 ? !ctx->have_bsr32 : !ctx->have_bsr64) return set_error(ctx, AXIA_ERR_STATE, "node-block matrix not assembled");
+  const int lanes = bsr_lanes(ctx, lanes_req);
+  int per_sm = 0;
+  const int grid_max = ctx->sm_count * 4;
+  (void)per_sm;
+  if (fp32) {
+    auto M = bsr_mat<float>(ctx, ctx->d_bval32);
+    switch (lanes) {
+      case 4: bsr_spmv_kernel<float, 4><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const float*)x, (float*)y); break;
+      case 16: bsr_spmv_kernel<float, 16><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const float*)x, (float*)y); break;
+      default: bsr_spmv_kernel<float, 8><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const float*)x, (float*)y); break;
+    }
+  } else {
+    auto M = bsr_mat<double>(ctx, ctx->d_bval64);
+    switch (lanes) {
+      case 4: bsr_spmv_kernel<double, 4><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const double*)x, (double*)y); break;
+      case 16: bsr_spmv_kernel<double, 16><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const double*)x, (double*)y); break;
+      default: bsr_spmv_kernel<double, 8><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const double*)x, (double*)y); break;
+    }
+  }
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  return AXIA_OK;
+}

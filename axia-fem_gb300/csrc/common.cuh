@@ -44,6 +44,13 @@ __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // Grid-wide barrier for a cooperative (co-resident) launch.  The wait is
 // bounded: after `limit_ns` the block records a timeout and returns false;
 // every caller then leaves its loop, so a stuck barrier ends all blocks.
@@ -84,18 +91,69 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, DevStatus* st, unsig
   return s_ok != 0;
 }
 
+// Grid-wide barrier that also reduces.  Every block has stored its partials of
+// nv values at partials[(slot0 + k) * gridDim.x + blockIdx.x]; the last block
+// to arrive sums them in ascending block order (a fixed order, so every run
+// gives the same bits) and publishes totals[slot0 + k] before it releases the
+// others.  Same bounded wait as grid_sync.  After it returns, every thread may
+// read totals[] (with ld.cg: they were written by another block).
+__device__ __forceinline__ bool grid_reduce_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns,
+                                                 const double* partials, double* totals, int slot0, int nv) {
+  __shared__ int s_ok2;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    unsigned g = 0;
+    int last = 0;
+    if (lane == 0) {
+      g = ld_acquire_gpu(&bar->gen);
+      __threadfence();
+      last = atomicAdd(&bar->count, 1u) == gridDim.x - 1;
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    int ok = 1;
+    if (last) {
+      __threadfence();
+      for (int k = 0; k < nv; ++k) {
+        double a = 0.0;
+        for (int j = lane; j < (int)gridDim.x; j += 32) a += __ldcg(partials + (size_t)(slot0 + k) * gridDim.x + j);
+        a = warp_sum(a);
+        if (lane == 0) totals[slot0 + k] = a;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        bar->count = 0;
+        __threadfence();
+        st_release_gpu(&bar->gen, g + 1);
+      }
+    } else if (lane == 0) {
+      unsigned long long t0 = global_ns();
+      unsigned spins = 0;
+      while (ld_acquire_gpu(&bar->gen) == g) {
+        if ((++spins & 63u) == 0 && global_ns() - t0 > limit_ns) {
+          atomicExch(&st->timeout, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    if (lane == 0) {
+      __threadfence();
+      if (*(volatile int*)&st->timeout) ok = 0;
+      s_ok2 = ok;
+    }
+  }
+  __syncthreads();
+  return s_ok2 != 0;
+}
+
 // Streaming (evict-first) loads for matrix data that is read once per sweep,
 // so the vectors keep their L2 lines.
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
 
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 
 // ---------------------------------------------------------------------------
 // Host side
@@ -148,7 +206,15 @@ struct axia_ctx {
   double* d_dinv = nullptr;     // [n_free]
   float* d_dinv32 = nullptr;    // [n_free]
   double* d_kfu0 = nullptr;     // [n_free]
-  bool assembled = false, have32 = false;
+  bool assembled = false, have32 = false, have_csr64 = false;
+
+  // node-block (3x3) form of the full-DOF system
+  int32_t* d_adj_ptr32 = nullptr;  // [n_nodes+1]
+  double* d_bval64 = nullptr;      // [9][n_adj]
+  float* d_bval32 = nullptr;       // [9][n_adj]
+  double* d_bdinv64 = nullptr;     // [ndof]
+  float* d_bdinv32 = nullptr;      // [ndof]
+  bool have_bsr64 = false, have_bsr32 = false;
 
   // element stiffness scratch
   double* d_ke = nullptr;
@@ -168,11 +234,23 @@ struct axia_ctx {
   float* d_p32 = nullptr;
   float* d_q32 = nullptr;
   double* d_partials = nullptr;
+  double* d_totals = nullptr;
   size_t partial_slots = 0;
   GridBarrier* d_bar = nullptr;
   DevStatus* d_status = nullptr;
   void* d_out = nullptr;        // PcgOut
   size_t vec_capacity = 0;
+  // full-DOF vectors of the node-block solve
+  double *d_bf = nullptr, *d_xf = nullptr, *d_rf = nullptr, *d_pf = nullptr, *d_qf = nullptr;
+  float *d_xf32 = nullptr, *d_rf32 = nullptr, *d_pf32 = nullptr, *d_qf32 = nullptr;
+  size_t full_capacity = 0;
+
+  // SIMP compliance state (forward -> backward)
+  double* d_rho = nullptr;      // [n_elem]
+  double* d_energy = nullptr;   // [n_elem]
+  double* d_grad = nullptr;     // [n_elem]
+  double simp_p = 3.0, simp_e0 = 1.0;
+  bool have_forward = false;
 
   double ms_setup = 0.0, ms_assemble = 0.0;
   int64_t last_bad = -1;

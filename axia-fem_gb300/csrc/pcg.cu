@@ -4,103 +4,40 @@
 // |diag| > 1e-30 guard, stop at ||r||_2 <= tol ||b||_2, error when the final
 // residual exceeds 10 tol ||b|| or |p.Ap| < 1e-30.  One cooperative launch runs
 // every iteration: the SpMV q = K p with the p.q partial sum, the x / r update
-// with the r.r and r.z partial sums, and the p update, separated by three
-// bounded grid barriers.  Dot products are reduced per block and then summed
-// by every block over all block partials in a fixed order, so every block
-// takes the same branch and the result is bitwise reproducible.
+// with the r.r and r.z partial sums, and the p update.  The two reductions are
+// reduce-and-sync grid barriers (the last block to arrive sums all block
+// partials in a fixed order and publishes the totals), the p update ends with
+// a plain grid barrier; every wait is bounded.  Every block sees the same
+// totals, takes the same branch, and results are bitwise reproducible.
 //
-// SpMV: L lanes per row (vectorised CSR), matrix values and column indices
-// loaded with evict-first hints so the vectors stay resident in L2.
+// SpMV: L lanes per CSR row (vectorised CSR), matrix values and column
+// indices loaded with evict-first hints so the vectors stay resident in L2.
+//
+// Mixed precision, two forms:
+//  * restart: classic iterative refinement -- FP32 inner PCG on the FP32 copy
+//    of K_ff to a residual reduction inner_rtol, FP64 update x += d and FP64
+//    residual r = b - K_ff x, repeated (host loop, one launch per inner solve);
+//  * reliable: one FP32 Krylov sequence in one launch; whenever its residual
+//    has dropped by inner_rtol since the last update, the FP32 correction is
+//    added to the FP64 solution and the FP32 residual is replaced by the FP64
+//    residual b - K_ff x (search direction kept).  Convergence is decided on
+//    the FP64 residual.
 #include <algorithm>
 #include <cmath>
 
-#include "common.cuh"
+#include "solver.cuh"
 
-constexpr int PCG_THREADS = 256;
-int pcg_lanes_for(const axia_ctx* ctx, bool fp32, int requested);
-constexpr int S_PQ = 0, S_RR = 1, S_RZ = 2, N_SLOTS = 3;
-
-struct PcgOut {
-  long long iters;
-  double residual;
-  double bnorm;
-  int status;
-  int pad;
-};
-
-template <typename V>
-struct PcgArgs {
-  int n;
-  const int* rowptr;
-  const int* col;
-  const V* val;
-  const V* dinv;
-  const V* b;
-  V* x;
-  V* r;
-  V* p;
-  V* q;
-  double* partials;  // [N_SLOTS][gridDim.x]
-  GridBarrier* bar;
-  DevStatus* st;
-  PcgOut* out;
-  double tol;
-  long long max_iter;
-  unsigned long long limit_ns;
-};
-
-template <int L, typename T>
-__device__ __forceinline__ T group_sum(T v) {
-#pragma unroll
-  for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// block-reduce up to two values and store them as this block's partials
-template <typename A>
-__device__ __forceinline__ void block_partials(A v0, A v1, int nv, double* partials, int slot0, int slot1) {
-  __shared__ A s_red[2][32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  v0 = warp_sum(v0);
-  if (nv > 1) v1 = warp_sum(v1);
-  if (lane == 0) {
-    s_red[0][warp] = v0;
-    s_red[1][warp] = v1;
+// One CSR row, L lanes: sum_k val[k] x[col[k]].
+template <typename V, typename A, int L>
+__device__ __forceinline__ A csr_row_dot(int row, int n, int sl, const int* __restrict__ rowptr,
+                                         const int* __restrict__ col, const V* __restrict__ val, const V* x) {
+  A s = 0;
+  if (row < n) {
+    const int beg = __ldg(rowptr + row), end = __ldg(rowptr + row + 1);
+#pragma unroll 4
+    for (int k = beg + sl; k < end; k += L) s = fma((A)ld_stream(val + k), (A)x[ld_stream(col + k)], s);
   }
-  __syncthreads();
-  if (warp == 0) {
-    A a0 = lane < nw ? s_red[0][lane] : A(0);
-    A a1 = lane < nw ? s_red[1][lane] : A(0);
-    a0 = warp_sum(a0);
-    if (nv > 1) a1 = warp_sum(a1);
-    if (lane == 0) {
-      partials[slot0 * gridDim.x + blockIdx.x] = (double)a0;
-      if (nv > 1) partials[slot1 * gridDim.x + blockIdx.x] = (double)a1;
-    }
-  }
-}
-
-// sum of all block partials of a slot, same order in every block
-template <typename A>
-__device__ __forceinline__ void grid_sums(const double* partials, int slot0, int slot1, int nv, A* r0, A* r1) {
-  __shared__ A s_out[2];
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    A a0 = 0, a1 = 0;
-    for (int k = lane; k < (int)gridDim.x; k += 32) {
-      a0 += (A)__ldcg(partials + slot0 * gridDim.x + k);
-      if (nv > 1) a1 += (A)__ldcg(partials + slot1 * gridDim.x + k);
-    }
-    a0 = warp_sum(a0);
-    if (nv > 1) a1 = warp_sum(a1);
-    if (lane == 0) {
-      s_out[0] = a0;
-      s_out[1] = a1;
-    }
-  }
-  __syncthreads();
-  *r0 = s_out[0];
-  if (nv > 1) *r1 = s_out[1];
+  return group_sum<L>(s);
 }
 
 template <typename V, int L>
@@ -124,11 +61,10 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_kernel(PcgArgs<V> P) {
     rz_p = fma(bi, z, rz_p);
     bb_p = fma(bi, bi, bb_p);
   }
-  block_partials<A>(rz_p, bb_p, 2, P.partials, S_RZ, S_RR);
-  if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
-  A rz, bb;
-  grid_sums<A>(P.partials, S_RZ, S_RR, 2, &rz, &bb);
-  const double bnorm = sqrt((double)bb);
+  block_partials<A>(bb_p, rz_p, 2, P.partials, S_RR, S_RZ);
+  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+  A rz = (A)total(P.totals, S_RZ);
+  const double bnorm = sqrt(total(P.totals, S_RR));
   long long iters = 0;
   double residual = bnorm;
   int status = AXIA_OK;
@@ -139,21 +75,15 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_kernel(PcgArgs<V> P) {
       A pq_p = 0;
       for (int base = gwarp * RPW; base < n; base += nwarps * RPW) {
         const int row = base + grp;
-        A s = 0;
-        if (row < n) {
-          const int beg = __ldg(P.rowptr + row), end = __ldg(P.rowptr + row + 1);
-          for (int k = beg + sl; k < end; k += L) s = fma((A)ld_stream(P.val + k), (A)P.p[ld_stream(P.col + k)], s);
-        }
-        s = group_sum<L>(s);
+        const A s = csr_row_dot<V, A, L>(row, n, sl, P.rowptr, P.col, P.val, P.p);
         if (row < n && sl == 0) {
           P.q[row] = (V)s;
           pq_p = fma((A)P.p[row], s, pq_p);
         }
       }
       block_partials<A>(pq_p, A(0), 1, P.partials, S_PQ, S_PQ);
-      if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
-      A pq;
-      grid_sums<A>(P.partials, S_PQ, S_PQ, 1, &pq, &pq);
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1)) return;
+      const A pq = (A)total(P.totals, S_PQ);
       if (!(fabs((double)pq) >= 1e-30)) {
         status = AXIA_ERR_ZERO_PIVOT;
         break;
@@ -169,10 +99,9 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_kernel(PcgArgs<V> P) {
         rzn_p = fma(ri, ri * P.dinv[i], rzn_p);
       }
       block_partials<A>(rr_p, rzn_p, 2, P.partials, S_RR, S_RZ);
-      if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
-      A rr, rzn;
-      grid_sums<A>(P.partials, S_RR, S_RZ, 2, &rr, &rzn);
-      residual = sqrt((double)rr);
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+      const A rzn = (A)total(P.totals, S_RZ);
+      residual = sqrt(total(P.totals, S_RR));
       if (!isfinite(residual)) {
         status = AXIA_ERR_NONFINITE;
         break;
@@ -192,6 +121,162 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_kernel(PcgArgs<V> P) {
     P.out->residual = residual;
     P.out->bnorm = bnorm;
     P.out->status = status;
+    P.out->updates = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Reliable-update mixed precision: FP32 CG on K32 with FP64 residual
+// replacement (Sleijpen & van der Vorst's reliable updating, the scheme used
+// for mixed-precision CG in lattice-QCD solvers).
+// ---------------------------------------------------------------------------
+struct ReliableArgs {
+  int n;
+  const int* rowptr;
+  const int* col;
+  const float* val32;
+  const double* val64;
+  const float* dinv32;
+  const double* b;   // FP64 right-hand side
+  double* x;         // FP64 solution
+  double* r;         // FP64 residual (scratch)
+  float* x32;        // FP32 correction since the last update
+  float* r32;
+  float* p32;
+  float* q32;
+  double* partials;
+  double* totals;
+  GridBarrier* bar;
+  DevStatus* st;
+  PcgOut* out;
+  double tol;
+  double delta;      // update when the FP32 residual fell by this factor
+  long long max_iter;
+  unsigned long long limit_ns;
+};
+
+template <int L32, int L64>
+__global__ void __launch_bounds__(PCG_THREADS, 4) pcg_reliable_kernel(ReliableArgs P) {
+  const int n = P.n;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nth = gridDim.x * blockDim.x;
+  const int gwarp = tid >> 5, nwarps = nth >> 5;
+  const int lane = threadIdx.x & 31;
+  // x = 0, r32 = b, x32 = 0, p = z = r32 / diag
+  float rz_p = 0.f;
+  double bb_p = 0.0;
+  for (int i = tid; i < n; i += nth) {
+    const double bi = P.b[i];
+    P.x[i] = 0.0;
+    const float ri = (float)bi;
+    P.r32[i] = ri;
+    P.x32[i] = 0.f;
+    const float z = ri * P.dinv32[i];
+    P.p32[i] = z;
+    rz_p = fmaf(ri, z, rz_p);
+    bb_p = fma(bi, bi, bb_p);
+  }
+  block_partials<double>(bb_p, (double)rz_p, 2, P.partials, S_RR, S_RZ);
+  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+  float rz = (float)total(P.totals, S_RZ);
+  const double bnorm = sqrt(total(P.totals, S_RR));
+  double rmax = bnorm;       // residual norm at the last update
+  double residual = bnorm;   // FP64 residual norm at the last update
+  long long iters = 0;
+  int updates = 0, status = AXIA_OK;
+  bool converged = bnorm < 1e-30;
+  if (converged) residual = 0.0;
+  for (long long it = 0; !converged && it < P.max_iter; ++it) {
+    iters = it + 1;
+    float pq_p = 0.f;
+    {
+      constexpr int RPW = 32 / L32;
+      const int sl = lane % L32, grp = lane / L32;
+      for (int base = gwarp * RPW; base < n; base += nwarps * RPW) {
+        const int row = base + grp;
+        const float s = csr_row_dot<float, float, L32>(row, n, sl, P.rowptr, P.col, P.val32, P.p32);
+        if (row < n && sl == 0) {
+          P.q32[row] = s;
+          pq_p = fmaf(P.p32[row], s, pq_p);
+        }
+      }
+    }
+    block_partials<float>(pq_p, 0.f, 1, P.partials, S_PQ, S_PQ);
+    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1)) return;
+    const float pq = (float)total(P.totals, S_PQ);
+    if (!(fabsf(pq) >= 1e-30f) || !isfinite(pq)) {
+      status = isfinite(pq) ? AXIA_ERR_ZERO_PIVOT : AXIA_ERR_NONFINITE;
+      break;
+    }
+    const float alpha = rz / pq;
+    float rr_p = 0.f, rzn_p = 0.f;
+    for (int i = tid; i < n; i += nth) {
+      P.x32[i] = fmaf(alpha, P.p32[i], P.x32[i]);
+      const float ri = fmaf(-alpha, P.q32[i], P.r32[i]);
+      P.r32[i] = ri;
+      rr_p = fmaf(ri, ri, rr_p);
+      rzn_p = fmaf(ri, ri * P.dinv32[i], rzn_p);
+    }
+    block_partials<float>(rr_p, rzn_p, 2, P.partials, S_RR, S_RZ);
+    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+    float rzn = (float)total(P.totals, S_RZ);
+    const double rnorm32 = sqrt(total(P.totals, S_RR));
+    if (!isfinite(rnorm32)) {
+      status = AXIA_ERR_NONFINITE;
+      break;
+    }
+    if (rnorm32 <= P.delta * rmax || rnorm32 <= P.tol * bnorm) {
+      // reliable update: x += x32 (FP64), r = b - K x (FP64), r32 = r
+      for (int i = tid; i < n; i += nth) {
+        P.x[i] += (double)P.x32[i];
+        P.x32[i] = 0.f;
+      }
+      if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+      double rr64_p = 0.0;
+      float rz_new_p = 0.f;
+      {
+        constexpr int RPW = 32 / L64;
+        const int sl = lane % L64, grp = lane / L64;
+        for (int base = gwarp * RPW; base < n; base += nwarps * RPW) {
+          const int row = base + grp;
+          const double s = csr_row_dot<double, double, L64>(row, n, sl, P.rowptr, P.col, P.val64, P.x);
+          if (row < n && sl == 0) {
+            const double ri = P.b[row] - s;
+            P.r[row] = ri;
+            rr64_p = fma(ri, ri, rr64_p);
+            const float r32 = (float)ri;
+            P.r32[row] = r32;
+            rz_new_p = fmaf(r32, r32 * P.dinv32[row], rz_new_p);
+          }
+        }
+      }
+      block_partials<double>(rr64_p, (double)rz_new_p, 2, P.partials, S_RR, S_RZ);
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+      ++updates;
+      residual = sqrt(total(P.totals, S_RR));
+      rzn = (float)total(P.totals, S_RZ);
+      rmax = residual;
+      if (!isfinite(residual)) {
+        status = AXIA_ERR_NONFINITE;
+        break;
+      }
+      if (residual <= P.tol * bnorm) {
+        converged = true;
+        break;
+      }
+    }
+    const float beta = rzn / rz;
+    rz = rzn;
+    for (int i = tid; i < n; i += nth) P.p32[i] = fmaf(beta, P.p32[i], P.r32[i] * P.dinv32[i]);
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+  }
+  if (status == AXIA_OK && residual > P.tol * bnorm * 10.0) status = AXIA_ERR_NOT_CONVERGED;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.out->iters = iters;
+    P.out->residual = residual;
+    P.out->bnorm = bnorm;
+    P.out->status = status;
+    P.out->updates = updates;
   }
 }
 
@@ -210,12 +295,7 @@ residual_kernel(int n, const int* rowptr, const int* col, const double* val, con
   double rr = 0;
   for (int base = gwarp * RPW; base < n; base += nwarps * RPW) {
     const int row = base + grp;
-    double s = 0;
-    if (row < n) {
-      const int beg = __ldg(rowptr + row), end = __ldg(rowptr + row + 1);
-      for (int k = beg + sl; k < end; k += L) s = fma(ld_stream(val + k), x[ld_stream(col + k)], s);
-    }
-    s = group_sum<L>(s);
+    const double s = csr_row_dot<double, double, L>(row, n, sl, rowptr, col, val, x);
     if (row < n && sl == 0) {
       const double ri = b[row] - s;
       r[row] = ri;
@@ -227,7 +307,7 @@ residual_kernel(int n, const int* rowptr, const int* col, const double* val, con
 
 // y = K x, standalone (the matrix product of Csr::matvec, linalg.rs:41-50)
 template <typename V, int L>
-__global__ void __launch_bounds__(PCG_THREADS)
+__global__ void __launch_bounds__(PCG_THREADS, 4)
 spmv_kernel(int n, const int* rowptr, const int* col, const V* val, const V* x, V* y) {
   constexpr int RPW = 32 / L;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
@@ -235,12 +315,7 @@ spmv_kernel(int n, const int* rowptr, const int* col, const V* val, const V* x, 
   const int lane = threadIdx.x & 31, sl = lane % L, grp = lane / L;
   for (int base = gwarp * RPW; base < n; base += nwarps * RPW) {
     const int row = base + grp;
-    V s = 0;
-    if (row < n) {
-      const int beg = __ldg(rowptr + row), end = __ldg(rowptr + row + 1);
-      for (int k = beg + sl; k < end; k += L) s = fma(ld_stream(val + k), __ldg(x + ld_stream(col + k)), s);
-    }
-    s = group_sum<L>(s);
+    const V s = csr_row_dot<V, V, L>(row, n, sl, rowptr, col, val, x);
     if (row < n && sl == 0) y[row] = s;
   }
 }
@@ -260,6 +335,8 @@ static int launch_spmv_t(axia_ctx* ctx, const V* val, const V* x, V* y) {
 template <typename V>
 static int launch_spmv(axia_ctx* ctx, const V* val, const V* x, V* y, int lanes) {
   switch (lanes) {
+    case 1: return launch_spmv_t<V, 1>(ctx, val, x, y);
+    case 2: return launch_spmv_t<V, 2>(ctx, val, x, y);
     case 4: return launch_spmv_t<V, 4>(ctx, val, x, y);
     case 8: return launch_spmv_t<V, 8>(ctx, val, x, y);
     case 16: return launch_spmv_t<V, 16>(ctx, val, x, y);
@@ -307,13 +384,14 @@ static int pick_lanes(double avg_row, bool fp32) {
     if (avg_row <= 128) return 8;
     return 16;
   }
-  if (avg_row <= 48) return 4;
-  if (avg_row <= 160) return 4;
-  return 8;
+  if (avg_row <= 24) return 4;
+  if (avg_row <= 160) return 8;
+  return 16;
 }
 
 int pcg_lanes_for(const axia_ctx* ctx, bool fp32, int requested) {
-  if (requested == 4 || requested == 8 || requested == 16 || requested == 32) return requested;
+  if (requested == 1 || requested == 2 || requested == 4 || requested == 8 || requested == 16 || requested == 32)
+    return requested;
   double avg = ctx->n_free ? (double)ctx->nnz / (double)ctx->n_free : 1.0;
   return pick_lanes(avg, fp32);
 }
@@ -321,13 +399,8 @@ int pcg_lanes_for(const axia_ctx* ctx, bool fp32, int requested) {
 template <typename V, int L>
 static int launch_pcg_t(axia_ctx* ctx, PcgArgs<V>& P) {
   auto kern = pcg_kernel<V, L>;
-  int per_sm = 0;
-  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PCG_THREADS, 0));
-  if (per_sm < 1) return set_error(ctx, AXIA_ERR_CUDA, "PCG kernel does not fit on an SM");
-  int grid = per_sm * ctx->sm_count;
-  int need = (P.n + PCG_THREADS - 1) / PCG_THREADS;
-  grid = std::max(1, std::min(grid, std::max(need, ctx->sm_count)));
-  if ((size_t)grid * N_SLOTS > ctx->partial_slots) return set_error(ctx, AXIA_ERR_STATE, "partials buffer too small");
+  int grid = 0;
+  AXIA_TRY(coop_grid(ctx, (const void*)kern, P.n, &grid));
   void* params[] = {&P};
   AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params, 0, ctx->stream));
   ctx->launches++;
@@ -337,6 +410,8 @@ static int launch_pcg_t(axia_ctx* ctx, PcgArgs<V>& P) {
 template <typename V>
 int launch_pcg(axia_ctx* ctx, PcgArgs<V>& P, int lanes) {
   switch (lanes) {
+    case 1: return launch_pcg_t<V, 1>(ctx, P);
+    case 2: return launch_pcg_t<V, 2>(ctx, P);
     case 4: return launch_pcg_t<V, 4>(ctx, P);
     case 8: return launch_pcg_t<V, 8>(ctx, P);
     case 16: return launch_pcg_t<V, 16>(ctx, P);
@@ -344,25 +419,33 @@ int launch_pcg(axia_ctx* ctx, PcgArgs<V>& P, int lanes) {
   }
 }
 
-// one persistent PCG launch bracketed by CUDA events on the launching stream
-template <typename V>
-static int timed_pcg(axia_ctx* ctx, PcgArgs<V>& P, int lanes, axia_solve_info* info) {
-  cudaEvent_t a, b;
-  AXIA_CUDA(ctx, cudaEventCreate(&a));
-  AXIA_CUDA(ctx, cudaEventCreate(&b));
-  cudaEventRecord(a, ctx->stream);
-  int st = launch_pcg<V>(ctx, P, lanes);
-  cudaEventRecord(b, ctx->stream);
-  if (st == AXIA_OK) {
-    cudaEventSynchronize(b);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
-    info->ms_pcg_kernel += ms;
-    info->pcg_launches += 1;
+template <int L32, int L64>
+static int launch_reliable_t(axia_ctx* ctx, ReliableArgs& P) {
+  auto kern = pcg_reliable_kernel<L32, L64>;
+  int grid = 0;
+  AXIA_TRY(coop_grid(ctx, (const void*)kern, P.n, &grid));
+  void* params[] = {&P};
+  AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params, 0, ctx->stream));
+  ctx->launches++;
+  return AXIA_OK;
+}
+
+template <int L64>
+static int launch_reliable_l32(axia_ctx* ctx, ReliableArgs& P, int l32) {
+  switch (l32) {
+    case 4: return launch_reliable_t<4, L64>(ctx, P);
+    case 16: return launch_reliable_t<16, L64>(ctx, P);
+    case 32: return launch_reliable_t<32, L64>(ctx, P);
+    default: return launch_reliable_t<8, L64>(ctx, P);
   }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  return st;
+}
+
+static int launch_reliable(axia_ctx* ctx, ReliableArgs& P, int l32, int l64) {
+  switch (l64) {
+    case 2: return launch_reliable_l32<2>(ctx, P, l32);
+    case 8: return launch_reliable_l32<8>(ctx, P, l32);
+    default: return launch_reliable_l32<4>(ctx, P, l32);
+  }
 }
 
 static int ensure_solver_buffers(axia_ctx* ctx, bool mixed) {
@@ -385,25 +468,14 @@ static int ensure_solver_buffers(axia_ctx* ctx, bool mixed) {
   return AXIA_OK;
 }
 
-static int read_out(axia_ctx* ctx, PcgOut* o) {
-  AXIA_CUDA(ctx, cudaMemcpyAsync(o, ctx->d_out, sizeof(PcgOut), cudaMemcpyDeviceToHost, ctx->stream));
-  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  DevStatus hs;
-  AXIA_TRY(read_dev_status(ctx, &hs));
-  if (hs.timeout) return set_error(ctx, AXIA_ERR_TIMEOUT, "a grid barrier of the PCG kernel ran past its time limit");
-  return AXIA_OK;
-}
-
 static double residual_norm(axia_ctx* ctx, const double* b, const double* x, double* r) {
   const int n = (int)ctx->n_free;
   int grid = ctx->sm_count * 4;
   int lanes = pcg_lanes_for(ctx, false, 0);
   ctx->launches++;
   switch (lanes) {
-    case 4: residual_kernel<4><<<grid, PCG_THREADS, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val, b, x, r, ctx->d_partials); break;
     case 8: residual_kernel<8><<<grid, PCG_THREADS, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val, b, x, r, ctx->d_partials); break;
-    case 16: residual_kernel<16><<<grid, PCG_THREADS, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val, b, x, r, ctx->d_partials); break;
-    default: residual_kernel<32><<<grid, PCG_THREADS, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val, b, x, r, ctx->d_partials); break;
+    default: residual_kernel<4><<<grid, PCG_THREADS, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val, b, x, r, ctx->d_partials); break;
   }
   std::vector<double> h(grid);
   cudaMemcpyAsync(h.data(), ctx->d_partials, grid * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
@@ -427,28 +499,35 @@ int pcg_solve(axia_ctx* ctx, const axia_solve_opts* opts, axia_solve_info* info)
   PcgOut o{};
   if (!mixed) {
     PcgArgs<double> P{n, ctx->d_rowptr, ctx->d_col, ctx->d_val, ctx->d_dinv, ctx->d_b, ctx->d_x, ctx->d_r, ctx->d_p,
-                      ctx->d_q, ctx->d_partials, ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out, opts->rtol, max_iter,
-                      limit_ns};
-    AXIA_TRY(timed_pcg<double>(ctx, P, lanes, info));
+                      ctx->d_q, ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out,
+                      opts->rtol, max_iter, limit_ns};
+    AXIA_TRY(timed_launch(ctx, info, [&] { return launch_pcg<double>(ctx, P, lanes); }));
     AXIA_TRY(read_out(ctx, &o));
     info->iters = o.iters;
     info->outer_iters = 1;
     info->residual = o.residual;
     info->bnorm = o.bnorm;
-    if (o.status != AXIA_OK) {
-      if (o.status == AXIA_ERR_NOT_CONVERGED)
-        return set_error(ctx, o.status, "CG did not converge (residual " + std::to_string(o.residual) + " after " +
-                                            std::to_string(o.iters) + " iterations)");
-      if (o.status == AXIA_ERR_ZERO_PIVOT) return set_error(ctx, o.status, "CG: zero pivot, matrix not positive definite");
-      return set_error(ctx, o.status, "CG: non-finite iterate");
-    }
+    if (o.status != AXIA_OK) return status_error(ctx, o);
     return AXIA_OK;
   }
-  // mixed: FP64 iterative refinement around an FP32 PCG on K32
+  if (opts->refine_mode == AXIA_REFINE_RELIABLE) {
+    const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.1;
+    ReliableArgs P{n, ctx->d_rowptr, ctx->d_col, ctx->d_val32, ctx->d_val, ctx->d_dinv32, ctx->d_b, ctx->d_x,
+                   ctx->d_r, ctx->d_x32, ctx->d_r32, ctx->d_p32, ctx->d_q32, ctx->d_partials, ctx->d_totals,
+                   ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out, opts->rtol, delta, max_iter, limit_ns};
+    const int l64 = pcg_lanes_for(ctx, false, 0);
+    AXIA_TRY(timed_launch(ctx, info, [&] { return launch_reliable(ctx, P, lanes, l64); }));
+    AXIA_TRY(read_out(ctx, &o));
+    info->iters = o.iters;
+    info->outer_iters = o.updates;
+    info->residual = o.residual;
+    info->bnorm = o.bnorm;
+    if (o.status != AXIA_OK) return status_error(ctx, o);
+    return AXIA_OK;
+  }
+  // restart: FP64 iterative refinement around an FP32 PCG on K32
   const int tb = 256, gb = ctx->sm_count * 8;
   AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_x, 0, n * sizeof(double), ctx->stream));
-  AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_r, ctx->d_b, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  std::vector<double> hb(1);
   double bnorm = residual_norm(ctx, ctx->d_b, ctx->d_x, ctx->d_r);  // x = 0: r = b, ||b||
   info->bnorm = bnorm;
   info->iters = 0;
@@ -467,9 +546,9 @@ int pcg_solve(axia_ctx* ctx, const axia_solve_opts* opts, axia_solve_info* info)
     // inner tolerance: the requested reduction, but no tighter than needed to reach rtol
     double itol = std::max(inner, 0.5 * opts->rtol * bnorm / rnorm);
     PcgArgs<float> P{n, ctx->d_rowptr, ctx->d_col, ctx->d_val32, ctx->d_dinv32, ctx->d_b32, ctx->d_x32, ctx->d_r32,
-                     ctx->d_p32, ctx->d_q32, ctx->d_partials, ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out, itol,
-                     max_iter, limit_ns};
-    AXIA_TRY(timed_pcg<float>(ctx, P, lanes, info));
+                     ctx->d_p32, ctx->d_q32, ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status,
+                     (PcgOut*)ctx->d_out, itol, max_iter, limit_ns};
+    AXIA_TRY(timed_launch(ctx, info, [&] { return launch_pcg<float>(ctx, P, lanes); }));
     AXIA_TRY(read_out(ctx, &o));
     info->iters += o.iters;
     info->outer_iters = outer + 1;
@@ -515,6 +594,7 @@ int ensure_pcg_state(axia_ctx* ctx) {
     ctx->partial_slots = (size_t)N_SLOTS * 16 * 1024;
     AXIA_TRY(dev_alloc(ctx, &ctx->d_partials, ctx->partial_slots));
   }
+  if (!ctx->d_totals) AXIA_TRY(dev_alloc(ctx, &ctx->d_totals, 16));
   if (!ctx->d_bar) AXIA_TRY(dev_alloc(ctx, &ctx->d_bar, 1));
   if (!ctx->d_out) {
     PcgOut* o = nullptr;

@@ -1,0 +1,133 @@
+// solver.cuh -- pieces shared by the CSR (pcg.cu) and node-block (bsr.cu)
+// persistent Krylov kernels: block partial sums, the PCG result record and
+// the CSR argument pack.
+#pragma once
+
+#include "common.cuh"
+
+constexpr int PCG_THREADS = 512;
+int pcg_lanes_for(const axia_ctx* ctx, bool fp32, int requested);
+constexpr int S_PQ = 0, S_RR = 1, S_RZ = 2, N_SLOTS = 3;
+
+// result of one persistent solve, written by block 0
+struct PcgOut {
+  long long iters;
+  double residual;
+  double bnorm;
+  int status;
+  int updates;
+};
+
+template <typename V>
+struct PcgArgs {
+  int n;
+  const int* rowptr;
+  const int* col;
+  const V* val;
+  const V* dinv;
+  const V* b;
+  V* x;
+  V* r;
+  V* p;
+  V* q;
+  double* partials;  // [N_SLOTS][gridDim.x]
+  double* totals;    // [N_SLOTS]
+  GridBarrier* bar;
+  DevStatus* st;
+  PcgOut* out;
+  double tol;
+  long long max_iter;
+  unsigned long long limit_ns;
+};
+
+template <int L, typename T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-reduce up to two values and store them as this block's partials
+template <typename A>
+__device__ __forceinline__ void block_partials(A v0, A v1, int nv, double* partials, int slot0, int slot1) {
+  __shared__ A s_red[2][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  v0 = warp_sum(v0);
+  if (nv > 1) v1 = warp_sum(v1);
+  if (lane == 0) {
+    s_red[0][warp] = v0;
+    s_red[1][warp] = v1;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    A a0 = lane < nw ? s_red[0][lane] : A(0);
+    A a1 = lane < nw ? s_red[1][lane] : A(0);
+    a0 = warp_sum(a0);
+    if (nv > 1) a1 = warp_sum(a1);
+    if (lane == 0) {
+      partials[slot0 * gridDim.x + blockIdx.x] = (double)a0;
+      if (nv > 1) partials[slot1 * gridDim.x + blockIdx.x] = (double)a1;
+    }
+  }
+}
+
+__device__ __forceinline__ double total(const double* totals, int slot) { return __ldcg(totals + slot); }
+
+
+// ---------------------------------------------------------------------------
+// Host helpers for the persistent launches
+// ---------------------------------------------------------------------------
+inline int coop_grid(axia_ctx* ctx, const void* kern, int n, int* grid_out) {
+  int per_sm = 0;
+  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PCG_THREADS, 0));
+  if (per_sm < 1) return set_error(ctx, AXIA_ERR_CUDA, "PCG kernel does not fit on an SM");
+  int grid = per_sm * ctx->sm_count;
+  int need = (n + PCG_THREADS - 1) / PCG_THREADS;
+  grid = std::max(1, std::min(grid, std::max(need, ctx->sm_count)));
+  if ((size_t)grid * N_SLOTS > ctx->partial_slots) return set_error(ctx, AXIA_ERR_STATE, "partials buffer too small");
+  *grid_out = grid;
+  return AXIA_OK;
+}
+
+
+// one persistent launch bracketed by CUDA events on the launching stream
+template <typename F>
+inline int timed_launch(axia_ctx* ctx, axia_solve_info* info, F&& launch) {
+  cudaEvent_t a, b;
+  AXIA_CUDA(ctx, cudaEventCreate(&a));
+  AXIA_CUDA(ctx, cudaEventCreate(&b));
+  cudaEventRecord(a, ctx->stream);
+  int st = launch();
+  cudaEventRecord(b, ctx->stream);
+  if (st == AXIA_OK) {
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    info->ms_pcg_kernel += ms;
+    info->pcg_launches += 1;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return st;
+}
+
+
+inline int read_out(axia_ctx* ctx, PcgOut* o) {
+  AXIA_CUDA(ctx, cudaMemcpyAsync(o, ctx->d_out, sizeof(PcgOut), cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  DevStatus hs;
+  AXIA_TRY(read_dev_status(ctx, &hs));
+  if (hs.timeout) return set_error(ctx, AXIA_ERR_TIMEOUT, "a grid barrier of the PCG kernel ran past its time limit");
+  return AXIA_OK;
+}
+
+
+inline int status_error(axia_ctx* ctx, const PcgOut& o) {
+  if (o.status == AXIA_ERR_NOT_CONVERGED)
+    return set_error(ctx, o.status, "CG did not converge (residual " + std::to_string(o.residual) + " after " +
+                                        std::to_string(o.iters) + " iterations)");
+  if (o.status == AXIA_ERR_ZERO_PIVOT) return set_error(ctx, o.status, "CG: zero pivot, matrix not positive definite");
+  return set_error(ctx, o.status, "CG: non-finite iterate");
+}
+
+

@@ -113,6 +113,18 @@ def pcg_iter_bytes(nnz, n, vbytes):
     return (vbytes + 4) * nnz + 4 * (n + 1) + 2 * vbytes * n + 7 * vbytes * n + 4 * vbytes * n
 
 
+def bsr_spmv_bytes(nblocks, n_nodes, vbytes):
+    """Algorithmic bytes of y = K x in the node-block form: 9 values and one
+    int32 block column per block, int32 block-row pointers, x and y once."""
+    return (9 * vbytes + 4) * nblocks + 4 * (n_nodes + 1) + 2 * vbytes * 3 * n_nodes
+
+
+def bsr_pcg_iter_bytes(nblocks, n_nodes, vbytes):
+    """One CG iteration on the node-block form (full-DOF vectors)."""
+    nd = 3 * n_nodes
+    return (9 * vbytes + 4) * nblocks + 4 * (n_nodes + 1) + 2 * vbytes * nd + 11 * vbytes * nd
+
+
 def cpu_baseline(n=CPU_SAMPLE_N, threads=1):
     """The CPU restatement of the reference's *STATIC path (oracle/) on a
     bounded sample: the same block, loads and BCs at n^3, full path
@@ -166,7 +178,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lanes64", type=int, default=0)
     ap.add_argument("--lanes32", type=int, default=0)
-    ap.add_argument("--inner", type=float, default=1e-3)
+    ap.add_argument("--lanes32csr", type=int, default=0)
+    ap.add_argument("--delta", type=float, default=0.01, help="reliable-update residual reduction")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -206,7 +219,7 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    def timed(prec, u_dev, lanes):
+    def timed(asm_flags, solve_kw, u_dev):
         infos = []
         times = []
         for k in range(args.warmup + args.steps):
@@ -217,9 +230,8 @@ def main():
             b = torch.cuda.Event(enable_timing=True)
             with torch.cuda.stream(stream):
                 a.record(stream)
-                ctx.assemble(prec)
-                info = ctx.solve_device(f_dev.data_ptr(), u_dev.data_ptr(), rtol=RTOL, precision=prec,
-                                        inner_rtol=args.inner, spmv_lanes=lanes)
+                ctx.assemble_ex(asm_flags)
+                info = ctx.solve_device(f_dev.data_ptr(), u_dev.data_ptr(), rtol=RTOL, **solve_kw)
                 b.record(stream)
             b.synchronize()
             if k >= args.warmup:
@@ -234,33 +246,54 @@ def main():
             ms = float(t.item())
         return ms, infos, launches
 
+    fp64_kw = dict(precision=L.PREC_FP64, spmv_lanes=args.lanes64, matrix_format=L.FORMAT_CSR)
+    mixed_kw = dict(precision=L.PREC_MIXED, refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta,
+                    spmv_lanes=args.lanes32, matrix_format=L.FORMAT_BSR3)
+    mixed_csr_kw = dict(precision=L.PREC_MIXED, refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta,
+                        spmv_lanes=args.lanes32csr, matrix_format=L.FORMAT_CSR)
+    umc = torch.empty_like(f_dev)
     with ClockSampler(local) as clk:
-        ms64, inf64, la64 = timed(L.PREC_FP64, u64, args.lanes64)
-        msmx, infmx, lamx = timed(L.PREC_MIXED, umx, args.lanes32)
+        ms64, inf64, la64 = timed(L.ASM_CSR64, fp64_kw, u64)
+        msmx, infmx, lamx = timed(L.ASM_BSR64 | L.ASM_BSR32, mixed_kw, umx)
+        msmc, infmc, lamc = timed(L.ASM_CSR64 | L.ASM_CSR32, mixed_csr_kw, umc)
     clocks = clk.summary()
 
-    # standalone SpMV bandwidth (FP64 and FP32), x in HBM, y written
+    # standalone SpMV bandwidth: CSR FP64 / FP32 (K_ff, n_free vectors) and the
+    # node-block form FP64 / FP32 (full-DOF vectors)
+    nd = 3 * model.n_nodes
+    spmv = {}
     x64 = torch.rand(n, dtype=torch.float64, device=f"cuda:{local}")
     y64 = torch.empty_like(x64)
     x32 = x64.float()
     y32 = torch.empty_like(x32)
-    spmv = {}
-    for name, prec, x, y, vb, lanes in (("fp64", L.PREC_FP64, x64, y64, 8, args.lanes64),
-                                         ("fp32", L.PREC_MIXED, x32, y32, 4, args.lanes32)):
+    xf64 = torch.rand(nd, dtype=torch.float64, device=f"cuda:{local}")
+    yf64 = torch.empty_like(xf64)
+    xf32 = xf64.float()
+    yf32 = torch.empty_like(xf32)
+    nblocks = ctx.n_blocks()
+    cases = (("csr_fp64", ctx.spmv_device, L.PREC_FP64, x64, y64, spmv_bytes(nnz, n, 8), args.lanes64),
+             ("csr_fp32", ctx.spmv_device, L.PREC_MIXED, x32, y32, spmv_bytes(nnz, n, 4), args.lanes32csr),
+             ("bsr_fp64", ctx.bsr_spmv_device, L.PREC_FP64, xf64, yf64, bsr_spmv_bytes(nblocks, model.n_nodes, 8), 0),
+             ("bsr_fp32", ctx.bsr_spmv_device, L.PREC_MIXED, xf32, yf32, bsr_spmv_bytes(nblocks, model.n_nodes, 4),
+              args.lanes32))
+    for name, fn, prec, x, y, nbytes, lanes in cases:
+        if name.startswith("csr"):
+            ctx.assemble_ex(L.ASM_CSR64 | L.ASM_CSR32)
+        else:
+            ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
         with torch.cuda.stream(stream):
             for _ in range(3):
-                ctx.spmv_device(prec, x.data_ptr(), y.data_ptr(), lanes)
+                fn(prec, x.data_ptr(), y.data_ptr(), lanes)
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             reps = 20
             a.record(stream)
             for _ in range(reps):
-                ctx.spmv_device(prec, x.data_ptr(), y.data_ptr(), lanes)
+                fn(prec, x.data_ptr(), y.data_ptr(), lanes)
             b.record(stream)
         b.synchronize()
         ms = a.elapsed_time(b) / reps
-        gbs = spmv_bytes(nnz, n, vb) / (ms * 1e-3) / 1e9
-        spmv[name] = {"ms": ms, "gbs": gbs}
+        spmv[name] = {"ms": ms, "gbs": nbytes / (ms * 1e-3) / 1e9, "bytes": nbytes}
 
     pk, pk_kind = peaks()
     hbm = pk["hbm_gbs"]
@@ -269,23 +302,28 @@ def main():
 
     # accuracy: mixed vs FP64 solution, both with true FP64 residual <= 1e-10 ||b||
     u64h = u64.cpu().numpy()
-    umxh = umx.cpu().numpy()
-    rel_mx = float(np.linalg.norm(umxh - u64h) / np.linalg.norm(u64h))
+    rel_mx = float(np.linalg.norm(umx.cpu().numpy() - u64h) / np.linalg.norm(u64h))
+    rel_mc = float(np.linalg.norm(umc.cpu().numpy() - u64h) / np.linalg.norm(u64h))
 
-    last64, lastmx = inf64[-1], infmx[-1]
+    last64, lastmx, lastmc = inf64[-1], infmx[-1], infmc[-1]
     mdofs = n / (msmx * 1e-3) / 1e6 * world
     mdofs64 = n / (ms64 * 1e-3) / 1e6 * world
+    mdofsmc = n / (msmc * 1e-3) / 1e6 * world
 
-    # roofline of the dominant kernel: the persistent FP32 PCG kernel of the mixed step
+    # roofline of the dominant kernel: the persistent FP32 node-block PCG of the mixed step
     it32 = statistics.mean(i["iters"] for i in infmx)
     k32_ms = statistics.mean(i["ms_pcg_kernel"] for i in infmx)
-    launches32 = statistics.mean(i["pcg_launches"] for i in infmx)
-    bytes32 = pcg_iter_bytes(nnz, n, 4) * it32 / launches32
-    ach32 = bytes32 / (k32_ms / launches32 * 1e-3) / 1e9
+    upd = statistics.mean(i["outer_iters"] for i in infmx)
+    bytes32 = bsr_pcg_iter_bytes(nblocks, model.n_nodes, 4) * it32 + bsr_spmv_bytes(nblocks, model.n_nodes, 8) * upd
+    ach32 = bytes32 / (k32_ms * 1e-3) / 1e9
     it64 = statistics.mean(i["iters"] for i in inf64)
     k64_ms = statistics.mean(i["ms_pcg_kernel"] for i in inf64)
     bytes64 = pcg_iter_bytes(nnz, n, 8) * it64
     ach64 = bytes64 / (k64_ms * 1e-3) / 1e9
+    itmc = statistics.mean(i["iters"] for i in infmc)
+    kmc_ms = statistics.mean(i["ms_pcg_kernel"] for i in infmc)
+    bytesmc = pcg_iter_bytes(nnz, n, 4) * itmc
+    achmc = bytesmc / (kmc_ms * 1e-3) / 1e9
 
     e2e = None
     if not args.no_e2e:
@@ -294,14 +332,14 @@ def main():
                model.bc_dof.nbytes + model.bc_val.nbytes + f_host.nbytes)
         d2h = f_host.nbytes
         ctx.set_stream(None)
+        mixed_kw["spmv_lanes"] = args.lanes32
         ts = []
         for k in range(args.warmup + args.steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             ctx.setup(model)
-            ctx.assemble(L.PREC_MIXED)
-            u, info = ctx.solve(f_host, rtol=RTOL, precision=L.PREC_MIXED, inner_rtol=args.inner,
-                                spmv_lanes=args.lanes32)
+            ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+            u, info = ctx.solve(f_host, rtol=RTOL, **mixed_kw)
             dt = time.perf_counter() - t0
             if k >= args.warmup:
                 ts.append(dt)
@@ -331,24 +369,32 @@ def main():
                                f"interior nodes perturbed +-0.15h", "n_free": n, "nnz_kff": nnz,
                    "rtol": RTOL, "step": "assemble + solve (symbolic setup once)",
                    "l2": "inputs (2.9 GB matrix) larger than L2, no flush", "parallelism": f"replicas x{world}"},
-        "fp64": {"value": mdofs64, "ms_per_step": ms64, "iters": last64["iters"],
+        "fp64": {"value": mdofs64, "ms_per_step": ms64, "iters": last64["iters"], "format": "CSR int32",
                  "ms_assemble": last64["ms_assemble"], "ms_solve": last64["ms_solve"],
                  "true_rel_residual": last64["true_residual"] / last64["bnorm"]},
         "mixed": {"value": mdofs, "ms_per_step": msmx, "inner_iters": lastmx["iters"],
-                  "outer_iters": lastmx["outer_iters"], "ms_assemble": lastmx["ms_assemble"],
-                  "ms_solve": lastmx["ms_solve"], "true_rel_residual": lastmx["true_residual"] / lastmx["bnorm"],
-                  "rel_err_vs_fp64": rel_mx},
+                  "reliable_updates": lastmx["outer_iters"], "format": "3x3 node blocks, int32 block columns",
+                  "ms_assemble": lastmx["ms_assemble"], "ms_solve": lastmx["ms_solve"],
+                  "true_rel_residual": lastmx["true_residual"] / lastmx["bnorm"], "rel_err_vs_fp64": rel_mx},
+        "mixed_csr": {"value": mdofsmc, "ms_per_step": msmc, "inner_iters": lastmc["iters"],
+                      "reliable_updates": lastmc["outer_iters"], "format": "CSR int32",
+                      "ms_assemble": lastmc["ms_assemble"], "ms_solve": lastmc["ms_solve"],
+                      "true_rel_residual": lastmc["true_residual"] / lastmc["bnorm"], "rel_err_vs_fp64": rel_mc},
         "speedup_mixed_vs_fp64": ms64 / msmx,
         "speedup_mixed_vs_fp64_solve": last64["ms_solve"] / lastmx["ms_solve"],
+        "speedup_mixed_csr_vs_fp64": ms64 / msmc,
         "setup_ms": setup_s * 1e3,
         "spmv": spmv,
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
-                     "traffic": None, "kernel": "pcg_kernel<float> (FP32 inner PCG, persistent)",
-                     "peak_source": f"{pk_kind} hbm_gbs", "bytes_per_launch": bytes32,
-                     "ms_per_launch": k32_ms / launches32},
+                     "traffic": None, "kernel": "pcg_bsr_reliable_kernel (FP32 node-block CG + FP64 updates)",
+                     "peak_source": f"{pk_kind} hbm_gbs", "bytes_per_launch": bytes32, "ms_per_launch": k32_ms},
         "roofline_fp64_pcg": {"bound": "hbm", "achieved": ach64, "peak": hbm, "unit": "GB/s", "frac": ach64 / hbm,
-                              "ms_per_launch": k64_ms, "bytes_per_launch": bytes64},
-        "gpu_launches": int(la64 + lamx),
+                              "kernel": "pcg_kernel<double> (CSR)", "ms_per_launch": k64_ms,
+                              "bytes_per_launch": bytes64},
+        "roofline_mixed_csr_pcg": {"bound": "hbm", "achieved": achmc, "peak": hbm, "unit": "GB/s",
+                                   "frac": achmc / hbm, "kernel": "pcg_reliable_kernel (CSR FP32 + FP64 updates)",
+                                   "ms_per_launch": kmc_ms, "bytes_per_launch": bytesmc},
+        "gpu_launches": int(la64 + lamx + lamc),
         "clocks": clocks,
         "e2e": e2e,
         "cpu_baseline": cpu,

@@ -63,6 +63,19 @@ typedef enum axia_precision {
   AXIA_PREC_MIXED = 1   /* K in FP32 CSR for an FP32 inner PCG, FP64 residual and update */
 } axia_precision;
 
+/* Matrix forms axia_gpu_assemble_ex can build (bit flags). */
+typedef enum axia_assemble_flags {
+  AXIA_ASM_CSR64 = 1,   /* K_ff in CSR, FP64 values (the reference's Csr, linalg.rs:3-8) */
+  AXIA_ASM_CSR32 = 2,   /* FP32 copy of the CSR values */
+  AXIA_ASM_BSR64 = 4,   /* full-DOF node-block (3x3) form, FP64 */
+  AXIA_ASM_BSR32 = 8    /* full-DOF node-block (3x3) form, FP32 */
+} axia_assemble_flags;
+
+typedef enum axia_matrix_format {
+  AXIA_FORMAT_CSR = 0,  /* solve on K_ff in CSR */
+  AXIA_FORMAT_BSR3 = 1  /* solve on the node-block form (prescribed DOFs as unit rows) */
+} axia_matrix_format;
+
 typedef enum axia_refine_mode {
   AXIA_REFINE_RESTART = 0,   /* classic iterative refinement: each inner solve restarts from 0 */
   AXIA_REFINE_RELIABLE = 1   /* one FP32 Krylov sequence, FP64 residual replaced at each update */
@@ -89,7 +102,9 @@ typedef struct axia_solve_opts {
   int32_t refine_mode;     /* axia_refine_mode (mixed only) */
   double inner_rtol;       /* mixed: residual reduction per refinement step (e.g. 1e-3) */
   int32_t max_outer;       /* mixed: refinement steps allowed */
-  int32_t spmv_lanes;      /* lanes per CSR row in the SpMV: 0 = automatic, else 4, 8, 16 or 32 */
+  int32_t spmv_lanes;      /* lanes per row in the SpMV: 0 = automatic, else 1..32 (power of two) */
+  int32_t matrix_format;   /* axia_matrix_format */
+  int32_t reserved;
 } axia_solve_opts;
 
 typedef struct axia_solve_info {
@@ -154,6 +169,10 @@ AXIA_API int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_
  * precision AXIA_PREC_MIXED also stores an FP32 copy of K_ff. */
 AXIA_API int32_t axia_gpu_assemble(axia_ctx* ctx, int32_t precision);
 
+/* As axia_gpu_assemble with an explicit set of matrix forms (axia_assemble_flags).
+ * K_fp u0 and the CSR diagonal are always built. */
+AXIA_API int32_t axia_gpu_assemble_ex(axia_ctx* ctx, int32_t flags);
+
 /* Static solve: rhs = f_free - K_fp u0, PCG on K_ff, u_full = u0 + T x
  * (reconstruct).  f_full[3*n_nodes] in, u_full[3*n_nodes] out (host). */
 AXIA_API int32_t axia_gpu_solve(axia_ctx* ctx, const double* f_full, double* u_full,
@@ -178,6 +197,34 @@ AXIA_API int64_t axia_gpu_kernel_launches(const axia_ctx* ctx);
  * product of Csr::matvec (solver/src/linalg.rs:41-50). */
 AXIA_API int32_t axia_gpu_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev,
                                       int32_t lanes);
+
+/* y = K x on the full-DOF node-block form (x, y of 3*n_nodes entries,
+ * double for AXIA_PREC_FP64, float for AXIA_PREC_MIXED). */
+AXIA_API int32_t axia_gpu_bsr_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev,
+                                          int32_t lanes);
+
+/* Number of 3x3 node blocks of the node-block form (node adjacency entries). */
+AXIA_API int64_t axia_gpu_node_blocks(const axia_ctx* ctx);
+
+/* Bilinear element form s_e = u_e^T K_e(E=1) v_e for every element of the
+ * mesh of the last setup (u_full, v_full: 3*n_nodes; s: n_elem).  With
+ * u = v it is twice the unit-modulus strain energy of each element.
+ * No reference counterpart (the reference has no sensitivity code). */
+AXIA_API int32_t axia_gpu_element_energy(axia_ctx* ctx, const double* u_full, const double* v_full, double* s);
+
+/* Forward half of the SIMP compliance pair (no reference counterpart):
+ * E_e = e0 rho_e^penal on the device, assemble (CSR or node-block by
+ * opts->matrix_format and opts->precision), solve K u = f, return u_full and
+ * compliance C = f . u.  Keeps rho and u on the device for the backward call.
+ * Prescribed displacements must be zero (compliance of a loaded structure). */
+AXIA_API int32_t axia_gpu_compliance_forward(axia_ctx* ctx, const double* rho, double penal, double e0,
+                                             const double* f_full, double* u_full, double* compliance,
+                                             const axia_solve_opts* opts, axia_solve_info* info);
+
+/* Backward half: grad[e] = dC/drho_e = -penal rho_e^(penal-1) e0 u_e^T K_e(1) u_e
+ * for all elements, from the state of the last forward call (the adjoint of
+ * the self-adjoint compliance problem is -u, so no second solve is needed). */
+AXIA_API int32_t axia_gpu_compliance_backward(axia_ctx* ctx, double* grad);
 
 /* Sizes of the assembled system: n_free and nnz. */
 AXIA_API int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz);

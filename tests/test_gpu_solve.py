@@ -70,10 +70,17 @@ def test_fp64_and_mixed_vs_direct(gpu_ctx, name, model):
     assert _rel(r64.u, u_ref) < 1e-8, name
     o = O.solve_static(model, solver=O.SOLVER_PCG, tol=1e-10)
     assert abs(r64.iters - o.iters) <= max(3, 0.02 * o.iters), (r64.iters, o.iters)
-    rmx = solve_linear(model, backend=SparseBackend.GpuMixed, rtol=1e-10, ctx=gpu_ctx)
-    assert _rel(rmx.u, u_ref) < 1e-8, name
-    assert rmx.info["outer_iters"] >= 1
-    assert rmx.info["true_residual"] <= 2e-10 * rmx.info["bnorm"]
+    for mode, fmt in ((_lib.REFINE_RESTART, _lib.FORMAT_CSR), (_lib.REFINE_RELIABLE, _lib.FORMAT_CSR),
+                      (_lib.REFINE_RELIABLE, _lib.FORMAT_BSR3)):
+        rmx = solve_linear(model, backend=SparseBackend.GpuMixed, rtol=1e-10, ctx=gpu_ctx, refine_mode=mode,
+                           matrix_format=fmt)
+        assert _rel(rmx.u, u_ref) < 1e-8, (name, mode, fmt)
+        assert rmx.info["outer_iters"] >= 1
+        assert rmx.info["true_residual"] <= 2e-10 * rmx.info["bnorm"], (name, mode, fmt)
+    # FP64 PCG on the node-block form: same recurrence as on K_ff in CSR
+    rb = solve_linear(model, backend=SparseBackend.Gpu, rtol=1e-10, ctx=gpu_ctx, matrix_format=_lib.FORMAT_BSR3)
+    assert _rel(rb.u, u_ref) < 1e-8, name
+    assert abs(rb.iters - r64.iters) <= max(2, 0.01 * r64.iters), (rb.iters, r64.iters)
 
 
 def test_solve_is_bitwise_deterministic(gpu_ctx):
@@ -136,6 +143,17 @@ def test_larger_block_properties(gpu_ctx, n):
     umx, imx = gpu_ctx.solve(f, rtol=1e-10, precision=_lib.PREC_MIXED)
     assert imx.true_residual <= 1e-10 * imx.bnorm * 1.0001
     assert _rel(umx, u64) < 1e-8
+    umr, imr = gpu_ctx.solve(f, rtol=1e-10, precision=_lib.PREC_MIXED, refine_mode=_lib.REFINE_RELIABLE,
+                             inner_rtol=0.1)
+    assert imr.true_residual <= 1e-10 * imr.bnorm * 1.0001
+    assert _rel(umr, u64) < 1e-8
+    # one FP32 Krylov sequence needs about as many iterations as FP64 PCG
+    assert imr.iters <= 1.3 * i64.iters
+    gpu_ctx.assemble_ex(_lib.ASM_CSR64 | _lib.ASM_CSR32 | _lib.ASM_BSR64 | _lib.ASM_BSR32)
+    umb, imb = gpu_ctx.solve(f, rtol=1e-10, precision=_lib.PREC_MIXED, refine_mode=_lib.REFINE_RELIABLE,
+                             inner_rtol=0.1, matrix_format=_lib.FORMAT_BSR3)
+    assert imb.true_residual <= 1e-10 * imb.bnorm * 1.0001
+    assert _rel(umb, u64) < 1e-8
     rng = np.random.default_rng(4)
     free = np.nonzero(m.free_mask())[0]
     f1 = np.zeros(m.ndof)
