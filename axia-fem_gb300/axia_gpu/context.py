@@ -170,6 +170,28 @@ class GpuContext:
         self._check(self.lib.axia_gpu_compliance_backward(self.h, L.ptr(g)), "compliance_backward")
         return g
 
+    def solve_batched(self, F, **kw):
+        """Solve many load cases (F: (nrhs, ndof)) -> U (nrhs, ndof), info, per-case relative residuals."""
+        Fm = _c(np.atleast_2d(F), np.float64)
+        nrhs = Fm.shape[0]
+        U = np.zeros_like(Fm)
+        rel = np.zeros(nrhs)
+        kw.setdefault("inner_rtol", 0.01)
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        self._check(self.lib.axia_gpu_solve_batched(self.h, nrhs, L.ptr(Fm), L.ptr(U), C.byref(o), C.byref(info),
+                                                    L.ptr(rel)), "solve_batched")
+        return U, info, rel
+
+    def solve_batched_device(self, nrhs, F_dev_ptr, U_dev_ptr, rel=None, **kw):
+        kw.setdefault("inner_rtol", 0.01)
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        rel = np.zeros(nrhs) if rel is None else rel
+        self._check(self.lib.axia_gpu_solve_batched_device(self.h, nrhs, C.c_void_p(F_dev_ptr), C.c_void_p(U_dev_ptr),
+                                                           C.byref(o), C.byref(info), L.ptr(rel)), "solve_batched")
+        return info, rel
+
     def export_system(self):
         """K_ff as (rowptr, col, val), the Jacobi diagonal and K_fp u0."""
         rp = np.zeros(self.n_free + 1, np.int32)

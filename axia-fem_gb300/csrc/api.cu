@@ -14,6 +14,8 @@ int element_energy(axia_ctx* ctx, const double* d_u, const double* d_v, double* 
 int simp_modulus(axia_ctx* ctx, const double* d_rho, double pexp, double e0);
 int simp_gradient(axia_ctx* ctx, const double* d_rho, const double* d_s, double pexp, double e0, double* d_g);
 int device_dot(axia_ctx* ctx, const double* a, const double* b, int64_t n, double* out);
+int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const axia_solve_opts* opts,
+                axia_solve_info* info, double* rel_res);
 int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args);
 struct PcgOut;
 int pcg_solve(axia_ctx* ctx, const axia_solve_opts* opts, axia_solve_info* info);
@@ -96,6 +98,15 @@ void free_mesh_state(axia_ctx* ctx) {
   dev_free(ctx->d_pf32);
   dev_free(ctx->d_qf32);
   ctx->full_capacity = 0;
+  dev_free(ctx->d_mB);
+  dev_free(ctx->d_mX);
+  dev_free(ctx->d_mX32);
+  dev_free(ctx->d_mR32);
+  dev_free(ctx->d_mP32);
+  dev_free(ctx->d_mQ32);
+  if (ctx->d_mout) cudaFree(ctx->d_mout);
+  ctx->d_mout = nullptr;
+  ctx->batch_capacity = 0;
   dev_free(ctx->d_rho);
   dev_free(ctx->d_energy);
   dev_free(ctx->d_grad);
@@ -458,6 +469,58 @@ int32_t axia_gpu_compliance_backward(axia_ctx* ctx, double* grad) {
   AXIA_CUDA(ctx, cudaMemcpyAsync(grad, ctx->d_grad, ctx->n_elem * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return AXIA_OK;
+}
+
+static int32_t batched_common(axia_ctx* ctx, int32_t nrhs, const double* d_F, double* d_U,
+                              const axia_solve_opts* opts, axia_solve_info* info, double* rel_res) {
+  axia_solve_info local{};
+  if (!info) info = &local;
+  std::memset(info, 0, sizeof(*info));
+  info->bad_index = -1;
+  axia_solve_opts o{};
+  if (opts) o = *opts;
+  if (!(o.rtol > 0.0)) o.rtol = 1e-8;
+  EventTimer t(ctx->stream);
+  int st = batch_solve(ctx, nrhs, d_F, d_U, &o, info, rel_res);
+  info->ms_solve = t.stop_ms();
+  fill_info_sizes(ctx, info);
+  info->status = st;
+  return st;
+}
+
+int32_t axia_gpu_solve_batched_device(axia_ctx* ctx, int32_t nrhs, const double* F_dev, double* U_dev,
+                                      const axia_solve_opts* opts, axia_solve_info* info, double* rel_res) {
+  if (!ctx || nrhs < 0 || (nrhs > 0 && (!F_dev || !U_dev))) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "batched solve before assemble");
+  if (nrhs == 0) return AXIA_OK;
+  return batched_common(ctx, nrhs, F_dev, U_dev, opts, info, rel_res);
+}
+
+int32_t axia_gpu_solve_batched(axia_ctx* ctx, int32_t nrhs, const double* F, double* U, const axia_solve_opts* opts,
+                               axia_solve_info* info, double* rel_res) {
+  if (!ctx || nrhs < 0 || (nrhs > 0 && (!F || !U))) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "batched solve before assemble");
+  if (nrhs == 0) return AXIA_OK;
+  const size_t count = (size_t)nrhs * (size_t)ctx->ndof;
+  for (size_t i = 0; i < count; ++i)
+    if (!std::isfinite(F[i])) return set_error(ctx, AXIA_ERR_NONFINITE, "load case entry not finite");
+  double *dF = nullptr, *dU = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &dF, count));
+  int st = dev_alloc(ctx, &dU, count);
+  if (st == AXIA_OK) {
+    cudaMemcpyAsync(dF, F, count * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    st = batched_common(ctx, nrhs, dF, dU, opts, info, rel_res);
+  }
+  if (st == AXIA_OK) {
+    if (cudaMemcpyAsync(U, dU, count * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      st = set_error(ctx, AXIA_ERR_CUDA, "copy of batched solutions");
+  }
+  dev_free(dF);
+  dev_free(dU);
+  return st;
 }
 
 int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz) {

@@ -1,0 +1,510 @@
+// batch.cu -- many load cases on one mesh in one persistent launch.
+//
+// 32 right-hand sides share every sweep over the node-block matrix: the
+// vectors are stored [nd][32] (the 32 load cases of a DOF contiguous), a warp
+// owns one block row, its four 8-lane groups walk the row's blocks, and each
+// lane applies the 3x3 block to 4 load cases with 16-byte vector loads, so a
+// block's 9 values are read once for 32 products.  Every column runs its own
+// Jacobi-PCG recurrence (solver/src/linalg.rs:199-259: its own alpha, beta,
+// convergence test) on the FP32 node-block matrix, with FP64 reliable updates
+// (x += x32, r = b - K x in FP64 for all columns) when every active column's
+// FP32 residual has dropped by delta, or one has reached the tolerance.
+// A converged column is frozen (alpha = beta = 0).
+#include <algorithm>
+#include <cmath>
+
+#include "solver.cuh"
+
+namespace {
+
+constexpr int NR = 32;   // load cases per column block
+constexpr int CPL = 4;   // load cases per lane
+constexpr int LPG = 8;   // lanes per group (LPG * CPL = NR)
+
+template <typename V>
+struct BsrMatM {
+  int n_nodes;
+  const int* adj_ptr;
+  const int* adj;
+  const V* val;  // [9][nb]
+  long long nb;
+};
+
+__device__ __forceinline__ void ld4(const float* p, float v[4]) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double v[4]) {
+  const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+  v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, const float v[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double v[4]) {
+  *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+  *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+}
+
+// Y[3a+i][4cl..4cl+3] for block row a; valid in the lanes of group 0 after the call.
+template <typename V>
+__device__ __forceinline__ void bsr_row_multi(int a, int lane, const BsrMatM<V>& M, const V* X, V y[3][CPL]) {
+  const int cl = lane % LPG, grp = lane / LPG;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) y[i][c] = V(0);
+  const int beg = __ldg(M.adj_ptr + a), end = __ldg(M.adj_ptr + a + 1);
+  for (int s = beg + grp; s < end; s += 32 / LPG) {
+    const int b = ld_stream(M.adj + s);
+    V v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = ld_stream(M.val + (long long)k * M.nb + s);
+    V x[3][CPL];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ld4(X + (size_t)(3 * b + j) * NR + CPL * cl, x[j]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int c = 0; c < CPL; ++c)
+        y[i][c] = fma(v[3 * i], x[0][c], fma(v[3 * i + 1], x[1][c], fma(v[3 * i + 2], x[2][c], y[i][c])));
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 8);
+      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 16);
+    }
+}
+
+// Per-column partial sums of this block: v[c] is this thread's contribution
+// to column 4*(tid%8)+c.  Written to partials[(slot0 + col) * G + block].
+template <typename A>
+__device__ __forceinline__ void block_partials_cols(const A v[CPL], double* partials, int slot0) {
+  __shared__ double s_cols[32][NR];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  double t[CPL];
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) {
+    t[c] = (double)v[c];
+    t[c] += __shfl_xor_sync(0xffffffffu, t[c], 8);
+    t[c] += __shfl_xor_sync(0xffffffffu, t[c], 16);
+  }
+  if (lane < LPG) {
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) s_cols[warp][CPL * lane + c] = t[c];
+  }
+  __syncthreads();
+  if (threadIdx.x < NR) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += s_cols[w][threadIdx.x];
+    partials[(size_t)(slot0 + threadIdx.x) * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+// Reduce-and-sync over nv partial slots; the last block to arrive sums them
+// (one warp per slot, ascending block order) and publishes totals[slot0..].
+__device__ __forceinline__ bool grid_reduce_sync_wide(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns,
+                                                      const double* partials, double* totals, int slot0, int nv) {
+  __shared__ int s_last, s_ok;
+  __shared__ unsigned s_gen;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_gen = ld_acquire_gpu(&bar->gen);
+    __threadfence();
+    s_last = atomicAdd(&bar->count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  int ok = 1;
+  if (s_last) {
+    __threadfence();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int k = warp; k < nv; k += nw) {
+      double a = 0.0;
+      for (int j = lane; j < (int)gridDim.x; j += 32) a += __ldcg(partials + (size_t)(slot0 + k) * gridDim.x + j);
+      a = warp_sum(a);
+      if (lane == 0) totals[slot0 + k] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bar->count = 0;
+      __threadfence();
+      st_release_gpu(&bar->gen, s_gen + 1);
+    }
+  } else if (threadIdx.x == 0) {
+    unsigned long long t0 = global_ns();
+    unsigned spins = 0;
+    while (ld_acquire_gpu(&bar->gen) == s_gen) {
+      if ((++spins & 63u) == 0 && global_ns() - t0 > limit_ns) {
+        atomicExch(&st->timeout, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (*(volatile int*)&st->timeout) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+struct MultiOut {
+  long long iters;
+  int updates;
+  int status;
+  double bnorm[NR];
+  double residual[NR];
+  long long col_iters[NR];
+};
+
+struct MultiArgs {
+  BsrMatM<float> M32;
+  BsrMatM<double> M64;
+  int nd;
+  const float* dinv32;  // [nd]
+  const double* B;      // [nd][NR]
+  double* X;            // [nd][NR]
+  float* X32;
+  float* R32;
+  float* P32;
+  float* Q32;
+  double* partials;     // [>= 2 NR][G]
+  double* totals;       // [>= 2 NR]
+  GridBarrier* bar;
+  DevStatus* st;
+  MultiOut* out;
+  double tol;
+  double delta;
+  long long max_iter;
+  unsigned long long limit_ns;
+};
+
+constexpr int SL_A = 0, SL_B = NR;  // two banks of NR slots
+
+__global__ void __launch_bounds__(PCG_THREADS, 1) pcg_bsr_multi_kernel(MultiArgs P) {
+  __shared__ double s_rz[NR], s_bnorm[NR], s_rmax[NR], s_res[NR];
+  __shared__ float s_alpha[NR], s_beta[NR];
+  __shared__ int s_active[NR], s_flag;
+  __shared__ long long s_citers[NR];
+  const int nd = P.nd, n_nodes = P.M32.n_nodes;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const int gwarp = tid >> 5, nwarps = nth >> 5;
+  const int cq = tid % LPG;            // this thread's column quad in the vector phases
+  const long long nq = (long long)nd * LPG;  // float4 chunks of an [nd][NR] vector
+  // init: x = 0, r32 = b, p = z = r32 / diag, per-column r.z and b.b
+  {
+    float rz_p[CPL] = {0, 0, 0, 0};
+    double bb_p[CPL] = {0, 0, 0, 0};
+    for (long long q = tid; q < nq; q += nth) {
+      const long long row = q / LPG;
+      double bv[CPL];
+      ld4(P.B + q * CPL, bv);
+      const float di = P.dinv32[row];
+      float r[CPL], z[CPL];
+      const double zero4[CPL] = {0, 0, 0, 0};
+      const float fz4[CPL] = {0, 0, 0, 0};
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        r[c] = (float)bv[c];
+        z[c] = r[c] * di;
+        rz_p[c] = fmaf(r[c], z[c], rz_p[c]);
+        bb_p[c] = fma(bv[c], bv[c], bb_p[c]);
+      }
+      st4(P.X + q * CPL, zero4);
+      st4(P.X32 + q * CPL, fz4);
+      st4(P.R32 + q * CPL, r);
+      st4(P.P32 + q * CPL, z);
+    }
+    block_partials_cols<double>(bb_p, P.partials, SL_A);
+    __syncthreads();
+    block_partials_cols<float>(rz_p, P.partials, SL_B);
+  }
+  if (!grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, 0, 2 * NR)) return;
+  if (threadIdx.x < NR) {
+    const int c = threadIdx.x;
+    s_bnorm[c] = sqrt(__ldcg(P.totals + SL_A + c));
+    s_rz[c] = __ldcg(P.totals + SL_B + c);
+    s_rmax[c] = s_bnorm[c];
+    s_res[c] = s_bnorm[c];
+    s_active[c] = s_bnorm[c] >= 1e-30;
+    s_citers[c] = 0;
+    if (!s_active[c]) s_res[c] = 0.0;
+  }
+  __syncthreads();
+  long long iters = 0;
+  int updates = 0, status = AXIA_OK;
+  for (long long it = 0; it < P.max_iter; ++it) {
+    int any = 0;
+    for (int c = 0; c < NR; ++c) any |= s_active[c];
+    if (!any) break;
+    iters = it + 1;
+    // Q = K P (FP32) and per-column p.q
+    float pq_p[CPL] = {0, 0, 0, 0};
+    for (int a = gwarp; a < n_nodes; a += nwarps) {
+      float y[3][CPL];
+      bsr_row_multi<float>(a, lane, P.M32, P.P32, y);
+      if (lane < LPG) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const size_t off = (size_t)(3 * a + i) * NR + CPL * lane;
+          st4(P.Q32 + off, y[i]);
+          float p[CPL];
+          ld4(P.P32 + off, p);
+#pragma unroll
+          for (int c = 0; c < CPL; ++c) pq_p[c] = fmaf(p[c], y[i][c], pq_p[c]);
+        }
+      }
+    }
+    // lanes 0..7 hold column quads 0..7 of their warp: same mapping as tid % 8
+    block_partials_cols<float>(pq_p, P.partials, SL_A);
+    if (!grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, SL_A, NR)) return;
+    if (threadIdx.x < NR) {
+      const int c = threadIdx.x;
+      const double pq = __ldcg(P.totals + SL_A + c);
+      float al = 0.f;
+      if (s_active[c]) {
+        if (!(fabs(pq) >= 1e-30) || !isfinite(pq)) {
+          s_active[c] = 0;  // breakdown: freeze the column, report below
+          s_res[c] = -1.0;
+        } else {
+          al = (float)(s_rz[c] / pq);
+          s_citers[c] = it + 1;
+        }
+      }
+      s_alpha[c] = al;
+    }
+    __syncthreads();
+    float rr_p[CPL] = {0, 0, 0, 0}, rzn_p[CPL] = {0, 0, 0, 0};
+    for (long long q = tid; q < nq; q += nth) {
+      const long long row = q / LPG;
+      const int c0 = CPL * (int)(q % LPG);
+      float x[CPL], r[CPL], p[CPL], qq[CPL];
+      ld4(P.X32 + q * CPL, x);
+      ld4(P.R32 + q * CPL, r);
+      ld4(P.P32 + q * CPL, p);
+      ld4(P.Q32 + q * CPL, qq);
+      const float di = P.dinv32[row];
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        const float al = s_alpha[c0 + c];
+        x[c] = fmaf(al, p[c], x[c]);
+        r[c] = fmaf(-al, qq[c], r[c]);
+        rr_p[c] = fmaf(r[c], r[c], rr_p[c]);
+        rzn_p[c] = fmaf(r[c], r[c] * di, rzn_p[c]);
+      }
+      st4(P.X32 + q * CPL, x);
+      st4(P.R32 + q * CPL, r);
+    }
+    block_partials_cols<float>(rr_p, P.partials, SL_A);
+    __syncthreads();
+    block_partials_cols<float>(rzn_p, P.partials, SL_B);
+    if (!grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, 0, 2 * NR)) return;
+    if (threadIdx.x == 0) {
+      int all_dropped = 1, candidate = 0, seen = 0;
+      for (int c = 0; c < NR; ++c) {
+        if (!s_active[c]) continue;
+        seen = 1;
+        const double rn = sqrt(__ldcg(P.totals + SL_A + c));
+        if (!isfinite(rn)) candidate = 1;
+        if (rn > P.delta * s_rmax[c]) all_dropped = 0;
+        if (rn <= P.tol * s_bnorm[c]) candidate = 1;
+      }
+      s_flag = seen && (all_dropped || candidate);
+    }
+    __syncthreads();
+    if (s_flag) {
+      // reliable update for all columns: x += x32, r = b - K x (FP64), r32 = r
+      for (long long q = tid; q < nq; q += nth) {
+        double x[CPL];
+        float x32[CPL];
+        const float fz4[CPL] = {0, 0, 0, 0};
+        ld4(P.X + q * CPL, x);
+        ld4(P.X32 + q * CPL, x32);
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) x[c] += (double)x32[c];
+        st4(P.X + q * CPL, x);
+        st4(P.X32 + q * CPL, fz4);
+      }
+      if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+      double rr64[CPL] = {0, 0, 0, 0};
+      float rz2[CPL] = {0, 0, 0, 0};
+      for (int a = gwarp; a < n_nodes; a += nwarps) {
+        double y[3][CPL];
+        bsr_row_multi<double>(a, lane, P.M64, P.X, y);
+        if (lane < LPG) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            const size_t off = (size_t)(3 * a + i) * NR + CPL * lane;
+            double bv[CPL];
+            ld4(P.B + off, bv);
+            const float di = P.dinv32[3 * a + i];
+            float r32[CPL];
+#pragma unroll
+            for (int c = 0; c < CPL; ++c) {
+              const double rv = bv[c] - y[i][c];
+              rr64[c] = fma(rv, rv, rr64[c]);
+              r32[c] = (float)rv;
+              rz2[c] = fmaf(r32[c], r32[c] * di, rz2[c]);
+            }
+            st4(P.R32 + off, r32);
+          }
+        }
+      }
+      block_partials_cols<double>(rr64, P.partials, SL_A);
+      __syncthreads();
+      block_partials_cols<float>(rz2, P.partials, SL_B);
+      if (!grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, 0, 2 * NR)) return;
+      ++updates;
+      if (threadIdx.x < NR) {
+        const int c = threadIdx.x;
+        const double rn = sqrt(__ldcg(P.totals + SL_A + c));
+        if (s_active[c]) {
+          s_res[c] = rn;
+          s_rmax[c] = rn;
+          if (rn <= P.tol * s_bnorm[c]) s_active[c] = 0;  // converged
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x < NR) {
+      const int c = threadIdx.x;
+      const double rzn = __ldcg(P.totals + SL_B + c);
+      s_beta[c] = s_active[c] ? (float)(rzn / s_rz[c]) : 0.f;
+      s_rz[c] = rzn;
+    }
+    __syncthreads();
+    for (long long q = tid; q < nq; q += nth) {
+      const long long row = q / LPG;
+      const int c0 = CPL * (int)(q % LPG);
+      float p[CPL], r[CPL];
+      ld4(P.P32 + q * CPL, p);
+      ld4(P.R32 + q * CPL, r);
+      const float di = P.dinv32[row];
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) p[c] = s_active[c0 + c] ? fmaf(s_beta[c0 + c], p[c], r[c] * di) : 0.f;
+      st4(P.P32 + q * CPL, p);
+    }
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+  }
+  int any_active = 0, broke = 0;
+  for (int c = 0; c < NR; ++c) {
+    any_active |= s_active[c];
+    broke |= s_res[c] < 0.0;
+  }
+  if (broke) status = AXIA_ERR_ZERO_PIVOT;
+  else if (any_active) status = AXIA_ERR_NOT_CONVERGED;
+  if (blockIdx.x == 0 && threadIdx.x < NR) {
+    const int c = threadIdx.x;
+    P.out->bnorm[c] = s_bnorm[c];
+    P.out->residual[c] = s_res[c];
+    P.out->col_iters[c] = s_citers[c];
+    if (c == 0) {
+      P.out->iters = iters;
+      P.out->updates = updates;
+      P.out->status = status;
+    }
+  }
+}
+
+// B[d][c] = f_c[d] - K_fp u0 (free d), 0 (prescribed d); columns >= nrhs zero
+__global__ void k_batch_rhs(int64_t nd, int nrhs, const int32_t* ind_of, const double* F, const double* kfu0,
+                            double* B) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nd * NR; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t d = t / NR;
+    const int c = (int)(t % NR);
+    const int r = ind_of[d];
+    B[t] = (c < nrhs && r >= 0) ? F[(int64_t)c * nd + d] - kfu0[r] : 0.0;
+  }
+}
+// U_c[d] = u0[d] + X[d][c] on free DOFs
+__global__ void k_batch_out(int64_t nd, int nrhs, const int32_t* ind_of, const double* u0, const double* X, double* U) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nd * nrhs; t += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(t / nd);
+    const int64_t d = t % nd;
+    U[t] = ind_of[d] >= 0 ? u0[d] + X[d * NR + c] : u0[d];
+  }
+}
+
+}  // namespace
+
+// Solves nrhs load cases (F, U: [nrhs][nd] device arrays) 32 at a time.
+int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const axia_solve_opts* opts,
+                axia_solve_info* info, double* rel_res) {
+  if (!ctx->have_bsr64 || !ctx->have_bsr32)
+    return set_error(ctx, AXIA_ERR_STATE, "batched solve needs the node-block forms (AXIA_ASM_BSR64 | AXIA_ASM_BSR32)");
+  const int64_t nd = ctx->ndof;
+  const size_t blk = (size_t)nd * NR;
+  if (ctx->batch_capacity < blk) {
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_mB, blk));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_mX, blk));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_mX32, blk));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_mR32, blk));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_mP32, blk));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_mQ32, blk));
+    ctx->batch_capacity = blk;
+  }
+  if (!ctx->d_mout) {
+    MultiOut* o = nullptr;
+    AXIA_TRY(dev_alloc(ctx, &o, 1));
+    ctx->d_mout = o;
+  }
+  const long long max_iter = opts->max_iter > 0 ? opts->max_iter : std::max<long long>(4LL * ctx->n_free, 200);
+  const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.01;
+  auto kern = pcg_bsr_multi_kernel;
+  int grid = 0;
+  AXIA_TRY(coop_grid(ctx, (const void*)kern, (int)std::min<int64_t>(nd, INT32_MAX), &grid));
+  if ((size_t)grid * 2 * NR > ctx->partial_slots) grid = (int)(ctx->partial_slots / (2 * NR));
+  info->iters = 0;
+  info->outer_iters = 0;
+  double worst = 0.0;
+  for (int c0 = 0; c0 < nrhs; c0 += NR) {
+    const int nc = std::min(NR, nrhs - c0);
+    AXIA_TRY(reset_dev_status(ctx));
+    k_batch_rhs<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(nd, nc, ctx->d_ind_of, d_F + (int64_t)c0 * nd, ctx->d_kfu0,
+                                                           ctx->d_mB);
+    ctx->launches++;
+    AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
+    MultiArgs P{BsrMatM<float>{(int)ctx->n_nodes, ctx->d_adj_ptr32, ctx->d_adj, ctx->d_bval32, (long long)ctx->n_adj},
+                BsrMatM<double>{(int)ctx->n_nodes, ctx->d_adj_ptr32, ctx->d_adj, ctx->d_bval64, (long long)ctx->n_adj},
+                (int)nd, ctx->d_bdinv32, ctx->d_mB, ctx->d_mX, ctx->d_mX32, ctx->d_mR32, ctx->d_mP32, ctx->d_mQ32,
+                ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (MultiOut*)ctx->d_mout, opts->rtol, delta,
+                max_iter, 2000000000ull};
+    AXIA_TRY(timed_launch(ctx, info, [&]() -> int {
+      void* params[] = {&P};
+      AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params, 0,
+                                                 ctx->stream));
+      ctx->launches++;
+      return AXIA_OK;
+    }));
+    MultiOut o;
+    AXIA_CUDA(ctx, cudaMemcpyAsync(&o, ctx->d_mout, sizeof(MultiOut), cudaMemcpyDeviceToHost, ctx->stream));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    DevStatus hs;
+    AXIA_TRY(read_dev_status(ctx, &hs));
+    if (hs.timeout) return set_error(ctx, AXIA_ERR_TIMEOUT, "a grid barrier of the batched PCG ran past its limit");
+    info->iters = std::max<int64_t>(info->iters, o.iters);
+    info->outer_iters += o.updates;
+    for (int c = 0; c < nc; ++c) {
+      const double rr = o.bnorm[c] > 0 ? o.residual[c] / o.bnorm[c] : 0.0;
+      if (rel_res) rel_res[c0 + c] = rr;
+      worst = std::max(worst, rr);
+    }
+    if (o.status != AXIA_OK) {
+      if (o.status == AXIA_ERR_ZERO_PIVOT) return set_error(ctx, o.status, "batched CG: zero pivot in a load case");
+      return set_error(ctx, o.status, "batched CG did not converge in " + std::to_string(o.iters) + " iterations");
+    }
+    k_batch_out<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(nd, nc, ctx->d_ind_of, ctx->d_u0, ctx->d_mX,
+                                                           d_U + (int64_t)c0 * nd);
+    ctx->launches++;
+    AXIA_CUDA(ctx, cudaGetLastError());
+  }
+  info->residual = worst;
+  info->bnorm = 1.0;
+  return AXIA_OK;
+}

@@ -244,6 +244,11 @@ struct axia_ctx {
   double *d_bf = nullptr, *d_xf = nullptr, *d_rf = nullptr, *d_pf = nullptr, *d_qf = nullptr;
   float *d_xf32 = nullptr, *d_rf32 = nullptr, *d_pf32 = nullptr, *d_qf32 = nullptr;
   size_t full_capacity = 0;
+  // batched load cases ([ndof][32] blocks)
+  double *d_mB = nullptr, *d_mX = nullptr;
+  float *d_mX32 = nullptr, *d_mR32 = nullptr, *d_mP32 = nullptr, *d_mQ32 = nullptr;
+  void* d_mout = nullptr;
+  size_t batch_capacity = 0;
 
   // SIMP compliance state (forward -> backward)
   double* d_rho = nullptr;      // [n_elem]

@@ -591,10 +591,10 @@ int reconstruct(axia_ctx* ctx, double* d_u) {
 
 int ensure_pcg_state(axia_ctx* ctx) {
   if (!ctx->d_partials) {
-    ctx->partial_slots = (size_t)N_SLOTS * 16 * 1024;
+    ctx->partial_slots = (size_t)64 * 2048;  // up to 64 reduction slots x 2048 blocks
     AXIA_TRY(dev_alloc(ctx, &ctx->d_partials, ctx->partial_slots));
   }
-  if (!ctx->d_totals) AXIA_TRY(dev_alloc(ctx, &ctx->d_totals, 16));
+  if (!ctx->d_totals) AXIA_TRY(dev_alloc(ctx, &ctx->d_totals, 64));
   if (!ctx->d_bar) AXIA_TRY(dev_alloc(ctx, &ctx->d_bar, 1));
   if (!ctx->d_out) {
     PcgOut* o = nullptr;

@@ -180,6 +180,9 @@ def main():
     ap.add_argument("--lanes32", type=int, default=0)
     ap.add_argument("--lanes32csr", type=int, default=0)
     ap.add_argument("--delta", type=float, default=0.01, help="reliable-update residual reduction")
+    ap.add_argument("--only", choices=["mixed", "fp64", "spmv"], default=None,
+                    help="run one solve (or SpMV sweep) once and exit: the profiling entry")
+    ap.add_argument("--max-iter", type=int, default=0, help="with --only: cap the CG iterations")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -213,6 +216,29 @@ def main():
     f_dev = torch.from_numpy(f_host).to(f"cuda:{local}")
     u64 = torch.empty_like(f_dev)
     umx = torch.empty_like(f_dev)
+
+    if args.only:
+        if args.only == "spmv":
+            ctx.assemble_ex(L.ASM_CSR64 | L.ASM_CSR32 | L.ASM_BSR64 | L.ASM_BSR32)
+            nd = 3 * model.n_nodes
+            xf32 = torch.rand(nd, device=f"cuda:{local}")
+            yf32 = torch.empty_like(xf32)
+            with torch.cuda.stream(stream):
+                for _ in range(5):
+                    ctx.bsr_spmv_device(L.PREC_MIXED, xf32.data_ptr(), yf32.data_ptr(), args.lanes32)
+        else:
+            mixed = args.only == "mixed"
+            ctx.assemble_ex((L.ASM_BSR64 | L.ASM_BSR32) if mixed else L.ASM_CSR64)
+            kw = dict(precision=L.PREC_MIXED, refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta,
+                      matrix_format=L.FORMAT_BSR3) if mixed else dict(precision=L.PREC_FP64)
+            try:
+                with torch.cuda.stream(stream):
+                    info = ctx.solve_device(f_dev.data_ptr(), u64.data_ptr(), rtol=RTOL, max_iter=args.max_iter, **kw)
+                print(json.dumps({"only": args.only, "iters": info.iters, "ms_kernel": info.ms_pcg_kernel}))
+            except Exception as e:  # a capped iteration count ends as NOT_CONVERGED
+                print(json.dumps({"only": args.only, "status": str(e)[:120]}))
+        torch.cuda.synchronize()
+        return
 
     def barrier():
         torch.cuda.synchronize()

@@ -226,6 +226,19 @@ AXIA_API int32_t axia_gpu_compliance_forward(axia_ctx* ctx, const double* rho, d
  * the self-adjoint compliance problem is -u, so no second solve is needed). */
 AXIA_API int32_t axia_gpu_compliance_backward(axia_ctx* ctx, double* grad);
 
+/* Many load cases on the assembled mesh in one persistent launch per 32 of
+ * them (the reference solves each load case with its own solve_kff call,
+ * linalg.rs:311): F and U are [nrhs][3*n_nodes] host arrays (U = u0 + T x per
+ * case), each case runs its own Jacobi-PCG recurrence (alpha, beta,
+ * convergence) on the FP32 node-block matrix with FP64 reliable updates
+ * (opts->inner_rtol = the residual drop between updates) and stops at
+ * opts->rtol.  Needs axia_gpu_assemble_ex(AXIA_ASM_BSR64 | AXIA_ASM_BSR32).
+ * rel_res (nrhs entries, may be NULL) receives ||b - K x|| / ||b|| per case. */
+AXIA_API int32_t axia_gpu_solve_batched(axia_ctx* ctx, int32_t nrhs, const double* F, double* U,
+                                        const axia_solve_opts* opts, axia_solve_info* info, double* rel_res);
+AXIA_API int32_t axia_gpu_solve_batched_device(axia_ctx* ctx, int32_t nrhs, const double* F_dev, double* U_dev,
+                                               const axia_solve_opts* opts, axia_solve_info* info, double* rel_res);
+
 /* Sizes of the assembled system: n_free and nnz. */
 AXIA_API int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz);
 

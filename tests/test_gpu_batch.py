@@ -1,0 +1,66 @@
+"""Batched load cases (axia_gpu_solve_batched): every case against its own
+direct solve (SciPy SuperLU on the oracle's K_ff) and against the
+single-case GPU solve.  Relative displacement error <= 1e-8 at rtol 1e-10."""
+import numpy as np
+import pytest
+
+from axia_gpu import _lib, meshgen
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _direct_all(model, F):
+    ref = O.solve_static(model, solver=O.SOLVER_PCG, tol=1e-6, keep_csr=True, f=F[0])
+    free = model.free_mask()
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    n = ref.n_free
+    K = sp.csr_matrix((ref.data, ref.indices, ref.indptr), shape=(n, n)).tocsc()
+    lu = spla.splu(K)
+    out = np.zeros_like(F)
+    for c in range(F.shape[0]):
+        out[c][free] = lu.solve(F[c][free])
+    return out
+
+
+def test_batched_cases_match_direct_and_single(gpu_ctx):
+    n = 10
+    m = meshgen.block_c3d8_multiload(n=n, nrhs=40)
+    F = m.cload_batch.copy()
+    F[5] = 0.0                       # a case without load converges at once
+    gpu_ctx.setup(m).assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+    U, info, rel = gpu_ctx.solve_batched(F, rtol=1e-10)
+    assert info.iters > 0 and np.all(rel <= 1e-10 * 1.0001)
+    ref = _direct_all(m, F)
+    for c in range(F.shape[0]):
+        if c == 5:
+            assert np.all(U[c] == 0.0)
+            continue
+        err = np.linalg.norm(U[c] - ref[c]) / np.linalg.norm(ref[c])
+        assert err < 1e-8, (c, err)
+    u1, i1 = gpu_ctx.solve(F[7], rtol=1e-10, precision=_lib.PREC_MIXED, refine_mode=_lib.REFINE_RELIABLE,
+                           inner_rtol=0.01, matrix_format=_lib.FORMAT_BSR3)
+    assert np.linalg.norm(U[7] - u1) / np.linalg.norm(u1) < 1e-8
+
+
+def test_batched_needs_node_block_forms(gpu_ctx):
+    m = meshgen.block_c3d8_multiload(n=4, nrhs=2)
+    gpu_ctx.setup(m).assemble()
+    with pytest.raises(_lib.AxiaError) as e:
+        gpu_ctx.solve_batched(m.cload_batch)
+    assert e.value.code == _lib.ERR_STATE
+
+
+def test_batched_prescribed_values(gpu_ctx):
+    m = meshgen.cantilever_c3d8(nx=6, ny=3, nz=3)
+    tip = np.nonzero(np.isclose(m.coords[:, 0], 6.0))[0]
+    m.bc_dof = np.concatenate([m.bc_dof, 3 * tip + 2])
+    m.bc_val = np.concatenate([m.bc_val, np.full(tip.shape[0], -0.01)])
+    F = np.stack([m.cload * s for s in (0.0, 1.0, -2.0)])
+    gpu_ctx.setup(m).assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+    U, info, rel = gpu_ctx.solve_batched(F, rtol=1e-11)
+    for c in range(3):
+        ref = O.solve_static(m, solver=O.SOLVER_CHOLESKY, f=F[c])
+        assert np.linalg.norm(U[c] - ref.u) / np.linalg.norm(ref.u) < 1e-8, c
+        assert np.allclose(U[c][3 * tip + 2], -0.01)
