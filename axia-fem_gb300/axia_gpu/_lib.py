@@ -78,6 +78,8 @@ SIGNATURES = [
     ("axia_gpu_last_error", C.c_char_p, [_P]),
     ("axia_gpu_element_ke", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int64, _P, _P, C.c_double, _P, _P,
                                         C.POINTER(C.c_int64)]),
+    ("axia_gpu_element_ke_noalloc", C.c_int32, [C.c_int32, C.c_int32, C.c_int64, _P, _P, C.c_double, _P, _P,
+                                                C.POINTER(C.c_int64)]),
     ("axia_face_loads", C.c_int32, [C.c_int32, C.c_int64, _P, _P, C.c_int64, _P, _P, _P, _P, C.POINTER(C.c_int64)]),
     ("axia_gpu_setup", C.c_int32, [_P, C.POINTER(Mesh), C.c_int64, _P, _P]),
     ("axia_gpu_assemble", C.c_int32, [_P, C.c_int32]),

@@ -146,6 +146,23 @@ AXIA_API int32_t axia_gpu_element_ke(axia_ctx* ctx, int32_t nn, int32_t reduced,
                             const double* xyz, const double* e, double nu, double* ke,
                             double* vol, int64_t* bad_elem);
 
+/* Batched element stiffness that allocates no GPU memory and needs no
+ * context.  No counterpart in the reference: it exists for callers that must
+ * not call cudaMalloc -- hosts whose device memory belongs to another
+ * allocator or to a budget they may not exceed, and latency-critical loops
+ * where an allocation's implicit device synchronization is not acceptable.
+ * Same arguments, results and error codes as axia_gpu_element_ke (host
+ * buffers in and out), on the current CUDA device.  Limit: n_elem <= 2048
+ * for nn = 8 and <= 512 for nn = 20 (AXIA_ERR_TOO_LARGE above).  Its device
+ * memory is one fixed 16 MiB array per device, held until the process exits;
+ * the first call on a device looks up that array's address and uploads the
+ * element tables, so make it before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race (calls within one process are
+ * serialized). */
+AXIA_API int32_t axia_gpu_element_ke_noalloc(int32_t nn, int32_t reduced, int64_t n_elem, const double* xyz,
+                                             const double* e, double nu, double* ke, double* vol,
+                                             int64_t* bad_elem);
+
 /* Consistent nodal forces of face pressures added into f_full[3*n_nodes], in
  * list order, on the host (apply_pressure solver/src/analysis.rs:1365-1396 ->
  * hex8_face_pressure elem.rs:891-950 / hex20_face_pressure quadratic.rs:275-315).
