@@ -91,10 +91,15 @@ SIGNATURES = [
     ("axia_gpu_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32]),
     ("axia_gpu_bsr_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32]),
     ("axia_gpu_node_blocks", C.c_int64, [_P]),
+    ("axia_gpu_setup_multi", C.c_int32, [_P, C.c_int32, C.POINTER(Mesh), _P, _P, _P]),
+    ("axia_gpu_solve_multi", C.c_int32, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), _P, _P]),
+    ("axia_gpu_solve_multi_device", C.c_int32, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), _P, _P]),
     ("axia_gpu_solve_batched", C.c_int32, [_P, C.c_int32, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), _P]),
     ("axia_gpu_solve_batched_device", C.c_int32, [_P, C.c_int32, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo),
                                                   _P]),
     ("axia_gpu_element_energy", C.c_int32, [_P, _P, _P, _P]),
+    ("axia_gpu_recover", C.c_int32, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P]),
+    ("axia_gpu_recover_device", C.c_int32, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P]),
     ("axia_gpu_compliance_forward", C.c_int32, [_P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_double),
                                                 C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
     ("axia_gpu_compliance_backward", C.c_int32, [_P, _P]),

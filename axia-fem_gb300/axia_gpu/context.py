@@ -81,6 +81,58 @@ class GpuContext:
         self.n_free, self.nnz = n.value, nnz.value
         return self
 
+    def setup_multi(self, models):
+        """Several independent meshes as one context (concatenated node and element lists)."""
+        self.models = list(models)
+        n = len(self.models)
+        keep = []
+        meshes = (L.Mesh * n)()
+        nbc = np.zeros(n, np.int64)
+        dof_ptrs = (C.c_void_p * n)()
+        val_ptrs = (C.c_void_p * n)()
+        for k, m in enumerate(self.models):
+            co, cn, e = _c(m.coords, np.float64), _c(m.conn, np.int32), _c(m.e_elem, np.float64)
+            bd, bv = _c(m.bc_dof, np.int64), _c(m.bc_val, np.float64)
+            keep += [co, cn, e, bd, bv]
+            meshes[k] = L.Mesh(m.n_nodes, L.ptr(co), m.n_elem, m.nn, int(m.reduced), L.ptr(cn), L.ptr(e), 0.0,
+                               float(m.nu))
+            nbc[k] = bd.shape[0]
+            dof_ptrs[k] = L.ptr(bd)
+            val_ptrs[k] = L.ptr(bv)
+        self._check(self.lib.axia_gpu_setup_multi(self.h, n, meshes, L.ptr(nbc), C.cast(dof_ptrs, C.c_void_p),
+                                                  C.cast(val_ptrs, C.c_void_p)), "setup_multi")
+        self._multi_keep = keep
+        self.node0 = np.concatenate([[0], np.cumsum([m.n_nodes for m in self.models])]).astype(np.int64)
+        nf, nnz = C.c_int64(), C.c_int64()
+        self.lib.axia_gpu_system_size(self.h, C.byref(nf), C.byref(nnz))
+        self.n_free, self.nnz = nf.value, nnz.value
+        self.model = None
+        return self
+
+    def solve_multi(self, f_full, **kw):
+        """Solve all meshes of setup_multi: concatenated f -> (u, info, rel_res, iters)."""
+        f = _c(f_full, np.float64)
+        u = np.zeros_like(f)
+        n = len(self.models)
+        rel, its = np.zeros(n), np.zeros(n, np.int64)
+        kw.setdefault("inner_rtol", 0.01)
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        self._check(self.lib.axia_gpu_solve_multi(self.h, L.ptr(f), L.ptr(u), C.byref(o), C.byref(info), L.ptr(rel),
+                                                  L.ptr(its)), "solve_multi")
+        return u, info, rel, its
+
+    def solve_multi_device(self, f_dev_ptr, u_dev_ptr, **kw):
+        n = len(self.models)
+        rel, its = np.zeros(n), np.zeros(n, np.int64)
+        kw.setdefault("inner_rtol", 0.01)
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        self._check(self.lib.axia_gpu_solve_multi_device(self.h, C.c_void_p(f_dev_ptr), C.c_void_p(u_dev_ptr),
+                                                         C.byref(o), C.byref(info), L.ptr(rel), L.ptr(its)),
+                    "solve_multi")
+        return info, rel, its
+
     def assemble(self, precision=L.PREC_FP64):
         self._check(self.lib.axia_gpu_assemble(self.h, int(precision)), "assemble")
         return self
@@ -151,6 +203,30 @@ class GpuContext:
         s = np.zeros(self.model.n_elem)
         self._check(self.lib.axia_gpu_element_energy(self.h, L.ptr(u), L.ptr(v), L.ptr(s)), "element_energy")
         return s
+
+    def recover(self, u_full, f_full=None, e_strain=None):
+        """Nodal stresses [n][6], strains [n][6], von Mises [n], reactions K u - f [ndof]
+        and element mean stresses [n_elem][6] for the displacement u_full."""
+        m = self.model
+        u = _c(u_full, np.float64)
+        f = None if f_full is None else _c(f_full, np.float64)
+        if e_strain is None:
+            e_strain = float(np.asarray(m.e_elem, dtype=np.float64).ravel()[0]) if m.n_elem else 1.0
+        stress = np.zeros((m.n_nodes, 6))
+        strain = np.zeros((m.n_nodes, 6))
+        vm = np.zeros(m.n_nodes)
+        rf = np.zeros(m.ndof)
+        emean = np.zeros((m.n_elem, 6))
+        self._check(self.lib.axia_gpu_recover(self.h, L.ptr(u), None if f is None else L.ptr(f), float(e_strain),
+                                              L.ptr(stress), L.ptr(strain), L.ptr(vm), L.ptr(rf), L.ptr(emean)),
+                    "recover")
+        return stress, strain, vm, rf, emean
+
+    def recover_device(self, u_ptr, f_ptr, e_strain, stress_ptr=None, strain_ptr=None, vm_ptr=None, rf_ptr=None,
+                       elem_ptr=None):
+        """Device-pointer form of recover (ordered on the context's stream)."""
+        self._check(self.lib.axia_gpu_recover_device(self.h, u_ptr, f_ptr, float(e_strain), stress_ptr, strain_ptr,
+                                                     vm_ptr, rf_ptr, elem_ptr), "recover_device")
 
     def compliance_forward(self, rho, penal, e0, f_full, **kw):
         """SIMP forward: E = e0 rho^penal, solve, return (u, C, info)."""

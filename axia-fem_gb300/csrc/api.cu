@@ -14,6 +14,7 @@ int element_energy(axia_ctx* ctx, const double* d_u, const double* d_v, double* 
 int simp_modulus(axia_ctx* ctx, const double* d_rho, double pexp, double e0);
 int simp_gradient(axia_ctx* ctx, const double* d_rho, const double* d_s, double pexp, double e0, double* d_g);
 int device_dot(axia_ctx* ctx, const double* a, const double* b, int64_t n, double* out);
+void multimesh_release(axia_ctx* ctx);
 int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const axia_solve_opts* opts,
                 axia_solve_info* info, double* rel_res);
 int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args);
@@ -50,6 +51,9 @@ struct EventTimer {
 };
 
 void free_mesh_state(axia_ctx* ctx) {
+  multimesh_release(ctx);
+  ctx->mesh_node0.clear();
+  ctx->mesh_blocks.clear();
   dev_free(ctx->d_coords);
   dev_free(ctx->d_conn);
   dev_free(ctx->d_e);
@@ -97,6 +101,7 @@ void free_mesh_state(axia_ctx* ctx) {
   dev_free(ctx->d_rf32);
   dev_free(ctx->d_pf32);
   dev_free(ctx->d_qf32);
+  dev_free(ctx->d_zf32);
   ctx->full_capacity = 0;
   dev_free(ctx->d_mB);
   dev_free(ctx->d_mX);
@@ -110,6 +115,7 @@ void free_mesh_state(axia_ctx* ctx) {
   dev_free(ctx->d_rho);
   dev_free(ctx->d_energy);
   dev_free(ctx->d_grad);
+  dev_free(ctx->d_rec);
   ctx->have_forward = false;
   ctx->vec_capacity = 0;
   ctx->assembled = ctx->have32 = ctx->have_csr64 = ctx->have_bsr64 = ctx->have_bsr32 = false;

@@ -22,15 +22,6 @@
 
 #include "solver.cuh"
 
-template <typename V>
-struct BsrMat {
-  int n_nodes;
-  const int* adj_ptr;  // [n_nodes+1]
-  const int* adj;      // [nb]
-  const V* val;        // [9][nb]
-  long long nb;
-};
-
 // Block row a with L lanes: (y0, y1, y2) = sum_s K_as x_adj[s]
 template <typename V, typename A, int L>
 __device__ __forceinline__ void bsr_row(int a, int sl, const BsrMat<V>& M, const V* x, A& y0, A& y1, A& y2) {
@@ -183,39 +174,39 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_bsr_kernel(BsrPcgArgs<V> P) {
   }
 }
 
-struct BsrReliableArgs {
-  BsrMat<float> M32;
-  BsrMat<double> M64;
-  int nd;
-  const float* dinv32;
-  const double* b;
-  double* x;
-  float* x32;
-  float* r32;
-  float* p32;
-  float* q32;
+// FP32 CG on the FP32 node-block matrix with FP64 reliable updates (the
+// recurrence of pcg_reliable_kernel in pcg.cu on the node-block form): when
+// the FP32 residual has dropped by delta since the last update, x += x32 in
+// FP64 and r is replaced by the FP64 residual b - K x.
+// The rows a system occupies and the blocks that solve it: block rows
+// [node0, node1) of the node-block matrix, blocks rank = 0..nblk-1 of a group
+// with its own barrier, partial-sum area, totals and result record.
+struct SolveRange {
+  int node0, node1;
+  unsigned rank, nblk;
   double* partials;
   double* totals;
   GridBarrier* bar;
-  DevStatus* st;
   PcgOut* out;
-  double tol;
-  double delta;
-  long long max_iter;
-  unsigned long long limit_ns;
 };
 
-// FP32 CG on the FP32 node-block matrix with FP64 reliable updates
-// (the recurrence of pcg_reliable_kernel in pcg.cu on the node-block form).
 template <int L32, int L64>
-__global__ void __launch_bounds__(PCG_THREADS, 4) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
-  const int nd = P.nd, n_nodes = P.M32.n_nodes;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+__device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const SolveRange& R) {
+  const int n0 = R.node0, n1 = R.node1;
+  const int i0 = 3 * n0;
+  BsrMat<float> M32 = P.M32;
+  BsrMat<double> M64 = P.M64;
+  M32.n_nodes = n1;  // rows past the range read as empty
+  M64.n_nodes = n1;
+  const int tid = R.rank * blockDim.x + threadIdx.x, nth = R.nblk * blockDim.x;
   const int gwarp = tid >> 5, nwarps = nth >> 5;
   const int lane = threadIdx.x & 31;
+  const int nd = 3 * n1;  // vector loops run over [i0, 3 n1)
+  double* const partials = R.partials;
+  double* const totals = R.totals;
   float rz_p = 0.f;
   double bb_p = 0.0;
-  for (int i = tid; i < nd; i += nth) {
+  for (int i = i0 + tid; i < nd; i += nth) {
     const double bi = P.b[i];
     P.x[i] = 0.0;
     const float ri = (float)bi;
@@ -226,10 +217,10 @@ __global__ void __launch_bounds__(PCG_THREADS, 4) pcg_bsr_reliable_kernel(BsrRel
     rz_p = fmaf(ri, z, rz_p);
     bb_p = fma(bi, bi, bb_p);
   }
-  block_partials<double>(bb_p, (double)rz_p, 2, P.partials, S_RR, S_RZ);
-  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
-  float rz = (float)total(P.totals, S_RZ);
-  const double bnorm = sqrt(total(P.totals, S_RR));
+  block_partials<double>(bb_p, (double)rz_p, 2, partials, S_RR, S_RZ, R.nblk, R.rank);
+  if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk)) return;
+  float rz = (float)total(totals, S_RZ);
+  const double bnorm = sqrt(total(totals, S_RR));
   double rmax = bnorm, residual = bnorm;
   long long iters = 0;
   int updates = 0, status = AXIA_OK;
@@ -241,11 +232,11 @@ __global__ void __launch_bounds__(PCG_THREADS, 4) pcg_bsr_reliable_kernel(BsrRel
     {
       constexpr int RPW = 32 / L32;
       const int sl = lane % L32, grp = lane / L32;
-      for (int base = gwarp * RPW; base < n_nodes; base += nwarps * RPW) {
+      for (int base = n0 + gwarp * RPW; base < n1; base += nwarps * RPW) {
         const int a = base + grp;
         float y0, y1, y2;
-        bsr_row<float, float, L32>(a, sl, P.M32, P.p32, y0, y1, y2);
-        if (a < n_nodes && sl == 0) {
+        bsr_row<float, float, L32>(a, sl, M32, P.p32, y0, y1, y2);
+        if (a < n1 && sl == 0) {
           P.q32[3 * a] = y0;
           P.q32[3 * a + 1] = y1;
           P.q32[3 * a + 2] = y2;
@@ -255,46 +246,46 @@ __global__ void __launch_bounds__(PCG_THREADS, 4) pcg_bsr_reliable_kernel(BsrRel
         }
       }
     }
-    block_partials<float>(pq_p, 0.f, 1, P.partials, S_PQ, S_PQ);
-    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1)) return;
-    const float pq = (float)total(P.totals, S_PQ);
+    block_partials<float>(pq_p, 0.f, 1, partials, S_PQ, S_PQ, R.nblk, R.rank);
+    if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_PQ, 1, R.nblk)) return;
+    const float pq = (float)total(totals, S_PQ);
     if (!(fabsf(pq) >= 1e-30f) || !isfinite(pq)) {
       status = isfinite(pq) ? AXIA_ERR_ZERO_PIVOT : AXIA_ERR_NONFINITE;
       break;
     }
     const float alpha = rz / pq;
     float rr_p = 0.f, rzn_p = 0.f;
-    for (int i = tid; i < nd; i += nth) {
+    for (int i = i0 + tid; i < nd; i += nth) {
       P.x32[i] = fmaf(alpha, P.p32[i], P.x32[i]);
       const float ri = fmaf(-alpha, P.q32[i], P.r32[i]);
       P.r32[i] = ri;
       rr_p = fmaf(ri, ri, rr_p);
       rzn_p = fmaf(ri, ri * P.dinv32[i], rzn_p);
     }
-    block_partials<float>(rr_p, rzn_p, 2, P.partials, S_RR, S_RZ);
-    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
-    float rzn = (float)total(P.totals, S_RZ);
-    const double rnorm32 = sqrt(total(P.totals, S_RR));
+    block_partials<float>(rr_p, rzn_p, 2, partials, S_RR, S_RZ, R.nblk, R.rank);
+    if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk)) return;
+    float rzn = (float)total(totals, S_RZ);
+    const double rnorm32 = sqrt(total(totals, S_RR));
     if (!isfinite(rnorm32)) {
       status = AXIA_ERR_NONFINITE;
       break;
     }
     if (rnorm32 <= P.delta * rmax || rnorm32 <= P.tol * bnorm) {
-      for (int i = tid; i < nd; i += nth) {
+      for (int i = i0 + tid; i < nd; i += nth) {
         P.x[i] += (double)P.x32[i];
         P.x32[i] = 0.f;
       }
-      if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+      if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
       double rr64_p = 0.0;
       float rz_new_p = 0.f;
       {
         constexpr int RPW = 32 / L64;
         const int sl = lane % L64, grp = lane / L64;
-        for (int base = gwarp * RPW; base < n_nodes; base += nwarps * RPW) {
+        for (int base = n0 + gwarp * RPW; base < n1; base += nwarps * RPW) {
           const int a = base + grp;
           double y[3];
-          bsr_row<double, double, L64>(a, sl, P.M64, P.x, y[0], y[1], y[2]);
-          if (a < n_nodes && sl == 0) {
+          bsr_row<double, double, L64>(a, sl, M64, P.x, y[0], y[1], y[2]);
+          if (a < n1 && sl == 0) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               const int i = 3 * a + c;
@@ -307,11 +298,11 @@ __global__ void __launch_bounds__(PCG_THREADS, 4) pcg_bsr_reliable_kernel(BsrRel
           }
         }
       }
-      block_partials<double>(rr64_p, (double)rz_new_p, 2, P.partials, S_RR, S_RZ);
-      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+      block_partials<double>(rr64_p, (double)rz_new_p, 2, partials, S_RR, S_RZ, R.nblk, R.rank);
+      if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk)) return;
       ++updates;
-      residual = sqrt(total(P.totals, S_RR));
-      rzn = (float)total(P.totals, S_RZ);
+      residual = sqrt(total(totals, S_RR));
+      rzn = (float)total(totals, S_RZ);
       rmax = residual;
       if (!isfinite(residual)) {
         status = AXIA_ERR_NONFINITE;
@@ -324,17 +315,38 @@ __global__ void __launch_bounds__(PCG_THREADS, 4) pcg_bsr_reliable_kernel(BsrRel
     }
     const float beta = rzn / rz;
     rz = rzn;
-    for (int i = tid; i < nd; i += nth) P.p32[i] = fmaf(beta, P.p32[i], P.r32[i] * P.dinv32[i]);
-    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+    for (int i = i0 + tid; i < nd; i += nth) P.p32[i] = fmaf(beta, P.p32[i], P.r32[i] * P.dinv32[i]);
+    if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
   }
   if (status == AXIA_OK && residual > P.tol * bnorm * 10.0) status = AXIA_ERR_NOT_CONVERGED;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    P.out->iters = iters;
-    P.out->residual = residual;
-    P.out->bnorm = bnorm;
-    P.out->status = status;
-    P.out->updates = updates;
+  if (R.rank == 0 && threadIdx.x == 0) {
+    R.out->iters = iters;
+    R.out->residual = residual;
+    R.out->bnorm = bnorm;
+    R.out->status = status;
+    R.out->updates = updates;
   }
+}
+
+template <int L32, int L64>
+__global__ void __launch_bounds__(PCG_THREADS, 3) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
+  const SolveRange R{0, P.M32.n_nodes, blockIdx.x, gridDim.x, P.partials, P.totals, P.bar, P.out};
+  reliable_body<L32, L64>(P, R);
+}
+
+// Independent systems on disjoint node ranges of one node-block matrix (the
+// meshes of axia_gpu_setup_multi): block b belongs to group cta_group[b] and
+// solves that group's system with the group's own barrier, partial sums,
+// totals and result, so each system converges and exits on its own.
+template <int L32, int L64>
+__global__ void __launch_bounds__(PCG_THREADS, 2)
+pcg_group_reliable_kernel(BsrReliableArgs P, const MeshGroup* groups, const int* cta_group, GridBarrier* bars,
+                          double* totals4, PcgOut* outs) {
+  const int g = cta_group[blockIdx.x];
+  const MeshGroup G = groups[g];
+  const SolveRange R{G.node0, G.node1, blockIdx.x - (unsigned)G.cta0, (unsigned)G.ncta, P.partials + G.part_off,
+                     totals4 + 4 * g, bars + g, outs + g};
+  reliable_body<L32, L64>(P, R);
 }
 
 // b[d] = f[d] - K_fp u0 for free d, 0 for prescribed d
@@ -400,6 +412,7 @@ static int ensure_full_buffers(axia_ctx* ctx, bool mixed) {
       AXIA_TRY(dev_alloc(ctx, &ctx->d_rf32, nd));
       AXIA_TRY(dev_alloc(ctx, &ctx->d_pf32, nd));
       AXIA_TRY(dev_alloc(ctx, &ctx->d_qf32, nd));
+      AXIA_TRY(dev_alloc(ctx, &ctx->d_zf32, nd));
     }
     ctx->full_capacity = nd;
   }
@@ -440,11 +453,65 @@ static int launch_bsr_rel_t(axia_ctx* ctx, BsrReliableArgs& P) {
 
 static int launch_bsr_rel(axia_ctx* ctx, BsrReliableArgs& P, int l32) {
   switch (l32) {
-    case 2: return launch_bsr_rel_t<2, 8>(ctx, P);
-    case 4: return launch_bsr_rel_t<4, 8>(ctx, P);
-    case 16: return launch_bsr_rel_t<16, 8>(ctx, P);
-    default: return launch_bsr_rel_t<8, 8>(ctx, P);
+    case 2: return launch_bsr_rel_t<2, 4>(ctx, P);
+    case 4: return launch_bsr_rel_t<4, 4>(ctx, P);
+    case 16: return launch_bsr_rel_t<16, 4>(ctx, P);
+    default: return launch_bsr_rel_t<8, 4>(ctx, P);
   }
+}
+
+// Occupancy of the group kernel (blocks per SM) for the grid size of a multi-mesh solve.
+int group_kernel_capacity(axia_ctx* ctx, int lanes, int* per_sm) {
+  const void* kern = lanes == 16 ? (const void*)pcg_group_reliable_kernel<16, 8>
+                                 : (lanes == 4 ? (const void*)pcg_group_reliable_kernel<4, 8>
+                                               : (const void*)pcg_group_reliable_kernel<8, 8>);
+  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, PCG_THREADS, 0));
+  return AXIA_OK;
+}
+
+// Cooperative launch of the group kernel on ctx->stream (capturable).
+int launch_group_reliable(axia_ctx* ctx, BsrReliableArgs& P, const MeshGroup* groups, const int* cta_group,
+                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes) {
+  void* params[] = {&P, &groups, &cta_group, &bars, &totals4, &outs};
+  const void* kern = lanes == 16 ? (const void*)pcg_group_reliable_kernel<16, 8>
+                                 : (lanes == 4 ? (const void*)pcg_group_reliable_kernel<4, 8>
+                                               : (const void*)pcg_group_reliable_kernel<8, 8>);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(PCG_THREADS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  AXIA_CUDA(ctx, cudaLaunchKernelExC(&cfg, kern, params));
+  ctx->launches++;
+  return AXIA_OK;
+}
+
+int launch_full_rhs(axia_ctx* ctx, const double* d_f) {
+  k_build_rhs_full<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(ctx->ndof, ctx->d_ind_of, d_f, ctx->d_kfu0, ctx->d_bf);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  return AXIA_OK;
+}
+
+int launch_full_reconstruct(axia_ctx* ctx, double* d_u) {
+  k_reconstruct_full<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(ctx->ndof, ctx->d_ind_of, ctx->d_u0, ctx->d_xf, d_u);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  return AXIA_OK;
+}
+
+int prepare_full_buffers(axia_ctx* ctx) { return ensure_full_buffers(ctx, true); }
+
+BsrReliableArgs make_reliable_args(axia_ctx* ctx, double rtol, double delta, long long max_iter) {
+  return BsrReliableArgs{bsr_mat<float>(ctx, ctx->d_bval32), bsr_mat<double>(ctx, ctx->d_bval64), (int)ctx->ndof,
+                         ctx->d_bdinv32, ctx->d_bf, ctx->d_xf, ctx->d_xf32, ctx->d_rf32, ctx->d_pf32, ctx->d_qf32,
+                         ctx->d_zf32, ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status,
+                         (PcgOut*)ctx->d_out, rtol, delta, max_iter, 2000000000ull};
 }
 
 static double bsr_residual(axia_ctx* ctx, const double* b, const double* x) {
@@ -485,7 +552,7 @@ int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_op
     const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.1;
     BsrReliableArgs P{bsr_mat<float>(ctx, ctx->d_bval32), bsr_mat<double>(ctx, ctx->d_bval64), (int)nd,
                       ctx->d_bdinv32, ctx->d_bf, ctx->d_xf, ctx->d_xf32, ctx->d_rf32, ctx->d_pf32, ctx->d_qf32,
-                      ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out, opts->rtol,
+                      ctx->d_zf32, ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out, opts->rtol,
                       delta, max_iter, limit_ns};
     AXIA_TRY(timed_launch(ctx, info, [&] { return launch_bsr_rel(ctx, P, lanes); }));
   }

@@ -59,7 +59,8 @@ struct GridBarrier {
   unsigned gen;
 };
 
-__device__ __forceinline__ bool grid_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns) {
+// Barrier over a group of nblk co-resident blocks (the whole grid: nblk = gridDim.x).
+__device__ __forceinline__ bool group_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns, unsigned nblk) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -67,7 +68,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, DevStatus* st, unsig
     unsigned g = ld_acquire_gpu(&bar->gen);
     __threadfence();
     unsigned arrived = atomicAdd(&bar->count, 1u);
-    if (arrived == gridDim.x - 1) {
+    if (arrived == nblk - 1) {
       bar->count = 0;
       __threadfence();
       st_release_gpu(&bar->gen, g + 1);
@@ -91,14 +92,19 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, DevStatus* st, unsig
   return s_ok != 0;
 }
 
+__device__ __forceinline__ bool grid_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns) {
+  return group_sync(bar, st, limit_ns, gridDim.x);
+}
+
 // Grid-wide barrier that also reduces.  Every block has stored its partials of
 // nv values at partials[(slot0 + k) * gridDim.x + blockIdx.x]; the last block
 // to arrive sums them in ascending block order (a fixed order, so every run
 // gives the same bits) and publishes totals[slot0 + k] before it releases the
 // others.  Same bounded wait as grid_sync.  After it returns, every thread may
 // read totals[] (with ld.cg: they were written by another block).
-__device__ __forceinline__ bool grid_reduce_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns,
-                                                 const double* partials, double* totals, int slot0, int nv) {
+__device__ __forceinline__ bool group_reduce_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns,
+                                                  const double* partials, double* totals, int slot0, int nv,
+                                                  unsigned nblk) {
   __shared__ int s_ok2;
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -108,7 +114,7 @@ __device__ __forceinline__ bool grid_reduce_sync(GridBarrier* bar, DevStatus* st
     if (lane == 0) {
       g = ld_acquire_gpu(&bar->gen);
       __threadfence();
-      last = atomicAdd(&bar->count, 1u) == gridDim.x - 1;
+      last = atomicAdd(&bar->count, 1u) == nblk - 1;
     }
     last = __shfl_sync(0xffffffffu, last, 0);
     int ok = 1;
@@ -116,7 +122,7 @@ __device__ __forceinline__ bool grid_reduce_sync(GridBarrier* bar, DevStatus* st
       __threadfence();
       for (int k = 0; k < nv; ++k) {
         double a = 0.0;
-        for (int j = lane; j < (int)gridDim.x; j += 32) a += __ldcg(partials + (size_t)(slot0 + k) * gridDim.x + j);
+        for (int j = lane; j < (int)nblk; j += 32) a += __ldcg(partials + (size_t)(slot0 + k) * nblk + j);
         a = warp_sum(a);
         if (lane == 0) totals[slot0 + k] = a;
       }
@@ -135,7 +141,7 @@ __device__ __forceinline__ bool grid_reduce_sync(GridBarrier* bar, DevStatus* st
           ok = 0;
           break;
         }
-        __nanosleep(32);
+        if (spins > 256) __nanosleep(16);
       }
     }
     if (lane == 0) {
@@ -146,6 +152,11 @@ __device__ __forceinline__ bool grid_reduce_sync(GridBarrier* bar, DevStatus* st
   }
   __syncthreads();
   return s_ok2 != 0;
+}
+
+__device__ __forceinline__ bool grid_reduce_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns,
+                                                 const double* partials, double* totals, int slot0, int nv) {
+  return group_reduce_sync(bar, st, limit_ns, partials, totals, slot0, nv, gridDim.x);
 }
 
 // Streaming (evict-first) loads for matrix data that is read once per sweep,
@@ -242,7 +253,7 @@ struct axia_ctx {
   size_t vec_capacity = 0;
   // full-DOF vectors of the node-block solve
   double *d_bf = nullptr, *d_xf = nullptr, *d_rf = nullptr, *d_pf = nullptr, *d_qf = nullptr;
-  float *d_xf32 = nullptr, *d_rf32 = nullptr, *d_pf32 = nullptr, *d_qf32 = nullptr;
+  float *d_xf32 = nullptr, *d_rf32 = nullptr, *d_pf32 = nullptr, *d_qf32 = nullptr, *d_zf32 = nullptr;
   size_t full_capacity = 0;
   // batched load cases ([ndof][32] blocks)
   double *d_mB = nullptr, *d_mX = nullptr;
@@ -250,12 +261,31 @@ struct axia_ctx {
   void* d_mout = nullptr;
   size_t batch_capacity = 0;
 
+  // multi-mesh solve: node ranges per mesh, CTA groups, captured graph
+  std::vector<int64_t> mesh_node0;    // [n_meshes+1] first node of each mesh
+  std::vector<int64_t> mesh_blocks;   // [n_meshes] node blocks of each mesh
+  std::vector<int> multi_ctas;        // [n_meshes] blocks of each group
+  unsigned char* d_mgroups = nullptr; // MeshGroup[n_meshes]
+  int* d_mcta = nullptr;              // group of every block
+  GridBarrier* d_mbars = nullptr;
+  double* d_mtotals = nullptr;
+  unsigned char* d_mouts = nullptr;   // PcgOut[n_meshes]
+  int multi_grid = 0, multi_lanes = 0;
+  void* multi_graph = nullptr;        // cudaGraphExec_t
+  const double* graph_f = nullptr;
+  double* graph_u = nullptr;
+  double graph_rtol = 0, graph_delta = 0;
+  long long graph_max_iter = 0;
+
   // SIMP compliance state (forward -> backward)
   double* d_rho = nullptr;      // [n_elem]
   double* d_energy = nullptr;   // [n_elem]
   double* d_grad = nullptr;     // [n_elem]
   double simp_p = 3.0, simp_e0 = 1.0;
   bool have_forward = false;
+
+  // stress recovery / reactions: per (element, local node) 6 stresses + 3 forces
+  double* d_rec = nullptr;      // [n_elem*nn*9]
 
   double ms_setup = 0.0, ms_assemble = 0.0;
   int64_t last_bad = -1;

@@ -48,8 +48,10 @@ __device__ __forceinline__ T group_sum(T v) {
 }
 
 // block-reduce up to two values and store them as this block's partials
+// (block `rank` of a group of nblk blocks; the whole grid by default)
 template <typename A>
-__device__ __forceinline__ void block_partials(A v0, A v1, int nv, double* partials, int slot0, int slot1) {
+__device__ __forceinline__ void block_partials(A v0, A v1, int nv, double* partials, int slot0, int slot1,
+                                               unsigned nblk = 0, unsigned rank = 0) {
   __shared__ A s_red[2][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   v0 = warp_sum(v0);
@@ -65,14 +67,68 @@ __device__ __forceinline__ void block_partials(A v0, A v1, int nv, double* parti
     a0 = warp_sum(a0);
     if (nv > 1) a1 = warp_sum(a1);
     if (lane == 0) {
-      partials[slot0 * gridDim.x + blockIdx.x] = (double)a0;
-      if (nv > 1) partials[slot1 * gridDim.x + blockIdx.x] = (double)a1;
+      if (nblk == 0) {
+        nblk = gridDim.x;
+        rank = blockIdx.x;
+      }
+      partials[slot0 * nblk + rank] = (double)a0;
+      if (nv > 1) partials[slot1 * nblk + rank] = (double)a1;
     }
   }
 }
 
 __device__ __forceinline__ double total(const double* totals, int slot) { return __ldcg(totals + slot); }
 
+
+// ---------------------------------------------------------------------------
+// Node-block (3x3) matrix and the mixed-precision argument pack (bsr.cu)
+// ---------------------------------------------------------------------------
+template <typename V>
+struct BsrMat {
+  int n_nodes;
+  const int* adj_ptr;  // [n_nodes+1]
+  const int* adj;      // [nb]
+  const V* val;        // [9][nb]
+  long long nb;
+};
+
+// one system of a multi-mesh solve: its block rows and its blocks
+struct MeshGroup {
+  int node0, node1;   // block rows [node0, node1)
+  int cta0, ncta;     // blocks [cta0, cta0 + ncta) of the launch
+  long long part_off; // offset of its partial-sum area
+};
+
+struct BsrReliableArgs {
+  BsrMat<float> M32;
+  BsrMat<double> M64;
+  int nd;
+  const float* dinv32;
+  const double* b;
+  double* x;
+  float* x32;
+  float* r32;
+  float* p32;
+  float* q32;
+  float* z32;
+  double* partials;
+  double* totals;
+  GridBarrier* bar;
+  DevStatus* st;
+  PcgOut* out;
+  double tol;
+  double delta;
+  long long max_iter;
+  unsigned long long limit_ns;
+};
+
+BsrReliableArgs make_reliable_args(axia_ctx* ctx, double rtol, double delta, long long max_iter);
+int group_kernel_capacity(axia_ctx* ctx, int lanes, int* per_sm);
+int launch_group_reliable(axia_ctx* ctx, BsrReliableArgs& P, const MeshGroup* groups, const int* cta_group,
+                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes);
+int launch_full_rhs(axia_ctx* ctx, const double* d_f);
+int launch_full_reconstruct(axia_ctx* ctx, double* d_u);
+int prepare_full_buffers(axia_ctx* ctx);
 
 // ---------------------------------------------------------------------------
 // Host helpers for the persistent launches

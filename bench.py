@@ -125,6 +125,16 @@ def bsr_pcg_iter_bytes(nblocks, n_nodes, vbytes):
     return (9 * vbytes + 4) * nblocks + 4 * (n_nodes + 1) + 2 * vbytes * nd + 11 * vbytes * nd
 
 
+def recover_bytes(n_elem, nn, n_nodes):
+    """Algorithmic bytes of stress recovery + reactions: per element the
+    connectivity twice, E once, 9 doubles per (element, node) written and read
+    back; per node coordinates, u, f and the incidence pointer read, stress,
+    strain, von Mises and reactions written."""
+    per_elem = 2 * 4 * nn + 8 + 2 * 72 * nn + 48
+    per_node = 24 + 24 + 24 + 8 + 48 + 48 + 8 + 24
+    return per_elem * n_elem + per_node * n_nodes
+
+
 def cpu_baseline(n=CPU_SAMPLE_N, threads=1):
     """The CPU restatement of the reference's *STATIC path (oracle/) on a
     bounded sample: the same block, loads and BCs at n^3, full path
@@ -140,6 +150,183 @@ def cpu_baseline(n=CPU_SAMPLE_N, threads=1):
             "sample": f"C3D8 {n}^3 block, same loads/BCs, full path to rtol {RTOL:g} "
                       f"({r.n_free} free DOFs, {r.iters} PCG iterations, {dt:.2f} s)",
             "seconds": dt, "iters": r.iters}
+
+
+class Timer:
+    """CUDA events on the stream the library launches on (torch's current stream)."""
+
+    def __init__(self, torch, stream):
+        self.torch, self.stream = torch, stream
+
+    def __call__(self, fn, warmup, steps):
+        torch = self.torch
+        out, ms = None, []
+        for k in range(warmup + steps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(self.stream):
+                a.record(self.stream)
+                out = fn()
+                b.record(self.stream)
+            b.synchronize()
+            if k >= warmup:
+                ms.append(a.elapsed_time(b))
+        return sum(ms) / len(ms), out
+
+
+def _gpu_env(args):
+    import torch
+    from axia_gpu import GpuContext
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ctx = GpuContext(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    return torch, ctx, stream, Timer(torch, stream), local
+
+
+def _line(args, workload, value, ms, extra):
+    out = {"metric": METRIC, "value": value, "unit": "MDOF/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "data": "synthetic (seeded structured hexahedral meshes)",
+           "config": {"workload": workload}}
+    out.update(extra)
+    print(json.dumps(out))
+
+
+def run_c3(args):
+    """C3D20 50^3 block, base clamped, random top traction: mixed (FP32 node-block
+    inner CG, FP64 reliable updates) vs FP64 CSR PCG, both to rtol 1e-10."""
+    import numpy as np
+    from axia_gpu import _lib as L, meshgen
+    torch, ctx, stream, timer, local = _gpu_env(args)
+    n = args.n if args.n != 100 else 50
+    m = meshgen.block_c3d20_traction(n=n)
+    ctx.setup(m)
+    f = torch.from_numpy(ctx.load_vector(m)).to(f"cuda:{local}")
+    u64, umx = torch.empty_like(f), torch.empty_like(f)
+
+    def step64():
+        ctx.assemble_ex(L.ASM_CSR64)
+        return ctx.solve_device(f.data_ptr(), u64.data_ptr(), rtol=RTOL, spmv_lanes=args.lanes64)
+
+    def stepmx():
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        return ctx.solve_device(f.data_ptr(), umx.data_ptr(), rtol=RTOL, precision=L.PREC_MIXED,
+                                refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta, matrix_format=L.FORMAT_BSR3,
+                                spmv_lanes=args.lanes32)
+    ms64, i64 = timer(step64, args.warmup, args.steps)
+    msmx, imx = timer(stepmx, args.warmup, args.steps)
+    rel = float(torch.linalg.norm(umx - u64) / torch.linalg.norm(u64))
+    nf = ctx.n_free
+    _line(args, f"C3D20 block {n}^3, 27-point Gauss, E=70000 nu=0.33, base clamped, top traction N(0,1)",
+          nf / (msmx * 1e-3) / 1e6, msmx,
+          {"dtype": "f32+f64", "config": {"workload": f"C3D20 {n}^3", "n_free": nf, "nnz_kff": ctx.nnz,
+                                          "node_blocks": ctx.n_blocks(), "rtol": RTOL},
+           "fp64": {"value": nf / (ms64 * 1e-3) / 1e6, "ms_per_step": ms64, "iters": i64.iters,
+                    "ms_assemble": i64.ms_assemble, "true_rel_residual": i64.true_residual / i64.bnorm},
+           "mixed": {"ms_per_step": msmx, "inner_iters": imx.iters, "reliable_updates": imx.outer_iters,
+                     "ms_assemble": imx.ms_assemble, "true_rel_residual": imx.true_residual / imx.bnorm,
+                     "rel_err_vs_fp64": rel},
+           "speedup_mixed_vs_fp64": ms64 / msmx})
+
+
+def run_c4a(args):
+    """C3D8 80^3 block with 32 random surface load cases in one batched launch."""
+    from axia_gpu import _lib as L, meshgen
+    torch, ctx, stream, timer, local = _gpu_env(args)
+    n = args.n if args.n != 100 else 80
+    m = meshgen.block_c3d8_multiload(n=n, nrhs=32)
+    ctx.setup(m)
+    F = torch.from_numpy(m.cload_batch).to(f"cuda:{local}")
+    U = torch.empty_like(F)
+
+    def step():
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        return ctx.solve_batched_device(32, F.data_ptr(), U.data_ptr(), rtol=RTOL, inner_rtol=args.delta)
+    ms, (info, rel) = timer(step, args.warmup, args.steps)
+    # one case through the single-RHS mixed path for comparison
+    u1 = torch.empty(m.ndof, dtype=torch.float64, device=f"cuda:{local}")
+
+    def single():
+        return ctx.solve_device(F[0].data_ptr(), u1.data_ptr(), rtol=RTOL, precision=L.PREC_MIXED,
+                                refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta, matrix_format=L.FORMAT_BSR3)
+    ms1, i1 = timer(single, 1, 2)
+    err = float(torch.linalg.norm(U[0] - u1) / torch.linalg.norm(u1))
+    nf = ctx.n_free
+    _line(args, f"C3D8 block {n}^3, x=0 clamped, 32 load cases (5% of surface nodes, N(0,1))",
+          32 * nf / (ms * 1e-3) / 1e6, ms,
+          {"dtype": "f32+f64", "config": {"workload": f"C3D8 {n}^3 x 32 load cases", "n_free": nf, "rhs": 32},
+           "batched": {"iters": info.iters, "reliable_updates": info.outer_iters, "max_rel_residual": float(rel.max()),
+                       "ms_kernel": info.ms_pcg_kernel},
+           "single_case": {"ms": ms1, "iters": i1.iters, "rel_err_batched_vs_single": err},
+           "speedup_vs_32_single_solves": 32 * ms1 / ms})
+
+
+def run_c4b(args):
+    """64 independent C3D8 cubes (edges 10..40) in one cooperative launch from a CUDA graph."""
+    import numpy as np
+    from axia_gpu import _lib as L, meshgen
+    torch, ctx, stream, timer, local = _gpu_env(args)
+    cubes = meshgen.cube_family(count=64, lo=10, hi=40)
+    ctx.setup_multi(cubes)
+    f = torch.from_numpy(np.concatenate([c.cload for c in cubes])).to(f"cuda:{local}")
+    u = torch.empty_like(f)
+
+    def step():
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        return ctx.solve_multi_device(f.data_ptr(), u.data_ptr(), rtol=RTOL, inner_rtol=args.delta)
+    ms, (info, rel, its) = timer(step, args.warmup, args.steps)
+    nf = ctx.n_free
+    _line(args, "64 C3D8 cubes, edge counts U{10..40} (seeded), x=0 clamped, random surface loads",
+          nf / (ms * 1e-3) / 1e6, ms,
+          {"dtype": "f32+f64", "config": {"workload": "64 cubes", "n_free": nf, "meshes": 64,
+                                          "sizes": [int(c.shape[0]) for c in cubes]},
+           "multi": {"max_iters": int(its.max()), "min_iters": int(its.min()), "max_rel_residual": float(rel.max()),
+                     "ms_kernel": info.ms_pcg_kernel, "ms_assemble": info.ms_assemble}})
+
+
+def run_c5(args):
+    """SIMP beam 100x50x50: FP64 forward solve, adjoint gradient of all elements,
+    checked against central differences (h = 1e-6) on 20 seeded elements."""
+    import numpy as np
+    from axia_gpu import _lib as L, meshgen
+    from oracle import oracle as O
+    torch, ctx, stream, timer, local = _gpu_env(args)
+    m = meshgen.simp_beam(nx=100, ny=50, nz=50)
+    ctx.setup(m)
+    f = ctx.load_vector(m)
+    t0 = time.perf_counter()
+    u, c, info = ctx.compliance_forward(m.rho, m.pexp, m.e0, f, rtol=1e-12)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g = ctx.compliance_backward()
+    t_bwd = time.perf_counter() - t0
+    rng = np.random.default_rng(20261203)
+    pick = rng.choice(m.n_elem, 20, replace=False)
+    h = 1e-6
+    worst_exact, worst_direct = 0.0, 0.0
+    for k in pick:
+        rp, rm = m.rho.copy(), m.rho.copy()
+        rp[k] += h
+        rm[k] -= h
+        up, cp, _ = ctx.compliance_forward(rp, m.pexp, m.e0, f, rtol=1e-12)
+        um, cm, _ = ctx.compliance_forward(rm, m.pexp, m.e0, f, rtol=1e-12)
+        d = (3 * m.conn[k][:, None] + np.arange(3)).ravel()
+        ke, _ = O.element_ke(m.coords[m.conn[k]], 1.0, m.nu)
+        dc = -(m.e0 * rp[k] ** m.pexp - m.e0 * rm[k] ** m.pexp) * (up[d] @ ke @ um[d])
+        worst_exact = max(worst_exact, abs(dc / (2 * h) - g[k]) / abs(g[k]))
+        worst_direct = max(worst_direct, abs((cp - cm) / (2 * h) - g[k]) / abs(g[k]))
+    m.e_elem = m.e0 * m.rho ** m.pexp
+    g_cpu = O.compliance_grad(m, m.rho, m.pexp, m.e0, u)
+    nf = ctx.n_free
+    _line(args, "SIMP beam 100x50x50 C3D8, E=rho^3, rho~U[0.3,1], tip load", nf / t_fwd / 1e6, t_fwd * 1e3,
+          {"dtype": "f64", "config": {"workload": "C3D8 100x50x50 SIMP", "n_free": nf, "elements": m.n_elem},
+           "forward": {"iters": info.iters, "ms_solve": info.ms_solve, "compliance": c},
+           "backward_ms": t_bwd * 1e3,
+           "gradient_vs_cpu_analytic_max_rel": float(np.abs(g - g_cpu).max() / np.abs(g_cpu).max()),
+           "fd_20_elements": {"h": h, "max_rel_err_exact_difference": worst_exact,
+                              "max_rel_err_direct_difference": worst_direct}})
 
 
 def run_reference(args):
@@ -183,11 +370,16 @@ def main():
     ap.add_argument("--only", choices=["mixed", "fp64", "spmv"], default=None,
                     help="run one solve (or SpMV sweep) once and exit: the profiling entry")
     ap.add_argument("--max-iter", type=int, default=0, help="with --only: cap the CG iterations")
+    ap.add_argument("--workload", choices=["c2", "c3", "c4a", "c4b", "c5"], default="c2",
+                    help="c2 (default): the 100^3 C3D8 block; others: the remaining configurations")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "c2":
+        {"c3": run_c3, "c4a": run_c4a, "c4b": run_c4b, "c5": run_c5}[args.workload](args)
         return
 
     import numpy as np
@@ -202,7 +394,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    from axia_gpu import GpuContext, _lib as L, meshgen
+    from axia_gpu import GpuContext, _lib as L, meshgen, replicas
 
     model = meshgen.block_c3d8_pressure(n=args.n)
     ctx = GpuContext(local)
@@ -266,10 +458,7 @@ def main():
         barrier()
         launches = ctx.kernel_launches() - l0
         ms = sum(times) / len(times)
-        if dist is not None:
-            t = torch.tensor([ms], device=f"cuda:{local}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replicas.max_over_ranks(ms, dist, f"cuda:{local}")
         return ms, infos, launches
 
     fp64_kw = dict(precision=L.PREC_FP64, spmv_lanes=args.lanes64, matrix_format=L.FORMAT_CSR)
@@ -326,6 +515,24 @@ def main():
     for v in spmv.values():
         v["frac_of_hbm"] = v["gbs"] / hbm
 
+    # post-solve recovery of the mixed solution: nodal stress, strain, von Mises,
+    # element means and reactions K u - f (two kernels)
+    nn_ = model.n_nodes
+    rec_out = {k: torch.empty(sz, dtype=torch.float64, device=f"cuda:{local}")
+               for k, sz in (("stress", 6 * nn_), ("strain", 6 * nn_), ("vm", nn_), ("rf", nd),
+                             ("elem", 6 * model.n_elem))}
+    e_ref = float(model.e_elem[0])
+
+    def recover():
+        ctx.recover_device(umx.data_ptr(), f_dev.data_ptr(), e_ref, rec_out["stress"].data_ptr(),
+                           rec_out["strain"].data_ptr(), rec_out["vm"].data_ptr(), rec_out["rf"].data_ptr(),
+                           rec_out["elem"].data_ptr())
+    ms_rec, _ = Timer(torch, stream)(recover, 3, 10)
+    rec_bytes = recover_bytes(model.n_elem, model.nn, nn_)
+    recovery = {"ms": ms_rec, "bytes": rec_bytes, "gbs": rec_bytes / (ms_rec * 1e-3) / 1e9,
+                "kernels": "element_recover_kernel<8,8> + k_recover_nodes",
+                "bound": "fp64 pipe (about 7 kFLOP per C3D8 element)"}
+
     # accuracy: mixed vs FP64 solution, both with true FP64 residual <= 1e-10 ||b||
     u64h = u64.cpu().numpy()
     rel_mx = float(np.linalg.norm(umx.cpu().numpy() - u64h) / np.linalg.norm(u64h))
@@ -370,10 +577,7 @@ def main():
             if k >= args.warmup:
                 ts.append(dt)
         e2e_s = sum(ts) / len(ts)
-        if dist is not None:
-            t = torch.tensor([e2e_s], device=f"cuda:{local}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = replicas.max_over_ranks(e2e_s, dist, f"cuda:{local}")
         e2e = {"value": n / e2e_s / 1e6 * world, "unit": "MDOF/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
 
@@ -411,6 +615,7 @@ def main():
         "speedup_mixed_csr_vs_fp64": ms64 / msmc,
         "setup_ms": setup_s * 1e3,
         "spmv": spmv,
+        "recovery": recovery,
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
                      "traffic": None, "kernel": "pcg_bsr_reliable_kernel (FP32 node-block CG + FP64 updates)",
                      "peak_source": f"{pk_kind} hbm_gbs", "bytes_per_launch": bytes32, "ms_per_launch": k32_ms},

@@ -256,6 +256,54 @@ AXIA_API int32_t axia_gpu_solve_batched(axia_ctx* ctx, int32_t nrhs, const doubl
 AXIA_API int32_t axia_gpu_solve_batched_device(axia_ctx* ctx, int32_t nrhs, const double* F_dev, double* U_dev,
                                                const axia_solve_opts* opts, axia_solve_info* info, double* rel_res);
 
+/* Several independent meshes in one context (no reference counterpart: the
+ * reference solves each model on its own).  The meshes (same nn, reduced and
+ * nu) are concatenated, node and element indices offset per mesh, and set up
+ * as one; bc_dof[k] / bc_val[k] (n_bc[k] entries) are mesh k's own DOF
+ * indices.  Assemble afterwards with AXIA_ASM_BSR64 | AXIA_ASM_BSR32.  The
+ * concatenated full-DOF vector has mesh k's DOFs at 3 * (first node of k). */
+AXIA_API int32_t axia_gpu_setup_multi(axia_ctx* ctx, int32_t n_meshes, const axia_mesh* meshes,
+                                      const int64_t* n_bc, const int64_t* const* bc_dof,
+                                      const double* const* bc_val);
+
+/* Solves every mesh of axia_gpu_setup_multi in one cooperative launch,
+ * replayed from a captured CUDA graph: each mesh gets its own group of blocks
+ * and runs its own mixed-precision CG (FP32 node-block CG, FP64 reliable
+ * updates every opts->inner_rtol drop) to opts->rtol.  f_full / u_full are the
+ * concatenated vectors (host here, device in the _device form).  rel_res and
+ * iters (n_meshes entries, may be NULL) receive each mesh's relative
+ * residual and iteration count; info->bad_index names a failing mesh. */
+AXIA_API int32_t axia_gpu_solve_multi(axia_ctx* ctx, const double* f_full, double* u_full,
+                                      const axia_solve_opts* opts, axia_solve_info* info, double* rel_res,
+                                      int64_t* iters);
+AXIA_API int32_t axia_gpu_solve_multi_device(axia_ctx* ctx, const double* f_full_dev, double* u_full_dev,
+                                             const axia_solve_opts* opts, axia_solve_info* info, double* rel_res,
+                                             int64_t* iters);
+
+/* Post-solve recovery for the displacement u_full [ndof] of the set-up mesh
+ * (replaces the loops after the solve in solve_linear,
+ * solver/src/analysis.rs:1027-1035 and 1061-1174):
+ *   rf          [ndof]        K u - f over all DOFs (reactions at prescribed
+ *                             DOFs); f_full NULL means f = 0
+ *   stress      [n_nodes][6]  nodal averaged stresses, Voigt xx yy zz xy yz zx
+ *                             (element nodal stresses hex8_nodal_stress
+ *                             elem.rs:744-779 / hex20_nodal_stress
+ *                             quadratic.rs:148-225, summed per node and
+ *                             divided by the node's element count)
+ *   strain      [n_nodes][6]  from the averaged stress with modulus e_strain
+ *                             and the mesh's nu (engineering shears; the
+ *                             reference takes its first material's E)
+ *   vm          [n_nodes]     von Mises of the averaged stress (elem.rs:651-660)
+ *   elem_stress [n_elem][6]   mean of each element's nodal stresses
+ * Any output may be NULL.  Host arrays; the _device form takes device
+ * pointers, runs on the context's stream and returns when the work is queued
+ * and its status read. */
+AXIA_API int32_t axia_gpu_recover(axia_ctx* ctx, const double* u_full, const double* f_full, double e_strain,
+                                  double* stress, double* strain, double* vm, double* rf, double* elem_stress);
+AXIA_API int32_t axia_gpu_recover_device(axia_ctx* ctx, const double* u_full_dev, const double* f_full_dev,
+                                         double e_strain, double* stress, double* strain, double* vm, double* rf,
+                                         double* elem_stress);
+
 /* Sizes of the assembled system: n_free and nnz. */
 AXIA_API int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz);
 

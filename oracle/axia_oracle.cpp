@@ -553,6 +553,109 @@ double residual_of(const Csr& a, const double* x, const double* b) {
   return std::sqrt(s);
 }
 
+// elem.rs:725-742
+void sigma_from_b(const double* b, int nrow, int n, const double* d, const double* ue, double* sig) {
+  double eps[6];
+  for (int r = 0; r < nrow; ++r) {
+    double t = 0.0;
+    for (int j = 0; j < n; ++j) t += b[r * n + j] * ue[j];
+    eps[r] = t;
+  }
+  for (int r = 0; r < nrow; ++r) {
+    double t = 0.0;
+    for (int k = 0; k < nrow; ++k) t += d[r * nrow + k] * eps[k];
+    sig[r] = t;
+  }
+}
+
+// elem.rs:744-779: Gauss-point stresses at HEX_XI * G2, extrapolated with the
+// trilinear shapes evaluated at HEX_XI * sqrt(3)
+int hex8_nodal_stress(const double* xyz, const double* ue, double e, double nu, double out[8][6]) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const int n = 24;
+  double gsig[8][6];
+  std::vector<double> b(6 * n);
+  for (int i = 0; i < 8; ++i) {
+    double N[8], dn[8][3], dndx[8][3], det;
+    hex8_shape(HEX_XI[i][0] * G2, HEX_XI[i][1] * G2, HEX_XI[i][2] * G2, N, dn);
+    st = hex_dndx<8>(xyz, dn, dndx, &det);
+    if (st) return st;
+    std::fill(b.begin(), b.end(), 0.0);
+    fill_b3(b.data(), 8, dndx);
+    sigma_from_b(b.data(), 6, n, d, ue, gsig[i]);
+  }
+  const double s3 = std::sqrt(3.0);
+  for (int a = 0; a < 8; ++a) {
+    double N[8], dn[8][3];
+    hex8_shape(HEX_XI[a][0] * s3, HEX_XI[a][1] * s3, HEX_XI[a][2] * s3, N, dn);
+    for (int c = 0; c < 6; ++c) {
+      double v = 0.0;
+      for (int g = 0; g < 8; ++g) v += N[g] * gsig[g][c];
+      out[a][c] = v;
+    }
+  }
+  return OK;
+}
+
+// quadratic.rs:227-244
+void lagrange1d(const double* pts, int n, double x, double* w) {
+  for (int i = 0; i < n; ++i) {
+    w[i] = 1.0;
+    for (int j = 0; j < n; ++j) {
+      if (i == j) continue;
+      w[i] *= (x - pts[j]) / (pts[i] - pts[j]);
+    }
+  }
+}
+
+// quadratic.rs:148-171 + hex20_extrapolate 205-225
+int hex20_nodal_stress(const double* xyz, const double* ue, double e, double nu, bool reduced, double out[20][6]) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const int n = 60;
+  std::vector<double> gp, b(6 * n);
+  hex_gauss(reduced, gp);
+  const int ng = (int)gp.size() / 4;
+  std::vector<double> gsig((size_t)ng * 6);
+  for (int g = 0; g < ng; ++g) {
+    double N[20], dn[20][3], dndx[20][3], det;
+    hex20_shape(gp[4 * g], gp[4 * g + 1], gp[4 * g + 2], N, dn);
+    st = hex_dndx<20>(xyz, dn, dndx, &det);
+    if (st) return st;
+    std::fill(b.begin(), b.end(), 0.0);
+    fill_b3(b.data(), 20, dndx);
+    sigma_from_b(b.data(), 6, n, d, ue, &gsig[6 * g]);
+  }
+  const double p2[2] = {-G2, G2};
+  const double* pts = reduced ? p2 : G3;
+  const int n1 = reduced ? 2 : 3;
+  for (int a = 0; a < 20; ++a) {
+    double lx[3], ly[3], lz[3];
+    lagrange1d(pts, n1, HEX20_XI[a][0], lx);
+    lagrange1d(pts, n1, HEX20_XI[a][1], ly);
+    lagrange1d(pts, n1, HEX20_XI[a][2], lz);
+    for (int c = 0; c < 6; ++c) out[a][c] = 0.0;
+    int idx = 0;
+    for (int i = 0; i < n1; ++i)
+      for (int j = 0; j < n1; ++j)
+        for (int k = 0; k < n1; ++k, ++idx) {
+          const double w = lx[i] * ly[j] * lz[k];
+          for (int c = 0; c < 6; ++c) out[a][c] += w * gsig[6 * idx + c];
+        }
+  }
+  return OK;
+}
+
+// elem.rs:651-660
+double von_mises(const double* s) {
+  const double sx = s[0], sy = s[1], sz = s[2], txy = s[3], tyz = s[4], tzx = s[5];
+  return std::sqrt(0.5 * ((sx - sy) * (sx - sy) + (sy - sz) * (sy - sz) + (sz - sx) * (sz - sx)) +
+                   3.0 * (txy * txy + tyz * tyz + tzx * tzx));
+}
+
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -828,6 +931,75 @@ int or_solve_kff(int64_t n, int64_t nt, const int64_t* ti, const int64_t* tj, co
   info[0] = (double)iters;
   info[1] = res;
   return st;
+}
+
+// Nodal averaged stresses (analysis.rs:1061-1153 without thermal terms):
+// element nodal stresses (hex8_nodal_stress / hex20_nodal_stress), summed per
+// node in element order and divided by the number of contributing elements;
+// von Mises per node (elem.rs:651-660).  stress [n_nodes][6], vm [n_nodes],
+// emean [n_elem][6] = mean of the element's nodal stresses ("stress_gp",
+// analysis.rs:1141-1152); vm and emean may be null.
+int or_nodal_stress(int64_t n_nodes, const double* coords, int nn, int reduced, int64_t n_elem, const int32_t* conn,
+                    const double* e_elem, double nu, const double* u_full, double* stress, double* vm, double* emean,
+                    int64_t* bad) {
+  std::vector<double> acc((size_t)n_nodes * 6, 0.0), cnt(n_nodes, 0.0);
+  double xyz[60], ue[60], sn[20][6];
+  for (int64_t e = 0; e < n_elem; ++e) {
+    const int32_t* c = conn + e * nn;
+    for (int a = 0; a < nn; ++a)
+      for (int q = 0; q < 3; ++q) {
+        xyz[3 * a + q] = coords[3 * (int64_t)c[a] + q];
+        ue[3 * a + q] = u_full[3 * (int64_t)c[a] + q];
+      }
+    int st = nn == 8 ? hex8_nodal_stress(xyz, ue, e_elem[e], nu, sn)
+                     : hex20_nodal_stress(xyz, ue, e_elem[e], nu, reduced != 0, sn);
+    if (st) {
+      *bad = e;
+      return st;
+    }
+    for (int a = 0; a < nn; ++a) {
+      for (int k = 0; k < 6; ++k) acc[6 * (size_t)c[a] + k] += sn[a][k];
+      cnt[c[a]] += 1.0;
+    }
+    if (emean)
+      for (int k = 0; k < 6; ++k) {
+        double m = 0.0;
+        for (int a = 0; a < nn; ++a) m += sn[a][k] / (double)nn;
+        emean[6 * e + k] = m;
+      }
+  }
+  for (int64_t i = 0; i < n_nodes; ++i) {
+    for (int k = 0; k < 6; ++k) stress[6 * i + k] = cnt[i] > 0.0 ? acc[6 * i + k] / cnt[i] : 0.0;
+    if (vm) vm[i] = von_mises(stress + 6 * i);
+  }
+  return OK;
+}
+
+// Reactions K u - f over the raw element triplets (analysis.rs:1027-1035).
+int or_reactions(int64_t n_nodes, const double* coords, int nn, int reduced, int64_t n_elem, const int32_t* conn,
+                 const double* e_elem, double nu, const double* u_full, const double* f_full, double* rf,
+                 int64_t* bad) {
+  const int m = 3 * nn;
+  std::vector<double> ke((size_t)m * m), ku(3 * (size_t)n_nodes, 0.0);
+  double xyz[60], vol;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    const int32_t* c = conn + e * nn;
+    for (int a = 0; a < nn; ++a)
+      for (int q = 0; q < 3; ++q) xyz[3 * a + q] = coords[3 * (int64_t)c[a] + q];
+    int st = element_ke(nn, xyz, e_elem[e], nu, reduced, ke.data(), &vol);
+    if (st) {
+      *bad = e;
+      return st;
+    }
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) {
+        const double v = ke[(size_t)i * m + j];
+        if (std::fabs(v) > 0.0)
+          ku[3 * (size_t)c[i / 3] + i % 3] += v * u_full[3 * (size_t)c[j / 3] + j % 3];
+      }
+  }
+  for (int64_t d = 0; d < 3 * n_nodes; ++d) rf[d] = ku[d] - f_full[d];
+  return OK;
 }
 
 // ||K x - b|| <= 1e-8 max(||b||, 1) + 1e-10 (sparse_native.rs:1572-1578)

@@ -65,6 +65,10 @@ def lib():
         L.or_solve_kff.argtypes = [C.c_int64, C.c_int64, _i64, _i64, _d, _d, C.c_int, C.c_double,
                                    C.c_int64, C.c_int, _d, _d]
         L.or_residual_ok.argtypes = [C.c_double, C.c_double]
+        L.or_nodal_stress.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int64, _i32, _d, C.c_double, _d, _d,
+                                      C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]
+        L.or_reactions.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int64, _i32, _d, C.c_double, _d, _d, _d,
+                                   C.POINTER(C.c_int64)]
         L.or_compliance_grad.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int64, _i32, _d, C.c_double,
                                          C.c_double, C.c_double, _d, _d, C.POINTER(C.c_int64)]
         _lib = L
@@ -198,6 +202,50 @@ def solve_kff(n, ti, tj, tv, rhs, solver=SOLVER_PCG, tol=1e-8, max_iter=0, nthre
     if st:
         raise OracleError(st, "solve_kff")
     return x, int(info[0]), float(info[1])
+
+
+def nodal_stress(model, u_full, elem_mean=False):
+    """Nodal averaged Voigt stresses [n_nodes][6] and von Mises [n_nodes]
+    (and, with elem_mean, the element means [n_elem][6])."""
+    st_ = np.zeros((model.n_nodes, 6))
+    vm = np.zeros(model.n_nodes)
+    em = np.zeros((model.n_elem, 6))
+    bad = C.c_int64(-1)
+    st = lib().or_nodal_stress(model.n_nodes, np.ascontiguousarray(model.coords).ravel(), model.nn,
+                               int(model.reduced), model.n_elem,
+                               np.ascontiguousarray(model.conn, dtype=np.int32).ravel(),
+                               np.ascontiguousarray(model.e_elem, np.float64), float(model.nu),
+                               np.ascontiguousarray(u_full, np.float64), st_.ravel(), vm.ctypes.data,
+                               em.ctypes.data, C.byref(bad))
+    if st:
+        raise OracleError(st, f"nodal_stress element {bad.value}")
+    return (st_, vm, em) if elem_mean else (st_, vm)
+
+
+def nodal_strain(stress, e, nu):
+    """Strain from the averaged stress (analysis.rs:1160-1172)."""
+    s = np.asarray(stress, dtype=np.float64)
+    tr = s[:, 0] + s[:, 1] + s[:, 2]
+    out = np.zeros_like(s)
+    for c in range(3):
+        out[:, c] = ((1.0 + nu) * s[:, c] - nu * tr) / e
+    g2 = e / (1.0 + nu)
+    out[:, 3:] = s[:, 3:] / g2
+    return out
+
+
+def reactions(model, u_full, f_full):
+    """K u - f over all DOFs (reactions at prescribed DOFs)."""
+    rf = np.zeros(model.ndof)
+    bad = C.c_int64(-1)
+    st = lib().or_reactions(model.n_nodes, np.ascontiguousarray(model.coords).ravel(), model.nn, int(model.reduced),
+                            model.n_elem, np.ascontiguousarray(model.conn, dtype=np.int32).ravel(),
+                            np.ascontiguousarray(model.e_elem, np.float64), float(model.nu),
+                            np.ascontiguousarray(u_full, np.float64), np.ascontiguousarray(f_full, np.float64), rf,
+                            C.byref(bad))
+    if st:
+        raise OracleError(st, f"reactions element {bad.value}")
+    return rf
 
 
 def residual_ok(residual, bnorm):

@@ -30,6 +30,10 @@ PINS = {
                                      "source": "solver/src/lib.rs:464-496 (sparse_backends_agree_on_c3d8_patch)"},
     "patch_c3d20_mean_ux": {"value": -0.01, "tol": 1e-5, "nodes_1based": [2, 3, 6, 7],
                             "source": "solver/src/lib.rs:751-763 (patch_test_c3d20)"},
+    "patch_c3d8_mean_sxx": {"value": 210.0, "tol": 1e-3,
+                            "source": "solver/src/lib.rs:440-446 (patch_test_c3d8: mean nodal sxx, vm > 0)"},
+    "patch_c3d20_mean_sxx": {"value": -210.0, "tol": 1.0,
+                             "source": "solver/src/lib.rs:764-772 (patch_test_c3d20: mean nodal sxx)"},
     "hex20_partition_of_unity": {"value": 1.0, "tol": 1e-12,
                                  "source": "solver/src/quadratic.rs:890-894 (hex20_partition)"},
     "quad8_partition_of_unity": {"value": 1.0, "tol": 1e-12,
@@ -70,6 +74,9 @@ def main():
     r = O.solve_static(m, solver=O.SOLVER_CHOLESKY)
     v["cantilever_20x4x4"] = {"n_free": r.n_free, "nnz_kff": r.nnz, "tip_uz_min": float(r.u[2::3].min()),
                               "u": r.u.tolist(), "solver": "oracle dense Cholesky (linalg.rs:78-117)"}
+    stress, vm = O.nodal_stress(m, r.u)
+    rf = O.reactions(m, r.u, r.f)
+    v["cantilever_20x4x4"].update({"vm": vm.tolist(), "sxx": stress[:, 0].tolist(), "rf": rf.tolist()})
     fe = O.face_pressure(distorted_hex8(), 4, 1.0)
     v["hex8_face_p4"] = {"fe": fe.tolist()}
     fe = O.face_pressure(distorted_hex20(), 2, 1.0)

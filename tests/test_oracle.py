@@ -128,3 +128,37 @@ def test_prescribed_nonzero_and_last_bc_wins():
     assert np.allclose(r.u[3 * tip], 0.01)
     # reactions at the clamp balance the reactions at the driven face
     assert abs(r.rf[0::3].sum()) < 1e-8 * np.abs(r.rf).max()
+
+
+def test_patch_stress_pins():
+    """Mean nodal sxx of the reference's patch tests (lib.rs:440-446, 764-772)."""
+    m = meshgen.patch_c3d8()
+    r = O.solve_static(m, solver=O.SOLVER_CHOLESKY)
+    s, vm = O.nodal_stress(m, r.u)
+    pin = PINS["patch_c3d8_mean_sxx"]
+    assert abs(s[:, 0].mean() - pin["value"]) < pin["tol"]
+    assert vm[0] > 0.0
+    m = meshgen.patch_c3d20()
+    r = O.solve_static(m, solver=O.SOLVER_CHOLESKY)
+    s, _ = O.nodal_stress(m, r.u)
+    pin = PINS["patch_c3d20_mean_sxx"]
+    assert abs(s[:, 0].mean() - pin["value"]) < pin["tol"]
+
+
+def test_reactions_balance_and_golden():
+    """K u - f vanishes at free DOFs and the reactions balance the applied load."""
+    m = meshgen.cantilever_c3d8()
+    r = O.solve_static(m, solver=O.SOLVER_CHOLESKY, reactions=True)
+    rf = O.reactions(m, r.u, r.f)
+    free = np.ones(m.ndof, bool)
+    free[m.bc_dof] = False
+    scale = np.abs(r.f).max()
+    assert np.abs(rf[free]).max() < 1e-8 * scale
+    for q in range(3):
+        # rigid translations are in the null space of K: sum of reactions = -sum of loads
+        assert abs(rf[q::3].sum() + r.f[q::3].sum()) < 1e-8 * scale * m.n_nodes
+    np.testing.assert_allclose(rf, r.rf, rtol=0, atol=1e-9 * scale)
+    g = VEC["cantilever_20x4x4"]
+    np.testing.assert_allclose(rf, g["rf"], rtol=0, atol=1e-9 * scale)
+    s, vm = O.nodal_stress(m, np.array(g["u"]))
+    np.testing.assert_allclose(vm, g["vm"], rtol=1e-12, atol=1e-12 * np.abs(vm).max())
