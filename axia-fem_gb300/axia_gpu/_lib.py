@@ -56,7 +56,7 @@ class Mesh(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iter", C.c_int64), ("precision", C.c_int32),
                 ("refine_mode", C.c_int32), ("inner_rtol", C.c_double), ("max_outer", C.c_int32),
-                ("spmv_lanes", C.c_int32), ("matrix_format", C.c_int32), ("reserved", C.c_int32)]
+                ("spmv_lanes", C.c_int32), ("matrix_format", C.c_int32), ("spmv_vec", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -89,7 +89,7 @@ SIGNATURES = [
     ("axia_gpu_set_stream", C.c_int32, [_P, _P]),
     ("axia_gpu_kernel_launches", C.c_int64, [_P]),
     ("axia_gpu_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32]),
-    ("axia_gpu_bsr_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32]),
+    ("axia_gpu_bsr_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32, C.c_int32]),
     ("axia_gpu_node_blocks", C.c_int64, [_P]),
     ("axia_gpu_setup_multi", C.c_int32, [_P, C.c_int32, C.POINTER(Mesh), _P, _P, _P]),
     ("axia_gpu_solve_multi", C.c_int32, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), _P, _P]),
@@ -99,6 +99,10 @@ SIGNATURES = [
                                                   _P]),
     ("axia_gpu_element_energy", C.c_int32, [_P, _P, _P, _P]),
     ("axia_gpu_recover", C.c_int32, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P]),
+    ("axia_gpu_solve_triplets", C.c_int32, [_P, C.c_int64, C.c_int64, _P, _P, _P, _P, _P, C.POINTER(SolveOpts),
+                                            C.POINTER(SolveInfo)]),
+    ("axia_gpu_solve_csr", C.c_int32, [_P, C.c_int64, _P, _P, _P, _P, _P, C.POINTER(SolveOpts),
+                                       C.POINTER(SolveInfo)]),
     ("axia_gpu_recover_device", C.c_int32, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P]),
     ("axia_gpu_compliance_forward", C.c_int32, [_P, _P, C.c_double, C.c_double, _P, _P, C.POINTER(C.c_double),
                                                 C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),

@@ -76,10 +76,13 @@ class GpuContext:
                    L.ptr(self._conn), L.ptr(self._e), 0.0, float(model.nu))
         self._check(self.lib.axia_gpu_setup(self.h, C.byref(m), self._bc_dof.shape[0], L.ptr(self._bc_dof),
                                             L.ptr(self._bc_val)), "setup")
+        self._refresh_sizes()
+        return self
+
+    def _refresh_sizes(self):
         n, nnz = C.c_int64(), C.c_int64()
         self.lib.axia_gpu_system_size(self.h, C.byref(n), C.byref(nnz))
         self.n_free, self.nnz = n.value, nnz.value
-        return self
 
     def setup_multi(self, models):
         """Several independent meshes as one context (concatenated node and element lists)."""
@@ -158,9 +161,9 @@ class GpuContext:
 
     @staticmethod
     def opts(rtol=1e-8, max_iter=0, precision=L.PREC_FP64, refine_mode=L.REFINE_RESTART, inner_rtol=1e-3,
-             max_outer=50, spmv_lanes=0, matrix_format=L.FORMAT_CSR):
+             max_outer=50, spmv_lanes=0, matrix_format=L.FORMAT_CSR, spmv_vec=0):
         return L.SolveOpts(rtol, max_iter, precision, refine_mode, inner_rtol, max_outer, spmv_lanes,
-                           matrix_format, 0)
+                           matrix_format, spmv_vec)
 
     def set_stream(self, stream_handle: int | None):
         """Issue the context's work on a caller's cudaStream_t (None: own stream)."""
@@ -177,9 +180,9 @@ class GpuContext:
         self._check(self.lib.axia_gpu_spmv_device(self.h, int(precision), C.c_void_p(x_dev_ptr),
                                                   C.c_void_p(y_dev_ptr), int(lanes)), "spmv")
 
-    def bsr_spmv_device(self, precision, x_dev_ptr, y_dev_ptr, lanes=0):
+    def bsr_spmv_device(self, precision, x_dev_ptr, y_dev_ptr, lanes=0, vec=0):
         self._check(self.lib.axia_gpu_bsr_spmv_device(self.h, int(precision), C.c_void_p(x_dev_ptr),
-                                                      C.c_void_p(y_dev_ptr), int(lanes)), "bsr_spmv")
+                                                      C.c_void_p(y_dev_ptr), int(lanes), int(vec)), "bsr_spmv")
 
     def solve(self, f_full, **kw):
         f = _c(f_full, np.float64)
@@ -267,6 +270,44 @@ class GpuContext:
         self._check(self.lib.axia_gpu_solve_batched_device(self.h, nrhs, C.c_void_p(F_dev_ptr), C.c_void_p(U_dev_ptr),
                                                            C.byref(o), C.byref(info), L.ptr(rel)), "solve_batched")
         return info, rel
+
+    def solve_kff(self, n, trips, rhs, **kw):
+        """solve_kff on the GPU (linalg.rs:311 with PCG): trips = (i, j, v) arrays in the
+        caller's order; returns (x, info).  Replaces any mesh set up on the context."""
+        ti = _c(trips[0], np.int64)
+        tj = _c(trips[1], np.int64)
+        tv = _c(trips[2], np.float64)
+        b = _c(rhs, np.float64)
+        x = np.zeros(int(n))
+        kw.setdefault("rtol", 1e-8)
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        self.model = None
+        try:
+            self._check(self.lib.axia_gpu_solve_triplets(self.h, int(n), int(ti.shape[0]), L.ptr(ti), L.ptr(tj),
+                                                         L.ptr(tv), L.ptr(b), L.ptr(x), C.byref(o), C.byref(info)),
+                        "solve_kff")
+        finally:
+            self._refresh_sizes()
+        return x, info
+
+    def solve_csr(self, n, indptr, indices, data, rhs, **kw):
+        """The same for a caller's CSR (int64 indptr / indices, full symmetric storage)."""
+        p = _c(indptr, np.int64)
+        c = _c(indices, np.int64)
+        v = _c(data, np.float64)
+        b = _c(rhs, np.float64)
+        x = np.zeros(int(n))
+        kw.setdefault("rtol", 1e-8)
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        self.model = None
+        try:
+            self._check(self.lib.axia_gpu_solve_csr(self.h, int(n), L.ptr(p), L.ptr(c), L.ptr(v), L.ptr(b), L.ptr(x),
+                                                    C.byref(o), C.byref(info)), "solve_csr")
+        finally:
+            self._refresh_sizes()
+        return x, info
 
     def export_system(self):
         """K_ff as (rowptr, col, val), the Jacobi diagonal and K_fp u0."""

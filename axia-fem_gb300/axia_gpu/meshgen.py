@@ -12,6 +12,7 @@ same mesh on every machine.
 """
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -278,3 +279,20 @@ def patch_c3d20():
     bc = np.array([3 * n + d for n, d in bcs], dtype=np.int64)
     return Model("patch_c3d20", coords, conn, 20, np.array([210000.0]), 0.3, bc, np.zeros(bc.shape[0]),
                  np.zeros(60), np.array([0], np.int64), np.array([FACE_XMAX], np.int32), np.array([210.0]))
+
+
+def from_fixture(path):
+    """A model from a JSON fixture with the fields of Model (tests/golden/le10_*.json:
+    coords, 0-based conn, e, nu, bc_dof, bc_val, dload_elem/face/p)."""
+    import json
+    d = json.load(open(path))
+    coords = np.array(d["coords"], dtype=np.float64)
+    conn = np.array(d["conn"], dtype=np.int32)
+    nn = conn.shape[1]
+    m = Model(os.path.splitext(os.path.basename(path))[0], coords, conn, nn,
+              np.full(conn.shape[0], float(d["e"])), float(d["nu"]),
+              np.array(d["bc_dof"], np.int64), np.array(d["bc_val"], np.float64), np.zeros(3 * coords.shape[0]),
+              np.array(d["dload_elem"], np.int64), np.array(d["dload_face"], np.int32),
+              np.array(d["dload_p"], np.float64))
+    m.node_d = int(d.get("node_d", -1))
+    return m

@@ -9,7 +9,7 @@
 int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0);
 int numeric_assemble(axia_ctx* ctx, int flags);
 int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_opts* opts, axia_solve_info* info);
-int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req);
+int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req, int vec_req);
 int element_energy(axia_ctx* ctx, const double* d_u, const double* d_v, double* d_s);
 int simp_modulus(axia_ctx* ctx, const double* d_rho, double pexp, double e0);
 int simp_gradient(axia_ctx* ctx, const double* d_rho, const double* d_s, double pexp, double e0, double* d_g);
@@ -26,6 +26,10 @@ int reconstruct(axia_ctx* ctx, double* d_u);
 int true_residual(axia_ctx* ctx, double* out);
 int prepare_solve(axia_ctx* ctx, bool mixed);
 int spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req);
+int raw_system_from_triplets(axia_ctx* ctx, int64_t n, int64_t nt, const int64_t* h_i, const int64_t* h_j,
+                             const double* h_v, bool fp32);
+int raw_system_from_csr(axia_ctx* ctx, int64_t n, const int64_t* h_indptr, const int64_t* h_indices,
+                        const double* h_data, bool fp32);
 
 namespace {
 
@@ -52,6 +56,7 @@ struct EventTimer {
 
 void free_mesh_state(axia_ctx* ctx) {
   multimesh_release(ctx);
+  ctx->h_ind_of.clear();
   ctx->mesh_node0.clear();
   ctx->mesh_blocks.clear();
   dev_free(ctx->d_coords);
@@ -88,6 +93,9 @@ void free_mesh_state(axia_ctx* ctx) {
   dev_free(ctx->d_p32);
   dev_free(ctx->d_q32);
   dev_free(ctx->d_adj_ptr32);
+  dev_free(ctx->d_qptr);
+  dev_free(ctx->d_qadj);
+  ctx->nbq = 0;
   dev_free(ctx->d_bval64);
   dev_free(ctx->d_bval32);
   dev_free(ctx->d_bdinv64);
@@ -310,7 +318,7 @@ int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const
 int32_t axia_gpu_assemble_ex(axia_ctx* ctx, int32_t flags) {
   if (!ctx) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
-  if (!ctx->d_rowptr) return set_error(ctx, AXIA_ERR_STATE, "assemble before setup");
+  if (!ctx->d_rowptr || !ctx->d_conn) return set_error(ctx, AXIA_ERR_STATE, "assemble before setup");
   if (flags <= 0 || flags > 15) return set_error(ctx, AXIA_ERR_INVALID_ARG, "assemble: unknown matrix forms");
   EventTimer t(ctx->stream);
   int st = numeric_assemble(ctx, flags);
@@ -365,7 +373,7 @@ int32_t axia_gpu_solve_device(axia_ctx* ctx, const double* f_full_dev, double* u
                               const axia_solve_opts* opts, axia_solve_info* info) {
   if (!ctx || !f_full_dev || !u_full_dev) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
-  if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "solve before assemble");
+  if (!ctx->assembled || !ctx->d_ind_of) return set_error(ctx, AXIA_ERR_STATE, "solve before assemble");
   return solve_common(ctx, f_full_dev, u_full_dev, opts, info);
 }
 
@@ -373,7 +381,7 @@ int32_t axia_gpu_solve(axia_ctx* ctx, const double* f_full, double* u_full, cons
                        axia_solve_info* info) {
   if (!ctx || !f_full || !u_full) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
-  if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "solve before assemble");
+  if (!ctx->assembled || !ctx->d_ind_of) return set_error(ctx, AXIA_ERR_STATE, "solve before assemble");
   for (int64_t d = 0; d < ctx->ndof; ++d)
     if (!std::isfinite(f_full[d])) return set_error(ctx, AXIA_ERR_NONFINITE, "load vector entry " + std::to_string(d) + " not finite");
   if (!ctx->d_f) AXIA_TRY(dev_alloc(ctx, &ctx->d_f, (size_t)ctx->ndof));
@@ -384,6 +392,74 @@ int32_t axia_gpu_solve(axia_ctx* ctx, const double* f_full, double* u_full, cons
   AXIA_CUDA(ctx, cudaMemcpyAsync(u_full, ctx->d_u, ctx->ndof * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return AXIA_OK;
+}
+
+// PCG on the context's raw K_ff (from triplets or CSR): rhs -> x, both host arrays.
+static int32_t solve_raw(axia_ctx* ctx, const double* rhs, double* x, const axia_solve_opts* opts,
+                         axia_solve_info* info) {
+  axia_solve_info local{};
+  if (!info) info = &local;
+  std::memset(info, 0, sizeof(*info));
+  info->bad_index = -1;
+  axia_solve_opts o{};
+  if (opts) o = *opts;
+  if (!(o.rtol > 0.0)) o.rtol = 1e-8;  // solve_kff's PCG tolerance (linalg.rs:363)
+  if (o.matrix_format != AXIA_FORMAT_CSR)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "solve_kff: caller systems are CSR; node blocks need a mesh");
+  const bool mixed = o.precision == AXIA_PREC_MIXED;
+  EventTimer t(ctx->stream);
+  int st = ensure_pcg_state(ctx);
+  if (st == AXIA_OK) st = prepare_solve(ctx, mixed);
+  if (st == AXIA_OK && cudaMemcpyAsync(ctx->d_b, rhs, ctx->n_free * sizeof(double), cudaMemcpyHostToDevice,
+                                       ctx->stream) != cudaSuccess)
+    st = set_error(ctx, AXIA_ERR_CUDA, "solve_kff: rhs upload");
+  if (st == AXIA_OK) st = pcg_solve(ctx, &o, info);
+  info->ms_solve = t.stop_ms();
+  if (st == AXIA_OK) {
+    true_residual(ctx, &info->true_residual);
+    if (cudaMemcpyAsync(x, ctx->d_x, ctx->n_free * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      st = set_error(ctx, AXIA_ERR_CUDA, "solve_kff: solution download");
+  }
+  info->n_free = ctx->n_free;
+  info->nnz = ctx->nnz;
+  info->bad_index = ctx->last_bad;
+  info->status = st;
+  return st;
+}
+
+static int check_raw_rhs(axia_ctx* ctx, int64_t n, const double* rhs) {
+  for (int64_t d = 0; d < n; ++d)
+    if (!std::isfinite(rhs[d]))
+      return set_error(ctx, AXIA_ERR_NONFINITE, "solve_kff: rhs entry " + std::to_string(d) + " not finite");
+  return AXIA_OK;
+}
+
+int32_t axia_gpu_solve_triplets(axia_ctx* ctx, int64_t n, int64_t n_trips, const int64_t* ti, const int64_t* tj,
+                                const double* tv, const double* rhs, double* x, const axia_solve_opts* opts,
+                                axia_solve_info* info) {
+  if (!ctx || !rhs || !x || n <= 0 || n_trips < 0 || (n_trips > 0 && (!ti || !tj || !tv)))
+    return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  AXIA_TRY(check_raw_rhs(ctx, n, rhs));
+  free_mesh_state(ctx);
+  const bool mixed = opts && opts->precision == AXIA_PREC_MIXED;
+  AXIA_TRY(raw_system_from_triplets(ctx, n, n_trips, ti, tj, tv, mixed));
+  return solve_raw(ctx, rhs, x, opts, info);
+}
+
+int32_t axia_gpu_solve_csr(axia_ctx* ctx, int64_t n, const int64_t* indptr, const int64_t* indices,
+                           const double* data, const double* rhs, double* x, const axia_solve_opts* opts,
+                           axia_solve_info* info) {
+  if (!ctx || !indptr || !rhs || !x || n <= 0) return AXIA_ERR_INVALID_ARG;
+  if (indptr[n] > 0 && (!indices || !data)) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  AXIA_TRY(check_raw_rhs(ctx, n, rhs));
+  free_mesh_state(ctx);
+  const bool mixed = opts && opts->precision == AXIA_PREC_MIXED;
+  AXIA_TRY(raw_system_from_csr(ctx, n, indptr, indices, data, mixed));
+  return solve_raw(ctx, rhs, x, opts, info);
 }
 
 int32_t axia_gpu_set_stream(axia_ctx* ctx, void* stream) {
@@ -406,11 +482,12 @@ int32_t axia_gpu_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev
   return spmv_device(ctx, fp32, x_dev, y_dev, lanes);
 }
 
-int32_t axia_gpu_bsr_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev, int32_t lanes) {
+int32_t axia_gpu_bsr_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev, int32_t lanes,
+                                 int32_t vec) {
   if (!ctx || !x_dev || !y_dev) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "spmv before assemble");
-  return bsr_spmv_device(ctx, precision == AXIA_PREC_MIXED, x_dev, y_dev, lanes);
+  return bsr_spmv_device(ctx, precision == AXIA_PREC_MIXED, x_dev, y_dev, lanes, vec);
 }
 
 int64_t axia_gpu_node_blocks(const axia_ctx* ctx) { return ctx ? ctx->n_adj : -1; }
@@ -440,7 +517,7 @@ int32_t axia_gpu_compliance_forward(axia_ctx* ctx, const double* rho, double pen
                                     axia_solve_info* info) {
   if (!ctx || !rho || !f_full || !u_full || !compliance) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
-  if (!ctx->d_rowptr) return set_error(ctx, AXIA_ERR_STATE, "compliance before setup");
+  if (!ctx->d_rowptr || !ctx->d_conn) return set_error(ctx, AXIA_ERR_STATE, "compliance before setup");
   if (!(e0 > 0.0) || !std::isfinite(penal)) return set_error(ctx, AXIA_ERR_MATERIAL, "SIMP needs E0 > 0 and a finite p");
   ctx->have_forward = false;
   if (!ctx->d_rho) AXIA_TRY(dev_alloc(ctx, &ctx->d_rho, (size_t)std::max<int64_t>(ctx->n_elem, 1)));
@@ -549,7 +626,8 @@ int32_t axia_gpu_export_system(const axia_ctx* ctx_c, int32_t* rowptr, int32_t* 
   if (val && !ctx->have_csr64) return set_error(ctx, AXIA_ERR_STATE, "export of CSR values needs AXIA_ASM_CSR64");
   if (val) AXIA_CUDA(ctx, cudaMemcpy(val, ctx->d_val, nnz * sizeof(double), cudaMemcpyDeviceToHost));
   if (diag) AXIA_CUDA(ctx, cudaMemcpy(diag, ctx->d_diag, n * sizeof(double), cudaMemcpyDeviceToHost));
-  if (kfu0) AXIA_CUDA(ctx, cudaMemcpy(kfu0, ctx->d_kfu0, n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (kfu0 && ctx->d_kfu0) AXIA_CUDA(ctx, cudaMemcpy(kfu0, ctx->d_kfu0, n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (kfu0 && !ctx->d_kfu0) std::memset(kfu0, 0, n * sizeof(double));
   return AXIA_OK;
 }
 

@@ -343,6 +343,21 @@ __device__ __forceinline__ int first_free(const int32_t* ind_of, int b) {
 }
 
 // column indices of every free row, warp per node
+// padded block-row lengths: each row rounded up to a multiple of 4 blocks
+__global__ void k_quad_counts(int64_t n_nodes, const int64_t* adj_ptr, int64_t* qcnt) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a <= n_nodes; a += (int64_t)gridDim.x * blockDim.x)
+    qcnt[a] = a < n_nodes ? ((adj_ptr[a + 1] - adj_ptr[a] + 3) & ~(int64_t)3) : 0;
+}
+
+// padded block columns: the row's adjacency, then the row's own node as filler
+__global__ void k_quad_fill(int64_t n_nodes, const int64_t* adj_ptr, const int32_t* adj, const int64_t* qptr,
+                            int32_t* qadj) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n_nodes; a += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s0 = adj_ptr[a], len = adj_ptr[a + 1] - s0, q0 = qptr[a], qlen = qptr[a + 1] - q0;
+    for (int64_t s = 0; s < qlen; ++s) qadj[q0 + s] = s < len ? adj[s0 + s] : (int32_t)a;
+  }
+}
+
 __global__ void k_fill_columns(int64_t n_nodes, const int64_t* adj_ptr, const int32_t* adj,
                                const int32_t* adj_off, const int32_t* ind_of, const int32_t* rowptr,
                                int32_t* col) {
@@ -396,7 +411,8 @@ struct GatherArgs {
   float* bval32;
   double* bdinv64;    // full-DOF 1/diag, 1 on prescribed DOFs
   float* bdinv32;
-  int64_t nb;
+  const int32_t* qptr;  // padded node-block row starts
+  int64_t nb;           // padded block count (plane stride)
 };
 
 __global__ void k_gather(GatherArgs g) {
@@ -475,7 +491,7 @@ __global__ void k_gather(GatherArgs g) {
         const bool fi = g.ind_of[3 * a + i] >= 0, fj = g.ind_of[3 * (int64_t)b + j] >= 0;
         const bool dg = (b == a) && (i == j);
         const double v = (fi && fj) ? acc[s * 9 + ij] : (dg ? 1.0 : 0.0);
-        const int64_t pos = (int64_t)ij * g.nb + s0 + s;
+        const int64_t pos = (int64_t)ij * g.nb + g.qptr[a] + s;
         if (g.bval64) g.bval64[pos] = v;
         if (g.bval32) g.bval32[pos] = (float)v;
         if (dg) {
@@ -639,6 +655,28 @@ int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0) {
   AXIA_TRY(dev_alloc(ctx, &ctx->d_adj_ptr32, n_nodes + 1));
   k_to_i32<<<grid_for(n_nodes + 1, 256, ctx->sm_count), 256, 0, s>>>(n_nodes + 1, d_adj_ptr, ctx->d_adj_ptr32);
   ctx->launches++;
+  // padded block rows of the node-block form
+  {
+    int64_t *d_qcnt = nullptr, *d_qptr64 = nullptr;
+    AXIA_TRY(dev_alloc(ctx, &d_qcnt, n_nodes + 1));
+    AXIA_TRY(dev_alloc(ctx, &d_qptr64, n_nodes + 1));
+    k_quad_counts<<<grid_for(n_nodes + 1, 256, ctx->sm_count), 256, 0, s>>>(n_nodes, d_adj_ptr, d_qcnt);
+    ctx->launches++;
+    int64_t nbq = 0;
+    AXIA_TRY(device_exclusive_scan(ctx, d_qcnt, d_qptr64, n_nodes + 1, &nbq));
+    if (nbq >= (int64_t)INT32_MAX) return set_error(ctx, AXIA_ERR_TOO_LARGE, "node blocks exceed 2^31-1");
+    ctx->nbq = nbq;
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_qptr, n_nodes + 1));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_qadj, (size_t)std::max<int64_t>(nbq, 4)));
+    k_to_i32<<<grid_for(n_nodes + 1, 256, ctx->sm_count), 256, 0, s>>>(n_nodes + 1, d_qptr64, ctx->d_qptr);
+    k_quad_fill<<<grid_for(n_nodes, 256, ctx->sm_count), 256, 0, s>>>(n_nodes, d_adj_ptr, ctx->d_adj, d_qptr64,
+                                                                       ctx->d_qadj);
+    ctx->launches += 2;
+    AXIA_CUDA(ctx, cudaGetLastError());
+    AXIA_CUDA(ctx, cudaStreamSynchronize(s));
+    dev_free(d_qcnt);
+    dev_free(d_qptr64);
+  }
   // keep the 64-bit pointers for the gather
   dev_free(ctx->d_ne_ptr);
   dev_free(ctx->d_adj_ptr);
@@ -686,8 +724,15 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   if (!ctx->d_dinv) AXIA_TRY(dev_alloc(ctx, &ctx->d_dinv, ctx->n_free));
   if (csr32 && !ctx->d_dinv32) AXIA_TRY(dev_alloc(ctx, &ctx->d_dinv32, ctx->n_free));
   if (!ctx->d_kfu0) AXIA_TRY(dev_alloc(ctx, &ctx->d_kfu0, ctx->n_free));
-  if (bsr64 && !ctx->d_bval64) AXIA_TRY(dev_alloc(ctx, &ctx->d_bval64, (size_t)(9 * ctx->n_adj)));
-  if (bsr32 && !ctx->d_bval32) AXIA_TRY(dev_alloc(ctx, &ctx->d_bval32, (size_t)(9 * ctx->n_adj)));
+  // padding blocks stay zero: they are cleared once here and never written
+  if (bsr64 && !ctx->d_bval64) {
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_bval64, (size_t)(9 * ctx->nbq)));
+    AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bval64, 0, (size_t)(9 * ctx->nbq) * sizeof(double), s));
+  }
+  if (bsr32 && !ctx->d_bval32) {
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_bval32, (size_t)(9 * ctx->nbq)));
+    AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bval32, 0, (size_t)(9 * ctx->nbq) * sizeof(float), s));
+  }
   if ((bsr64 || bsr32) && !ctx->d_bdinv64) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv64, (size_t)ctx->ndof));
   if (bsr32 && !ctx->d_bdinv32) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv32, (size_t)ctx->ndof));
   AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_kfu0, 0, ctx->n_free * sizeof(double), s));
@@ -716,7 +761,8 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   g.bval32 = bsr32 ? ctx->d_bval32 : nullptr;
   g.bdinv64 = (bsr64 || bsr32) ? ctx->d_bdinv64 : nullptr;
   g.bdinv32 = bsr32 ? ctx->d_bdinv32 : nullptr;
-  g.nb = ctx->n_adj;
+  g.qptr = ctx->d_qptr;
+  g.nb = ctx->nbq;
   AXIA_TRY(run_gather(ctx, g));
   AXIA_CUDA(ctx, cudaStreamSynchronize(s));
   DevStatus hs;

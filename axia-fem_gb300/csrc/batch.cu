@@ -470,8 +470,8 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
                                                            ctx->d_mB);
     ctx->launches++;
     AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
-    MultiArgs P{BsrMatM<float>{(int)ctx->n_nodes, ctx->d_adj_ptr32, ctx->d_adj, ctx->d_bval32, (long long)ctx->n_adj},
-                BsrMatM<double>{(int)ctx->n_nodes, ctx->d_adj_ptr32, ctx->d_adj, ctx->d_bval64, (long long)ctx->n_adj},
+    MultiArgs P{BsrMatM<float>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval32, (long long)ctx->nbq},
+                BsrMatM<double>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq},
                 (int)nd, ctx->d_bdinv32, ctx->d_mB, ctx->d_mX, ctx->d_mX32, ctx->d_mR32, ctx->d_mP32, ctx->d_mQ32,
                 ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (MultiOut*)ctx->d_mout, opts->rtol, delta,
                 max_iter, 2000000000ull};

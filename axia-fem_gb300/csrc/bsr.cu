@@ -2,11 +2,15 @@
 // persistent Krylov kernels on it.
 //
 // Layout: one block row per node a, one 3x3 block per adjacent node b (the
-// node adjacency of the symbolic phase, sorted), values stored as nine
-// structure-of-arrays planes val[k][s] (k = 3 i + j) so lanes that walk
-// consecutive blocks of a row load consecutive addresses.  Index traffic is
-// one int32 per 9 values: 4.44 bytes per nonzero in FP32 (CSR: 8) and 8.44 in
-// FP64 (CSR: 12).
+// node adjacency of the symbolic phase, sorted), each block row padded with
+// zero blocks to a multiple of 4 blocks; values stored as nine
+// structure-of-arrays planes val[k][s] (k = 3 i + j).  A lane loads VEC = 1,
+// 2 or 4 consecutive blocks of its row with one vector load per plane (and
+// one for their block columns), so a warp has 4 to 16 times the bytes of a
+// one-block-per-lane loop in flight: the SpMV is bound by DRAM latency
+// unless each lane keeps enough loads outstanding.  Index traffic is one
+// int32 per 9 values: 4.44 bytes per nonzero in FP32 (CSR: 8) and 8.44 in
+// FP64 (CSR: 12), plus the padding (C3D8 interior rows: 27 -> 28 blocks).
 //
 // The system is the full-DOF form of K_ff: rows and columns of prescribed
 // DOFs are zero except a unit diagonal, their right-hand side is zero.  CG on
@@ -18,31 +22,87 @@
 // solver/src/linalg.rs:199-259, FP64 or FP32) and pcg_bsr_reliable_kernel
 // (FP32 inner CG with FP64 reliable updates, the mixed form).
 #include <algorithm>
+#include <type_traits>
+#include <vector>
 #include <cmath>
 
 #include "solver.cuh"
 
-// Block row a with L lanes: (y0, y1, y2) = sum_s K_as x_adj[s]
-template <typename V, typename A, int L>
+// Vector loads of VEC consecutive entries (streaming: the matrix is read once per use).
+template <typename V, int VEC>
+__device__ __forceinline__ void ldv(const V* p, V (&o)[VEC]);
+template <>
+__device__ __forceinline__ void ldv<float, 1>(const float* p, float (&o)[1]) { o[0] = __ldcs(p); }
+template <>
+__device__ __forceinline__ void ldv<float, 2>(const float* p, float (&o)[2]) {
+  const float2 t = __ldcs(reinterpret_cast<const float2*>(p));
+  o[0] = t.x;
+  o[1] = t.y;
+}
+template <>
+__device__ __forceinline__ void ldv<float, 4>(const float* p, float (&o)[4]) {
+  const float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+  o[0] = t.x;
+  o[1] = t.y;
+  o[2] = t.z;
+  o[3] = t.w;
+}
+template <>
+__device__ __forceinline__ void ldv<double, 1>(const double* p, double (&o)[1]) { o[0] = __ldcs(p); }
+template <>
+__device__ __forceinline__ void ldv<double, 2>(const double* p, double (&o)[2]) {
+  const double2 t = __ldcs(reinterpret_cast<const double2*>(p));
+  o[0] = t.x;
+  o[1] = t.y;
+}
+template <int VEC>
+__device__ __forceinline__ void ldi(const int* p, int (&o)[VEC]);
+template <>
+__device__ __forceinline__ void ldi<1>(const int* p, int (&o)[1]) { o[0] = __ldcs(p); }
+template <>
+__device__ __forceinline__ void ldi<2>(const int* p, int (&o)[2]) {
+  const int2 t = __ldcs(reinterpret_cast<const int2*>(p));
+  o[0] = t.x;
+  o[1] = t.y;
+}
+template <>
+__device__ __forceinline__ void ldi<4>(const int* p, int (&o)[4]) {
+  const int4 t = __ldcs(reinterpret_cast<const int4*>(p));
+  o[0] = t.x;
+  o[1] = t.y;
+  o[2] = t.z;
+  o[3] = t.w;
+}
+
+// Block row a with L lanes, each taking VEC consecutive blocks per step:
+// (y0, y1, y2) = sum_s K_as x_adj[s].  Row starts, row lengths and the plane
+// stride are multiples of 4 blocks, so every vector load is aligned.
+template <typename V, typename A, int VEC, int L>
 __device__ __forceinline__ void bsr_row(int a, int sl, const BsrMat<V>& M, const V* x, A& y0, A& y1, A& y2) {
   y0 = y1 = y2 = A(0);
   if (a < M.n_nodes) {
     const int beg = __ldg(M.adj_ptr + a), end = __ldg(M.adj_ptr + a + 1);
     const long long nb = M.nb;
-#pragma unroll 2
-    for (int s = beg + sl; s < end; s += L) {
-      const int b = ld_stream(M.adj + s);
-      const A x0 = (A)x[3 * b], x1 = (A)x[3 * b + 1], x2 = (A)x[3 * b + 2];
-      const V* v = M.val + s;
-      y0 = fma((A)ld_stream(v), x0, y0);
-      y0 = fma((A)ld_stream(v + nb), x1, y0);
-      y0 = fma((A)ld_stream(v + 2 * nb), x2, y0);
-      y1 = fma((A)ld_stream(v + 3 * nb), x0, y1);
-      y1 = fma((A)ld_stream(v + 4 * nb), x1, y1);
-      y1 = fma((A)ld_stream(v + 5 * nb), x2, y1);
-      y2 = fma((A)ld_stream(v + 6 * nb), x0, y2);
-      y2 = fma((A)ld_stream(v + 7 * nb), x1, y2);
-      y2 = fma((A)ld_stream(v + 8 * nb), x2, y2);
+#pragma unroll(VEC == 1 ? 2 : 1)
+    for (int s = beg + sl * VEC; s < end; s += L * VEC) {
+      int b[VEC];
+      ldi<VEC>(M.adj + s, b);
+      V k[9][VEC];
+#pragma unroll
+      for (int p = 0; p < 9; ++p) ldv<V, VEC>(M.val + p * nb + s, k[p]);
+#pragma unroll
+      for (int t = 0; t < VEC; ++t) {
+        const A x0 = (A)x[3 * b[t]], x1 = (A)x[3 * b[t] + 1], x2 = (A)x[3 * b[t] + 2];
+        y0 = fma((A)k[0][t], x0, y0);
+        y0 = fma((A)k[1][t], x1, y0);
+        y0 = fma((A)k[2][t], x2, y0);
+        y1 = fma((A)k[3][t], x0, y1);
+        y1 = fma((A)k[4][t], x1, y1);
+        y1 = fma((A)k[5][t], x2, y1);
+        y2 = fma((A)k[6][t], x0, y2);
+        y2 = fma((A)k[7][t], x1, y2);
+        y2 = fma((A)k[8][t], x2, y2);
+      }
     }
   }
   y0 = group_sum<L>(y0);
@@ -50,7 +110,7 @@ __device__ __forceinline__ void bsr_row(int a, int sl, const BsrMat<V>& M, const
   y2 = group_sum<L>(y2);
 }
 
-template <typename V, int L>
+template <typename V, int VEC, int L>
 __global__ void __launch_bounds__(PCG_THREADS) bsr_spmv_kernel(BsrMat<V> M, const V* x, V* y) {
   constexpr int RPW = 32 / L;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
@@ -59,7 +119,7 @@ __global__ void __launch_bounds__(PCG_THREADS) bsr_spmv_kernel(BsrMat<V> M, cons
   for (int base = gwarp * RPW; base < M.n_nodes; base += nwarps * RPW) {
     const int a = base + grp;
     V y0, y1, y2;
-    bsr_row<V, V, L>(a, sl, M, x, y0, y1, y2);
+    bsr_row<V, V, VEC, L>(a, sl, M, x, y0, y1, y2);
     if (a < M.n_nodes && sl == 0) {
       y[3 * a] = y0;
       y[3 * a + 1] = y1;
@@ -121,7 +181,7 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_bsr_kernel(BsrPcgArgs<V> P) {
       for (int base = gwarp * RPW; base < n_nodes; base += nwarps * RPW) {
         const int a = base + grp;
         A y0, y1, y2;
-        bsr_row<V, A, L>(a, sl, P.M, P.p, y0, y1, y2);
+        bsr_row<V, A, 1, L>(a, sl, P.M, P.p, y0, y1, y2);
         if (a < n_nodes && sl == 0) {
           P.q[3 * a] = (V)y0;
           P.q[3 * a + 1] = (V)y1;
@@ -190,7 +250,7 @@ struct SolveRange {
   PcgOut* out;
 };
 
-template <int L32, int L64>
+template <int L32, int V32, int L64, int V64>
 __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const SolveRange& R) {
   const int n0 = R.node0, n1 = R.node1;
   const int i0 = 3 * n0;
@@ -235,7 +295,7 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
       for (int base = n0 + gwarp * RPW; base < n1; base += nwarps * RPW) {
         const int a = base + grp;
         float y0, y1, y2;
-        bsr_row<float, float, L32>(a, sl, M32, P.p32, y0, y1, y2);
+        bsr_row<float, float, V32, L32>(a, sl, M32, P.p32, y0, y1, y2);
         if (a < n1 && sl == 0) {
           P.q32[3 * a] = y0;
           P.q32[3 * a + 1] = y1;
@@ -284,7 +344,7 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
         for (int base = n0 + gwarp * RPW; base < n1; base += nwarps * RPW) {
           const int a = base + grp;
           double y[3];
-          bsr_row<double, double, L64>(a, sl, M64, P.x, y[0], y[1], y[2]);
+          bsr_row<double, double, V64, L64>(a, sl, M64, P.x, y[0], y[1], y[2]);
           if (a < n1 && sl == 0) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -328,17 +388,27 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
   }
 }
 
-template <int L32, int L64>
-__global__ void __launch_bounds__(PCG_THREADS, 3) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
+// FP64 reliable updates: 4 lanes per block row; 2 blocks per load where the
+// register budget allows it (the 4-block FP32 variants run 2 blocks per SM).
+constexpr int kL64 = 4;
+template <int V32>
+__host__ __device__ constexpr int rel_v64() { return V32 >= 4 ? 2 : 1; }
+
+// Blocks per SM: vector loads of 4 blocks need the registers of 2 blocks per SM.
+template <int V32>
+__host__ __device__ constexpr int rel_min_blocks() { return V32 >= 4 ? 2 : 3; }
+
+template <int L32, int V32>
+__global__ void __launch_bounds__(PCG_THREADS, rel_min_blocks<V32>()) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
   const SolveRange R{0, P.M32.n_nodes, blockIdx.x, gridDim.x, P.partials, P.totals, P.bar, P.out};
-  reliable_body<L32, L64>(P, R);
+  reliable_body<L32, V32, kL64, rel_v64<V32>()>(P, R);
 }
 
 // Independent systems on disjoint node ranges of one node-block matrix (the
 // meshes of axia_gpu_setup_multi): block b belongs to group cta_group[b] and
 // solves that group's system with the group's own barrier, partial sums,
 // totals and result, so each system converges and exits on its own.
-template <int L32, int L64>
+template <int L32, int V32>
 __global__ void __launch_bounds__(PCG_THREADS, 2)
 pcg_group_reliable_kernel(BsrReliableArgs P, const MeshGroup* groups, const int* cta_group, GridBarrier* bars,
                           double* totals4, PcgOut* outs) {
@@ -346,7 +416,7 @@ pcg_group_reliable_kernel(BsrReliableArgs P, const MeshGroup* groups, const int*
   const MeshGroup G = groups[g];
   const SolveRange R{G.node0, G.node1, blockIdx.x - (unsigned)G.cta0, (unsigned)G.ncta, P.partials + G.part_off,
                      totals4 + 4 * g, bars + g, outs + g};
-  reliable_body<L32, L64>(P, R);
+  reliable_body<L32, V32, kL64, 2>(P, R);
 }
 
 // b[d] = f[d] - K_fp u0 for free d, 0 for prescribed d
@@ -373,7 +443,7 @@ __global__ void __launch_bounds__(PCG_THREADS) bsr_residual_kernel(BsrMat<double
   for (int base = gwarp * RPW; base < M.n_nodes; base += nwarps * RPW) {
     const int a = base + grp;
     double y0, y1, y2;
-    bsr_row<double, double, L>(a, sl, M, x, y0, y1, y2);
+    bsr_row<double, double, 2, L>(a, sl, M, x, y0, y1, y2);
     if (a < M.n_nodes && sl == 0) {
       const double r0 = b[3 * a] - y0, r1 = b[3 * a + 1] - y1, r2 = b[3 * a + 2] - y2;
       rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, rr)));
@@ -385,9 +455,58 @@ __global__ void __launch_bounds__(PCG_THREADS) bsr_residual_kernel(BsrMat<double
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-// Lanes per block row: about one block per lane (C3D8 interior rows have 27
-// blocks, C3D20 corner rows 81); measured on GB300 at 100^3 C3D8, 16 lanes
-// beat 8 by 1.3x for FP32.
+// Lanes per block row and blocks per lane load.  FP32: 4 blocks per load;
+// lanes so that a row of the mesh's mean length takes one or two steps.
+// FP64: 2 blocks per load.  Requests outside the instantiated set fall back
+// to the automatic choice.
+struct RowLayout {
+  int lanes, vec;
+};
+static RowLayout bsr_layout(const axia_ctx* ctx, bool fp32, int lanes_req, int vec_req) {
+  const double avg = ctx->n_nodes ? (double)ctx->nbq / (double)ctx->n_nodes : 4.0;  // padded blocks per row
+  RowLayout r{0, 0};
+  r.vec = (vec_req == 1 || vec_req == 2 || (fp32 && vec_req == 4)) ? vec_req : (fp32 ? 4 : 2);
+  const double steps = avg / r.vec;  // vector steps per row
+  const int auto_l = steps <= 3 ? 2 : (steps <= 6 ? 4 : (steps <= 12 ? 8 : 16));
+  r.lanes = (lanes_req == 2 || lanes_req == 4 || lanes_req == 8 || lanes_req == 16) ? lanes_req : auto_l;
+  // instantiated: vec 4 with 2/4/8 lanes, vec 2 with 4/8, vec 1 with 4/8/16
+  if (r.vec == 4 && r.lanes == 16) r.lanes = 8;
+  if (r.vec == 2 && (r.lanes == 2 || r.lanes == 16)) r.lanes = r.lanes == 2 ? 4 : 8;
+  if (r.vec == 1 && r.lanes == 2) r.lanes = 4;
+  return r;
+}
+
+// Calls f(integral_constant<int, L>, integral_constant<int, VEC>) for an instantiated layout.
+template <typename F>
+static int with_layout(RowLayout r, F&& f) {
+  using std::integral_constant;
+  if (r.vec == 4) {
+    if (r.lanes == 2) return f(integral_constant<int, 2>{}, integral_constant<int, 4>{});
+    if (r.lanes == 4) return f(integral_constant<int, 4>{}, integral_constant<int, 4>{});
+    return f(integral_constant<int, 8>{}, integral_constant<int, 4>{});
+  }
+  if (r.vec == 2) {
+    if (r.lanes == 4) return f(integral_constant<int, 4>{}, integral_constant<int, 2>{});
+    return f(integral_constant<int, 8>{}, integral_constant<int, 2>{});
+  }
+  if (r.lanes == 4) return f(integral_constant<int, 4>{}, integral_constant<int, 1>{});
+  if (r.lanes == 8) return f(integral_constant<int, 8>{}, integral_constant<int, 1>{});
+  return f(integral_constant<int, 16>{}, integral_constant<int, 1>{});
+}
+
+// The FP64 subset: 1 or 2 blocks per load (a 4-block FP64 load would be 32 bytes).
+template <typename F>
+static int with_layout64(RowLayout r, F&& f) {
+  using std::integral_constant;
+  if (r.vec >= 2) {
+    if (r.lanes == 4) return f(integral_constant<int, 4>{}, integral_constant<int, 2>{});
+    return f(integral_constant<int, 8>{}, integral_constant<int, 2>{});
+  }
+  if (r.lanes == 4) return f(integral_constant<int, 4>{}, integral_constant<int, 1>{});
+  if (r.lanes == 8) return f(integral_constant<int, 8>{}, integral_constant<int, 1>{});
+  return f(integral_constant<int, 16>{}, integral_constant<int, 1>{});
+}
+
 static int bsr_lanes(const axia_ctx* ctx, int requested) {
   if (requested == 2 || requested == 4 || requested == 8 || requested == 16) return requested;
   double avg = ctx->n_nodes ? (double)ctx->n_adj / (double)ctx->n_nodes : 1.0;  // blocks per block row
@@ -396,7 +515,7 @@ static int bsr_lanes(const axia_ctx* ctx, int requested) {
 
 template <typename V>
 static BsrMat<V> bsr_mat(const axia_ctx* ctx, const V* val) {
-  return BsrMat<V>{(int)ctx->n_nodes, ctx->d_adj_ptr32, ctx->d_adj, val, (long long)ctx->n_adj};
+  return BsrMat<V>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, val, (long long)ctx->nbq};
 }
 
 static int ensure_full_buffers(axia_ctx* ctx, bool mixed) {
@@ -440,9 +559,9 @@ static int launch_bsr_pcg(axia_ctx* ctx, BsrPcgArgs<V>& P, int lanes) {
   }
 }
 
-template <int L32, int L64>
+template <int L32, int V32>
 static int launch_bsr_rel_t(axia_ctx* ctx, BsrReliableArgs& P) {
-  auto kern = pcg_bsr_reliable_kernel<L32, L64>;
+  auto kern = pcg_bsr_reliable_kernel<L32, V32>;
   int grid = 0;
   AXIA_TRY(coop_grid(ctx, (const void*)kern, P.nd, &grid));
   void* params[] = {&P};
@@ -451,31 +570,27 @@ static int launch_bsr_rel_t(axia_ctx* ctx, BsrReliableArgs& P) {
   return AXIA_OK;
 }
 
-static int launch_bsr_rel(axia_ctx* ctx, BsrReliableArgs& P, int l32) {
-  switch (l32) {
-    case 2: return launch_bsr_rel_t<2, 4>(ctx, P);
-    case 4: return launch_bsr_rel_t<4, 4>(ctx, P);
-    case 16: return launch_bsr_rel_t<16, 4>(ctx, P);
-    default: return launch_bsr_rel_t<8, 4>(ctx, P);
-  }
+static int launch_bsr_rel(axia_ctx* ctx, BsrReliableArgs& P, RowLayout r) {
+  return with_layout(r, [&](auto l, auto v) { return launch_bsr_rel_t<decltype(l)::value, decltype(v)::value>(ctx, P); });
 }
 
 // Occupancy of the group kernel (blocks per SM) for the grid size of a multi-mesh solve.
-int group_kernel_capacity(axia_ctx* ctx, int lanes, int* per_sm) {
-  const void* kern = lanes == 16 ? (const void*)pcg_group_reliable_kernel<16, 8>
-                                 : (lanes == 4 ? (const void*)pcg_group_reliable_kernel<4, 8>
-                                               : (const void*)pcg_group_reliable_kernel<8, 8>);
-  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, PCG_THREADS, 0));
-  return AXIA_OK;
+int group_kernel_capacity(axia_ctx* ctx, int lanes, int vec, int* per_sm) {
+  return with_layout(RowLayout{lanes, vec}, [&](auto l, auto v) {
+    const void* kern = (const void*)pcg_group_reliable_kernel<decltype(l)::value, decltype(v)::value>;
+    AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, PCG_THREADS, 0));
+    return (int)AXIA_OK;
+  });
 }
-
 // Cooperative launch of the group kernel on ctx->stream (capturable).
 int launch_group_reliable(axia_ctx* ctx, BsrReliableArgs& P, const MeshGroup* groups, const int* cta_group,
-                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes) {
+                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes, int vec) {
   void* params[] = {&P, &groups, &cta_group, &bars, &totals4, &outs};
-  const void* kern = lanes == 16 ? (const void*)pcg_group_reliable_kernel<16, 8>
-                                 : (lanes == 4 ? (const void*)pcg_group_reliable_kernel<4, 8>
-                                               : (const void*)pcg_group_reliable_kernel<8, 8>);
+  const void* kern = nullptr;
+  with_layout(RowLayout{lanes, vec}, [&](auto l, auto v) {
+    kern = (const void*)pcg_group_reliable_kernel<decltype(l)::value, decltype(v)::value>;
+    return 0;
+  });
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(PCG_THREADS);
@@ -489,6 +604,13 @@ int launch_group_reliable(axia_ctx* ctx, BsrReliableArgs& P, const MeshGroup* gr
   AXIA_CUDA(ctx, cudaLaunchKernelExC(&cfg, kern, params));
   ctx->launches++;
   return AXIA_OK;
+}
+
+// The layout (lanes, blocks per load) a multi-mesh solve uses for a request.
+void group_layout(const axia_ctx* ctx, int lanes_req, int vec_req, int* lanes, int* vec) {
+  const RowLayout r = bsr_layout(ctx, true, lanes_req, vec_req);
+  *lanes = r.lanes;
+  *vec = r.vec;
 }
 
 int launch_full_rhs(axia_ctx* ctx, const double* d_f) {
@@ -541,6 +663,7 @@ int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_op
   const long long max_iter = opts->max_iter > 0 ? opts->max_iter : std::max<long long>(4LL * ctx->n_free, 200);
   const unsigned long long limit_ns = 2000000000ull;
   const int lanes = bsr_lanes(ctx, opts->spmv_lanes);
+  const RowLayout lay = bsr_layout(ctx, true, opts->spmv_lanes, opts->spmv_vec);
   AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
   PcgOut o{};
   if (!mixed) {
@@ -554,7 +677,7 @@ int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_op
                       ctx->d_bdinv32, ctx->d_bf, ctx->d_xf, ctx->d_xf32, ctx->d_rf32, ctx->d_pf32, ctx->d_qf32,
                       ctx->d_zf32, ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out, opts->rtol,
                       delta, max_iter, limit_ns};
-    AXIA_TRY(timed_launch(ctx, info, [&] { return launch_bsr_rel(ctx, P, lanes); }));
+    AXIA_TRY(timed_launch(ctx, info, [&] { return launch_bsr_rel(ctx, P, lay); }));
   }
   AXIA_TRY(read_out(ctx, &o));
   info->iters = o.iters;
@@ -569,26 +692,25 @@ int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_op
   return AXIA_OK;
 }
 
-int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req) {
+int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req, int vec_req) {
   if (fp32 ? !ctx->have_bsr32 : !ctx->have_bsr64) return set_error(ctx, AXIA_ERR_STATE, "node-block matrix not assembled");
-  const int lanes = bsr_lanes(ctx, lanes_req);
-  int per_sm = 0;
   const int grid_max = ctx->sm_count * 4;
-  (void)per_sm;
   if (fp32) {
-    auto M = bsr_mat<float>(ctx, ctx->d_bval32);
-    switch (lanes) {
-      case 4: bsr_spmv_kernel<float, 4><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const float*)x, (float*)y); break;
-      case 16: bsr_spmv_kernel<float, 16><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const float*)x, (float*)y); break;
-      default: bsr_spmv_kernel<float, 8><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const float*)x, (float*)y); break;
-    }
+    const auto M = bsr_mat<float>(ctx, ctx->d_bval32);
+    with_layout(bsr_layout(ctx, true, lanes_req, vec_req), [&](auto l, auto v) {
+      bsr_spmv_kernel<float, decltype(v)::value, decltype(l)::value>
+          <<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const float*)x, (float*)y);
+      return 0;
+    });
   } else {
-    auto M = bsr_mat<double>(ctx, ctx->d_bval64);
-    switch (lanes) {
-      case 4: bsr_spmv_kernel<double, 4><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const double*)x, (double*)y); break;
-      case 16: bsr_spmv_kernel<double, 16><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const double*)x, (double*)y); break;
-      default: bsr_spmv_kernel<double, 8><<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const double*)x, (double*)y); break;
-    }
+    const auto M = bsr_mat<double>(ctx, ctx->d_bval64);
+    RowLayout r = bsr_layout(ctx, false, lanes_req, vec_req);
+    if (r.vec >= 2 && r.lanes == 2) r.lanes = 4;
+    with_layout64(r, [&](auto l, auto v) {
+      bsr_spmv_kernel<double, decltype(v)::value, decltype(l)::value>
+          <<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const double*)x, (double*)y);
+      return 0;
+    });
   }
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());

@@ -219,10 +219,15 @@ struct axia_ctx {
   double* d_kfu0 = nullptr;     // [n_free]
   bool assembled = false, have32 = false, have_csr64 = false;
 
-  // node-block (3x3) form of the full-DOF system
-  int32_t* d_adj_ptr32 = nullptr;  // [n_nodes+1]
-  double* d_bval64 = nullptr;      // [9][n_adj]
-  float* d_bval32 = nullptr;       // [9][n_adj]
+  // node-block (3x3) form of the full-DOF system: block rows padded to a
+  // multiple of 4 blocks (pad column = the row's node, value 0) so that lanes
+  // load 2 or 4 consecutive blocks of a row with one vector load per plane
+  int32_t* d_adj_ptr32 = nullptr;  // [n_nodes+1] unpadded block-row starts
+  int32_t* d_qptr = nullptr;       // [n_nodes+1] padded block-row starts (multiples of 4)
+  int32_t* d_qadj = nullptr;       // [nbq] padded block columns
+  int64_t nbq = 0;                 // padded block count
+  double* d_bval64 = nullptr;      // [9][nbq]
+  float* d_bval32 = nullptr;       // [9][nbq]
   double* d_bdinv64 = nullptr;     // [ndof]
   float* d_bdinv32 = nullptr;      // [ndof]
   bool have_bsr64 = false, have_bsr32 = false;
@@ -270,7 +275,7 @@ struct axia_ctx {
   GridBarrier* d_mbars = nullptr;
   double* d_mtotals = nullptr;
   unsigned char* d_mouts = nullptr;   // PcgOut[n_meshes]
-  int multi_grid = 0, multi_lanes = 0;
+  int multi_grid = 0, multi_lanes = 0, multi_vec = 0;
   void* multi_graph = nullptr;        // cudaGraphExec_t
   const double* graph_f = nullptr;
   double* graph_u = nullptr;

@@ -35,10 +35,10 @@ void drop_graph(axia_ctx* ctx) {
   ctx->multi_graph = nullptr;
 }
 
-int plan_groups(axia_ctx* ctx, int lanes) {
+int plan_groups(axia_ctx* ctx, int lanes, int vec) {
   const int nm = (int)ctx->mesh_node0.size() - 1;
   int per_sm = 0;
-  AXIA_TRY(group_kernel_capacity(ctx, lanes, &per_sm));
+  AXIA_TRY(group_kernel_capacity(ctx, lanes, vec, &per_sm));
   const int cap = std::max(1, per_sm) * ctx->sm_count;
   if (nm > cap)
     return set_error(ctx, AXIA_ERR_TOO_LARGE, std::to_string(nm) + " meshes exceed the " + std::to_string(cap) +
@@ -50,16 +50,28 @@ int plan_groups(axia_ctx* ctx, int lanes) {
     w[k] = std::max(1.0, (double)ctx->mesh_blocks[k]) * std::max(1.0, std::cbrt(nodes));
     wsum += w[k];
   }
+  // blocks in proportion to the work, at least one each; the blocks left by
+  // rounding down go to the groups with the largest remainders
   std::vector<int> nc(nm);
+  std::vector<double> rem(nm);
   int total = 0;
   for (int k = 0; k < nm; ++k) {
-    nc[k] = std::max(1, (int)std::floor(cap * w[k] / wsum));
+    const double share = cap * w[k] / wsum;
+    nc[k] = std::max(1, (int)std::floor(share));
+    rem[k] = share - std::floor(share);
     total += nc[k];
   }
   while (total > cap) {  // trim the largest groups
     int big = (int)(std::max_element(nc.begin(), nc.end()) - nc.begin());
     --nc[big];
     --total;
+  }
+  while (total < cap) {
+    int k = (int)(std::max_element(rem.begin(), rem.end()) - rem.begin());
+    if (rem[k] <= 0.0) break;
+    ++nc[k];
+    rem[k] = 0.0;
+    ++total;
   }
   std::vector<MeshGroup> groups(nm);
   std::vector<int> cta_group(total);
@@ -81,6 +93,7 @@ int plan_groups(axia_ctx* ctx, int lanes) {
   AXIA_CUDA(ctx, cudaMemcpy(ctx->d_mcta, cta_group.data(), sizeof(int) * total, cudaMemcpyHostToDevice));
   ctx->multi_grid = total;
   ctx->multi_lanes = lanes;
+  ctx->multi_vec = vec;
   ctx->multi_ctas.assign(nc.begin(), nc.end());
   drop_graph(ctx);
   return AXIA_OK;
@@ -99,7 +112,7 @@ int capture_graph(axia_ctx* ctx, const double* d_f, double* d_u, double rtol, do
   if (rc == AXIA_OK)
     rc = launch_group_reliable(ctx, args, (const MeshGroup*)ctx->d_mgroups,
                                ctx->d_mcta, ctx->d_mbars, ctx->d_mtotals, (PcgOut*)ctx->d_mouts, ctx->multi_grid,
-                               ctx->multi_lanes);
+                               ctx->multi_lanes, ctx->multi_vec);
   if (rc == AXIA_OK) rc = launch_full_reconstruct(ctx, d_u);
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   ctx->launches = launches_before;
@@ -128,8 +141,9 @@ int solve_multi_device(axia_ctx* ctx, const double* d_f, double* d_u, const axia
     return set_error(ctx, AXIA_ERR_STATE, "solve_multi needs axia_gpu_assemble_ex(AXIA_ASM_BSR64 | AXIA_ASM_BSR32)");
   const int nm = (int)ctx->mesh_node0.size() - 1;
   AXIA_TRY(prepare_full_buffers(ctx));
-  const int lanes = opts->spmv_lanes == 4 || opts->spmv_lanes == 8 || opts->spmv_lanes == 16 ? opts->spmv_lanes : 16;
-  if (ctx->multi_grid == 0 || ctx->multi_lanes != lanes) AXIA_TRY(plan_groups(ctx, lanes));
+  int lanes = 0, vec = 0;
+  group_layout(ctx, opts->spmv_lanes, opts->spmv_vec, &lanes, &vec);
+  if (ctx->multi_grid == 0 || ctx->multi_lanes != lanes || ctx->multi_vec != vec) AXIA_TRY(plan_groups(ctx, lanes, vec));
   const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.01;
   long long max_iter = opts->max_iter > 0 ? opts->max_iter : 0;
   if (max_iter == 0) {
@@ -198,6 +212,7 @@ void multimesh_release(axia_ctx* ctx) {
   dev_free(ctx->d_mouts);
   ctx->multi_grid = 0;
   ctx->multi_lanes = 0;
+  ctx->multi_vec = 0;
   ctx->multi_ctas.clear();
 }
 

@@ -123,9 +123,10 @@ struct BsrReliableArgs {
 };
 
 BsrReliableArgs make_reliable_args(axia_ctx* ctx, double rtol, double delta, long long max_iter);
-int group_kernel_capacity(axia_ctx* ctx, int lanes, int* per_sm);
+int group_kernel_capacity(axia_ctx* ctx, int lanes, int vec, int* per_sm);
+void group_layout(const axia_ctx* ctx, int lanes_req, int vec_req, int* lanes, int* vec);
 int launch_group_reliable(axia_ctx* ctx, BsrReliableArgs& P, const MeshGroup* groups, const int* cta_group,
-                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes);
+                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes, int vec);
 int launch_full_rhs(axia_ctx* ctx, const double* d_f);
 int launch_full_reconstruct(axia_ctx* ctx, double* d_u);
 int prepare_full_buffers(axia_ctx* ctx);

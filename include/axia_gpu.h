@@ -104,7 +104,7 @@ typedef struct axia_solve_opts {
   int32_t max_outer;       /* mixed: refinement steps allowed */
   int32_t spmv_lanes;      /* lanes per row in the SpMV: 0 = automatic, else 1..32 (power of two) */
   int32_t matrix_format;   /* axia_matrix_format */
-  int32_t reserved;
+  int32_t spmv_vec;        /* node-block form: blocks per lane load (1, 2, 4; 0 = automatic) */
 } axia_solve_opts;
 
 typedef struct axia_solve_info {
@@ -216,9 +216,10 @@ AXIA_API int32_t axia_gpu_spmv_device(axia_ctx* ctx, int32_t precision, const vo
                                       int32_t lanes);
 
 /* y = K x on the full-DOF node-block form (x, y of 3*n_nodes entries,
- * double for AXIA_PREC_FP64, float for AXIA_PREC_MIXED). */
+ * double for AXIA_PREC_FP64, float for AXIA_PREC_MIXED); lanes per block row
+ * and blocks per lane load (vec) as in axia_solve_opts, 0 = automatic. */
 AXIA_API int32_t axia_gpu_bsr_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev,
-                                          int32_t lanes);
+                                          int32_t lanes, int32_t vec);
 
 /* Number of 3x3 node blocks of the node-block form (node adjacency entries). */
 AXIA_API int64_t axia_gpu_node_blocks(const axia_ctx* ctx);
@@ -303,6 +304,29 @@ AXIA_API int32_t axia_gpu_recover(axia_ctx* ctx, const double* u_full, const dou
 AXIA_API int32_t axia_gpu_recover_device(axia_ctx* ctx, const double* u_full_dev, const double* f_full_dev,
                                          double e_strain, double* stress, double* strain, double* vm, double* rf,
                                          double* elem_stress);
+
+/* solve_kff on the GPU for callers that build K_ff themselves (replaces
+ * solver/src/linalg.rs:311 with the PCG backend, and csr_from_triplets
+ * linalg.rs:10-38 before it): n_trips triplets (ti, tj, tv) in the caller's
+ * order; entries with ti or tj >= n or tv == 0 (or NaN) are dropped, equal
+ * (i, j) are summed in input order after a stable sort, exactly as the
+ * reference.  Then Jacobi PCG from x = 0 to ||r|| <= opts->rtol ||rhs||
+ * (rtol <= 0: 1e-8 as solve_kff's PCG, linalg.rs:363; max_iter <= 0:
+ * max(4n, 200)); opts->precision MIXED runs the FP32 inner / FP64 update
+ * solver on an FP32 copy.  x [n] out; info->iters, residual, bnorm,
+ * true_residual, nnz.  A negative index is AXIA_ERR_INVALID_ARG (bad_index =
+ * the triplet).  Replaces any mesh set up on the context (call
+ * axia_gpu_setup again for the mesh path).  opts->matrix_format must be CSR. */
+AXIA_API int32_t axia_gpu_solve_triplets(axia_ctx* ctx, int64_t n, int64_t n_trips, const int64_t* ti,
+                                         const int64_t* tj, const double* tv, const double* rhs, double* x,
+                                         const axia_solve_opts* opts, axia_solve_info* info);
+
+/* The same for a caller's CSR (the reference's Csr: int64 indptr [n+1],
+ * indices [nnz], data [nnz], full symmetric storage).  An index outside
+ * [0, n) is AXIA_ERR_INVALID_ARG. */
+AXIA_API int32_t axia_gpu_solve_csr(axia_ctx* ctx, int64_t n, const int64_t* indptr, const int64_t* indices,
+                                    const double* data, const double* rhs, double* x, const axia_solve_opts* opts,
+                                    axia_solve_info* info);
 
 /* Sizes of the assembled system: n_free and nnz. */
 AXIA_API int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz);

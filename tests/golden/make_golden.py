@@ -34,6 +34,14 @@ PINS = {
                             "source": "solver/src/lib.rs:440-446 (patch_test_c3d8: mean nodal sxx, vm > 0)"},
     "patch_c3d20_mean_sxx": {"value": -210.0, "tol": 1.0,
                              "source": "solver/src/lib.rs:764-772 (patch_test_c3d20: mean nodal sxx)"},
+    "le10_c3d20_syy_D": {"value": -5.51, "tol": 0.005, "target": -5.38, "target_rel_tol": 0.05,
+                         "fixture": "le10_c3d20.json",
+                         "source": "solver/src/nafems.rs:49-67 (nafems_le10_thick_plate, target -5.38 within 5 %); "
+                                   "examples/nafems/README.md:13 (the reference's result -5.51)"},
+    "le10_c3d20_fine_syy_D": {"value": -5.50, "tol": 0.005, "target": -5.38, "target_rel_tol": 0.03,
+                              "fixture": "le10_c3d20_fine.json",
+                              "source": "solver/src/nafems.rs:70-88 (refined, target within 3 %); "
+                                        "examples/nafems/README.md:14 (the reference's result -5.50)"},
     "hex20_partition_of_unity": {"value": 1.0, "tol": 1e-12,
                                  "source": "solver/src/quadratic.rs:890-894 (hex20_partition)"},
     "quad8_partition_of_unity": {"value": 1.0, "tol": 1e-12,

@@ -107,3 +107,29 @@ def test_recover_device_pointers_and_errors(gpu_ctx):
     # strain with a non-positive modulus is a material error
     with pytest.raises(RuntimeError, match="MATERIAL|strain"):
         gpu_ctx.recover(ref.u, ref.f, e_strain=0.0)
+
+
+@pytest.mark.parametrize("key", ["le10_c3d20_syy_D", "le10_c3d20_fine_syy_D"])
+@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED])
+def test_nafems_le10_through_gpu(gpu_ctx, key, precision):
+    """The reference's LE10 decks end to end on the GPU: face pressure, C3D20
+    assembly, solve, stress recovery; sigma_yy(D) against the oracle and the
+    reference's pins (nafems.rs:49-88)."""
+    pin = GOLD["pins"][key]
+    m = meshgen.from_fixture(os.path.join(os.path.dirname(__file__), "golden", pin["fixture"]))
+    ref = O.solve_static(m, solver=O.SOLVER_PCG, tol=1e-12)
+    s_ref, _ = O.nodal_stress(m, ref.u)
+    gpu_ctx.setup(m)
+    f = gpu_ctx.load_vector(m)
+    if precision == _lib.PREC_FP64:
+        gpu_ctx.assemble(precision)
+        u, _ = gpu_ctx.solve(f, rtol=1e-12)
+    else:
+        gpu_ctx.assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+        u, _ = gpu_ctx.solve(f, rtol=1e-12, precision=precision, refine_mode=_lib.REFINE_RELIABLE, inner_rtol=0.1,
+                             matrix_format=_lib.FORMAT_BSR3)
+    stress, _, _, rf, _ = gpu_ctx.recover(u, f)
+    syy = stress[m.node_d, 1]
+    assert abs(syy - s_ref[m.node_d, 1]) <= 1e-8 * abs(s_ref[m.node_d, 1])
+    assert abs(syy - pin["value"]) <= pin["tol"]
+    assert abs(syy - pin["target"]) / abs(pin["target"]) < pin["target_rel_tol"]

@@ -162,3 +162,17 @@ def test_reactions_balance_and_golden():
     np.testing.assert_allclose(rf, g["rf"], rtol=0, atol=1e-9 * scale)
     s, vm = O.nodal_stress(m, np.array(g["u"]))
     np.testing.assert_allclose(vm, g["vm"], rtol=1e-12, atol=1e-12 * np.abs(vm).max())
+
+
+@pytest.mark.parametrize("key", ["le10_c3d20_syy_D", "le10_c3d20_fine_syy_D"])
+def test_nafems_le10_stress_pin(key):
+    """NAFEMS LE10 on the reference's own decks: sigma_yy at node D equals the
+    reference's result (README, 2 decimals) and the NAFEMS target within the
+    reference test's tolerance (nafems.rs:49-88)."""
+    pin = PINS[key]
+    m = meshgen.from_fixture(os.path.join(os.path.dirname(__file__), "golden", pin["fixture"]))
+    r = O.solve_static(m, solver=O.SOLVER_PCG, tol=1e-12)
+    s, _ = O.nodal_stress(m, r.u)
+    syy = s[m.node_d, 1]
+    assert abs(syy - pin["value"]) <= pin["tol"]
+    assert abs(syy - pin["target"]) / abs(pin["target"]) < pin["target_rel_tol"]
