@@ -101,6 +101,8 @@ SIGNATURES = [
     ("axia_gpu_recover", C.c_int32, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P]),
     ("axia_gpu_solve_triplets", C.c_int32, [_P, C.c_int64, C.c_int64, _P, _P, _P, _P, _P, C.POINTER(SolveOpts),
                                             C.POINTER(SolveInfo)]),
+    ("axia_gpu_autotune", C.c_int32, [_P, C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_double)]),
     ("axia_gpu_solve_csr", C.c_int32, [_P, C.c_int64, _P, _P, _P, _P, _P, C.POINTER(SolveOpts),
                                        C.POINTER(SolveInfo)]),
     ("axia_gpu_recover_device", C.c_int32, [_P, _P, _P, C.c_double, _P, _P, _P, _P, _P]),

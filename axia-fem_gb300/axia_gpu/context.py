@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -270,6 +271,14 @@ class GpuContext:
         self._check(self.lib.axia_gpu_solve_batched_device(self.h, nrhs, C.c_void_p(F_dev_ptr), C.c_void_p(U_dev_ptr),
                                                            C.byref(o), C.byref(info), L.ptr(rel)), "solve_batched")
         return info, rel
+
+    def autotune(self, cache_path=None):
+        """Time the node-block layouts of the mixed solver on the assembled mesh and keep
+        the fastest for later solves; returns (lanes, vec, us_per_iter)."""
+        lanes, vec, us = C.c_int32(), C.c_int32(), C.c_double()
+        path = None if cache_path is None else os.fsencode(cache_path)
+        self._check(self.lib.axia_gpu_autotune(self.h, path, C.byref(lanes), C.byref(vec), C.byref(us)), "autotune")
+        return lanes.value, vec.value, us.value
 
     def solve_kff(self, n, trips, rhs, **kw):
         """solve_kff on the GPU (linalg.rs:311 with PCG): trips = (i, j, v) arrays in the

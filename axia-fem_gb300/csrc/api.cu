@@ -26,6 +26,7 @@ int reconstruct(axia_ctx* ctx, double* d_u);
 int true_residual(axia_ctx* ctx, double* out);
 int prepare_solve(axia_ctx* ctx, bool mixed);
 int spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req);
+int bsr_autotune(axia_ctx* ctx, const char* cache_path, int* lanes_out, int* vec_out, double* us_out);
 int raw_system_from_triplets(axia_ctx* ctx, int64_t n, int64_t nt, const int64_t* h_i, const int64_t* h_j,
                              const double* h_v, bool fp32);
 int raw_system_from_csr(axia_ctx* ctx, int64_t n, const int64_t* h_indptr, const int64_t* h_indices,
@@ -460,6 +461,17 @@ int32_t axia_gpu_solve_csr(axia_ctx* ctx, int64_t n, const int64_t* indptr, cons
   const bool mixed = opts && opts->precision == AXIA_PREC_MIXED;
   AXIA_TRY(raw_system_from_csr(ctx, n, indptr, indices, data, mixed));
   return solve_raw(ctx, rhs, x, opts, info);
+}
+
+int32_t axia_gpu_autotune(axia_ctx* ctx, const char* cache_path, int32_t* lanes, int32_t* vec,
+                          double* us_per_iter) {
+  if (!ctx || !lanes || !vec) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  int l = 0, v = 0;
+  AXIA_TRY(bsr_autotune(ctx, cache_path, &l, &v, us_per_iter));
+  *lanes = l;
+  *vec = v;
+  return AXIA_OK;
 }
 
 int32_t axia_gpu_set_stream(axia_ctx* ctx, void* stream) {

@@ -22,6 +22,9 @@
 // solver/src/linalg.rs:199-259, FP64 or FP32) and pcg_bsr_reliable_kernel
 // (FP32 inner CG with FP64 reliable updates, the mixed form).
 #include <algorithm>
+#include <string>
+#include <cstdlib>
+#include <cstdio>
 #include <type_traits>
 #include <vector>
 #include <cmath>
@@ -465,6 +468,7 @@ struct RowLayout {
 static RowLayout bsr_layout(const axia_ctx* ctx, bool fp32, int lanes_req, int vec_req) {
   const double avg = ctx->n_nodes ? (double)ctx->nbq / (double)ctx->n_nodes : 4.0;  // padded blocks per row
   RowLayout r{0, 0};
+  if (fp32 && lanes_req == 0 && vec_req == 0 && ctx->tuned_vec > 0) return RowLayout{ctx->tuned_lanes, ctx->tuned_vec};
   r.vec = (vec_req == 1 || vec_req == 2 || (fp32 && vec_req == 4)) ? vec_req : (fp32 ? 4 : 2);
   const double steps = avg / r.vec;  // vector steps per row
   const int auto_l = steps <= 3 ? 2 : (steps <= 6 ? 4 : (steps <= 12 ? 8 : 16));
@@ -714,5 +718,125 @@ int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_
   }
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());
+  return AXIA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner for the layout of the FP32 inner loop
+// ---------------------------------------------------------------------------
+// Candidates: the instantiated (lanes, blocks per load) pairs.  Each runs the
+// mixed solver's persistent kernel for a fixed number of CG iterations on a
+// unit load (ones on free DOFs), timed with CUDA events on the context's
+// stream; the fastest per iteration wins.  Results are cached in a text file
+// of JSON lines {"key": ..., "lanes": L, "vec": V, "us_per_iter": t}, keyed by
+// the device name and the shape of the matrix (nodes per element, reduced
+// integration, padded blocks per row, node count bucket).
+namespace {
+
+__global__ void k_fill_ones(int64_t n, double* f) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    f[i] = 1.0;
+}
+
+std::string tune_key(const axia_ctx* ctx) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, ctx->device);
+  const double rb = ctx->n_nodes ? (double)ctx->nbq / (double)ctx->n_nodes : 0.0;
+  int bucket = 0;
+  for (int64_t n = ctx->n_nodes; n > 1; n >>= 1) ++bucket;
+  std::string name(prop.name);
+  for (char& c : name)
+    if (c == '"' || c == '\\') c = '_';
+  return name + "|nn=" + std::to_string(ctx->nn) + "|r=" + std::to_string(ctx->reduced) +
+         "|rowblocks=" + std::to_string((int)std::lround(rb)) + "|log2nodes=" + std::to_string(bucket);
+}
+
+bool cache_lookup(const char* path, const std::string& key, int* lanes, int* vec) {
+  FILE* fh = path ? std::fopen(path, "r") : nullptr;
+  if (!fh) return false;
+  char line[1024];
+  const std::string want = "\"key\": \"" + key + "\"";
+  bool found = false;
+  while (std::fgets(line, sizeof(line), fh)) {
+    const std::string l(line);
+    if (l.find(want) == std::string::npos) continue;
+    const size_t pl = l.find("\"lanes\": "), pv = l.find("\"vec\": ");
+    if (pl == std::string::npos || pv == std::string::npos) continue;
+    *lanes = std::atoi(l.c_str() + pl + 9);
+    *vec = std::atoi(l.c_str() + pv + 7);
+    found = true;  // the last matching line wins
+  }
+  std::fclose(fh);
+  return found;
+}
+
+}  // namespace
+
+int bsr_autotune(axia_ctx* ctx, const char* cache_path, int* lanes_out, int* vec_out, double* us_out) {
+  if (!ctx->have_bsr32 || !ctx->have_bsr64)
+    return set_error(ctx, AXIA_ERR_STATE, "autotune needs axia_gpu_assemble_ex(AXIA_ASM_BSR64 | AXIA_ASM_BSR32)");
+  const std::string key = tune_key(ctx);
+  int l = 0, v = 0;
+  if (cache_lookup(cache_path, key, &l, &v)) {
+    const RowLayout r = bsr_layout(ctx, true, l, v);
+    if (r.lanes == l && r.vec == v) {
+      ctx->tuned_lanes = l;
+      ctx->tuned_vec = v;
+      *lanes_out = l;
+      *vec_out = v;
+      if (us_out) *us_out = 0.0;
+      return AXIA_OK;
+    }
+  }
+  AXIA_TRY(ensure_full_buffers(ctx, true));
+  double* d_ones = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_ones, (size_t)ctx->ndof));
+  k_fill_ones<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>(ctx->ndof, d_ones);
+  int st = launch_full_rhs(ctx, d_ones);
+  const RowLayout cands[] = {{8, 4}, {4, 4}, {2, 4}, {8, 2}, {4, 2}, {16, 1}, {8, 1}, {4, 1}};
+  const long long iters = 40;
+  double best = 1e300;
+  RowLayout pick{0, 0};
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (st == AXIA_OK && (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess))
+    st = set_error(ctx, AXIA_ERR_CUDA, "autotune events");
+  for (const RowLayout& c : cands) {
+    if (st != AXIA_OK) break;
+    BsrReliableArgs P = make_reliable_args(ctx, 1e-30, 0.01, iters);
+    float best_c = 1e30f;
+    for (int rep = 0; rep < 2 && st == AXIA_OK; ++rep) {
+      if ((st = reset_dev_status(ctx)) != AXIA_OK) break;
+      cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream);
+      cudaEventRecord(a, ctx->stream);
+      st = launch_bsr_rel(ctx, P, c);
+      cudaEventRecord(b, ctx->stream);
+      if (st != AXIA_OK) break;
+      PcgOut o{};
+      if ((st = read_out(ctx, &o)) != AXIA_OK) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      best_c = std::min(best_c, ms / (float)std::max<long long>(o.iters, 1));
+    }
+    if (st == AXIA_OK && best_c < best) {
+      best = best_c;
+      pick = c;
+    }
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  dev_free(d_ones);
+  if (st != AXIA_OK) return st;
+  ctx->tuned_lanes = pick.lanes;
+  ctx->tuned_vec = pick.vec;
+  *lanes_out = pick.lanes;
+  *vec_out = pick.vec;
+  if (us_out) *us_out = best * 1e3;
+  if (cache_path) {
+    if (FILE* fh = std::fopen(cache_path, "a")) {
+      std::fprintf(fh, "{\"key\": \"%s\", \"lanes\": %d, \"vec\": %d, \"us_per_iter\": %.3f}\n", key.c_str(),
+                   pick.lanes, pick.vec, best * 1e3);
+      std::fclose(fh);
+    }
+  }
   return AXIA_OK;
 }

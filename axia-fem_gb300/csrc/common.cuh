@@ -276,6 +276,7 @@ struct axia_ctx {
   double* d_mtotals = nullptr;
   unsigned char* d_mouts = nullptr;   // PcgOut[n_meshes]
   int multi_grid = 0, multi_lanes = 0, multi_vec = 0;
+  int tuned_lanes = 0, tuned_vec = 0;  // node-block layout chosen by axia_gpu_autotune (0: none)
   void* multi_graph = nullptr;        // cudaGraphExec_t
   const double* graph_f = nullptr;
   double* graph_u = nullptr;

@@ -100,6 +100,15 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# DRAM bytes per algorithmic byte of pcg_bsr_reliable_kernel<8, 4>, from the ncu
+# capture of the same kernel on the 60^3 block (75.49 GB over 300 iterations
+# against 273.5 MB of algorithmic bytes per iteration; the matrix, padding
+# included, is streamed once per iteration and the CG vectors stay in L2);
+# scaled to a launch here by its algorithmic bytes (traffic grows with the
+# iteration count and the matrix size).
+MIXED_TRAFFIC_PER_ALG_BYTE = 0.920
+
+
 def spmv_bytes(nnz, n, vbytes):
     """Algorithmic bytes of y = K x in CSR with int32 indices: values, columns,
     row pointers, x once, y once."""
@@ -467,6 +476,12 @@ def main():
     mixed_csr_kw = dict(precision=L.PREC_MIXED, refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta,
                         spmv_lanes=args.lanes32csr, matrix_format=L.FORMAT_CSR)
     umc = torch.empty_like(f_dev)
+    # layout of the FP32 inner loop, picked by the library's autotuner (untimed)
+    ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+    tuned = {"lanes": None, "vec": None}
+    if not args.lanes32:
+        lanes_t, vec_t, us_t = ctx.autotune()
+        tuned = {"lanes": lanes_t, "vec": vec_t, "us_per_iter": us_t}
     with ClockSampler(local) as clk:
         ms64, inf64, la64 = timed(L.ASM_CSR64, fp64_kw, u64)
         msmx, infmx, lamx = timed(L.ASM_BSR64 | L.ASM_BSR32, mixed_kw, umx)
@@ -533,10 +548,21 @@ def main():
                 "kernels": "element_recover_kernel<8,8> + k_recover_nodes",
                 "bound": "fp64 pipe (about 7 kFLOP per C3D8 element)"}
 
-    # accuracy: mixed vs FP64 solution, both with true FP64 residual <= 1e-10 ||b||
+    # accuracy: mixed vs FP64 solution, both with true FP64 residual <= 1e-10 ||b||, and both
+    # against an FP64 solve to rtol 1e-12 (untimed; the direct oracle does not reach 3M DOF)
     u64h = u64.cpu().numpy()
     rel_mx = float(np.linalg.norm(umx.cpu().numpy() - u64h) / np.linalg.norm(u64h))
     rel_mc = float(np.linalg.norm(umc.cpu().numpy() - u64h) / np.linalg.norm(u64h))
+    ctx.assemble_ex(L.ASM_CSR64)
+    utight = torch.empty_like(f_dev)
+    with torch.cuda.stream(stream):
+        itight = ctx.solve_device(f_dev.data_ptr(), utight.data_ptr(), rtol=1e-12, precision=L.PREC_FP64)
+    torch.cuda.synchronize()
+    uth = utight.cpu().numpy()
+    tight = {"rtol": 1e-12, "iters": itight.iters, "true_rel_residual": itight.true_residual / itight.bnorm,
+             "rel_err_fp64": float(np.linalg.norm(u64h - uth) / np.linalg.norm(uth)),
+             "rel_err_mixed": float(np.linalg.norm(umx.cpu().numpy() - uth) / np.linalg.norm(uth)),
+             "rel_err_mixed_csr": float(np.linalg.norm(umc.cpu().numpy() - uth) / np.linalg.norm(uth))}
 
     last64, lastmx, lastmc = inf64[-1], infmx[-1], infmc[-1]
     mdofs = n / (msmx * 1e-3) / 1e6 * world
@@ -610,6 +636,8 @@ def main():
                       "reliable_updates": lastmc["outer_iters"], "format": "CSR int32",
                       "ms_assemble": lastmc["ms_assemble"], "ms_solve": lastmc["ms_solve"],
                       "true_rel_residual": lastmc["true_residual"] / lastmc["bnorm"], "rel_err_vs_fp64": rel_mc},
+        "vs_fp64_rtol_1e-12": tight,
+        "layout_fp32": tuned,
         "speedup_mixed_vs_fp64": ms64 / msmx,
         "speedup_mixed_vs_fp64_solve": last64["ms_solve"] / lastmx["ms_solve"],
         "speedup_mixed_csr_vs_fp64": ms64 / msmc,
@@ -617,7 +645,10 @@ def main():
         "spmv": spmv,
         "recovery": recovery,
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
-                     "traffic": None, "kernel": "pcg_bsr_reliable_kernel (FP32 node-block CG + FP64 updates)",
+                     "traffic": bytes32 * MIXED_TRAFFIC_PER_ALG_BYTE,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same kernel at 60^3, "
+                                       "per algorithmic byte, scaled to this launch",
+                     "kernel": "pcg_bsr_reliable_kernel (FP32 node-block CG + FP64 updates)",
                      "peak_source": f"{pk_kind} hbm_gbs", "bytes_per_launch": bytes32, "ms_per_launch": k32_ms},
         "roofline_fp64_pcg": {"bound": "hbm", "achieved": ach64, "peak": hbm, "unit": "GB/s", "frac": ach64 / hbm,
                               "kernel": "pcg_kernel<double> (CSR)", "ms_per_launch": k64_ms,

@@ -328,6 +328,19 @@ AXIA_API int32_t axia_gpu_solve_csr(axia_ctx* ctx, int64_t n, const int64_t* ind
                                     const double* data, const double* rhs, double* x, const axia_solve_opts* opts,
                                     axia_solve_info* info);
 
+/* Picks the node-block layout of the mixed solver's FP32 inner loop (lanes
+ * per block row, blocks per lane load) for the assembled mesh by timing each
+ * instantiated layout for 40 CG iterations of the persistent kernel, and
+ * uses it for later solves whose opts leave spmv_lanes and spmv_vec at 0.
+ * cache_path (may be NULL): a text file of JSON lines; a stored choice for
+ * the same device and matrix shape is reused without timing, a new one is
+ * appended.  Needs axia_gpu_assemble_ex(AXIA_ASM_BSR64 | AXIA_ASM_BSR32).
+ * us_per_iter (may be NULL) receives the winner's time per iteration (0 when
+ * it came from the cache).  No reference counterpart (the reference has no
+ * GPU kernels to tune). */
+AXIA_API int32_t axia_gpu_autotune(axia_ctx* ctx, const char* cache_path, int32_t* lanes, int32_t* vec,
+                                   double* us_per_iter);
+
 /* Sizes of the assembled system: n_free and nnz. */
 AXIA_API int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz);
 
