@@ -78,6 +78,42 @@ __device__ __forceinline__ void bsr_row_multi(int a, int lane, const BsrMatM<V>&
     }
 }
 
+// Y[3a+i][4 cl + 2 h + c], c = 0, 1: two of the lane's four load cases in FP64.
+// The FP64 residual of a reliable update runs in two such halves so that the
+// kernel fits the register budget of two blocks per SM.
+__device__ __forceinline__ void bsr_row_multi_half(int a, int lane, const BsrMatM<double>& M, const double* X, int h,
+                                                   double y[3][2]) {
+  const int cl = lane % LPG, grp = lane / LPG;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) y[i][0] = y[i][1] = 0.0;
+  const int beg = __ldg(M.adj_ptr + a), end = __ldg(M.adj_ptr + a + 1);
+  for (int s = beg + grp; s < end; s += 32 / LPG) {
+    const int b = ld_stream(M.adj + s);
+    double v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = ld_stream(M.val + (long long)k * M.nb + s);
+    double x[3][2];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double2 t = *reinterpret_cast<const double2*>(X + (size_t)(3 * b + j) * NR + CPL * cl + 2 * h);
+      x[j][0] = t.x;
+      x[j][1] = t.y;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+        y[i][c] = fma(v[3 * i], x[0][c], fma(v[3 * i + 1], x[1][c], fma(v[3 * i + 2], x[2][c], y[i][c])));
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 8);
+      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 16);
+    }
+}
+
 // Per-column partial sums of this block: v[c] is this thread's contribution
 // to column 4*(tid%8)+c.  Written to partials[(slot0 + col) * G + block].
 template <typename A>
@@ -186,7 +222,7 @@ struct MultiArgs {
 
 constexpr int SL_A = 0, SL_B = NR;  // two banks of NR slots
 
-__global__ void __launch_bounds__(PCG_THREADS, 1) pcg_bsr_multi_kernel(MultiArgs P) {
+__global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs P) {
   __shared__ double s_rz[NR], s_bnorm[NR], s_rmax[NR], s_res[NR];
   __shared__ float s_alpha[NR], s_beta[NR];
   __shared__ int s_active[NR], s_flag;
@@ -335,24 +371,24 @@ __global__ void __launch_bounds__(PCG_THREADS, 1) pcg_bsr_multi_kernel(MultiArgs
       double rr64[CPL] = {0, 0, 0, 0};
       float rz2[CPL] = {0, 0, 0, 0};
       for (int a = gwarp; a < n_nodes; a += nwarps) {
-        double y[3][CPL];
-        bsr_row_multi<double>(a, lane, P.M64, P.X, y);
-        if (lane < LPG) {
 #pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            const size_t off = (size_t)(3 * a + i) * NR + CPL * lane;
-            double bv[CPL];
-            ld4(P.B + off, bv);
-            const float di = P.dinv32[3 * a + i];
-            float r32[CPL];
+        for (int h = 0; h < 2; ++h) {
+          double y[3][2];
+          bsr_row_multi_half(a, lane, P.M64, P.X, h, y);
+          if (lane < LPG) {
 #pragma unroll
-            for (int c = 0; c < CPL; ++c) {
-              const double rv = bv[c] - y[i][c];
-              rr64[c] = fma(rv, rv, rr64[c]);
-              r32[c] = (float)rv;
-              rz2[c] = fmaf(r32[c], r32[c] * di, rz2[c]);
+            for (int i = 0; i < 3; ++i) {
+              const size_t off = (size_t)(3 * a + i) * NR + CPL * lane + 2 * h;
+              const double2 bv = *reinterpret_cast<const double2*>(P.B + off);
+              const float di = P.dinv32[3 * a + i];
+              const double rv0 = bv.x - y[i][0], rv1 = bv.y - y[i][1];
+              rr64[2 * h] = fma(rv0, rv0, rr64[2 * h]);
+              rr64[2 * h + 1] = fma(rv1, rv1, rr64[2 * h + 1]);
+              const float2 r32 = make_float2((float)rv0, (float)rv1);
+              rz2[2 * h] = fmaf(r32.x, r32.x * di, rz2[2 * h]);
+              rz2[2 * h + 1] = fmaf(r32.y, r32.y * di, rz2[2 * h + 1]);
+              *reinterpret_cast<float2*>(P.R32 + off) = r32;
             }
-            st4(P.R32 + off, r32);
           }
         }
       }

@@ -376,7 +376,7 @@ def main():
     ap.add_argument("--lanes32", type=int, default=0)
     ap.add_argument("--lanes32csr", type=int, default=0)
     ap.add_argument("--delta", type=float, default=0.01, help="reliable-update residual reduction")
-    ap.add_argument("--only", choices=["mixed", "fp64", "spmv"], default=None,
+    ap.add_argument("--only", choices=["mixed", "fp64", "spmv", "batch"], default=None,
                     help="run one solve (or SpMV sweep) once and exit: the profiling entry")
     ap.add_argument("--max-iter", type=int, default=0, help="with --only: cap the CG iterations")
     ap.add_argument("--workload", choices=["c2", "c3", "c4a", "c4b", "c5"], default="c2",
@@ -404,6 +404,23 @@ def main():
         dist.init_process_group("nccl")
 
     from axia_gpu import GpuContext, _lib as L, meshgen, replicas
+
+    if args.only == "batch":
+        # one batched solve of 32 load cases on an n^3 block: the profiling entry of the batched kernel
+        m = meshgen.block_c3d8_multiload(n=args.n, nrhs=32)
+        ctx = GpuContext(local)
+        ctx.setup(m)
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        F = torch.from_numpy(m.cload_batch).to(f"cuda:{local}")
+        U = torch.empty_like(F)
+        try:
+            info, rel = ctx.solve_batched_device(32, F.data_ptr(), U.data_ptr(), rtol=RTOL, inner_rtol=args.delta,
+                                                 max_iter=args.max_iter)
+            print(json.dumps({"only": "batch", "iters": info.iters, "ms_kernel": info.ms_pcg_kernel}))
+        except Exception as e:  # a capped iteration count ends as NOT_CONVERGED
+            print(json.dumps({"only": "batch", "status": str(e)[:120]}))
+        torch.cuda.synchronize()
+        return
 
     model = meshgen.block_c3d8_pressure(n=args.n)
     ctx = GpuContext(local)

@@ -904,6 +904,220 @@ void or_csr_export(const OrCsr* h, int64_t* indptr, int64_t* indices, double* da
 }
 void or_csr_free(OrCsr* h) { delete h; }
 
+// ---------------------------------------------------------------------------
+// DofMap with multi-point constraints (constraint.rs:8-136, 138-172, 207-217,
+// coalesce 219-235).  An MPC is u_slave = sum_m alpha_m u_m + u0.  Prescribed
+// DOFs: later entries of the list win (the HashMap insert of analysis.rs:556-565).
+// ---------------------------------------------------------------------------
+struct OrDofMap {
+  int64_t n_full = 0, n_ind = 0;
+  std::vector<double> u0;
+  std::vector<std::vector<std::pair<int64_t, double>>> t_row;
+  std::vector<int64_t> ind_of;
+};
+
+namespace {
+// constraint.rs:219-235: stable sort by DOF, merge equal DOFs in order, a run
+// starts only with a non-zero term, then drop |alpha| <= 1e-16
+std::vector<std::pair<int64_t, double>> coalesce(std::vector<std::pair<int64_t, double>> terms) {
+  std::stable_sort(terms.begin(), terms.end(),
+                   [](const std::pair<int64_t, double>& a, const std::pair<int64_t, double>& b) { return a.first < b.first; });
+  std::vector<std::pair<int64_t, double>> out;
+  for (const auto& t : terms) {
+    if (!out.empty() && out.back().first == t.first) {
+      out.back().second += t.second;
+      continue;
+    }
+    if (std::fabs(t.second) > 0.0) out.push_back(t);
+  }
+  std::vector<std::pair<int64_t, double>> kept;
+  for (const auto& t : out)
+    if (std::fabs(t.second) > 1e-16) kept.push_back(t);
+  return kept;
+}
+}  // namespace
+
+// mpc_ptr [n_mpc+1] delimits each MPC's masters in mpc_master / mpc_alpha.
+int or_dofmap_build(int64_t ndof, int64_t n_presc, const int64_t* presc_dof, const double* presc_val, int64_t n_mpc,
+                    const int64_t* mpc_slave, const int64_t* mpc_ptr, const int64_t* mpc_master,
+                    const double* mpc_alpha, const double* mpc_u0, OrDofMap** out) {
+  auto* m = new OrDofMap();
+  m->n_full = ndof;
+  m->u0.assign(ndof, 0.0);
+  std::vector<char> is_presc(ndof, 0);
+  std::vector<double> presc(ndof, 0.0);
+  for (int64_t k = 0; k < n_presc; ++k) {
+    const int64_t d = presc_dof[k];
+    if (d < 0 || d >= ndof) continue;
+    is_presc[d] = 1;
+    presc[d] = presc_val[k];
+  }
+  for (int64_t d = 0; d < ndof; ++d)
+    if (is_presc[d]) m->u0[d] = presc[d];
+  // slave_of: the last MPC naming a slave wins (HashMap::insert replaces)
+  std::vector<int64_t> slave_of(ndof, -1);
+  for (int64_t i = 0; i < n_mpc; ++i) {
+    const int64_t s = mpc_slave[i];
+    if (s < 0 || s >= ndof) continue;
+    if (is_presc[s]) continue;
+    slave_of[s] = i;
+  }
+  std::vector<std::vector<std::pair<int64_t, double>>> alphas(ndof);
+  for (int64_t si = 0; si < n_mpc; ++si) {
+    const int64_t s = mpc_slave[si];
+    if (s < 0 || s >= ndof || slave_of[s] != si) continue;
+    std::vector<std::pair<int64_t, double>> terms;
+    for (int64_t k = mpc_ptr[si]; k < mpc_ptr[si + 1]; ++k) terms.push_back({mpc_master[k], mpc_alpha[k]});
+    double particular = mpc_u0[si];
+    for (int pass = 0; pass < 32; ++pass) {
+      std::vector<std::pair<int64_t, double>> next;
+      bool changed = false;
+      for (const auto& t : terms) {
+        const int64_t d = t.first;
+        const double a = t.second;
+        const int64_t k = (d >= 0 && d < ndof) ? slave_of[d] : -1;
+        if (k >= 0) {
+          changed = true;
+          particular += a * mpc_u0[k];
+          for (int64_t q = mpc_ptr[k]; q < mpc_ptr[k + 1]; ++q) next.push_back({mpc_master[q], a * mpc_alpha[q]});
+        } else {
+          next.push_back({d, a});
+        }
+      }
+      terms = coalesce(next);
+      if (!changed) break;
+    }
+    std::vector<std::pair<int64_t, double>> ind_terms;
+    for (const auto& t : terms) {
+      const int64_t d = t.first;
+      if (d < 0 || d >= ndof) {
+        delete m;
+        return ERR_INVALID_ARG;
+      }
+      if (is_presc[d]) {
+        particular += t.second * presc[d];
+      } else if (slave_of[d] >= 0) {
+        delete m;
+        return ERR_INVALID_ARG;  // "MPC: zyklische Mehrpunktbedingung."
+      } else {
+        ind_terms.push_back(t);
+      }
+    }
+    alphas[s] = ind_terms;
+    m->u0[s] = particular;
+  }
+  std::vector<char> is_ind(ndof, 1);
+  bool any_slave = false;
+  for (int64_t d = 0; d < ndof; ++d) {
+    if (is_presc[d]) is_ind[d] = 0;
+    if (slave_of[d] >= 0) {
+      is_ind[d] = 0;
+      any_slave = true;
+    }
+  }
+  m->ind_of.assign(ndof, -1);
+  for (int64_t d = 0; d < ndof; ++d)
+    if (is_ind[d]) m->ind_of[d] = m->n_ind++;
+  bool any_presc = false;
+  for (int64_t d = 0; d < ndof; ++d) any_presc = any_presc || is_presc[d];
+  if (m->n_ind == 0 && !any_slave && !any_presc) {
+    delete m;
+    return ERR_NO_FREE_DOF;
+  }
+  m->t_row.assign(ndof, {});
+  for (int64_t d = 0; d < ndof; ++d) {
+    if (is_ind[d]) {
+      m->t_row[d].push_back({m->ind_of[d], 1.0});
+    } else if (slave_of[d] >= 0) {
+      for (const auto& t : alphas[d]) {
+        const int64_t col = m->ind_of[t.first];
+        if (col >= 0 && std::fabs(t.second) > 0.0) m->t_row[d].push_back({col, t.second});
+      }
+    }
+  }
+  *out = m;
+  return OK;
+}
+
+int64_t or_dofmap_n_ind(const OrDofMap* m) { return m->n_ind; }
+
+// T as CSR over full DOFs (t_ptr [n_full+1], t_col, t_val) and u0
+int64_t or_dofmap_export(const OrDofMap* m, int64_t* t_ptr, int64_t* t_col, double* t_val, double* u0) {
+  int64_t k = 0;
+  for (int64_t d = 0; d < m->n_full; ++d) {
+    if (t_ptr) t_ptr[d] = k;
+    for (const auto& t : m->t_row[d]) {
+      if (t_col) t_col[k] = t.first;
+      if (t_val) t_val[k] = t.second;
+      ++k;
+    }
+  }
+  if (t_ptr) t_ptr[m->n_full] = k;
+  if (u0)
+    for (int64_t d = 0; d < m->n_full; ++d) u0[d] = m->u0[d];
+  return k;
+}
+
+void or_dofmap_free(OrDofMap* m) { delete m; }
+
+// DofMap::reduce (constraint.rs:138-172) followed by csr_from_triplets and the
+// chosen solver, then reconstruct (207-217): the MPC path of solve_linear
+// (analysis.rs:1018-1025).  CSR of K_ff and rhs returned through the handle.
+int or_solve_reduced(const OrDofMap* m, int64_t nt, const int64_t* ti, const int64_t* tj, const double* tv,
+                     const double* f_full, int solver, double tol, int64_t max_iter, double* u_full, double* info,
+                     OrCsr** csr_out, double* rhs_out) {
+  const int64_t n = m->n_ind;
+  std::vector<double> rhs(n, 0.0);
+  for (int64_t i = 0; i < m->n_full; ++i) {
+    const double fi = f_full[i];
+    if (std::fabs(fi) == 0.0) continue;
+    for (const auto& t : m->t_row[i]) rhs[t.first] += t.second * fi;
+  }
+  std::vector<Trip> ff;
+  for (int64_t k = 0; k < nt; ++k) {
+    const int64_t i = ti[k], j = tj[k];
+    const double v = tv[k];
+    if (i < 0 || j < 0 || i >= m->n_full || j >= m->n_full || std::fabs(v) == 0.0) continue;
+    const double u0j = m->u0[j];
+    for (const auto& a : m->t_row[i]) {
+      if (std::fabs(u0j) > 0.0) rhs[a.first] -= v * a.second * u0j;
+      for (const auto& b : m->t_row[j]) ff.push_back({(uint64_t)a.first, (uint64_t)b.first, v * a.second * b.second});
+    }
+  }
+  auto* h = new OrCsr();
+  csr_from_triplets((size_t)n, ff, h->csr);
+  std::vector<double> x(n, 0.0);
+  int st = OK;
+  if (solver == 1) {
+    std::vector<double> dense((size_t)n * n, 0.0);
+    for (int64_t i = 0; i < n; ++i)
+      for (uint64_t k = h->csr.indptr[i]; k < h->csr.indptr[i + 1]; ++k)
+        dense[(size_t)i * n + h->csr.indices[k]] = h->csr.data[k];
+    st = chol_solve(dense.data(), (size_t)n, rhs.data(), x.data());
+    info[0] = 1;
+    info[1] = st == OK ? residual_of(h->csr, x.data(), rhs.data()) : 0.0;
+  } else {
+    size_t mi = max_iter > 0 ? (size_t)max_iter : std::max<size_t>(4 * (size_t)n, 200);
+    size_t iters = 0;
+    double res = 0.0;
+    st = pcg(h->csr, rhs.data(), tol, mi, 1, x.data(), &iters, &res);
+    info[0] = (double)iters;
+    info[1] = res;
+  }
+  for (int64_t d = 0; d < m->n_full; ++d) {
+    double u = m->u0[d];
+    for (const auto& t : m->t_row[d]) u += t.second * x[t.first];
+    u_full[d] = u;
+  }
+  if (rhs_out)
+    for (int64_t i = 0; i < n; ++i) rhs_out[i] = rhs[i];
+  if (csr_out)
+    *csr_out = h;
+  else
+    delete h;
+  return st;
+}
+
 // solve_kff's CSR + backend part (linalg.rs:311-404) on caller triplets:
 // csr_from_triplets, then dense Cholesky (solver=1) or PCG (solver=2).
 // info = {iters, residual}.

@@ -69,6 +69,15 @@ def lib():
                                       C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]
         L.or_reactions.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int64, _i32, _d, C.c_double, _d, _d, _d,
                                    C.POINTER(C.c_int64)]
+        L.or_dofmap_build.argtypes = [C.c_int64, C.c_int64, _i64, _d, C.c_int64, _i64, _i64, _i64, _d, _d,
+                                      C.POINTER(C.c_void_p)]
+        L.or_dofmap_n_ind.argtypes = [C.c_void_p]
+        L.or_dofmap_n_ind.restype = C.c_int64
+        L.or_dofmap_export.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.or_dofmap_export.restype = C.c_int64
+        L.or_dofmap_free.argtypes = [C.c_void_p]
+        L.or_solve_reduced.argtypes = [C.c_void_p, C.c_int64, _i64, _i64, _d, _d, C.c_int, C.c_double, C.c_int64,
+                                       _d, _d, C.POINTER(C.c_void_p), C.c_void_p]
         L.or_compliance_grad.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int64, _i32, _d, C.c_double,
                                          C.c_double, C.c_double, _d, _d, C.POINTER(C.c_int64)]
         _lib = L
@@ -273,3 +282,83 @@ def direct_solve(indptr, indices, data, rhs):
     n = indptr.shape[0] - 1
     K = sp.csr_matrix((data, indices, indptr), shape=(n, n)).tocsc()
     return spla.splu(K, permc_spec="COLAMD").solve(rhs)
+
+
+def mpc_arrays(mpcs):
+    """(slave, [(master, alpha), ...], u0) tuples -> flat arrays (slave, ptr, master, alpha, u0)."""
+    slave = np.array([m[0] for m in mpcs], np.int64)
+    ptr = np.zeros(len(mpcs) + 1, np.int64)
+    for k, m in enumerate(mpcs):
+        ptr[k + 1] = ptr[k] + len(m[1])
+    master = np.array([t[0] for m in mpcs for t in m[1]], np.int64)
+    alpha = np.array([t[1] for m in mpcs for t in m[1]], np.float64)
+    u0 = np.array([m[2] for m in mpcs], np.float64)
+    return slave, ptr, master, alpha, u0
+
+
+class DofMap:
+    """DofMap::build with MPCs (constraint.rs:26-136): T as CSR over full DOFs and u0."""
+
+    def __init__(self, ndof, presc_dof, presc_val, mpcs):
+        L = lib()
+        self.h = C.c_void_p()
+        sl, ptr, ma, al, u0 = mpc_arrays(mpcs)
+        st = L.or_dofmap_build(int(ndof), len(presc_dof), np.ascontiguousarray(presc_dof, np.int64),
+                               np.ascontiguousarray(presc_val, np.float64), len(mpcs), sl, ptr,
+                               ma if ma.size else np.zeros(1, np.int64), al if al.size else np.zeros(1),
+                               u0 if u0.size else np.zeros(1), C.byref(self.h))
+        if st:
+            raise OracleError(st, "dofmap_build")
+        self.ndof = int(ndof)
+        self.n_ind = int(L.or_dofmap_n_ind(self.h))
+        nnz = int(L.or_dofmap_export(self.h, None, None, None, None))
+        self.t_ptr = np.zeros(ndof + 1, np.int64)
+        self.t_col = np.zeros(max(nnz, 1), np.int64)
+        self.t_val = np.zeros(max(nnz, 1))
+        self.u0 = np.zeros(ndof)
+        L.or_dofmap_export(self.h, self.t_ptr.ctypes.data, self.t_col.ctypes.data, self.t_val.ctypes.data,
+                           self.u0.ctypes.data)
+        self.t_col, self.t_val = self.t_col[:nnz], self.t_val[:nnz]
+
+    def solve(self, ti, tj, tv, f_full, solver=SOLVER_CHOLESKY, tol=1e-8, max_iter=0):
+        """reduce -> csr_from_triplets -> solve -> reconstruct; returns u_full, info, (indptr, indices, data), rhs."""
+        L = lib()
+        u = np.zeros(self.ndof)
+        info = np.zeros(2)
+        h = C.c_void_p()
+        rhs = np.zeros(max(self.n_ind, 1))
+        st = L.or_solve_reduced(self.h, len(tv), np.ascontiguousarray(ti, np.int64), np.ascontiguousarray(tj, np.int64),
+                                np.ascontiguousarray(tv, np.float64), np.ascontiguousarray(f_full, np.float64),
+                                int(solver), float(tol), int(max_iter), u, info, C.byref(h), rhs.ctypes.data)
+        csr = None
+        if h.value:
+            n, nnz = L.or_csr_n(h), L.or_csr_nnz(h)
+            indptr, indices, data = np.zeros(n + 1, np.int64), np.zeros(nnz, np.int64), np.zeros(nnz)
+            L.or_csr_export(h, indptr, indices, data)
+            L.or_csr_free(h)
+            csr = (indptr, indices, data)
+        if st:
+            raise OracleError(st, "solve_reduced")
+        return u, info, csr, rhs[:self.n_ind]
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().or_dofmap_free(self.h)
+        except Exception:
+            pass
+
+
+def element_triplets(model):
+    """Full-DOF element triplets in the reference's push order (analysis.rs:651-668):
+    elements ascending, Ke row-major, zero entries skipped."""
+    ti, tj, tv = [], [], []
+    for e in range(model.n_elem):
+        ke, _ = element_ke(model.coords[model.conn[e]], float(model.e_elem[e]), model.nu, reduced=model.reduced)
+        g = (3 * model.conn[e][:, None].astype(np.int64) + np.arange(3)).ravel()
+        I, J = np.meshgrid(g, g, indexing="ij")
+        keep = ke != 0.0
+        ti.append(I[keep])
+        tj.append(J[keep])
+        tv.append(ke[keep])
+    return np.concatenate(ti), np.concatenate(tj), np.concatenate(tv)
