@@ -300,6 +300,26 @@ class GpuContext:
             self._refresh_sizes()
         return x, info
 
+    def solve_reduced(self, dofmap, trips, f_full, **kw):
+        """The MPC path of solve_linear: DofMap::reduce of full-DOF triplets and the load,
+        csr_from_triplets, PCG, reconstruct; returns (u_full, info)."""
+        ti = _c(trips[0], np.int64)
+        tj = _c(trips[1], np.int64)
+        tv = _c(trips[2], np.float64)
+        f = _c(f_full, np.float64)
+        u = np.zeros(dofmap.ndof)
+        kw.setdefault("rtol", 1e-8)
+        o = self.opts(**kw)
+        info = L.SolveInfo()
+        self.model = None
+        try:
+            self._check(self.lib.axia_gpu_solve_reduced(self.h, dofmap.h, int(ti.shape[0]), L.ptr(ti), L.ptr(tj),
+                                                        L.ptr(tv), L.ptr(f), L.ptr(u), C.byref(o), C.byref(info)),
+                        "solve_reduced")
+        finally:
+            self._refresh_sizes()
+        return u, info
+
     def solve_csr(self, n, indptr, indices, data, rhs, **kw):
         """The same for a caller's CSR (int64 indptr / indices, full symmetric storage)."""
         p = _c(indptr, np.int64)

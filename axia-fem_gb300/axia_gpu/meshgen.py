@@ -296,3 +296,57 @@ def from_fixture(path):
               np.array(d["dload_p"], np.float64))
     m.node_d = int(d.get("node_d", -1))
     return m
+
+
+# Corner order of the six tetrahedra of a cube split along its main diagonal
+# (Kuhn subdivision): tet = (v000, v000 + e_a, v000 + e_a + e_b, v111) for the six
+# axis orders (a, b, c); odd orders are listed with two nodes swapped so every
+# tetrahedron has a positive Jacobian (elem.rs:221-231 node order).
+_KUHN = [((0, 1, 2), False), ((0, 2, 1), True), ((1, 0, 2), True), ((1, 2, 0), False),
+         ((2, 0, 1), False), ((2, 1, 0), True)]
+# midside nodes of C3D10 in CalculiX order: edges 0-1, 1-2, 2-0, 0-3, 1-3, 2-3
+TET10_EDGES = [(0, 1), (1, 2), (2, 0), (0, 3), (1, 3), (2, 3)]
+
+
+def structured_tets(nx, ny, nz, nn=4, h=1.0):
+    """coords, conn (C3D4 or C3D10, 6 tets per cube) and the doubled lattice position of each node."""
+    cells = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    corners = []
+    for order, swap in _KUHN:
+        v = [np.zeros(3, np.int64)]
+        for ax in order:
+            step = v[-1].copy()
+            step[ax] += 1
+            v.append(step)
+        t = [v[0], v[1], v[2], v[3]]
+        if swap:
+            t[1], t[2] = t[2], t[1]
+        corners.append(np.stack(t))
+    corners = np.stack(corners)                            # (6, 4, 3) unit-cube offsets
+    tet = (2 * (cells[:, None, None, :] + corners[None])).reshape(-1, 4, 3)  # doubled lattice
+    pts = [tet[:, a] for a in range(4)]
+    if nn == 10:
+        pts += [(tet[:, a] + tet[:, b]) // 2 for a, b in TET10_EDGES]
+    allp = np.stack(pts, axis=1)                           # (n_tet, nn, 3)
+    mx, my = 2 * nx + 1, 2 * ny + 1
+    key = allp[..., 0] + mx * (allp[..., 1] + my * allp[..., 2])
+    uniq, inv = np.unique(key.ravel(), return_inverse=True)
+    conn = inv.reshape(key.shape).astype(np.int32)
+    lat = np.stack([uniq % mx, (uniq // mx) % my, uniq // (mx * my)], axis=1)
+    coords = lat.astype(np.float64) * (0.5 * h)
+    return coords, conn, lat
+
+
+def block_tet(n=6, nn=4, h=1.0, e=210000.0, nu=0.3, fx_total=1000.0, perturb=0.0, seed=7):
+    """C3D4 / C3D10 n^3 cube block (6 tets per cube): x=0 clamped, a total force fx_total
+    split evenly over the x=L nodes (the reference applies no face pressure to tetrahedra,
+    analysis.rs:1447), interior nodes optionally perturbed."""
+    coords, conn, lat = structured_tets(n, n, n, nn, h)
+    if perturb > 0:
+        coords = perturb_interior(coords, lat, (2 * n, 2 * n, 2 * n), perturb, 0.5 * h, seed)
+    bc = _clamp_dofs(lat[:, 0] == 0)
+    tip = np.nonzero(lat[:, 0] == 2 * n)[0]
+    f = np.zeros(3 * coords.shape[0])
+    f[3 * tip] = fx_total / len(tip)
+    return Model(f"c3d{nn}_block_{n}", coords, conn, nn, np.full(conn.shape[0], e), nu, bc, np.zeros(bc.shape[0]),
+                 f, shape=(n, n, n))

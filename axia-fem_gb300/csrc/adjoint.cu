@@ -115,12 +115,11 @@ element_energy_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const do
       contrib = s_w[g] * dens / det;                                         // w det * density
     }
     // segmented sum over the NG lanes of each element
-    if (NG == 8) {
-      contrib += __shfl_xor_sync(0xffffffffu, contrib, 4);
-      contrib += __shfl_xor_sync(0xffffffffu, contrib, 2);
-      contrib += __shfl_xor_sync(0xffffffffu, contrib, 1);
+    if constexpr ((NG & (NG - 1)) == 0) {
+#pragma unroll
+      for (int o = NG / 2; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
     } else {
-      contrib = warp_sum(contrib);
+      contrib = warp_sum(contrib);  // one element per warp
     }
     if (active_lane && g == 0 && e < n_elem) s_out[e] = contrib;
     __syncwarp();
@@ -169,6 +168,18 @@ int element_energy(axia_ctx* ctx, const double* d_u, const double* d_v, double* 
     const int64_t per_block = 8 * 4;
     const unsigned grid = (unsigned)std::min<int64_t>((ctx->n_elem + per_block - 1) / per_block, ctx->sm_count * 16);
     element_energy_kernel<8, 8><<<std::max(1u, grid), threads, 0, ctx->stream>>>(
+        ctx->n_elem, ctx->d_conn, ctx->d_coords, d_u, d_v, dn, w, c_lam, c_mu, d_s, ctx->d_status);
+  } else if (ctx->nn == 4) {
+    const int threads = 128;
+    const int64_t per_block = 4 * 32;
+    const unsigned grid = (unsigned)std::min<int64_t>((ctx->n_elem + per_block - 1) / per_block, ctx->sm_count * 16);
+    element_energy_kernel<4, 1><<<std::max(1u, grid), threads, 0, ctx->stream>>>(
+        ctx->n_elem, ctx->d_conn, ctx->d_coords, d_u, d_v, dn, w, c_lam, c_mu, d_s, ctx->d_status);
+  } else if (ctx->nn == 10) {
+    const int threads = 128;
+    const int64_t per_block = 4 * 8;
+    const unsigned grid = (unsigned)std::min<int64_t>((ctx->n_elem + per_block - 1) / per_block, ctx->sm_count * 16);
+    element_energy_kernel<10, 4><<<std::max(1u, grid), threads, 0, ctx->stream>>>(
         ctx->n_elem, ctx->d_conn, ctx->d_coords, d_u, d_v, dn, w, c_lam, c_mu, d_s, ctx->d_status);
   } else if (ctx->ngp == 27) {
     const int threads = 128;

@@ -5,6 +5,7 @@
 #include <cstring>
 
 #include "element.cuh"
+#include "solver.cuh"
 
 int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0);
 int numeric_assemble(axia_ctx* ctx, int flags);
@@ -27,6 +28,7 @@ int true_residual(axia_ctx* ctx, double* out);
 int prepare_solve(axia_ctx* ctx, bool mixed);
 int spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req);
 int bsr_autotune(axia_ctx* ctx, const char* cache_path, int* lanes_out, int* vec_out, double* us_out);
+int64_t dofmap_n_full(const axia_dofmap* m);
 int raw_system_from_triplets(axia_ctx* ctx, int64_t n, int64_t nt, const int64_t* h_i, const int64_t* h_j,
                              const double* h_v, bool fp32);
 int raw_system_from_csr(axia_ctx* ctx, int64_t n, const int64_t* h_indptr, const int64_t* h_indices,
@@ -202,8 +204,8 @@ int32_t axia_gpu_element_ke(axia_ctx* ctx, int32_t nn, int32_t reduced, int64_t 
   if (!ctx) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   if (bad_elem) *bad_elem = -1;
-  if ((nn != 8 && nn != 20) || n_elem < 0 || (n_elem > 0 && (!xyz || !e || !ke)))
-    return set_error(ctx, AXIA_ERR_INVALID_ARG, "element_ke: nn must be 8 or 20 and buffers non-null");
+  if ((nn != 4 && nn != 8 && nn != 10 && nn != 20) || n_elem < 0 || (n_elem > 0 && (!xyz || !e || !ke)))
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "element_ke: nn must be 4, 8, 10 or 20 and buffers non-null");
   if (nu >= 0.5 || nu <= -1.0 || !std::isfinite(nu))  // d_iso_3d, elem.rs:42-44
     return set_error(ctx, AXIA_ERR_MATERIAL, "invalid Poisson ratio nu=" + std::to_string(nu));
   if (n_elem == 0) return AXIA_OK;
@@ -260,7 +262,8 @@ int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const
   if (!ctx || !mesh) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   auto t0 = std::chrono::steady_clock::now();
-  if ((mesh->nn != 8 && mesh->nn != 20) || mesh->n_nodes <= 0 || mesh->n_elem < 0 || !mesh->coords ||
+  if ((mesh->nn != 4 && mesh->nn != 8 && mesh->nn != 10 && mesh->nn != 20) || mesh->n_nodes <= 0 ||
+      mesh->n_elem < 0 || !mesh->coords ||
       (mesh->n_elem > 0 && !mesh->conn) || n_bc < 0 || (n_bc > 0 && (!bc_dof || !bc_val)))
     return set_error(ctx, AXIA_ERR_INVALID_ARG, "setup: bad mesh description");
   if (mesh->n_elem >= (1LL << 26)) return set_error(ctx, AXIA_ERR_TOO_LARGE, "setup: more than 2^26 elements");
@@ -272,7 +275,7 @@ int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const
   free_mesh_state(ctx);
   ctx->nn = mesh->nn;
   ctx->reduced = mesh->nn == 20 && mesh->reduced ? 1 : 0;
-  ctx->ngp = (mesh->nn == 8 || ctx->reduced) ? 8 : 27;
+  ctx->ngp = mesh->nn == 4 ? 1 : mesh->nn == 10 ? 4 : (mesh->nn == 8 || ctx->reduced) ? 8 : 27;
   ctx->n_nodes = mesh->n_nodes;
   ctx->n_elem = mesh->n_elem;
   ctx->nu = mesh->nu;
@@ -396,7 +399,7 @@ int32_t axia_gpu_solve(axia_ctx* ctx, const double* f_full, double* u_full, cons
 }
 
 // PCG on the context's raw K_ff (from triplets or CSR): rhs -> x, both host arrays.
-static int32_t solve_raw(axia_ctx* ctx, const double* rhs, double* x, const axia_solve_opts* opts,
+static int32_t solve_raw(axia_ctx* ctx, const double* rhs, const double* d_rhs, double* x, const axia_solve_opts* opts,
                          axia_solve_info* info) {
   axia_solve_info local{};
   if (!info) info = &local;
@@ -411,16 +414,17 @@ static int32_t solve_raw(axia_ctx* ctx, const double* rhs, double* x, const axia
   EventTimer t(ctx->stream);
   int st = ensure_pcg_state(ctx);
   if (st == AXIA_OK) st = prepare_solve(ctx, mixed);
-  if (st == AXIA_OK && cudaMemcpyAsync(ctx->d_b, rhs, ctx->n_free * sizeof(double), cudaMemcpyHostToDevice,
+  if (st == AXIA_OK && cudaMemcpyAsync(ctx->d_b, d_rhs ? d_rhs : rhs, ctx->n_free * sizeof(double),
+                                       d_rhs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                        ctx->stream) != cudaSuccess)
     st = set_error(ctx, AXIA_ERR_CUDA, "solve_kff: rhs upload");
   if (st == AXIA_OK) st = pcg_solve(ctx, &o, info);
   info->ms_solve = t.stop_ms();
   if (st == AXIA_OK) {
     true_residual(ctx, &info->true_residual);
-    if (cudaMemcpyAsync(x, ctx->d_x, ctx->n_free * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+    if (x && (cudaMemcpyAsync(x, ctx->d_x, ctx->n_free * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) !=
+                  cudaSuccess ||
+              cudaStreamSynchronize(ctx->stream) != cudaSuccess))
       st = set_error(ctx, AXIA_ERR_CUDA, "solve_kff: solution download");
   }
   info->n_free = ctx->n_free;
@@ -447,7 +451,44 @@ int32_t axia_gpu_solve_triplets(axia_ctx* ctx, int64_t n, int64_t n_trips, const
   free_mesh_state(ctx);
   const bool mixed = opts && opts->precision == AXIA_PREC_MIXED;
   AXIA_TRY(raw_system_from_triplets(ctx, n, n_trips, ti, tj, tv, mixed));
-  return solve_raw(ctx, rhs, x, opts, info);
+  return solve_raw(ctx, rhs, nullptr, x, opts, info);
+}
+
+int32_t axia_gpu_solve_reduced(axia_ctx* ctx, const axia_dofmap* map, int64_t n_trips, const int64_t* ti,
+                               const int64_t* tj, const double* tv, const double* f_full, double* u_full,
+                               const axia_solve_opts* opts, axia_solve_info* info) {
+  if (!ctx || !map || !f_full || !u_full || n_trips < 0 || (n_trips > 0 && (!ti || !tj || !tv)))
+    return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  const int64_t nf = axia_dofmap_export(map, nullptr, nullptr, nullptr, nullptr, nullptr) >= 0 ? dofmap_n_full(map) : 0;
+  AXIA_TRY(check_raw_rhs(ctx, nf, f_full));
+  free_mesh_state(ctx);
+  AXIA_TRY(reset_dev_status(ctx));
+  const bool mixed = opts && opts->precision == AXIA_PREC_MIXED;
+  ReducedSystem S;
+  int st = reduce_system(ctx, map, n_trips, ti, tj, tv, f_full, mixed, &S);
+  if (st == AXIA_OK && S.n_ind == 0) {  // everything prescribed or slaved: u = u0
+    if (cudaMemcpyAsync(u_full, S.u0, nf * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      st = set_error(ctx, AXIA_ERR_CUDA, "copy of u0");
+    if (info) {
+      std::memset(info, 0, sizeof(*info));
+      info->bad_index = -1;
+    }
+    S.release();
+    return st;
+  }
+  if (st == AXIA_OK) st = solve_raw(ctx, nullptr, S.rhs, nullptr, opts, info);
+  double* du = nullptr;
+  if (st == AXIA_OK) st = dev_alloc(ctx, &du, (size_t)nf);
+  if (st == AXIA_OK) st = reconstruct_system(ctx, S, ctx->d_x, du);
+  if (st == AXIA_OK && (cudaMemcpyAsync(u_full, du, nf * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) !=
+                            cudaSuccess ||
+                        cudaStreamSynchronize(ctx->stream) != cudaSuccess))
+    st = set_error(ctx, AXIA_ERR_CUDA, "copy of u");
+  dev_free(du);
+  S.release();
+  return st;
 }
 
 int32_t axia_gpu_solve_csr(axia_ctx* ctx, int64_t n, const int64_t* indptr, const int64_t* indices,
@@ -460,7 +501,7 @@ int32_t axia_gpu_solve_csr(axia_ctx* ctx, int64_t n, const int64_t* indptr, cons
   free_mesh_state(ctx);
   const bool mixed = opts && opts->precision == AXIA_PREC_MIXED;
   AXIA_TRY(raw_system_from_csr(ctx, n, indptr, indices, data, mixed));
-  return solve_raw(ctx, rhs, x, opts, info);
+  return solve_raw(ctx, rhs, nullptr, x, opts, info);
 }
 
 int32_t axia_gpu_autotune(axia_ctx* ctx, const char* cache_path, int32_t* lanes, int32_t* vec,
@@ -517,7 +558,9 @@ int32_t axia_gpu_element_energy(axia_ctx* ctx, const double* u_full, const doubl
     cudaMemcpyAsync(dv, v_full, ctx->ndof * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
     st = element_energy(ctx, du, dv, ctx->d_energy);
   }
-  if (st == AXIA_OK && cudaMemcpy(s, ctx->d_energy, ctx->n_elem * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+  if (st == AXIA_OK && (cudaMemcpyAsync(s, ctx->d_energy, ctx->n_elem * sizeof(double), cudaMemcpyDeviceToHost,
+                                       ctx->stream) != cudaSuccess ||
+                        cudaStreamSynchronize(ctx->stream) != cudaSuccess))
     st = set_error(ctx, AXIA_ERR_CUDA, "copy of element energies");
   dev_free(du);
   dev_free(dv);
@@ -631,6 +674,7 @@ int32_t axia_gpu_export_system(const axia_ctx* ctx_c, int32_t* rowptr, int32_t* 
   if (!ctx) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   if (!ctx->d_rowptr) return set_error(ctx, AXIA_ERR_STATE, "export before setup");
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the copies below run on the legacy stream
   const int64_t n = ctx->n_free, nnz = ctx->nnz;
   if (rowptr) AXIA_CUDA(ctx, cudaMemcpy(rowptr, ctx->d_rowptr, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost));
   if (col) AXIA_CUDA(ctx, cudaMemcpy(col, ctx->d_col, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));

@@ -71,6 +71,35 @@ void dshape_hex20(double xi, double eta, double zeta, double* dn) {
   }
 }
 
+// quadratic.rs:546-580 (tet10 in volume coordinates l1 = 1 - r - s - t, l2..l4 = r, s, t)
+void dshape_tet10(double r, double s, double t, double* dn) {
+  const double l1 = 1.0 - r - s - t, l2 = r, l3 = s, l4 = t;
+  const double d1 = 4.0 * l1 - 1.0, d2 = 4.0 * l2 - 1.0, d3 = 4.0 * l3 - 1.0, d4 = 4.0 * l4 - 1.0;
+  const double v[30] = {-d1, -d1, -d1, d2, 0.0, 0.0, 0.0, d3, 0.0, 0.0, 0.0, d4,
+                        4.0 * (l1 - l2), -4.0 * l2, -4.0 * l2,
+                        4.0 * l3, 4.0 * l2, 0.0,
+                        -4.0 * l3, 4.0 * (l1 - l3), -4.0 * l3,
+                        -4.0 * l4, -4.0 * l4, 4.0 * (l1 - l4),
+                        4.0 * l4, 0.0, 4.0 * l2,
+                        0.0, 4.0 * l4, 4.0 * l3};
+  for (int k = 0; k < 30; ++k) dn[k] = v[k];
+}
+
+// elem.rs:221-248: linear tetrahedron, constant dN/dxi
+void dshape_tet4(double* dn) {
+  const double v[12] = {-1.0, -1.0, -1.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+  for (int k = 0; k < 12; ++k) dn[k] = v[k];
+}
+
+const double kTetA = 0.5854101966249685, kTetB = 0.1381966011250105;  // quadratic.rs:611-612
+
+}  // namespace
+
+// dN/dxi of the quadratic tetrahedron at (r, s, t), [10][3] (used by the recovery tables)
+void tet10_dshape(double r, double s, double t, double* dn) { dshape_tet10(r, s, t, dn); }
+
+namespace {
+
 struct HostTables {
   std::vector<double> dn, w;
   std::vector<int> e0, e1, blk;
@@ -79,7 +108,12 @@ struct HostTables {
 HostTables make_tables(int nn, int ng) {
   HostTables t;
   std::vector<double> pts;  // xi, eta, zeta, w
-  if (ng == 8) {
+  if (nn == 4) {
+    pts = {0.25, 0.25, 0.25, 1.0 / 6.0};  // constant strain: one point, weight = reference volume
+  } else if (nn == 10) {
+    const double w = 1.0 / 24.0;  // quadratic.rs:613-614
+    pts = {kTetB, kTetB, kTetB, w, kTetA, kTetB, kTetB, w, kTetB, kTetA, kTetB, w, kTetB, kTetB, kTetA, w};
+  } else if (ng == 8) {
     const double g[2] = {-kG2, kG2};
     for (double a : g)
       for (double b : g)
@@ -94,8 +128,12 @@ HostTables make_tables(int nn, int ng) {
   for (int g = 0; g < ng; ++g) {
     if (nn == 8)
       dshape_hex8(pts[4 * g], pts[4 * g + 1], pts[4 * g + 2], &t.dn[(size_t)g * nn * 3]);
-    else
+    else if (nn == 20)
       dshape_hex20(pts[4 * g], pts[4 * g + 1], pts[4 * g + 2], &t.dn[(size_t)g * nn * 3]);
+    else if (nn == 10)
+      dshape_tet10(pts[4 * g], pts[4 * g + 1], pts[4 * g + 2], &t.dn[(size_t)g * nn * 3]);
+    else
+      dshape_tet4(&t.dn[(size_t)g * nn * 3]);
     t.w[g] = pts[4 * g + 3];
   }
   // entries of blocks a <= b; diagonal blocks keep i <= j
@@ -129,10 +167,14 @@ struct DevTables {
   int* blk = nullptr;
 };
 
-DevTables g_tab[3];  // hex8, hex20 (27 gp), hex20r (8 gp) -- per process, device 0..n share by device id
-int g_tab_device[3] = {-1, -1, -1};
+DevTables g_tab[5];  // hex8, hex20 (27 gp), hex20r (8 gp), tet4, tet10 -- per process, by device id
+int g_tab_device[5] = {-1, -1, -1, -1, -1};
 
-int table_index(int nn, int ng) { return nn == 8 ? 0 : (ng == 27 ? 1 : 2); }
+int table_index(int nn, int ng) {
+  if (nn == 4) return 3;
+  if (nn == 10) return 4;
+  return nn == 8 ? 0 : (ng == 27 ? 1 : 2);
+}
 
 int ensure_tables(axia_ctx* ctx, int nn, int ng, ElemTables* out) {
   int ti = table_index(nn, ng);
@@ -196,7 +238,9 @@ int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args) {
   if (nn == 8) return launch_element_ke<8, 8, 8>(ctx, args);
   if (nn == 20 && !reduced) return launch_element_ke<20, 27, 4>(ctx, args);
   if (nn == 20 && reduced) return launch_element_ke<20, 8, 4>(ctx, args);
-  return set_error(ctx, AXIA_ERR_INVALID_ARG, "nn must be 8 or 20");
+  if (nn == 4) return launch_element_ke<4, 1, 8>(ctx, args);
+  if (nn == 10) return launch_element_ke<10, 4, 8>(ctx, args);
+  return set_error(ctx, AXIA_ERR_INVALID_ARG, "nn must be 4, 8, 10 or 20");
 }
 
 // ---------------------------------------------------------------------------

@@ -1,9 +1,11 @@
-// element.cuh -- C3D8 / C3D20(R) element stiffness on the device, one warp
-// per element.
+// element.cuh -- C3D8 / C3D20(R) / C3D4 / C3D10 element stiffness on the
+// device, one warp per element.
 //
 // Restates, with an isotropic closed form for the contraction, the
-// reference's hex8_stiffness (solver/src/elem.rs:194-219) and hex20_stiffness
-// (solver/src/quadratic.rs:122-146): Ke = sum_gp w det(J) B^T D B.
+// reference's hex8_stiffness (solver/src/elem.rs:194-219), hex20_stiffness
+// (solver/src/quadratic.rs:122-146), tet4_stiffness (elem.rs:221-248, one
+// point, weight 1/6) and tet10_stiffness (quadratic.rs:607-627, 4 points,
+// weights 1/24): Ke = sum_gp w det(J) B^T D B.
 //
 // For isotropic D (d_iso_3d, elem.rs:41-59) the 3x3 block of nodes (a, b) is
 //   K_ab[i][j] = lam A_ab[i][j] + mu A_ab[j][i] + mu delta_ij tr(A_ab),

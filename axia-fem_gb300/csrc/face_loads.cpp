@@ -53,8 +53,12 @@ extern "C" int32_t axia_face_loads(int32_t nn, int64_t n_nodes, const double* co
                                    int64_t n_loads, const int64_t* elem, const int32_t* face, const double* p,
                                    double* f_full, int64_t* bad_load) {
   if (bad_load) *bad_load = -1;
-  if ((nn != 8 && nn != 20) || n_loads < 0 || (n_loads > 0 && (!coords || !conn || !elem || !face || !p || !f_full)))
+  if ((nn != 4 && nn != 8 && nn != 10 && nn != 20) || n_loads < 0 ||
+      (n_loads > 0 && (!coords || !conn || !elem || !face || !p || !f_full)))
     return AXIA_ERR_INVALID_ARG;
+  // apply_pressure has no tetrahedron arm (analysis.rs:1447): a face pressure on
+  // C3D4 / C3D10 adds nothing, as in the reference
+  if (nn == 4 || nn == 10) return AXIA_OK;
   const int nf = nn == 8 ? 4 : 8;
   const double g2 = 0.5773502691896257;
   const double g3[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};

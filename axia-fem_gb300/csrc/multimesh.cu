@@ -171,7 +171,8 @@ int solve_multi_device(axia_ctx* ctx, const double* d_f, double* d_u, const axia
   info->ms_pcg_kernel = ms;
   info->pcg_launches = 1;
   std::vector<PcgOut> outs(nm);
-  AXIA_CUDA(ctx, cudaMemcpy(outs.data(), ctx->d_mouts, sizeof(PcgOut) * nm, cudaMemcpyDeviceToHost));
+  AXIA_CUDA(ctx, cudaMemcpyAsync(outs.data(), ctx->d_mouts, sizeof(PcgOut) * nm, cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   DevStatus hs;
   AXIA_TRY(read_dev_status(ctx, &hs));
   if (hs.timeout) return set_error(ctx, AXIA_ERR_TIMEOUT, "a group barrier of the multi-mesh solve ran past its limit");

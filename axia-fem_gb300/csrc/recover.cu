@@ -1,7 +1,7 @@
 // recover.cu -- nodal stress recovery and reactions after a solve.
 //
-// Replaces, for C3D8 / C3D20 / C3D20R with an isotropic material, the
-// post-solve loops of the reference's solve_linear:
+// Replaces, for C3D8 / C3D20 / C3D20R / C3D4 / C3D10 with an isotropic
+// material, the post-solve loops of the reference's solve_linear:
 //   reactions      solver/src/analysis.rs:1027-1035   ku = sum of element K u, rf = ku - f
 //   nodal stresses solver/src/analysis.rs:1061-1153   element nodal stresses summed per
 //                                                     node in element order / element count
@@ -10,6 +10,8 @@
 //                  with the trilinear shapes at HEX_XI*sqrt(3)); hex20_nodal_stress and
 //                  hex20_extrapolate quadratic.rs:148-225 (hex_gauss points, tensor-product
 //                  Lagrange extrapolation, lagrange1d quadratic.rs:227-244)
+//                  tet4_nodal_stress elem.rs:781-795 (one constant stress), tet10_nodal_stress
+//                  quadratic.rs:678-702 (stress evaluated at the ten nodes)
 //   element mean   "stress_gp" analysis.rs:1141-1152 (mean of the element's nodal stresses)
 //
 // Two kernels.  element_recover_kernel: lanes are (element, Gauss point)
@@ -30,6 +32,7 @@
 #include "solver.cuh"
 
 int element_tables_for(axia_ctx* ctx, int nn, int ng, const double** dn, const double** w);
+void tet10_dshape(double r, double s, double t, double* dn);
 
 namespace {
 
@@ -127,7 +130,7 @@ element_recover_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const d
         if (!(fabs(det) >= 1e-18)) {
           record_error(st, e, isfinite(det) ? AXIA_ERR_SINGULAR_JACOBIAN : AXIA_ERR_NONFINITE);
           det = 1.0;
-        } else if (det <= 0.0) {
+        } else if (det <= 0.0 && s_w[g] > 0.0) {  // integration points only
           record_error(st, e, AXIA_ERR_NEG_JACOBIAN);
         }
         const double E = e_elem[e];
@@ -302,15 +305,44 @@ struct XTab {
   int* perm = nullptr;
   int device = -1;
 };
-XTab g_xtab[3];  // hex8, hex20, hex20r
+XTab g_xtab[5];  // hex8, hex20, hex20r, tet4, tet10
+
+// The points the recovery kernel evaluates and how nodes take their stress:
+//  * hexahedra: the stiffness Gauss points, extrapolated to the nodes (X above);
+//  * C3D4: its one point (constant stress, elem.rs:781-795), every node takes it;
+//  * C3D10: the 4 Gauss points (weights 1/24, for the internal forces) and the
+//    10 nodes themselves (weight 0; tet10_nodal_stress evaluates the stress at
+//    the nodes, quadratic.rs:678-702), node a taking point 4 + a.
+struct RecTables {
+  const double* dn;
+  const double* w;
+  const double* x;
+  const int* perm;
+};
+struct TetRecTab {
+  double* dn = nullptr;
+  double* w = nullptr;
+  int device = -1;
+};
+TetRecTab g_tet10_rec;
 
 int ensure_xtab(axia_ctx* ctx, const double** x, const int** perm) {
-  const int ti = ctx->nn == 8 ? 0 : (ctx->ngp == 27 ? 1 : 2);
+  const int ti = ctx->nn == 4 ? 3 : ctx->nn == 10 ? 4 : ctx->nn == 8 ? 0 : (ctx->ngp == 27 ? 1 : 2);
   XTab& t = g_xtab[ti];
   if (t.device != ctx->device) {
     std::vector<double> hx;
     std::vector<int> hp;
-    extrapolation_table(ctx->nn, ctx->ngp, hx, hp);
+    if (ctx->nn == 4) {
+      hx.assign(4, 1.0);
+      hp.assign(1, 0);
+    } else if (ctx->nn == 10) {
+      hx.assign(10 * 14, 0.0);
+      for (int a = 0; a < 10; ++a) hx[a * 14 + 4 + a] = 1.0;
+      hp.resize(14);
+      for (int m = 0; m < 14; ++m) hp[m] = m;
+    } else {
+      extrapolation_table(ctx->nn, ctx->ngp, hx, hp);
+    }
     AXIA_CUDA(ctx, cudaMalloc(&t.x, hx.size() * sizeof(double)));
     AXIA_CUDA(ctx, cudaMalloc(&t.perm, hp.size() * sizeof(int)));
     AXIA_CUDA(ctx, cudaMemcpy(t.x, hx.data(), hx.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -319,6 +351,29 @@ int ensure_xtab(axia_ctx* ctx, const double** x, const int** perm) {
   }
   *x = t.x;
   *perm = t.perm;
+  return AXIA_OK;
+}
+
+int recover_tables(axia_ctx* ctx, RecTables* r) {
+  AXIA_TRY(ensure_xtab(ctx, &r->x, &r->perm));
+  if (ctx->nn != 10) return element_tables_for(ctx, ctx->nn, ctx->ngp, &r->dn, &r->w);
+  TetRecTab& t = g_tet10_rec;
+  if (t.device != ctx->device) {
+    const double a = 0.5854101966249685, b = 0.1381966011250105;  // quadratic.rs:611-612
+    const double pts[14][3] = {{b, b, b}, {a, b, b}, {b, a, b}, {b, b, a},
+                               {0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0.5, 0, 0},
+                               {0.5, 0.5, 0}, {0, 0.5, 0}, {0, 0, 0.5}, {0.5, 0, 0.5}, {0, 0.5, 0.5}};
+    std::vector<double> dn(14 * 30), w(14, 0.0);
+    for (int m = 0; m < 14; ++m) tet10_dshape(pts[m][0], pts[m][1], pts[m][2], &dn[m * 30]);
+    for (int m = 0; m < 4; ++m) w[m] = 1.0 / 24.0;
+    AXIA_CUDA(ctx, cudaMalloc(&t.dn, dn.size() * sizeof(double)));
+    AXIA_CUDA(ctx, cudaMalloc(&t.w, w.size() * sizeof(double)));
+    AXIA_CUDA(ctx, cudaMemcpy(t.dn, dn.data(), dn.size() * sizeof(double), cudaMemcpyHostToDevice));
+    AXIA_CUDA(ctx, cudaMemcpy(t.w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
+    t.device = ctx->device;
+  }
+  r->dn = t.dn;
+  r->w = t.w;
   return AXIA_OK;
 }
 
@@ -343,17 +398,19 @@ int recover_device(axia_ctx* ctx, const double* d_u, const double* d_f, double e
   if (d_strain && !(e_strain > 0.0)) return set_error(ctx, AXIA_ERR_MATERIAL, "strain conversion needs E > 0");
   if (ctx->n_elem == 0) return AXIA_OK;
   if (!ctx->d_rec) AXIA_TRY(dev_alloc(ctx, &ctx->d_rec, (size_t)ctx->n_elem * ctx->nn * kRec));
-  const double *dn = nullptr, *w = nullptr, *xt = nullptr;
-  const int* perm = nullptr;
-  AXIA_TRY(element_tables_for(ctx, ctx->nn, ctx->ngp, &dn, &w));
-  AXIA_TRY(ensure_xtab(ctx, &xt, &perm));
+  RecTables t{};
+  AXIA_TRY(recover_tables(ctx, &t));
   AXIA_TRY(reset_dev_status(ctx));
   if (ctx->nn == 8)
-    launch_element_recover<8, 8>(ctx, d_u, dn, w, xt, perm, d_emean);
+    launch_element_recover<8, 8>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
+  else if (ctx->nn == 4)
+    launch_element_recover<4, 1>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
+  else if (ctx->nn == 10)
+    launch_element_recover<10, 14>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
   else if (ctx->ngp == 27)
-    launch_element_recover<20, 27>(ctx, d_u, dn, w, xt, perm, d_emean);
+    launch_element_recover<20, 27>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
   else
-    launch_element_recover<20, 8>(ctx, d_u, dn, w, xt, perm, d_emean);
+    launch_element_recover<20, 8>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());
   const unsigned grid = (unsigned)std::max<int64_t>(

@@ -131,6 +131,44 @@ int launch_full_rhs(axia_ctx* ctx, const double* d_f);
 int launch_full_reconstruct(axia_ctx* ctx, double* d_u);
 int prepare_full_buffers(axia_ctx* ctx);
 
+// Sorted (key, value) pairs and their runs of equal keys (triplets.cu).
+struct Runs {
+  uint64_t* key = nullptr;  // sorted keys
+  double* val = nullptr;    // values in sorted order
+  int64_t* head = nullptr;  // first position of each run
+  int64_t nv = 0, n_runs = 0;
+  void release() {
+    dev_free(key);
+    dev_free(val);
+    dev_free(head);
+    n_runs = nv = 0;
+  }
+};
+int sort_runs(axia_ctx* ctx, const uint64_t* dk, const double* dv, int64_t nt, int64_t nv, int end_bit, Runs* out);
+int key_bits(uint64_t max_key);
+int csr_from_runs(axia_ctx* ctx, int64_t n, const Runs& R, bool fp32);
+int vector_from_runs(axia_ctx* ctx, int64_t n, const Runs& R, double* d_out);
+
+// Device copy of a DOF map (T, u0) and the reduced right-hand side (reduce.cu).
+struct ReducedSystem {
+  int64_t n_full = 0, n_ind = 0;
+  int64_t* t_ptr = nullptr;
+  int64_t* t_col = nullptr;
+  double* t_val = nullptr;
+  double* u0 = nullptr;
+  double* rhs = nullptr;
+  void release() {
+    dev_free(t_ptr);
+    dev_free(t_col);
+    dev_free(t_val);
+    dev_free(u0);
+    dev_free(rhs);
+  }
+};
+int reduce_system(axia_ctx* ctx, const axia_dofmap* map, int64_t nt, const int64_t* h_i, const int64_t* h_j,
+                  const double* h_v, const double* h_f, bool fp32, ReducedSystem* S);
+int reconstruct_system(axia_ctx* ctx, const ReducedSystem& S, const double* d_x, double* d_u);
+
 // ---------------------------------------------------------------------------
 // Host helpers for the persistent launches
 // ---------------------------------------------------------------------------

@@ -75,6 +75,18 @@ __global__ void k_run_sum(int64_t nnz, int64_t nv, int64_t n, const uint64_t* __
   }
 }
 
+// One thread per run: out[key] = run values summed from 0.0 in order.
+__global__ void k_run_sum_vector(int64_t n_runs, int64_t nv, const uint64_t* __restrict__ key,
+                                 const double* __restrict__ val, const int64_t* __restrict__ head,
+                                 double* __restrict__ out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_runs; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = head[r], e = r + 1 < n_runs ? head[r + 1] : nv;
+    double v = 0.0;
+    for (int64_t q = s; q < e; ++q) v += val[q];
+    out[key[s]] = v;
+  }
+}
+
 __global__ void k_csr_to_i32(int64_t n, int64_t nnz, const int64_t* __restrict__ indptr,
                              const int64_t* __restrict__ indices, int32_t* __restrict__ rowptr,
                              int32_t* __restrict__ col, DevStatus* st) {
@@ -157,98 +169,126 @@ int check_status(axia_ctx* ctx, const char* what) {
 
 }  // namespace
 
+// Stable radix sort of (key, value) over end_bit key bits and the runs of
+// equal keys among the first nv sorted entries (the entries to drop carry a
+// sentinel key above every valid one, so they sort last).  dk / dv are the
+// unsorted inputs (nt entries) and are left untouched.
+int sort_runs(axia_ctx* ctx, const uint64_t* dk, const double* dv, int64_t nt, int64_t nv, int end_bit, Runs* out) {
+  *out = Runs{};
+  out->nv = nv;
+  if (nt <= 0 || nv <= 0) return AXIA_OK;
+  const size_t m = (size_t)nt;
+  AXIA_TRY(dev_alloc(ctx, &out->key, m));
+  AXIA_TRY(dev_alloc(ctx, &out->val, m));
+  size_t temp_bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, dk, out->key, dv, out->val, nt, 0, end_bit, ctx->stream);
+  void* temp = nullptr;
+  if (cudaMalloc(&temp, std::max<size_t>(temp_bytes, 1)) != cudaSuccess)
+    return set_error(ctx, AXIA_ERR_OOM, "sort workspace");
+  const cudaError_t e = cub::DeviceRadixSort::SortPairs(temp, temp_bytes, dk, out->key, dv, out->val, nt, 0, end_bit,
+                                                        ctx->stream);
+  cudaStreamSynchronize(ctx->stream);  // the sort has finished with its workspace
+  cudaFree(temp);
+  if (e != cudaSuccess) return set_error(ctx, AXIA_ERR_CUDA, "radix sort");
+  ctx->launches++;
+  int64_t *flag = nullptr, *pos = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &flag, (size_t)nv));
+  int st = dev_alloc(ctx, &pos, (size_t)nv);
+  if (st == AXIA_OK) {
+    k_run_flags<<<grid_for(ctx, nv), 256, 0, ctx->stream>>>(nv, out->key, flag);
+    ctx->launches++;
+    st = device_exclusive_scan(ctx, flag, pos, nv, &out->n_runs);
+  }
+  if (st == AXIA_OK && out->n_runs > 0) st = dev_alloc(ctx, &out->head, (size_t)out->n_runs);
+  if (st == AXIA_OK && out->n_runs > 0) {
+    k_run_heads<<<grid_for(ctx, nv), 256, 0, ctx->stream>>>(nv, out->key, pos, out->head);
+    ctx->launches++;
+  }
+  dev_free(flag);
+  dev_free(pos);
+  if (st == AXIA_OK && cudaGetLastError() != cudaSuccess) st = set_error(ctx, AXIA_ERR_CUDA, "run kernels");
+  return st;
+}
+
+int key_bits(uint64_t max_key) {
+  int b = 1;
+  while (b < 64 && (max_key >> b) != 0) ++b;
+  return b;
+}
+
+// The context's raw CSR from sorted runs of keys i*n + j.
+int csr_from_runs(axia_ctx* ctx, int64_t n, const Runs& R, bool fp32) {
+  const int64_t nnz = R.n_runs;
+  if (nnz >= (int64_t)INT32_MAX) return set_error(ctx, AXIA_ERR_TOO_LARGE, "K_ff: nnz exceeds int32");
+  AXIA_TRY(alloc_raw(ctx, n, nnz, fp32));
+  if (nnz > 0) {
+    k_run_sum<<<grid_for(ctx, nnz), 256, 0, ctx->stream>>>(nnz, R.nv, n, R.key, R.val, R.head, ctx->d_rowptr,
+                                                           ctx->d_col, ctx->d_val, fp32 ? ctx->d_val32 : nullptr);
+    ctx->launches++;
+  } else {
+    cudaMemsetAsync(ctx->d_rowptr, 0, (n + 1) * sizeof(int32_t), ctx->stream);
+  }
+  if (cudaGetLastError() != cudaSuccess) return set_error(ctx, AXIA_ERR_CUDA, "CSR kernels");
+  return finish_raw(ctx, n, nnz, fp32);
+}
+
+// out[key] = the run's values summed from 0.0 in order; keys without a run get 0.
+int vector_from_runs(axia_ctx* ctx, int64_t n, const Runs& R, double* d_out) {
+  AXIA_CUDA(ctx, cudaMemsetAsync(d_out, 0, std::max<int64_t>(n, 1) * sizeof(double), ctx->stream));
+  if (R.n_runs > 0) {
+    k_run_sum_vector<<<grid_for(ctx, R.n_runs), 256, 0, ctx->stream>>>(R.n_runs, R.nv, R.key, R.val, R.head, d_out);
+    ctx->launches++;
+  }
+  AXIA_CUDA(ctx, cudaGetLastError());
+  return AXIA_OK;
+}
+
 // K_ff from triplets (host arrays) into the context's CSR (int32 indices).
 int raw_system_from_triplets(axia_ctx* ctx, int64_t n, int64_t nt, const int64_t* h_i, const int64_t* h_j,
                              const double* h_v, bool fp32) {
   if (n <= 0 || n >= (int64_t)INT32_MAX || nt < 0) return set_error(ctx, AXIA_ERR_INVALID_ARG, "solve_kff: bad n or triplet count");
   AXIA_TRY(reset_dev_status(ctx));
   int64_t *di = nullptr, *dj = nullptr;
-  double *dv = nullptr, *dv_sorted = nullptr;
-  uint64_t *dk = nullptr, *dk_sorted = nullptr;
+  double* dv = nullptr;
+  uint64_t* dk = nullptr;
   unsigned long long* dcount = nullptr;
-  int64_t *flag = nullptr, *pos = nullptr, *head = nullptr;
-  void* temp = nullptr;
+  Runs R;
   int st = AXIA_OK;
-  auto fail = [&](int code) {
+  auto done = [&](int code) {
     dev_free(di);
     dev_free(dj);
     dev_free(dv);
-    dev_free(dv_sorted);
     dev_free(dk);
-    dev_free(dk_sorted);
     dev_free(dcount);
-    dev_free(flag);
-    dev_free(pos);
-    dev_free(head);
-    if (temp) cudaFree(temp);
+    R.release();
     return code;
   };
   const size_t m = (size_t)std::max<int64_t>(nt, 1);
   if ((st = dev_alloc(ctx, &di, m)) || (st = dev_alloc(ctx, &dj, m)) || (st = dev_alloc(ctx, &dv, m)) ||
       (st = dev_alloc(ctx, &dk, m)) || (st = dev_alloc(ctx, &dcount, 1)))
-    return fail(st);
+    return done(st);
   if (nt > 0) {
     if (cudaMemcpyAsync(di, h_i, nt * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
         cudaMemcpyAsync(dj, h_j, nt * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
         cudaMemcpyAsync(dv, h_v, nt * sizeof(double), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
-      return fail(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: triplet upload"));
+      return done(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: triplet upload"));
   }
   cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), ctx->stream);
   if (nt > 0) {
     k_trip_keys<<<grid_for(ctx, nt), 256, 0, ctx->stream>>>(nt, n, di, dj, dv, dk, dcount, ctx->d_status);
     ctx->launches++;
   }
-  if (cudaGetLastError() != cudaSuccess) return fail(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: key kernel"));
-  if ((st = check_status(ctx, "solve_kff triplets"))) return fail(st);
-  dev_free(di);
-  dev_free(dj);
-  unsigned long long nv_h = 0;
-  if (cudaMemcpy(&nv_h, dcount, sizeof(nv_h), cudaMemcpyDeviceToHost) != cudaSuccess)
-    return fail(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: count"));
-  const int64_t nv = (int64_t)nv_h;
-  // stable radix sort of (key, value) over the bits that n*n needs
-  const uint64_t sentinel = (uint64_t)n * (uint64_t)n;
-  int end_bit = 1;
-  while (end_bit < 64 && (sentinel >> end_bit) != 0) ++end_bit;
-  if (nt > 0) {
-    if ((st = dev_alloc(ctx, &dk_sorted, m)) || (st = dev_alloc(ctx, &dv_sorted, m))) return fail(st);
-    size_t temp_bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, dk, dk_sorted, dv, dv_sorted, nt, 0, end_bit, ctx->stream);
-    if (cudaMalloc(&temp, std::max<size_t>(temp_bytes, 1)) != cudaSuccess)
-      return fail(set_error(ctx, AXIA_ERR_OOM, "solve_kff: sort workspace"));
-    if (cub::DeviceRadixSort::SortPairs(temp, temp_bytes, dk, dk_sorted, dv, dv_sorted, nt, 0, end_bit,
-                                        ctx->stream) != cudaSuccess)
-      return fail(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: radix sort"));
-    ctx->launches++;
-    cudaFree(temp);
-    temp = nullptr;
-    dev_free(dk);
-    dev_free(dv);
-  }
-  // run heads -> unique (i, j) entries
-  int64_t nnz = 0;
-  if (nv > 0) {
-    if ((st = dev_alloc(ctx, &flag, (size_t)nv)) || (st = dev_alloc(ctx, &pos, (size_t)nv))) return fail(st);
-    k_run_flags<<<grid_for(ctx, nv), 256, 0, ctx->stream>>>(nv, dk_sorted, flag);
-    ctx->launches++;
-    if ((st = device_exclusive_scan(ctx, flag, pos, nv, &nnz))) return fail(st);
-  }
-  if (nnz >= (int64_t)INT32_MAX) return fail(set_error(ctx, AXIA_ERR_TOO_LARGE, "solve_kff: nnz exceeds int32"));
-  if ((st = alloc_raw(ctx, n, nnz, fp32))) return fail(st);
-  if (nnz > 0) {
-    if ((st = dev_alloc(ctx, &head, (size_t)nnz))) return fail(st);
-    k_run_heads<<<grid_for(ctx, nv), 256, 0, ctx->stream>>>(nv, dk_sorted, pos, head);
-    k_run_sum<<<grid_for(ctx, nnz), 256, 0, ctx->stream>>>(nnz, nv, n, dk_sorted, dv_sorted, head, ctx->d_rowptr,
-                                                           ctx->d_col, ctx->d_val, fp32 ? ctx->d_val32 : nullptr);
-    ctx->launches += 2;
-  } else {
-    cudaMemsetAsync(ctx->d_rowptr, 0, (n + 1) * sizeof(int32_t), ctx->stream);
-  }
-  if (cudaGetLastError() != cudaSuccess) return fail(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: CSR kernels"));
-  if ((st = finish_raw(ctx, n, nnz, fp32))) return fail(st);
+  if (cudaGetLastError() != cudaSuccess) return done(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: key kernel"));
+  if ((st = check_status(ctx, "solve_kff triplets"))) return done(st);
+  unsigned long long nv = 0;  // ordered after the key kernel on the context's (non-blocking) stream
+  if (cudaMemcpyAsync(&nv, dcount, sizeof(nv), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+    return done(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: count"));
+  if ((st = sort_runs(ctx, dk, dv, nt, (int64_t)nv, key_bits((uint64_t)n * (uint64_t)n), &R))) return done(st);
+  if ((st = csr_from_runs(ctx, n, R, fp32))) return done(st);
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess)
-    return fail(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: CSR build"));
-  return fail(AXIA_OK);
+    return done(set_error(ctx, AXIA_ERR_CUDA, "solve_kff: CSR build"));
+  return done(AXIA_OK);
 }
 
 // K_ff from a CSR the caller built (int64 indptr / indices, as the reference's Csr).

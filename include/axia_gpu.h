@@ -87,8 +87,8 @@ typedef struct axia_mesh {
   int64_t n_nodes;
   const double* coords;    /* [n_nodes][3] */
   int64_t n_elem;
-  int32_t nn;              /* nodes per element: 8 (C3D8) or 20 (C3D20) */
-  int32_t reduced;         /* 1: C3D20R, 2x2x2 Gauss points (quadratic.rs:100-120) */
+  int32_t nn;              /* nodes per element: 8 (C3D8), 20 (C3D20), 4 (C3D4) or 10 (C3D10) */
+  int32_t reduced;         /* 1: C3D20R, 2x2x2 Gauss points (quadratic.rs:100-120); ignored otherwise */
   const int32_t* conn;     /* [n_elem][nn], 0-based node indices, CalculiX node order */
   const double* e_elem;    /* [n_elem] Young's modulus per element, or NULL */
   double e;                /* Young's modulus when e_elem == NULL */
@@ -340,6 +340,42 @@ AXIA_API int32_t axia_gpu_solve_csr(axia_ctx* ctx, int64_t n, const int64_t* ind
  * GPU kernels to tune). */
 AXIA_API int32_t axia_gpu_autotune(axia_ctx* ctx, const char* cache_path, int32_t* lanes, int32_t* vec,
                                    double* us_per_iter);
+
+/* ---- DOF map with multi-point constraints (constraint.rs:8-136) ---------- */
+typedef struct axia_dofmap axia_dofmap;
+
+/* DofMap::build: prescribed DOFs (later entries win, analysis.rs:556-565)
+ * and MPCs u_slave = sum_k alpha_k u_master_k + u0 (the reference's Mpc,
+ * constraint.rs:8-14; MPC i has masters mpc_master[mpc_ptr[i] ..
+ * mpc_ptr[i+1]) with mpc_alpha), into u = u0 + T x with nested slaves
+ * expanded and prescribed masters folded into u0, exactly as the reference
+ * (last MPC per slave wins, 32 expansion passes, coalesce).  A cyclic MPC or
+ * a master outside [0, ndof) is AXIA_ERR_INVALID_ARG; no free DOF, no slave
+ * and nothing prescribed is AXIA_ERR_NO_FREE_DOF (constraint.rs:111-113).
+ * Host object, no device memory. */
+AXIA_API int32_t axia_dofmap_build(int64_t ndof, int64_t n_presc, const int64_t* presc_dof,
+                                   const double* presc_val, int64_t n_mpc, const int64_t* mpc_slave,
+                                   const int64_t* mpc_ptr, const int64_t* mpc_master, const double* mpc_alpha,
+                                   const double* mpc_u0, axia_dofmap** out);
+/* Independent DOF count n_ind (-1 for NULL). */
+AXIA_API int64_t axia_dofmap_n_ind(const axia_dofmap* map);
+/* Copies T (CSR over the ndof full DOFs: t_ptr [ndof+1], t_col / t_val
+ * [nnz]), u0 [ndof] and ind_of [ndof] (-1: prescribed or slave); any
+ * pointer may be NULL.  Returns nnz(T). */
+AXIA_API int64_t axia_dofmap_export(const axia_dofmap* map, int64_t* t_ptr, int64_t* t_col, double* t_val,
+                                    double* u0, int64_t* ind_of);
+AXIA_API void axia_dofmap_free(axia_dofmap* map);
+
+/* The MPC path of solve_linear (analysis.rs:1018-1025) on the GPU:
+ * DofMap::reduce (constraint.rs:138-172) of the caller's full-DOF triplets
+ * (ti, tj, tv in the caller's order) and load f_full [ndof], then
+ * csr_from_triplets, the PCG of axia_gpu_solve_triplets (opts as there) and
+ * reconstruct u_full = u0 + T x (constraint.rs:207-217).  K_ff and the
+ * reduced right-hand side equal the reference's bit for bit.  Replaces any
+ * mesh set up on the context. */
+AXIA_API int32_t axia_gpu_solve_reduced(axia_ctx* ctx, const axia_dofmap* map, int64_t n_trips, const int64_t* ti,
+                                        const int64_t* tj, const double* tv, const double* f_full, double* u_full,
+                                        const axia_solve_opts* opts, axia_solve_info* info);
 
 /* Sizes of the assembled system: n_free and nnz. */
 AXIA_API int32_t axia_gpu_system_size(const axia_ctx* ctx, int64_t* n_free, int64_t* nnz);

@@ -28,6 +28,9 @@
 //                             diag (52-63), chol_solve (78-117), pcg (199-259),
 //                             residual_of (268-278)
 //   solver/src/sparse_native.rs residual_ok (1572-1578)
+//   solver/src/elem.rs        tet4_stiffness (221-248), tet4_nodal_stress (781-795)
+//   solver/src/quadratic.rs   tet10_shape / tet10_dndx / tet10_stiffness (546-627),
+//                             tet10_nodal_stress (678-702)
 // The compliance-gradient routine at the end has no reference counterpart:
 // the reference has no adjoint code.  It restates dC/drho_e =
 // -p rho_e^(p-1) E0 u_e^T K_e(E=1) u_e on top of the restated hex8 stiffness.
@@ -371,7 +374,99 @@ int hex20_face_pressure(const double* xyz, int face, double p, double fe[60]) {
   return OK;
 }
 
+// elem.rs:221-248: constant-strain tetrahedron, J from the edge vectors,
+// Ke = vol B^T D B with vol = det / 6
+int tet4_dndx(const double* xyz, double dndx[4][3], double* det_out) {
+  double j[3][3];
+  for (int p = 0; p < 3; ++p)
+    for (int q = 0; q < 3; ++q) j[q][p] = xyz[3 * (p + 1) + q] - xyz[q];
+  double inv[3][3], det;
+  int st = invert3(j, inv, &det);
+  if (st) return st;
+  if (det <= 0.0) return ERR_NEG_JACOBIAN;
+  const double dn[4][3] = {{-1.0, -1.0, -1.0}, {1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
+  for (int a = 0; a < 4; ++a)
+    for (int i = 0; i < 3; ++i) dndx[a][i] = inv[0][i] * dn[a][0] + inv[1][i] * dn[a][1] + inv[2][i] * dn[a][2];
+  *det_out = det;
+  return OK;
+}
+
+int tet4_stiffness(const double* xyz, double e, double nu, double* ke, double* vol_out) {
+  double dndx[4][3], det;
+  int st = tet4_dndx(xyz, dndx, &det);
+  if (st) return st;
+  const double vol = det / 6.0;
+  double d[36];
+  st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const int n = 12;
+  std::fill(ke, ke + n * n, 0.0);
+  std::vector<double> b(6 * n, 0.0), tmp;
+  fill_b3(b.data(), 4, dndx);
+  gemm_bt_d_b(ke, n, b.data(), 6, d, vol, tmp);
+  *vol_out = vol;
+  return OK;
+}
+
+// quadratic.rs:546-580: quadratic tetrahedron in volume coordinates
+void tet10_shape(double r, double s, double t, double n[10], double dn[10][3]) {
+  const double l1 = 1.0 - r - s - t, l2 = r, l3 = s, l4 = t;
+  n[0] = l1 * (2.0 * l1 - 1.0);
+  n[1] = l2 * (2.0 * l2 - 1.0);
+  n[2] = l3 * (2.0 * l3 - 1.0);
+  n[3] = l4 * (2.0 * l4 - 1.0);
+  n[4] = 4.0 * l1 * l2;
+  n[5] = 4.0 * l2 * l3;
+  n[6] = 4.0 * l3 * l1;
+  n[7] = 4.0 * l1 * l4;
+  n[8] = 4.0 * l2 * l4;
+  n[9] = 4.0 * l3 * l4;
+  const double d1 = 4.0 * l1 - 1.0, d2 = 4.0 * l2 - 1.0, d3 = 4.0 * l3 - 1.0, d4 = 4.0 * l4 - 1.0;
+  const double t_[10][3] = {{-d1, -d1, -d1},
+                            {d2, 0.0, 0.0},
+                            {0.0, d3, 0.0},
+                            {0.0, 0.0, d4},
+                            {4.0 * (l1 - l2), -4.0 * l2, -4.0 * l2},
+                            {4.0 * l3, 4.0 * l2, 0.0},
+                            {-4.0 * l3, 4.0 * (l1 - l3), -4.0 * l3},
+                            {-4.0 * l4, -4.0 * l4, 4.0 * (l1 - l4)},
+                            {4.0 * l4, 0.0, 4.0 * l2},
+                            {0.0, 4.0 * l4, 4.0 * l3}};
+  for (int a = 0; a < 10; ++a)
+    for (int p = 0; p < 3; ++p) dn[a][p] = t_[a][p];
+}
+
+const double TET_A = 0.5854101966249685, TET_B = 0.1381966011250105;  // quadratic.rs:611-612
+const double TET_PTS[4][3] = {{TET_B, TET_B, TET_B}, {TET_A, TET_B, TET_B}, {TET_B, TET_A, TET_B}, {TET_B, TET_B, TET_A}};
+
+// quadratic.rs:607-627
+int tet10_stiffness(const double* xyz, double e, double nu, double* ke, double* vol_out) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const int n = 30;
+  std::fill(ke, ke + n * n, 0.0);
+  double vol = 0.0;
+  const double w = 1.0 / 24.0;
+  std::vector<double> b(6 * n), tmp;
+  for (int g = 0; g < 4; ++g) {
+    double N[10], dn[10][3], dndx[10][3], det;
+    tet10_shape(TET_PTS[g][0], TET_PTS[g][1], TET_PTS[g][2], N, dn);
+    st = hex_dndx<10>(xyz, dn, dndx, &det);
+    if (st) return st;
+    if (det <= 0.0) return ERR_NEG_JACOBIAN;
+    std::fill(b.begin(), b.end(), 0.0);
+    fill_b3(b.data(), 10, dndx);
+    gemm_bt_d_b(ke, n, b.data(), 6, d, w * det, tmp);
+    vol += w * det;
+  }
+  *vol_out = vol;
+  return OK;
+}
+
 int element_ke(int nn, const double* xyz, double e, double nu, int reduced, double* ke, double* vol) {
+  if (nn == 4) return tet4_stiffness(xyz, e, nu, ke, vol);
+  if (nn == 10) return tet10_stiffness(xyz, e, nu, ke, vol);
   if (nn == 8) {
     double d[36];
     int st = d_iso_3d(e, nu, d);
@@ -649,6 +744,45 @@ int hex20_nodal_stress(const double* xyz, const double* ue, double e, double nu,
   return OK;
 }
 
+// elem.rs:781-795: one constant stress for all four nodes
+int tet4_nodal_stress(const double* xyz, const double* ue, double e, double nu, double out[20][6]) {
+  double dndx[4][3], det;
+  int st = tet4_dndx(xyz, dndx, &det);
+  if (st) return st;
+  double d[36];
+  st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const int n = 12;
+  std::vector<double> b(6 * n, 0.0);
+  fill_b3(b.data(), 4, dndx);
+  double sig[6];
+  sigma_from_b(b.data(), 6, n, d, ue, sig);
+  for (int a = 0; a < 4; ++a)
+    for (int c = 0; c < 6; ++c) out[a][c] = sig[c];
+  return OK;
+}
+
+// quadratic.rs:678-702: stresses evaluated at the ten nodes
+int tet10_nodal_stress(const double* xyz, const double* ue, double e, double nu, double out[20][6]) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const double rst[10][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0.5, 0, 0},
+                             {0.5, 0.5, 0}, {0, 0.5, 0}, {0, 0, 0.5}, {0.5, 0, 0.5}, {0, 0.5, 0.5}};
+  const int n = 30;
+  std::vector<double> b(6 * n);
+  for (int a = 0; a < 10; ++a) {
+    double N[10], dn[10][3], dndx[10][3], det;
+    tet10_shape(rst[a][0], rst[a][1], rst[a][2], N, dn);
+    st = hex_dndx<10>(xyz, dn, dndx, &det);
+    if (st) return st;
+    std::fill(b.begin(), b.end(), 0.0);
+    fill_b3(b.data(), 10, dndx);
+    sigma_from_b(b.data(), 6, n, d, ue, out[a]);
+  }
+  return OK;
+}
+
 // elem.rs:651-660
 double von_mises(const double* s) {
   const double sx = s[0], sy = s[1], sz = s[2], txy = s[3], tyz = s[4], tzx = s[5];
@@ -692,6 +826,10 @@ int or_element_ke(int nn, const double* xyz, double e, double nu, int reduced, d
 int or_face_pressure(int nn, const double* xyz, int face, double p, double* fe) {
   if (nn == 8) return hex8_face_pressure(xyz, face, p, fe);
   if (nn == 20) return hex20_face_pressure(xyz, face, p, fe);
+  if (nn == 4 || nn == 10) {  // apply_pressure has no tetrahedron arm (analysis.rs:1447): no load
+    std::fill(fe, fe + 3 * nn, 0.0);
+    return OK;
+  }
   return ERR_INVALID_ARG;
 }
 
@@ -1165,8 +1303,10 @@ int or_nodal_stress(int64_t n_nodes, const double* coords, int nn, int reduced, 
         xyz[3 * a + q] = coords[3 * (int64_t)c[a] + q];
         ue[3 * a + q] = u_full[3 * (int64_t)c[a] + q];
       }
-    int st = nn == 8 ? hex8_nodal_stress(xyz, ue, e_elem[e], nu, sn)
-                     : hex20_nodal_stress(xyz, ue, e_elem[e], nu, reduced != 0, sn);
+    int st = nn == 8    ? hex8_nodal_stress(xyz, ue, e_elem[e], nu, sn)
+             : nn == 20 ? hex20_nodal_stress(xyz, ue, e_elem[e], nu, reduced != 0, sn)
+             : nn == 10 ? tet10_nodal_stress(xyz, ue, e_elem[e], nu, sn)
+                        : tet4_nodal_stress(xyz, ue, e_elem[e], nu, sn);
     if (st) {
       *bad = e;
       return st;

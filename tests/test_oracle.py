@@ -176,3 +176,35 @@ def test_nafems_le10_stress_pin(key):
     syy = s[m.node_d, 1]
     assert abs(syy - pin["value"]) <= pin["tol"]
     assert abs(syy - pin["target"]) / abs(pin["target"]) < pin["target_rel_tol"]
+
+
+def _tet_patch(nn):
+    """2x2x2 cube block of tetrahedra stretched by u_x = 0.01 on x = 2 (rigid modes removed)."""
+    m = meshgen.block_tet(n=2, nn=nn)
+    lat = np.round(m.coords * 2).astype(int)
+    x0 = np.nonzero(lat[:, 0] == 0)[0]
+    x1 = np.nonzero(lat[:, 0] == 4)[0]
+    o = x0[np.argmin(np.abs(m.coords[x0]).sum(1))]
+    yax = x0[np.argmax(m.coords[x0, 1] - 10 * np.abs(m.coords[x0, 2]))]
+    zax = x0[np.argmax(m.coords[x0, 2] - 10 * np.abs(m.coords[x0, 1]))]
+    bc = list(3 * x0) + [3 * o + 1, 3 * o + 2, 3 * yax + 2, 3 * zax + 1]
+    vals = [0.0] * len(bc) + [0.01] * len(x1)
+    bc += list(3 * x1)
+    m.bc_dof = np.array(bc, np.int64)
+    m.bc_val = np.array(vals)
+    m.cload = np.zeros(m.ndof)
+    return m
+
+
+@pytest.mark.parametrize("nn", [4, 10])
+def test_tetrahedra_patch_and_rigid_modes(nn):
+    """C3D4 / C3D10 (elem.rs:221-248, quadratic.rs:546-702): six rigid-body modes per
+    element and a uniform-strain patch reproduced exactly (sxx = E * 0.01 / 2)."""
+    m = _tet_patch(nn)
+    ke, vol = O.element_ke(m.coords[m.conn[0]], 210000.0, 0.3)
+    w = np.linalg.eigvalsh(ke)
+    assert (np.abs(w) < 1e-8 * w.max()).sum() == 6 and vol > 0
+    r = O.solve_static(m, solver=O.SOLVER_CHOLESKY)
+    s, _ = O.nodal_stress(m, r.u)
+    np.testing.assert_allclose(s[:, 0], 1050.0, rtol=1e-10)
+    np.testing.assert_allclose(s[:, 1:], 0.0, atol=1e-8)
