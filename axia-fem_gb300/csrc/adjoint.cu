@@ -126,6 +126,24 @@ element_energy_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const do
   }
 }
 
+// C3D8R / C3D8I: s_e = u_e^T K_e v_e / E_e from the assembled element stiffness (the
+// hourglass and condensed parts are linear in E too); one warp per element
+__global__ void k_ke_energy(int64_t n_elem, const int32_t* __restrict__ conn, const double* __restrict__ ke,
+                            const double* __restrict__ e_elem, const double* __restrict__ u,
+                            const double* __restrict__ v, double* __restrict__ s_out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); e < n_elem; e += warps) {
+    const int64_t d = lane < 24 ? 3 * (int64_t)conn[e * 8 + lane / 3] + lane % 3 : 0;
+    const double ve = lane < 24 ? v[d] : 0.0, ue = lane < 24 ? u[d] : 0.0;
+    double kv = 0.0;
+    const double* row = ke + e * 576 + (int64_t)(lane < 24 ? lane : 0) * 24;
+    for (int j = 0; j < 24; ++j) kv = fma(row[j], __shfl_sync(0xffffffffu, ve, j), kv);
+    const double t = warp_sum(lane < 24 ? ue * kv : 0.0);
+    if (lane == 0) s_out[e] = t / e_elem[e];
+  }
+}
+
 // E_e = e0 rho_e^p
 __global__ void k_simp_modulus(int64_t n, const double* rho, double pexp, double e0, double* e_out, DevStatus* st) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -163,7 +181,12 @@ int element_energy(axia_ctx* ctx, const double* d_u, const double* d_v, double* 
   const double *dn = nullptr, *w = nullptr;
   AXIA_TRY(element_tables_for(ctx, ctx->nn, ctx->ngp, &dn, &w));
   AXIA_TRY(reset_dev_status(ctx));
-  if (ctx->nn == 8) {
+  if (ctx->nn == 8 && ctx->reduced) {
+    if (!ctx->assembled || !ctx->d_ke)
+      return set_error(ctx, AXIA_ERR_STATE, "element energy of C3D8R / C3D8I needs the assembled element stiffness");
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((ctx->n_elem + 3) / 4, ctx->sm_count * 16));
+    k_ke_energy<<<grid, 128, 0, ctx->stream>>>(ctx->n_elem, ctx->d_conn, ctx->d_ke, ctx->d_e, d_u, d_v, d_s);
+  } else if (ctx->nn == 8) {
     const int threads = 256;
     const int64_t per_block = 8 * 4;
     const unsigned grid = (unsigned)std::min<int64_t>((ctx->n_elem + per_block - 1) / per_block, ctx->sm_count * 16);

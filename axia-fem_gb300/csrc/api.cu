@@ -274,8 +274,12 @@ int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const
     return set_error(ctx, AXIA_ERR_MATERIAL, "invalid Young's modulus E=" + std::to_string(mesh->e));
   free_mesh_state(ctx);
   ctx->nn = mesh->nn;
-  ctx->reduced = mesh->nn == 20 && mesh->reduced ? 1 : 0;
-  ctx->ngp = mesh->nn == 4 ? 1 : mesh->nn == 10 ? 4 : (mesh->nn == 8 || ctx->reduced) ? 8 : 27;
+  // nn = 8: reduced 1 = C3D8R, 2 = C3D8I; nn = 20: reduced 1 = C3D20R
+  ctx->reduced = mesh->nn == 20 ? (mesh->reduced ? 1 : 0)
+                 : mesh->nn == 8 ? ((mesh->reduced == 1 || mesh->reduced == 2) ? mesh->reduced : 0)
+                                 : 0;
+  ctx->ngp = mesh->nn == 4 ? 1 : mesh->nn == 10 ? 4 : (mesh->nn == 8 && ctx->reduced == 1) ? 1
+             : (mesh->nn == 8 || ctx->reduced) ? 8 : 27;
   ctx->n_nodes = mesh->n_nodes;
   ctx->n_elem = mesh->n_elem;
   ctx->nu = mesh->nu;

@@ -108,7 +108,9 @@ struct HostTables {
 HostTables make_tables(int nn, int ng) {
   HostTables t;
   std::vector<double> pts;  // xi, eta, zeta, w
-  if (nn == 4) {
+  if (nn == 8 && ng == 1) {
+    pts = {0.0, 0.0, 0.0, 8.0};  // C3D8R: the centre, weight 8 (vol = 8 det J0, extra.rs:407)
+  } else if (nn == 4) {
     pts = {0.25, 0.25, 0.25, 1.0 / 6.0};  // constant strain: one point, weight = reference volume
   } else if (nn == 10) {
     const double w = 1.0 / 24.0;  // quadratic.rs:613-614
@@ -167,10 +169,11 @@ struct DevTables {
   int* blk = nullptr;
 };
 
-DevTables g_tab[5];  // hex8, hex20 (27 gp), hex20r (8 gp), tet4, tet10 -- per process, by device id
-int g_tab_device[5] = {-1, -1, -1, -1, -1};
+DevTables g_tab[6];  // hex8, hex20 (27 gp), hex20r (8 gp), tet4, tet10, hex8r (1 gp) -- by device id
+int g_tab_device[6] = {-1, -1, -1, -1, -1, -1};
 
 int table_index(int nn, int ng) {
+  if (nn == 8 && ng == 1) return 5;
   if (nn == 4) return 3;
   if (nn == 10) return 4;
   return nn == 8 ? 0 : (ng == 27 ? 1 : 2);
@@ -233,8 +236,22 @@ int element_tables_for(axia_ctx* ctx, int nn, int ng, const double** dn, const d
 }
 
 // Runs the element kernel for nn / reduced on args (device pointers).
+int run_hex8r_hourglass(axia_ctx* ctx, const ElemArgs& args);
+int run_hex8i_condense(axia_ctx* ctx, const ElemArgs& args, const double* dn_tab);
+
+// nn = 8: reduced 1 = C3D8R (centre point + hourglass), 2 = C3D8I (incompatible modes)
 int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args) {
   if (args.n_elem == 0) return AXIA_OK;
+  if (nn == 8 && reduced == 1) {
+    AXIA_TRY((launch_element_ke<8, 1, 8>(ctx, args)));
+    return run_hex8r_hourglass(ctx, args);
+  }
+  if (nn == 8 && reduced == 2) {
+    AXIA_TRY((launch_element_ke<8, 8, 8>(ctx, args)));
+    ElemTables tab;
+    AXIA_TRY(ensure_tables(ctx, 8, 8, &tab));
+    return run_hex8i_condense(ctx, args, tab.dn);
+  }
   if (nn == 8) return launch_element_ke<8, 8, 8>(ctx, args);
   if (nn == 20 && !reduced) return launch_element_ke<20, 27, 4>(ctx, args);
   if (nn == 20 && reduced) return launch_element_ke<20, 8, 4>(ctx, args);

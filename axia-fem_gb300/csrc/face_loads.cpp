@@ -7,7 +7,8 @@
 // normal r_xi x r_eta, and the traction is +p n_in (positive p compresses).
 // C3D8 faces use 2x2 Gauss with bilinear shapes (elem.rs:891-950), C3D20
 // faces 3x3 Gauss with 8-node serendipity shapes (quadratic.rs:275-315,
-// quad8_shape quadratic.rs:328-353).  Loads are added in list order.
+// quad8_shape quadratic.rs:328-353).  Wedge faces follow extra.rs (below).
+// Loads are added in list order.
 #include <cmath>
 #include <cstdint>
 
@@ -47,18 +48,116 @@ void face_shape(int nf, double s, double t, double* n, double (*dn)[2]) {
   }
 }
 
+// Wedge faces (solver/src/extra.rs:184-195 C3D6, 869-880 C3D15): P1 and P2
+// are the triangles, P3..P5 the quadrilaterals; corners first, then mid-sides.
+const int kWedgeTri[2][6] = {{0, 1, 2, 6, 7, 8}, {3, 5, 4, 11, 10, 9}};
+const int kWedgeQuad[3][8] = {{0, 1, 4, 3, 6, 13, 9, 12}, {1, 2, 5, 4, 7, 14, 10, 13}, {2, 0, 3, 5, 8, 12, 11, 14}};
+
+inline void cross3(const double* u, const double* v, double* n) {
+  n[0] = u[1] * v[2] - u[2] * v[1];
+  n[1] = u[2] * v[0] - u[0] * v[2];
+  n[2] = u[0] * v[1] - u[1] * v[0];
+}
+
+// One wedge face into fe (element-local, 3 per node).  The traction is
+// -p r_xi x r_eta, the wedge lists winding outward (extra.rs:197-253 and
+// 882-954): flat triangle = a third of -p * area vector per corner; 6-node
+// triangle = 3 points of weight 1/6; quadrilaterals = 2x2 / 3x3 Gauss.
+void wedge_face(int nn, int fid, const double* coords, const int32_t* c, double p, double* fe) {
+  const bool quad = fid >= 3;
+  const int* fl = quad ? kWedgeQuad[fid - 3] : kWedgeTri[fid - 1];
+  const int nf = quad ? (nn == 6 ? 4 : 8) : (nn == 6 ? 3 : 6);
+  double x[8][3];
+  for (int a = 0; a < nf; ++a)
+    for (int q = 0; q < 3; ++q) x[a][q] = coords[3 * (int64_t)c[fl[a]] + q];
+  if (nf == 3) {
+    const double u[3] = {x[1][0] - x[0][0], x[1][1] - x[0][1], x[1][2] - x[0][2]};
+    const double v[3] = {x[2][0] - x[0][0], x[2][1] - x[0][1], x[2][2] - x[0][2]};
+    double nrm[3];
+    cross3(u, v, nrm);
+    const double sc = -p * 0.5 / 3.0;
+    for (int a = 0; a < 3; ++a)
+      for (int q = 0; q < 3; ++q) fe[3 * fl[a] + q] += sc * nrm[q];
+    return;
+  }
+  if (nf == 6) {
+    const double pts[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {2.0 / 3.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}};
+    for (const auto& g : pts) {
+      const double l1 = g[0], l2 = g[1], l3 = 1.0 - l1 - l2;
+      const double n[6] = {l1 * (2.0 * l1 - 1.0), l2 * (2.0 * l2 - 1.0), l3 * (2.0 * l3 - 1.0),
+                           4.0 * l1 * l2,         4.0 * l2 * l3,         4.0 * l3 * l1};
+      const double d1[6] = {4.0 * l1 - 1.0, 0.0, -(4.0 * l3 - 1.0), 4.0 * l2, -4.0 * l2, 4.0 * (l3 - l1)};
+      const double d2[6] = {0.0, 4.0 * l2 - 1.0, -(4.0 * l3 - 1.0), 4.0 * l1, 4.0 * (l3 - l2), -4.0 * l1};
+      double rs[3] = {0, 0, 0}, rt[3] = {0, 0, 0}, nrm[3];
+      for (int a = 0; a < 6; ++a)
+        for (int q = 0; q < 3; ++q) {
+          rs[q] += d1[a] * x[a][q];
+          rt[q] += d2[a] * x[a][q];
+        }
+      cross3(rs, rt, nrm);
+      for (int a = 0; a < 6; ++a)
+        for (int q = 0; q < 3; ++q) fe[3 * fl[a] + q] += -p * n[a] * nrm[q] * (1.0 / 6.0);
+    }
+    return;
+  }
+  const double g2 = 0.5773502691896257;
+  const double g3[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};
+  const double w3[3] = {0.5555555555555556, 0.8888888888888888, 0.5555555555555556};
+  const int m = nf == 4 ? 2 : 3;
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) {
+      const double s = nf == 4 ? (i ? g2 : -g2) : g3[i], t = nf == 4 ? (j ? g2 : -g2) : g3[j];
+      double n[8], dn[8][2], rs[3] = {0, 0, 0}, rt[3] = {0, 0, 0}, nrm[3];
+      face_shape(nf, s, t, n, dn);
+      for (int a = 0; a < nf; ++a)
+        for (int q = 0; q < 3; ++q) {
+          rs[q] += dn[a][0] * x[a][q];
+          rt[q] += dn[a][1] * x[a][q];
+        }
+      cross3(rs, rt, nrm);
+      if (nf == 4) {
+        for (int a = 0; a < 4; ++a)
+          for (int q = 0; q < 3; ++q) fe[3 * fl[a] + q] += -p * n[a] * nrm[q];
+      } else {
+        const double w = w3[i] * w3[j];
+        for (int a = 0; a < 8; ++a)
+          for (int q = 0; q < 3; ++q) fe[3 * fl[a] + q] += -p * n[a] * nrm[q] * w;
+      }
+    }
+}
+
 }  // namespace
 
 extern "C" int32_t axia_face_loads(int32_t nn, int64_t n_nodes, const double* coords, const int32_t* conn,
                                    int64_t n_loads, const int64_t* elem, const int32_t* face, const double* p,
                                    double* f_full, int64_t* bad_load) {
   if (bad_load) *bad_load = -1;
-  if ((nn != 4 && nn != 8 && nn != 10 && nn != 20) || n_loads < 0 ||
+  if ((nn != 4 && nn != 6 && nn != 8 && nn != 10 && nn != 15 && nn != 20) || n_loads < 0 ||
       (n_loads > 0 && (!coords || !conn || !elem || !face || !p || !f_full)))
     return AXIA_ERR_INVALID_ARG;
   // apply_pressure has no tetrahedron arm (analysis.rs:1447): a face pressure on
   // C3D4 / C3D10 adds nothing, as in the reference
   if (nn == 4 || nn == 10) return AXIA_OK;
+  if (nn == 6 || nn == 15) {
+    for (int64_t k = 0; k < n_loads; ++k) {
+      const int fid = face[k];
+      if (fid < 1 || fid > 5 || !std::isfinite(p[k])) {
+        if (bad_load) *bad_load = k;
+        return fid < 1 || fid > 5 ? AXIA_ERR_INVALID_ARG : AXIA_ERR_NONFINITE;
+      }
+      const int32_t* c = conn + elem[k] * nn;
+      for (int a = 0; a < nn; ++a)
+        if (c[a] < 0 || c[a] >= n_nodes) {
+          if (bad_load) *bad_load = k;
+          return AXIA_ERR_INVALID_ARG;
+        }
+      double fe[45] = {};
+      wedge_face(nn, fid, coords, c, p[k], fe);
+      for (int a = 0; a < nn; ++a)
+        for (int q = 0; q < 3; ++q) f_full[3 * (int64_t)c[a] + q] += fe[3 * a + q];
+    }
+    return AXIA_OK;
+  }
   const int nf = nn == 8 ? 4 : 8;
   const double g2 = 0.5773502691896257;
   const double g3[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};

@@ -258,6 +258,23 @@ __global__ void k_recover_nodes(int64_t n_nodes, int nn, const int64_t* __restri
   }
 }
 
+// one warp per C3D8 element: rows 0..23 of K_e u_e into the force slots of rec
+__global__ void k_ke_force(int64_t n_elem, const int32_t* __restrict__ conn, const double* __restrict__ ke,
+                           const double* __restrict__ u, double* __restrict__ rec) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t e = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); e < n_elem; e += warps) {
+    const double ue = lane < 24 ? u[3 * (int64_t)conn[e * 8 + lane / 3] + lane % 3] : 0.0;
+    double f = 0.0;
+    const double* row = ke + e * 576 + (int64_t)(lane < 24 ? lane : 0) * 24;
+    for (int j = 0; j < 24; ++j) {
+      const double uj = __shfl_sync(0xffffffffu, ue, j);
+      f = fma(row[j], uj, f);
+    }
+    if (lane < 24) rec[(e * 8 + lane / 3) * kRec + 6 + lane % 3] = f;
+  }
+}
+
 // lagrange1d quadratic.rs:227-244
 void lagrange_weights(const double* pts, int n, double x, double* w) {
   for (int i = 0; i < n; ++i) {
@@ -305,7 +322,7 @@ struct XTab {
   int* perm = nullptr;
   int device = -1;
 };
-XTab g_xtab[5];  // hex8, hex20, hex20r, tet4, tet10
+XTab g_xtab[6];  // hex8, hex20, hex20r, tet4, tet10, hex8r
 
 // The points the recovery kernel evaluates and how nodes take their stress:
 //  * hexahedra: the stiffness Gauss points, extrapolated to the nodes (X above);
@@ -327,13 +344,14 @@ struct TetRecTab {
 TetRecTab g_tet10_rec;
 
 int ensure_xtab(axia_ctx* ctx, const double** x, const int** perm) {
-  const int ti = ctx->nn == 4 ? 3 : ctx->nn == 10 ? 4 : ctx->nn == 8 ? 0 : (ctx->ngp == 27 ? 1 : 2);
+  const int ti = ctx->nn == 4 ? 3 : ctx->nn == 10 ? 4 : (ctx->nn == 8 && ctx->ngp == 1) ? 5 : ctx->nn == 8 ? 0
+                                                                                          : (ctx->ngp == 27 ? 1 : 2);
   XTab& t = g_xtab[ti];
   if (t.device != ctx->device) {
     std::vector<double> hx;
     std::vector<int> hp;
-    if (ctx->nn == 4) {
-      hx.assign(4, 1.0);
+    if (ctx->nn == 4 || (ctx->nn == 8 && ctx->ngp == 1)) {  // one point, every node takes its stress
+      hx.assign(ctx->nn, 1.0);
       hp.assign(1, 0);
     } else if (ctx->nn == 10) {
       hx.assign(10 * 14, 0.0);
@@ -395,13 +413,17 @@ void launch_element_recover(axia_ctx* ctx, const double* d_u, const double* dn, 
 int recover_device(axia_ctx* ctx, const double* d_u, const double* d_f, double e_strain, double* d_stress,
                    double* d_strain, double* d_vm, double* d_rf, double* d_emean) {
   if (!ctx->d_conn || !ctx->d_ne_ptr) return set_error(ctx, AXIA_ERR_STATE, "recovery before setup");
+  if (ctx->nn == 8 && ctx->reduced && (!ctx->assembled || !ctx->d_ke))
+    return set_error(ctx, AXIA_ERR_STATE, "recovery of C3D8R / C3D8I needs the assembled element stiffness");
   if (d_strain && !(e_strain > 0.0)) return set_error(ctx, AXIA_ERR_MATERIAL, "strain conversion needs E > 0");
   if (ctx->n_elem == 0) return AXIA_OK;
   if (!ctx->d_rec) AXIA_TRY(dev_alloc(ctx, &ctx->d_rec, (size_t)ctx->n_elem * ctx->nn * kRec));
   RecTables t{};
   AXIA_TRY(recover_tables(ctx, &t));
   AXIA_TRY(reset_dev_status(ctx));
-  if (ctx->nn == 8)
+  if (ctx->nn == 8 && ctx->ngp == 1)
+    launch_element_recover<8, 1>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
+  else if (ctx->nn == 8)
     launch_element_recover<8, 8>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
   else if (ctx->nn == 4)
     launch_element_recover<4, 1>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
@@ -413,6 +435,14 @@ int recover_device(axia_ctx* ctx, const double* d_u, const double* d_f, double e
     launch_element_recover<20, 8>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());
+  if (ctx->nn == 8 && ctx->reduced) {
+    // C3D8R / C3D8I: the internal forces include the hourglass / condensed parts,
+    // so they come from the assembled element stiffness: f_e = K_e u_e
+    k_ke_force<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((ctx->n_elem + 3) / 4, ctx->sm_count * 16)), 128, 0,
+                 ctx->stream>>>(ctx->n_elem, ctx->d_conn, ctx->d_ke, d_u, ctx->d_rec);
+    ctx->launches++;
+    AXIA_CUDA(ctx, cudaGetLastError());
+  }
   const unsigned grid = (unsigned)std::max<int64_t>(
       1, std::min<int64_t>((ctx->n_nodes + 255) / 256, (int64_t)ctx->sm_count * 16));
   k_recover_nodes<<<grid, 256, 0, ctx->stream>>>(ctx->n_nodes, ctx->nn, ctx->d_ne_ptr, ctx->d_ne, ctx->d_rec, d_f,

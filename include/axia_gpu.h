@@ -88,7 +88,8 @@ typedef struct axia_mesh {
   const double* coords;    /* [n_nodes][3] */
   int64_t n_elem;
   int32_t nn;              /* nodes per element: 8 (C3D8), 20 (C3D20), 4 (C3D4) or 10 (C3D10) */
-  int32_t reduced;         /* 1: C3D20R, 2x2x2 Gauss points (quadratic.rs:100-120); ignored otherwise */
+  int32_t reduced;         /* nn = 20: 1 = C3D20R, 2x2x2 Gauss points (quadratic.rs:100-120);
+                              nn = 8: 1 = C3D8R (extra.rs:400-457), 2 = C3D8I (extra.rs:256-388) */
   const int32_t* conn;     /* [n_elem][nn], 0-based node indices, CalculiX node order */
   const double* e_elem;    /* [n_elem] Young's modulus per element, or NULL */
   double e;                /* Young's modulus when e_elem == NULL */
@@ -137,10 +138,13 @@ AXIA_API void axia_gpu_destroy(axia_ctx* ctx);
 /* Message of the last failed call on ctx ("" when none). */
 AXIA_API const char* axia_gpu_last_error(const axia_ctx* ctx);
 
-/* Batched element_ke (solver/src/elem.rs:344-375 Hex8 arm, :487-495 Hex20
- * arm, hex8_stiffness elem.rs:194-219, hex20_stiffness quadratic.rs:122-146):
- * for n_elem elements with nn nodes each, xyz[n_elem][nn][3] -> ke[n_elem]
- * [3nn][3nn] row-major (DOF order node-major, x y z) and vol[n_elem].
+/* Batched element_ke (solver/src/elem.rs:344-375 Hex8 / Hex8R / Hex8I /
+ * Tet4 arms, :487-495 Hex20 arm, :496 Tet10 arm; hex8_stiffness
+ * elem.rs:194-219, hex20_stiffness quadratic.rs:122-146, tet4_stiffness
+ * elem.rs:221-248, tet10_stiffness quadratic.rs:607-627, hex8r / hex8i
+ * extra.rs:256-457): for n_elem elements with nn (4, 8, 10, 20) nodes each,
+ * xyz[n_elem][nn][3] -> ke[n_elem][3nn][3nn] row-major (DOF order
+ * node-major, x y z) and vol[n_elem]; `reduced` as in axia_mesh.
  * e[n_elem] per element.  On an element error *bad_elem holds its index. */
 AXIA_API int32_t axia_gpu_element_ke(axia_ctx* ctx, int32_t nn, int32_t reduced, int64_t n_elem,
                             const double* xyz, const double* e, double nu, double* ke,

@@ -29,6 +29,11 @@
 //                             residual_of (268-278)
 //   solver/src/sparse_native.rs residual_ok (1572-1578)
 //   solver/src/elem.rs        tet4_stiffness (221-248), tet4_nodal_stress (781-795)
+//   solver/src/extra.rs       invert_n (8-49), hex8i_stiffness (256-388), hex8i_nodal_stress
+//                             (390-395, = hex8_nodal_stress), hex8r_stiffness (400-457),
+//                             hex8r_nodal_stress (460-472), wedge_shape / wedge6_stiffness /
+//                             wedge6_nodal_stress / wedge6_face_pressure (64-255),
+//                             wedge15_* (701-955)
 //   solver/src/quadratic.rs   tet10_shape / tet10_dndx / tet10_stiffness (546-627),
 //                             tet10_nodal_stress (678-702)
 // The compliance-gradient routine at the end has no reference counterpart:
@@ -464,9 +469,287 @@ int tet10_stiffness(const double* xyz, double e, double nu, double* ke, double* 
   return OK;
 }
 
+// extra.rs:8-49: Gauss-Jordan with partial pivoting, singular below 1e-18
+int invert_n(const std::vector<double>& a, int n, std::vector<double>& inv) {
+  std::vector<double> m = a;
+  inv.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    double best = std::fabs(m[(size_t)k * n + k]);
+    for (int i = k + 1; i < n; ++i) {
+      const double v = std::fabs(m[(size_t)i * n + k]);
+      if (v > best) {
+        best = v;
+        piv = i;
+      }
+    }
+    if (best < 1e-18) return ERR_SINGULAR_JACOBIAN;  // "Kleine Matrix singulaer" (extra.rs:25)
+    if (piv != k)
+      for (int j = 0; j < n; ++j) {
+        std::swap(m[(size_t)k * n + j], m[(size_t)piv * n + j]);
+        std::swap(inv[(size_t)k * n + j], inv[(size_t)piv * n + j]);
+      }
+    const double d = m[(size_t)k * n + k];
+    for (int j = 0; j < n; ++j) {
+      m[(size_t)k * n + j] /= d;
+      inv[(size_t)k * n + j] /= d;
+    }
+    for (int i = 0; i < n; ++i) {
+      if (i == k) continue;
+      const double f = m[(size_t)i * n + k];
+      for (int j = 0; j < n; ++j) {
+        m[(size_t)i * n + j] -= f * m[(size_t)k * n + j];
+        inv[(size_t)i * n + j] -= f * inv[(size_t)k * n + j];
+      }
+    }
+  }
+  return OK;
+}
+
+// extra.rs:256-388: C3D8 with nine incompatible modes (Wilson-Taylor, modes
+// mapped with the centre Jacobian), condensed statically
+int hex8i_stiffness(const double* xyz, double e, double nu, double* kee, double* vol_out) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const int n = 24, ni = 9;
+  std::fill(kee, kee + n * n, 0.0);
+  std::vector<double> kea((size_t)n * ni, 0.0), kaa((size_t)ni * ni, 0.0);
+  double vol = 0.0;
+  double N0[8], dn0[8][3], dndx0[8][3], det0;
+  hex8_shape(0.0, 0.0, 0.0, N0, dn0);
+  st = hex_dndx<8>(xyz, dn0, dndx0, &det0);
+  if (st) return st;
+  if (det0 <= 0.0) return ERR_NEG_JACOBIAN;
+  double j0[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int a = 0; a < 8; ++a)
+    for (int p = 0; p < 3; ++p)
+      for (int q = 0; q < 3; ++q) j0[q][p] += dn0[a][p] * xyz[3 * a + q];
+  double inv0[3][3], dj;
+  st = invert3(j0, inv0, &dj);
+  if (st) return st;
+  const double pts[2] = {-G2, G2};
+  std::vector<double> be(6 * n), ba(6 * ni), tmp, tmp2(6 * ni);
+  for (double xi : pts)
+    for (double eta : pts)
+      for (double zeta : pts) {
+        double N[8], dn[8][3], dndx[8][3], det;
+        hex8_shape(xi, eta, zeta, N, dn);
+        st = hex_dndx<8>(xyz, dn, dndx, &det);
+        if (st) return st;
+        if (det <= 0.0) return ERR_NEG_JACOBIAN;
+        std::fill(be.begin(), be.end(), 0.0);
+        fill_b3(be.data(), 8, dndx);
+        gemm_bt_d_b(kee, n, be.data(), 6, d, det, tmp);
+        vol += det;
+        std::fill(ba.begin(), ba.end(), 0.0);
+        const double dparent[3][3] = {{-2.0 * xi, 0.0, 0.0}, {0.0, -2.0 * eta, 0.0}, {0.0, 0.0, -2.0 * zeta}};
+        for (int m = 0; m < 3; ++m) {
+          double g[3];
+          for (int i = 0; i < 3; ++i)
+            g[i] = inv0[0][i] * dparent[m][0] + inv0[1][i] * dparent[m][1] + inv0[2][i] * dparent[m][2];
+          for (int dir = 0; dir < 3; ++dir) {
+            const int col = m * 3 + dir;
+            if (dir == 0) {
+              ba[0 * ni + col] = g[0];
+              ba[3 * ni + col] = g[1];
+              ba[5 * ni + col] = g[2];
+            } else if (dir == 1) {
+              ba[1 * ni + col] = g[1];
+              ba[3 * ni + col] = g[0];
+              ba[4 * ni + col] = g[2];
+            } else {
+              ba[2 * ni + col] = g[2];
+              ba[4 * ni + col] = g[1];
+              ba[5 * ni + col] = g[0];
+            }
+          }
+        }
+        for (int i = 0; i < 6; ++i)
+          for (int j = 0; j < ni; ++j) {
+            double t = 0.0;
+            for (int k = 0; k < 6; ++k) t += d[i * 6 + k] * ba[k * ni + j];
+            tmp2[i * ni + j] = t;
+          }
+        for (int i = 0; i < ni; ++i)
+          for (int j = 0; j < ni; ++j) {
+            double t = 0.0;
+            for (int k = 0; k < 6; ++k) t += ba[k * ni + i] * tmp2[k * ni + j];
+            kaa[(size_t)i * ni + j] += det * t;
+          }
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < ni; ++j) {
+            double t = 0.0;
+            for (int k = 0; k < 6; ++k) t += be[k * n + i] * tmp2[k * ni + j];
+            kea[(size_t)i * ni + j] += det * t;
+          }
+      }
+  std::vector<double> kinv;
+  st = invert_n(kaa, ni, kinv);
+  if (st) return st;
+  std::vector<double> t((size_t)ni * n);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < ni; ++i) {
+      double x = 0.0;
+      for (int k = 0; k < ni; ++k) x += kinv[(size_t)i * ni + k] * kea[(size_t)j * ni + k];
+      t[(size_t)i * n + j] = x;
+    }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double x = 0.0;
+      for (int k = 0; k < ni; ++k) x += kea[(size_t)i * ni + k] * t[(size_t)k * n + j];
+      kee[(size_t)i * n + j] -= x;
+    }
+  *vol_out = vol;
+  return OK;
+}
+
+const double HOURGLASS[4][8] = {{1, -1, 1, -1, 1, -1, 1, -1},  // extra.rs:413-418
+                                {1, 1, -1, -1, -1, -1, 1, 1},
+                                {1, -1, -1, 1, -1, 1, 1, -1},
+                                {-1, 1, -1, 1, 1, -1, 1, -1}};
+
+// extra.rs:400-457: one-point C3D8 plus Flanagan-Belytschko hourglass stiffness
+int hex8r_stiffness(const double* xyz, double e, double nu, double* ke, double* vol_out) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const int n = 24;
+  std::fill(ke, ke + n * n, 0.0);
+  double N[8], dn[8][3], dndx[8][3], det;
+  hex8_shape(0.0, 0.0, 0.0, N, dn);
+  st = hex_dndx<8>(xyz, dn, dndx, &det);
+  if (st) return st;
+  if (det <= 0.0) return ERR_NEG_JACOBIAN;
+  const double vol = 8.0 * det;
+  std::vector<double> b(6 * n, 0.0), tmp;
+  fill_b3(b.data(), 8, dndx);
+  gemm_bt_d_b(ke, n, b.data(), 6, d, vol, tmp);
+  double gamma[4][8];
+  for (int al = 0; al < 4; ++al) {
+    double hx[3] = {0.0, 0.0, 0.0};
+    for (int a = 0; a < 8; ++a)
+      for (int j = 0; j < 3; ++j) hx[j] += HOURGLASS[al][a] * xyz[3 * a + j];
+    for (int a = 0; a < 8; ++a) {
+      double g = HOURGLASS[al][a];
+      for (int j = 0; j < 3; ++j) g -= hx[j] * dndx[a][j];
+      gamma[al][a] = g;
+    }
+  }
+  const double mu = e / (2.0 * (1.0 + nu));
+  const double coeff = 0.1 * mu * std::pow(vol, 1.0 / 3.0);
+  for (int al = 0; al < 4; ++al) {
+    double g2 = 0.0;
+    for (int a = 0; a < 8; ++a) g2 += gamma[al][a] * gamma[al][a];
+    if (g2 < 1e-30) continue;
+    const double q = coeff / std::max(g2, 1e-30);
+    for (int a = 0; a < 8; ++a)
+      for (int bn = 0; bn < 8; ++bn) {
+        const double v = q * gamma[al][a] * gamma[al][bn];
+        for (int dir = 0; dir < 3; ++dir) ke[(3 * a + dir) * n + (3 * bn + dir)] += v;
+      }
+  }
+  *vol_out = vol;
+  return OK;
+}
+
+// extra.rs:64-87: linear wedge, triangle coordinates (xi, eta) x zeta
+void wedge6_shape(double xi, double eta, double zeta, double n[6], double dn[6][3]) {
+  const double l1 = xi, l2 = eta, l3 = 1.0 - xi - eta, zm = 0.5 * (1.0 - zeta), zp = 0.5 * (1.0 + zeta);
+  n[0] = l1 * zm; n[1] = l2 * zm; n[2] = l3 * zm; n[3] = l1 * zp; n[4] = l2 * zp; n[5] = l3 * zp;
+  const double t[6][3] = {{zm, 0.0, -0.5 * l1}, {0.0, zm, -0.5 * l2}, {-zm, -zm, -0.5 * l3},
+                          {zp, 0.0, 0.5 * l1},  {0.0, zp, 0.5 * l2},  {-zp, -zp, 0.5 * l3}};
+  for (int a = 0; a < 6; ++a)
+    for (int p = 0; p < 3; ++p) dn[a][p] = t[a][p];
+}
+
+// extra.rs:701-756: quadratic wedge
+void wedge15_shape(double xi, double eta, double zeta, double n[15], double dn[15][3]) {
+  const double l1 = xi, l2 = eta, l3 = 1.0 - xi - eta, zm = 1.0 - zeta, zp = 1.0 + zeta;
+  n[0] = 0.5 * l1 * zm * (2.0 * l1 - 2.0 - zeta);
+  n[1] = 0.5 * l2 * zm * (2.0 * l2 - 2.0 - zeta);
+  n[2] = 0.5 * l3 * zm * (2.0 * l3 - 2.0 - zeta);
+  n[3] = 0.5 * l1 * zp * (2.0 * l1 - 2.0 + zeta);
+  n[4] = 0.5 * l2 * zp * (2.0 * l2 - 2.0 + zeta);
+  n[5] = 0.5 * l3 * zp * (2.0 * l3 - 2.0 + zeta);
+  n[6] = 2.0 * l1 * l2 * zm;
+  n[7] = 2.0 * l2 * l3 * zm;
+  n[8] = 2.0 * l3 * l1 * zm;
+  n[9] = 2.0 * l1 * l2 * zp;
+  n[10] = 2.0 * l2 * l3 * zp;
+  n[11] = 2.0 * l3 * l1 * zp;
+  n[12] = l1 * (1.0 - zeta * zeta);
+  n[13] = l2 * (1.0 - zeta * zeta);
+  n[14] = l3 * (1.0 - zeta * zeta);
+  const double d1b = 0.5 * zm * (4.0 * l1 - 2.0 - zeta), d2b = 0.5 * zm * (4.0 * l2 - 2.0 - zeta),
+               d3b = 0.5 * zm * (4.0 * l3 - 2.0 - zeta);
+  const double d1t = 0.5 * zp * (4.0 * l1 - 2.0 + zeta), d2t = 0.5 * zp * (4.0 * l2 - 2.0 + zeta),
+               d3t = 0.5 * zp * (4.0 * l3 - 2.0 + zeta);
+  const double o = 1.0 - zeta * zeta;
+  const double t[15][3] = {{d1b, 0.0, -0.5 * l1 * (2.0 * l1 - 1.0 - 2.0 * zeta)},
+                           {0.0, d2b, -0.5 * l2 * (2.0 * l2 - 1.0 - 2.0 * zeta)},
+                           {-d3b, -d3b, -0.5 * l3 * (2.0 * l3 - 1.0 - 2.0 * zeta)},
+                           {d1t, 0.0, 0.5 * l1 * (2.0 * l1 - 1.0 + 2.0 * zeta)},
+                           {0.0, d2t, 0.5 * l2 * (2.0 * l2 - 1.0 + 2.0 * zeta)},
+                           {-d3t, -d3t, 0.5 * l3 * (2.0 * l3 - 1.0 + 2.0 * zeta)},
+                           {2.0 * l2 * zm, 2.0 * l1 * zm, -2.0 * l1 * l2},
+                           {-2.0 * l2 * zm, 2.0 * (l3 - l2) * zm, -2.0 * l2 * l3},
+                           {2.0 * (l3 - l1) * zm, -2.0 * l1 * zm, -2.0 * l3 * l1},
+                           {2.0 * l2 * zp, 2.0 * l1 * zp, 2.0 * l1 * l2},
+                           {-2.0 * l2 * zp, 2.0 * (l3 - l2) * zp, 2.0 * l2 * l3},
+                           {2.0 * (l3 - l1) * zp, -2.0 * l1 * zp, 2.0 * l3 * l1},
+                           {o, 0.0, -2.0 * zeta * l1},
+                           {0.0, o, -2.0 * zeta * l2},
+                           {-o, -o, -2.0 * zeta * l3}};
+  for (int a = 0; a < 15; ++a)
+    for (int p = 0; p < 3; ++p) dn[a][p] = t[a][p];
+}
+
+const double WTRI[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {2.0 / 3.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}};  // extra.rs:114
+
+// extra.rs:109-132 (C3D6: 3 triangle points x 2 in zeta, w = 1/6) and 783-819
+// (C3D15: 3 triangle points x 3 in zeta, w = W3 / 6)
+template <int NN>
+int wedge_stiffness(const double* xyz, double e, double nu, double* ke, double* vol_out) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const int n = 3 * NN;
+  std::fill(ke, ke + n * n, 0.0);
+  double vol = 0.0;
+  std::vector<double> b(6 * n), tmp;
+  const int nz = NN == 6 ? 2 : 3;
+  for (int t = 0; t < 3; ++t)
+    for (int k = 0; k < nz; ++k) {
+      const double zeta = NN == 6 ? (k == 0 ? -G2 : G2) : G3[k];
+      const double w0 = NN == 6 ? 1.0 / 6.0 : (1.0 / 6.0) * W3[k];
+      double N[NN], dn[NN][3], dndx[NN][3], det;
+      if (NN == 6)
+        wedge6_shape(WTRI[t][0], WTRI[t][1], zeta, (double*)N, (double(*)[3])dn);
+      else
+        wedge15_shape(WTRI[t][0], WTRI[t][1], zeta, (double*)N, (double(*)[3])dn);
+      st = hex_dndx<NN>(xyz, dn, dndx, &det);
+      if (st) return st;
+      if (det <= 0.0) return ERR_NEG_JACOBIAN;
+      const double w = det * w0;
+      std::fill(b.begin(), b.end(), 0.0);
+      fill_b3(b.data(), NN, dndx);
+      gemm_bt_d_b(ke, n, b.data(), 6, d, w, tmp);
+      vol += w;
+    }
+  *vol_out = vol;
+  return OK;
+}
+
+// nn = 8: reduced 0 = C3D8, 1 = C3D8R, 2 = C3D8I; nn = 20: reduced 1 = C3D20R
 int element_ke(int nn, const double* xyz, double e, double nu, int reduced, double* ke, double* vol) {
+  if (nn == 8 && reduced == 1) return hex8r_stiffness(xyz, e, nu, ke, vol);
+  if (nn == 8 && reduced == 2) return hex8i_stiffness(xyz, e, nu, ke, vol);
   if (nn == 4) return tet4_stiffness(xyz, e, nu, ke, vol);
   if (nn == 10) return tet10_stiffness(xyz, e, nu, ke, vol);
+  if (nn == 6) return wedge_stiffness<6>(xyz, e, nu, ke, vol);
+  if (nn == 15) return wedge_stiffness<15>(xyz, e, nu, ke, vol);
   if (nn == 8) {
     double d[36];
     int st = d_iso_3d(e, nu, d);
@@ -744,6 +1027,51 @@ int hex20_nodal_stress(const double* xyz, const double* ue, double e, double nu,
   return OK;
 }
 
+// extra.rs:460-472: the centre stress at all eight nodes
+int hex8r_nodal_stress(const double* xyz, const double* ue, double e, double nu, double out[20][6]) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  double N[8], dn[8][3], dndx[8][3], det;
+  hex8_shape(0.0, 0.0, 0.0, N, dn);
+  st = hex_dndx<8>(xyz, dn, dndx, &det);
+  if (st) return st;
+  const int n = 24;
+  std::vector<double> b(6 * n, 0.0);
+  fill_b3(b.data(), 8, dndx);
+  double sig[6];
+  sigma_from_b(b.data(), 6, n, d, ue, sig);
+  for (int a = 0; a < 8; ++a)
+    for (int c = 0; c < 6; ++c) out[a][c] = sig[c];
+  return OK;
+}
+
+// extra.rs:134-154 / 821-850: stresses evaluated at the wedge's nodes
+template <int NN>
+int wedge_nodal_stress(const double* xyz, const double* ue, double e, double nu, double out[20][6]) {
+  double d[36];
+  int st = d_iso_3d(e, nu, d);
+  if (st) return st;
+  const double pts[15][3] = {{1, 0, -1}, {0, 1, -1}, {0, 0, -1}, {1, 0, 1},    {0, 1, 1},
+                             {0, 0, 1},  {0.5, 0.5, -1}, {0, 0.5, -1}, {0.5, 0, -1}, {0.5, 0.5, 1},
+                             {0, 0.5, 1}, {0.5, 0, 1},  {1, 0, 0},   {0, 1, 0},    {0, 0, 0}};
+  const int n = 3 * NN;
+  std::vector<double> b(6 * n);
+  for (int a = 0; a < NN; ++a) {
+    double N[NN], dn[NN][3], dndx[NN][3], det;
+    if (NN == 6)
+      wedge6_shape(pts[a][0], pts[a][1], pts[a][2], (double*)N, (double(*)[3])dn);
+    else
+      wedge15_shape(pts[a][0], pts[a][1], pts[a][2], (double*)N, (double(*)[3])dn);
+    st = hex_dndx<NN>(xyz, dn, dndx, &det);
+    if (st) return st;
+    std::fill(b.begin(), b.end(), 0.0);
+    fill_b3(b.data(), NN, dndx);
+    sigma_from_b(b.data(), 6, n, d, ue, out[a]);
+  }
+  return OK;
+}
+
 // elem.rs:781-795: one constant stress for all four nodes
 int tet4_nodal_stress(const double* xyz, const double* ue, double e, double nu, double out[20][6]) {
   double dndx[4][3], det;
@@ -823,7 +1151,128 @@ int or_element_ke(int nn, const double* xyz, double e, double nu, int reduced, d
   return element_ke(nn, xyz, e, nu, reduced, ke, vol);
 }
 
+namespace {
+// extra.rs:197-213: flat triangle, a third of -p * area vector per node
+void tri_face_load(double* fe, const double* xyz, const int idx[3], double p) {
+  const double* a = xyz + 3 * idx[0];
+  const double* b = xyz + 3 * idx[1];
+  const double* c = xyz + 3 * idx[2];
+  const double ux[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+  const double vx[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+  const double nx = ux[1] * vx[2] - ux[2] * vx[1];
+  const double ny = ux[2] * vx[0] - ux[0] * vx[2];
+  const double nz = ux[0] * vx[1] - ux[1] * vx[0];
+  const double sc = -p * 0.5 / 3.0;
+  for (int k = 0; k < 3; ++k) {
+    fe[3 * idx[k]] += sc * nx;
+    fe[3 * idx[k] + 1] += sc * ny;
+    fe[3 * idx[k] + 2] += sc * nz;
+  }
+}
+
+// extra.rs:215-253: bilinear quadrilateral, 2x2 Gauss
+void quad_face_load(double* fe, const double* xyz, const int idx[4], double p) {
+  const double pts[2] = {-G2, G2};
+  for (double xi : pts)
+    for (double eta : pts) {
+      double n[4], dnxi[4], dneta[4];
+      for (int i = 0; i < 4; ++i) {
+        const double x = QUAD_XI[i][0], e = QUAD_XI[i][1];
+        n[i] = 0.25 * (1.0 + x * xi) * (1.0 + e * eta);
+        dnxi[i] = 0.25 * x * (1.0 + e * eta);
+        dneta[i] = 0.25 * e * (1.0 + x * xi);
+      }
+      double rxi[3] = {0, 0, 0}, reta[3] = {0, 0, 0};
+      for (int a = 0; a < 4; ++a)
+        for (int k = 0; k < 3; ++k) {
+          rxi[k] += dnxi[a] * xyz[3 * idx[a] + k];
+          reta[k] += dneta[a] * xyz[3 * idx[a] + k];
+        }
+      const double nx = rxi[1] * reta[2] - rxi[2] * reta[1];
+      const double ny = rxi[2] * reta[0] - rxi[0] * reta[2];
+      const double nz = rxi[0] * reta[1] - rxi[1] * reta[0];
+      for (int a = 0; a < 4; ++a) {
+        fe[3 * idx[a]] += -p * n[a] * nx;
+        fe[3 * idx[a] + 1] += -p * n[a] * ny;
+        fe[3 * idx[a] + 2] += -p * n[a] * nz;
+      }
+    }
+}
+
+// extra.rs:882-924: quadratic triangle, 3 points, w = 1/6
+void tri6_face_load(double* fe, const double* xyz, const int idx[6], double p) {
+  const double w0 = 1.0 / 6.0;
+  for (int g = 0; g < 3; ++g) {
+    const double l1 = WTRI[g][0], l2 = WTRI[g][1], l3 = 1.0 - l1 - l2;
+    const double ns[6] = {l1 * (2.0 * l1 - 1.0), l2 * (2.0 * l2 - 1.0), l3 * (2.0 * l3 - 1.0),
+                          4.0 * l1 * l2,         4.0 * l2 * l3,         4.0 * l3 * l1};
+    const double dn1[6] = {4.0 * l1 - 1.0, 0.0, -(4.0 * l3 - 1.0), 4.0 * l2, -4.0 * l2, 4.0 * (l3 - l1)};
+    const double dn2[6] = {0.0, 4.0 * l2 - 1.0, -(4.0 * l3 - 1.0), 4.0 * l1, 4.0 * (l3 - l2), -4.0 * l1};
+    double rxi[3] = {0, 0, 0}, reta[3] = {0, 0, 0};
+    for (int a = 0; a < 6; ++a)
+      for (int k = 0; k < 3; ++k) {
+        rxi[k] += dn1[a] * xyz[3 * idx[a] + k];
+        reta[k] += dn2[a] * xyz[3 * idx[a] + k];
+      }
+    const double nx = rxi[1] * reta[2] - rxi[2] * reta[1];
+    const double ny = rxi[2] * reta[0] - rxi[0] * reta[2];
+    const double nz = rxi[0] * reta[1] - rxi[1] * reta[0];
+    for (int a = 0; a < 6; ++a) {
+      fe[3 * idx[a]] += -p * ns[a] * nx * w0;
+      fe[3 * idx[a] + 1] += -p * ns[a] * ny * w0;
+      fe[3 * idx[a] + 2] += -p * ns[a] * nz * w0;
+    }
+  }
+}
+
+// extra.rs:926-954: serendipity quadrilateral, 3x3 Gauss
+void quad8_face_load(double* fe, const double* xyz, const int idx[8], double p) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      const double w = W3[i] * W3[j];
+      double ns[8], dn[8][2];
+      quad8_shape(G3[i], G3[j], ns, dn);
+      double rxi[3] = {0, 0, 0}, reta[3] = {0, 0, 0};
+      for (int a = 0; a < 8; ++a)
+        for (int k = 0; k < 3; ++k) {
+          rxi[k] += dn[a][0] * xyz[3 * idx[a] + k];
+          reta[k] += dn[a][1] * xyz[3 * idx[a] + k];
+        }
+      const double nx = rxi[1] * reta[2] - rxi[2] * reta[1];
+      const double ny = rxi[2] * reta[0] - rxi[0] * reta[2];
+      const double nz = rxi[0] * reta[1] - rxi[1] * reta[0];
+      for (int a = 0; a < 8; ++a) {
+        fe[3 * idx[a]] += -p * ns[a] * nx * w;
+        fe[3 * idx[a] + 1] += -p * ns[a] * ny * w;
+        fe[3 * idx[a] + 2] += -p * ns[a] * nz * w;
+      }
+    }
+}
+
+// extra.rs:184-195 and 869-880
+int wedge_face_pressure(int nn, const double* xyz, int face, double p, double* fe) {
+  std::fill(fe, fe + 3 * nn, 0.0);
+  if (nn == 6) {
+    static const int t1[3] = {0, 1, 2}, t2[3] = {3, 5, 4};
+    static const int q[3][4] = {{0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}};
+    if (face == 1) tri_face_load(fe, xyz, t1, p);
+    else if (face == 2) tri_face_load(fe, xyz, t2, p);
+    else if (face >= 3 && face <= 5) quad_face_load(fe, xyz, q[face - 3], p);
+    else return ERR_INVALID_ARG;
+    return OK;
+  }
+  static const int t1[6] = {0, 1, 2, 6, 7, 8}, t2[6] = {3, 5, 4, 11, 10, 9};
+  static const int q[3][8] = {{0, 1, 4, 3, 6, 13, 9, 12}, {1, 2, 5, 4, 7, 14, 10, 13}, {2, 0, 3, 5, 8, 12, 11, 14}};
+  if (face == 1) tri6_face_load(fe, xyz, t1, p);
+  else if (face == 2) tri6_face_load(fe, xyz, t2, p);
+  else if (face >= 3 && face <= 5) quad8_face_load(fe, xyz, q[face - 3], p);
+  else return ERR_INVALID_ARG;
+  return OK;
+}
+}  // namespace
+
 int or_face_pressure(int nn, const double* xyz, int face, double p, double* fe) {
+  if (nn == 6 || nn == 15) return wedge_face_pressure(nn, xyz, face, p, fe);
   if (nn == 8) return hex8_face_pressure(xyz, face, p, fe);
   if (nn == 20) return hex20_face_pressure(xyz, face, p, fe);
   if (nn == 4 || nn == 10) {  // apply_pressure has no tetrahedron arm (analysis.rs:1447): no load
@@ -1303,9 +1752,12 @@ int or_nodal_stress(int64_t n_nodes, const double* coords, int nn, int reduced, 
         xyz[3 * a + q] = coords[3 * (int64_t)c[a] + q];
         ue[3 * a + q] = u_full[3 * (int64_t)c[a] + q];
       }
-    int st = nn == 8    ? hex8_nodal_stress(xyz, ue, e_elem[e], nu, sn)
+    int st = (nn == 8 && reduced == 1) ? hex8r_nodal_stress(xyz, ue, e_elem[e], nu, sn)
+             : nn == 8  ? hex8_nodal_stress(xyz, ue, e_elem[e], nu, sn)
              : nn == 20 ? hex20_nodal_stress(xyz, ue, e_elem[e], nu, reduced != 0, sn)
              : nn == 10 ? tet10_nodal_stress(xyz, ue, e_elem[e], nu, sn)
+             : nn == 6  ? wedge_nodal_stress<6>(xyz, ue, e_elem[e], nu, sn)
+             : nn == 15 ? wedge_nodal_stress<15>(xyz, ue, e_elem[e], nu, sn)
                         : tet4_nodal_stress(xyz, ue, e_elem[e], nu, sn);
     if (st) {
       *bad = e;

@@ -208,3 +208,19 @@ def test_tetrahedra_patch_and_rigid_modes(nn):
     s, _ = O.nodal_stress(m, r.u)
     np.testing.assert_allclose(s[:, 0], 1050.0, rtol=1e-10)
     np.testing.assert_allclose(s[:, 1:], 0.0, atol=1e-8)
+
+
+@pytest.mark.parametrize("variant", [1, 2], ids=["C3D8R", "C3D8I"])
+def test_hex8_variants_rigid_modes_and_patch(variant):
+    """C3D8R / C3D8I (extra.rs:256-472): six rigid-body modes, and the C3D8
+    patch test (lib.rs:429-446) reproduced: u_x = 0.01, sxx = 210."""
+    m = meshgen.patch_c3d8()
+    ke, vol = O.element_ke(m.coords[m.conn[0]], 210000.0, 0.3, reduced=variant)
+    w = np.linalg.eigvalsh(ke)
+    assert (np.abs(w) < 1e-8 * w.max()).sum() == 6
+    m.reduced = variant
+    r = O.solve_static(m, solver=O.SOLVER_CHOLESKY)
+    pin = PINS["patch_c3d8_mean_ux"]
+    assert abs(_mean_ux(r.u, pin["nodes_1based"]) - pin["value"]) < pin["tol"]
+    s, _ = O.nodal_stress(m, r.u)
+    assert abs(s[:, 0].mean() - 210.0) < 1e-3
