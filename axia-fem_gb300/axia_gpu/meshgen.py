@@ -350,3 +350,51 @@ def block_tet(n=6, nn=4, h=1.0, e=210000.0, nu=0.3, fx_total=1000.0, perturb=0.0
     f[3 * tip] = fx_total / len(tip)
     return Model(f"c3d{nn}_block_{n}", coords, conn, nn, np.full(conn.shape[0], e), nu, bc, np.zeros(bc.shape[0]),
                  f, shape=(n, n, n))
+
+
+# Wedges: each cube cell is cut along its xy diagonal into two triangular prisms
+# extruded in z.  Corner order (solver/src/extra.rs:84-107): bottom triangle
+# (0, 1, 2) at zeta = -1 with (x0 - x2) x (x1 - x2) pointing to the top face,
+# then the top triangle (3, 4, 5); C3D15 adds mid-sides 6..8 (bottom edges 0-1,
+# 1-2, 2-0), 9..11 (top edges) and 12..14 (vertical edges 0-3, 1-4, 2-5).
+_WEDGE_TRI = [((1, 0), (1, 1), (0, 0)), ((1, 1), (0, 1), (0, 0))]
+WEDGE15_EDGES = [(0, 1), (1, 2), (2, 0), (3, 4), (4, 5), (5, 3), (0, 3), (1, 4), (2, 5)]
+
+
+def structured_wedges(nx, ny, nz, nn=6, h=1.0):
+    """coords, conn (C3D6 or C3D15, 2 wedges per cube) and the doubled lattice position of each node."""
+    cells = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    corners = []
+    for tri in _WEDGE_TRI:
+        bot = [(a, b, 0) for a, b in tri]
+        top = [(a, b, 1) for a, b in tri]
+        corners.append(np.array(bot + top, np.int64))
+    corners = np.stack(corners)                            # (2, 6, 3) unit-cube offsets
+    wed = (2 * (cells[:, None, None, :] + corners[None])).reshape(-1, 6, 3)
+    pts = [wed[:, a] for a in range(6)]
+    if nn == 15:
+        pts += [(wed[:, a] + wed[:, b]) // 2 for a, b in WEDGE15_EDGES]
+    allp = np.stack(pts, axis=1)
+    mx, my = 2 * nx + 1, 2 * ny + 1
+    key = allp[..., 0] + mx * (allp[..., 1] + my * allp[..., 2])
+    uniq, inv = np.unique(key.ravel(), return_inverse=True)
+    conn = inv.reshape(key.shape).astype(np.int32)
+    lat = np.stack([uniq % mx, (uniq // mx) % my, uniq // (mx * my)], axis=1)
+    coords = lat.astype(np.float64) * (0.5 * h)
+    return coords, conn, lat
+
+
+def block_wedge(n=6, nn=6, h=1.0, e=210000.0, nu=0.3, p=10.0, perturb=0.0, seed=7):
+    """C3D6 / C3D15 n^3 cube block (2 wedges per cube): x=0 clamped, pressure p on the
+    x=L faces (face P3 = nodes 0-1-4-3 of the first wedge of each cell lies on x = 1
+    of the cell; the traction -p n_out pushes inward), interior nodes optionally perturbed."""
+    coords, conn, lat = structured_wedges(n, n, n, nn, h)
+    if perturb > 0:
+        coords = perturb_interior(coords, lat, (2 * n, 2 * n, 2 * n), perturb, 0.5 * h, seed)
+    bc = _clamp_dofs(lat[:, 0] == 0)
+    cell_x = np.arange(conn.shape[0]) // 2 // (n * n)      # cells are ordered x-major
+    loaded = np.nonzero((cell_x == n - 1) & (np.arange(conn.shape[0]) % 2 == 0))[0]
+    m = Model(f"c3d{nn}_block_{n}", coords, conn, nn, np.full(conn.shape[0], e), nu, bc, np.zeros(bc.shape[0]),
+              np.zeros(3 * coords.shape[0]), loaded.astype(np.int64), np.full(loaded.shape[0], 3, np.int32),
+              np.full(loaded.shape[0], p), shape=(n, n, n))
+    return m

@@ -7,7 +7,7 @@
 // The element kernel evaluates the bilinear element form s_e = u_e^T K_e(1) v_e
 // matrix-free at the Gauss points of the reference's element
 // (hex8_stiffness solver/src/elem.rs:194-219, hex20_stiffness
-// solver/src/quadratic.rs:122-146):
+// solver/src/quadratic.rs:122-146, tetrahedra and wedges likewise):
 //   s_e = sum_gp w det J [lam tr(eps_u) tr(eps_v) + 2 mu eps_u:eps_v + mu gam_u.gam_v]
 // (Voigt, engineering shears: the isotropic D of d_iso_3d, elem.rs:41-59, at E=1).
 // Lanes are (element, Gauss point) pairs, 32/NG elements per warp, so every
@@ -118,8 +118,14 @@ element_energy_kernel(int64_t n_elem, const int32_t* __restrict__ conn, const do
     if constexpr ((NG & (NG - 1)) == 0) {
 #pragma unroll
       for (int o = NG / 2; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
-    } else {
+    } else if constexpr (EPW == 1) {
       contrib = warp_sum(contrib);  // one element per warp
+    } else {
+      // lane le * NG sums its element's NG lanes in order (C3D6: 5 x 6, C3D15: 3 x 9)
+      double t = contrib;
+#pragma unroll
+      for (int k = 1; k < NG; ++k) t += __shfl_down_sync(0xffffffffu, contrib, k);
+      contrib = t;
     }
     if (active_lane && g == 0 && e < n_elem) s_out[e] = contrib;
     __syncwarp();
@@ -204,6 +210,16 @@ int element_energy(axia_ctx* ctx, const double* d_u, const double* d_v, double* 
     const unsigned grid = (unsigned)std::min<int64_t>((ctx->n_elem + per_block - 1) / per_block, ctx->sm_count * 16);
     element_energy_kernel<10, 4><<<std::max(1u, grid), threads, 0, ctx->stream>>>(
         ctx->n_elem, ctx->d_conn, ctx->d_coords, d_u, d_v, dn, w, c_lam, c_mu, d_s, ctx->d_status);
+  } else if (ctx->nn == 6 || ctx->nn == 15) {
+    const int threads = 128;
+    const int64_t per_block = 4 * (ctx->nn == 6 ? 32 / 6 : 32 / 9);
+    const unsigned grid = (unsigned)std::min<int64_t>((ctx->n_elem + per_block - 1) / per_block, ctx->sm_count * 16);
+    if (ctx->nn == 6)
+      element_energy_kernel<6, 6><<<std::max(1u, grid), threads, 0, ctx->stream>>>(
+          ctx->n_elem, ctx->d_conn, ctx->d_coords, d_u, d_v, dn, w, c_lam, c_mu, d_s, ctx->d_status);
+    else
+      element_energy_kernel<15, 9><<<std::max(1u, grid), threads, 0, ctx->stream>>>(
+          ctx->n_elem, ctx->d_conn, ctx->d_coords, d_u, d_v, dn, w, c_lam, c_mu, d_s, ctx->d_status);
   } else if (ctx->ngp == 27) {
     const int threads = 128;
     const int64_t per_block = 4;

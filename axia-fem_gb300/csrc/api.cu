@@ -204,8 +204,9 @@ int32_t axia_gpu_element_ke(axia_ctx* ctx, int32_t nn, int32_t reduced, int64_t 
   if (!ctx) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   if (bad_elem) *bad_elem = -1;
-  if ((nn != 4 && nn != 8 && nn != 10 && nn != 20) || n_elem < 0 || (n_elem > 0 && (!xyz || !e || !ke)))
-    return set_error(ctx, AXIA_ERR_INVALID_ARG, "element_ke: nn must be 4, 8, 10 or 20 and buffers non-null");
+  if ((nn != 4 && nn != 6 && nn != 8 && nn != 10 && nn != 15 && nn != 20) || n_elem < 0 ||
+      (n_elem > 0 && (!xyz || !e || !ke)))
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "element_ke: nn must be 4, 6, 8, 10, 15 or 20 and buffers non-null");
   if (nu >= 0.5 || nu <= -1.0 || !std::isfinite(nu))  // d_iso_3d, elem.rs:42-44
     return set_error(ctx, AXIA_ERR_MATERIAL, "invalid Poisson ratio nu=" + std::to_string(nu));
   if (n_elem == 0) return AXIA_OK;
@@ -262,7 +263,8 @@ int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const
   if (!ctx || !mesh) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   auto t0 = std::chrono::steady_clock::now();
-  if ((mesh->nn != 4 && mesh->nn != 8 && mesh->nn != 10 && mesh->nn != 20) || mesh->n_nodes <= 0 ||
+  if ((mesh->nn != 4 && mesh->nn != 6 && mesh->nn != 8 && mesh->nn != 10 && mesh->nn != 15 && mesh->nn != 20) ||
+      mesh->n_nodes <= 0 ||
       mesh->n_elem < 0 || !mesh->coords ||
       (mesh->n_elem > 0 && !mesh->conn) || n_bc < 0 || (n_bc > 0 && (!bc_dof || !bc_val)))
     return set_error(ctx, AXIA_ERR_INVALID_ARG, "setup: bad mesh description");
@@ -278,8 +280,8 @@ int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const
   ctx->reduced = mesh->nn == 20 ? (mesh->reduced ? 1 : 0)
                  : mesh->nn == 8 ? ((mesh->reduced == 1 || mesh->reduced == 2) ? mesh->reduced : 0)
                                  : 0;
-  ctx->ngp = mesh->nn == 4 ? 1 : mesh->nn == 10 ? 4 : (mesh->nn == 8 && ctx->reduced == 1) ? 1
-             : (mesh->nn == 8 || ctx->reduced) ? 8 : 27;
+  ctx->ngp = mesh->nn == 4 ? 1 : mesh->nn == 10 ? 4 : mesh->nn == 6 ? 6 : mesh->nn == 15 ? 9
+             : (mesh->nn == 8 && ctx->reduced == 1) ? 1 : (mesh->nn == 8 || ctx->reduced) ? 8 : 27;
   ctx->n_nodes = mesh->n_nodes;
   ctx->n_elem = mesh->n_elem;
   ctx->nu = mesh->nu;

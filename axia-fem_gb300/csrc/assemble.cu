@@ -93,10 +93,54 @@ void dshape_tet4(double* dn) {
 
 const double kTetA = 0.5854101966249685, kTetB = 0.1381966011250105;  // quadratic.rs:611-612
 
+// extra.rs:64-87: linear wedge in (l1, l2) = (xi, eta), l3 = 1 - xi - eta, zeta in [-1, 1]
+void dshape_wedge6(double xi, double eta, double zeta, double* dn) {
+  const double l1 = xi, l2 = eta, l3 = 1.0 - xi - eta, zm = 0.5 * (1.0 - zeta), zp = 0.5 * (1.0 + zeta);
+  const double v[18] = {zm, 0.0, -0.5 * l1, 0.0, zm, -0.5 * l2, -zm, -zm, -0.5 * l3,
+                        zp, 0.0, 0.5 * l1,  0.0, zp, 0.5 * l2,  -zp, -zp, 0.5 * l3};
+  for (int k = 0; k < 18; ++k) dn[k] = v[k];
+}
+
+// extra.rs:701-756: quadratic wedge; corner a of triangle position l_a, mid-sides
+// 6..8 / 9..11 on the bottom / top edges (0-1, 1-2, 2-0), 12..14 on the vertical edges
+void dshape_wedge15(double xi, double eta, double zeta, double* dn) {
+  const double l[3] = {xi, eta, 1.0 - xi - eta};
+  const double dl[3][2] = {{1.0, 0.0}, {0.0, 1.0}, {-1.0, -1.0}};  // d l_a / d(xi, eta)
+  for (int c = 0; c < 6; ++c) {  // corners: 0.5 l (1 + s zeta)(2 l - 2 + s zeta)
+    const int a = c % 3;
+    const double sg = c < 3 ? -1.0 : 1.0, z = 1.0 + sg * zeta, la = l[a];
+    const double dla = 0.5 * z * (4.0 * la - 2.0 + sg * zeta);
+    dn[3 * c] = dla * dl[a][0];
+    dn[3 * c + 1] = dla * dl[a][1];
+    dn[3 * c + 2] = 0.5 * sg * la * (2.0 * la - 1.0 + 2.0 * sg * zeta);
+  }
+  for (int m = 0; m < 6; ++m) {  // triangle-edge mid-sides: 2 l_a l_b (1 + s zeta)
+    const int a = m % 3, b = (a + 1) % 3;
+    const double sg = m < 3 ? -1.0 : 1.0, z = 1.0 + sg * zeta;
+    for (int p = 0; p < 2; ++p) dn[3 * (6 + m) + p] = 2.0 * z * (dl[a][p] * l[b] + l[a] * dl[b][p]);
+    dn[3 * (6 + m) + 2] = 2.0 * sg * l[a] * l[b];
+  }
+  for (int a = 0; a < 3; ++a) {  // vertical mid-sides: l_a (1 - zeta^2)
+    const double o = 1.0 - zeta * zeta;
+    dn[3 * (12 + a)] = o * dl[a][0];
+    dn[3 * (12 + a) + 1] = o * dl[a][1];
+    dn[3 * (12 + a) + 2] = -2.0 * zeta * l[a];
+  }
+}
+
+// the three triangle points of the wedge rules (extra.rs:114, 783-797)
+const double kTri[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {2.0 / 3.0, 1.0 / 6.0}, {1.0 / 6.0, 2.0 / 3.0}};
+
 }  // namespace
 
-// dN/dxi of the quadratic tetrahedron at (r, s, t), [10][3] (used by the recovery tables)
-void tet10_dshape(double r, double s, double t, double* dn) { dshape_tet10(r, s, t, dn); }
+// dN/dxi [nn][3] at a parametric point of a C3D4 / C3D6 / C3D10 / C3D15 element
+// (used by the recovery tables, which also evaluate the stress at the nodes)
+void element_dshape(int nn, double r, double s, double t, double* dn) {
+  if (nn == 10) dshape_tet10(r, s, t, dn);
+  else if (nn == 6) dshape_wedge6(r, s, t, dn);
+  else if (nn == 15) dshape_wedge15(r, s, t, dn);
+  else dshape_tet4(dn);
+}
 
 namespace {
 
@@ -115,6 +159,12 @@ HostTables make_tables(int nn, int ng) {
   } else if (nn == 10) {
     const double w = 1.0 / 24.0;  // quadratic.rs:613-614
     pts = {kTetB, kTetB, kTetB, w, kTetA, kTetB, kTetB, w, kTetB, kTetA, kTetB, w, kTetB, kTetB, kTetA, w};
+  } else if (nn == 6) {  // extra.rs:114-121: triangle points x zeta = -G2, +G2, weight 1/6
+    for (const auto& tp : kTri)
+      for (double z : {-kG2, kG2}) pts.insert(pts.end(), {tp[0], tp[1], z, 1.0 / 6.0});
+  } else if (nn == 15) {  // extra.rs:783-797: triangle points x 3-point Gauss in zeta
+    for (const auto& tp : kTri)
+      for (int k = 0; k < 3; ++k) pts.insert(pts.end(), {tp[0], tp[1], kG3[k], (1.0 / 6.0) * kW3[k]});
   } else if (ng == 8) {
     const double g[2] = {-kG2, kG2};
     for (double a : g)
@@ -132,10 +182,8 @@ HostTables make_tables(int nn, int ng) {
       dshape_hex8(pts[4 * g], pts[4 * g + 1], pts[4 * g + 2], &t.dn[(size_t)g * nn * 3]);
     else if (nn == 20)
       dshape_hex20(pts[4 * g], pts[4 * g + 1], pts[4 * g + 2], &t.dn[(size_t)g * nn * 3]);
-    else if (nn == 10)
-      dshape_tet10(pts[4 * g], pts[4 * g + 1], pts[4 * g + 2], &t.dn[(size_t)g * nn * 3]);
     else
-      dshape_tet4(&t.dn[(size_t)g * nn * 3]);
+      element_dshape(nn, pts[4 * g], pts[4 * g + 1], pts[4 * g + 2], &t.dn[(size_t)g * nn * 3]);
     t.w[g] = pts[4 * g + 3];
   }
   // entries of blocks a <= b; diagonal blocks keep i <= j
@@ -169,13 +217,16 @@ struct DevTables {
   int* blk = nullptr;
 };
 
-DevTables g_tab[6];  // hex8, hex20 (27 gp), hex20r (8 gp), tet4, tet10, hex8r (1 gp) -- by device id
-int g_tab_device[6] = {-1, -1, -1, -1, -1, -1};
+// hex8, hex20 (27 gp), hex20r (8 gp), tet4, tet10, hex8r (1 gp), wedge6, wedge15 -- by device id
+DevTables g_tab[8];
+int g_tab_device[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
 
 int table_index(int nn, int ng) {
   if (nn == 8 && ng == 1) return 5;
   if (nn == 4) return 3;
   if (nn == 10) return 4;
+  if (nn == 6) return 6;
+  if (nn == 15) return 7;
   return nn == 8 ? 0 : (ng == 27 ? 1 : 2);
 }
 
@@ -257,7 +308,9 @@ int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args) {
   if (nn == 20 && reduced) return launch_element_ke<20, 8, 4>(ctx, args);
   if (nn == 4) return launch_element_ke<4, 1, 8>(ctx, args);
   if (nn == 10) return launch_element_ke<10, 4, 8>(ctx, args);
-  return set_error(ctx, AXIA_ERR_INVALID_ARG, "nn must be 4, 8, 10 or 20");
+  if (nn == 6) return launch_element_ke<6, 6, 8>(ctx, args);
+  if (nn == 15) return launch_element_ke<15, 9, 4>(ctx, args);
+  return set_error(ctx, AXIA_ERR_INVALID_ARG, "nn must be 4, 6, 8, 10, 15 or 20");
 }
 
 // ---------------------------------------------------------------------------

@@ -231,8 +231,14 @@ element_ke_kernel(ElemArgs args, ElemTables tab) {
     }
     fence_async_smem();
     __syncwarp();
-    // 8. bulk store of the finished Ke
-    if (lane == 0) bulk_store_s2g(args.ke_out + e * T::KE, KEs, (unsigned)(T::KE * sizeof(double)));
+    // 8. bulk store of the finished Ke; a bulk copy needs 16-byte aligned ends, which
+    // an odd Ke size (C3D15: 45 x 45 doubles) does not give every element, so that
+    // one is stored by the warp
+    if constexpr (T::KE % 2 == 0) {
+      if (lane == 0) bulk_store_s2g(args.ke_out + e * T::KE, KEs, (unsigned)(T::KE * sizeof(double)));
+    } else {
+      for (int k = lane; k < T::KE; k += 32) args.ke_out[e * T::KE + k] = KEs[k];
+    }
     __syncwarp();
   }
   if (lane == 0) bulk_wait_all();

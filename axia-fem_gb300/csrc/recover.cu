@@ -1,7 +1,7 @@
 // recover.cu -- nodal stress recovery and reactions after a solve.
 //
-// Replaces, for C3D8 / C3D20 / C3D20R / C3D4 / C3D10 with an isotropic
-// material, the post-solve loops of the reference's solve_linear:
+// Replaces, for C3D8 / C3D8R / C3D8I / C3D20 / C3D20R / C3D4 / C3D10 / C3D6 / C3D15
+// with an isotropic material, the post-solve loops of the reference's solve_linear:
 //   reactions      solver/src/analysis.rs:1027-1035   ku = sum of element K u, rf = ku - f
 //   nodal stresses solver/src/analysis.rs:1061-1153   element nodal stresses summed per
 //                                                     node in element order / element count
@@ -11,7 +11,9 @@
 //                  hex20_extrapolate quadratic.rs:148-225 (hex_gauss points, tensor-product
 //                  Lagrange extrapolation, lagrange1d quadratic.rs:227-244)
 //                  tet4_nodal_stress elem.rs:781-795 (one constant stress), tet10_nodal_stress
-//                  quadratic.rs:678-702 (stress evaluated at the ten nodes)
+//                  quadratic.rs:678-702 (stress evaluated at the ten nodes);
+//                  wedge6_nodal_stress / wedge15_nodal_stress extra.rs:134-153, 821-850
+//                  (stress evaluated at the nodes)
 //   element mean   "stress_gp" analysis.rs:1141-1152 (mean of the element's nodal stresses)
 //
 // Two kernels.  element_recover_kernel: lanes are (element, Gauss point)
@@ -32,7 +34,7 @@
 #include "solver.cuh"
 
 int element_tables_for(axia_ctx* ctx, int nn, int ng, const double** dn, const double** w);
-void tet10_dshape(double r, double s, double t, double* dn);
+void element_dshape(int nn, double r, double s, double t, double* dn);
 
 namespace {
 
@@ -322,42 +324,64 @@ struct XTab {
   int* perm = nullptr;
   int device = -1;
 };
-XTab g_xtab[6];  // hex8, hex20, hex20r, tet4, tet10, hex8r
+XTab g_xtab[8];  // hex8, hex20, hex20r, tet4, tet10, hex8r, wedge6, wedge15
 
 // The points the recovery kernel evaluates and how nodes take their stress:
 //  * hexahedra: the stiffness Gauss points, extrapolated to the nodes (X above);
 //  * C3D4: its one point (constant stress, elem.rs:781-795), every node takes it;
-//  * C3D10: the 4 Gauss points (weights 1/24, for the internal forces) and the
-//    10 nodes themselves (weight 0; tet10_nodal_stress evaluates the stress at
-//    the nodes, quadratic.rs:678-702), node a taking point 4 + a.
+//  * C3D10, C3D6, C3D15: the stiffness Gauss points (for the internal forces)
+//    followed by the nodes themselves (weight 0), node a taking point NG + a:
+//    tet10_nodal_stress (quadratic.rs:678-702), wedge6_nodal_stress
+//    (extra.rs:134-153) and wedge15_nodal_stress (extra.rs:821-850) evaluate the
+//    stress at the nodes.
 struct RecTables {
   const double* dn;
   const double* w;
   const double* x;
   const int* perm;
 };
-struct TetRecTab {
+struct NodeRecTab {
   double* dn = nullptr;
   double* w = nullptr;
   int device = -1;
 };
-TetRecTab g_tet10_rec;
+NodeRecTab g_node_rec[3];  // tet10, wedge6, wedge15
+
+// stiffness Gauss points of the element kinds whose stress is evaluated at the nodes
+int node_eval_gauss(int nn) { return nn == 10 ? 4 : nn == 6 ? 6 : 9; }
+
+// parametric positions of the nodes (tet10: quadratic.rs:680-691; wedges: extra.rs:137-144, 824-840)
+std::vector<double> node_points(int nn) {
+  if (nn == 10)
+    return {0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1, 0.5, 0, 0, 0.5, 0.5, 0, 0, 0.5, 0, 0, 0, 0.5, 0.5, 0, 0.5, 0, 0.5, 0.5};
+  std::vector<double> p = {1, 0, -1, 0, 1, -1, 0, 0, -1, 1, 0, 1, 0, 1, 1, 0, 0, 1};
+  if (nn == 15) {
+    const std::vector<double> mid = {0.5, 0.5, -1, 0, 0.5, -1, 0.5, 0, -1, 0.5, 0.5, 1, 0, 0.5, 1,
+                                     0.5, 0,   1,  1, 0,   0,  0,   1, 0,  0,   0,   0};
+    p.insert(p.end(), mid.begin(), mid.end());
+  }
+  return p;
+}
+
+int node_eval_index(int nn) { return nn == 10 ? 0 : nn == 6 ? 1 : 2; }
 
 int ensure_xtab(axia_ctx* ctx, const double** x, const int** perm) {
-  const int ti = ctx->nn == 4 ? 3 : ctx->nn == 10 ? 4 : (ctx->nn == 8 && ctx->ngp == 1) ? 5 : ctx->nn == 8 ? 0
-                                                                                          : (ctx->ngp == 27 ? 1 : 2);
+  const int nn = ctx->nn;
+  const int ti = nn == 4 ? 3 : nn == 10 ? 4 : nn == 6 ? 6 : nn == 15 ? 7 : (nn == 8 && ctx->ngp == 1) ? 5
+               : nn == 8 ? 0 : (ctx->ngp == 27 ? 1 : 2);
   XTab& t = g_xtab[ti];
   if (t.device != ctx->device) {
     std::vector<double> hx;
     std::vector<int> hp;
-    if (ctx->nn == 4 || (ctx->nn == 8 && ctx->ngp == 1)) {  // one point, every node takes its stress
-      hx.assign(ctx->nn, 1.0);
+    if (nn == 4 || (nn == 8 && ctx->ngp == 1)) {  // one point, every node takes its stress
+      hx.assign(nn, 1.0);
       hp.assign(1, 0);
-    } else if (ctx->nn == 10) {
-      hx.assign(10 * 14, 0.0);
-      for (int a = 0; a < 10; ++a) hx[a * 14 + 4 + a] = 1.0;
-      hp.resize(14);
-      for (int m = 0; m < 14; ++m) hp[m] = m;
+    } else if (nn == 10 || nn == 6 || nn == 15) {
+      const int ng = node_eval_gauss(nn), np = ng + nn;
+      hx.assign((size_t)nn * np, 0.0);
+      for (int a = 0; a < nn; ++a) hx[(size_t)a * np + ng + a] = 1.0;
+      hp.resize(np);
+      for (int m = 0; m < np; ++m) hp[m] = m;
     } else {
       extrapolation_table(ctx->nn, ctx->ngp, hx, hp);
     }
@@ -374,16 +398,20 @@ int ensure_xtab(axia_ctx* ctx, const double** x, const int** perm) {
 
 int recover_tables(axia_ctx* ctx, RecTables* r) {
   AXIA_TRY(ensure_xtab(ctx, &r->x, &r->perm));
-  if (ctx->nn != 10) return element_tables_for(ctx, ctx->nn, ctx->ngp, &r->dn, &r->w);
-  TetRecTab& t = g_tet10_rec;
+  const int nn = ctx->nn;
+  if (nn != 10 && nn != 6 && nn != 15) return element_tables_for(ctx, nn, ctx->ngp, &r->dn, &r->w);
+  NodeRecTab& t = g_node_rec[node_eval_index(nn)];
   if (t.device != ctx->device) {
-    const double a = 0.5854101966249685, b = 0.1381966011250105;  // quadratic.rs:611-612
-    const double pts[14][3] = {{b, b, b}, {a, b, b}, {b, a, b}, {b, b, a},
-                               {0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0.5, 0, 0},
-                               {0.5, 0.5, 0}, {0, 0.5, 0}, {0, 0, 0.5}, {0.5, 0, 0.5}, {0, 0.5, 0.5}};
-    std::vector<double> dn(14 * 30), w(14, 0.0);
-    for (int m = 0; m < 14; ++m) tet10_dshape(pts[m][0], pts[m][1], pts[m][2], &dn[m * 30]);
-    for (int m = 0; m < 4; ++m) w[m] = 1.0 / 24.0;
+    // the stiffness points and weights first, then the nodes with weight 0
+    const double *gdn = nullptr, *gw = nullptr;
+    const int ng = node_eval_gauss(nn), np = ng + nn;
+    AXIA_TRY(element_tables_for(ctx, nn, ng, &gdn, &gw));
+    std::vector<double> dn((size_t)np * nn * 3), w(np, 0.0);
+    AXIA_CUDA(ctx, cudaMemcpy(dn.data(), gdn, (size_t)ng * nn * 3 * sizeof(double), cudaMemcpyDeviceToHost));
+    AXIA_CUDA(ctx, cudaMemcpy(w.data(), gw, (size_t)ng * sizeof(double), cudaMemcpyDeviceToHost));
+    const std::vector<double> pts = node_points(nn);
+    for (int a = 0; a < nn; ++a)
+      element_dshape(nn, pts[3 * a], pts[3 * a + 1], pts[3 * a + 2], &dn[(size_t)(ng + a) * nn * 3]);
     AXIA_CUDA(ctx, cudaMalloc(&t.dn, dn.size() * sizeof(double)));
     AXIA_CUDA(ctx, cudaMalloc(&t.w, w.size() * sizeof(double)));
     AXIA_CUDA(ctx, cudaMemcpy(t.dn, dn.data(), dn.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -429,6 +457,10 @@ int recover_device(axia_ctx* ctx, const double* d_u, const double* d_f, double e
     launch_element_recover<4, 1>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
   else if (ctx->nn == 10)
     launch_element_recover<10, 14>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
+  else if (ctx->nn == 6)
+    launch_element_recover<6, 12>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
+  else if (ctx->nn == 15)
+    launch_element_recover<15, 24>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
   else if (ctx->ngp == 27)
     launch_element_recover<20, 27>(ctx, d_u, t.dn, t.w, t.x, t.perm, d_emean);
   else

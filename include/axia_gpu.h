@@ -87,7 +87,8 @@ typedef struct axia_mesh {
   int64_t n_nodes;
   const double* coords;    /* [n_nodes][3] */
   int64_t n_elem;
-  int32_t nn;              /* nodes per element: 8 (C3D8), 20 (C3D20), 4 (C3D4) or 10 (C3D10) */
+  int32_t nn;              /* nodes per element: 8 (C3D8), 20 (C3D20), 4 (C3D4), 10 (C3D10),
+                              6 (C3D6) or 15 (C3D15) */
   int32_t reduced;         /* nn = 20: 1 = C3D20R, 2x2x2 Gauss points (quadratic.rs:100-120);
                               nn = 8: 1 = C3D8R (extra.rs:400-457), 2 = C3D8I (extra.rs:256-388) */
   const int32_t* conn;     /* [n_elem][nn], 0-based node indices, CalculiX node order */
@@ -139,10 +140,12 @@ AXIA_API void axia_gpu_destroy(axia_ctx* ctx);
 AXIA_API const char* axia_gpu_last_error(const axia_ctx* ctx);
 
 /* Batched element_ke (solver/src/elem.rs:344-375 Hex8 / Hex8R / Hex8I /
- * Tet4 arms, :487-495 Hex20 arm, :496 Tet10 arm; hex8_stiffness
- * elem.rs:194-219, hex20_stiffness quadratic.rs:122-146, tet4_stiffness
- * elem.rs:221-248, tet10_stiffness quadratic.rs:607-627, hex8r / hex8i
- * extra.rs:256-457): for n_elem elements with nn (4, 8, 10, 20) nodes each,
+ * Tet4 arms, :394-411 Wedge6 / Wedge15 arms, :487-495 Hex20 arm, :496 Tet10
+ * arm; hex8_stiffness elem.rs:194-219, hex20_stiffness quadratic.rs:122-146,
+ * tet4_stiffness elem.rs:221-248, tet10_stiffness quadratic.rs:607-627,
+ * hex8r / hex8i extra.rs:256-457, wedge6_stiffness extra.rs:109-132,
+ * wedge15_stiffness extra.rs:799-819): for n_elem elements with nn
+ * (4, 6, 8, 10, 15, 20) nodes each,
  * xyz[n_elem][nn][3] -> ke[n_elem][3nn][3nn] row-major (DOF order
  * node-major, x y z) and vol[n_elem]; `reduced` as in axia_mesh.
  * e[n_elem] per element.  On an element error *bad_elem holds its index. */
@@ -169,8 +172,12 @@ AXIA_API int32_t axia_gpu_element_ke_noalloc(int32_t nn, int32_t reduced, int64_
 
 /* Consistent nodal forces of face pressures added into f_full[3*n_nodes], in
  * list order, on the host (apply_pressure solver/src/analysis.rs:1365-1396 ->
- * hex8_face_pressure elem.rs:891-950 / hex20_face_pressure quadratic.rs:275-315).
- * face is 1..6 (P1..P6); positive pressure compresses. */
+ * hex8_face_pressure elem.rs:891-950 / hex20_face_pressure quadratic.rs:275-315
+ * / wedge6_face_pressure extra.rs:184-195 / wedge15_face_pressure
+ * extra.rs:869-880).  face is 1..6 (P1..P6; wedges 1..5); positive pressure
+ * compresses, except on the wedges' triangles P1 / P2, whose node lists wind
+ * the other way (kept as in the reference).  Tetrahedra take no pressure
+ * (apply_pressure has no arm for them). */
 AXIA_API int32_t axia_face_loads(int32_t nn, int64_t n_nodes, const double* coords, const int32_t* conn,
                         int64_t n_loads, const int64_t* elem, const int32_t* face,
                         const double* p, double* f_full, int64_t* bad_load);

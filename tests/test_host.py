@@ -39,7 +39,9 @@ def test_struct_layouts_match_header():
 
 
 @pytest.mark.parametrize("model", [meshgen.block_c3d8_pressure(n=5), meshgen.block_c3d20_traction(n=3),
-                                   meshgen.patch_c3d20()])
+                                   meshgen.patch_c3d20(), meshgen.block_wedge(n=3, nn=6, perturb=0.2),
+                                   meshgen.block_wedge(n=2, nn=15, perturb=0.2)],
+                         ids=["c3d8", "c3d20", "patch20", "c3d6", "c3d15"])
 def test_face_loads_match_oracle(model):
     lib = _lib.load()
     f = np.array(model.cload, dtype=np.float64, copy=True)
@@ -54,6 +56,21 @@ def test_face_loads_match_oracle(model):
     assert st == 0
     ref = O.load_vector(model)
     assert np.abs(f - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max())
+    if model.nn in (6, 15):
+        # every face of a wedge (extra.rs:184-195, 869-880), bit for bit
+        for face in range(1, 6):
+            mm = meshgen.block_wedge(n=2, nn=model.nn, perturb=0.2)
+            mm.dload_elem = np.arange(mm.conn.shape[0], dtype=np.int64)
+            mm.dload_face = np.full(mm.conn.shape[0], face, np.int32)
+            mm.dload_p = np.linspace(-3.0, 7.0, mm.conn.shape[0])
+            g = np.zeros(3 * mm.n_nodes)
+            el = np.ascontiguousarray(mm.dload_elem)
+            st = lib.axia_face_loads(mm.nn, mm.n_nodes, np.ascontiguousarray(mm.coords).ctypes.data,
+                                     np.ascontiguousarray(mm.conn, np.int32).ctypes.data, el.shape[0],
+                                     el.ctypes.data, mm.dload_face.ctypes.data, mm.dload_p.ctypes.data,
+                                     g.ctypes.data, ctypes.byref(bad))
+            assert st == 0
+            np.testing.assert_array_equal(g, O.load_vector(mm))
 
 
 def test_face_loads_reject_bad_face():

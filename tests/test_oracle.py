@@ -224,3 +224,55 @@ def test_hex8_variants_rigid_modes_and_patch(variant):
     assert abs(_mean_ux(r.u, pin["nodes_1based"]) - pin["value"]) < pin["tol"]
     s, _ = O.nodal_stress(m, r.u)
     assert abs(s[:, 0].mean() - 210.0) < 1e-3
+
+
+def _wedge_patch(nn):
+    """2x2x2 block of wedges stretched by u_x = 0.01 on x = 2 (rigid modes removed)."""
+    m = meshgen.block_wedge(n=2, nn=nn)
+    lat = np.round(m.coords * 2).astype(int)
+    x0 = np.nonzero(lat[:, 0] == 0)[0]
+    x1 = np.nonzero(lat[:, 0] == 4)[0]
+    o = x0[np.argmin(np.abs(m.coords[x0]).sum(1))]
+    yax = x0[np.argmax(m.coords[x0, 1] - 10 * np.abs(m.coords[x0, 2]))]
+    zax = x0[np.argmax(m.coords[x0, 2] - 10 * np.abs(m.coords[x0, 1]))]
+    bc = list(3 * x0) + [3 * o + 1, 3 * o + 2, 3 * yax + 2, 3 * zax + 1]
+    vals = [0.0] * len(bc) + [0.01] * len(x1)
+    bc += list(3 * x1)
+    m.bc_dof = np.array(bc, np.int64)
+    m.bc_val = np.array(vals)
+    m.dload_elem = np.zeros(0, np.int64)
+    m.dload_face = np.zeros(0, np.int32)
+    m.dload_p = np.zeros(0)
+    return m
+
+
+@pytest.mark.parametrize("nn", [6, 15], ids=["C3D6", "C3D15"])
+def test_wedges_patch_and_rigid_modes(nn):
+    """C3D6 / C3D15 (extra.rs:84-182, 701-820): six rigid-body modes per element, the
+    volume of a unit half-cube, and a uniform-strain patch reproduced (sxx = E * 0.01 / 2)."""
+    m = _wedge_patch(nn)
+    ke, vol = O.element_ke(m.coords[m.conn[0]], 210000.0, 0.3)
+    w = np.linalg.eigvalsh(ke)
+    assert (np.abs(w) < 1e-8 * w.max()).sum() == 6
+    assert abs(vol - 0.5) < 1e-14
+    r = O.solve_static(m, solver=O.SOLVER_CHOLESKY)
+    s, _ = O.nodal_stress(m, r.u)
+    np.testing.assert_allclose(s[:, 0], 1050.0, rtol=1e-9)
+    np.testing.assert_allclose(s[:, 1:], 0.0, atol=1e-7)
+
+
+@pytest.mark.parametrize("nn", [6, 15], ids=["C3D6", "C3D15"])
+def test_wedge_face_pressure_resultant(nn):
+    """Resultant of a uniform pressure p = 2 on each face of the unit wedge with corners
+    (1,0), (1,1), (0,0).  The quadrilaterals P3..P5 push inward (-p * outward area);
+    the triangle lists of extra.rs:187-188 wind against the positive-Jacobian corner
+    order, so on P1 / P2 a positive p pulls outward -- the oracle and the host face
+    loads keep that as it is."""
+    m = meshgen.block_wedge(n=1, nn=nn)
+    xyz = m.coords[m.conn[0]]
+    expect = {1: [0, 0, -0.5], 2: [0, 0, 0.5], 3: [-1.0, 0, 0], 4: [1.0, -1.0, 0], 5: [0, 1.0, 0]}
+    for face, vec in expect.items():
+        fe = O.face_pressure(xyz, face, 2.0).reshape(-1, 3).sum(0)
+        np.testing.assert_allclose(fe, 2.0 * np.array(vec), atol=1e-13)
+    with pytest.raises(O.OracleError):
+        O.face_pressure(xyz, 6, 1.0)
