@@ -45,6 +45,8 @@ ASM_BSR64 = 4
 ASM_BSR32 = 8
 FORMAT_CSR = 0
 FORMAT_BSR3 = 1
+PRECOND_JACOBI = 0
+PRECOND_COARSE = 1
 
 
 class Mesh(C.Structure):
@@ -56,7 +58,8 @@ class Mesh(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iter", C.c_int64), ("precision", C.c_int32),
                 ("refine_mode", C.c_int32), ("inner_rtol", C.c_double), ("max_outer", C.c_int32),
-                ("spmv_lanes", C.c_int32), ("matrix_format", C.c_int32), ("spmv_vec", C.c_int32)]
+                ("spmv_lanes", C.c_int32), ("matrix_format", C.c_int32), ("spmv_vec", C.c_int32),
+                ("preconditioner", C.c_int32), ("coarse_nodes", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -91,6 +94,7 @@ SIGNATURES = [
     ("axia_gpu_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32]),
     ("axia_gpu_bsr_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32, C.c_int32]),
     ("axia_gpu_node_blocks", C.c_int64, [_P]),
+    ("axia_gpu_coarse_size", C.c_int32, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("axia_gpu_setup_multi", C.c_int32, [_P, C.c_int32, C.POINTER(Mesh), _P, _P, _P]),
     ("axia_gpu_solve_multi", C.c_int32, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), _P, _P]),
     ("axia_gpu_solve_multi_device", C.c_int32, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), _P, _P]),

@@ -162,9 +162,10 @@ class GpuContext:
 
     @staticmethod
     def opts(rtol=1e-8, max_iter=0, precision=L.PREC_FP64, refine_mode=L.REFINE_RESTART, inner_rtol=1e-3,
-             max_outer=50, spmv_lanes=0, matrix_format=L.FORMAT_CSR, spmv_vec=0):
+             max_outer=50, spmv_lanes=0, matrix_format=L.FORMAT_CSR, spmv_vec=0, preconditioner=0,
+             coarse_nodes=0):
         return L.SolveOpts(rtol, max_iter, precision, refine_mode, inner_rtol, max_outer, spmv_lanes,
-                           matrix_format, spmv_vec)
+                           matrix_format, spmv_vec, preconditioner, coarse_nodes)
 
     def set_stream(self, stream_handle: int | None):
         """Issue the context's work on a caller's cudaStream_t (None: own stream)."""
@@ -173,6 +174,12 @@ class GpuContext:
     def n_blocks(self) -> int:
         """3x3 node blocks of the node-block form."""
         return int(self.lib.axia_gpu_node_blocks(self.h))
+
+    def coarse_size(self):
+        """(subdomains, coarse unknowns) of the last two-level solve."""
+        ns, nc = C.c_int64(0), C.c_int64(0)
+        self._check(self.lib.axia_gpu_coarse_size(self.h, C.byref(ns), C.byref(nc)), "coarse_size")
+        return int(ns.value), int(nc.value)
 
     def kernel_launches(self) -> int:
         return int(self.lib.axia_gpu_kernel_launches(self.h))

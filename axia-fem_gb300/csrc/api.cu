@@ -59,6 +59,7 @@ struct EventTimer {
 
 void free_mesh_state(axia_ctx* ctx) {
   multimesh_release(ctx);
+  coarse_release(ctx);
   ctx->h_ind_of.clear();
   ctx->mesh_node0.clear();
   ctx->mesh_blocks.clear();
@@ -354,6 +355,10 @@ static int32_t solve_common(axia_ctx* ctx, const double* d_f, double* d_u, const
     o.precision = AXIA_PREC_FP64;
   }
   if (!(o.rtol > 0.0)) o.rtol = 1e-8;
+  if (o.preconditioner != AXIA_PRECOND_JACOBI &&
+      (o.preconditioner != AXIA_PRECOND_COARSE || o.matrix_format != AXIA_FORMAT_BSR3 ||
+       o.precision != AXIA_PREC_MIXED))
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "the coarse preconditioner needs the mixed node-block solve");
   EventTimer t(ctx->stream);
   int st = AXIA_OK;
   if (ctx->n_free > 0 && o.matrix_format == AXIA_FORMAT_BSR3) {
@@ -414,8 +419,9 @@ static int32_t solve_raw(axia_ctx* ctx, const double* rhs, const double* d_rhs, 
   axia_solve_opts o{};
   if (opts) o = *opts;
   if (!(o.rtol > 0.0)) o.rtol = 1e-8;  // solve_kff's PCG tolerance (linalg.rs:363)
-  if (o.matrix_format != AXIA_FORMAT_CSR)
-    return set_error(ctx, AXIA_ERR_INVALID_ARG, "solve_kff: caller systems are CSR; node blocks need a mesh");
+  if (o.matrix_format != AXIA_FORMAT_CSR || o.preconditioner != AXIA_PRECOND_JACOBI)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG,
+                     "solve_kff: caller systems are CSR with Jacobi; node blocks and the coarse space need a mesh");
   const bool mixed = o.precision == AXIA_PREC_MIXED;
   EventTimer t(ctx->stream);
   int st = ensure_pcg_state(ctx);

@@ -897,5 +897,6 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   ctx->have_bsr64 = bsr64;
   ctx->have_bsr32 = bsr32;
   ctx->assembled = true;
+  ctx->assemble_gen++;
   return AXIA_OK;
 }

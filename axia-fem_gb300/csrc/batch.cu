@@ -490,6 +490,8 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
     AXIA_TRY(dev_alloc(ctx, &o, 1));
     ctx->d_mout = o;
   }
+  if (opts->preconditioner != AXIA_PRECOND_JACOBI)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "batched load cases: Jacobi preconditioner only");
   const long long max_iter = opts->max_iter > 0 ? opts->max_iter : std::max<long long>(4LL * ctx->n_free, 200);
   const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.01;
   auto kern = pcg_bsr_multi_kernel;

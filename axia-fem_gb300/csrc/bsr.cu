@@ -29,7 +29,7 @@
 #include <vector>
 #include <cmath>
 
-#include "solver.cuh"
+#include "coarse.cuh"
 
 // Vector loads of VEC consecutive entries (streaming: the matrix is read once per use).
 template <typename V, int VEC>
@@ -253,7 +253,21 @@ struct SolveRange {
   PcgOut* out;
 };
 
-template <int L32, int V32, int L64, int V64>
+// The coarse part of the two-level preconditioner for the current r32:
+// restriction, grid barrier, y = M r_c, and r_c . y reduced over the group.
+__device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const SolveRange& R, int gwarp, int nwarps,
+                                            int lane, float* rz_c) {
+  __shared__ __align__(16) float s_rc[COARSE_MAX];
+  coarse_restrict(P.C, P.r32, gwarp, nwarps, lane);
+  if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return false;
+  const float acc = coarse_solve(P.C, s_rc, gwarp, nwarps, lane);
+  block_partials<float>(acc, 0.f, 1, R.partials, S_RC, S_RC, R.nblk, R.rank);
+  if (!group_reduce_sync(R.bar, P.st, P.limit_ns, R.partials, R.totals, S_RC, 1, R.nblk)) return false;
+  *rz_c = (float)total(R.totals, S_RC);
+  return true;
+}
+
+template <int L32, int V32, int L64, int V64, bool COARSE = false>
 __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const SolveRange& R) {
   const int n0 = R.node0, n1 = R.node1;
   const int i0 = 3 * n0;
@@ -289,6 +303,15 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
   int updates = 0, status = AXIA_OK;
   bool converged = bnorm < 1e-30;
   if (converged) residual = 0.0;
+  if constexpr (COARSE) {
+    if (!converged) {  // p = D^-1 b + Z M Z^T b
+      float rz_c = 0.f;
+      if (!coarse_step(P, R, gwarp, nwarps, lane, &rz_c)) return;
+      rz += rz_c;
+      coarse_update_p(P.C, n0, n1, tid, nth, 0.f, P.r32, P.dinv32, P.p32, true);
+      if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
+    }
+  }
   for (long long it = 0; !converged && it < P.max_iter; ++it) {
     iters = it + 1;
     float pq_p = 0.f;
@@ -376,9 +399,17 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
         break;
       }
     }
+    if constexpr (COARSE) {
+      float rz_c = 0.f;
+      if (!coarse_step(P, R, gwarp, nwarps, lane, &rz_c)) return;
+      rzn += rz_c;
+    }
     const float beta = rzn / rz;
     rz = rzn;
-    for (int i = i0 + tid; i < nd; i += nth) P.p32[i] = fmaf(beta, P.p32[i], P.r32[i] * P.dinv32[i]);
+    if constexpr (COARSE)
+      coarse_update_p(P.C, n0, n1, tid, nth, beta, P.r32, P.dinv32, P.p32, false);
+    else
+      for (int i = i0 + tid; i < nd; i += nth) P.p32[i] = fmaf(beta, P.p32[i], P.r32[i] * P.dinv32[i]);
     if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
   }
   if (status == AXIA_OK && residual > P.tol * bnorm * 10.0) status = AXIA_ERR_NOT_CONVERGED;
@@ -401,10 +432,10 @@ __host__ __device__ constexpr int rel_v64() { return V32 >= 4 ? 2 : 1; }
 template <int V32>
 __host__ __device__ constexpr int rel_min_blocks() { return V32 >= 4 ? 2 : 3; }
 
-template <int L32, int V32>
+template <int L32, int V32, bool COARSE = false>
 __global__ void __launch_bounds__(PCG_THREADS, rel_min_blocks<V32>()) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
   const SolveRange R{0, P.M32.n_nodes, blockIdx.x, gridDim.x, P.partials, P.totals, P.bar, P.out};
-  reliable_body<L32, V32, kL64, rel_v64<V32>()>(P, R);
+  reliable_body<L32, V32, kL64, rel_v64<V32>(), COARSE>(P, R);
 }
 
 // Independent systems on disjoint node ranges of one node-block matrix (the
@@ -563,9 +594,9 @@ static int launch_bsr_pcg(axia_ctx* ctx, BsrPcgArgs<V>& P, int lanes) {
   }
 }
 
-template <int L32, int V32>
+template <int L32, int V32, bool COARSE>
 static int launch_bsr_rel_t(axia_ctx* ctx, BsrReliableArgs& P) {
-  auto kern = pcg_bsr_reliable_kernel<L32, V32>;
+  auto kern = pcg_bsr_reliable_kernel<L32, V32, COARSE>;
   int grid = 0;
   AXIA_TRY(coop_grid(ctx, (const void*)kern, P.nd, &grid));
   void* params[] = {&P};
@@ -575,7 +606,11 @@ static int launch_bsr_rel_t(axia_ctx* ctx, BsrReliableArgs& P) {
 }
 
 static int launch_bsr_rel(axia_ctx* ctx, BsrReliableArgs& P, RowLayout r) {
-  return with_layout(r, [&](auto l, auto v) { return launch_bsr_rel_t<decltype(l)::value, decltype(v)::value>(ctx, P); });
+  if (P.C.n_sub > 0)
+    return with_layout(
+        r, [&](auto l, auto v) { return launch_bsr_rel_t<decltype(l)::value, decltype(v)::value, true>(ctx, P); });
+  return with_layout(
+      r, [&](auto l, auto v) { return launch_bsr_rel_t<decltype(l)::value, decltype(v)::value, false>(ctx, P); });
 }
 
 // Occupancy of the group kernel (blocks per SM) for the grid size of a multi-mesh solve.
@@ -658,6 +693,8 @@ int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_op
   const bool mixed = opts->precision == AXIA_PREC_MIXED;
   if (!ctx->have_bsr64 || (mixed && !ctx->have_bsr32))
     return set_error(ctx, AXIA_ERR_STATE, "node-block solve needs axia_gpu_assemble_ex with the BSR flags");
+  if (opts->preconditioner != AXIA_PRECOND_JACOBI && (opts->preconditioner != AXIA_PRECOND_COARSE || !mixed))
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "the coarse preconditioner needs the mixed node-block solve");
   AXIA_TRY(ensure_full_buffers(ctx, mixed));
   AXIA_TRY(reset_dev_status(ctx));
   const int64_t nd = ctx->ndof;
@@ -681,6 +718,11 @@ int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_op
                       ctx->d_bdinv32, ctx->d_bf, ctx->d_xf, ctx->d_xf32, ctx->d_rf32, ctx->d_pf32, ctx->d_qf32,
                       ctx->d_zf32, ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out, opts->rtol,
                       delta, max_iter, limit_ns};
+    if (opts->preconditioner == AXIA_PRECOND_COARSE) {
+      AXIA_TRY(coarse_prepare(ctx, opts->coarse_nodes, &P.C));
+      AXIA_TRY(reset_dev_status(ctx));
+      AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
+    }
     AXIA_TRY(timed_launch(ctx, info, [&] { return launch_bsr_rel(ctx, P, lay); }));
   }
   AXIA_TRY(read_out(ctx, &o));

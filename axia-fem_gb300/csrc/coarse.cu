@@ -1,0 +1,986 @@
+// coarse.cu -- setup of the coarse space of the two-level preconditioner
+// (the per-iteration phases are in coarse.cuh).
+//
+// No reference counterpart: the reference preconditions its CG with the
+// diagonal only (solver/src/linalg.rs:199-259).
+//
+// Space (once per mesh and constraint set):
+//   * bounding box -> a uniform grid of at most COARSE_MAX / 6 boxes of about
+//     `nodes_target` nodes each; every non-empty box is a subdomain;
+//   * the nodes sorted by subdomain (stable radix sort: ascending node order
+//     inside each subdomain), cut into chunks of COARSE_CHUNK nodes;
+//   * centre c_I, and per node (x_a - c_I) / h and its free-DOF mask (geo);
+//   * per subdomain the Gram matrix G = Z_I^T Z_I over the free DOFs and
+//     T = L^-T from its Cholesky factor, modes whose pivot vanishes dropped
+//     (a subdomain with few free nodes has dependent rigid-body modes).
+// Operator (after every assembly, from the FP64 node-block matrix):
+//   * every node row a that is not interior to its subdomain: for each
+//     subdomain J its blocks reach, Z_a^T sum_{b in row a, b in J} K_ab Z_b
+//     (6 x 6, FP64); rows are split into items keyed (I(a), J), written in
+//     row order;
+//   * a stable radix sort by key, then every run summed in item order gives
+//     S_IJ = Z_I^T K Z_J; A_IJ = T_I^T S_IJ T_J goes into a dense FP64 matrix;
+//   * A scaled to unit diagonal, rounded to FP32 and inverted in place by a
+//     symmetric blocked Gauss-Jordan elimination (64 x 64 tiles, one
+//     cooperative launch, three bounded grid barriers per tile step);
+//   * M = T diag(s) A^-1 diag(s) T^T per subdomain pair, in FP32.
+// Every sum has a fixed order: the same inputs give the same bits.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include <cub/cub.cuh>
+
+#include "coarse.cuh"
+
+namespace {
+
+constexpr int GJ_T = 64;          // Gauss-Jordan tile
+constexpr int GJ_THREADS = 256;   // 16 x 16 threads, 4 x 4 outputs each
+constexpr int ROW_SLOTS = 8;      // subdomains accumulated per pass over a node row
+
+struct CoarseState {
+  int nodes_target = 0;
+  int64_t op_gen = -1;           // assembly the operator was built from
+  CoarseArgs args{};
+  double h = 0.0;
+  int* sub_node = nullptr;
+  int4* chunk = nullptr;
+  int* chunk_ptr = nullptr;
+  float4* geo = nullptr;
+  int* sub_ptr = nullptr;        // [n_sub + 1]
+  double* tmat = nullptr;        // [n_sub][6][6]
+  float* minv = nullptr;         // [nc][ncp]
+  float* part = nullptr;         // [n_chunks][6]
+  float* yc = nullptr;           // [ncp]
+  void release() {
+    dev_free(sub_node);
+    dev_free(chunk);
+    dev_free(chunk_ptr);
+    dev_free(geo);
+    dev_free(sub_ptr);
+    dev_free(tmat);
+    dev_free(minv);
+    dev_free(part);
+    dev_free(yc);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Space
+// ---------------------------------------------------------------------------
+__global__ void k_bbox(int64_t n, const double* __restrict__ xyz, double* out) {
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x)
+    for (int d = 0; d < 3; ++d) {
+      const double v = xyz[3 * a + d];
+      lo[d] = fmin(lo[d], v);
+      hi[d] = fmax(hi[d], v);
+    }
+  __shared__ double s[6][32];
+  for (int d = 0; d < 3; ++d) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+      hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+    }
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int d = 0; d < 3; ++d) {
+      s[d][w] = lo[d];
+      s[3 + d][w] = hi[d];
+    }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = s[threadIdx.x][0];
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k)
+      v = threadIdx.x < 3 ? fmin(v, s[threadIdx.x][k]) : fmax(v, s[threadIdx.x][k]);
+    out[6 * blockIdx.x + threadIdx.x] = v;
+  }
+}
+
+struct Grid3 {
+  double x0, y0, z0, h;
+  int nx, ny, nz;
+};
+
+__device__ __forceinline__ int cell_of(const Grid3& g, double x, double y, double z) {
+  const int ix = min(max((int)floor((x - g.x0) / g.h), 0), g.nx - 1);
+  const int iy = min(max((int)floor((y - g.y0) / g.h), 0), g.ny - 1);
+  const int iz = min(max((int)floor((z - g.z0) / g.h), 0), g.nz - 1);
+  return ix + g.nx * (iy + g.ny * iz);
+}
+
+__global__ void k_cell_count(int64_t n, const double* __restrict__ xyz, Grid3 g, int* cell, int* count) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+    const int c = cell_of(g, xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]);
+    cell[a] = c;
+    atomicAdd(count + c, 1);
+  }
+}
+
+__global__ void k_sub_of_node(int64_t n, const int* cell, const int* cell_sub, int* sub, int* iota) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+    sub[a] = cell_sub[cell[a]];
+    iota[a] = (int)a;
+  }
+}
+
+// warp per subdomain: centre = mean of its node coordinates (fixed lane order)
+__global__ void k_sub_centre(int n_sub, const int* sub_ptr, const int* sub_node, const double* __restrict__ xyz,
+                             double* centre) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < n_sub; I += nw) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    const int b = sub_ptr[I], e = sub_ptr[I + 1];
+    for (int k = b + lane; k < e; k += 32) {
+      const int a = sub_node[k];
+      s0 += xyz[3 * a];
+      s1 += xyz[3 * a + 1];
+      s2 += xyz[3 * a + 2];
+    }
+    s0 = warp_sum(s0);
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    if (lane == 0) {
+      const double inv = 1.0 / (double)(e - b);
+      centre[3 * I] = s0 * inv;
+      centre[3 * I + 1] = s1 * inv;
+      centre[3 * I + 2] = s2 * inv;
+    }
+  }
+}
+
+__global__ void k_geo(int64_t n, const double* __restrict__ xyz, const int* sub, const double* centre, double inv_h,
+                      const int32_t* ind_of, float4* geo) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+    const int I = sub[a];
+    unsigned m = 0;
+    for (int d = 0; d < 3; ++d)
+      if (ind_of[3 * a + d] >= 0) m |= 1u << d;
+    geo[a] = make_float4((float)((xyz[3 * a] - centre[3 * I]) * inv_h),
+                         (float)((xyz[3 * a + 1] - centre[3 * I + 1]) * inv_h),
+                         (float)((xyz[3 * a + 2] - centre[3 * I + 2]) * inv_h), __uint_as_float(((unsigned)I << 3) | m));
+  }
+}
+
+// rows of Z_a (masked): row d of the 3 x 6 block, in double
+__device__ __forceinline__ void z_row(float4 g, int d, double r[6]) {
+  const unsigned m = geo_bits(g);
+  const double X = g.x, Y = g.y, Z = g.z;
+  for (int k = 0; k < 6; ++k) r[k] = 0.0;
+  if (!(m & (1u << d))) return;
+  r[d] = 1.0;
+  if (d == 0) {
+    r[4] = Z;
+    r[5] = -Y;
+  } else if (d == 1) {
+    r[3] = -Z;
+    r[5] = X;
+  } else {
+    r[3] = Y;
+    r[4] = -X;
+  }
+}
+
+// warp per subdomain: G = Z_I^T Z_I, then T = L^-T on the kept modes
+__global__ void k_sub_gram(int n_sub, const int* sub_ptr, const int* sub_node, const float4* geo, double* tmat) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < n_sub; I += nw) {
+    double G[21];
+    for (int k = 0; k < 21; ++k) G[k] = 0.0;
+    for (int k = sub_ptr[I] + lane; k < sub_ptr[I + 1]; k += 32) {
+      const float4 g = geo[sub_node[k]];
+      for (int d = 0; d < 3; ++d) {
+        double r[6];
+        z_row(g, d, r);
+        int q = 0;
+        for (int i = 0; i < 6; ++i)
+          for (int j = 0; j <= i; ++j, ++q) G[q] = fma(r[i], r[j], G[q]);
+      }
+    }
+    for (int k = 0; k < 21; ++k) G[k] = warp_sum(G[k]);
+    if (lane == 0) {
+      double A[6][6], L[6][6] = {}, Li[6][6] = {};
+      int q = 0;
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j <= i; ++j, ++q) A[i][j] = A[j][i] = G[q];
+      double gmax = 0.0;
+      for (int i = 0; i < 6; ++i) gmax = fmax(gmax, A[i][i]);
+      bool keep[6];
+      for (int j = 0; j < 6; ++j) {
+        double d = A[j][j];
+        for (int k = 0; k < j; ++k) d -= L[j][k] * L[j][k];
+        keep[j] = gmax > 0.0 && d > 1e-9 * gmax;
+        if (!keep[j]) continue;
+        L[j][j] = sqrt(d);
+        for (int i = j + 1; i < 6; ++i) {
+          double s = A[i][j];
+          for (int k = 0; k < j; ++k) s -= L[i][k] * L[j][k];
+          L[i][j] = s / L[j][j];
+        }
+      }
+      for (int c = 0; c < 6; ++c) {
+        if (!keep[c]) continue;
+        Li[c][c] = 1.0 / L[c][c];
+        for (int i = c + 1; i < 6; ++i) {
+          if (!keep[i]) continue;
+          double s = 0.0;
+          for (int k = c; k < i; ++k)
+            if (keep[k]) s += L[i][k] * Li[k][c];
+          Li[i][c] = -s / L[i][i];
+        }
+      }
+      for (int k = 0; k < 6; ++k)
+        for (int i = 0; i < 6; ++i) tmat[36 * I + 6 * k + i] = Li[i][k];  // T = Li^T
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Operator
+// ---------------------------------------------------------------------------
+
+// A node row whose blocks all lie in its own subdomain, with every DOF of
+// the row's nodes free, contributes Z_a^T (K Z_I)_a = 0: the element
+// stiffnesses annihilate rigid-body motions (up to the rounding of geo), so
+// the row is left out.  Same test in the count and in the fill.
+__device__ __forceinline__ bool row_is_interior(int beg, int end, const int* __restrict__ adj, const float4* geo,
+                                                unsigned ma, int lane) {
+  const unsigned want = (ma & ~7u) | 7u;
+  if (ma != want) return false;
+  bool ok = true;
+  for (int s = beg + lane; s < end; s += 32) ok = ok && geo_bits(__ldg(geo + __ldg(adj + s))) == want;
+  return __all_sync(0xffffffffu, ok);
+}
+
+// The distinct subdomains of a node row's blocks, in order of first
+// appearance; lane k holds the k-th.  Returns their count (> 32: overflow).
+__device__ __forceinline__ int row_subdomains(int beg, int end, const int* __restrict__ adj, const float4* geo,
+                                              int lane, int* mine) {
+  int n = 0;
+  *mine = -1;
+  for (int s0 = beg; s0 < end; s0 += 32) {
+    const int s = s0 + lane;
+    const int J = s < end ? (int)(geo_bits(__ldg(geo + __ldg(adj + s))) >> 3) : -1;
+    unsigned pending = __ballot_sync(0xffffffffu, J >= 0);
+    while (pending) {
+      const int l = __ffs(pending) - 1;
+      const int Jl = __shfl_sync(0xffffffffu, J, l);
+      const bool have = __ballot_sync(0xffffffffu, lane < n && *mine == Jl) != 0;
+      if (!have) {
+        if (lane == n) *mine = Jl;
+        ++n;
+      }
+      pending &= ~__ballot_sync(0xffffffffu, J == Jl);
+    }
+  }
+  return n;
+}
+
+__global__ void k_row_count(int n_nodes, const int* __restrict__ ptr, const int* __restrict__ adj, const float4* geo,
+                            int* cnt, DevStatus* st) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; a < n_nodes; a += nw) {
+    const int beg = __ldg(ptr + a), end = __ldg(ptr + a + 1);
+    int n = 0;
+    if (!row_is_interior(beg, end, adj, geo, geo_bits(__ldg(geo + a)), lane)) {
+      int mine;
+      n = row_subdomains(beg, end, adj, geo, lane, &mine);
+    }
+    if (n > ROW_SLOTS * 4 && lane == 0) record_error(st, a, AXIA_ERR_INVALID_ARG);
+    if (lane == 0) cnt[a] = min(n, ROW_SLOTS * 4);
+  }
+}
+
+constexpr int ROW_WARPS = 8;
+constexpr int WS = 19;  // padded stride of a lane's 18 W entries in shared memory
+
+// Items of row a: for each subdomain J its blocks reach,
+//   W = sum_{b in J} M_a K_ab M_b Z_b   (3 x 6, M = free-DOF masks; lane e < 18
+// holds entry e, summed over the row's blocks in order), then C = Z_a^T W.
+__global__ void __launch_bounds__(32 * ROW_WARPS) k_row_items(int n_nodes, int n_sub, BsrMat<double> K,
+                                                               const float4* geo, const int* __restrict__ off,
+                                                               unsigned* keys, double* vals) {
+  __shared__ double s_w[ROW_WARPS][32 * WS];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double* sw = s_w[wid];
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const long long nb = K.nb;
+  for (int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; a < n_nodes; a += nw) {
+    const int o = __ldg(off + a), n = __ldg(off + a + 1) - o;
+    if (n == 0) continue;  // interior row (warp-uniform)
+    const int beg = __ldg(K.adj_ptr + a), end = __ldg(K.adj_ptr + a + 1);
+    int mine;
+    row_subdomains(beg, end, K.adj, geo, lane, &mine);
+    const float4 ga = __ldg(geo + a);
+    const unsigned ma = geo_bits(ga);
+    const int I = (int)(ma >> 3);
+    for (int g0 = 0; g0 < n; g0 += ROW_SLOTS) {
+      double acc[ROW_SLOTS];
+#pragma unroll
+      for (int k = 0; k < ROW_SLOTS; ++k) acc[k] = 0.0;
+      for (int s0 = beg; s0 < end; s0 += 32) {
+        const int s = s0 + lane;
+        int J = -1;
+        if (s < end) {
+          const int b = __ldg(K.adj + s);
+          const float4 gb = __ldg(geo + b);
+          const unsigned mb = geo_bits(gb);
+          J = (int)(mb >> 3);
+          double Kc[3][3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const double v = __ldg(K.val + (3 * i + j) * nb + s);
+              Kc[i][j] = ((ma >> i) & (mb >> j) & 1u) ? v : 0.0;
+            }
+          const double Xb = gb.x, Yb = gb.y, Zb = gb.z;
+          double* w = sw + lane * WS;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {  // row i of Kc Z_b
+            w[6 * i + 0] = Kc[i][0];
+            w[6 * i + 1] = Kc[i][1];
+            w[6 * i + 2] = Kc[i][2];
+            w[6 * i + 3] = fma(Yb, Kc[i][2], -Zb * Kc[i][1]);
+            w[6 * i + 4] = fma(Zb, Kc[i][0], -Xb * Kc[i][2]);
+            w[6 * i + 5] = fma(Xb, Kc[i][1], -Yb * Kc[i][0]);
+          }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < ROW_SLOTS; ++k) {
+          if (g0 + k >= n) break;
+          const int Jk = __shfl_sync(0xffffffffu, mine, g0 + k);
+          for (unsigned m = __ballot_sync(0xffffffffu, J == Jk); m; m &= m - 1) {
+            const int l = __ffs(m) - 1;
+            if (lane < 18) acc[k] += sw[l * WS + lane];
+          }
+        }
+        __syncwarp();
+      }
+      const double Xa = ga.x, Ya = ga.y, Za = ga.z;
+#pragma unroll
+      for (int k = 0; k < ROW_SLOTS; ++k) {
+        if (g0 + k >= n) break;
+        const int Jk = __shfl_sync(0xffffffffu, mine, g0 + k);
+        const int item = o + g0 + k;
+        if (lane == 0) keys[item] = (unsigned)I * (unsigned)n_sub + (unsigned)Jk;
+        // C[i][j] = (Z_a^T W)[i][j]; W[r][j] sits on lane 6 r + j
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int e = lane + 32 * h;
+          const int j = (e < 36 ? e : 0) % 6, i = (e < 36 ? e : 0) / 6;
+          const double w0 = __shfl_sync(0xffffffffu, acc[k], j);
+          const double w1 = __shfl_sync(0xffffffffu, acc[k], 6 + j);
+          const double w2 = __shfl_sync(0xffffffffu, acc[k], 12 + j);
+          double c = i == 0 ? w0 : i == 1 ? w1 : i == 2 ? w2
+                   : i == 3 ? fma(Ya, w2, -Za * w1) : i == 4 ? fma(Za, w0, -Xa * w2) : fma(Xa, w1, -Ya * w0);
+          if (e < 36) vals[(size_t)item * 36 + e] = c;
+        }
+      }
+    }
+  }
+}
+
+// warp per run of equal (I, J): S = sum of its items in sorted order, then
+// A_IJ = T_I^T S T_J into the dense matrix (row stride ld)
+__global__ void k_run_sum(int n_runs, int n_sub, const unsigned* run_key, const int* run_off, const int* run_cnt,
+                          const int* perm, const double* __restrict__ vals, const double* __restrict__ tmat,
+                          double* A, int ld) {
+  __shared__ double s_S[8][36], s_U[8][36];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_runs; r += nw) {
+    const int I = (int)(run_key[r] / (unsigned)n_sub), J = (int)(run_key[r] % (unsigned)n_sub);
+    const int b = run_off[r], e = b + run_cnt[r];
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll 4
+    for (int k = b; k < e; ++k) {
+      const double* v = vals + (size_t)perm[k] * 36;
+      s0 += v[lane];
+      if (lane < 4) s1 += v[32 + lane];
+    }
+    s_S[w][lane] = s0;
+    if (lane < 4) s_S[w][32 + lane] = s1;
+    __syncwarp();
+    const double* TI = tmat + 36 * I;
+    const double* TJ = tmat + 36 * J;
+    // U = S T_J
+    for (int q = lane; q < 36; q += 32) {
+      const int k = q / 6, j = q % 6;
+      double u = 0.0;
+      for (int l = 0; l < 6; ++l) u = fma(s_S[w][6 * k + l], TJ[6 * l + j], u);
+      s_U[w][q] = u;
+    }
+    __syncwarp();
+    for (int q = lane; q < 36; q += 32) {
+      const int i = q / 6, j = q % 6;
+      double v = 0.0;
+      for (int k = 0; k < 6; ++k) v = fma(TI[6 * k + i], s_U[w][6 * k + j], v);
+      A[(size_t)(6 * I + i) * ld + 6 * J + j] = v;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void k_scale_to_f32(int ncp, const double* A, const double* scale, float* B) {
+  const int64_t n2 = (int64_t)ncp * ncp;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n2; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / ncp), j = (int)(t % ncp);
+    const double si = scale[i], sj = scale[j];
+    B[t] = (si == 0.0 || sj == 0.0) ? (i == j ? 1.0f : 0.0f) : (float)(A[t] * si * sj);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Blocked Gauss-Jordan inverse of an SPD matrix (FP32, in place, no pivoting).
+// Step k with P = A_kk^-1 and the new row panel R_j = P A_kj (j != k):
+//   A_ij <- A_ij - A_ik R_j  (i, j != k),  A_kj <- R_j,  A_ik <- -R_i^T,  A_kk <- P.
+// With S_i = -1 for the block indices eliminated so far and +1 for the rest,
+// every intermediate satisfies A_ij = S_i S_j A_ji^T (the final inverse,
+// S = -1 throughout, is symmetric).  So the trailing update runs over the
+// tiles with j <= i and mirrors them with that sign, and the new column panel
+// is A_ik = -S_i R_i^T.
+// ---------------------------------------------------------------------------
+constexpr int GJ_LD = GJ_T + 4;   // shared-memory row stride (16-byte aligned rows)
+
+struct GjArgs {
+  float* A;
+  int n;             // multiple of GJ_T
+  float* piv;        // [GJ_T][GJ_T] P of the current step
+  GridBarrier* bar;
+  DevStatus* st;
+  unsigned long long limit_ns;
+};
+
+// operand tiles: sa[q][r] = X[r][q] (transposed), sb[q][c] = Y[q][c]
+__device__ __forceinline__ void gj_load_t(float (*sa)[GJ_LD], const float* g, int ld) {
+  for (int t = threadIdx.x; t < GJ_T * GJ_T; t += blockDim.x) sa[t % GJ_T][t / GJ_T] = g[(size_t)(t / GJ_T) * ld + t % GJ_T];
+}
+__device__ __forceinline__ void gj_load(float (*sb)[GJ_LD], const float* g, int ld) {
+  for (int t = threadIdx.x; t < GJ_T * GJ_T / 4; t += blockDim.x) {
+    const int r = t / (GJ_T / 4), c = 4 * (t % (GJ_T / 4));
+    *reinterpret_cast<float4*>(&sb[r][c]) = *reinterpret_cast<const float4*>(g + (size_t)r * ld + c);
+  }
+}
+
+// out[4][4] = rows 4ty.. / cols 4tx.. of X Y
+__device__ __forceinline__ void gj_mul(float (*sa)[GJ_LD], float (*sb)[GJ_LD], float out[4][4]) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) out[r][c] = 0.f;
+#pragma unroll 8
+  for (int q = 0; q < GJ_T; ++q) {
+    const float4 x = *reinterpret_cast<const float4*>(&sa[q][4 * ty]);
+    const float4 y = *reinterpret_cast<const float4*>(&sb[q][4 * tx]);
+    const float xr[4] = {x.x, x.y, x.z, x.w}, yc[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) out[r][c] = fmaf(xr[r], yc[c], out[r][c]);
+  }
+}
+
+// column panel of step k: tile (i, k) = -S_i tile (k, i)^T (i != k; S_i = -1 for i < k)
+__device__ __forceinline__ void gj_column_panel(const GjArgs& P, int k, int first, int stride) {
+  const int nt = P.n / GJ_T, ld = P.n;
+  for (int i = first; i < nt; i += stride) {
+    if (i == k) continue;
+    const float sg = i < k ? 1.f : -1.f;
+    const float* src = P.A + (size_t)k * GJ_T * ld + (size_t)i * GJ_T;
+    float* dst = P.A + (size_t)i * GJ_T * ld + (size_t)k * GJ_T;
+    for (int t = threadIdx.x; t < GJ_T * GJ_T; t += blockDim.x) {
+      const int r = t / GJ_T, c = t % GJ_T;  // coalesced reads of src row r
+      dst[(size_t)c * ld + r] = sg * src[(size_t)r * ld + c];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P) {
+  __shared__ __align__(16) float sa[GJ_T][GJ_LD];
+  __shared__ __align__(16) float sb[GJ_T][GJ_LD];
+  const int nt = P.n / GJ_T, ld = P.n;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  auto tile = [&](int i, int j) { return P.A + (size_t)i * GJ_T * ld + (size_t)j * GJ_T; };
+  for (int k = 0; k < nt; ++k) {
+    // 1. block 0 stores the previous P and inverts tile (k, k) (double-buffered
+    //    in-place Gauss-Jordan, one barrier per pivot); the other blocks write
+    //    the previous step's column panel
+    if (blockIdx.x == 0) {
+      if (k > 0)
+        for (int t = threadIdx.x; t < GJ_T * GJ_T; t += blockDim.x)
+          tile(k - 1, k - 1)[(size_t)(t / GJ_T) * ld + t % GJ_T] = P.piv[t];
+      gj_load(sa, tile(k, k), ld);
+      float (*cur)[GJ_LD] = sa;
+      float (*nxt)[GJ_LD] = sb;
+      for (int p = 0; p < GJ_T; ++p) {
+        __syncthreads();
+        const float piv = cur[p][p];
+        if (threadIdx.x == 0 && (!(piv > 0.f) || !isfinite(piv))) record_error(P.st, k * GJ_T + p, AXIA_ERR_ZERO_PIVOT);
+        const float d = 1.0f / piv;
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int i = 4 * ty + r, j = 4 * tx + c;
+            float v;
+            if (i == p) v = j == p ? d : cur[p][j] * d;
+            else if (j == p) v = -cur[i][p] * d;
+            else v = fmaf(-cur[i][p] * d, cur[p][j], cur[i][j]);
+            nxt[i][j] = v;
+          }
+        float (*t)[GJ_LD] = cur;
+        cur = nxt;
+        nxt = t;
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < GJ_T * GJ_T; t += blockDim.x) P.piv[t] = cur[t / GJ_T][t % GJ_T];
+    } else if (k > 0) {
+      gj_column_panel(P, k - 1, blockIdx.x - 1, gridDim.x - 1);
+    }
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+    // 2. row panel: A_kj <- P A_kj
+    for (int j = blockIdx.x; j < nt; j += gridDim.x) {
+      if (j == k) continue;
+      __syncthreads();
+      gj_load_t(sa, P.piv, GJ_T);
+      gj_load(sb, tile(k, j), ld);
+      __syncthreads();
+      float o[4][4];
+      gj_mul(sa, sb, o);
+      float* g = tile(k, j);
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        *reinterpret_cast<float4*>(g + (size_t)(4 * ty + r) * ld + 4 * tx) = make_float4(o[r][0], o[r][1], o[r][2], o[r][3]);
+    }
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+    // 3. trailing tiles j <= i (i, j != k): A_ij -= A_ik R_j, mirrored into A_ji
+    const int m = nt - 1, ntiles = m * (m + 1) / 2;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      int i = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
+      while (i * (i + 1) / 2 > t) --i;
+      while ((i + 1) * (i + 2) / 2 <= t) ++i;
+      int j = t - i * (i + 1) / 2;
+      if (i >= k) ++i;
+      if (j >= k) ++j;
+      __syncthreads();
+      gj_load_t(sa, tile(i, k), ld);
+      gj_load(sb, tile(k, j), ld);
+      __syncthreads();
+      float o[4][4];
+      gj_mul(sa, sb, o);
+      float* g = tile(i, j);
+      float v[4][4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const float4 c = *reinterpret_cast<const float4*>(g + (size_t)(4 * ty + r) * ld + 4 * tx);
+        v[r][0] = c.x - o[r][0];
+        v[r][1] = c.y - o[r][1];
+        v[r][2] = c.z - o[r][2];
+        v[r][3] = c.w - o[r][3];
+        *reinterpret_cast<float4*>(g + (size_t)(4 * ty + r) * ld + 4 * tx) = make_float4(v[r][0], v[r][1], v[r][2], v[r][3]);
+      }
+      if (i != j) {  // A_ji = S_i S_j A_ij^T
+        const float sg = (i < k) == (j < k) ? 1.f : -1.f;
+        float* h = tile(j, i);
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          *reinterpret_cast<float4*>(h + (size_t)(4 * tx + c) * ld + 4 * ty) =
+              make_float4(sg * v[0][c], sg * v[1][c], sg * v[2][c], sg * v[3][c]);
+      }
+    }
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+  }
+  // the last step's P and column panel
+  const int k = nt - 1;
+  if (blockIdx.x == 0) {
+    for (int t = threadIdx.x; t < GJ_T * GJ_T; t += blockDim.x)
+      tile(k, k)[(size_t)(t / GJ_T) * ld + t % GJ_T] = P.piv[t];
+  } else {
+    gj_column_panel(P, k, blockIdx.x - 1, gridDim.x - 1);
+  }
+}
+
+// M_IJ = T_I diag(s_I) B_IJ diag(s_J) T_J^T in the raw mode basis (thread per pair)
+__global__ void k_minv(int n_sub, int ncp, const float* __restrict__ B, const double* __restrict__ scale,
+                       const double* __restrict__ tmat, float* M) {
+  const int64_t npair = (int64_t)n_sub * n_sub;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < npair; t += (int64_t)gridDim.x * blockDim.x) {
+    const int I = (int)(t / n_sub), J = (int)(t % n_sub);
+    const double* TI = tmat + 36 * I;
+    const double* TJ = tmat + 36 * J;
+    double Bs[6][6];
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j)
+        Bs[i][j] = (double)B[(size_t)(6 * I + i) * ncp + 6 * J + j] * scale[6 * I + i] * scale[6 * J + j];
+    // U[i][l] = sum_j Bs[i][j] T_J[l][j]
+    double U[6][6];
+    for (int i = 0; i < 6; ++i)
+      for (int l = 0; l < 6; ++l) {
+        double u = 0.0;
+        for (int j = 0; j < 6; ++j) u = fma(Bs[i][j], TJ[6 * l + j], u);
+        U[i][l] = u;
+      }
+    for (int k = 0; k < 6; ++k)
+      for (int l = 0; l < 6; ++l) {
+        double v = 0.0;
+        for (int i = 0; i < 6; ++i) v = fma(TI[6 * k + i], U[i][l], v);
+        M[(size_t)(6 * I + k) * ncp + 6 * J + l] = (float)v;
+      }
+  }
+}
+
+int read_status(axia_ctx* ctx, const char* what) {
+  DevStatus hs;
+  AXIA_TRY(read_dev_status(ctx, &hs));
+  if (hs.first_error != ~0ull) {
+    ctx->last_bad = (int64_t)(hs.first_error >> 8);
+    return set_error(ctx, (int)(hs.first_error & 0xff), std::string("coarse space: ") + what);
+  }
+  if (hs.timeout) return set_error(ctx, AXIA_ERR_TIMEOUT, std::string("coarse space: barrier timeout in ") + what);
+  return AXIA_OK;
+}
+
+template <typename T>
+int copy_to_host(axia_ctx* ctx, T* h, const T* d, size_t n) {
+  AXIA_CUDA(ctx, cudaMemcpyAsync(h, d, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXIA_OK;
+}
+
+template <typename T>
+int copy_to_device(axia_ctx* ctx, T* d, const T* h, size_t n) {
+  AXIA_CUDA(ctx, cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXIA_OK;
+}
+
+int grid_for(const axia_ctx* ctx, int64_t n, int threads) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, (int64_t)ctx->sm_count * 16));
+}
+
+// subdomains, chunks, geo and T for the current mesh and constraints
+int build_space(axia_ctx* ctx, CoarseState* S) {
+  const int64_t n = ctx->n_nodes;
+  if (n >= (1LL << 28)) return set_error(ctx, AXIA_ERR_TOO_LARGE, "coarse space: too many nodes");
+  const int bb_grid = (int)std::min<int64_t>((n + 255) / 256, 1024);
+  double* d_bb = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_bb, (size_t)6 * bb_grid));
+  k_bbox<<<bb_grid, 256, 0, ctx->stream>>>(n, ctx->d_coords, d_bb);
+  ctx->launches++;
+  std::vector<double> hb((size_t)6 * bb_grid);
+  int st = copy_to_host(ctx, hb.data(), d_bb, hb.size());
+  dev_free(d_bb);
+  AXIA_TRY(st);
+  double lo[3] = {hb[0], hb[1], hb[2]}, hi[3] = {hb[3], hb[4], hb[5]};
+  for (int b = 1; b < bb_grid; ++b)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], hb[6 * b + d]);
+      hi[d] = std::max(hi[d], hb[6 * b + 3 + d]);
+    }
+  double ext[3], emax = 0.0;
+  for (int d = 0; d < 3; ++d) emax = std::max(emax, ext[d] = hi[d] - lo[d]);
+  if (!(emax > 0.0) || !std::isfinite(emax)) emax = 1.0;
+  const int max_boxes = COARSE_MAX / 6;
+  const int64_t target = std::max<int64_t>(1, std::min<int64_t>(max_boxes, n / std::max(1, S->nodes_target)));
+  double vol = 1.0;
+  for (int d = 0; d < 3; ++d) vol *= std::max(ext[d], 1e-3 * emax);
+  double h = std::cbrt(vol / (double)target);
+  Grid3 g{};
+  for (int it = 0; it < 400; ++it) {
+    g.nx = std::max(1, (int)std::ceil(ext[0] / h - 1e-9));
+    g.ny = std::max(1, (int)std::ceil(ext[1] / h - 1e-9));
+    g.nz = std::max(1, (int)std::ceil(ext[2] / h - 1e-9));
+    if ((int64_t)g.nx * g.ny * g.nz <= target) break;
+    h *= 1.02;
+  }
+  if ((int64_t)g.nx * g.ny * g.nz > target) {  // one box
+    g.nx = g.ny = g.nz = 1;
+    h = 2.0 * emax;
+  }
+  g.x0 = lo[0];
+  g.y0 = lo[1];
+  g.z0 = lo[2];
+  g.h = h;
+  S->h = h;
+  const int ncell = g.nx * g.ny * g.nz;
+  int *d_cell = nullptr, *d_count = nullptr, *d_sub = nullptr, *d_iota = nullptr, *d_cellsub = nullptr;
+  int* d_sub_sorted = nullptr;
+  double* d_centre = nullptr;
+  void* d_temp = nullptr;
+  st = AXIA_OK;
+  do {
+    if ((st = dev_alloc(ctx, &d_cell, (size_t)n))) break;
+    if ((st = dev_alloc(ctx, &d_count, (size_t)ncell))) break;
+    AXIA_CUDA(ctx, cudaMemsetAsync(d_count, 0, ncell * sizeof(int), ctx->stream));
+    k_cell_count<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, ctx->d_coords, g, d_cell, d_count);
+    ctx->launches++;
+    std::vector<int> count(ncell), cell_sub(ncell, -1);
+    if ((st = copy_to_host(ctx, count.data(), d_count, (size_t)ncell))) break;
+    int n_sub = 0;
+    std::vector<int> sub_ptr(1, 0);
+    for (int c = 0; c < ncell; ++c)
+      if (count[c] > 0) {
+        cell_sub[c] = n_sub++;
+        sub_ptr.push_back(sub_ptr.back() + count[c]);
+      }
+    // chunks of COARSE_CHUNK nodes inside every subdomain
+    std::vector<int4> chunk;
+    std::vector<int> chunk_ptr(1, 0);
+    for (int I = 0; I < n_sub; ++I) {
+      for (int b = sub_ptr[I]; b < sub_ptr[I + 1]; b += COARSE_CHUNK)
+        chunk.push_back(make_int4(I, b, std::min(b + COARSE_CHUNK, sub_ptr[I + 1]), 0));
+      chunk_ptr.push_back((int)chunk.size());
+    }
+    CoarseArgs& A = S->args;
+    A.n_sub = n_sub;
+    A.nc = 6 * n_sub;
+    A.ncp = ((A.nc + GJ_T - 1) / GJ_T) * GJ_T;
+    A.n_chunks = (int)chunk.size();
+    if ((st = dev_alloc(ctx, &d_cellsub, (size_t)ncell))) break;
+    if ((st = copy_to_device(ctx, d_cellsub, cell_sub.data(), (size_t)ncell))) break;
+    if ((st = dev_alloc(ctx, &d_sub, (size_t)n))) break;
+    if ((st = dev_alloc(ctx, &d_iota, (size_t)n))) break;
+    if ((st = dev_alloc(ctx, &d_sub_sorted, (size_t)n))) break;
+    if ((st = dev_alloc(ctx, &S->sub_node, (size_t)n))) break;
+    k_sub_of_node<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, d_cell, d_cellsub, d_sub, d_iota);
+    ctx->launches++;
+    size_t temp_bytes = 0;
+    int bits = 1;
+    while ((1 << bits) < n_sub && bits < 30) ++bits;
+    cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, d_sub, d_sub_sorted, d_iota, S->sub_node, (int)n, 0, bits,
+                                    ctx->stream);
+    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(temp_bytes, 16)));
+    AXIA_CUDA(ctx, cub::DeviceRadixSort::SortPairs(d_temp, temp_bytes, d_sub, d_sub_sorted, d_iota, S->sub_node,
+                                                   (int)n, 0, bits, ctx->stream));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if ((st = dev_alloc(ctx, &S->sub_ptr, sub_ptr.size()))) break;
+    if ((st = copy_to_device(ctx, S->sub_ptr, sub_ptr.data(), sub_ptr.size()))) break;
+    if ((st = dev_alloc(ctx, &S->chunk, chunk.size()))) break;
+    if ((st = copy_to_device(ctx, S->chunk, chunk.data(), chunk.size()))) break;
+    if ((st = dev_alloc(ctx, &S->chunk_ptr, chunk_ptr.size()))) break;
+    if ((st = copy_to_device(ctx, S->chunk_ptr, chunk_ptr.data(), chunk_ptr.size()))) break;
+    if ((st = dev_alloc(ctx, &d_centre, (size_t)3 * n_sub))) break;
+    if ((st = dev_alloc(ctx, &S->geo, (size_t)n))) break;
+    if ((st = dev_alloc(ctx, &S->tmat, (size_t)36 * n_sub))) break;
+    k_sub_centre<<<grid_for(ctx, (int64_t)n_sub * 32, 256), 256, 0, ctx->stream>>>(n_sub, S->sub_ptr, S->sub_node,
+                                                                                  ctx->d_coords, d_centre);
+    k_geo<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, ctx->d_coords, d_sub, d_centre, 1.0 / h, ctx->d_ind_of,
+                                                          S->geo);
+    k_sub_gram<<<grid_for(ctx, (int64_t)n_sub * 32, 128), 128, 0, ctx->stream>>>(n_sub, S->sub_ptr, S->sub_node,
+                                                                                S->geo, S->tmat);
+    ctx->launches += 3;
+    AXIA_CUDA(ctx, cudaGetLastError());
+    if ((st = dev_alloc(ctx, &S->part, (size_t)6 * A.n_chunks))) break;
+    if ((st = dev_alloc(ctx, &S->yc, (size_t)A.ncp))) break;
+    if ((st = dev_alloc(ctx, &S->minv, (size_t)A.nc * A.ncp))) break;
+    AXIA_CUDA(ctx, cudaMemsetAsync(S->yc, 0, A.ncp * sizeof(float), ctx->stream));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    A.sub_node = S->sub_node;
+    A.chunk = S->chunk;
+    A.chunk_ptr = S->chunk_ptr;
+    A.geo = S->geo;
+    A.minv = S->minv;
+    A.part = S->part;
+    A.yc = S->yc;
+  } while (false);
+  if (d_temp) cudaFree(d_temp);
+  dev_free(d_cell);
+  dev_free(d_count);
+  dev_free(d_sub);
+  dev_free(d_iota);
+  dev_free(d_cellsub);
+  dev_free(d_sub_sorted);
+  dev_free(d_centre);
+  return st;
+}
+
+// coarse operator and its inverse from the assembled FP64 node-block matrix
+int build_operator(axia_ctx* ctx, CoarseState* S) {
+  CoarseArgs& A = S->args;
+  const int n = (int)ctx->n_nodes, n_sub = A.n_sub, nc = A.nc, ncp = A.ncp;
+  const BsrMat<double> K{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq};
+  int *d_cnt = nullptr, *d_off = nullptr, *d_iota = nullptr, *d_perm = nullptr, *d_run_off = nullptr,
+      *d_run_cnt = nullptr, *d_nruns = nullptr;
+  unsigned *d_keys = nullptr, *d_keys_sorted = nullptr, *d_run_key = nullptr;
+  double *d_vals = nullptr, *d_a64 = nullptr, *d_scale = nullptr;
+  float *d_a32 = nullptr, *d_piv = nullptr;
+  void* d_temp = nullptr;
+  int st = AXIA_OK;
+  do {
+    AXIA_TRY(reset_dev_status(ctx));
+    if ((st = dev_alloc(ctx, &d_cnt, (size_t)n + 1))) break;
+    if ((st = dev_alloc(ctx, &d_off, (size_t)n + 1))) break;
+    AXIA_CUDA(ctx, cudaMemsetAsync(d_cnt + n, 0, sizeof(int), ctx->stream));
+    k_row_count<<<grid_for(ctx, (int64_t)n * 32, 256), 256, 0, ctx->stream>>>(n, ctx->d_qptr, ctx->d_qadj, A.geo,
+                                                                             d_cnt, ctx->d_status);
+    ctx->launches++;
+    if ((st = read_status(ctx, "a node row touches more than 32 subdomains (raise coarse_nodes)"))) break;
+    size_t tb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, d_cnt, d_off, n + 1, ctx->stream);
+    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
+    AXIA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(d_temp, tb, d_cnt, d_off, n + 1, ctx->stream));
+    int n_items = 0;
+    if ((st = copy_to_host(ctx, &n_items, d_off + n, 1))) break;
+    cudaFree(d_temp);
+    d_temp = nullptr;
+    if ((st = dev_alloc(ctx, &d_keys, (size_t)n_items))) break;
+    if ((st = dev_alloc(ctx, &d_keys_sorted, (size_t)n_items))) break;
+    if ((st = dev_alloc(ctx, &d_vals, (size_t)n_items * 36))) break;
+    if ((st = dev_alloc(ctx, &d_iota, (size_t)n_items))) break;
+    if ((st = dev_alloc(ctx, &d_perm, (size_t)n_items))) break;
+    k_row_items<<<grid_for(ctx, (int64_t)n * 32, 32 * ROW_WARPS), 32 * ROW_WARPS, 0, ctx->stream>>>(
+        n, n_sub, K, A.geo, d_off, d_keys, d_vals);
+    ctx->launches++;
+    AXIA_CUDA(ctx, cudaGetLastError());
+    {
+      std::vector<int> iota(n_items);
+      for (int i = 0; i < n_items; ++i) iota[i] = i;
+      if ((st = copy_to_device(ctx, d_iota, iota.data(), (size_t)n_items))) break;
+    }
+    int bits = 1;
+    while ((1ull << bits) < (unsigned long long)n_sub * n_sub && bits < 32) ++bits;
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, d_keys, d_keys_sorted, d_iota, d_perm, n_items, 0, bits,
+                                    ctx->stream);
+    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
+    AXIA_CUDA(ctx, cub::DeviceRadixSort::SortPairs(d_temp, tb, d_keys, d_keys_sorted, d_iota, d_perm, n_items, 0,
+                                                   bits, ctx->stream));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(d_temp);
+    d_temp = nullptr;
+    if ((st = dev_alloc(ctx, &d_run_key, (size_t)n_items))) break;
+    if ((st = dev_alloc(ctx, &d_run_cnt, (size_t)n_items))) break;
+    if ((st = dev_alloc(ctx, &d_run_off, (size_t)n_items))) break;
+    if ((st = dev_alloc(ctx, &d_nruns, 1))) break;
+    cub::DeviceRunLengthEncode::Encode(nullptr, tb, d_keys_sorted, d_run_key, d_run_cnt, d_nruns, n_items,
+                                       ctx->stream);
+    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
+    AXIA_CUDA(ctx, cub::DeviceRunLengthEncode::Encode(d_temp, tb, d_keys_sorted, d_run_key, d_run_cnt, d_nruns,
+                                                      n_items, ctx->stream));
+    int n_runs = 0;
+    if ((st = copy_to_host(ctx, &n_runs, d_nruns, 1))) break;
+    cudaFree(d_temp);
+    d_temp = nullptr;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, d_run_cnt, d_run_off, n_runs, ctx->stream);
+    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
+    AXIA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(d_temp, tb, d_run_cnt, d_run_off, n_runs, ctx->stream));
+    if ((st = dev_alloc(ctx, &d_a64, (size_t)ncp * ncp))) break;
+    AXIA_CUDA(ctx, cudaMemsetAsync(d_a64, 0, (size_t)ncp * ncp * sizeof(double), ctx->stream));
+    k_run_sum<<<grid_for(ctx, (int64_t)n_runs * 32, 256), 256, 0, ctx->stream>>>(
+        n_runs, n_sub, d_run_key, d_run_off, d_run_cnt, d_perm, d_vals, S->tmat, d_a64, ncp);
+    ctx->launches++;
+    AXIA_CUDA(ctx, cudaGetLastError());
+    // unit-diagonal scaling; modes without stiffness (dropped or padding) become identity
+    std::vector<double> diag(ncp), scale(ncp, 0.0);
+    AXIA_CUDA(ctx, cudaMemcpy2DAsync(diag.data(), sizeof(double), d_a64, (size_t)(ncp + 1) * sizeof(double),
+                                     sizeof(double), ncp, cudaMemcpyDeviceToHost, ctx->stream));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double dmax = 0.0;
+    for (int i = 0; i < nc; ++i) dmax = std::max(dmax, std::isfinite(diag[i]) ? diag[i] : 0.0);
+    for (int i = 0; i < nc; ++i)
+      if (diag[i] > 1e-12 * dmax && std::isfinite(diag[i])) scale[i] = 1.0 / std::sqrt(diag[i]);
+    if ((st = dev_alloc(ctx, &d_scale, (size_t)ncp))) break;
+    if ((st = copy_to_device(ctx, d_scale, scale.data(), (size_t)ncp))) break;
+    if ((st = dev_alloc(ctx, &d_a32, (size_t)ncp * ncp))) break;
+    k_scale_to_f32<<<grid_for(ctx, (int64_t)ncp * ncp, 256), 256, 0, ctx->stream>>>(ncp, d_a64, d_scale, d_a32);
+    ctx->launches++;
+    dev_free(d_a64);
+    // in-place inverse
+    if ((st = dev_alloc(ctx, &d_piv, (size_t)GJ_T * GJ_T))) break;
+    {
+      int per_sm = 0;
+      AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_inverse, GJ_THREADS, 0));
+      if (per_sm < 1) {
+        st = set_error(ctx, AXIA_ERR_CUDA, "coarse space: inverse kernel does not fit");
+        break;
+      }
+      const int nt = ncp / GJ_T;
+      const int grid = std::max(2, std::min(std::min(per_sm, 2) * ctx->sm_count, std::max(2, nt * (nt - 1) / 2)));
+      AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
+      GjArgs P{d_a32, ncp, d_piv, ctx->d_bar, ctx->d_status, 2000000000ull};
+      void* params[] = {&P};
+      AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_gj_inverse, dim3(grid), dim3(GJ_THREADS), params, 0,
+                                                 ctx->stream));
+      ctx->launches++;
+    }
+    if ((st = read_status(ctx, "coarse operator is not positive definite"))) break;
+    AXIA_CUDA(ctx, cudaMemsetAsync(S->minv, 0, (size_t)nc * ncp * sizeof(float), ctx->stream));
+    k_minv<<<grid_for(ctx, (int64_t)n_sub * n_sub, 128), 128, 0, ctx->stream>>>(n_sub, ncp, d_a32, d_scale, S->tmat,
+                                                                               S->minv);
+    ctx->launches++;
+    AXIA_CUDA(ctx, cudaGetLastError());
+    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } while (false);
+  if (d_temp) cudaFree(d_temp);
+  dev_free(d_cnt);
+  dev_free(d_off);
+  dev_free(d_iota);
+  dev_free(d_perm);
+  dev_free(d_run_off);
+  dev_free(d_run_cnt);
+  dev_free(d_nruns);
+  dev_free(d_keys);
+  dev_free(d_keys_sorted);
+  dev_free(d_run_key);
+  dev_free(d_vals);
+  dev_free(d_a64);
+  dev_free(d_scale);
+  dev_free(d_a32);
+  dev_free(d_piv);
+  return st;
+}
+
+}  // namespace
+
+void coarse_release(axia_ctx* ctx) {
+  auto* S = static_cast<CoarseState*>(ctx->coarse);
+  if (!S) return;
+  S->release();
+  delete S;
+  ctx->coarse = nullptr;
+}
+
+// The coarse space of the current mesh (built on first use, or when the
+// requested subdomain size changes) and its operator for the current
+// assembly (rebuilt after every assembly).
+int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out) {
+  if (!ctx->have_bsr64) return set_error(ctx, AXIA_ERR_STATE, "coarse space needs the FP64 node-block matrix");
+  if (nodes_target <= 0) nodes_target = 2000;
+  auto* S = static_cast<CoarseState*>(ctx->coarse);
+  if (S && S->nodes_target != nodes_target) {
+    coarse_release(ctx);
+    S = nullptr;
+  }
+  if (!S) {
+    S = new CoarseState();
+    S->nodes_target = nodes_target;
+    ctx->coarse = S;
+    const int st = build_space(ctx, S);
+    if (st) {
+      coarse_release(ctx);
+      return st;
+    }
+  }
+  if (S->op_gen != ctx->assemble_gen) {
+    AXIA_TRY(build_operator(ctx, S));
+    S->op_gen = ctx->assemble_gen;
+  }
+  *out = S->args;
+  return AXIA_OK;
+}
+
+extern "C" int32_t axia_gpu_coarse_size(const axia_ctx* ctx, int64_t* n_sub, int64_t* n_coarse) {
+  if (!ctx || !n_sub || !n_coarse) return AXIA_ERR_INVALID_ARG;
+  const auto* S = static_cast<const CoarseState*>(ctx->coarse);
+  *n_sub = S ? S->args.n_sub : 0;
+  *n_coarse = S ? S->args.nc : 0;
+  return AXIA_OK;
+}

@@ -293,6 +293,10 @@ struct axia_ctx {
   // stress recovery / reactions: per (element, local node) 6 stresses + 3 forces
   double* d_rec = nullptr;      // [n_elem*nn*9]
 
+  // two-level preconditioner: coarse space of the mesh and its operator (coarse.cu)
+  void* coarse = nullptr;       // CoarseState
+  int64_t assemble_gen = 0;     // numeric assemblies so far (the operator follows K)
+
   double ms_setup = 0.0, ms_assemble = 0.0;
   int64_t last_bad = -1;
 };
@@ -341,5 +345,6 @@ void dev_free(T*& p) {
 int device_exclusive_scan(axia_ctx* ctx, const int64_t* d_in, int64_t* d_out, int64_t n, int64_t* total);
 
 // status word helpers
+void coarse_release(axia_ctx* ctx);
 int read_dev_status(axia_ctx* ctx, DevStatus* st_host);
 int reset_dev_status(axia_ctx* ctx);

@@ -139,6 +139,8 @@ int solve_multi_device(axia_ctx* ctx, const double* d_f, double* d_u, const axia
   if (ctx->mesh_node0.size() < 2) return set_error(ctx, AXIA_ERR_STATE, "solve_multi needs axia_gpu_setup_multi");
   if (!ctx->have_bsr64 || !ctx->have_bsr32)
     return set_error(ctx, AXIA_ERR_STATE, "solve_multi needs axia_gpu_assemble_ex(AXIA_ASM_BSR64 | AXIA_ASM_BSR32)");
+  if (opts->preconditioner != AXIA_PRECOND_JACOBI)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "solve_multi: Jacobi preconditioner only");
   const int nm = (int)ctx->mesh_node0.size() - 1;
   AXIA_TRY(prepare_full_buffers(ctx));
   int lanes = 0, vec = 0;

@@ -99,6 +99,24 @@ struct MeshGroup {
   long long part_off; // offset of its partial-sum area
 };
 
+constexpr int COARSE_MAX = 4096;    // coarse unknowns (6 per subdomain, padded to 64)
+constexpr int COARSE_CHUNK = 256;   // nodes per restriction chunk
+constexpr int S_RC = 3;             // partial-sum slot of r_c . y
+
+struct CoarseArgs {
+  int n_sub;             // subdomains (0: no coarse space)
+  int nc;                // 6 n_sub
+  int ncp;               // nc rounded up to a multiple of 64 (row stride of minv)
+  int n_chunks;
+  const int* sub_node;   // [n_nodes] nodes by subdomain, ascending within each
+  const int4* chunk;     // [n_chunks] (subdomain, first, end) ranges of sub_node
+  const int* chunk_ptr;  // [n_sub + 1] chunks of each subdomain
+  const float4* geo;     // [n_nodes] (x_a - c_I) / h, .w = bits (I << 3 | free-DOF mask)
+  const float* minv;     // [nc][ncp] M, zero in the padding
+  float* part;           // [n_chunks][6] restriction partials
+  float* yc;             // [ncp] coarse correction y = M r_c
+};
+
 struct BsrReliableArgs {
   BsrMat<float> M32;
   BsrMat<double> M64;
@@ -120,6 +138,7 @@ struct BsrReliableArgs {
   double delta;
   long long max_iter;
   unsigned long long limit_ns;
+  CoarseArgs C;      // two-level preconditioner (n_sub = 0: Jacobi only)
 };
 
 BsrReliableArgs make_reliable_args(axia_ctx* ctx, double rtol, double delta, long long max_iter);

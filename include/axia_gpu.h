@@ -97,6 +97,14 @@ typedef struct axia_mesh {
   double nu;               /* Poisson's ratio */
 } axia_mesh;
 
+typedef enum axia_preconditioner {
+  AXIA_PRECOND_JACOBI = 0,  /* diagonal scaling, as linalg.rs:199-259 */
+  AXIA_PRECOND_COARSE = 1   /* two-level: diagonal + a coarse space of the rigid-body modes of
+                               subdomains (boxes of about coarse_nodes nodes).  Mixed precision
+                               on the node-block form only; no reference counterpart -- the
+                               solution is the same, the iteration count drops */
+} axia_preconditioner;
+
 typedef struct axia_solve_opts {
   double rtol;             /* stop when ||r||_2 <= rtol ||b||_2 (reference: 1e-8, linalg.rs:363) */
   int64_t max_iter;        /* <= 0: max(4 n, 200) as linalg.rs:376 */
@@ -107,6 +115,8 @@ typedef struct axia_solve_opts {
   int32_t spmv_lanes;      /* lanes per row in the SpMV: 0 = automatic, else 1..32 (power of two) */
   int32_t matrix_format;   /* axia_matrix_format */
   int32_t spmv_vec;        /* node-block form: blocks per lane load (1, 2, 4; 0 = automatic) */
+  int32_t preconditioner;  /* axia_preconditioner (0 = Jacobi) */
+  int32_t coarse_nodes;    /* AXIA_PRECOND_COARSE: nodes per subdomain (0 = 2000; at most 682 subdomains) */
 } axia_solve_opts;
 
 typedef struct axia_solve_info {
@@ -234,6 +244,10 @@ AXIA_API int32_t axia_gpu_bsr_spmv_device(axia_ctx* ctx, int32_t precision, cons
 
 /* Number of 3x3 node blocks of the node-block form (node adjacency entries). */
 AXIA_API int64_t axia_gpu_node_blocks(const axia_ctx* ctx);
+
+/* Size of the coarse space the last AXIA_PRECOND_COARSE solve used: subdomains
+ * and coarse unknowns (6 per subdomain; 0 and 0 before such a solve). */
+AXIA_API int32_t axia_gpu_coarse_size(const axia_ctx* ctx, int64_t* n_sub, int64_t* n_coarse);
 
 /* Bilinear element form s_e = u_e^T K_e(E=1) v_e for every element of the
  * mesh of the last setup (u_full, v_full: 3*n_nodes; s: n_elem).  With

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layouts_match_header():
     # field order and sizes of the ABI structs (x86-64 and aarch64 share them)
     assert ctypes.sizeof(_lib.Mesh) == 8 * 3 + 4 * 2 + 8 * 4
-    assert ctypes.sizeof(_lib.SolveOpts) == 8 + 8 + 4 + 4 + 8 + 4 + 4 + 4 + 4
+    assert ctypes.sizeof(_lib.SolveOpts) == 8 + 8 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 4 + 4
     assert ctypes.sizeof(_lib.SolveInfo) == 8 * 4 + 8 * 7 + 8 + 8 + 4 + 4
 
 
