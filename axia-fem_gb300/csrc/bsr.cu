@@ -253,13 +253,11 @@ struct SolveRange {
   PcgOut* out;
 };
 
-// The coarse part of the two-level preconditioner for the current r32:
-// restriction, grid barrier, y = M r_c, and r_c . y reduced over the group.
+// The coarse solve of the two-level preconditioner, r_c complete:
+// y = M r_c, and r_c . y reduced over the group.
 __device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const SolveRange& R, int gwarp, int nwarps,
                                             int lane, float* rz_c) {
   __shared__ __align__(16) float s_rc[COARSE_MAX];
-  coarse_restrict(P.C, P.r32, gwarp, nwarps, lane);
-  if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return false;
   const float acc = coarse_solve(P.C, s_rc, gwarp, nwarps, lane);
   block_partials<float>(acc, 0.f, 1, R.partials, S_RC, S_RC, R.nblk, R.rank);
   if (!group_reduce_sync(R.bar, P.st, P.limit_ns, R.partials, R.totals, S_RC, 1, R.nblk)) return false;
@@ -306,6 +304,8 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
   if constexpr (COARSE) {
     if (!converged) {  // p = D^-1 b + Z M Z^T b
       float rz_c = 0.f;
+      coarse_restrict(P.C, P.r32, gwarp, nwarps, lane);
+      if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
       if (!coarse_step(P, R, gwarp, nwarps, lane, &rz_c)) return;
       rz += rz_c;
       coarse_update_p(P.C, n0, n1, tid, nth, 0.f, P.r32, P.dinv32, P.p32, true);
@@ -341,12 +341,16 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
     }
     const float alpha = rz / pq;
     float rr_p = 0.f, rzn_p = 0.f;
-    for (int i = i0 + tid; i < nd; i += nth) {
-      P.x32[i] = fmaf(alpha, P.p32[i], P.x32[i]);
-      const float ri = fmaf(-alpha, P.q32[i], P.r32[i]);
-      P.r32[i] = ri;
-      rr_p = fmaf(ri, ri, rr_p);
-      rzn_p = fmaf(ri, ri * P.dinv32[i], rzn_p);
+    if constexpr (COARSE) {
+      coarse_update_restrict(P.C, alpha, P.x32, P.p32, P.q32, P.r32, P.dinv32, gwarp, nwarps, lane, rr_p, rzn_p);
+    } else {
+      for (int i = i0 + tid; i < nd; i += nth) {
+        P.x32[i] = fmaf(alpha, P.p32[i], P.x32[i]);
+        const float ri = fmaf(-alpha, P.q32[i], P.r32[i]);
+        P.r32[i] = ri;
+        rr_p = fmaf(ri, ri, rr_p);
+        rzn_p = fmaf(ri, ri * P.dinv32[i], rzn_p);
+      }
     }
     block_partials<float>(rr_p, rzn_p, 2, partials, S_RR, S_RZ, R.nblk, R.rank);
     if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk)) return;
@@ -397,6 +401,10 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
       if (residual <= P.tol * bnorm) {
         converged = true;
         break;
+      }
+      if constexpr (COARSE) {  // r was replaced: restrict it again
+        coarse_restrict(P.C, P.r32, gwarp, nwarps, lane);
+        if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
       }
     }
     if constexpr (COARSE) {

@@ -53,6 +53,8 @@ struct CoarseState {
   double* tmat = nullptr;        // [n_sub][6][6]
   float* minv = nullptr;         // [nc][ncp]
   float* part = nullptr;         // [n_chunks][6]
+  float* rc = nullptr;           // [ncp]
+  int* cnt = nullptr;            // [n_sub]
   float* yc = nullptr;           // [ncp]
   void release() {
     dev_free(sub_node);
@@ -63,6 +65,8 @@ struct CoarseState {
     dev_free(tmat);
     dev_free(minv);
     dev_free(part);
+    dev_free(rc);
+    dev_free(cnt);
     dev_free(yc);
   }
 };
@@ -781,6 +785,9 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     AXIA_CUDA(ctx, cudaGetLastError());
     if ((st = dev_alloc(ctx, &S->part, (size_t)6 * A.n_chunks))) break;
     if ((st = dev_alloc(ctx, &S->yc, (size_t)A.ncp))) break;
+    if ((st = dev_alloc(ctx, &S->rc, (size_t)A.ncp))) break;
+    if ((st = dev_alloc(ctx, &S->cnt, (size_t)n_sub))) break;
+    AXIA_CUDA(ctx, cudaMemsetAsync(S->rc, 0, A.ncp * sizeof(float), ctx->stream));
     if ((st = dev_alloc(ctx, &S->minv, (size_t)A.nc * A.ncp))) break;
     AXIA_CUDA(ctx, cudaMemsetAsync(S->yc, 0, A.ncp * sizeof(float), ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -790,6 +797,8 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     A.geo = S->geo;
     A.minv = S->minv;
     A.part = S->part;
+    A.rc = S->rc;
+    A.cnt = S->cnt;
     A.yc = S->yc;
   } while (false);
   if (d_temp) cudaFree(d_temp);
@@ -973,6 +982,8 @@ int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out) {
     AXIA_TRY(build_operator(ctx, S));
     S->op_gen = ctx->assemble_gen;
   }
+  // arrival counters of the restriction (a stopped solve may leave them set)
+  AXIA_CUDA(ctx, cudaMemsetAsync(S->cnt, 0, (size_t)S->args.n_sub * sizeof(int), ctx->stream));
   *out = S->args;
   return AXIA_OK;
 }

@@ -14,10 +14,14 @@
 //   z = D^-1 r + Z M Z^T r ,   M = (Z^T K Z)^+ ,
 // M in the raw mode basis (the per-subdomain orthonormalisation and the
 // dropped modes folded in at setup).  Per CG iteration that is three phases:
-//   restrict  partials of Z^T r over fixed chunks of each subdomain's node list
-//   solve     every block sums the partials into r_c (shared memory, fixed
-//             order), warps take rows of y = M r_c, and r_c . y = r . Z y
-//             (the coarse part of r . z) goes into a partial-sum slot
+//   restrict  inside the x / r update, which runs node by node over fixed
+//             chunks of each subdomain's node list: partials of Z^T r per
+//             chunk, summed in chunk order by the warp that finishes a
+//             subdomain's last chunk (after an FP64 residual replaced r, a
+//             separate pass does the same)
+//   solve     every block copies r_c to shared memory, warps take rows of
+//             y = M r_c, and r_c . y = r . Z y (the coarse part of r . z) goes
+//             into a partial-sum slot
 //   prolong   inside the search-direction update, one node per thread:
 //             p = D^-1 r + Z y + beta p
 // All sums run in a fixed order, so the solve stays bitwise reproducible.
@@ -34,54 +38,95 @@ int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out);
 
 __device__ __forceinline__ unsigned geo_bits(float4 g) { return __float_as_uint(g.w); }
 
-// Restriction partials: chunk c of subdomain I gets sum over its nodes of Z_a^T r_a.
+// Z_a^T r_a of one node added to v (r masked by the node's free DOFs)
+__device__ __forceinline__ void zt_add(float4 g, float rx, float ry, float rz, float (&v)[6]) {
+  v[0] += rx;
+  v[1] += ry;
+  v[2] += rz;
+  v[3] = fmaf(g.y, rz, fmaf(-g.z, ry, v[3]));
+  v[4] = fmaf(g.z, rx, fmaf(-g.x, rz, v[4]));
+  v[5] = fmaf(g.x, ry, fmaf(-g.y, rx, v[5]));
+}
+
+// Chunk c of subdomain I is done: its six sums go to part[c]; the warp that
+// finishes the last chunk of I adds the chunk sums in chunk order (the same
+// bits whichever warp that is) into r_c[6 I ..] and re-arms the counter.
+__device__ __forceinline__ void coarse_chunk_finish(const CoarseArgs& C, int c, int I, float (&v)[6], int lane) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) v[k] = warp_sum(v[k]);
+  if (lane < 6) {
+    const float x = lane == 0 ? v[0] : lane == 1 ? v[1] : lane == 2 ? v[2] : lane == 3 ? v[3] : lane == 4 ? v[4] : v[5];
+    C.part[6 * c + lane] = x;
+  }
+  __threadfence();
+  __syncwarp();
+  const int c0 = __ldg(C.chunk_ptr + I), c1 = __ldg(C.chunk_ptr + I + 1);
+  int last = 0;
+  if (lane == 0) last = atomicAdd(C.cnt + I, 1) == c1 - c0 - 1;
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (last) {
+    __threadfence();
+    if (lane < 6) {
+      float s = 0.f;
+      for (int k = c0; k < c1; ++k) s += __ldcg(C.part + 6 * k + lane);
+      C.rc[6 * I + lane] = s;
+    }
+    if (lane == 0) atomicExch(C.cnt + I, 0);
+  }
+}
+
+// r_c = Z^T r over the chunks (after an FP64 residual replaced r, and at the start)
 __device__ __forceinline__ void coarse_restrict(const CoarseArgs& C, const float* r, int gwarp, int nwarps,
                                                 int lane) {
   for (int c = gwarp; c < C.n_chunks; c += nwarps) {
     const int4 ch = C.chunk[c];
-    float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f, v4 = 0.f, v5 = 0.f;
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll 4
     for (int k = ch.y + lane; k < ch.z; k += 32) {
       const int a = __ldg(C.sub_node + k);
       const float4 g = __ldg(C.geo + a);
       const unsigned m = geo_bits(g);
-      const float rx = (m & 1u) ? r[3 * a] : 0.f;
-      const float ry = (m & 2u) ? r[3 * a + 1] : 0.f;
-      const float rz = (m & 4u) ? r[3 * a + 2] : 0.f;
-      v0 += rx;
-      v1 += ry;
-      v2 += rz;
-      v3 = fmaf(g.y, rz, fmaf(-g.z, ry, v3));
-      v4 = fmaf(g.z, rx, fmaf(-g.x, rz, v4));
-      v5 = fmaf(g.x, ry, fmaf(-g.y, rx, v5));
+      zt_add(g, (m & 1u) ? r[3 * a] : 0.f, (m & 2u) ? r[3 * a + 1] : 0.f, (m & 4u) ? r[3 * a + 2] : 0.f, v);
     }
-    v0 = warp_sum(v0);
-    v1 = warp_sum(v1);
-    v2 = warp_sum(v2);
-    v3 = warp_sum(v3);
-    v4 = warp_sum(v4);
-    v5 = warp_sum(v5);
-    if (lane < 6) {
-      const float v = lane == 0 ? v0 : lane == 1 ? v1 : lane == 2 ? v2 : lane == 3 ? v3 : lane == 4 ? v4 : v5;
-      C.part[6 * c + lane] = v;
-    }
+    coarse_chunk_finish(C, c, ch.x, v, lane);
   }
 }
 
-// r_c into shared memory (every block the same sums in the same order), then
-// rows of y = M r_c over the warps of the group.  Returns this thread's share
-// of r_c . y (nonzero on lane 0 of warps that own rows).
-__device__ __forceinline__ float coarse_solve(const CoarseArgs& C, float* s_rc, int gwarp, int nwarps, int lane) {
-  for (int t = threadIdx.x; t < C.ncp; t += blockDim.x) {
-    float s = 0.f;
-    if (t < C.nc) {
-      const int I = t / 6, i = t - 6 * I;
-      const int c1 = __ldg(C.chunk_ptr + I + 1);
-#pragma unroll 4
-      for (int c = __ldg(C.chunk_ptr + I); c < c1; ++c) s += C.part[6 * c + i];
+// The CG update x += alpha p, r -= alpha q node by node in subdomain order,
+// with the partial sums of r.r and r.D^-1 r and the restriction of the new r.
+__device__ __forceinline__ void coarse_update_restrict(const CoarseArgs& C, float alpha, float* x, const float* p,
+                                                       const float* q, float* r, const float* dinv, int gwarp,
+                                                       int nwarps, int lane, float& rr_p, float& rz_p) {
+  for (int c = gwarp; c < C.n_chunks; c += nwarps) {
+    const int4 ch = C.chunk[c];
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 2
+    for (int k = ch.y + lane; k < ch.z; k += 32) {
+      const int a = __ldg(C.sub_node + k);
+      const float4 g = __ldg(C.geo + a);
+      const unsigned m = geo_bits(g);
+      float rv[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int i = 3 * a + d;
+        x[i] = fmaf(alpha, p[i], x[i]);
+        const float ri = fmaf(-alpha, q[i], r[i]);
+        r[i] = ri;
+        rr_p = fmaf(ri, ri, rr_p);
+        rz_p = fmaf(ri, ri * dinv[i], rz_p);
+        rv[d] = ((m >> d) & 1u) ? ri : 0.f;
+      }
+      zt_add(g, rv[0], rv[1], rv[2], v);
     }
-    s_rc[t] = s;
+    coarse_chunk_finish(C, c, ch.x, v, lane);
   }
+}
+
+// r_c into shared memory, then rows of y = M r_c over the warps of the group.
+// Returns this thread's share of r_c . y (nonzero on lane 0 of warps that own rows).
+__device__ __forceinline__ float coarse_solve(const CoarseArgs& C, float* s_rc, int gwarp, int nwarps, int lane) {
+  for (int t = threadIdx.x; t < (C.ncp >> 2); t += blockDim.x)
+    reinterpret_cast<float4*>(s_rc)[t] = __ldcg(reinterpret_cast<const float4*>(C.rc) + t);
   __syncthreads();
   float acc = 0.f;
   const int nq = C.ncp >> 2;

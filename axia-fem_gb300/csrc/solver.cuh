@@ -114,6 +114,8 @@ struct CoarseArgs {
   const float4* geo;     // [n_nodes] (x_a - c_I) / h, .w = bits (I << 3 | free-DOF mask)
   const float* minv;     // [nc][ncp] M, zero in the padding
   float* part;           // [n_chunks][6] restriction partials
+  float* rc;             // [ncp] restricted residual Z^T r (zero in the padding)
+  int* cnt;              // [n_sub] chunks of each subdomain done (reset by the last)
   float* yc;             // [ncp] coarse correction y = M r_c
 };
 
