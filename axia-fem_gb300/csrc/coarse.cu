@@ -52,6 +52,20 @@ struct CoarseState {
   int* sub_ptr = nullptr;        // [n_sub + 1]
   double* tmat = nullptr;        // [n_sub][6][6]
   float* minv = nullptr;         // [nc][ncp]
+  // operator scratch, kept for the rebuilds after every assembly
+  int* off = nullptr;            // [n_nodes + 1] first item of each node row
+  unsigned* keys = nullptr;      // [n_items] subdomain pair I * n_sub + J
+  double* vals = nullptr;        // [n_items][36]
+  int* perm = nullptr;           // [n_items] items in (I, J) order (stable)
+  unsigned* run_key = nullptr;   // [n_runs]
+  int* run_off = nullptr;        // [n_runs]
+  int* run_cnt = nullptr;        // [n_runs]
+  int n_items = 0, n_runs = 0;
+  bool items_fresh = false;      // vals already hold the current K's items
+  double* a64 = nullptr;         // [ncp][ncp]
+  float* a32 = nullptr;          // [ncp][ncp] inverted in place
+  double* scale = nullptr;       // [ncp]
+  float* piv = nullptr;          // [GJ_T][GJ_T]
   float* part = nullptr;         // [n_chunks][6]
   float* rc = nullptr;           // [ncp]
   int* cnt = nullptr;            // [n_sub]
@@ -64,6 +78,17 @@ struct CoarseState {
     dev_free(sub_ptr);
     dev_free(tmat);
     dev_free(minv);
+    dev_free(off);
+    dev_free(keys);
+    dev_free(vals);
+    dev_free(perm);
+    dev_free(run_key);
+    dev_free(run_off);
+    dev_free(run_cnt);
+    dev_free(a64);
+    dev_free(a32);
+    dev_free(scale);
+    dev_free(piv);
     dev_free(part);
     dev_free(rc);
     dev_free(cnt);
@@ -515,38 +540,58 @@ __global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P) {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   auto tile = [&](int i, int j) { return P.A + (size_t)i * GJ_T * ld + (size_t)j * GJ_T; };
   for (int k = 0; k < nt; ++k) {
-    // 1. block 0 stores the previous P and inverts tile (k, k) (double-buffered
-    //    in-place Gauss-Jordan, one barrier per pivot); the other blocks write
-    //    the previous step's column panel
+    // 1. block 0 stores the previous P and inverts tile (k, k) (in-place
+    //    Gauss-Jordan in registers); the other blocks write the previous
+    //    step's column panel
     if (blockIdx.x == 0) {
       if (k > 0)
         for (int t = threadIdx.x; t < GJ_T * GJ_T; t += blockDim.x)
           tile(k - 1, k - 1)[(size_t)(t / GJ_T) * ld + t % GJ_T] = P.piv[t];
-      gj_load(sa, tile(k, k), ld);
-      float (*cur)[GJ_LD] = sa;
-      float (*nxt)[GJ_LD] = sb;
+      // thread (ty, tx) keeps rows 4ty.., columns 4tx.. of the tile in
+      // registers; per pivot the owners publish row p and column p
+      // (double-buffered, one barrier per pivot)
+      float a[4][4];
+      const float* src = tile(k, k);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const float4 v = *reinterpret_cast<const float4*>(src + (size_t)(4 * ty + r) * ld + 4 * tx);
+        a[r][0] = v.x;
+        a[r][1] = v.y;
+        a[r][2] = v.z;
+        a[r][3] = v.w;
+      }
+      float* srow = &sa[0][0];  // [2][GJ_T]
+      float* scol = &sb[0][0];  // [2][GJ_T]
       for (int p = 0; p < GJ_T; ++p) {
+        const int b = (p & 1) * GJ_T, po = p >> 2, pi = p & 3;
+        if (ty == po)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) srow[b + 4 * tx + c] = a[pi][c];
+        if (tx == po)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) scol[b + 4 * ty + r] = a[r][pi];
         __syncthreads();
-        const float piv = cur[p][p];
+        const float piv = srow[b + p];
         if (threadIdx.x == 0 && (!(piv > 0.f) || !isfinite(piv))) record_error(P.st, k * GJ_T + p, AXIA_ERR_ZERO_PIVOT);
         const float d = 1.0f / piv;
+        float rv[4], cv[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) rv[c] = srow[b + 4 * tx + c];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) cv[r] = scol[b + 4 * ty + r] * d;
 #pragma unroll
         for (int r = 0; r < 4; ++r)
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
-            const int i = 4 * ty + r, j = 4 * tx + c;
-            float v;
-            if (i == p) v = j == p ? d : cur[p][j] * d;
-            else if (j == p) v = -cur[i][p] * d;
-            else v = fmaf(-cur[i][p] * d, cur[p][j], cur[i][j]);
-            nxt[i][j] = v;
+            const bool ip = 4 * ty + r == p, jp = 4 * tx + c == p;
+            a[r][c] = ip ? (jp ? d : rv[c] * d) : (jp ? -cv[r] : fmaf(-cv[r], rv[c], a[r][c]));
           }
-        float (*t)[GJ_LD] = cur;
-        cur = nxt;
-        nxt = t;
       }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) P.piv[(4 * ty + r) * GJ_T + 4 * tx + c] = a[r][c];
       __syncthreads();
-      for (int t = threadIdx.x; t < GJ_T * GJ_T; t += blockDim.x) P.piv[t] = cur[t / GJ_T][t % GJ_T];
     } else if (k > 0) {
       gj_column_panel(P, k - 1, blockIdx.x - 1, gridDim.x - 1);
     }
@@ -812,139 +857,153 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
   return st;
 }
 
-// coarse operator and its inverse from the assembled FP64 node-block matrix
-int build_operator(axia_ctx* ctx, CoarseState* S) {
+// Items of the node rows and their runs: they depend on the subdomains and
+// the constraints only, so they are built once per space.
+int build_item_structure(axia_ctx* ctx, CoarseState* S) {
   CoarseArgs& A = S->args;
-  const int n = (int)ctx->n_nodes, n_sub = A.n_sub, nc = A.nc, ncp = A.ncp;
-  const BsrMat<double> K{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq};
-  int *d_cnt = nullptr, *d_off = nullptr, *d_iota = nullptr, *d_perm = nullptr, *d_run_off = nullptr,
-      *d_run_cnt = nullptr, *d_nruns = nullptr;
-  unsigned *d_keys = nullptr, *d_keys_sorted = nullptr, *d_run_key = nullptr;
-  double *d_vals = nullptr, *d_a64 = nullptr, *d_scale = nullptr;
-  float *d_a32 = nullptr, *d_piv = nullptr;
+  const int n = (int)ctx->n_nodes, n_sub = A.n_sub;
+  int *d_cnt = nullptr, *d_iota = nullptr, *d_nruns = nullptr;
+  unsigned* d_keys_sorted = nullptr;
   void* d_temp = nullptr;
   int st = AXIA_OK;
   do {
-    AXIA_TRY(reset_dev_status(ctx));
+    if ((st = reset_dev_status(ctx))) break;
     if ((st = dev_alloc(ctx, &d_cnt, (size_t)n + 1))) break;
-    if ((st = dev_alloc(ctx, &d_off, (size_t)n + 1))) break;
+    if ((st = dev_alloc(ctx, &S->off, (size_t)n + 1))) break;
     AXIA_CUDA(ctx, cudaMemsetAsync(d_cnt + n, 0, sizeof(int), ctx->stream));
     k_row_count<<<grid_for(ctx, (int64_t)n * 32, 256), 256, 0, ctx->stream>>>(n, ctx->d_qptr, ctx->d_qadj, A.geo,
                                                                              d_cnt, ctx->d_status);
     ctx->launches++;
     if ((st = read_status(ctx, "a node row touches more than 32 subdomains (raise coarse_nodes)"))) break;
     size_t tb = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, tb, d_cnt, d_off, n + 1, ctx->stream);
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, d_cnt, S->off, n + 1, ctx->stream);
     AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
-    AXIA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(d_temp, tb, d_cnt, d_off, n + 1, ctx->stream));
-    int n_items = 0;
-    if ((st = copy_to_host(ctx, &n_items, d_off + n, 1))) break;
+    AXIA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(d_temp, tb, d_cnt, S->off, n + 1, ctx->stream));
+    if ((st = copy_to_host(ctx, &S->n_items, S->off + n, 1))) break;
     cudaFree(d_temp);
     d_temp = nullptr;
-    if ((st = dev_alloc(ctx, &d_keys, (size_t)n_items))) break;
-    if ((st = dev_alloc(ctx, &d_keys_sorted, (size_t)n_items))) break;
-    if ((st = dev_alloc(ctx, &d_vals, (size_t)n_items * 36))) break;
-    if ((st = dev_alloc(ctx, &d_iota, (size_t)n_items))) break;
-    if ((st = dev_alloc(ctx, &d_perm, (size_t)n_items))) break;
+    const int ni = std::max(S->n_items, 1);
+    if ((st = dev_alloc(ctx, &S->keys, (size_t)ni))) break;
+    if ((st = dev_alloc(ctx, &d_keys_sorted, (size_t)ni))) break;
+    if ((st = dev_alloc(ctx, &S->vals, (size_t)ni * 36))) break;
+    if ((st = dev_alloc(ctx, &d_iota, (size_t)ni))) break;
+    if ((st = dev_alloc(ctx, &S->perm, (size_t)ni))) break;
+    const BsrMat<double> K{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq};
     k_row_items<<<grid_for(ctx, (int64_t)n * 32, 32 * ROW_WARPS), 32 * ROW_WARPS, 0, ctx->stream>>>(
-        n, n_sub, K, A.geo, d_off, d_keys, d_vals);
+        n, n_sub, K, A.geo, S->off, S->keys, S->vals);
     ctx->launches++;
     AXIA_CUDA(ctx, cudaGetLastError());
     {
-      std::vector<int> iota(n_items);
-      for (int i = 0; i < n_items; ++i) iota[i] = i;
-      if ((st = copy_to_device(ctx, d_iota, iota.data(), (size_t)n_items))) break;
+      std::vector<int> iota(ni);
+      for (int i = 0; i < ni; ++i) iota[i] = i;
+      if ((st = copy_to_device(ctx, d_iota, iota.data(), (size_t)ni))) break;
     }
     int bits = 1;
     while ((1ull << bits) < (unsigned long long)n_sub * n_sub && bits < 32) ++bits;
-    cub::DeviceRadixSort::SortPairs(nullptr, tb, d_keys, d_keys_sorted, d_iota, d_perm, n_items, 0, bits,
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, S->keys, d_keys_sorted, d_iota, S->perm, S->n_items, 0, bits,
                                     ctx->stream);
     AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
-    AXIA_CUDA(ctx, cub::DeviceRadixSort::SortPairs(d_temp, tb, d_keys, d_keys_sorted, d_iota, d_perm, n_items, 0,
-                                                   bits, ctx->stream));
+    AXIA_CUDA(ctx, cub::DeviceRadixSort::SortPairs(d_temp, tb, S->keys, d_keys_sorted, d_iota, S->perm, S->n_items,
+                                                   0, bits, ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     cudaFree(d_temp);
     d_temp = nullptr;
-    if ((st = dev_alloc(ctx, &d_run_key, (size_t)n_items))) break;
-    if ((st = dev_alloc(ctx, &d_run_cnt, (size_t)n_items))) break;
-    if ((st = dev_alloc(ctx, &d_run_off, (size_t)n_items))) break;
+    if ((st = dev_alloc(ctx, &S->run_key, (size_t)ni))) break;
+    if ((st = dev_alloc(ctx, &S->run_cnt, (size_t)ni))) break;
+    if ((st = dev_alloc(ctx, &S->run_off, (size_t)ni))) break;
     if ((st = dev_alloc(ctx, &d_nruns, 1))) break;
-    cub::DeviceRunLengthEncode::Encode(nullptr, tb, d_keys_sorted, d_run_key, d_run_cnt, d_nruns, n_items,
+    cub::DeviceRunLengthEncode::Encode(nullptr, tb, d_keys_sorted, S->run_key, S->run_cnt, d_nruns, S->n_items,
                                        ctx->stream);
     AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
-    AXIA_CUDA(ctx, cub::DeviceRunLengthEncode::Encode(d_temp, tb, d_keys_sorted, d_run_key, d_run_cnt, d_nruns,
-                                                      n_items, ctx->stream));
-    int n_runs = 0;
-    if ((st = copy_to_host(ctx, &n_runs, d_nruns, 1))) break;
+    AXIA_CUDA(ctx, cub::DeviceRunLengthEncode::Encode(d_temp, tb, d_keys_sorted, S->run_key, S->run_cnt, d_nruns,
+                                                      S->n_items, ctx->stream));
+    if ((st = copy_to_host(ctx, &S->n_runs, d_nruns, 1))) break;
     cudaFree(d_temp);
     d_temp = nullptr;
-    cub::DeviceScan::ExclusiveSum(nullptr, tb, d_run_cnt, d_run_off, n_runs, ctx->stream);
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, S->run_cnt, S->run_off, S->n_runs, ctx->stream);
     AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
-    AXIA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(d_temp, tb, d_run_cnt, d_run_off, n_runs, ctx->stream));
-    if ((st = dev_alloc(ctx, &d_a64, (size_t)ncp * ncp))) break;
-    AXIA_CUDA(ctx, cudaMemsetAsync(d_a64, 0, (size_t)ncp * ncp * sizeof(double), ctx->stream));
-    k_run_sum<<<grid_for(ctx, (int64_t)n_runs * 32, 256), 256, 0, ctx->stream>>>(
-        n_runs, n_sub, d_run_key, d_run_off, d_run_cnt, d_perm, d_vals, S->tmat, d_a64, ncp);
-    ctx->launches++;
-    AXIA_CUDA(ctx, cudaGetLastError());
-    // unit-diagonal scaling; modes without stiffness (dropped or padding) become identity
-    std::vector<double> diag(ncp), scale(ncp, 0.0);
-    AXIA_CUDA(ctx, cudaMemcpy2DAsync(diag.data(), sizeof(double), d_a64, (size_t)(ncp + 1) * sizeof(double),
-                                     sizeof(double), ncp, cudaMemcpyDeviceToHost, ctx->stream));
+    AXIA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(d_temp, tb, S->run_cnt, S->run_off, S->n_runs, ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    double dmax = 0.0;
-    for (int i = 0; i < nc; ++i) dmax = std::max(dmax, std::isfinite(diag[i]) ? diag[i] : 0.0);
-    for (int i = 0; i < nc; ++i)
-      if (diag[i] > 1e-12 * dmax && std::isfinite(diag[i])) scale[i] = 1.0 / std::sqrt(diag[i]);
-    if ((st = dev_alloc(ctx, &d_scale, (size_t)ncp))) break;
-    if ((st = copy_to_device(ctx, d_scale, scale.data(), (size_t)ncp))) break;
-    if ((st = dev_alloc(ctx, &d_a32, (size_t)ncp * ncp))) break;
-    k_scale_to_f32<<<grid_for(ctx, (int64_t)ncp * ncp, 256), 256, 0, ctx->stream>>>(ncp, d_a64, d_scale, d_a32);
-    ctx->launches++;
-    dev_free(d_a64);
-    // in-place inverse
-    if ((st = dev_alloc(ctx, &d_piv, (size_t)GJ_T * GJ_T))) break;
-    {
-      int per_sm = 0;
-      AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_inverse, GJ_THREADS, 0));
-      if (per_sm < 1) {
-        st = set_error(ctx, AXIA_ERR_CUDA, "coarse space: inverse kernel does not fit");
-        break;
-      }
-      const int nt = ncp / GJ_T;
-      const int grid = std::max(2, std::min(std::min(per_sm, 2) * ctx->sm_count, std::max(2, nt * (nt - 1) / 2)));
-      AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
-      GjArgs P{d_a32, ncp, d_piv, ctx->d_bar, ctx->d_status, 2000000000ull};
-      void* params[] = {&P};
-      AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_gj_inverse, dim3(grid), dim3(GJ_THREADS), params, 0,
-                                                 ctx->stream));
-      ctx->launches++;
-    }
-    if ((st = read_status(ctx, "coarse operator is not positive definite"))) break;
-    AXIA_CUDA(ctx, cudaMemsetAsync(S->minv, 0, (size_t)nc * ncp * sizeof(float), ctx->stream));
-    k_minv<<<grid_for(ctx, (int64_t)n_sub * n_sub, 128), 128, 0, ctx->stream>>>(n_sub, ncp, d_a32, d_scale, S->tmat,
-                                                                               S->minv);
-    ctx->launches++;
-    AXIA_CUDA(ctx, cudaGetLastError());
-    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const size_t ncp = (size_t)A.ncp;
+    if ((st = dev_alloc(ctx, &S->a64, ncp * ncp))) break;
+    if ((st = dev_alloc(ctx, &S->a32, ncp * ncp))) break;
+    if ((st = dev_alloc(ctx, &S->scale, ncp))) break;
+    if ((st = dev_alloc(ctx, &S->piv, (size_t)GJ_T * GJ_T))) break;
+    S->items_fresh = true;  // the values of this pass belong to the current K
   } while (false);
   if (d_temp) cudaFree(d_temp);
   dev_free(d_cnt);
-  dev_free(d_off);
   dev_free(d_iota);
-  dev_free(d_perm);
-  dev_free(d_run_off);
-  dev_free(d_run_cnt);
   dev_free(d_nruns);
-  dev_free(d_keys);
   dev_free(d_keys_sorted);
-  dev_free(d_run_key);
-  dev_free(d_vals);
-  dev_free(d_a64);
-  dev_free(d_scale);
-  dev_free(d_a32);
-  dev_free(d_piv);
   return st;
+}
+
+// s_i = 1 / sqrt(A_ii) for the coarse unknowns whose diagonal is positive
+// (above 1e-12 of the largest), 0 for the rest and the padding (one block)
+__global__ void k_diag_scale(int nc, int ncp, const double* A, double* scale) {
+  __shared__ double red[32];
+  double m = 0.0;
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+    const double d = A[(size_t)i * ncp + i];
+    if (isfinite(d)) m = fmax(m, d);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) red[0] = m;
+  }
+  __syncthreads();
+  const double dmax = red[0];
+  for (int i = threadIdx.x; i < ncp; i += blockDim.x) {
+    const double d = i < nc ? A[(size_t)i * ncp + i] : 0.0;
+    scale[i] = (i < nc && isfinite(d) && d > 1e-12 * dmax) ? 1.0 / sqrt(d) : 0.0;
+  }
+}
+
+// coarse operator and its inverse from the assembled FP64 node-block matrix
+int build_operator(axia_ctx* ctx, CoarseState* S) {
+  CoarseArgs& A = S->args;
+  const int n = (int)ctx->n_nodes, n_sub = A.n_sub, nc = A.nc, ncp = A.ncp;
+  const BsrMat<double> K{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq};
+  if (!S->off) AXIA_TRY(build_item_structure(ctx, S));
+  if (!S->items_fresh) {
+    k_row_items<<<grid_for(ctx, (int64_t)n * 32, 32 * ROW_WARPS), 32 * ROW_WARPS, 0, ctx->stream>>>(
+        n, n_sub, K, A.geo, S->off, S->keys, S->vals);
+    ctx->launches++;
+  }
+  S->items_fresh = false;
+  AXIA_CUDA(ctx, cudaMemsetAsync(S->a64, 0, (size_t)ncp * ncp * sizeof(double), ctx->stream));
+  k_run_sum<<<grid_for(ctx, (int64_t)S->n_runs * 32, 256), 256, 0, ctx->stream>>>(
+      S->n_runs, n_sub, S->run_key, S->run_off, S->run_cnt, S->perm, S->vals, S->tmat, S->a64, ncp);
+  // unit-diagonal scaling; modes without stiffness (dropped or padding) become identity
+  k_diag_scale<<<1, 1024, 0, ctx->stream>>>(nc, ncp, S->a64, S->scale);
+  k_scale_to_f32<<<grid_for(ctx, (int64_t)ncp * ncp, 256), 256, 0, ctx->stream>>>(ncp, S->a64, S->scale, S->a32);
+  ctx->launches += 3;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  AXIA_TRY(reset_dev_status(ctx));
+  {
+    int per_sm = 0;
+    AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_inverse, GJ_THREADS, 0));
+    if (per_sm < 1) return set_error(ctx, AXIA_ERR_CUDA, "coarse space: inverse kernel does not fit");
+    const int nt = ncp / GJ_T;
+    const int grid = std::max(2, std::min(std::min(per_sm, 2) * ctx->sm_count, std::max(2, nt * (nt - 1) / 2)));
+    AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
+    GjArgs P{S->a32, ncp, S->piv, ctx->d_bar, ctx->d_status, 2000000000ull};
+    void* params[] = {&P};
+    AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_gj_inverse, dim3(grid), dim3(GJ_THREADS), params, 0,
+                                               ctx->stream));
+    ctx->launches++;
+  }
+  AXIA_CUDA(ctx, cudaMemsetAsync(S->minv, 0, (size_t)nc * ncp * sizeof(float), ctx->stream));
+  k_minv<<<grid_for(ctx, (int64_t)n_sub * n_sub, 128), 128, 0, ctx->stream>>>(n_sub, ncp, S->a32, S->scale, S->tmat,
+                                                                             S->minv);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  return read_status(ctx, "coarse operator is not positive definite");
 }
 
 }  // namespace

@@ -239,20 +239,36 @@ def run_c3(args):
         return ctx.solve_device(f.data_ptr(), umx.data_ptr(), rtol=RTOL, precision=L.PREC_MIXED,
                                 refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta, matrix_format=L.FORMAT_BSR3,
                                 spmv_lanes=args.lanes32)
+    uco = torch.empty_like(f)
+
+    def stepco():
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        return ctx.solve_device(f.data_ptr(), uco.data_ptr(), rtol=RTOL, precision=L.PREC_MIXED,
+                                refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta, matrix_format=L.FORMAT_BSR3,
+                                spmv_lanes=args.lanes32, preconditioner=L.PRECOND_COARSE,
+                                coarse_nodes=args.coarse_nodes)
     ms64, i64 = timer(step64, args.warmup, args.steps)
     msmx, imx = timer(stepmx, args.warmup, args.steps)
+    msco, ico = timer(stepco, args.warmup, args.steps)
     rel = float(torch.linalg.norm(umx - u64) / torch.linalg.norm(u64))
+    relco = float(torch.linalg.norm(uco - u64) / torch.linalg.norm(u64))
     nf = ctx.n_free
+    n_sub, n_coarse = ctx.coarse_size()
     _line(args, f"C3D20 block {n}^3, 27-point Gauss, E=70000 nu=0.33, base clamped, top traction N(0,1)",
-          nf / (msmx * 1e-3) / 1e6, msmx,
+          nf / (msco * 1e-3) / 1e6, msco,
           {"dtype": "f32+f64", "config": {"workload": f"C3D20 {n}^3", "n_free": nf, "nnz_kff": ctx.nnz,
-                                          "node_blocks": ctx.n_blocks(), "rtol": RTOL},
+                                          "node_blocks": ctx.n_blocks(), "rtol": RTOL,
+                                          "preconditioner": f"diagonal + coarse space ({n_sub} subdomains)"},
+           "mixed_coarse": {"ms_per_step": msco, "inner_iters": ico.iters, "reliable_updates": ico.outer_iters,
+                            "ms_assemble": ico.ms_assemble, "ms_pcg_kernel": ico.ms_pcg_kernel,
+                            "true_rel_residual": ico.true_residual / ico.bnorm, "rel_err_vs_fp64": relco,
+                            "subdomains": n_sub, "coarse_unknowns": n_coarse},
            "fp64": {"value": nf / (ms64 * 1e-3) / 1e6, "ms_per_step": ms64, "iters": i64.iters,
                     "ms_assemble": i64.ms_assemble, "true_rel_residual": i64.true_residual / i64.bnorm},
            "mixed": {"ms_per_step": msmx, "inner_iters": imx.iters, "reliable_updates": imx.outer_iters,
                      "ms_assemble": imx.ms_assemble, "true_rel_residual": imx.true_residual / imx.bnorm,
                      "rel_err_vs_fp64": rel},
-           "speedup_mixed_vs_fp64": ms64 / msmx})
+           "speedup_mixed_vs_fp64": ms64 / msco, "speedup_mixed_jacobi_vs_fp64": ms64 / msmx})
 
 
 def run_c4a(args):
