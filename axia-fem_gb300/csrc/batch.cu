@@ -13,7 +13,7 @@
 #include <algorithm>
 #include <cmath>
 
-#include "solver.cuh"
+#include "coarse.cuh"
 
 namespace {
 
@@ -218,10 +218,154 @@ struct MultiArgs {
   double delta;
   long long max_iter;
   unsigned long long limit_ns;
+  CoarseArgs C;         // two-level preconditioner (n_sub = 0: Jacobi only)
 };
 
 constexpr int SL_A = 0, SL_B = NR;  // two banks of NR slots
 
+// ---------------------------------------------------------------------------
+// Two-level preconditioner for 32 columns (the single-column form is in
+// coarse.cuh): restriction per chunk of a subdomain's nodes with four 8-lane
+// groups taking four nodes at a time (lane cl of a group: columns 4cl..4cl+3),
+// the last warp of a subdomain summing its chunk partials in chunk order;
+// y = M r_c as tasks (row, column quad) with lanes over the coarse unknowns;
+// the prolongation inside the search-direction update.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void coarse_restrict_m(const CoarseArgs& C, const float* R, int gwarp, int nwarps,
+                                                  int lane) {
+  const int cl = lane % LPG, grp = lane / LPG;
+  for (int ci = gwarp; ci < C.n_chunks; ci += nwarps) {
+    const int4 ch = C.chunk[ci];
+    float v[6][CPL];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) v[i][c] = 0.f;
+#pragma unroll 2
+    for (int k = ch.y + grp; k < ch.z; k += 32 / LPG) {
+      const int a = __ldg(C.sub_node + k);
+      const float4 g = __ldg(C.geo + a);
+      const unsigned m = geo_bits(g);
+      float r[3][CPL];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        if ((m >> d) & 1u) {
+          ld4(R + (size_t)(3 * a + d) * NR + CPL * cl, r[d]);
+        } else {
+#pragma unroll
+          for (int c = 0; c < CPL; ++c) r[d][c] = 0.f;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        v[0][c] += r[0][c];
+        v[1][c] += r[1][c];
+        v[2][c] += r[2][c];
+        v[3][c] = fmaf(g.y, r[2][c], fmaf(-g.z, r[1][c], v[3][c]));
+        v[4][c] = fmaf(g.z, r[0][c], fmaf(-g.x, r[2][c], v[4][c]));
+        v[5][c] = fmaf(g.x, r[1][c], fmaf(-g.y, r[0][c], v[5][c]));
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        v[i][c] += __shfl_xor_sync(0xffffffffu, v[i][c], 8);
+        v[i][c] += __shfl_xor_sync(0xffffffffu, v[i][c], 16);
+      }
+    if (grp == 0)
+#pragma unroll
+      for (int i = 0; i < 6; ++i) st4(C.part_m + ((size_t)ci * 6 + i) * NR + CPL * cl, v[i]);
+    __threadfence();
+    __syncwarp();
+    const int I = ch.x, c0 = __ldg(C.chunk_ptr + I), c1 = __ldg(C.chunk_ptr + I + 1);
+    int last = 0;
+    if (lane == 0) last = atomicAdd(C.cnt + I, 1) == c1 - c0 - 1;
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (last) {
+      __threadfence();
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        float sum = 0.f;
+        for (int k = c0; k < c1; ++k) sum += __ldcg(C.part_m + ((size_t)k * 6 + i) * NR + lane);
+        C.rc_m[(size_t)(6 * I + i) * NR + lane] = sum;
+      }
+      if (lane == 0) atomicExch(C.cnt + I, 0);
+    }
+  }
+}
+
+// Y = M R_c; per column r_c . y into partials[(slot0 + col) * G + block]
+__device__ __forceinline__ void coarse_solve_m(const CoarseArgs& C, int gwarp, int nwarps, int lane, double* partials,
+                                               int slot0) {
+  __shared__ float s_cc[PCG_THREADS / 32][NR];
+  const int warp = threadIdx.x >> 5;
+  s_cc[warp][lane] = 0.f;
+  __syncwarp();
+  const int ntask = C.nc * LPG;
+  for (int t = gwarp; t < ntask; t += nwarps) {
+    const int i = t / LPG, cq = t - i * LPG;
+    const float* mrow = C.minv + (size_t)i * C.ncp;
+    float acc[CPL] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+    for (int j = lane; j < C.nc; j += 32) {
+      const float mv = __ldg(mrow + j);
+      float rv[CPL];
+      ld4(C.rc_m + (size_t)j * NR + CPL * cq, rv);
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) acc[c] = fmaf(mv, rv[c], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) acc[c] = warp_sum(acc[c]);
+    if (lane == 0) {
+      st4(C.yc_m + (size_t)i * NR + CPL * cq, acc);
+      float rv[CPL];
+      ld4(C.rc_m + (size_t)i * NR + CPL * cq, rv);
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) s_cc[warp][CPL * cq + c] = fmaf(rv[c], acc[c], s_cc[warp][CPL * cq + c]);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  if (threadIdx.x < NR) {
+    double sum = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += s_cc[w][threadIdx.x];
+    partials[(size_t)(slot0 + threadIdx.x) * gridDim.x + blockIdx.x] = sum;
+  }
+}
+
+// coarse part of z at DOF row `row`, columns c0..c0+3
+__device__ __forceinline__ void coarse_prolong_m(const CoarseArgs& C, long long row, int c0, float zc[CPL]) {
+  const int a = (int)(row / 3), d = (int)(row - 3LL * a);
+  const float4 g = __ldg(C.geo + a);
+  const unsigned m = geo_bits(g);
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) zc[c] = 0.f;
+  if (!((m >> d) & 1u)) return;
+  const float* Y = C.yc_m + (size_t)(6 * (m >> 3)) * NR + c0;
+  float t[CPL], u[CPL], w[CPL];
+  float cu, cw;
+  if (d == 0) {
+    ld4(Y, t), ld4(Y + 4 * NR, u), ld4(Y + 5 * NR, w), cu = g.z, cw = -g.y;
+  } else if (d == 1) {
+    ld4(Y + NR, t), ld4(Y + 3 * NR, u), ld4(Y + 5 * NR, w), cu = -g.z, cw = g.x;
+  } else {
+    ld4(Y + 2 * NR, t), ld4(Y + 3 * NR, u), ld4(Y + 4 * NR, w), cu = g.y, cw = -g.x;
+  }
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) zc[c] = fmaf(cu, u[c], fmaf(cw, w[c], t[c]));
+}
+
+// the coarse half of the preconditioner for the current R32: restriction,
+// barrier, Y = M R_c and the per-column r . Z y reduced into totals[SL_A..]
+__device__ __forceinline__ bool coarse_step_m(const MultiArgs& P, int gwarp, int nwarps, int lane) {
+  coarse_restrict_m(P.C, P.R32, gwarp, nwarps, lane);
+  if (!grid_sync(P.bar, P.st, P.limit_ns)) return false;
+  coarse_solve_m(P.C, gwarp, nwarps, lane, P.partials, SL_A);
+  return grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, SL_A, NR);
+}
+
+template <bool COARSE>
 __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs P) {
   __shared__ double s_rz[NR], s_bnorm[NR], s_rmax[NR], s_res[NR];
   __shared__ float s_alpha[NR], s_beta[NR];
@@ -273,6 +417,19 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
     if (!s_active[c]) s_res[c] = 0.0;
   }
   __syncthreads();
+  if constexpr (COARSE) {  // P = D^-1 B + Z M Z^T B
+    if (!coarse_step_m(P, gwarp, nwarps, lane)) return;
+    if (threadIdx.x < NR) s_rz[threadIdx.x] += __ldcg(P.totals + SL_A + threadIdx.x);
+    for (long long q = tid; q < nq; q += nth) {
+      float p[CPL], zc[CPL];
+      ld4(P.P32 + q * CPL, p);
+      coarse_prolong_m(P.C, q / LPG, CPL * (int)(q % LPG), zc);
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) p[c] += zc[c];
+      st4(P.P32 + q * CPL, p);
+    }
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+  }
   long long iters = 0;
   int updates = 0, status = AXIA_OK;
   for (long long it = 0; it < P.max_iter; ++it) {
@@ -408,9 +565,13 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
       }
       __syncthreads();
     }
+    if constexpr (COARSE) {
+      if (!coarse_step_m(P, gwarp, nwarps, lane)) return;
+    }
     if (threadIdx.x < NR) {
       const int c = threadIdx.x;
-      const double rzn = __ldcg(P.totals + SL_B + c);
+      double rzn = __ldcg(P.totals + SL_B + c);
+      if constexpr (COARSE) rzn += __ldcg(P.totals + SL_A + c);
       s_beta[c] = s_active[c] ? (float)(rzn / s_rz[c]) : 0.f;
       s_rz[c] = rzn;
     }
@@ -418,12 +579,14 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
     for (long long q = tid; q < nq; q += nth) {
       const long long row = q / LPG;
       const int c0 = CPL * (int)(q % LPG);
-      float p[CPL], r[CPL];
+      float p[CPL], r[CPL], zc[CPL] = {0.f, 0.f, 0.f, 0.f};
       ld4(P.P32 + q * CPL, p);
       ld4(P.R32 + q * CPL, r);
+      if constexpr (COARSE) coarse_prolong_m(P.C, row, c0, zc);
       const float di = P.dinv32[row];
 #pragma unroll
-      for (int c = 0; c < CPL; ++c) p[c] = s_active[c0 + c] ? fmaf(s_beta[c0 + c], p[c], r[c] * di) : 0.f;
+      for (int c = 0; c < CPL; ++c)
+        p[c] = s_active[c0 + c] ? fmaf(s_beta[c0 + c], p[c], fmaf(r[c], di, zc[c])) : 0.f;
       st4(P.P32 + q * CPL, p);
     }
     if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
@@ -490,11 +653,14 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
     AXIA_TRY(dev_alloc(ctx, &o, 1));
     ctx->d_mout = o;
   }
-  if (opts->preconditioner != AXIA_PRECOND_JACOBI)
-    return set_error(ctx, AXIA_ERR_INVALID_ARG, "batched load cases: Jacobi preconditioner only");
+  if (opts->preconditioner != AXIA_PRECOND_JACOBI && opts->preconditioner != AXIA_PRECOND_COARSE)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "batched load cases: unknown preconditioner");
+  const bool coarse = opts->preconditioner == AXIA_PRECOND_COARSE;
+  CoarseArgs cargs{};
+  if (coarse) AXIA_TRY(coarse_prepare_batched(ctx, opts->coarse_nodes, &cargs));
   const long long max_iter = opts->max_iter > 0 ? opts->max_iter : std::max<long long>(4LL * ctx->n_free, 200);
   const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.01;
-  auto kern = pcg_bsr_multi_kernel;
+  auto kern = coarse ? pcg_bsr_multi_kernel<true> : pcg_bsr_multi_kernel<false>;
   int grid = 0;
   AXIA_TRY(coop_grid(ctx, (const void*)kern, (int)std::min<int64_t>(nd, INT32_MAX), &grid));
   if ((size_t)grid * 2 * NR > ctx->partial_slots) grid = (int)(ctx->partial_slots / (2 * NR));
@@ -512,7 +678,7 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
                 BsrMatM<double>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq},
                 (int)nd, ctx->d_bdinv32, ctx->d_mB, ctx->d_mX, ctx->d_mX32, ctx->d_mR32, ctx->d_mP32, ctx->d_mQ32,
                 ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (MultiOut*)ctx->d_mout, opts->rtol, delta,
-                max_iter, 2000000000ull};
+                max_iter, 2000000000ull, cargs};
     AXIA_TRY(timed_launch(ctx, info, [&]() -> int {
       void* params[] = {&P};
       AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params, 0,

@@ -69,6 +69,9 @@ struct CoarseState {
   float* part = nullptr;         // [n_chunks][6]
   float* rc = nullptr;           // [ncp]
   int* cnt = nullptr;            // [n_sub]
+  float* part_m = nullptr;       // [n_chunks][6][32] (batched solve)
+  float* rc_m = nullptr;         // [ncp][32]
+  float* yc_m = nullptr;         // [ncp][32]
   float* yc = nullptr;           // [ncp]
   void release() {
     dev_free(sub_node);
@@ -89,6 +92,9 @@ struct CoarseState {
     dev_free(a32);
     dev_free(scale);
     dev_free(piv);
+    dev_free(part_m);
+    dev_free(rc_m);
+    dev_free(yc_m);
     dev_free(part);
     dev_free(rc);
     dev_free(cnt);
@@ -1043,6 +1049,24 @@ int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out) {
   }
   // arrival counters of the restriction (a stopped solve may leave them set)
   AXIA_CUDA(ctx, cudaMemsetAsync(S->cnt, 0, (size_t)S->args.n_sub * sizeof(int), ctx->stream));
+  *out = S->args;
+  return AXIA_OK;
+}
+
+// The same, plus the 32-column buffers of the batched solve.
+int coarse_prepare_batched(axia_ctx* ctx, int nodes_target, CoarseArgs* out) {
+  AXIA_TRY(coarse_prepare(ctx, nodes_target, out));
+  auto* S = static_cast<CoarseState*>(ctx->coarse);
+  if (!S->part_m) {
+    AXIA_TRY(dev_alloc(ctx, &S->part_m, (size_t)S->args.n_chunks * 6 * 32));
+    AXIA_TRY(dev_alloc(ctx, &S->rc_m, (size_t)S->args.ncp * 32));
+    AXIA_TRY(dev_alloc(ctx, &S->yc_m, (size_t)S->args.ncp * 32));
+    AXIA_CUDA(ctx, cudaMemsetAsync(S->rc_m, 0, (size_t)S->args.ncp * 32 * sizeof(float), ctx->stream));
+    AXIA_CUDA(ctx, cudaMemsetAsync(S->yc_m, 0, (size_t)S->args.ncp * 32 * sizeof(float), ctx->stream));
+    S->args.part_m = S->part_m;
+    S->args.rc_m = S->rc_m;
+    S->args.yc_m = S->yc_m;
+  }
   *out = S->args;
   return AXIA_OK;
 }

@@ -35,6 +35,8 @@
 // Builds (or reuses) the coarse space of the current mesh and its operator
 // for the current assembly (coarse.cu); nodes_target <= 0: 2000.
 int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out);
+// The same with the 32-column buffers of the batched load-case solve.
+int coarse_prepare_batched(axia_ctx* ctx, int nodes_target, CoarseArgs* out);
 
 __device__ __forceinline__ unsigned geo_bits(float4 g) { return __float_as_uint(g.w); }
 

@@ -117,6 +117,10 @@ struct CoarseArgs {
   float* rc;             // [ncp] restricted residual Z^T r (zero in the padding)
   int* cnt;              // [n_sub] chunks of each subdomain done (reset by the last)
   float* yc;             // [ncp] coarse correction y = M r_c
+  // 32 load cases at once (batch.cu): [n_chunks][6][32], [ncp][32], [ncp][32]
+  float* part_m;
+  float* rc_m;
+  float* yc_m;
 };
 
 struct BsrReliableArgs {

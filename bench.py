@@ -281,24 +281,38 @@ def run_c4a(args):
     F = torch.from_numpy(m.cload_batch).to(f"cuda:{local}")
     U = torch.empty_like(F)
 
+    def step_jacobi():
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        return ctx.solve_batched_device(32, F.data_ptr(), Uj.data_ptr(), rtol=RTOL, inner_rtol=args.delta)
+
     def step():
         ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
-        return ctx.solve_batched_device(32, F.data_ptr(), U.data_ptr(), rtol=RTOL, inner_rtol=args.delta)
+        return ctx.solve_batched_device(32, F.data_ptr(), U.data_ptr(), rtol=RTOL, inner_rtol=args.delta,
+                                        preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
+    Uj = torch.empty_like(F)
+    msj, (infoj, relj) = timer(step_jacobi, args.warmup, args.steps)
     ms, (info, rel) = timer(step, args.warmup, args.steps)
+    n_sub, n_coarse = ctx.coarse_size()
+    err_j = float(torch.linalg.norm(U - Uj) / torch.linalg.norm(Uj))
     # one case through the single-RHS mixed path for comparison
     u1 = torch.empty(m.ndof, dtype=torch.float64, device=f"cuda:{local}")
 
     def single():
         return ctx.solve_device(F[0].data_ptr(), u1.data_ptr(), rtol=RTOL, precision=L.PREC_MIXED,
-                                refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta, matrix_format=L.FORMAT_BSR3)
+                                refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta, matrix_format=L.FORMAT_BSR3,
+                                preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
     ms1, i1 = timer(single, 1, 2)
     err = float(torch.linalg.norm(U[0] - u1) / torch.linalg.norm(u1))
     nf = ctx.n_free
     _line(args, f"C3D8 block {n}^3, x=0 clamped, 32 load cases (5% of surface nodes, N(0,1))",
           32 * nf / (ms * 1e-3) / 1e6, ms,
-          {"dtype": "f32+f64", "config": {"workload": f"C3D8 {n}^3 x 32 load cases", "n_free": nf, "rhs": 32},
+          {"dtype": "f32+f64", "config": {"workload": f"C3D8 {n}^3 x 32 load cases", "n_free": nf, "rhs": 32,
+                                          "preconditioner": f"diagonal + coarse space ({n_sub} subdomains)"},
            "batched": {"iters": info.iters, "reliable_updates": info.outer_iters, "max_rel_residual": float(rel.max()),
-                       "ms_kernel": info.ms_pcg_kernel},
+                       "ms_kernel": info.ms_pcg_kernel, "coarse_unknowns": n_coarse,
+                       "rel_err_vs_jacobi_batched": err_j},
+           "batched_jacobi": {"ms_per_step": msj, "iters": infoj.iters, "reliable_updates": infoj.outer_iters,
+                              "max_rel_residual": float(relj.max()), "ms_kernel": infoj.ms_pcg_kernel},
            "single_case": {"ms": ms1, "iters": i1.iters, "rel_err_batched_vs_single": err},
            "speedup_vs_32_single_solves": 32 * ms1 / ms})
 
@@ -336,9 +350,19 @@ def run_c5(args):
     m = meshgen.simp_beam(nx=100, ny=50, nz=50)
     ctx.setup(m)
     f = ctx.load_vector(m)
+    # forward solves: FP64 CSR Jacobi-PCG (the reference's algorithm) and the mixed
+    # node-block solve with the two-level preconditioner, both to rtol 1e-12
+    fwd = dict(rtol=1e-12, precision=L.PREC_MIXED, refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta,
+               matrix_format=L.FORMAT_BSR3, preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
+    ctx.compliance_forward(m.rho, m.pexp, m.e0, f, rtol=1e-12)  # warm-up
     t0 = time.perf_counter()
-    u, c, info = ctx.compliance_forward(m.rho, m.pexp, m.e0, f, rtol=1e-12)
+    u64, c64, info64 = ctx.compliance_forward(m.rho, m.pexp, m.e0, f, rtol=1e-12)
+    t_fwd64 = time.perf_counter() - t0
+    ctx.compliance_forward(m.rho, m.pexp, m.e0, f, **fwd)  # warm-up
+    t0 = time.perf_counter()
+    u, c, info = ctx.compliance_forward(m.rho, m.pexp, m.e0, f, **fwd)
     t_fwd = time.perf_counter() - t0
+    rel_u = float(np.linalg.norm(u - u64) / np.linalg.norm(u64))
     t0 = time.perf_counter()
     g = ctx.compliance_backward()
     t_bwd = time.perf_counter() - t0
@@ -350,8 +374,8 @@ def run_c5(args):
         rp, rm = m.rho.copy(), m.rho.copy()
         rp[k] += h
         rm[k] -= h
-        up, cp, _ = ctx.compliance_forward(rp, m.pexp, m.e0, f, rtol=1e-12)
-        um, cm, _ = ctx.compliance_forward(rm, m.pexp, m.e0, f, rtol=1e-12)
+        up, cp, _ = ctx.compliance_forward(rp, m.pexp, m.e0, f, **fwd)
+        um, cm, _ = ctx.compliance_forward(rm, m.pexp, m.e0, f, **fwd)
         d = (3 * m.conn[k][:, None] + np.arange(3)).ravel()
         ke, _ = O.element_ke(m.coords[m.conn[k]], 1.0, m.nu)
         dc = -(m.e0 * rp[k] ** m.pexp - m.e0 * rm[k] ** m.pexp) * (up[d] @ ke @ um[d])
@@ -361,8 +385,12 @@ def run_c5(args):
     g_cpu = O.compliance_grad(m, m.rho, m.pexp, m.e0, u)
     nf = ctx.n_free
     _line(args, "SIMP beam 100x50x50 C3D8, E=rho^3, rho~U[0.3,1], tip load", nf / t_fwd / 1e6, t_fwd * 1e3,
-          {"dtype": "f64", "config": {"workload": "C3D8 100x50x50 SIMP", "n_free": nf, "elements": m.n_elem},
-           "forward": {"iters": info.iters, "ms_solve": info.ms_solve, "compliance": c},
+          {"dtype": "f32+f64", "config": {"workload": "C3D8 100x50x50 SIMP", "n_free": nf, "elements": m.n_elem,
+                                          "forward": "mixed node-block, two-level preconditioner, rtol 1e-12"},
+           "forward": {"iters": info.iters, "reliable_updates": info.outer_iters, "ms_solve": info.ms_solve,
+                       "ms_total": t_fwd * 1e3, "compliance": c, "rel_err_vs_fp64": rel_u},
+           "forward_fp64": {"iters": info64.iters, "ms_solve": info64.ms_solve, "ms_total": t_fwd64 * 1e3,
+                            "compliance": c64},
            "backward_ms": t_bwd * 1e3,
            "gradient_vs_cpu_analytic_max_rel": float(np.abs(g - g_cpu).max() / np.abs(g_cpu).max()),
            "fd_20_elements": {"h": h, "max_rel_err_exact_difference": worst_exact,

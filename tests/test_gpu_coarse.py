@@ -102,3 +102,30 @@ def test_coarse_rejected_outside_the_mixed_node_block_solve(gpu_ctx):
         assert e.value.code == _lib.ERR_INVALID_ARG
     u, _ = gpu_ctx.solve(f, rtol=1e-10, **MIXED_BSR)  # context still usable
     assert np.all(np.isfinite(u))
+
+
+def test_batched_load_cases_with_the_coarse_space(gpu_ctx):
+    """The 32-column kernel (batch.cu) with the same preconditioner: every case
+    against the Jacobi batched solve and its own direct solve, 40 cases (two
+    launches, the second with 8 columns), one case without load."""
+    m = meshgen.block_c3d8_multiload(n=12, nrhs=40)
+    F = m.cload_batch.copy()
+    F[5] = 0.0
+    gpu_ctx.setup(m).assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+    Uj, ij, _ = gpu_ctx.solve_batched(F, rtol=1e-10)
+    Uc, ic, rel = gpu_ctx.solve_batched(F, rtol=1e-10, preconditioner=_lib.PRECOND_COARSE, coarse_nodes=150)
+    assert np.all(rel <= 1e-10 * 1.0001)
+    assert ic.iters < ij.iters, (ic.iters, ij.iters)
+    assert np.all(Uc[5] == 0.0)
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    ref = O.solve_static(m, solver=O.SOLVER_PCG, tol=1e-6, keep_csr=True, f=F[0])
+    free = m.free_mask()
+    lu = spla.splu(sp.csr_matrix((ref.data, ref.indices, ref.indptr), shape=(ref.n_free, ref.n_free)).tocsc())
+    for c in range(F.shape[0]):
+        if c == 5:
+            continue
+        u = np.zeros(m.ndof)
+        u[free] = lu.solve(F[c][free])
+        assert _rel(Uc[c], u) < 1e-8, c
+        assert _rel(Uc[c], Uj[c]) < 1e-8, c
