@@ -529,44 +529,77 @@ struct GatherArgs {
   int64_t nb;           // padded block count (plane stride)
 };
 
+// incident elements whose column slots are looked up at once (x nodes per
+// element <= GATHER_SLOTS), and the Ke values per lane of one element's row block
+constexpr int GATHER_SLOTS = 64;
+constexpr int GATHER_VPL = 6;  // ceil(3 * 60 / 32): C3D20
+
 __global__ void k_gather(GatherArgs g) {
   extern __shared__ __align__(16) unsigned char s_gather[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   const int nn = g.nn, ndof_e = 3 * nn, ke_size = ndof_e * ndof_e;
+  const int per = 3 * ndof_e, nv = (per + 31) / 32;
+  const int batch = max(1, GATHER_SLOTS / nn);
   unsigned char* base = s_gather + (size_t)warp * g.warp_stride;
   double* acc = (double*)base;                                   // [max_adj][9]
   int32_t* s_adj = (int32_t*)(base + (size_t)g.max_adj * 72);    // [max_adj]
-  int32_t* s_slot = s_adj + g.max_adj;                           // [nn]
+  int32_t* s_slot = s_adj + g.max_adj;                           // [GATHER_SLOTS]
+  int32_t* s_code = s_slot + GATHER_SLOTS;                       // [GATHER_SLOTS]
   for (int64_t a = (int64_t)blockIdx.x * wpb + warp; a < g.n_nodes; a += (int64_t)gridDim.x * wpb) {
     const int64_t s0 = g.adj_ptr[a];
     const int nadj = (int)(g.adj_ptr[a + 1] - s0);
     for (int t = lane; t < nadj; t += 32) s_adj[t] = g.adj[s0 + t];
     for (int t = lane; t < nadj * 9; t += 32) acc[t] = 0.0;
     __syncwarp();
-    for (int64_t k = g.ne_ptr[a]; k < g.ne_ptr[a + 1]; ++k) {
-      const int32_t code = g.ne[k];
-      const int64_t e = code >> 5;
-      const int la = code & 31;
-      if (lane < nn) {
-        int b = g.conn[e * nn + lane];
+    const int64_t kend = g.ne_ptr[a + 1];
+    for (int64_t k0 = g.ne_ptr[a]; k0 < kend; k0 += batch) {
+      const int nbat = kend - k0 < batch ? (int)(kend - k0) : batch;
+      // element codes and the column slots of their nodes, all at once
+      for (int t = lane; t < nbat; t += 32) s_code[t] = g.ne[k0 + t];
+      __syncwarp();
+      for (int t = lane; t < nbat * nn; t += 32) {
+        const int b = g.conn[(int64_t)(s_code[t / nn] >> 5) * nn + t % nn];
         int lo = 0, hi = nadj - 1;
         while (lo < hi) {
           int mid = (lo + hi) >> 1;
           if (s_adj[mid] < b) lo = mid + 1; else hi = mid;
         }
-        s_slot[lane] = lo;
+        s_slot[t] = lo;
       }
       __syncwarp();
-      const double* rowblk = g.ke + e * (int64_t)ke_size + (int64_t)(3 * la) * ndof_e;
-      for (int t = lane; t < 3 * ndof_e; t += 32) {
-        double v = __ldcs(rowblk + t);
-        int i = t / ndof_e, c = t % ndof_e;
-        acc[s_slot[c / 3] * 9 + i * 3 + (c % 3)] += v;
+      // element by element in ascending element order, the next element's
+      // row block loaded while the current one is summed
+      double cur[GATHER_VPL], nxt[GATHER_VPL];
+      auto load = [&](int j, double* v) {
+        const int32_t code = s_code[j];
+        const double* rowblk = g.ke + (int64_t)(code >> 5) * ke_size + (int64_t)(3 * (code & 31)) * ndof_e;
+#pragma unroll
+        for (int m = 0; m < GATHER_VPL; ++m) {
+          const int t = lane + 32 * m;
+          v[m] = (m < nv && t < per) ? __ldcs(rowblk + t) : 0.0;
+        }
+      };
+      load(0, cur);
+      for (int j = 0; j < nbat; ++j) {
+        if (j + 1 < nbat) load(j + 1, nxt);
+#pragma unroll
+        for (int m = 0; m < GATHER_VPL; ++m) {
+          const int t = lane + 32 * m;
+          if (m < nv && t < per) {
+            const int i = t / ndof_e, c = t - i * ndof_e;
+            acc[s_slot[j * nn + c / 3] * 9 + i * 3 + (c % 3)] += cur[m];
+          }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int m = 0; m < GATHER_VPL; ++m) cur[m] = nxt[m];
       }
-      __syncwarp();
     }
-    for (int i = 0; i < 3; ++i) {
+    // K_ff in CSR, and K_fp u0 -- skipped for a node-block-only assembly
+    // without prescribed values (the diagonal is then written below)
+    const bool csr_pass = g.val || g.val32 || g.any_u0;
+    for (int i = 0; csr_pass && i < 3; ++i) {
       const int r = g.ind_of[3 * a + i];
       if (r < 0) continue;
       const int64_t rs = g.rowptr[r];
@@ -612,6 +645,12 @@ __global__ void k_gather(GatherArgs g) {
           const double di = fi ? (fabs(v) > 1e-30 ? 1.0 / v : 1.0) : 1.0;
           if (g.bdinv64) g.bdinv64[3 * a + i] = di;
           if (g.bdinv32) g.bdinv32[3 * a + i] = (float)di;
+          if (!csr_pass && fi) {  // the K_ff diagonal the CSR pass would have written
+            const int r = g.ind_of[3 * a + i];
+            g.diag[r] = v;
+            g.dinv[r] = di;
+            if (g.dinv32) g.dinv32[r] = (float)di;
+          }
         }
       }
     }
@@ -620,7 +659,7 @@ __global__ void k_gather(GatherArgs g) {
 }
 
 int run_gather(axia_ctx* ctx, GatherArgs args) {
-  size_t per_warp = (size_t)args.max_adj * 9 * sizeof(double) + (size_t)(args.max_adj + args.nn) * 4;
+  size_t per_warp = (size_t)args.max_adj * 9 * sizeof(double) + (size_t)(args.max_adj + 2 * GATHER_SLOTS) * 4;
   per_warp = (per_warp + 15) & ~(size_t)15;
   if (per_warp > 200 * 1024) return set_error(ctx, AXIA_ERR_TOO_LARGE, "node adjacency too large for the gather");
   int warps = 8;

@@ -22,7 +22,8 @@
 //     S_IJ = Z_I^T K Z_J; A_IJ = T_I^T S_IJ T_J goes into a dense FP64 matrix;
 //   * A scaled to unit diagonal, rounded to FP32 and inverted in place by a
 //     symmetric blocked Gauss-Jordan elimination (64 x 64 tiles, one
-//     cooperative launch, three bounded grid barriers per tile step);
+//     cooperative launch, three bounded grid barriers per tile step, the next
+//     pivot tile inverted during the current trailing update);
 //   * M = T diag(s) A^-1 diag(s) T^T per subdomain pair, in FP32.
 // Every sum has a fixed order: the same inputs give the same bits.
 #include <algorithm>
@@ -65,7 +66,7 @@ struct CoarseState {
   double* a64 = nullptr;         // [ncp][ncp]
   float* a32 = nullptr;          // [ncp][ncp] inverted in place
   double* scale = nullptr;       // [ncp]
-  float* piv = nullptr;          // [GJ_T][GJ_T]
+  float* piv = nullptr;          // [2][GJ_T][GJ_T]
   float* part = nullptr;         // [n_chunks][6]
   float* rc = nullptr;           // [ncp]
   int* cnt = nullptr;            // [n_sub]
@@ -488,7 +489,7 @@ constexpr int GJ_LD = GJ_T + 4;   // shared-memory row stride (16-byte aligned r
 struct GjArgs {
   float* A;
   int n;             // multiple of GJ_T
-  float* piv;        // [GJ_T][GJ_T] P of the current step
+  float* piv;        // [2][GJ_T][GJ_T] P of step k in buffer k & 1
   GridBarrier* bar;
   DevStatus* st;
   unsigned long long limit_ns;
@@ -524,6 +525,27 @@ __device__ __forceinline__ void gj_mul(float (*sa)[GJ_LD], float (*sb)[GJ_LD], f
   }
 }
 
+// thread (ty, tx)'s 4 x 4 part of a tile into registers
+__device__ __forceinline__ void gj_load_regs(float (&a)[4][4], const float* g, int ld) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float4 v = *reinterpret_cast<const float4*>(g + (size_t)(4 * ty + r) * ld + 4 * tx);
+    a[r][0] = v.x;
+    a[r][1] = v.y;
+    a[r][2] = v.z;
+    a[r][3] = v.w;
+  }
+}
+
+// a dense 64 x 64 buffer into a tile of the matrix
+__device__ __forceinline__ void gj_store_global(const float* src, float* g, int ld) {
+  for (int t = threadIdx.x; t < GJ_T * GJ_T / 4; t += blockDim.x) {
+    const int r = t / (GJ_T / 4), c = 4 * (t % (GJ_T / 4));
+    *reinterpret_cast<float4*>(g + (size_t)r * ld + c) = *reinterpret_cast<const float4*>(src + (size_t)r * GJ_T + c);
+  }
+}
+
 // column panel of step k: tile (i, k) = -S_i tile (k, i)^T (i != k; S_i = -1 for i < k)
 __device__ __forceinline__ void gj_column_panel(const GjArgs& P, int k, int first, int stride) {
   const int nt = P.n / GJ_T, ld = P.n;
@@ -539,87 +561,121 @@ __device__ __forceinline__ void gj_column_panel(const GjArgs& P, int k, int firs
   }
 }
 
+// In-place Gauss-Jordan inverse of one 64 x 64 SPD tile held in registers:
+// thread (ty, tx) owns rows 4ty.., columns 4tx..; per pivot the owners publish
+// row p and column p (double-buffered, one block barrier per pivot).
+__device__ __forceinline__ void gj_invert_regs(float (&a)[4][4], float* srow, float* scol, DevStatus* st,
+                                               int base) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (int p = 0; p < GJ_T; ++p) {
+    const int b = (p & 1) * GJ_T, po = p >> 2, pi = p & 3;
+    // register indices stay compile-time constants (no local-memory copy of a)
+    if (ty == po)
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        if (r == pi)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) srow[b + 4 * tx + c] = a[r][c];
+    if (tx == po)
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (c == pi)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) scol[b + 4 * ty + r] = a[r][c];
+    __syncthreads();
+    const float piv = srow[b + p];
+    if (threadIdx.x == 0 && (!(piv > 0.f) || !isfinite(piv))) record_error(st, base + p, AXIA_ERR_ZERO_PIVOT);
+    const float d = 1.0f / piv;
+    float rv[4], cv[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) rv[c] = srow[b + 4 * tx + c];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) cv[r] = scol[b + 4 * ty + r] * d;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const bool ip = 4 * ty + r == p, jp = 4 * tx + c == p;
+        a[r][c] = ip ? (jp ? d : rv[c] * d) : (jp ? -cv[r] : fmaf(-cv[r], rv[c], a[r][c]));
+      }
+  }
+}
+
+__device__ __forceinline__ void gj_store_regs(const float (&a)[4][4], float* g, int ld) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    *reinterpret_cast<float4*>(g + (size_t)(4 * ty + r) * ld + 4 * tx) = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
+}
+
+// Step k uses P_k = piv[k & 1].  The next pivot tile (k+1, k+1) is a trailing
+// tile of step k: block 0 updates it alone and inverts it at once (lookahead)
+// while the other blocks update the remaining tiles, so no step waits for a
+// serial pivot inversion except the first.
 __global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P) {
   __shared__ __align__(16) float sa[GJ_T][GJ_LD];
   __shared__ __align__(16) float sb[GJ_T][GJ_LD];
   const int nt = P.n / GJ_T, ld = P.n;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   auto tile = [&](int i, int j) { return P.A + (size_t)i * GJ_T * ld + (size_t)j * GJ_T; };
+  auto piv = [&](int k) { return P.piv + (size_t)(k & 1) * GJ_T * GJ_T; };
   for (int k = 0; k < nt; ++k) {
-    // 1. block 0 stores the previous P and inverts tile (k, k) (in-place
-    //    Gauss-Jordan in registers); the other blocks write the previous
-    //    step's column panel
+    // 1. block 0 stores P_(k-1) into its tile (and inverts tile (0, 0) at
+    //    k = 0); the other blocks write step k-1's column panel
     if (blockIdx.x == 0) {
-      if (k > 0)
-        for (int t = threadIdx.x; t < GJ_T * GJ_T; t += blockDim.x)
-          tile(k - 1, k - 1)[(size_t)(t / GJ_T) * ld + t % GJ_T] = P.piv[t];
-      // thread (ty, tx) keeps rows 4ty.., columns 4tx.. of the tile in
-      // registers; per pivot the owners publish row p and column p
-      // (double-buffered, one barrier per pivot)
-      float a[4][4];
-      const float* src = tile(k, k);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const float4 v = *reinterpret_cast<const float4*>(src + (size_t)(4 * ty + r) * ld + 4 * tx);
-        a[r][0] = v.x;
-        a[r][1] = v.y;
-        a[r][2] = v.z;
-        a[r][3] = v.w;
-      }
-      float* srow = &sa[0][0];  // [2][GJ_T]
-      float* scol = &sb[0][0];  // [2][GJ_T]
-      for (int p = 0; p < GJ_T; ++p) {
-        const int b = (p & 1) * GJ_T, po = p >> 2, pi = p & 3;
-        if (ty == po)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) srow[b + 4 * tx + c] = a[pi][c];
-        if (tx == po)
-#pragma unroll
-          for (int r = 0; r < 4; ++r) scol[b + 4 * ty + r] = a[r][pi];
+      if (k > 0) gj_store_global(piv(k - 1), tile(k - 1, k - 1), ld);
+      if (k == 0) {
+        float a[4][4];
+        gj_load_regs(a, tile(0, 0), ld);
+        gj_invert_regs(a, &sa[0][0], &sb[0][0], P.st, 0);
+        gj_store_regs(a, piv(0), GJ_T);
         __syncthreads();
-        const float piv = srow[b + p];
-        if (threadIdx.x == 0 && (!(piv > 0.f) || !isfinite(piv))) record_error(P.st, k * GJ_T + p, AXIA_ERR_ZERO_PIVOT);
-        const float d = 1.0f / piv;
-        float rv[4], cv[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) rv[c] = srow[b + 4 * tx + c];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) cv[r] = scol[b + 4 * ty + r] * d;
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const bool ip = 4 * ty + r == p, jp = 4 * tx + c == p;
-            a[r][c] = ip ? (jp ? d : rv[c] * d) : (jp ? -cv[r] : fmaf(-cv[r], rv[c], a[r][c]));
-          }
       }
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) P.piv[(4 * ty + r) * GJ_T + 4 * tx + c] = a[r][c];
-      __syncthreads();
     } else if (k > 0) {
       gj_column_panel(P, k - 1, blockIdx.x - 1, gridDim.x - 1);
     }
     if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
-    // 2. row panel: A_kj <- P A_kj
+    // 2. row panel: A_kj <- P_k A_kj
     for (int j = blockIdx.x; j < nt; j += gridDim.x) {
       if (j == k) continue;
       __syncthreads();
-      gj_load_t(sa, P.piv, GJ_T);
+      gj_load_t(sa, piv(k), GJ_T);
       gj_load(sb, tile(k, j), ld);
       __syncthreads();
       float o[4][4];
       gj_mul(sa, sb, o);
-      float* g = tile(k, j);
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-        *reinterpret_cast<float4*>(g + (size_t)(4 * ty + r) * ld + 4 * tx) = make_float4(o[r][0], o[r][1], o[r][2], o[r][3]);
+      gj_store_regs(o, tile(k, j), ld);
     }
     if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
-    // 3. trailing tiles j <= i (i, j != k): A_ij -= A_ik R_j, mirrored into A_ji
+    // 3. trailing tiles j <= i (i, j != k): A_ij -= A_ik R_j, mirrored into
+    //    A_ji; block 0 takes tile (k+1, k+1) alone and inverts it
     const int m = nt - 1, ntiles = m * (m + 1) / 2;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const bool ahead = k + 1 < nt && gridDim.x > 1;
+    const int tdiag = ahead ? k * (k + 1) / 2 + k : -1;  // (k+1, k+1) in the compressed numbering
+    if (ahead && blockIdx.x == 0) {
+      __syncthreads();
+      gj_load_t(sa, tile(k + 1, k), ld);
+      gj_load(sb, tile(k, k + 1), ld);
+      __syncthreads();
+      float o[4][4], a[4][4];
+      gj_mul(sa, sb, o);
+      const float* g = tile(k + 1, k + 1);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const float4 c = *reinterpret_cast<const float4*>(g + (size_t)(4 * ty + r) * ld + 4 * tx);
+        a[r][0] = c.x - o[r][0];
+        a[r][1] = c.y - o[r][1];
+        a[r][2] = c.z - o[r][2];
+        a[r][3] = c.w - o[r][3];
+      }
+      __syncthreads();  // sa / sb are reused as the row / column buffers
+      gj_invert_regs(a, &sa[0][0], &sb[0][0], P.st, (k + 1) * GJ_T);
+      gj_store_regs(a, piv(k + 1), GJ_T);
+    }
+    const int first = ahead ? (int)blockIdx.x - 1 : (int)blockIdx.x;
+    const int stride = ahead ? (int)gridDim.x - 1 : (int)gridDim.x;
+    for (int t = first; first >= 0 && t < ntiles; t += stride) {
+      if (t == tdiag) continue;
       int i = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
       while (i * (i + 1) / 2 > t) --i;
       while ((i + 1) * (i + 2) / 2 <= t) ++i;
@@ -657,8 +713,7 @@ __global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P) {
   // the last step's P and column panel
   const int k = nt - 1;
   if (blockIdx.x == 0) {
-    for (int t = threadIdx.x; t < GJ_T * GJ_T; t += blockDim.x)
-      tile(k, k)[(size_t)(t / GJ_T) * ld + t % GJ_T] = P.piv[t];
+    gj_store_global(piv(k), tile(k, k), ld);
   } else {
     gj_column_panel(P, k, blockIdx.x - 1, gridDim.x - 1);
   }
@@ -934,7 +989,7 @@ int build_item_structure(axia_ctx* ctx, CoarseState* S) {
     if ((st = dev_alloc(ctx, &S->a64, ncp * ncp))) break;
     if ((st = dev_alloc(ctx, &S->a32, ncp * ncp))) break;
     if ((st = dev_alloc(ctx, &S->scale, ncp))) break;
-    if ((st = dev_alloc(ctx, &S->piv, (size_t)GJ_T * GJ_T))) break;
+    if ((st = dev_alloc(ctx, &S->piv, (size_t)2 * GJ_T * GJ_T))) break;
     S->items_fresh = true;  // the values of this pass belong to the current K
   } while (false);
   if (d_temp) cudaFree(d_temp);
