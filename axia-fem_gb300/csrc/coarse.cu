@@ -918,6 +918,10 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
   return st;
 }
 
+__global__ void k_iota(int n, int* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = i;
+}
+
 // Items of the node rows and their runs: they depend on the subdomains and
 // the constraints only, so they are built once per space.
 int build_item_structure(axia_ctx* ctx, CoarseState* S) {
@@ -954,11 +958,8 @@ int build_item_structure(axia_ctx* ctx, CoarseState* S) {
         n, n_sub, K, A.geo, S->off, S->keys, S->vals);
     ctx->launches++;
     AXIA_CUDA(ctx, cudaGetLastError());
-    {
-      std::vector<int> iota(ni);
-      for (int i = 0; i < ni; ++i) iota[i] = i;
-      if ((st = copy_to_device(ctx, d_iota, iota.data(), (size_t)ni))) break;
-    }
+    k_iota<<<grid_for(ctx, ni, 256), 256, 0, ctx->stream>>>(ni, d_iota);
+    ctx->launches++;
     int bits = 1;
     while ((1ull << bits) < (unsigned long long)n_sub * n_sub && bits < 32) ++bits;
     cub::DeviceRadixSort::SortPairs(nullptr, tb, S->keys, d_keys_sorted, d_iota, S->perm, S->n_items, 0, bits,
