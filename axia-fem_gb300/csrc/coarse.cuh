@@ -102,7 +102,7 @@ __device__ __forceinline__ void coarse_update_restrict(const CoarseArgs& C, floa
   for (int c = gwarp; c < C.n_chunks; c += nwarps) {
     const int4 ch = C.chunk[c];
     float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 2
+#pragma unroll 4
     for (int k = ch.y + lane; k < ch.z; k += 32) {
       const int a = __ldg(C.sub_node + k);
       const float4 g = __ldg(C.geo + a);
@@ -138,7 +138,7 @@ __device__ __forceinline__ float coarse_solve(const CoarseArgs& C, float* s_rc, 
     float s = 0.f;
 #pragma unroll 4
     for (int j = lane; j < nq; j += 32) {
-      const float4 mv = __ldg(m + j);
+      const float4 mv = __ldcs(m + j);  // streamed: M must not push the CG vectors out of L2
       const float4 rv = rc4[j];
       s = fmaf(mv.x, rv.x, fmaf(mv.y, rv.y, fmaf(mv.z, rv.z, fmaf(mv.w, rv.w, s))));
     }
