@@ -192,9 +192,11 @@ class GpuContext:
         self._check(self.lib.axia_gpu_bsr_spmv_device(self.h, int(precision), C.c_void_p(x_dev_ptr),
                                                       C.c_void_p(y_dev_ptr), int(lanes), int(vec)), "bsr_spmv")
 
-    def solve(self, f_full, **kw):
+    def solve(self, f_full, out=None, **kw):
+        """u for the load vector f_full (host arrays; out: a float64 array of the same
+        size to write u into, e.g. in pinned memory)."""
         f = _c(f_full, np.float64)
-        u = np.zeros_like(f)
+        u = np.zeros_like(f) if out is None else out
         o = self.opts(**kw)
         info = L.SolveInfo()
         self._check(self.lib.axia_gpu_solve(self.h, L.ptr(f), L.ptr(u), C.byref(o), C.byref(info)), "solve")

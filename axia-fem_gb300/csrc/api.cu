@@ -58,76 +58,78 @@ struct EventTimer {
 };
 
 void free_mesh_state(axia_ctx* ctx) {
+  // nothing of the old state may still be in use once its blocks are pooled
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   multimesh_release(ctx);
   coarse_release(ctx);
   ctx->h_ind_of.clear();
   ctx->mesh_node0.clear();
   ctx->mesh_blocks.clear();
-  dev_free(ctx->d_coords);
-  dev_free(ctx->d_conn);
-  dev_free(ctx->d_e);
-  dev_free(ctx->d_ind_of);
-  dev_free(ctx->d_u0);
-  dev_free(ctx->d_ne_ptr);
-  dev_free(ctx->d_ne);
-  dev_free(ctx->d_adj_ptr);
-  dev_free(ctx->d_adj);
-  dev_free(ctx->d_adj_off);
-  dev_free(ctx->d_node_rowlen);
-  dev_free(ctx->d_rowptr);
-  dev_free(ctx->d_col);
-  dev_free(ctx->d_val);
-  dev_free(ctx->d_val32);
-  dev_free(ctx->d_diag);
-  dev_free(ctx->d_dinv);
-  dev_free(ctx->d_dinv32);
-  dev_free(ctx->d_kfu0);
-  dev_free(ctx->d_ke);
+  dev_release(ctx, ctx->d_coords);
+  dev_release(ctx, ctx->d_conn);
+  dev_release(ctx, ctx->d_e);
+  dev_release(ctx, ctx->d_ind_of);
+  dev_release(ctx, ctx->d_u0);
+  dev_release(ctx, ctx->d_ne_ptr);
+  dev_release(ctx, ctx->d_ne);
+  dev_release(ctx, ctx->d_adj_ptr);
+  dev_release(ctx, ctx->d_adj);
+  dev_release(ctx, ctx->d_adj_off);
+  dev_release(ctx, ctx->d_node_rowlen);
+  dev_release(ctx, ctx->d_rowptr);
+  dev_release(ctx, ctx->d_col);
+  dev_release(ctx, ctx->d_val);
+  dev_release(ctx, ctx->d_val32);
+  dev_release(ctx, ctx->d_diag);
+  dev_release(ctx, ctx->d_dinv);
+  dev_release(ctx, ctx->d_dinv32);
+  dev_release(ctx, ctx->d_kfu0);
+  dev_release(ctx, ctx->d_ke);
   ctx->ke_elems = 0;
-  dev_free(ctx->d_f);
-  dev_free(ctx->d_u);
-  dev_free(ctx->d_b);
-  dev_free(ctx->d_x);
-  dev_free(ctx->d_r);
-  dev_free(ctx->d_p);
-  dev_free(ctx->d_q);
-  dev_free(ctx->d_b32);
-  dev_free(ctx->d_x32);
-  dev_free(ctx->d_r32);
-  dev_free(ctx->d_p32);
-  dev_free(ctx->d_q32);
-  dev_free(ctx->d_adj_ptr32);
-  dev_free(ctx->d_qptr);
-  dev_free(ctx->d_qadj);
+  dev_release(ctx, ctx->d_f);
+  dev_release(ctx, ctx->d_u);
+  dev_release(ctx, ctx->d_b);
+  dev_release(ctx, ctx->d_x);
+  dev_release(ctx, ctx->d_r);
+  dev_release(ctx, ctx->d_p);
+  dev_release(ctx, ctx->d_q);
+  dev_release(ctx, ctx->d_b32);
+  dev_release(ctx, ctx->d_x32);
+  dev_release(ctx, ctx->d_r32);
+  dev_release(ctx, ctx->d_p32);
+  dev_release(ctx, ctx->d_q32);
+  dev_release(ctx, ctx->d_adj_ptr32);
+  dev_release(ctx, ctx->d_qptr);
+  dev_release(ctx, ctx->d_qadj);
   ctx->nbq = 0;
-  dev_free(ctx->d_bval64);
-  dev_free(ctx->d_bval32);
-  dev_free(ctx->d_bdinv64);
-  dev_free(ctx->d_bdinv32);
-  dev_free(ctx->d_bf);
-  dev_free(ctx->d_xf);
-  dev_free(ctx->d_rf);
-  dev_free(ctx->d_pf);
-  dev_free(ctx->d_qf);
-  dev_free(ctx->d_xf32);
-  dev_free(ctx->d_rf32);
-  dev_free(ctx->d_pf32);
-  dev_free(ctx->d_qf32);
-  dev_free(ctx->d_zf32);
+  dev_release(ctx, ctx->d_bval64);
+  dev_release(ctx, ctx->d_bval32);
+  dev_release(ctx, ctx->d_bdinv64);
+  dev_release(ctx, ctx->d_bdinv32);
+  dev_release(ctx, ctx->d_bf);
+  dev_release(ctx, ctx->d_xf);
+  dev_release(ctx, ctx->d_rf);
+  dev_release(ctx, ctx->d_pf);
+  dev_release(ctx, ctx->d_qf);
+  dev_release(ctx, ctx->d_xf32);
+  dev_release(ctx, ctx->d_rf32);
+  dev_release(ctx, ctx->d_pf32);
+  dev_release(ctx, ctx->d_qf32);
+  dev_release(ctx, ctx->d_zf32);
   ctx->full_capacity = 0;
-  dev_free(ctx->d_mB);
-  dev_free(ctx->d_mX);
-  dev_free(ctx->d_mX32);
-  dev_free(ctx->d_mR32);
-  dev_free(ctx->d_mP32);
-  dev_free(ctx->d_mQ32);
+  dev_release(ctx, ctx->d_mB);
+  dev_release(ctx, ctx->d_mX);
+  dev_release(ctx, ctx->d_mX32);
+  dev_release(ctx, ctx->d_mR32);
+  dev_release(ctx, ctx->d_mP32);
+  dev_release(ctx, ctx->d_mQ32);
   if (ctx->d_mout) cudaFree(ctx->d_mout);
   ctx->d_mout = nullptr;
   ctx->batch_capacity = 0;
-  dev_free(ctx->d_rho);
-  dev_free(ctx->d_energy);
-  dev_free(ctx->d_grad);
-  dev_free(ctx->d_rec);
+  dev_release(ctx, ctx->d_rho);
+  dev_release(ctx, ctx->d_energy);
+  dev_release(ctx, ctx->d_grad);
+  dev_release(ctx, ctx->d_rec);
   ctx->have_forward = false;
   ctx->vec_capacity = 0;
   ctx->assembled = ctx->have32 = ctx->have_csr64 = ctx->have_bsr64 = ctx->have_bsr32 = false;
@@ -189,6 +191,7 @@ void axia_gpu_destroy(axia_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_mesh_state(ctx);
+  dev_pool_clear(ctx);
   dev_free(ctx->d_partials);
   dev_free(ctx->d_totals);
   dev_free(ctx->d_bar);

@@ -74,32 +74,32 @@ struct CoarseState {
   float* rc_m = nullptr;         // [ncp][32]
   float* yc_m = nullptr;         // [ncp][32]
   float* yc = nullptr;           // [ncp]
-  void release() {
-    dev_free(sub_node);
-    dev_free(chunk);
-    dev_free(chunk_ptr);
-    dev_free(geo);
-    dev_free(sub_ptr);
-    dev_free(tmat);
-    dev_free(minv);
-    dev_free(off);
-    dev_free(keys);
-    dev_free(vals);
-    dev_free(perm);
-    dev_free(run_key);
-    dev_free(run_off);
-    dev_free(run_cnt);
-    dev_free(a64);
-    dev_free(a32);
-    dev_free(scale);
-    dev_free(piv);
-    dev_free(part_m);
-    dev_free(rc_m);
-    dev_free(yc_m);
-    dev_free(part);
-    dev_free(rc);
-    dev_free(cnt);
-    dev_free(yc);
+  void release(axia_ctx* ctx) {
+    dev_release(ctx, sub_node);
+    dev_release(ctx, chunk);
+    dev_release(ctx, chunk_ptr);
+    dev_release(ctx, geo);
+    dev_release(ctx, sub_ptr);
+    dev_release(ctx, tmat);
+    dev_release(ctx, minv);
+    dev_release(ctx, off);
+    dev_release(ctx, keys);
+    dev_release(ctx, vals);
+    dev_release(ctx, perm);
+    dev_release(ctx, run_key);
+    dev_release(ctx, run_off);
+    dev_release(ctx, run_cnt);
+    dev_release(ctx, a64);
+    dev_release(ctx, a32);
+    dev_release(ctx, scale);
+    dev_release(ctx, piv);
+    dev_release(ctx, part_m);
+    dev_release(ctx, rc_m);
+    dev_release(ctx, yc_m);
+    dev_release(ctx, part);
+    dev_release(ctx, rc);
+    dev_release(ctx, cnt);
+    dev_release(ctx, yc);
   }
 };
 
@@ -1073,7 +1073,8 @@ int build_operator(axia_ctx* ctx, CoarseState* S) {
 void coarse_release(axia_ctx* ctx) {
   auto* S = static_cast<CoarseState*>(ctx->coarse);
   if (!S) return;
-  S->release();
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  S->release(ctx);
   delete S;
   ctx->coarse = nullptr;
 }

@@ -5,7 +5,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/axia_gpu.h"
@@ -299,6 +301,12 @@ struct axia_ctx {
 
   double ms_setup = 0.0, ms_assemble = 0.0;
   int64_t last_bad = -1;
+
+  // device blocks of a released mesh state, kept for the next setup of the
+  // same sizes (cudaFree of large blocks synchronises and costs milliseconds)
+  std::unordered_map<void*, size_t> dev_bytes;  // live blocks from dev_alloc
+  std::multimap<size_t, void*> dev_pool;         // released blocks by size
+  size_t dev_pool_bytes = 0;
 };
 
 // set ctx->last_error and return code
@@ -319,20 +327,56 @@ int set_error(axia_ctx* ctx, int code, const std::string& msg);
     if (_s != AXIA_OK) return _s; \
   } while (0)
 
+constexpr size_t DEV_POOL_CAP = (size_t)32 << 30;  // released bytes a context keeps at most
+
 template <typename T>
 int dev_alloc(axia_ctx* ctx, T** p, size_t count) {
   if (*p) {
+    ctx->dev_bytes.erase((void*)*p);
     cudaFree(*p);
     *p = nullptr;
   }
   if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  const size_t bytes = (count * sizeof(T) + 511) & ~(size_t)511;
+  auto it = ctx->dev_pool.find(bytes);
+  if (it != ctx->dev_pool.end()) {  // a released block of this size
+    *p = (T*)it->second;
+    ctx->dev_pool.erase(it);
+    ctx->dev_pool_bytes -= bytes;
+    ctx->dev_bytes[(void*)*p] = bytes;
+    return AXIA_OK;
+  }
+  cudaError_t e = cudaMalloc((void**)p, bytes);
   if (e != cudaSuccess) {
     *p = nullptr;
-    return set_error(ctx, AXIA_ERR_OOM, std::string("cudaMalloc ") + std::to_string(count * sizeof(T)) +
+    return set_error(ctx, AXIA_ERR_OOM, std::string("cudaMalloc ") + std::to_string(bytes) +
                                             " bytes: " + cudaGetErrorString(e));
   }
+  ctx->dev_bytes[(void*)*p] = bytes;
   return AXIA_OK;
+}
+
+// Releases a block of the mesh state into the context's pool (the caller has
+// synchronised the context's stream), or frees it when the pool is full.
+template <typename T>
+void dev_release(axia_ctx* ctx, T*& p) {
+  if (!p) return;
+  auto it = ctx->dev_bytes.find((void*)p);
+  if (it != ctx->dev_bytes.end() && ctx->dev_pool_bytes + it->second <= DEV_POOL_CAP) {
+    ctx->dev_pool.emplace(it->second, (void*)p);
+    ctx->dev_pool_bytes += it->second;
+  } else {
+    cudaFree(p);
+  }
+  if (it != ctx->dev_bytes.end()) ctx->dev_bytes.erase(it);
+  p = nullptr;
+}
+
+// frees every pooled block
+inline void dev_pool_clear(axia_ctx* ctx) {
+  for (auto& kv : ctx->dev_pool) cudaFree(kv.second);
+  ctx->dev_pool.clear();
+  ctx->dev_pool_bytes = 0;
 }
 
 template <typename T>

@@ -16,8 +16,8 @@ already resident in HBM (the symbolic setup is done once, before timing).
           n_free / step time; the coarse operator is rebuilt in every step
   mixed : the same with the diagonal preconditioner only (the reference's)
   fp64  : the plain FP64 Jacobi-PCG path timed the same way
-  e2e   : the same metric through the C ABI with host buffers: setup (mesh
-          upload + symbolic) + assemble + solve(host f -> host u) per step
+  e2e   : the same metric through the C ABI with host buffers (pinned): setup
+          (mesh upload + symbolic) + assemble + solve(host f -> host u) per step
 --impl reference times the CPU restatement of the reference's path on the
 host cores instead (see cpu_baseline).
 """
@@ -681,18 +681,30 @@ def main():
     e2e = None
     if not args.no_e2e:
         # through the C ABI with host buffers: setup (mesh upload) + assemble + solve (host f -> host u)
-        h2d = (model.coords.nbytes + model.conn.astype(np.int32).nbytes + model.e_elem.nbytes +
-               model.bc_dof.nbytes + model.bc_val.nbytes + f_host.nbytes)
-        d2h = f_host.nbytes
+        # the inputs live in pinned host memory (as a caller's buffers would); u goes to pinned memory
+        import copy
+
+        def pinned(a):
+            t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+            arr = t.numpy()
+            arr[...] = a
+            return arr
+        pm = copy.copy(model)
+        pm.coords, pm.conn = pinned(np.ascontiguousarray(model.coords)), pinned(model.conn.astype(np.int32))
+        pm.e_elem, pm.bc_dof, pm.bc_val = pinned(model.e_elem), pinned(model.bc_dof), pinned(model.bc_val)
+        f_pin, u_pin = pinned(f_host), pinned(np.zeros_like(f_host))
+        h2d = (pm.coords.nbytes + pm.conn.nbytes + pm.e_elem.nbytes + pm.bc_dof.nbytes + pm.bc_val.nbytes +
+               f_pin.nbytes)
+        d2h = u_pin.nbytes
         ctx.set_stream(None)
         mixed_kw["spmv_lanes"] = args.lanes32
         ts = []
         for k in range(args.warmup + args.steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            ctx.setup(model)
+            ctx.setup(pm)
             ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
-            u, info = ctx.solve(f_host, rtol=RTOL, **coarse_kw)
+            u, info = ctx.solve(f_pin, out=u_pin, rtol=RTOL, **coarse_kw)
             dt = time.perf_counter() - t0
             if k >= args.warmup:
                 ts.append(dt)
