@@ -7,7 +7,7 @@
 #include "element.cuh"
 #include "solver.cuh"
 
-int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0);
+int symbolic_setup(axia_ctx* ctx, int64_t n_bc, const int64_t* d_bc_dof, const double* d_bc_val);
 int numeric_assemble(axia_ctx* ctx, int flags);
 int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_opts* opts, axia_solve_info* info);
 int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req, int vec_req);
@@ -62,7 +62,6 @@ void free_mesh_state(axia_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   multimesh_release(ctx);
   coarse_release(ctx);
-  ctx->h_ind_of.clear();
   ctx->mesh_node0.clear();
   ctx->mesh_blocks.clear();
   dev_release(ctx, ctx->d_coords);
@@ -292,18 +291,20 @@ int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const
   ctx->ndof = 3 * mesh->n_nodes;
   ctx->last_bad = -1;
   const int64_t ndof = ctx->ndof;
-  // prescribed DOFs, last BC wins (analysis.rs:556-565)
-  std::vector<uint8_t> presc(ndof, 0);
-  std::vector<double> u0(ndof, 0.0);
+  // prescribed DOFs, last BC wins (analysis.rs:556-565): checked here, mapped on the device
   for (int64_t k = 0; k < n_bc; ++k) {
     const int64_t d = bc_dof[k];
     if (d < 0 || d >= ndof) return set_error(ctx, AXIA_ERR_INVALID_ARG, "BC " + std::to_string(k) + " names DOF out of range");
     if (!std::isfinite(bc_val[k])) return set_error(ctx, AXIA_ERR_NONFINITE, "BC " + std::to_string(k) + " value not finite");
-    presc[d] = 1;
-    u0[d] = bc_val[k];
   }
-  ctx->any_u0 = false;
-  for (int64_t d = 0; d < ndof; ++d) ctx->any_u0 |= (u0[d] != 0.0);
+  int64_t* d_bc_dof = nullptr;
+  double* d_bc_val = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_bc_dof, (size_t)std::max<int64_t>(n_bc, 1)));
+  AXIA_TRY(dev_alloc(ctx, &d_bc_val, (size_t)std::max<int64_t>(n_bc, 1)));
+  if (n_bc > 0) {
+    AXIA_CUDA(ctx, cudaMemcpyAsync(d_bc_dof, bc_dof, n_bc * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    AXIA_CUDA(ctx, cudaMemcpyAsync(d_bc_val, bc_val, n_bc * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  }
   AXIA_TRY(dev_alloc(ctx, &ctx->d_coords, (size_t)(3 * mesh->n_nodes)));
   AXIA_TRY(dev_alloc(ctx, &ctx->d_conn, (size_t)(mesh->n_elem * mesh->nn)));
   AXIA_TRY(dev_alloc(ctx, &ctx->d_e, (size_t)std::max<int64_t>(mesh->n_elem, 1)));
@@ -321,7 +322,10 @@ int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   }
   AXIA_TRY(reset_dev_status(ctx));
-  int st = symbolic_setup(ctx, presc.data(), u0.data());
+  int st = symbolic_setup(ctx, n_bc, d_bc_dof, d_bc_val);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  dev_release(ctx, d_bc_dof);
+  dev_release(ctx, d_bc_val);
   if (st != AXIA_OK) return st;
   if (ctx->n_free == 0 && n_bc == 0)  // constraint.rs:111-113
     return set_error(ctx, AXIA_ERR_NO_FREE_DOF, "model without free degrees of freedom");
@@ -702,10 +706,14 @@ int32_t axia_gpu_export_system(const axia_ctx* ctx_c, int32_t* rowptr, int32_t* 
   return AXIA_OK;
 }
 
-int32_t axia_gpu_export_dofmap(const axia_ctx* ctx, int32_t* ind_of) {
+int32_t axia_gpu_export_dofmap(const axia_ctx* ctx_c, int32_t* ind_of) {
+  axia_ctx* ctx = const_cast<axia_ctx*>(ctx_c);
   if (!ctx || !ind_of) return AXIA_ERR_INVALID_ARG;
-  if (ctx->h_ind_of.empty()) return AXIA_ERR_STATE;
-  std::memcpy(ind_of, ctx->h_ind_of.data(), ctx->h_ind_of.size() * sizeof(int32_t));
+  if (!ctx->d_ind_of) return AXIA_ERR_STATE;
+  AXIA_TRY(use_device(ctx));
+  AXIA_CUDA(ctx, cudaMemcpyAsync(ind_of, ctx->d_ind_of, ctx->ndof * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return AXIA_OK;
 }
 

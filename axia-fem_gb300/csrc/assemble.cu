@@ -688,7 +688,46 @@ static unsigned grid_for(int64_t n, int threads, int sm_count) {
   return (unsigned)std::max<int64_t>(g, 1);
 }
 
-int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0) {
+// prescribed DOFs from the BC list, last BC wins (analysis.rs:556-565): the
+// largest BC index per DOF, then its value
+__global__ void k_bc_winner(int64_t n_bc, const int64_t* bc_dof, int* win) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_bc; k += (int64_t)gridDim.x * blockDim.x)
+    atomicMax(win + bc_dof[k], (int)k);
+}
+__global__ void k_bc_apply(int64_t ndof, const int* win, const double* bc_val, uint8_t* presc, double* u0,
+                           int* any_u0) {
+  for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < ndof; d += (int64_t)gridDim.x * blockDim.x) {
+    const int k = win[d];
+    const double v = k >= 0 ? bc_val[k] : 0.0;
+    presc[d] = k >= 0;
+    u0[d] = v;
+    if (v != 0.0) *any_u0 = 1;
+  }
+}
+
+// largest ptr[a + 1] - ptr[a] over a < n
+__global__ void k_max_len(int64_t n, const int64_t* ptr, int* out) {
+  int m = 0;
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, (int)(ptr[a + 1] - ptr[a]));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+static int device_max_len(axia_ctx* ctx, int64_t n, const int64_t* d_ptr, int* result) {
+  int* d_m = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_m, 1));
+  AXIA_CUDA(ctx, cudaMemsetAsync(d_m, 0, sizeof(int), ctx->stream));
+  k_max_len<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, ctx->sm_count * 8)), 256, 0,
+              ctx->stream>>>(n, d_ptr, d_m);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaMemcpyAsync(result, d_m, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  dev_release(ctx, d_m);
+  return AXIA_OK;
+}
+
+int symbolic_setup(axia_ctx* ctx, int64_t n_bc, const int64_t* d_bc_dof, const double* d_bc_val) {
   const int64_t n_nodes = ctx->n_nodes, n_elem = ctx->n_elem, nn = ctx->nn, ndof = ctx->ndof;
   const int64_t n_items = n_elem * nn;
   cudaStream_t s = ctx->stream;
@@ -711,11 +750,8 @@ int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0) {
   int64_t total = 0;
   AXIA_TRY(device_exclusive_scan(ctx, d_cnt, d_ne_ptr, n_nodes + 1, &total));
   // per-node incidence maximum (for the adjacency candidate cap)
-  std::vector<int64_t> h_ptr(n_nodes + 1);
-  AXIA_CUDA(ctx, cudaMemcpyAsync(h_ptr.data(), d_ne_ptr, (n_nodes + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-  AXIA_CUDA(ctx, cudaStreamSynchronize(s));
   int max_inc = 0;
-  for (int64_t a = 0; a < n_nodes; ++a) max_inc = std::max<int>(max_inc, (int)(h_ptr[a + 1] - h_ptr[a]));
+  AXIA_TRY(device_max_len(ctx, n_nodes, d_ne_ptr, &max_inc));
   ctx->max_inc = max_inc;
   AXIA_TRY(dev_alloc(ctx, &ctx->d_ne, n_items));
   k_fill_incidence<<<grid_for(n_items, 256, ctx->sm_count), 256, 0, s>>>(n_items, (int)nn, ctx->d_conn, d_ne_ptr,
@@ -748,14 +784,7 @@ int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0) {
                                                 d_adj_ptr, ctx->d_adj, ctx->d_status);
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());
-  {
-    std::vector<int64_t> hp(n_nodes + 1);
-    AXIA_CUDA(ctx, cudaMemcpyAsync(hp.data(), d_adj_ptr, (n_nodes + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    AXIA_CUDA(ctx, cudaStreamSynchronize(s));
-    int mx = 0;
-    for (int64_t a = 0; a < n_nodes; ++a) mx = std::max<int>(mx, (int)(hp[a + 1] - hp[a]));
-    ctx->max_adj = mx;
-  }
+  AXIA_TRY(device_max_len(ctx, n_nodes, d_adj_ptr, &ctx->max_adj));
   // DOF map
   uint8_t* d_presc = nullptr;
   int64_t *d_flag = nullptr, *d_scan = nullptr;
@@ -764,8 +793,23 @@ int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0) {
   AXIA_TRY(dev_alloc(ctx, &d_scan, ndof + 1));
   AXIA_TRY(dev_alloc(ctx, &ctx->d_u0, ndof));
   AXIA_TRY(dev_alloc(ctx, &ctx->d_ind_of, ndof));
-  AXIA_CUDA(ctx, cudaMemcpyAsync(d_presc, h_presc, ndof, cudaMemcpyHostToDevice, s));
-  AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_u0, h_u0, ndof * sizeof(double), cudaMemcpyHostToDevice, s));
+  {
+    int *d_win = nullptr, *d_any = nullptr;
+    AXIA_TRY(dev_alloc(ctx, &d_win, ndof));
+    AXIA_TRY(dev_alloc(ctx, &d_any, 1));
+    AXIA_CUDA(ctx, cudaMemsetAsync(d_win, 0xff, ndof * sizeof(int), s));  // -1: no BC
+    AXIA_CUDA(ctx, cudaMemsetAsync(d_any, 0, sizeof(int), s));
+    if (n_bc > 0)
+      k_bc_winner<<<grid_for(n_bc, 256, ctx->sm_count), 256, 0, s>>>(n_bc, d_bc_dof, d_win);
+    k_bc_apply<<<grid_for(ndof, 256, ctx->sm_count), 256, 0, s>>>(ndof, d_win, d_bc_val, d_presc, ctx->d_u0, d_any);
+    ctx->launches += 2;
+    int any = 0;
+    AXIA_CUDA(ctx, cudaMemcpyAsync(&any, d_any, sizeof(int), cudaMemcpyDeviceToHost, s));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->any_u0 = any != 0;
+    dev_release(ctx, d_win);
+    dev_release(ctx, d_any);
+  }
   AXIA_CUDA(ctx, cudaMemsetAsync(d_flag + ndof, 0, sizeof(int64_t), s));
   k_free_flags<<<grid_for(ndof, 256, ctx->sm_count), 256, 0, s>>>(ndof, d_presc, d_cnt, d_flag);
   ctx->launches++;
@@ -827,24 +871,22 @@ int symbolic_setup(axia_ctx* ctx, const uint8_t* h_presc, const double* h_u0) {
     ctx->launches += 2;
     AXIA_CUDA(ctx, cudaGetLastError());
     AXIA_CUDA(ctx, cudaStreamSynchronize(s));
-    dev_free(d_qcnt);
-    dev_free(d_qptr64);
+    dev_release(ctx, d_qcnt);
+    dev_release(ctx, d_qptr64);
   }
   // keep the 64-bit pointers for the gather
   dev_free(ctx->d_ne_ptr);
   dev_free(ctx->d_adj_ptr);
   ctx->d_ne_ptr = d_ne_ptr;
   ctx->d_adj_ptr = d_adj_ptr;
-  dev_free(d_cnt);
-  dev_free(d_fill);
-  dev_free(d_adj_cnt);
-  dev_free(d_presc);
-  dev_free(d_flag);
-  dev_free(d_scan);
-  dev_free(d_rcnt);
-  dev_free(d_rptr);
-  ctx->h_ind_of.resize(ndof);
-  AXIA_CUDA(ctx, cudaMemcpy(ctx->h_ind_of.data(), ctx->d_ind_of, ndof * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  dev_release(ctx, d_cnt);
+  dev_release(ctx, d_fill);
+  dev_release(ctx, d_adj_cnt);
+  dev_release(ctx, d_presc);
+  dev_release(ctx, d_flag);
+  dev_release(ctx, d_scan);
+  dev_release(ctx, d_rcnt);
+  dev_release(ctx, d_rptr);
   return AXIA_OK;
 }
 

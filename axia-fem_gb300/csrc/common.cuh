@@ -197,7 +197,6 @@ struct axia_ctx {
   int32_t* d_ind_of = nullptr;  // [ndof], -1 prescribed
   double* d_u0 = nullptr;       // [ndof]
   bool any_u0 = false;
-  std::vector<int32_t> h_ind_of;
 
   // node incidence and adjacency
   int64_t* d_ne_ptr = nullptr;  // [n_nodes+1]
