@@ -234,7 +234,7 @@ constexpr int SL_A = 0, SL_B = NR;  // two banks of NR slots
 __device__ __forceinline__ void coarse_restrict_m(const CoarseArgs& C, const float* R, int gwarp, int nwarps,
                                                   int lane) {
   const int cl = lane % LPG, grp = lane / LPG;
-  for (int ci = gwarp; ci < C.n_chunks; ci += nwarps) {
+  for (int ci = C.chunk_lo + gwarp; ci < C.chunk_hi; ci += nwarps) {
     const int4 ch = C.chunk[ci];
     float v[6][CPL];
 #pragma unroll

@@ -255,10 +255,10 @@ struct SolveRange {
 
 // The coarse solve of the two-level preconditioner, r_c complete:
 // y = M r_c, and r_c . y reduced over the group.
-__device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const SolveRange& R, int gwarp, int nwarps,
-                                            int lane, float* rz_c) {
+__device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const CoarseArgs& C, const SolveRange& R,
+                                            int gwarp, int nwarps, int lane, float* rz_c) {
   __shared__ __align__(16) float s_rc[COARSE_MAX];
-  const float acc = coarse_solve(P.C, s_rc, gwarp, nwarps, lane);
+  const float acc = coarse_solve(C, s_rc, gwarp, nwarps, lane);
   block_partials<float>(acc, 0.f, 1, R.partials, S_RC, S_RC, R.nblk, R.rank);
   if (!group_reduce_sync(R.bar, P.st, P.limit_ns, R.partials, R.totals, S_RC, 1, R.nblk)) return false;
   *rz_c = (float)total(R.totals, S_RC);
@@ -266,7 +266,7 @@ __device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const Solv
 }
 
 template <int L32, int V32, int L64, int V64, bool COARSE = false>
-__device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const SolveRange& R) {
+__device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const CoarseArgs& C, const SolveRange& R) {
   const int n0 = R.node0, n1 = R.node1;
   const int i0 = 3 * n0;
   BsrMat<float> M32 = P.M32;
@@ -304,11 +304,11 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
   if constexpr (COARSE) {
     if (!converged) {  // p = D^-1 b + Z M Z^T b
       float rz_c = 0.f;
-      coarse_restrict(P.C, P.r32, gwarp, nwarps, lane);
+      coarse_restrict(C, P.r32, gwarp, nwarps, lane);
       if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
-      if (!coarse_step(P, R, gwarp, nwarps, lane, &rz_c)) return;
+      if (!coarse_step(P, C, R, gwarp, nwarps, lane, &rz_c)) return;
       rz += rz_c;
-      coarse_update_p(P.C, n0, n1, tid, nth, 0.f, P.r32, P.dinv32, P.p32, true);
+      coarse_update_p(C, n0, n1, tid, nth, 0.f, P.r32, P.dinv32, P.p32, true);
       if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
     }
   }
@@ -342,7 +342,7 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
     const float alpha = rz / pq;
     float rr_p = 0.f, rzn_p = 0.f;
     if constexpr (COARSE) {
-      coarse_update_restrict(P.C, alpha, P.x32, P.p32, P.q32, P.r32, P.dinv32, gwarp, nwarps, lane, rr_p, rzn_p);
+      coarse_update_restrict(C, alpha, P.x32, P.p32, P.q32, P.r32, P.dinv32, gwarp, nwarps, lane, rr_p, rzn_p);
     } else {
       for (int i = i0 + tid; i < nd; i += nth) {
         P.x32[i] = fmaf(alpha, P.p32[i], P.x32[i]);
@@ -403,19 +403,19 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const So
         break;
       }
       if constexpr (COARSE) {  // r was replaced: restrict it again
-        coarse_restrict(P.C, P.r32, gwarp, nwarps, lane);
+        coarse_restrict(C, P.r32, gwarp, nwarps, lane);
         if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
       }
     }
     if constexpr (COARSE) {
       float rz_c = 0.f;
-      if (!coarse_step(P, R, gwarp, nwarps, lane, &rz_c)) return;
+      if (!coarse_step(P, C, R, gwarp, nwarps, lane, &rz_c)) return;
       rzn += rz_c;
     }
     const float beta = rzn / rz;
     rz = rzn;
     if constexpr (COARSE)
-      coarse_update_p(P.C, n0, n1, tid, nth, beta, P.r32, P.dinv32, P.p32, false);
+      coarse_update_p(C, n0, n1, tid, nth, beta, P.r32, P.dinv32, P.p32, false);
     else
       for (int i = i0 + tid; i < nd; i += nth) P.p32[i] = fmaf(beta, P.p32[i], P.r32[i] * P.dinv32[i]);
     if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
@@ -443,14 +443,16 @@ __host__ __device__ constexpr int rel_min_blocks() { return V32 >= 4 ? 2 : 3; }
 template <int L32, int V32, bool COARSE = false>
 __global__ void __launch_bounds__(PCG_THREADS, rel_min_blocks<V32>()) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
   const SolveRange R{0, P.M32.n_nodes, blockIdx.x, gridDim.x, P.partials, P.totals, P.bar, P.out};
-  reliable_body<L32, V32, kL64, rel_v64<V32>(), COARSE>(P, R);
+  reliable_body<L32, V32, kL64, rel_v64<V32>(), COARSE>(P, P.C, R);
 }
 
 // Independent systems on disjoint node ranges of one node-block matrix (the
 // meshes of axia_gpu_setup_multi): block b belongs to group cta_group[b] and
 // solves that group's system with the group's own barrier, partial sums,
 // totals and result, so each system converges and exits on its own.
-template <int L32, int V32>
+// With the two-level preconditioner every group works on its own mesh's
+// restriction chunks and rows of the (block-diagonal) coarse inverse.
+template <int L32, int V32, bool COARSE = false>
 __global__ void __launch_bounds__(PCG_THREADS, 2)
 pcg_group_reliable_kernel(BsrReliableArgs P, const MeshGroup* groups, const int* cta_group, GridBarrier* bars,
                           double* totals4, PcgOut* outs) {
@@ -458,7 +460,14 @@ pcg_group_reliable_kernel(BsrReliableArgs P, const MeshGroup* groups, const int*
   const MeshGroup G = groups[g];
   const SolveRange R{G.node0, G.node1, blockIdx.x - (unsigned)G.cta0, (unsigned)G.ncta, P.partials + G.part_off,
                      totals4 + 4 * g, bars + g, outs + g};
-  reliable_body<L32, V32, kL64, 2>(P, R);
+  CoarseArgs C = P.C;
+  if constexpr (COARSE) {
+    C.chunk_lo = G.chunk0;
+    C.chunk_hi = G.chunk1;
+    C.row0 = G.row0;
+    C.row1 = G.row1;
+  }
+  reliable_body<L32, V32, kL64, 2, COARSE>(P, C, R);
 }
 
 // b[d] = f[d] - K_fp u0 for free d, 0 for prescribed d
@@ -622,20 +631,22 @@ static int launch_bsr_rel(axia_ctx* ctx, BsrReliableArgs& P, RowLayout r) {
 }
 
 // Occupancy of the group kernel (blocks per SM) for the grid size of a multi-mesh solve.
-int group_kernel_capacity(axia_ctx* ctx, int lanes, int vec, int* per_sm) {
+int group_kernel_capacity(axia_ctx* ctx, int lanes, int vec, int* per_sm, bool coarse) {
   return with_layout(RowLayout{lanes, vec}, [&](auto l, auto v) {
-    const void* kern = (const void*)pcg_group_reliable_kernel<decltype(l)::value, decltype(v)::value>;
+    const void* kern = coarse ? (const void*)pcg_group_reliable_kernel<decltype(l)::value, decltype(v)::value, true>
+                              : (const void*)pcg_group_reliable_kernel<decltype(l)::value, decltype(v)::value, false>;
     AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, PCG_THREADS, 0));
     return (int)AXIA_OK;
   });
 }
 // Cooperative launch of the group kernel on ctx->stream (capturable).
 int launch_group_reliable(axia_ctx* ctx, BsrReliableArgs& P, const MeshGroup* groups, const int* cta_group,
-                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes, int vec) {
+                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes, int vec, bool coarse) {
   void* params[] = {&P, &groups, &cta_group, &bars, &totals4, &outs};
   const void* kern = nullptr;
   with_layout(RowLayout{lanes, vec}, [&](auto l, auto v) {
-    kern = (const void*)pcg_group_reliable_kernel<decltype(l)::value, decltype(v)::value>;
+    kern = coarse ? (const void*)pcg_group_reliable_kernel<decltype(l)::value, decltype(v)::value, true>
+                  : (const void*)pcg_group_reliable_kernel<decltype(l)::value, decltype(v)::value, false>;
     return 0;
   });
   cudaLaunchConfig_t cfg = {};

@@ -54,6 +54,8 @@ struct CoarseState {
   double* tmat = nullptr;        // [n_sub][6][6]
   float* minv = nullptr;         // [nc][ncp]
   // operator scratch, kept for the rebuilds after every assembly
+  std::vector<int> h_chunk_ptr;  // [n_sub + 1]
+  std::vector<int> mesh_sub;     // [n_meshes + 1] subdomains of each mesh (one mesh: 0, n_sub)
   int* off = nullptr;            // [n_nodes + 1] first item of each node row
   unsigned* keys = nullptr;      // [n_items] subdomain pair I * n_sub + J
   double* vals = nullptr;        // [n_items][36]
@@ -106,9 +108,9 @@ struct CoarseState {
 // ---------------------------------------------------------------------------
 // Space
 // ---------------------------------------------------------------------------
-__global__ void k_bbox(int64_t n, const double* __restrict__ xyz, double* out) {
+__global__ void k_bbox(int64_t a0, int64_t a1, const double* __restrict__ xyz, double* out) {
   double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x)
+  for (int64_t a = a0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < a1; a += (int64_t)gridDim.x * blockDim.x)
     for (int d = 0; d < 3; ++d) {
       const double v = xyz[3 * a + d];
       lo[d] = fmin(lo[d], v);
@@ -148,9 +150,11 @@ __device__ __forceinline__ int cell_of(const Grid3& g, double x, double y, doubl
   return ix + g.nx * (iy + g.ny * iz);
 }
 
-__global__ void k_cell_count(int64_t n, const double* __restrict__ xyz, Grid3 g, int* cell, int* count) {
-  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
-    const int c = cell_of(g, xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]);
+// cells of the nodes [a0, a1) (one mesh) in the grid g, numbered from base
+__global__ void k_cell_count(int64_t a0, int64_t a1, const double* __restrict__ xyz, Grid3 g, int base, int* cell,
+                             int* count) {
+  for (int64_t a = a0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < a1; a += (int64_t)gridDim.x * blockDim.x) {
+    const int c = base + cell_of(g, xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]);
     cell[a] = c;
     atomicAdd(count + c, 1);
   }
@@ -189,10 +193,11 @@ __global__ void k_sub_centre(int n_sub, const int* sub_ptr, const int* sub_node,
   }
 }
 
-__global__ void k_geo(int64_t n, const double* __restrict__ xyz, const int* sub, const double* centre, double inv_h,
-                      const int32_t* ind_of, float4* geo) {
+__global__ void k_geo(int64_t n, const double* __restrict__ xyz, const int* sub, const double* centre,
+                      const double* sub_inv_h, const int32_t* ind_of, float4* geo) {
   for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
     const int I = sub[a];
+    const double inv_h = sub_inv_h[I];
     unsigned m = 0;
     for (int d = 0; d < 3; ++d)
       if (ind_of[3 * a + d] >= 0) m |= 1u << d;
@@ -781,67 +786,100 @@ int grid_for(const axia_ctx* ctx, int64_t n, int threads) {
 int build_space(axia_ctx* ctx, CoarseState* S) {
   const int64_t n = ctx->n_nodes;
   if (n >= (1LL << 28)) return set_error(ctx, AXIA_ERR_TOO_LARGE, "coarse space: too many nodes");
-  const int bb_grid = (int)std::min<int64_t>((n + 255) / 256, 1024);
-  double* d_bb = nullptr;
-  AXIA_TRY(dev_alloc(ctx, &d_bb, (size_t)6 * bb_grid));
-  k_bbox<<<bb_grid, 256, 0, ctx->stream>>>(n, ctx->d_coords, d_bb);
-  ctx->launches++;
-  std::vector<double> hb((size_t)6 * bb_grid);
-  int st = copy_to_host(ctx, hb.data(), d_bb, hb.size());
-  dev_free(d_bb);
-  AXIA_TRY(st);
-  double lo[3] = {hb[0], hb[1], hb[2]}, hi[3] = {hb[3], hb[4], hb[5]};
-  for (int b = 1; b < bb_grid; ++b)
-    for (int d = 0; d < 3; ++d) {
-      lo[d] = std::min(lo[d], hb[6 * b + d]);
-      hi[d] = std::max(hi[d], hb[6 * b + 3 + d]);
-    }
-  double ext[3], emax = 0.0;
-  for (int d = 0; d < 3; ++d) emax = std::max(emax, ext[d] = hi[d] - lo[d]);
-  if (!(emax > 0.0) || !std::isfinite(emax)) emax = 1.0;
+  // one grid of boxes per mesh (the meshes of axia_gpu_setup_multi are
+  // independent: no subdomain may hold nodes of two of them)
+  const int nm = ctx->mesh_node0.size() >= 2 ? (int)ctx->mesh_node0.size() - 1 : 1;
+  auto mesh_a0 = [&](int k) { return nm > 1 ? ctx->mesh_node0[k] : (int64_t)0; };
+  auto mesh_a1 = [&](int k) { return nm > 1 ? ctx->mesh_node0[k + 1] : n; };
   const int max_boxes = COARSE_MAX / 6;
-  const int64_t target = std::max<int64_t>(1, std::min<int64_t>(max_boxes, n / std::max(1, S->nodes_target)));
-  double vol = 1.0;
-  for (int d = 0; d < 3; ++d) vol *= std::max(ext[d], 1e-3 * emax);
-  double h = std::cbrt(vol / (double)target);
-  Grid3 g{};
-  for (int it = 0; it < 400; ++it) {
-    g.nx = std::max(1, (int)std::ceil(ext[0] / h - 1e-9));
-    g.ny = std::max(1, (int)std::ceil(ext[1] / h - 1e-9));
-    g.nz = std::max(1, (int)std::ceil(ext[2] / h - 1e-9));
-    if ((int64_t)g.nx * g.ny * g.nz <= target) break;
-    h *= 1.02;
+  std::vector<int64_t> target(nm);
+  int64_t tsum = 0;
+  for (int k = 0; k < nm; ++k) {
+    target[k] = std::max<int64_t>(1, (mesh_a1(k) - mesh_a0(k)) / std::max(1, S->nodes_target));
+    tsum += target[k];
   }
-  if ((int64_t)g.nx * g.ny * g.nz > target) {  // one box
-    g.nx = g.ny = g.nz = 1;
-    h = 2.0 * emax;
+  if (tsum > max_boxes)
+    for (int k = 0; k < nm; ++k) target[k] = std::max<int64_t>(1, target[k] * max_boxes / tsum);
+  std::vector<Grid3> grids(nm);
+  std::vector<int> cell_base(nm + 1, 0);
+  double* d_bb = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_bb, (size_t)6 * 1024));
+  for (int k = 0; k < nm; ++k) {
+    const int64_t nk = mesh_a1(k) - mesh_a0(k);
+    const int bb_grid = (int)std::max<int64_t>(1, std::min<int64_t>((nk + 255) / 256, 1024));
+    k_bbox<<<bb_grid, 256, 0, ctx->stream>>>(mesh_a0(k), mesh_a1(k), ctx->d_coords, d_bb);
+    ctx->launches++;
+    std::vector<double> hb((size_t)6 * bb_grid);
+    const int cst = copy_to_host(ctx, hb.data(), d_bb, hb.size());
+    if (cst) {
+      dev_free(d_bb);
+      return cst;
+    }
+    double lo[3] = {hb[0], hb[1], hb[2]}, hi[3] = {hb[3], hb[4], hb[5]};
+    for (int b = 1; b < bb_grid; ++b)
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = std::min(lo[d], hb[6 * b + d]);
+        hi[d] = std::max(hi[d], hb[6 * b + 3 + d]);
+      }
+    double ext[3], emax = 0.0;
+    for (int d = 0; d < 3; ++d) emax = std::max(emax, ext[d] = hi[d] - lo[d]);
+    if (!(emax > 0.0) || !std::isfinite(emax)) emax = 1.0;
+    double vol = 1.0;
+    for (int d = 0; d < 3; ++d) vol *= std::max(ext[d], 1e-3 * emax);
+    double h = std::cbrt(vol / (double)target[k]);
+    Grid3 g{};
+    for (int it = 0; it < 400; ++it) {
+      g.nx = std::max(1, (int)std::ceil(ext[0] / h - 1e-9));
+      g.ny = std::max(1, (int)std::ceil(ext[1] / h - 1e-9));
+      g.nz = std::max(1, (int)std::ceil(ext[2] / h - 1e-9));
+      if ((int64_t)g.nx * g.ny * g.nz <= target[k]) break;
+      h *= 1.02;
+    }
+    if ((int64_t)g.nx * g.ny * g.nz > target[k]) {  // one box
+      g.nx = g.ny = g.nz = 1;
+      h = 2.0 * emax;
+    }
+    g.x0 = lo[0];
+    g.y0 = lo[1];
+    g.z0 = lo[2];
+    g.h = h;
+    grids[k] = g;
+    cell_base[k + 1] = cell_base[k] + g.nx * g.ny * g.nz;
+    if (k == 0) S->h = h;
   }
-  g.x0 = lo[0];
-  g.y0 = lo[1];
-  g.z0 = lo[2];
-  g.h = h;
-  S->h = h;
-  const int ncell = g.nx * g.ny * g.nz;
+  dev_free(d_bb);
+  const int ncell = cell_base[nm];
+  if (ncell > max_boxes + nm)
+    return set_error(ctx, AXIA_ERR_TOO_LARGE, "coarse space: more than " + std::to_string(max_boxes) + " subdomains");
   int *d_cell = nullptr, *d_count = nullptr, *d_sub = nullptr, *d_iota = nullptr, *d_cellsub = nullptr;
   int* d_sub_sorted = nullptr;
-  double* d_centre = nullptr;
+  double *d_centre = nullptr, *d_inv_h = nullptr;
   void* d_temp = nullptr;
-  st = AXIA_OK;
+  int st = AXIA_OK;
   do {
     if ((st = dev_alloc(ctx, &d_cell, (size_t)n))) break;
     if ((st = dev_alloc(ctx, &d_count, (size_t)ncell))) break;
     AXIA_CUDA(ctx, cudaMemsetAsync(d_count, 0, ncell * sizeof(int), ctx->stream));
-    k_cell_count<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, ctx->d_coords, g, d_cell, d_count);
-    ctx->launches++;
+    for (int k = 0; k < nm; ++k) {
+      k_cell_count<<<grid_for(ctx, mesh_a1(k) - mesh_a0(k), 256), 256, 0, ctx->stream>>>(
+          mesh_a0(k), mesh_a1(k), ctx->d_coords, grids[k], cell_base[k], d_cell, d_count);
+      ctx->launches++;
+    }
     std::vector<int> count(ncell), cell_sub(ncell, -1);
     if ((st = copy_to_host(ctx, count.data(), d_count, (size_t)ncell))) break;
     int n_sub = 0;
     std::vector<int> sub_ptr(1, 0);
-    for (int c = 0; c < ncell; ++c)
-      if (count[c] > 0) {
-        cell_sub[c] = n_sub++;
-        sub_ptr.push_back(sub_ptr.back() + count[c]);
-      }
+    std::vector<double> sub_inv_h;
+    S->mesh_sub.assign(1, 0);
+    for (int k = 0; k < nm; ++k) {
+      for (int c = cell_base[k]; c < cell_base[k + 1]; ++c)
+        if (count[c] > 0) {
+          cell_sub[c] = n_sub++;
+          sub_ptr.push_back(sub_ptr.back() + count[c]);
+          sub_inv_h.push_back(1.0 / grids[k].h);
+        }
+      S->mesh_sub.push_back(n_sub);
+    }
     // chunks of COARSE_CHUNK nodes inside every subdomain
     std::vector<int4> chunk;
     std::vector<int> chunk_ptr(1, 0);
@@ -850,11 +888,16 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
         chunk.push_back(make_int4(I, b, std::min(b + COARSE_CHUNK, sub_ptr[I + 1]), 0));
       chunk_ptr.push_back((int)chunk.size());
     }
+    S->h_chunk_ptr = chunk_ptr;
     CoarseArgs& A = S->args;
     A.n_sub = n_sub;
     A.nc = 6 * n_sub;
     A.ncp = ((A.nc + GJ_T - 1) / GJ_T) * GJ_T;
     A.n_chunks = (int)chunk.size();
+    A.row0 = 0;
+    A.row1 = A.nc;
+    A.chunk_lo = 0;
+    A.chunk_hi = A.n_chunks;
     if ((st = dev_alloc(ctx, &d_cellsub, (size_t)ncell))) break;
     if ((st = copy_to_device(ctx, d_cellsub, cell_sub.data(), (size_t)ncell))) break;
     if ((st = dev_alloc(ctx, &d_sub, (size_t)n))) break;
@@ -883,7 +926,9 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     if ((st = dev_alloc(ctx, &S->tmat, (size_t)36 * n_sub))) break;
     k_sub_centre<<<grid_for(ctx, (int64_t)n_sub * 32, 256), 256, 0, ctx->stream>>>(n_sub, S->sub_ptr, S->sub_node,
                                                                                   ctx->d_coords, d_centre);
-    k_geo<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, ctx->d_coords, d_sub, d_centre, 1.0 / h, ctx->d_ind_of,
+    if ((st = dev_alloc(ctx, &d_inv_h, (size_t)n_sub))) break;
+    if ((st = copy_to_device(ctx, d_inv_h, sub_inv_h.data(), (size_t)n_sub))) break;
+    k_geo<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(n, ctx->d_coords, d_sub, d_centre, d_inv_h, ctx->d_ind_of,
                                                           S->geo);
     k_sub_gram<<<grid_for(ctx, (int64_t)n_sub * 32, 128), 128, 0, ctx->stream>>>(n_sub, S->sub_ptr, S->sub_node,
                                                                                 S->geo, S->tmat);
@@ -915,6 +960,7 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
   dev_free(d_cellsub);
   dev_free(d_sub_sorted);
   dev_free(d_centre);
+  dev_free(d_inv_h);
   return st;
 }
 
@@ -1125,6 +1171,25 @@ int coarse_prepare_batched(axia_ctx* ctx, int nodes_target, CoarseArgs* out) {
     S->args.yc_m = S->yc_m;
   }
   *out = S->args;
+  return AXIA_OK;
+}
+
+// per mesh of a multi-mesh context: its restriction chunks and coarse rows
+int coarse_mesh_ranges(const axia_ctx* ctx, std::vector<int>& chunk0, std::vector<int>& chunk1, std::vector<int>& row0,
+                       std::vector<int>& row1) {
+  const auto* S = static_cast<const CoarseState*>(ctx->coarse);
+  if (!S) return AXIA_ERR_STATE;
+  const int nm = (int)S->mesh_sub.size() - 1;
+  chunk0.resize(nm);
+  chunk1.resize(nm);
+  row0.resize(nm);
+  row1.resize(nm);
+  for (int k = 0; k < nm; ++k) {
+    chunk0[k] = S->h_chunk_ptr[S->mesh_sub[k]];
+    chunk1[k] = S->h_chunk_ptr[S->mesh_sub[k + 1]];
+    row0[k] = 6 * S->mesh_sub[k];
+    row1[k] = 6 * S->mesh_sub[k + 1];
+  }
   return AXIA_OK;
 }
 

@@ -37,6 +37,9 @@
 int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out);
 // The same with the 32-column buffers of the batched load-case solve.
 int coarse_prepare_batched(axia_ctx* ctx, int nodes_target, CoarseArgs* out);
+// Per mesh of a multi-mesh context: its restriction chunks and coarse rows.
+int coarse_mesh_ranges(const axia_ctx* ctx, std::vector<int>& chunk0, std::vector<int>& chunk1,
+                       std::vector<int>& row0, std::vector<int>& row1);
 
 __device__ __forceinline__ unsigned geo_bits(float4 g) { return __float_as_uint(g.w); }
 
@@ -80,7 +83,7 @@ __device__ __forceinline__ void coarse_chunk_finish(const CoarseArgs& C, int c, 
 // r_c = Z^T r over the chunks (after an FP64 residual replaced r, and at the start)
 __device__ __forceinline__ void coarse_restrict(const CoarseArgs& C, const float* r, int gwarp, int nwarps,
                                                 int lane) {
-  for (int c = gwarp; c < C.n_chunks; c += nwarps) {
+  for (int c = C.chunk_lo + gwarp; c < C.chunk_hi; c += nwarps) {
     const int4 ch = C.chunk[c];
     float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll 4
@@ -99,7 +102,7 @@ __device__ __forceinline__ void coarse_restrict(const CoarseArgs& C, const float
 __device__ __forceinline__ void coarse_update_restrict(const CoarseArgs& C, float alpha, float* x, const float* p,
                                                        const float* q, float* r, const float* dinv, int gwarp,
                                                        int nwarps, int lane, float& rr_p, float& rz_p) {
-  for (int c = gwarp; c < C.n_chunks; c += nwarps) {
+  for (int c = C.chunk_lo + gwarp; c < C.chunk_hi; c += nwarps) {
     const int4 ch = C.chunk[c];
     float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll 4
@@ -133,7 +136,7 @@ __device__ __forceinline__ float coarse_solve(const CoarseArgs& C, float* s_rc, 
   float acc = 0.f;
   const int nq = C.ncp >> 2;
   const float4* rc4 = reinterpret_cast<const float4*>(s_rc);
-  for (int row = gwarp; row < C.nc; row += nwarps) {
+  for (int row = C.row0 + gwarp; row < C.row1; row += nwarps) {
     const float4* m = reinterpret_cast<const float4*>(C.minv + (size_t)row * C.ncp);
     float s = 0.f;
 #pragma unroll 4

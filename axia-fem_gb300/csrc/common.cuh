@@ -277,6 +277,8 @@ struct axia_ctx {
   double* d_mtotals = nullptr;
   unsigned char* d_mouts = nullptr;   // PcgOut[n_meshes]
   int multi_grid = 0, multi_lanes = 0, multi_vec = 0;
+  bool multi_coarse = false;          // groups planned for the two-level kernel
+  const void* graph_coarse = nullptr; // coarse inverse the captured graph reads (null: diagonal only)
   int tuned_lanes = 0, tuned_vec = 0;  // node-block layout chosen by axia_gpu_autotune (0: none)
   void* multi_graph = nullptr;        // cudaGraphExec_t
   const double* graph_f = nullptr;

@@ -23,7 +23,7 @@
 #include <cstring>
 #include <vector>
 
-#include "solver.cuh"
+#include "coarse.cuh"
 
 extern "C" int32_t axia_gpu_setup(axia_ctx* ctx, const axia_mesh* mesh, int64_t n_bc, const int64_t* bc_dof,
                                   const double* bc_val);
@@ -35,10 +35,10 @@ void drop_graph(axia_ctx* ctx) {
   ctx->multi_graph = nullptr;
 }
 
-int plan_groups(axia_ctx* ctx, int lanes, int vec) {
+int plan_groups(axia_ctx* ctx, int lanes, int vec, bool coarse) {
   const int nm = (int)ctx->mesh_node0.size() - 1;
   int per_sm = 0;
-  AXIA_TRY(group_kernel_capacity(ctx, lanes, vec, &per_sm));
+  AXIA_TRY(group_kernel_capacity(ctx, lanes, vec, &per_sm, coarse));
   const int cap = std::max(1, per_sm) * ctx->sm_count;
   if (nm > cap)
     return set_error(ctx, AXIA_ERR_TOO_LARGE, std::to_string(nm) + " meshes exceed the " + std::to_string(cap) +
@@ -78,10 +78,10 @@ int plan_groups(axia_ctx* ctx, int lanes, int vec) {
   long long part = 0;
   int cta = 0;
   for (int k = 0; k < nm; ++k) {
-    groups[k] = MeshGroup{(int)ctx->mesh_node0[k], (int)ctx->mesh_node0[k + 1], cta, nc[k], part};
+    groups[k] = MeshGroup{(int)ctx->mesh_node0[k], (int)ctx->mesh_node0[k + 1], cta, nc[k], part, 0, 0, 0, 0};
     for (int j = 0; j < nc[k]; ++j) cta_group[cta + j] = k;
     cta += nc[k];
-    part += (long long)N_SLOTS * nc[k];
+    part += (long long)GROUP_SLOTS * nc[k];
   }
   if ((size_t)part > ctx->partial_slots) return set_error(ctx, AXIA_ERR_TOO_LARGE, "partials area too small");
   AXIA_TRY(dev_alloc(ctx, &ctx->d_mgroups, sizeof(MeshGroup) * nm));
@@ -94,14 +94,17 @@ int plan_groups(axia_ctx* ctx, int lanes, int vec) {
   ctx->multi_grid = total;
   ctx->multi_lanes = lanes;
   ctx->multi_vec = vec;
+  ctx->multi_coarse = coarse;
   ctx->multi_ctas.assign(nc.begin(), nc.end());
   drop_graph(ctx);
   return AXIA_OK;
 }
 
-int capture_graph(axia_ctx* ctx, const double* d_f, double* d_u, double rtol, double delta, long long max_iter) {
+int capture_graph(axia_ctx* ctx, const double* d_f, double* d_u, double rtol, double delta, long long max_iter,
+                  const CoarseArgs* coarse) {
   drop_graph(ctx);
   BsrReliableArgs args = make_reliable_args(ctx, rtol, delta, max_iter);
+  if (coarse) args.C = *coarse;
   const int64_t launches_before = ctx->launches;  // captured launches are counted when the graph runs
   cudaGraph_t g = nullptr;
   AXIA_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -112,7 +115,7 @@ int capture_graph(axia_ctx* ctx, const double* d_f, double* d_u, double rtol, do
   if (rc == AXIA_OK)
     rc = launch_group_reliable(ctx, args, (const MeshGroup*)ctx->d_mgroups,
                                ctx->d_mcta, ctx->d_mbars, ctx->d_mtotals, (PcgOut*)ctx->d_mouts, ctx->multi_grid,
-                               ctx->multi_lanes, ctx->multi_vec);
+                               ctx->multi_lanes, ctx->multi_vec, coarse != nullptr);
   if (rc == AXIA_OK) rc = launch_full_reconstruct(ctx, d_u);
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   ctx->launches = launches_before;
@@ -131,6 +134,29 @@ int capture_graph(axia_ctx* ctx, const double* d_f, double* d_u, double rtol, do
   ctx->graph_rtol = rtol;
   ctx->graph_delta = delta;
   ctx->graph_max_iter = max_iter;
+  ctx->graph_coarse = coarse ? (const void*)coarse->minv : nullptr;
+  return AXIA_OK;
+}
+
+// the restriction chunks and coarse rows of every group
+int set_group_ranges(axia_ctx* ctx) {
+  const int nm = (int)ctx->mesh_node0.size() - 1;
+  std::vector<int> c0, c1, r0, r1;
+  AXIA_TRY(coarse_mesh_ranges(ctx, c0, c1, r0, r1));
+  if ((int)c0.size() != nm) return set_error(ctx, AXIA_ERR_STATE, "coarse space does not match the meshes");
+  std::vector<MeshGroup> g(nm);
+  AXIA_CUDA(ctx, cudaMemcpyAsync(g.data(), ctx->d_mgroups, sizeof(MeshGroup) * nm, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int k = 0; k < nm; ++k) {
+    g[k].chunk0 = c0[k];
+    g[k].chunk1 = c1[k];
+    g[k].row0 = r0[k];
+    g[k].row1 = r1[k];
+  }
+  AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_mgroups, g.data(), sizeof(MeshGroup) * nm, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return AXIA_OK;
 }
 
@@ -139,13 +165,20 @@ int solve_multi_device(axia_ctx* ctx, const double* d_f, double* d_u, const axia
   if (ctx->mesh_node0.size() < 2) return set_error(ctx, AXIA_ERR_STATE, "solve_multi needs axia_gpu_setup_multi");
   if (!ctx->have_bsr64 || !ctx->have_bsr32)
     return set_error(ctx, AXIA_ERR_STATE, "solve_multi needs axia_gpu_assemble_ex(AXIA_ASM_BSR64 | AXIA_ASM_BSR32)");
-  if (opts->preconditioner != AXIA_PRECOND_JACOBI)
-    return set_error(ctx, AXIA_ERR_INVALID_ARG, "solve_multi: Jacobi preconditioner only");
+  if (opts->preconditioner != AXIA_PRECOND_JACOBI && opts->preconditioner != AXIA_PRECOND_COARSE)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "solve_multi: unknown preconditioner");
+  const bool coarse = opts->preconditioner == AXIA_PRECOND_COARSE;
   const int nm = (int)ctx->mesh_node0.size() - 1;
   AXIA_TRY(prepare_full_buffers(ctx));
   int lanes = 0, vec = 0;
   group_layout(ctx, opts->spmv_lanes, opts->spmv_vec, &lanes, &vec);
-  if (ctx->multi_grid == 0 || ctx->multi_lanes != lanes || ctx->multi_vec != vec) AXIA_TRY(plan_groups(ctx, lanes, vec));
+  if (ctx->multi_grid == 0 || ctx->multi_lanes != lanes || ctx->multi_vec != vec || ctx->multi_coarse != coarse)
+    AXIA_TRY(plan_groups(ctx, lanes, vec, coarse));
+  CoarseArgs cargs{};
+  if (coarse) {  // per-mesh subdomains; the operator follows every assembly (outside the graph)
+    AXIA_TRY(coarse_prepare(ctx, opts->coarse_nodes, &cargs));
+    AXIA_TRY(set_group_ranges(ctx));
+  }
   const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.01;
   long long max_iter = opts->max_iter > 0 ? opts->max_iter : 0;
   if (max_iter == 0) {
@@ -153,9 +186,10 @@ int solve_multi_device(axia_ctx* ctx, const double* d_f, double* d_u, const axia
     for (int k = 0; k < nm; ++k) biggest = std::max<int64_t>(biggest, 3 * (ctx->mesh_node0[k + 1] - ctx->mesh_node0[k]));
     max_iter = std::max<long long>(4 * biggest, 200);
   }
+  const void* coarse_key = coarse ? (const void*)cargs.minv : nullptr;
   if (!ctx->multi_graph || ctx->graph_f != d_f || ctx->graph_u != d_u || ctx->graph_rtol != opts->rtol ||
-      ctx->graph_delta != delta || ctx->graph_max_iter != max_iter)
-    AXIA_TRY(capture_graph(ctx, d_f, d_u, opts->rtol, delta, max_iter));
+      ctx->graph_delta != delta || ctx->graph_max_iter != max_iter || ctx->graph_coarse != coarse_key)
+    AXIA_TRY(capture_graph(ctx, d_f, d_u, opts->rtol, delta, max_iter, coarse ? &cargs : nullptr));
   AXIA_TRY(reset_dev_status(ctx));
   cudaEvent_t a, b;
   AXIA_CUDA(ctx, cudaEventCreate(&a));

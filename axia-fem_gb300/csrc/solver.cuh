@@ -97,7 +97,10 @@ struct MeshGroup {
   int node0, node1;   // block rows [node0, node1)
   int cta0, ncta;     // blocks [cta0, cta0 + ncta) of the launch
   long long part_off; // offset of its partial-sum area
+  int chunk0, chunk1; // its restriction chunks (two-level preconditioner)
+  int row0, row1;     // its coarse unknowns
 };
+constexpr int GROUP_SLOTS = 4;  // partial-sum slots per group: S_PQ, S_RR, S_RZ, S_RC
 
 constexpr int COARSE_MAX = 4096;    // coarse unknowns (6 per subdomain, padded to 64)
 constexpr int COARSE_CHUNK = 256;   // nodes per restriction chunk
@@ -106,6 +109,8 @@ constexpr int S_RC = 3;             // partial-sum slot of r_c . y
 struct CoarseArgs {
   int n_sub;             // subdomains (0: no coarse space)
   int nc;                // 6 n_sub
+  int row0, row1;        // the coarse unknowns whose rows of y = M r_c this launch (group) computes
+  int chunk_lo, chunk_hi;  // the restriction chunks this launch (group) handles
   int ncp;               // nc rounded up to a multiple of 64 (row stride of minv)
   int n_chunks;
   const int* sub_node;   // [n_nodes] nodes by subdomain, ascending within each
@@ -148,10 +153,10 @@ struct BsrReliableArgs {
 };
 
 BsrReliableArgs make_reliable_args(axia_ctx* ctx, double rtol, double delta, long long max_iter);
-int group_kernel_capacity(axia_ctx* ctx, int lanes, int vec, int* per_sm);
+int group_kernel_capacity(axia_ctx* ctx, int lanes, int vec, int* per_sm, bool coarse = false);
 void group_layout(const axia_ctx* ctx, int lanes_req, int vec_req, int* lanes, int* vec);
 int launch_group_reliable(axia_ctx* ctx, BsrReliableArgs& P, const MeshGroup* groups, const int* cta_group,
-                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes, int vec);
+                          GridBarrier* bars, double* totals4, PcgOut* outs, int grid, int lanes, int vec, bool coarse = false);
 int launch_full_rhs(axia_ctx* ctx, const double* d_f);
 int launch_full_reconstruct(axia_ctx* ctx, double* d_u);
 int prepare_full_buffers(axia_ctx* ctx);

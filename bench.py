@@ -327,17 +327,29 @@ def run_c4b(args):
     f = torch.from_numpy(np.concatenate([c.cload for c in cubes])).to(f"cuda:{local}")
     u = torch.empty_like(f)
 
-    def step():
+    def step_jacobi():
         ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
         return ctx.solve_multi_device(f.data_ptr(), u.data_ptr(), rtol=RTOL, inner_rtol=args.delta)
+
+    def step():
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        return ctx.solve_multi_device(f.data_ptr(), u.data_ptr(), rtol=RTOL, inner_rtol=args.delta,
+                                      preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes // 4)
+    msj, (infoj, relj, itsj) = timer(step_jacobi, args.warmup, args.steps)
+    uj = u.clone()
     ms, (info, rel, its) = timer(step, args.warmup, args.steps)
+    err_j = float(torch.linalg.norm(u - uj) / torch.linalg.norm(uj))
+    n_sub, n_coarse = ctx.coarse_size()
     nf = ctx.n_free
     _line(args, "64 C3D8 cubes, edge counts U{10..40} (seeded), x=0 clamped, random surface loads",
           nf / (ms * 1e-3) / 1e6, ms,
           {"dtype": "f32+f64", "config": {"workload": "64 cubes", "n_free": nf, "meshes": 64,
-                                          "sizes": [int(c.shape[0]) for c in cubes]},
+                                          "sizes": [int(c.shape[0]) for c in cubes],
+                                          "preconditioner": f"diagonal + per-mesh coarse spaces ({n_sub} subdomains)"},
            "multi": {"max_iters": int(its.max()), "min_iters": int(its.min()), "max_rel_residual": float(rel.max()),
-                     "ms_kernel": info.ms_pcg_kernel, "ms_assemble": info.ms_assemble}})
+                     "ms_kernel": info.ms_pcg_kernel, "ms_assemble": info.ms_assemble,
+                     "rel_err_vs_diagonal": err_j, "coarse_unknowns": n_coarse},
+           "multi_diagonal": {"ms_per_step": msj, "max_iters": int(itsj.max()), "ms_kernel": infoj.ms_pcg_kernel}})
 
 
 def run_c5(args):
