@@ -147,44 +147,29 @@ __device__ __forceinline__ bool grid_reduce_sync_wide(GridBarrier* bar, DevStatu
   __shared__ unsigned s_gen;
   __syncthreads();
   if (threadIdx.x == 0) {
-    s_gen = ld_acquire_gpu(&bar->gen);
-    __threadfence();
-    s_last = atomicAdd(&bar->count, 1u) == gridDim.x - 1;
+    int last;
+    s_gen = barrier_arrive(bar, gridDim.x, &last);
+    s_last = last;
   }
   __syncthreads();
   int ok = 1;
   if (s_last) {
-    __threadfence();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int k = warp; k < nv; k += nw) {
-      double a = 0.0;
-      for (int j = lane; j < (int)gridDim.x; j += 32) a += __ldcg(partials + (size_t)(slot0 + k) * gridDim.x + j);
+      const int cnt = lane < (int)gridDim.x ? ((int)gridDim.x - lane + 31) / 32 : 0;
+      double a = ldcg_sum(partials + (size_t)(slot0 + k) * gridDim.x + lane, 32, cnt);
       a = warp_sum(a);
       if (lane == 0) totals[slot0 + k] = a;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      bar->count = 0;
       __threadfence();
-      st_release_gpu(&bar->gen, s_gen + 1);
+      barrier_release(bar, s_gen);
     }
   } else if (threadIdx.x == 0) {
-    unsigned long long t0 = global_ns();
-    unsigned spins = 0;
-    while (ld_acquire_gpu(&bar->gen) == s_gen) {
-      if ((++spins & 63u) == 0 && global_ns() - t0 > limit_ns) {
-        atomicExch(&st->timeout, 1);
-        ok = 0;
-        break;
-      }
-      __nanosleep(32);
-    }
+    ok = barrier_wait(bar, st, limit_ns, s_gen);
   }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (*(volatile int*)&st->timeout) ok = 0;
-    s_ok = ok;
-  }
+  if (threadIdx.x == 0) s_ok = ok;
   __syncthreads();
   return s_ok != 0;
 }
@@ -285,11 +270,9 @@ __device__ __forceinline__ void coarse_restrict_m(const CoarseArgs& C, const flo
     if (last) {
       __threadfence();
 #pragma unroll
-      for (int i = 0; i < 6; ++i) {
-        float sum = 0.f;
-        for (int k = c0; k < c1; ++k) sum += __ldcg(C.part_m + ((size_t)k * 6 + i) * NR + lane);
-        C.rc_m[(size_t)(6 * I + i) * NR + lane] = sum;
-      }
+      for (int i = 0; i < 6; ++i)
+        C.rc_m[(size_t)(6 * I + i) * NR + lane] =
+            ldcg_sum(C.part_m + ((size_t)c0 * 6 + i) * NR + lane, (size_t)6 * NR, c1 - c0);
       if (lane == 0) atomicExch(C.cnt + I, 0);
     }
   }

@@ -171,9 +171,10 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_bsr_kernel(BsrPcgArgs<V> P) {
     bb_p = fma(bi, bi, bb_p);
   }
   block_partials<A>(bb_p, rz_p, 2, P.partials, S_RR, S_RZ);
-  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
-  A rz = (A)total(P.totals, S_RZ);
-  const double bnorm = sqrt(total(P.totals, S_RR));
+  double red[REDUCE_MAX_NV];
+  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2, red)) return;
+  A rz = (A)red[1];
+  const double bnorm = sqrt(red[0]);
   long long iters = 0;
   double residual = bnorm;
   int status = AXIA_OK;
@@ -195,8 +196,9 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_bsr_kernel(BsrPcgArgs<V> P) {
         }
       }
       block_partials<A>(pq_p, A(0), 1, P.partials, S_PQ, S_PQ);
-      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1)) return;
-      const A pq = (A)total(P.totals, S_PQ);
+      double red[REDUCE_MAX_NV];
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1, red)) return;
+      const A pq = (A)red[0];
       if (!(fabs((double)pq) >= 1e-30)) {
         status = AXIA_ERR_ZERO_PIVOT;
         break;
@@ -211,9 +213,9 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_bsr_kernel(BsrPcgArgs<V> P) {
         rzn_p = fma(ri, ri * P.dinv[i], rzn_p);
       }
       block_partials<A>(rr_p, rzn_p, 2, P.partials, S_RR, S_RZ);
-      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
-      const A rzn = (A)total(P.totals, S_RZ);
-      residual = sqrt(total(P.totals, S_RR));
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2, red)) return;
+      const A rzn = (A)red[1];
+      residual = sqrt(red[0]);
       if (!isfinite(residual)) {
         status = AXIA_ERR_NONFINITE;
         break;
@@ -260,8 +262,9 @@ __device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const Coar
   __shared__ __align__(16) float s_rc[COARSE_MAX];
   const float acc = coarse_solve(C, s_rc, gwarp, nwarps, lane);
   block_partials<float>(acc, 0.f, 1, R.partials, S_RC, S_RC, R.nblk, R.rank);
-  if (!group_reduce_sync(R.bar, P.st, P.limit_ns, R.partials, R.totals, S_RC, 1, R.nblk)) return false;
-  *rz_c = (float)total(R.totals, S_RC);
+  double red[REDUCE_MAX_NV];
+  if (!group_reduce_sync(R.bar, P.st, P.limit_ns, R.partials, R.totals, S_RC, 1, R.nblk, red)) return false;
+  *rz_c = (float)red[0];
   return true;
 }
 
@@ -293,9 +296,10 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
     bb_p = fma(bi, bi, bb_p);
   }
   block_partials<double>(bb_p, (double)rz_p, 2, partials, S_RR, S_RZ, R.nblk, R.rank);
-  if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk)) return;
-  float rz = (float)total(totals, S_RZ);
-  const double bnorm = sqrt(total(totals, S_RR));
+  double red[REDUCE_MAX_NV];
+  if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk, red)) return;
+  float rz = (float)red[1];
+  const double bnorm = sqrt(red[0]);
   double rmax = bnorm, residual = bnorm;
   long long iters = 0;
   int updates = 0, status = AXIA_OK;
@@ -333,8 +337,9 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
       }
     }
     block_partials<float>(pq_p, 0.f, 1, partials, S_PQ, S_PQ, R.nblk, R.rank);
-    if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_PQ, 1, R.nblk)) return;
-    const float pq = (float)total(totals, S_PQ);
+    double red[REDUCE_MAX_NV];
+    if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_PQ, 1, R.nblk, red)) return;
+    const float pq = (float)red[0];
     if (!(fabsf(pq) >= 1e-30f) || !isfinite(pq)) {
       status = isfinite(pq) ? AXIA_ERR_ZERO_PIVOT : AXIA_ERR_NONFINITE;
       break;
@@ -353,9 +358,9 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
       }
     }
     block_partials<float>(rr_p, rzn_p, 2, partials, S_RR, S_RZ, R.nblk, R.rank);
-    if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk)) return;
-    float rzn = (float)total(totals, S_RZ);
-    const double rnorm32 = sqrt(total(totals, S_RR));
+    if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk, red)) return;
+    float rzn = (float)red[1];
+    const double rnorm32 = sqrt(red[0]);
     if (!isfinite(rnorm32)) {
       status = AXIA_ERR_NONFINITE;
       break;
@@ -389,10 +394,11 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
         }
       }
       block_partials<double>(rr64_p, (double)rz_new_p, 2, partials, S_RR, S_RZ, R.nblk, R.rank);
-      if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk)) return;
+      double red[REDUCE_MAX_NV];
+      if (!group_reduce_sync(R.bar, P.st, P.limit_ns, partials, totals, S_RR, 2, R.nblk, red)) return;
       ++updates;
-      residual = sqrt(total(totals, S_RR));
-      rzn = (float)total(totals, S_RZ);
+      residual = sqrt(red[0]);
+      rzn = (float)red[1];
       rmax = residual;
       if (!isfinite(residual)) {
         status = AXIA_ERR_NONFINITE;

@@ -71,11 +71,7 @@ __device__ __forceinline__ void coarse_chunk_finish(const CoarseArgs& C, int c, 
   last = __shfl_sync(0xffffffffu, last, 0);
   if (last) {
     __threadfence();
-    if (lane < 6) {
-      float s = 0.f;
-      for (int k = c0; k < c1; ++k) s += __ldcg(C.part + 6 * k + lane);
-      C.rc[6 * I + lane] = s;
-    }
+    if (lane < 6) C.rc[6 * I + lane] = ldcg_sum(C.part + 6 * c0 + lane, 6, c1 - c0);
     if (lane == 0) atomicExch(C.cnt + I, 0);
   }
 }

@@ -53,41 +53,104 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// Grid-wide barrier for a cooperative (co-resident) launch.  The wait is
-// bounded: after `limit_ns` the block records a timeout and returns false;
-// every caller then leaves its loop, so a stuck barrier ends all blocks.
+// s = 0 + p[0] + p[stride] + ... + p[(n-1) stride] in that order, read with
+// ld.cg (values another block or warp wrote), eight loads in flight at a time.
+template <typename T>
+__device__ __forceinline__ T ldcg_sum(const T* p, size_t stride, int n) {
+  T s = T(0);
+  int k = 0;
+  for (; k + 8 <= n; k += 8) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldcg(p + (size_t)(k + u) * stride);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s += v[u];
+  }
+  for (; k < n; ++k) s += __ldcg(p + (size_t)k * stride);
+  return s;
+}
+
+// Grid-wide barrier for a cooperative (co-resident) launch: one 64-bit word,
+// generation in the upper half, arrivals at the current barrier in the lower
+// half (the host zeroes it before every launch).  An arrival is one atomic
+// add; the last block stores (generation + 1) << 32, which releases the
+// others and re-arms the count in one write (no block can arrive at the next
+// barrier before that store).  The wait is bounded: after `limit_ns`, or once
+// another block has recorded a timeout, the block records it and returns
+// false; every caller then leaves its loop, so a stuck barrier ends all blocks.
 struct GridBarrier {
-  unsigned count;
-  unsigned gen;
+  unsigned long long word;
+  unsigned long long pad[15];  // one L2 line per barrier
 };
+
+__device__ __forceinline__ unsigned long long ld_acquire_gpu64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed_gpu64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Arrival of the calling block (one thread): its writes are released and the
+// generation it waits past is returned; *last is set for the final arrival,
+// which has then acquired every other block's writes.  The blocks of a group
+// barrier (the CTAs of one system inside a multi-system launch, nblk <
+// gridDim.x) first read the word once: measured on 64 meshes in one launch,
+// the solve ran 22 % faster with that read, while a whole-grid barrier ran
+// 0.4 % slower with it, so only group barriers take it.
+__device__ __forceinline__ unsigned barrier_arrive(GridBarrier* bar, unsigned nblk, int* last) {
+  if (nblk != gridDim.x) (void)ld_acquire_gpu64(&bar->word);
+  __threadfence();
+  const unsigned long long old = atomicAdd(&bar->word, 1ull);
+  *last = (unsigned)(old & 0xffffffffull) == nblk - 1;
+  if (*last) __threadfence();
+  return (unsigned)(old >> 32);
+}
+
+__device__ __forceinline__ void barrier_release(GridBarrier* bar, unsigned g) {
+  st_release_gpu64(&bar->word, (unsigned long long)(g + 1u) << 32);
+}
+
+// Bounded wait (one thread) until generation g has been released.  The polls
+// are relaxed loads (an acquire load per poll costs the blocks that share the
+// SM measurably: 1 % on the two-level CG); the fence after the loop that saw
+// the release makes it an acquire.
+__device__ __forceinline__ bool barrier_wait(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns, unsigned g) {
+  const unsigned long long t0 = global_ns();
+  unsigned spins = 0;
+  while ((unsigned)(ld_relaxed_gpu64(&bar->word) >> 32) == g) {
+    if ((++spins & 63u) == 0) {
+      if (*(volatile int*)&st->timeout) return false;
+      if (global_ns() - t0 > limit_ns) {
+        atomicExch(&st->timeout, 1);
+        return false;
+      }
+    }
+    if (spins > 128) __nanosleep(32);
+  }
+  __threadfence();
+  return true;
+}
 
 // Barrier over a group of nblk co-resident blocks (the whole grid: nblk = gridDim.x).
 __device__ __forceinline__ bool group_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns, unsigned nblk) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
+    int last;
+    const unsigned g = barrier_arrive(bar, nblk, &last);
     int ok = 1;
-    unsigned g = ld_acquire_gpu(&bar->gen);
-    __threadfence();
-    unsigned arrived = atomicAdd(&bar->count, 1u);
-    if (arrived == nblk - 1) {
-      bar->count = 0;
-      __threadfence();
-      st_release_gpu(&bar->gen, g + 1);
-    } else {
-      unsigned long long t0 = global_ns();
-      unsigned spins = 0;
-      while (ld_acquire_gpu(&bar->gen) == g) {
-        if ((++spins & 63u) == 0 && global_ns() - t0 > limit_ns) {
-          atomicExch(&st->timeout, 1);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    if (*(volatile int*)&st->timeout) ok = 0;
+    if (last)
+      barrier_release(bar, g);
+    else
+      ok = barrier_wait(bar, st, limit_ns, g);
     s_ok = ok;
   }
   __syncthreads();
@@ -99,66 +162,92 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, DevStatus* st, unsig
 }
 
 // Grid-wide barrier that also reduces.  Every block has stored its partials of
-// nv values at partials[(slot0 + k) * gridDim.x + blockIdx.x]; the last block
-// to arrive sums them in ascending block order (a fixed order, so every run
-// gives the same bits) and publishes totals[slot0 + k] before it releases the
-// others.  Same bounded wait as grid_sync.  After it returns, every thread may
-// read totals[] (with ld.cg: they were written by another block).
-__device__ __forceinline__ bool group_reduce_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns,
-                                                  const double* partials, double* totals, int slot0, int nv,
-                                                  unsigned nblk) {
-  __shared__ int s_ok2;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    unsigned g = 0;
-    int last = 0;
-    if (lane == 0) {
-      g = ld_acquire_gpu(&bar->gen);
-      __threadfence();
-      last = atomicAdd(&bar->count, 1u) == nblk - 1;
-    }
-    last = __shfl_sync(0xffffffffu, last, 0);
-    int ok = 1;
-    if (last) {
-      __threadfence();
-      for (int k = 0; k < nv; ++k) {
-        double a = 0.0;
-        for (int j = lane; j < (int)nblk; j += 32) a += __ldcg(partials + (size_t)(slot0 + k) * nblk + j);
-        a = warp_sum(a);
-        if (lane == 0) totals[slot0 + k] = a;
-      }
-      __syncwarp();
-      if (lane == 0) {
-        bar->count = 0;
-        __threadfence();
-        st_release_gpu(&bar->gen, g + 1);
-      }
-    } else if (lane == 0) {
-      unsigned long long t0 = global_ns();
-      unsigned spins = 0;
-      while (ld_acquire_gpu(&bar->gen) == g) {
-        if ((++spins & 63u) == 0 && global_ns() - t0 > limit_ns) {
-          atomicExch(&st->timeout, 1);
-          ok = 0;
-          break;
-        }
-        if (spins > 256) __nanosleep(16);
-      }
-    }
-    if (lane == 0) {
-      __threadfence();
-      if (*(volatile int*)&st->timeout) ok = 0;
-      s_ok2 = ok;
+// nv <= 4 values at partials[(slot0 + k) * nblk + rank]; the last block to
+// arrive sums them with all its threads (one L2 round trip; thread t takes
+// blocks t, t + blockDim.x, ..., then warps and the warp sums in order: a fixed
+// order, so every run gives the same bits) and publishes totals[slot0 + k]
+// before it releases the others.  Same bounded wait as grid_sync.  With res,
+// thread 0 of every block copies the totals into shared memory and every
+// thread gets them in res[0..nv) (one L2 read per block instead of one per
+// warp on a single line); without, threads read totals[] with ld.cg.
+constexpr int REDUCE_MAX_NV = 4;
+
+// The last block's part of group_reduce_sync (every thread of the block calls
+// it).  Not inlined: its registers stay out of the allocation of the CG loops
+// that call the barrier.
+static __device__ __noinline__ void reduce_partials_last_block(const double* partials, double* totals, double* s_tot,
+                                                        int slot0, int nv, unsigned nblk) {
+  __shared__ double s_sum[REDUCE_MAX_NV][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  double a[REDUCE_MAX_NV];
+#pragma unroll
+  for (int k = 0; k < REDUCE_MAX_NV; ++k) a[k] = 0.0;
+  for (int j = threadIdx.x; j < (int)nblk; j += blockDim.x) {
+    double v[REDUCE_MAX_NV];
+#pragma unroll
+    for (int k = 0; k < REDUCE_MAX_NV; ++k) v[k] = k < nv ? __ldcg(partials + (size_t)(slot0 + k) * nblk + j) : 0.0;
+#pragma unroll
+    for (int k = 0; k < REDUCE_MAX_NV; ++k) a[k] += v[k];
+  }
+#pragma unroll
+  for (int k = 0; k < REDUCE_MAX_NV; ++k) {
+    if (k < nv) {
+      a[k] = warp_sum(a[k]);
+      if (lane == 0) s_sum[k][warp] = a[k];
     }
   }
   __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < REDUCE_MAX_NV; ++k) {
+      if (k < nv) {
+        double t = lane < nw ? s_sum[k][lane] : 0.0;
+        t = warp_sum(t);
+        if (lane == 0) {
+          totals[slot0 + k] = t;
+          s_tot[k] = t;
+        }
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ bool group_reduce_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns,
+                                                  const double* partials, double* totals, int slot0, int nv,
+                                                  unsigned nblk, double* res = nullptr) {
+  __shared__ int s_last, s_ok2;
+  __shared__ unsigned s_gen;
+  __shared__ double s_tot[REDUCE_MAX_NV];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int last;
+    s_gen = barrier_arrive(bar, nblk, &last);
+    s_last = last;
+  }
+  __syncthreads();
+  int ok = 1;
+  if (s_last) {
+    reduce_partials_last_block(partials, totals, s_tot, slot0, nv, nblk);
+    if (threadIdx.x == 0) {
+      __threadfence();
+      barrier_release(bar, s_gen);
+    }
+  } else if (threadIdx.x == 0) {
+    ok = barrier_wait(bar, st, limit_ns, s_gen);
+    if (ok && res)
+      for (int k = 0; k < nv; ++k) s_tot[k] = __ldcg(totals + slot0 + k);
+  }
+  if (threadIdx.x == 0) s_ok2 = ok;
+  __syncthreads();
+  if (res)
+    for (int k = 0; k < nv; ++k) res[k] = s_tot[k];
   return s_ok2 != 0;
 }
 
 __device__ __forceinline__ bool grid_reduce_sync(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns,
-                                                 const double* partials, double* totals, int slot0, int nv) {
-  return group_reduce_sync(bar, st, limit_ns, partials, totals, slot0, nv, gridDim.x);
+                                                 const double* partials, double* totals, int slot0, int nv,
+                                                 double* res = nullptr) {
+  return group_reduce_sync(bar, st, limit_ns, partials, totals, slot0, nv, gridDim.x, res);
 }
 
 // Streaming (evict-first) loads for matrix data that is read once per sweep,

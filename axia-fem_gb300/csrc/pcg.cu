@@ -62,9 +62,10 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_kernel(PcgArgs<V> P) {
     bb_p = fma(bi, bi, bb_p);
   }
   block_partials<A>(bb_p, rz_p, 2, P.partials, S_RR, S_RZ);
-  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
-  A rz = (A)total(P.totals, S_RZ);
-  const double bnorm = sqrt(total(P.totals, S_RR));
+  double red[REDUCE_MAX_NV];
+  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2, red)) return;
+  A rz = (A)red[1];
+  const double bnorm = sqrt(red[0]);
   long long iters = 0;
   double residual = bnorm;
   int status = AXIA_OK;
@@ -82,8 +83,9 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_kernel(PcgArgs<V> P) {
         }
       }
       block_partials<A>(pq_p, A(0), 1, P.partials, S_PQ, S_PQ);
-      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1)) return;
-      const A pq = (A)total(P.totals, S_PQ);
+      double red[REDUCE_MAX_NV];
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1, red)) return;
+      const A pq = (A)red[0];
       if (!(fabs((double)pq) >= 1e-30)) {
         status = AXIA_ERR_ZERO_PIVOT;
         break;
@@ -99,9 +101,9 @@ __global__ void __launch_bounds__(PCG_THREADS) pcg_kernel(PcgArgs<V> P) {
         rzn_p = fma(ri, ri * P.dinv[i], rzn_p);
       }
       block_partials<A>(rr_p, rzn_p, 2, P.partials, S_RR, S_RZ);
-      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
-      const A rzn = (A)total(P.totals, S_RZ);
-      residual = sqrt(total(P.totals, S_RR));
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2, red)) return;
+      const A rzn = (A)red[1];
+      residual = sqrt(red[0]);
       if (!isfinite(residual)) {
         status = AXIA_ERR_NONFINITE;
         break;
@@ -177,9 +179,10 @@ __global__ void __launch_bounds__(PCG_THREADS, 4) pcg_reliable_kernel(ReliableAr
     bb_p = fma(bi, bi, bb_p);
   }
   block_partials<double>(bb_p, (double)rz_p, 2, P.partials, S_RR, S_RZ);
-  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
-  float rz = (float)total(P.totals, S_RZ);
-  const double bnorm = sqrt(total(P.totals, S_RR));
+  double red[REDUCE_MAX_NV];
+  if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2, red)) return;
+  float rz = (float)red[1];
+  const double bnorm = sqrt(red[0]);
   double rmax = bnorm;       // residual norm at the last update
   double residual = bnorm;   // FP64 residual norm at the last update
   long long iters = 0;
@@ -202,8 +205,9 @@ __global__ void __launch_bounds__(PCG_THREADS, 4) pcg_reliable_kernel(ReliableAr
       }
     }
     block_partials<float>(pq_p, 0.f, 1, P.partials, S_PQ, S_PQ);
-    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1)) return;
-    const float pq = (float)total(P.totals, S_PQ);
+    double red[REDUCE_MAX_NV];
+    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_PQ, 1, red)) return;
+    const float pq = (float)red[0];
     if (!(fabsf(pq) >= 1e-30f) || !isfinite(pq)) {
       status = isfinite(pq) ? AXIA_ERR_ZERO_PIVOT : AXIA_ERR_NONFINITE;
       break;
@@ -218,9 +222,9 @@ __global__ void __launch_bounds__(PCG_THREADS, 4) pcg_reliable_kernel(ReliableAr
       rzn_p = fmaf(ri, ri * P.dinv32[i], rzn_p);
     }
     block_partials<float>(rr_p, rzn_p, 2, P.partials, S_RR, S_RZ);
-    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
-    float rzn = (float)total(P.totals, S_RZ);
-    const double rnorm32 = sqrt(total(P.totals, S_RR));
+    if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2, red)) return;
+    float rzn = (float)red[1];
+    const double rnorm32 = sqrt(red[0]);
     if (!isfinite(rnorm32)) {
       status = AXIA_ERR_NONFINITE;
       break;
@@ -251,10 +255,11 @@ __global__ void __launch_bounds__(PCG_THREADS, 4) pcg_reliable_kernel(ReliableAr
         }
       }
       block_partials<double>(rr64_p, (double)rz_new_p, 2, P.partials, S_RR, S_RZ);
-      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2)) return;
+      double red[REDUCE_MAX_NV];
+      if (!grid_reduce_sync(P.bar, P.st, P.limit_ns, P.partials, P.totals, S_RR, 2, red)) return;
       ++updates;
-      residual = sqrt(total(P.totals, S_RR));
-      rzn = (float)total(P.totals, S_RZ);
+      residual = sqrt(red[0]);
+      rzn = (float)red[1];
       rmax = residual;
       if (!isfinite(residual)) {
         status = AXIA_ERR_NONFINITE;
