@@ -184,6 +184,15 @@ class GpuContext:
     def kernel_launches(self) -> int:
         return int(self.lib.axia_gpu_kernel_launches(self.h))
 
+    def check_wait_limit(self, limit_us: int):
+        """Run one device wait that cannot complete with the given limit;
+        returns (status the host saw, probe kernel ms)."""
+        st = C.c_int32(0)
+        ms = C.c_double(0.0)
+        self._check(self.lib.axia_gpu_check_wait_limit(self.h, int(limit_us), C.byref(st), C.byref(ms)),
+                    "check_wait_limit")
+        return int(st.value), float(ms.value)
+
     def spmv_device(self, precision, x_dev_ptr, y_dev_ptr, lanes=0):
         self._check(self.lib.axia_gpu_spmv_device(self.h, int(precision), C.c_void_p(x_dev_ptr),
                                                   C.c_void_p(y_dev_ptr), int(lanes)), "spmv")

@@ -544,6 +544,42 @@ int32_t axia_gpu_set_stream(axia_ctx* ctx, void* stream) {
 
 int64_t axia_gpu_kernel_launches(const axia_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
+// One block at a barrier of two: the second arrival never comes, so the
+// bounded wait runs out, records the timeout and returns.
+__global__ void k_wait_probe(GridBarrier* bar, DevStatus* st, unsigned long long limit_ns) {
+  (void)group_sync(bar, st, limit_ns, 2u);
+}
+
+int32_t axia_gpu_check_wait_limit(axia_ctx* ctx, int64_t limit_us, int32_t* status, double* elapsed_ms) {
+  if (!ctx || !status || limit_us < 1 || limit_us > 10000000) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->d_bar) AXIA_TRY(dev_alloc(ctx, &ctx->d_bar, 1));
+  AXIA_TRY(reset_dev_status(ctx));
+  AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
+  cudaEvent_t a, b;
+  AXIA_CUDA(ctx, cudaEventCreate(&a));
+  AXIA_CUDA(ctx, cudaEventCreate(&b));
+  cudaEventRecord(a, ctx->stream);
+  k_wait_probe<<<1, 32, 0, ctx->stream>>>(ctx->d_bar, ctx->d_status, (unsigned long long)limit_us * 1000ull);
+  ctx->launches++;
+  cudaEventRecord(b, ctx->stream);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float ms = 0.f;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (e != cudaSuccess) return set_error(ctx, AXIA_ERR_CUDA, std::string("wait probe: ") + cudaGetErrorString(e));
+  DevStatus hs;
+  AXIA_TRY(read_dev_status(ctx, &hs));
+  *status = hs.timeout ? AXIA_ERR_TIMEOUT : AXIA_OK;
+  if (elapsed_ms) *elapsed_ms = ms;
+  AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
+  AXIA_TRY(reset_dev_status(ctx));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXIA_OK;
+}
+
 int32_t axia_gpu_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev, int32_t lanes) {
   if (!ctx || !x_dev || !y_dev) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));

@@ -229,6 +229,15 @@ AXIA_API int32_t axia_gpu_set_stream(axia_ctx* ctx, void* stream);
 /* Number of kernels the context has launched so far. */
 AXIA_API int64_t axia_gpu_kernel_launches(const axia_ctx* ctx);
 
+/* Diagnostic of the bounded device waits: runs one wait that cannot complete
+ * (a single block arriving at a grid barrier sized for two) with a limit of
+ * limit_us microseconds (1 .. 10,000,000) and reports what the host saw:
+ * *status = AXIA_ERR_TIMEOUT when the wait gave up and recorded it (the
+ * expected outcome), *elapsed_ms = the probe kernel's duration.  Barrier and
+ * status word are re-armed afterwards, so the context stays usable.  Returns
+ * AXIA_OK unless the call itself failed. */
+AXIA_API int32_t axia_gpu_check_wait_limit(axia_ctx* ctx, int64_t limit_us, int32_t* status, double* elapsed_ms);
+
 /* y = K_ff x on device vectors of n_free entries: FP64 (double x, y) with
  * precision AXIA_PREC_FP64, FP32 (float x, y, the FP32 copy of K_ff) with
  * AXIA_PREC_MIXED.  lanes: CSR lanes per row (0 = automatic).  The matrix
