@@ -361,6 +361,59 @@ __global__ void k_sort_incidence(int64_t n_nodes, const int64_t* ptr, int32_t* n
 // Adjacency of node a: sorted unique nodes of its incident elements.
 // mode 0 counts (cnt[a]), mode 1 writes adj[ptr[a] ...].  One warp per node;
 // candidates staged in shared memory (cap per warp = cap).
+// Sorted distinct neighbours of one node from its m <= 32 K candidates, in
+// registers: element i = 32 k + lane of a bitonic network over 32 K slots
+// (padding INT_MAX), partners within a lane swapped in registers, across
+// lanes exchanged by shuffles.  mode 0 returns the count, mode 1 also writes
+// the list (ascending) to out.
+template <int K>
+__device__ __forceinline__ int warp_sorted_unique(int m, int nn, const int32_t* conn, const int32_t* ne_b0, int lane,
+                                                  int mode, int32_t* out) {
+  int v[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int t = 32 * k + lane;
+    v[k] = t < m ? conn[(int64_t)(ne_b0[t / nn] >> 5) * nn + (t % nn)] : INT_MAX;
+  }
+#pragma unroll
+  for (int size = 2; size <= 32 * K; size <<= 1) {
+#pragma unroll
+    for (int j = size >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+        const int J = j >> 5;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          if (k & J) continue;
+          const bool asc = ((32 * k + lane) & size) == 0;
+          const int lo = min(v[k], v[k | J]), hi = max(v[k], v[k | J]);
+          v[k] = asc ? lo : hi;
+          v[k | J] = asc ? hi : lo;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const int o = __shfl_xor_sync(0xffffffffu, v[k], j);
+          const bool asc = ((32 * k + lane) & size) == 0;
+          const bool lower = (lane & j) == 0;
+          v[k] = (lower == asc) ? min(v[k], o) : max(v[k], o);
+        }
+      }
+    }
+  }
+  int count = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    int prev = __shfl_up_sync(0xffffffffu, v[k], 1);
+    const int last_prev = k > 0 ? __shfl_sync(0xffffffffu, v[k > 0 ? k - 1 : 0], 31) : INT_MIN;
+    if (lane == 0) prev = last_prev;
+    const bool f = v[k] != INT_MAX && v[k] != prev;
+    const unsigned bal = __ballot_sync(0xffffffffu, f);
+    if (mode == 1 && f) out[count + __popc(bal & ((1u << lane) - 1u))] = v[k];
+    count += __popc(bal);
+  }
+  return count;
+}
+
 __global__ void k_adjacency(int64_t n_nodes, int nn, const int32_t* conn, const int64_t* ne_ptr,
                             const int32_t* ne, int cap, int mode, int64_t* cnt, const int64_t* adj_ptr,
                             int32_t* adj, DevStatus* st) {
@@ -374,6 +427,18 @@ __global__ void k_adjacency(int64_t n_nodes, int nn, const int32_t* conn, const 
     int m = (int)(b1 - b0) * nn;
     if (m > cap) {
       if (lane == 0) record_error(st, a, AXIA_ERR_TOO_LARGE);
+      continue;
+    }
+    if (m <= 256) {  // register sort (warp-uniform branch: m is the node's)
+      int32_t* out = mode == 1 ? adj + adj_ptr[a] : nullptr;
+      int c;
+      if (m <= 64)
+        c = warp_sorted_unique<2>(m, nn, conn, ne + b0, lane, mode, out);
+      else if (m <= 128)
+        c = warp_sorted_unique<4>(m, nn, conn, ne + b0, lane, mode, out);
+      else
+        c = warp_sorted_unique<8>(m, nn, conn, ne + b0, lane, mode, out);
+      if (mode == 0 && lane == 0) cnt[a] = c;
       continue;
     }
     for (int t = lane; t < m; t += 32) {
