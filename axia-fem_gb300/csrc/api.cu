@@ -194,6 +194,7 @@ void axia_gpu_destroy(axia_ctx* ctx) {
   dev_free(ctx->d_partials);
   dev_free(ctx->d_totals);
   dev_free(ctx->d_bar);
+  dev_free(ctx->d_first_bad);
   dev_free(ctx->d_status);
   if (ctx->d_out) cudaFree(ctx->d_out);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -404,11 +405,12 @@ int32_t axia_gpu_solve(axia_ctx* ctx, const double* f_full, double* u_full, cons
   if (!ctx || !f_full || !u_full) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   if (!ctx->assembled || !ctx->d_ind_of) return set_error(ctx, AXIA_ERR_STATE, "solve before assemble");
-  for (int64_t d = 0; d < ctx->ndof; ++d)
-    if (!std::isfinite(f_full[d])) return set_error(ctx, AXIA_ERR_NONFINITE, "load vector entry " + std::to_string(d) + " not finite");
   if (!ctx->d_f) AXIA_TRY(dev_alloc(ctx, &ctx->d_f, (size_t)ctx->ndof));
   if (!ctx->d_u) AXIA_TRY(dev_alloc(ctx, &ctx->d_u, (size_t)ctx->ndof));
   AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_f, f_full, ctx->ndof * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  int64_t bad = -1;
+  AXIA_TRY(device_first_nonfinite(ctx, ctx->d_f, ctx->ndof, &bad));
+  if (bad >= 0) return set_error(ctx, AXIA_ERR_NONFINITE, "load vector entry " + std::to_string(bad) + " not finite");
   int st = solve_common(ctx, ctx->d_f, ctx->d_u, opts, info);
   if (st != AXIA_OK) return st;
   AXIA_CUDA(ctx, cudaMemcpyAsync(u_full, ctx->d_u, ctx->ndof * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -697,15 +699,18 @@ int32_t axia_gpu_solve_batched(axia_ctx* ctx, int32_t nrhs, const double* F, dou
   if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "batched solve before assemble");
   if (nrhs == 0) return AXIA_OK;
   const size_t count = (size_t)nrhs * (size_t)ctx->ndof;
-  for (size_t i = 0; i < count; ++i)
-    if (!std::isfinite(F[i])) return set_error(ctx, AXIA_ERR_NONFINITE, "load case entry not finite");
   double *dF = nullptr, *dU = nullptr;
   AXIA_TRY(dev_alloc(ctx, &dF, count));
   int st = dev_alloc(ctx, &dU, count);
+  if (st == AXIA_OK &&
+      cudaMemcpyAsync(dF, F, count * sizeof(double), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+    st = set_error(ctx, AXIA_ERR_CUDA, "copy of the load cases");
   if (st == AXIA_OK) {
-    cudaMemcpyAsync(dF, F, count * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
-    st = batched_common(ctx, nrhs, dF, dU, opts, info, rel_res);
+    int64_t bad = -1;
+    st = device_first_nonfinite(ctx, dF, (int64_t)count, &bad);
+    if (st == AXIA_OK && bad >= 0) st = set_error(ctx, AXIA_ERR_NONFINITE, "load case entry not finite");
   }
+  if (st == AXIA_OK) st = batched_common(ctx, nrhs, dF, dU, opts, info, rel_res);
   if (st == AXIA_OK) {
     if (cudaMemcpyAsync(U, dU, count * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
         cudaStreamSynchronize(ctx->stream) != cudaSuccess)

@@ -343,6 +343,7 @@ struct axia_ctx {
   double* d_totals = nullptr;
   size_t partial_slots = 0;
   GridBarrier* d_bar = nullptr;
+  unsigned long long* d_first_bad = nullptr;  // first non-finite entry found by device_first_nonfinite
   DevStatus* d_status = nullptr;
   void* d_out = nullptr;        // PcgOut
   size_t vec_capacity = 0;
@@ -482,3 +483,6 @@ int device_exclusive_scan(axia_ctx* ctx, const int64_t* d_in, int64_t* d_out, in
 void coarse_release(axia_ctx* ctx);
 int read_dev_status(axia_ctx* ctx, DevStatus* st_host);
 int reset_dev_status(axia_ctx* ctx);
+// Index of the first non-finite entry of the device vector d_v[0, n) (-1: all
+// finite), checked on the device; one 8-byte read-back.
+int device_first_nonfinite(axia_ctx* ctx, const double* d_v, int64_t n, int64_t* first);

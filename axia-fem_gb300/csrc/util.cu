@@ -23,6 +23,27 @@ int reset_dev_status(axia_ctx* ctx) {
   return AXIA_OK;
 }
 
+__global__ void k_first_nonfinite(int64_t n, const double* v, unsigned long long* first) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!isfinite(v[i])) atomicMin(first, (unsigned long long)i);
+}
+
+int device_first_nonfinite(axia_ctx* ctx, const double* d_v, int64_t n, int64_t* first) {
+  *first = -1;
+  if (n <= 0) return AXIA_OK;
+  if (!ctx->d_first_bad) AXIA_TRY(dev_alloc(ctx, &ctx->d_first_bad, 1));
+  AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_first_bad, 0xff, sizeof(unsigned long long), ctx->stream));
+  const int64_t want = (n + 255) / 256, cap = (int64_t)ctx->sm_count * 8;
+  k_first_nonfinite<<<(unsigned)(want < cap ? want : cap), 256, 0, ctx->stream>>>(n, d_v, ctx->d_first_bad);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  unsigned long long h = ~0ull;
+  AXIA_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_first_bad, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h != ~0ull) *first = (int64_t)h;
+  return AXIA_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Exclusive scan of int64 counts: block-local scan of SCAN_ITEMS per block,
 // scan of the block totals (recursively), then add the block offsets.
