@@ -33,7 +33,8 @@
 // part of the solver's argument pack).
 
 // Builds (or reuses) the coarse space of the current mesh and its operator
-// for the current assembly (coarse.cu); nodes_target <= 0: 2000.
+// for the current assembly (coarse.cu); nodes_target <= 0: about 53,000
+// node blocks per subdomain (2000 nodes for C3D8).
 int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out);
 // The same with the 32-column buffers of the batched load-case solve.
 int coarse_prepare_batched(axia_ctx* ctx, int nodes_target, CoarseArgs* out);

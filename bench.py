@@ -334,7 +334,7 @@ def run_c4b(args):
     def step():
         ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
         return ctx.solve_multi_device(f.data_ptr(), u.data_ptr(), rtol=RTOL, inner_rtol=args.delta,
-                                      preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes // 4)
+                                      preconditioner=L.PRECOND_COARSE, coarse_nodes=(args.coarse_nodes or 2000) // 4)
     msj, (infoj, relj, itsj) = timer(step_jacobi, args.warmup, args.steps)
     uj = u.clone()
     ms, (info, rel, its) = timer(step, args.warmup, args.steps)
@@ -447,7 +447,9 @@ def main():
     ap.add_argument("--lanes32", type=int, default=0)
     ap.add_argument("--lanes32csr", type=int, default=0)
     ap.add_argument("--delta", type=float, default=0.01, help="reliable-update residual reduction")
-    ap.add_argument("--coarse-nodes", type=int, default=2000, help="nodes per subdomain of the coarse space")
+    ap.add_argument("--coarse-nodes", type=int, default=0,
+                    help="nodes per subdomain of the coarse space (0: the library default, about 53,000 "
+                         "matrix node blocks per subdomain)")
     ap.add_argument("--only", choices=["mixed", "coarse", "fp64", "spmv", "batch"], default=None,
                     help="run one solve (or SpMV sweep) once and exit: the profiling entry")
     ap.add_argument("--max-iter", type=int, default=0, help="with --only: cap the CG iterations")

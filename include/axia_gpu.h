@@ -116,7 +116,9 @@ typedef struct axia_solve_opts {
   int32_t matrix_format;   /* axia_matrix_format */
   int32_t spmv_vec;        /* node-block form: blocks per lane load (1, 2, 4; 0 = automatic) */
   int32_t preconditioner;  /* axia_preconditioner (0 = Jacobi) */
-  int32_t coarse_nodes;    /* AXIA_PRECOND_COARSE: nodes per subdomain (0 = 2000; at most 682 subdomains) */
+  int32_t coarse_nodes;    /* AXIA_PRECOND_COARSE: nodes per subdomain (0 = about 53,000 matrix node
+                              blocks per subdomain: 2000 nodes for C3D8, ~950 for C3D20; at most 682
+                              subdomains) */
 } axia_solve_opts;
 
 typedef struct axia_solve_info {
