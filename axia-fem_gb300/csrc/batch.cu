@@ -55,8 +55,11 @@ __device__ __forceinline__ void bsr_row_multi(int a, int lane, const BsrMatM<V>&
 #pragma unroll
     for (int c = 0; c < CPL; ++c) y[i][c] = V(0);
   const int beg = __ldg(M.adj_ptr + a), end = __ldg(M.adj_ptr + a + 1);
+  // the next block's column is loaded one step ahead, so a step waits for one
+  // memory round trip (values and vector rows) instead of two in a row
+  int b = beg + grp < end ? ld_stream(M.adj + beg + grp) : 0;
   for (int s = beg + grp; s < end; s += 32 / LPG) {
-    const int b = ld_stream(M.adj + s);
+    const int b_next = s + 32 / LPG < end ? ld_stream(M.adj + s + 32 / LPG) : 0;
     V v[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) v[k] = ld_stream(M.val + (long long)k * M.nb + s);
@@ -68,6 +71,7 @@ __device__ __forceinline__ void bsr_row_multi(int a, int lane, const BsrMatM<V>&
 #pragma unroll
       for (int c = 0; c < CPL; ++c)
         y[i][c] = fma(v[3 * i], x[0][c], fma(v[3 * i + 1], x[1][c], fma(v[3 * i + 2], x[2][c], y[i][c])));
+    b = b_next;
   }
 #pragma unroll
   for (int i = 0; i < 3; ++i)
@@ -87,8 +91,9 @@ __device__ __forceinline__ void bsr_row_multi_half(int a, int lane, const BsrMat
 #pragma unroll
   for (int i = 0; i < 3; ++i) y[i][0] = y[i][1] = 0.0;
   const int beg = __ldg(M.adj_ptr + a), end = __ldg(M.adj_ptr + a + 1);
+  int b = beg + grp < end ? ld_stream(M.adj + beg + grp) : 0;
   for (int s = beg + grp; s < end; s += 32 / LPG) {
-    const int b = ld_stream(M.adj + s);
+    const int b_next = s + 32 / LPG < end ? ld_stream(M.adj + s + 32 / LPG) : 0;
     double v[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) v[k] = ld_stream(M.val + (long long)k * M.nb + s);
@@ -104,6 +109,7 @@ __device__ __forceinline__ void bsr_row_multi_half(int a, int lane, const BsrMat
 #pragma unroll
       for (int c = 0; c < 2; ++c)
         y[i][c] = fma(v[3 * i], x[0][c], fma(v[3 * i + 1], x[1][c], fma(v[3 * i + 2], x[2][c], y[i][c])));
+    b = b_next;
   }
 #pragma unroll
   for (int i = 0; i < 3; ++i)
