@@ -82,6 +82,74 @@ __device__ __forceinline__ void bsr_row_multi(int a, int lane, const BsrMatM<V>&
     }
 }
 
+// Rows of at most STAGE_B blocks (C3D8 rows have up to 27) are staged: while a
+// warp computes one block row, the matrix values and block columns of its
+// next row are copied to shared memory asynchronously (cp.async, 4 bytes per
+// lane and array), so a step of the row loop waits only for the vector rows
+// (mostly L1 / L2 hits), not for the matrix stream from DRAM.  Longer rows
+// take bsr_row_multi.
+constexpr int STAGE_B = 28;
+struct RowStage {
+  float v[9][STAGE_B];
+  int adj[STAGE_B];
+};
+constexpr size_t STAGE_BYTES = sizeof(RowStage) * 2 * (PCG_THREADS / 32);  // two per warp
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Starts the copy of row a into st (nothing for a >= n_nodes or a long row)
+// and closes the lane's copy group.
+__device__ __forceinline__ void stage_row(int a, int lane, const BsrMatM<float>& M, RowStage* st) {
+  if (a < M.n_nodes) {
+    const int beg = __ldg(M.adj_ptr + a), len = __ldg(M.adj_ptr + a + 1) - beg;
+    if (len <= STAGE_B && lane < len) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) cp_async4(&st->v[k][lane], M.val + (long long)k * M.nb + beg + lane);
+      cp_async4(&st->adj[lane], M.adj + beg + lane);
+    }
+  }
+  cp_async_commit();
+}
+
+// bsr_row_multi for a staged row (len <= STAGE_B blocks, copies complete).
+__device__ __forceinline__ void bsr_row_multi_staged(int len, int lane, const RowStage* st, const float* X,
+                                                     float y[3][CPL]) {
+  const int cl = lane % LPG, grp = lane / LPG;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) y[i][c] = 0.f;
+  for (int s = grp; s < len; s += 32 / LPG) {
+    const int b = st->adj[s];
+    float x[3][CPL];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ld4(X + (size_t)(3 * b + j) * NR + CPL * cl, x[j]);
+    float v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = st->v[k][s];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int c = 0; c < CPL; ++c)
+        y[i][c] = fmaf(v[3 * i], x[0][c], fmaf(v[3 * i + 1], x[1][c], fmaf(v[3 * i + 2], x[2][c], y[i][c])));
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 8);
+      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 16);
+    }
+}
+
 // Y[3a+i][4 cl + 2 h + c], c = 0, 1: two of the lane's four load cases in FP64.
 // The FP64 residual of a reliable update runs in two such halves so that the
 // kernel fits the register budget of two blocks per SM.
@@ -356,6 +424,7 @@ __device__ __forceinline__ bool coarse_step_m(const MultiArgs& P, int gwarp, int
 
 template <bool COARSE>
 __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs P) {
+  extern __shared__ RowStage s_stage[];  // STAGE_BYTES
   __shared__ double s_rz[NR], s_bnorm[NR], s_rmax[NR], s_res[NR];
   __shared__ float s_alpha[NR], s_beta[NR];
   __shared__ int s_active[NR], s_flag;
@@ -428,9 +497,20 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
     iters = it + 1;
     // Q = K P (FP32) and per-column p.q
     float pq_p[CPL] = {0, 0, 0, 0};
-    for (int a = gwarp; a < n_nodes; a += nwarps) {
+    RowStage* const stg = s_stage + 2 * (threadIdx.x >> 5);
+    stage_row(gwarp, lane, P.M32, stg);
+    int kb = 0;
+    for (int a = gwarp; a < n_nodes; a += nwarps, kb ^= 1) {
+      stage_row(a + nwarps, lane, P.M32, stg + (kb ^ 1));
+      cp_async_wait<1>();  // this row's copies (all but the group just opened)
+      __syncwarp();
       float y[3][CPL];
-      bsr_row_multi<float>(a, lane, P.M32, P.P32, y);
+      const int len = __ldg(P.M32.adj_ptr + a + 1) - __ldg(P.M32.adj_ptr + a);
+      if (len <= STAGE_B)
+        bsr_row_multi_staged(len, lane, stg + kb, P.P32, y);
+      else
+        bsr_row_multi<float>(a, lane, P.M32, P.P32, y);
+      __syncwarp();  // every lane is done with stg[kb] before it is refilled
       if (lane < LPG) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
@@ -443,6 +523,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
         }
       }
     }
+    cp_async_wait<0>();  // the last (empty or unused) group
     // lanes 0..7 hold column quads 0..7 of their warp: same mapping as tid % 8
     block_partials_cols<float>(pq_p, P.partials, SL_A);
     if (!grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, SL_A, NR)) return;
@@ -651,7 +732,9 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
   const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.01;
   auto kern = coarse ? pcg_bsr_multi_kernel<true> : pcg_bsr_multi_kernel<false>;
   int grid = 0;
-  AXIA_TRY(coop_grid(ctx, (const void*)kern, (int)std::min<int64_t>(nd, INT32_MAX), &grid));
+  // static + staging shared memory is above the 48 KB a block gets without opting in
+  AXIA_CUDA(ctx, cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STAGE_BYTES));
+  AXIA_TRY(coop_grid(ctx, (const void*)kern, (int)std::min<int64_t>(nd, INT32_MAX), &grid, STAGE_BYTES));
   if ((size_t)grid * 2 * NR > ctx->partial_slots) grid = (int)(ctx->partial_slots / (2 * NR));
   info->iters = 0;
   info->outer_iters = 0;
@@ -670,8 +753,8 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
                 max_iter, 2000000000ull, cargs};
     AXIA_TRY(timed_launch(ctx, info, [&]() -> int {
       void* params[] = {&P};
-      AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params, 0,
-                                                 ctx->stream));
+      AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params,
+                                                 STAGE_BYTES, ctx->stream));
       ctx->launches++;
       return AXIA_OK;
     }));

@@ -202,9 +202,9 @@ int reconstruct_system(axia_ctx* ctx, const ReducedSystem& S, const double* d_x,
 // ---------------------------------------------------------------------------
 // Host helpers for the persistent launches
 // ---------------------------------------------------------------------------
-inline int coop_grid(axia_ctx* ctx, const void* kern, int n, int* grid_out) {
+inline int coop_grid(axia_ctx* ctx, const void* kern, int n, int* grid_out, size_t dyn_smem = 0) {
   int per_sm = 0;
-  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PCG_THREADS, 0));
+  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PCG_THREADS, dyn_smem));
   if (per_sm < 1) return set_error(ctx, AXIA_ERR_CUDA, "PCG kernel does not fit on an SM");
   int grid = per_sm * ctx->sm_count;
   int need = (n + PCG_THREADS - 1) / PCG_THREADS;
