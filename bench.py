@@ -113,7 +113,7 @@ MIXED_TRAFFIC_PER_ALG_BYTE = 0.920
 # the same for pcg_bsr_reliable_kernel<8, 4, true> (two-level), from its ncu
 # capture on the 60^3 block (52.73 GB over 198 iterations and 5 FP64 updates
 # against 57.48 GB of algorithmic bytes, 64 subdomains)
-COARSE_TRAFFIC_PER_ALG_BYTE = 0.917
+COARSE_TRAFFIC_PER_ALG_BYTE = 0.919
 
 
 def spmv_bytes(nnz, n, vbytes):
