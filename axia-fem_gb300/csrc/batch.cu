@@ -362,7 +362,7 @@ __device__ __forceinline__ void coarse_solve_m(const CoarseArgs& C, int gwarp, i
   const int ntask = C.nc * LPG;
   for (int t = gwarp; t < ntask; t += nwarps) {
     const int i = t / LPG, cq = t - i * LPG;
-    const float* mrow = C.minv + (size_t)i * C.ncp;
+    const float* mrow = C.minv + (size_t)i * C.ldm;
     float acc[CPL] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 4
     for (int j = lane; j < C.nc; j += 32) {

@@ -472,6 +472,9 @@ pcg_group_reliable_kernel(BsrReliableArgs P, const MeshGroup* groups, const int*
     C.chunk_hi = G.chunk1;
     C.row0 = G.row0;
     C.row1 = G.row1;
+    C.col0 = G.col0;
+    C.ldm = G.ldm;
+    C.minv += G.moff;
   }
   reliable_body<L32, V32, kL64, 2, COARSE>(P, C, R);
 }

@@ -41,8 +41,24 @@ constexpr int GJ_T = 64;          // Gauss-Jordan tile
 constexpr int GJ_THREADS = 256;   // 16 x 16 threads, 4 x 4 outputs each
 constexpr int ROW_SLOTS = 8;      // subdomains accumulated per pass over a node row
 
+// One diagonal block of the coarse matrix: the unknowns [u0, u0 + n) of the
+// subdomains s0 .. s0 + n / 6 - 1, padded to p (a multiple of GJ_T), stored
+// as a dense p x p matrix at element offset off of a64 / a32 / minv.  One
+// block holds every subdomain, unless the space is built for a multi-mesh
+// solve: then each mesh has its own block (the meshes do not couple).
+struct CoarseBlk {
+  int u0, n, p, s0;
+  long long off;
+};
+
 struct CoarseState {
   int nodes_target = 0;
+  bool per_mesh = false;         // one block per mesh
+  std::vector<CoarseBlk> blk;
+  CoarseBlk* d_blk = nullptr;    // [n_blocks]
+  int* d_sub_blk = nullptr;      // [n_sub] block of every subdomain
+  long long blk_elems = 0;       // sum of p^2
+  int max_p = 0;
   int64_t op_gen = -1;           // assembly the operator was built from
   CoarseArgs args{};
   double h = 0.0;
@@ -52,7 +68,7 @@ struct CoarseState {
   float4* geo = nullptr;
   int* sub_ptr = nullptr;        // [n_sub + 1]
   double* tmat = nullptr;        // [n_sub][6][6]
-  float* minv = nullptr;         // [nc][ncp]
+  float* minv = nullptr;         // [blk_elems] block by block, p x p each
   // operator scratch, kept for the rebuilds after every assembly
   std::vector<int> h_chunk_ptr;  // [n_sub + 1]
   std::vector<int> mesh_sub;     // [n_meshes + 1] subdomains of each mesh (one mesh: 0, n_sub)
@@ -65,9 +81,9 @@ struct CoarseState {
   int* run_cnt = nullptr;        // [n_runs]
   int n_items = 0, n_runs = 0;
   bool items_fresh = false;      // vals already hold the current K's items
-  double* a64 = nullptr;         // [ncp][ncp]
-  float* a32 = nullptr;          // [ncp][ncp] inverted in place
-  double* scale = nullptr;       // [ncp]
+  double* a64 = nullptr;         // [blk_elems]
+  float* a32 = nullptr;          // [blk_elems] inverted in place
+  double* scale = nullptr;       // [ncp] per unknown
   float* piv = nullptr;          // [2][GJ_T][GJ_T]
   float* part = nullptr;         // [n_chunks][6]
   float* rc = nullptr;           // [ncp]
@@ -102,6 +118,8 @@ struct CoarseState {
     dev_release(ctx, rc);
     dev_release(ctx, cnt);
     dev_release(ctx, yc);
+    dev_release(ctx, d_blk);
+    dev_release(ctx, d_sub_blk);
   }
 };
 
@@ -433,12 +451,14 @@ __global__ void __launch_bounds__(32 * ROW_WARPS) k_row_items(int n_nodes, int n
 // A_IJ = T_I^T S T_J into the dense matrix (row stride ld)
 __global__ void k_run_sum(int n_runs, int n_sub, const unsigned* run_key, const int* run_off, const int* run_cnt,
                           const int* perm, const double* __restrict__ vals, const double* __restrict__ tmat,
-                          double* A, int ld) {
+                          double* A, const CoarseBlk* blk, const int* sub_blk) {
   __shared__ double s_S[8][36], s_U[8][36];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_runs; r += nw) {
     const int I = (int)(run_key[r] / (unsigned)n_sub), J = (int)(run_key[r] % (unsigned)n_sub);
+    const CoarseBlk B = blk[sub_blk[I]];
+    if (sub_blk[J] != sub_blk[I]) continue;  // never: the blocks (meshes) do not couple
     const int b = run_off[r], e = b + run_cnt[r];
     double s0 = 0.0, s1 = 0.0;
 #pragma unroll 4
@@ -464,18 +484,21 @@ __global__ void k_run_sum(int n_runs, int n_sub, const unsigned* run_key, const 
       const int i = q / 6, j = q % 6;
       double v = 0.0;
       for (int k = 0; k < 6; ++k) v = fma(TI[6 * k + i], s_U[w][6 * k + j], v);
-      A[(size_t)(6 * I + i) * ld + 6 * J + j] = v;
+      A[B.off + (size_t)(6 * I + i - B.u0) * B.p + 6 * J + j - B.u0] = v;
     }
     __syncwarp();
   }
 }
 
-__global__ void k_scale_to_f32(int ncp, const double* A, const double* scale, float* B) {
-  const int64_t n2 = (int64_t)ncp * ncp;
+// block blockIdx.y: B = diag(s) A diag(s) in FP32; unknowns without a scale
+// (dropped modes, padding) become identity rows and columns
+__global__ void k_scale_to_f32(const CoarseBlk* blk, const double* A, const double* scale, float* B) {
+  const CoarseBlk K = blk[blockIdx.y];
+  const int64_t n2 = (int64_t)K.p * K.p;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n2; t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(t / ncp), j = (int)(t % ncp);
-    const double si = scale[i], sj = scale[j];
-    B[t] = (si == 0.0 || sj == 0.0) ? (i == j ? 1.0f : 0.0f) : (float)(A[t] * si * sj);
+    const int i = (int)(t / K.p), j = (int)(t % K.p);
+    const double si = i < K.n ? scale[K.u0 + i] : 0.0, sj = j < K.n ? scale[K.u0 + j] : 0.0;
+    B[K.off + t] = (si == 0.0 || sj == 0.0) ? (i == j ? 1.0f : 0.0f) : (float)(A[K.off + t] * si * sj);
   }
 }
 
@@ -617,7 +640,8 @@ __device__ __forceinline__ void gj_store_regs(const float (&a)[4][4], float* g, 
 // tile of step k: block 0 updates it alone and inverts it at once (lookahead)
 // while the other blocks update the remaining tiles, so no step waits for a
 // serial pivot inversion except the first.
-__global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P) {
+// Inverts the n x n block at P.A in place; false when a barrier gave up.
+__device__ __forceinline__ bool gj_invert_block(GjArgs P) {
   __shared__ __align__(16) float sa[GJ_T][GJ_LD];
   __shared__ __align__(16) float sb[GJ_T][GJ_LD];
   const int nt = P.n / GJ_T, ld = P.n;
@@ -639,7 +663,7 @@ __global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P) {
     } else if (k > 0) {
       gj_column_panel(P, k - 1, blockIdx.x - 1, gridDim.x - 1);
     }
-    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return false;
     // 2. row panel: A_kj <- P_k A_kj
     for (int j = blockIdx.x; j < nt; j += gridDim.x) {
       if (j == k) continue;
@@ -651,7 +675,7 @@ __global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P) {
       gj_mul(sa, sb, o);
       gj_store_regs(o, tile(k, j), ld);
     }
-    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return false;
     // 3. trailing tiles j <= i (i, j != k): A_ij -= A_ik R_j, mirrored into
     //    A_ji; block 0 takes tile (k+1, k+1) alone and inverts it
     const int m = nt - 1, ntiles = m * (m + 1) / 2;
@@ -713,7 +737,7 @@ __global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P) {
               make_float4(sg * v[0][c], sg * v[1][c], sg * v[2][c], sg * v[3][c]);
       }
     }
-    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+    if (!grid_sync(P.bar, P.st, P.limit_ns)) return false;
   }
   // the last step's P and column panel
   const int k = nt - 1;
@@ -722,20 +746,36 @@ __global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P) {
   } else {
     gj_column_panel(P, k, blockIdx.x - 1, gridDim.x - 1);
   }
+  return true;
+}
+
+// The diagonal blocks of the coarse matrix one after the other (one cooperative
+// launch; the pivot buffers are reused, hence the barrier between blocks).
+__global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P, const CoarseBlk* blk, int nblk) {
+  for (int b = 0; b < nblk; ++b) {
+    if (b > 0 && !grid_sync(P.bar, P.st, P.limit_ns)) return;
+    GjArgs Q = P;
+    Q.A = P.A + blk[b].off;
+    Q.n = blk[b].p;
+    if (!gj_invert_block(Q)) return;
+  }
 }
 
 // M_IJ = T_I diag(s_I) B_IJ diag(s_J) T_J^T in the raw mode basis (thread per pair)
-__global__ void k_minv(int n_sub, int ncp, const float* __restrict__ B, const double* __restrict__ scale,
+__global__ void k_minv(const CoarseBlk* blk, const float* __restrict__ B, const double* __restrict__ scale,
                        const double* __restrict__ tmat, float* M) {
-  const int64_t npair = (int64_t)n_sub * n_sub;
+  const CoarseBlk K = blk[blockIdx.y];  // pairs of the subdomains of block blockIdx.y
+  const int ns = K.n / 6, ncp = K.p;
+  const int64_t npair = (int64_t)ns * ns;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < npair; t += (int64_t)gridDim.x * blockDim.x) {
-    const int I = (int)(t / n_sub), J = (int)(t % n_sub);
+    const int I = K.s0 + (int)(t / ns), J = K.s0 + (int)(t % ns);
     const double* TI = tmat + 36 * I;
     const double* TJ = tmat + 36 * J;
     double Bs[6][6];
     for (int i = 0; i < 6; ++i)
       for (int j = 0; j < 6; ++j)
-        Bs[i][j] = (double)B[(size_t)(6 * I + i) * ncp + 6 * J + j] * scale[6 * I + i] * scale[6 * J + j];
+        Bs[i][j] = (double)B[K.off + (size_t)(6 * I + i - K.u0) * ncp + 6 * J + j - K.u0] * scale[6 * I + i] *
+                   scale[6 * J + j];
     // U[i][l] = sum_j Bs[i][j] T_J[l][j]
     double U[6][6];
     for (int i = 0; i < 6; ++i)
@@ -748,7 +788,7 @@ __global__ void k_minv(int n_sub, int ncp, const float* __restrict__ B, const do
       for (int l = 0; l < 6; ++l) {
         double v = 0.0;
         for (int i = 0; i < 6; ++i) v = fma(TI[6 * k + i], U[i][l], v);
-        M[(size_t)(6 * I + k) * ncp + 6 * J + l] = (float)v;
+        M[K.off + (size_t)(6 * I + k - K.u0) * ncp + 6 * J + l - K.u0] = (float)v;
       }
   }
 }
@@ -798,8 +838,22 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     target[k] = std::max<int64_t>(1, (mesh_a1(k) - mesh_a0(k)) / std::max(1, S->nodes_target));
     tsum += target[k];
   }
-  if (tsum > max_boxes)
-    for (int k = 0; k < nm; ++k) target[k] = std::max<int64_t>(1, target[k] * max_boxes / tsum);
+  if (!S->per_mesh) {
+    if (tsum > max_boxes)
+      for (int k = 0; k < nm; ++k) target[k] = std::max<int64_t>(1, target[k] * max_boxes / tsum);
+  } else {
+    // a block per mesh: at most max_boxes subdomains each, and the blocked
+    // inversion (work ~ sum of block sizes cubed) at most twice that of one
+    // 3072-unknown block
+    const double budget = 2.0 * 3072.0 * 3072.0 * 3072.0;
+    for (int k = 0; k < nm; ++k) target[k] = std::min<int64_t>(target[k], max_boxes);
+    for (int it = 0; it < 200; ++it) {
+      double work = 0.0;
+      for (int k = 0; k < nm; ++k) work += std::pow(6.0 * (double)target[k], 3.0);
+      if (work <= budget) break;
+      for (int k = 0; k < nm; ++k) target[k] = std::max<int64_t>(1, (int64_t)(0.9 * (double)target[k]));
+    }
+  }
   std::vector<Grid3> grids(nm);
   std::vector<int> cell_base(nm + 1, 0);
   double* d_bb = nullptr;
@@ -849,7 +903,7 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
   }
   dev_free(d_bb);
   const int ncell = cell_base[nm];
-  if (ncell > max_boxes + nm)
+  if (!S->per_mesh && ncell > max_boxes + nm)
     return set_error(ctx, AXIA_ERR_TOO_LARGE, "coarse space: more than " + std::to_string(max_boxes) + " subdomains");
   int *d_cell = nullptr, *d_count = nullptr, *d_sub = nullptr, *d_iota = nullptr, *d_cellsub = nullptr;
   int* d_sub_sorted = nullptr;
@@ -898,6 +952,37 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     A.row1 = A.nc;
     A.chunk_lo = 0;
     A.chunk_hi = A.n_chunks;
+    // diagonal blocks of the coarse matrix
+    S->blk.clear();
+    if (!S->per_mesh || nm == 1) {
+      S->blk.push_back(CoarseBlk{0, A.nc, A.ncp, 0, 0});
+    } else {
+      long long off = 0;
+      for (int k = 0; k < nm; ++k) {
+        const int s0 = S->mesh_sub[k], ns = S->mesh_sub[k + 1] - s0;
+        const int nk = 6 * ns, pk = std::max(GJ_T, ((nk + GJ_T - 1) / GJ_T) * GJ_T);
+        S->blk.push_back(CoarseBlk{6 * s0, nk, pk, s0, off});
+        off += (long long)pk * pk;
+      }
+    }
+    S->blk_elems = 0;
+    S->max_p = 0;
+    int rc_len = A.ncp;
+    std::vector<int> sub_blk(n_sub);
+    for (int b = 0; b < (int)S->blk.size(); ++b) {
+      const CoarseBlk& B = S->blk[b];
+      S->blk_elems += (long long)B.p * B.p;
+      S->max_p = std::max(S->max_p, B.p);
+      rc_len = std::max(rc_len, B.u0 + B.p);
+      for (int I = B.s0; I < B.s0 + B.n / 6; ++I) sub_blk[I] = b;
+    }
+    A.ncp = rc_len;  // length of the r_c / y buffers (one block: the padded size)
+    A.col0 = 0;
+    A.ldm = S->blk.size() == 1 ? S->blk[0].p : 0;  // per-mesh views set their own
+    if ((st = dev_alloc(ctx, &S->d_blk, S->blk.size()))) break;
+    if ((st = copy_to_device(ctx, S->d_blk, S->blk.data(), S->blk.size()))) break;
+    if ((st = dev_alloc(ctx, &S->d_sub_blk, (size_t)n_sub))) break;
+    if ((st = copy_to_device(ctx, S->d_sub_blk, sub_blk.data(), (size_t)n_sub))) break;
     if ((st = dev_alloc(ctx, &d_cellsub, (size_t)ncell))) break;
     if ((st = copy_to_device(ctx, d_cellsub, cell_sub.data(), (size_t)ncell))) break;
     if ((st = dev_alloc(ctx, &d_sub, (size_t)n))) break;
@@ -939,7 +1024,7 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     if ((st = dev_alloc(ctx, &S->rc, (size_t)A.ncp))) break;
     if ((st = dev_alloc(ctx, &S->cnt, (size_t)n_sub))) break;
     AXIA_CUDA(ctx, cudaMemsetAsync(S->rc, 0, A.ncp * sizeof(float), ctx->stream));
-    if ((st = dev_alloc(ctx, &S->minv, (size_t)A.nc * A.ncp))) break;
+    if ((st = dev_alloc(ctx, &S->minv, (size_t)S->blk_elems))) break;
     AXIA_CUDA(ctx, cudaMemsetAsync(S->yc, 0, A.ncp * sizeof(float), ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     A.sub_node = S->sub_node;
@@ -1033,8 +1118,8 @@ int build_item_structure(axia_ctx* ctx, CoarseState* S) {
     AXIA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(d_temp, tb, S->run_cnt, S->run_off, S->n_runs, ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     const size_t ncp = (size_t)A.ncp;
-    if ((st = dev_alloc(ctx, &S->a64, ncp * ncp))) break;
-    if ((st = dev_alloc(ctx, &S->a32, ncp * ncp))) break;
+    if ((st = dev_alloc(ctx, &S->a64, (size_t)S->blk_elems))) break;
+    if ((st = dev_alloc(ctx, &S->a32, (size_t)S->blk_elems))) break;
     if ((st = dev_alloc(ctx, &S->scale, ncp))) break;
     if ((st = dev_alloc(ctx, &S->piv, (size_t)2 * GJ_T * GJ_T))) break;
     S->items_fresh = true;  // the values of this pass belong to the current K
@@ -1049,11 +1134,18 @@ int build_item_structure(axia_ctx* ctx, CoarseState* S) {
 
 // s_i = 1 / sqrt(A_ii) for the coarse unknowns whose diagonal is positive
 // (above 1e-12 of the largest), 0 for the rest and the padding (one block)
-__global__ void k_diag_scale(int nc, int ncp, const double* A, double* scale) {
+// diagonal entry of unknown i (its subdomain's block)
+__device__ __forceinline__ double coarse_diag(const double* A, const CoarseBlk* blk, const int* sub_blk, int i) {
+  const CoarseBlk K = blk[sub_blk[i / 6]];
+  return A[K.off + (size_t)(i - K.u0) * (K.p + 1)];
+}
+
+__global__ void k_diag_scale(int nc, int ncp, const double* A, const CoarseBlk* blk, const int* sub_blk,
+                             double* scale) {
   __shared__ double red[32];
   double m = 0.0;
   for (int i = threadIdx.x; i < nc; i += blockDim.x) {
-    const double d = A[(size_t)i * ncp + i];
+    const double d = coarse_diag(A, blk, sub_blk, i);
     if (isfinite(d)) m = fmax(m, d);
   }
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -1067,7 +1159,7 @@ __global__ void k_diag_scale(int nc, int ncp, const double* A, double* scale) {
   __syncthreads();
   const double dmax = red[0];
   for (int i = threadIdx.x; i < ncp; i += blockDim.x) {
-    const double d = i < nc ? A[(size_t)i * ncp + i] : 0.0;
+    const double d = i < nc ? coarse_diag(A, blk, sub_blk, i) : 0.0;
     scale[i] = (i < nc && isfinite(d) && d > 1e-12 * dmax) ? 1.0 / sqrt(d) : 0.0;
   }
 }
@@ -1084,12 +1176,18 @@ int build_operator(axia_ctx* ctx, CoarseState* S) {
     ctx->launches++;
   }
   S->items_fresh = false;
-  AXIA_CUDA(ctx, cudaMemsetAsync(S->a64, 0, (size_t)ncp * ncp * sizeof(double), ctx->stream));
+  const int nblk = (int)S->blk.size();
+  AXIA_CUDA(ctx, cudaMemsetAsync(S->a64, 0, (size_t)S->blk_elems * sizeof(double), ctx->stream));
   k_run_sum<<<grid_for(ctx, (int64_t)S->n_runs * 32, 256), 256, 0, ctx->stream>>>(
-      S->n_runs, n_sub, S->run_key, S->run_off, S->run_cnt, S->perm, S->vals, S->tmat, S->a64, ncp);
+      S->n_runs, n_sub, S->run_key, S->run_off, S->run_cnt, S->perm, S->vals, S->tmat, S->a64, S->d_blk,
+      S->d_sub_blk);
   // unit-diagonal scaling; modes without stiffness (dropped or padding) become identity
-  k_diag_scale<<<1, 1024, 0, ctx->stream>>>(nc, ncp, S->a64, S->scale);
-  k_scale_to_f32<<<grid_for(ctx, (int64_t)ncp * ncp, 256), 256, 0, ctx->stream>>>(ncp, S->a64, S->scale, S->a32);
+  k_diag_scale<<<1, 1024, 0, ctx->stream>>>(nc, ncp, S->a64, S->d_blk, S->d_sub_blk, S->scale);
+  {
+    const int gx = grid_for(ctx, (int64_t)S->max_p * S->max_p, 256);
+    k_scale_to_f32<<<dim3((unsigned)std::max(1, gx / std::max(1, std::min(nblk, 16))), (unsigned)nblk), 256, 0,
+                     ctx->stream>>>(S->d_blk, S->a64, S->scale, S->a32);
+  }
   ctx->launches += 3;
   AXIA_CUDA(ctx, cudaGetLastError());
   AXIA_TRY(reset_dev_status(ctx));
@@ -1097,18 +1195,24 @@ int build_operator(axia_ctx* ctx, CoarseState* S) {
     int per_sm = 0;
     AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_inverse, GJ_THREADS, 0));
     if (per_sm < 1) return set_error(ctx, AXIA_ERR_CUDA, "coarse space: inverse kernel does not fit");
-    const int nt = ncp / GJ_T;
+    const int nt = S->max_p / GJ_T;
     const int grid = std::max(2, std::min(std::min(per_sm, 2) * ctx->sm_count, std::max(2, nt * (nt - 1) / 2)));
     AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
-    GjArgs P{S->a32, ncp, S->piv, ctx->d_bar, ctx->d_status, 2000000000ull};
-    void* params[] = {&P};
+    GjArgs P{S->a32, S->max_p, S->piv, ctx->d_bar, ctx->d_status, 2000000000ull};
+    const CoarseBlk* dblk = S->d_blk;
+    void* params[] = {&P, &dblk, (void*)&nblk};
     AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_gj_inverse, dim3(grid), dim3(GJ_THREADS), params, 0,
                                                ctx->stream));
     ctx->launches++;
   }
-  AXIA_CUDA(ctx, cudaMemsetAsync(S->minv, 0, (size_t)nc * ncp * sizeof(float), ctx->stream));
-  k_minv<<<grid_for(ctx, (int64_t)n_sub * n_sub, 128), 128, 0, ctx->stream>>>(n_sub, ncp, S->a32, S->scale, S->tmat,
-                                                                             S->minv);
+  AXIA_CUDA(ctx, cudaMemsetAsync(S->minv, 0, (size_t)S->blk_elems * sizeof(float), ctx->stream));
+  {
+    int max_ns = 0;
+    for (const CoarseBlk& B : S->blk) max_ns = std::max(max_ns, B.n / 6);
+    const int gx = grid_for(ctx, (int64_t)max_ns * max_ns, 128);
+    k_minv<<<dim3((unsigned)std::max(1, gx / std::max(1, std::min(nblk, 16))), (unsigned)nblk), 128, 0,
+             ctx->stream>>>(S->d_blk, S->a32, S->scale, S->tmat, S->minv);
+  }
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());
   return read_status(ctx, "coarse operator is not positive definite");
@@ -1139,17 +1243,19 @@ static int default_nodes_target(const axia_ctx* ctx) {
   return (int)std::min(1.0e6, std::max(64.0, v));
 }
 
-int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out) {
+int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out, bool per_mesh) {
   if (!ctx->have_bsr64) return set_error(ctx, AXIA_ERR_STATE, "coarse space needs the FP64 node-block matrix");
   if (nodes_target <= 0) nodes_target = default_nodes_target(ctx);
+  per_mesh = per_mesh && ctx->mesh_node0.size() >= 3;  // two or more meshes
   auto* S = static_cast<CoarseState*>(ctx->coarse);
-  if (S && S->nodes_target != nodes_target) {
+  if (S && (S->nodes_target != nodes_target || S->per_mesh != per_mesh)) {
     coarse_release(ctx);
     S = nullptr;
   }
   if (!S) {
     S = new CoarseState();
     S->nodes_target = nodes_target;
+    S->per_mesh = per_mesh;
     ctx->coarse = S;
     const int st = build_space(ctx, S);
     if (st) {
@@ -1187,7 +1293,8 @@ int coarse_prepare_batched(axia_ctx* ctx, int nodes_target, CoarseArgs* out) {
 
 // per mesh of a multi-mesh context: its restriction chunks and coarse rows
 int coarse_mesh_ranges(const axia_ctx* ctx, std::vector<int>& chunk0, std::vector<int>& chunk1, std::vector<int>& row0,
-                       std::vector<int>& row1) {
+                       std::vector<int>& row1, std::vector<int>& col0, std::vector<int>& ldm,
+                       std::vector<long long>& moff) {
   const auto* S = static_cast<const CoarseState*>(ctx->coarse);
   if (!S) return AXIA_ERR_STATE;
   const int nm = (int)S->mesh_sub.size() - 1;
@@ -1195,11 +1302,19 @@ int coarse_mesh_ranges(const axia_ctx* ctx, std::vector<int>& chunk0, std::vecto
   chunk1.resize(nm);
   row0.resize(nm);
   row1.resize(nm);
+  col0.resize(nm);
+  ldm.resize(nm);
+  moff.resize(nm);
   for (int k = 0; k < nm; ++k) {
     chunk0[k] = S->h_chunk_ptr[S->mesh_sub[k]];
     chunk1[k] = S->h_chunk_ptr[S->mesh_sub[k + 1]];
     row0[k] = 6 * S->mesh_sub[k];
     row1[k] = 6 * S->mesh_sub[k + 1];
+    // one block for all meshes: every mesh reads it whole (col0 = 0)
+    const CoarseBlk& B = S->blk.size() == (size_t)nm ? S->blk[k] : S->blk[0];
+    col0[k] = B.u0;
+    ldm[k] = B.p;
+    moff[k] = B.off;
   }
   return AXIA_OK;
 }

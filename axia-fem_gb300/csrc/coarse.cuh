@@ -35,12 +35,16 @@
 // Builds (or reuses) the coarse space of the current mesh and its operator
 // for the current assembly (coarse.cu); nodes_target <= 0: about 53,000
 // node blocks per subdomain (2000 nodes for C3D8).
-int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out);
+// per_mesh (multi-mesh solve): a block of the coarse inverse per mesh, so
+// every mesh may have as many subdomains as one mesh alone.
+int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out, bool per_mesh = false);
 // The same with the 32-column buffers of the batched load-case solve.
 int coarse_prepare_batched(axia_ctx* ctx, int nodes_target, CoarseArgs* out);
-// Per mesh of a multi-mesh context: its restriction chunks and coarse rows.
+// Per mesh of a multi-mesh context: its restriction chunks, coarse rows and
+// block of the coarse inverse (padded size, element offset).
 int coarse_mesh_ranges(const axia_ctx* ctx, std::vector<int>& chunk0, std::vector<int>& chunk1,
-                       std::vector<int>& row0, std::vector<int>& row1);
+                       std::vector<int>& row0, std::vector<int>& row1, std::vector<int>& col0,
+                       std::vector<int>& ldm, std::vector<long long>& moff);
 
 __device__ __forceinline__ unsigned geo_bits(float4 g) { return __float_as_uint(g.w); }
 
@@ -124,17 +128,22 @@ __device__ __forceinline__ void coarse_update_restrict(const CoarseArgs& C, floa
   }
 }
 
-// r_c into shared memory, then rows of y = M r_c over the warps of the group.
-// Returns this thread's share of r_c . y (nonzero on lane 0 of warps that own rows).
+// The block's part of r_c into shared memory (zero past its unknowns), then
+// rows of y = M r_c over the warps of the group.  Returns this thread's share
+// of r_c . y (nonzero on lane 0 of warps that own rows).
 __device__ __forceinline__ float coarse_solve(const CoarseArgs& C, float* s_rc, int gwarp, int nwarps, int lane) {
-  for (int t = threadIdx.x; t < (C.ncp >> 2); t += blockDim.x)
-    reinterpret_cast<float4*>(s_rc)[t] = __ldcg(reinterpret_cast<const float4*>(C.rc) + t);
+  if (C.col0 == 0 && C.row0 == 0 && C.row1 == C.nc && C.ldm <= C.ncp) {  // the whole matrix: r_c is zero past nc
+    for (int t = threadIdx.x; t < (C.ldm >> 2); t += blockDim.x)
+      reinterpret_cast<float4*>(s_rc)[t] = __ldcg(reinterpret_cast<const float4*>(C.rc) + t);
+  } else {
+    for (int t = threadIdx.x; t < C.ldm; t += blockDim.x) s_rc[t] = C.col0 + t < C.row1 ? __ldcg(C.rc + C.col0 + t) : 0.f;
+  }
   __syncthreads();
   float acc = 0.f;
-  const int nq = C.ncp >> 2;
+  const int nq = C.ldm >> 2;
   const float4* rc4 = reinterpret_cast<const float4*>(s_rc);
   for (int row = C.row0 + gwarp; row < C.row1; row += nwarps) {
-    const float4* m = reinterpret_cast<const float4*>(C.minv + (size_t)row * C.ncp);
+    const float4* m = reinterpret_cast<const float4*>(C.minv + (size_t)(row - C.col0) * C.ldm);
     float s = 0.f;
 #pragma unroll 4
     for (int j = lane; j < nq; j += 32) {
@@ -145,7 +154,7 @@ __device__ __forceinline__ float coarse_solve(const CoarseArgs& C, float* s_rc, 
     s = warp_sum(s);
     if (lane == 0) {
       C.yc[row] = s;
-      acc = fmaf(s, s_rc[row], acc);
+      acc = fmaf(s, s_rc[row - C.col0], acc);
     }
   }
   return acc;

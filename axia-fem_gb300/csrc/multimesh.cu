@@ -138,11 +138,12 @@ int capture_graph(axia_ctx* ctx, const double* d_f, double* d_u, double rtol, do
   return AXIA_OK;
 }
 
-// the restriction chunks and coarse rows of every group
+// the restriction chunks, coarse rows and block of the coarse inverse of every group
 int set_group_ranges(axia_ctx* ctx) {
   const int nm = (int)ctx->mesh_node0.size() - 1;
-  std::vector<int> c0, c1, r0, r1;
-  AXIA_TRY(coarse_mesh_ranges(ctx, c0, c1, r0, r1));
+  std::vector<int> c0, c1, r0, r1, col0, ldm;
+  std::vector<long long> moff;
+  AXIA_TRY(coarse_mesh_ranges(ctx, c0, c1, r0, r1, col0, ldm, moff));
   if ((int)c0.size() != nm) return set_error(ctx, AXIA_ERR_STATE, "coarse space does not match the meshes");
   std::vector<MeshGroup> g(nm);
   AXIA_CUDA(ctx, cudaMemcpyAsync(g.data(), ctx->d_mgroups, sizeof(MeshGroup) * nm, cudaMemcpyDeviceToHost,
@@ -153,6 +154,9 @@ int set_group_ranges(axia_ctx* ctx) {
     g[k].chunk1 = c1[k];
     g[k].row0 = r0[k];
     g[k].row1 = r1[k];
+    g[k].col0 = col0[k];
+    g[k].ldm = ldm[k];
+    g[k].moff = moff[k];
   }
   AXIA_CUDA(ctx, cudaMemcpyAsync(ctx->d_mgroups, g.data(), sizeof(MeshGroup) * nm, cudaMemcpyHostToDevice,
                                  ctx->stream));
@@ -176,7 +180,7 @@ int solve_multi_device(axia_ctx* ctx, const double* d_f, double* d_u, const axia
     AXIA_TRY(plan_groups(ctx, lanes, vec, coarse));
   CoarseArgs cargs{};
   if (coarse) {  // per-mesh subdomains; the operator follows every assembly (outside the graph)
-    AXIA_TRY(coarse_prepare(ctx, opts->coarse_nodes, &cargs));
+    AXIA_TRY(coarse_prepare(ctx, opts->coarse_nodes, &cargs, true));
     AXIA_TRY(set_group_ranges(ctx));
   }
   const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.01;

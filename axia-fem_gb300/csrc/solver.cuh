@@ -99,6 +99,8 @@ struct MeshGroup {
   long long part_off; // offset of its partial-sum area
   int chunk0, chunk1; // its restriction chunks (two-level preconditioner)
   int row0, row1;     // its coarse unknowns
+  int col0, ldm;      // its block of the coarse inverse: first unknown, padded size
+  long long moff;     // element offset of that block
 };
 constexpr int GROUP_SLOTS = 4;  // partial-sum slots per group: S_PQ, S_RR, S_RZ, S_RC
 
@@ -111,13 +113,14 @@ struct CoarseArgs {
   int nc;                // 6 n_sub
   int row0, row1;        // the coarse unknowns whose rows of y = M r_c this launch (group) computes
   int chunk_lo, chunk_hi;  // the restriction chunks this launch (group) handles
-  int ncp;               // nc rounded up to a multiple of 64 (row stride of minv)
+  int ncp;               // length of rc / yc (one block: nc rounded up to a multiple of 64)
+  int col0, ldm;         // the block of M this launch (group) reads: unknowns col0 .., row stride ldm
   int n_chunks;
   const int* sub_node;   // [n_nodes] nodes by subdomain, ascending within each
   const int4* chunk;     // [n_chunks] (subdomain, first, end) ranges of sub_node
   const int* chunk_ptr;  // [n_sub + 1] chunks of each subdomain
   const float4* geo;     // [n_nodes] (x_a - c_I) / h, .w = bits (I << 3 | free-DOF mask)
-  const float* minv;     // [nc][ncp] M, zero in the padding
+  const float* minv;     // this launch's block of M: [rows][ldm], row r at (r - col0) ldm, zero in the padding
   float* part;           // [n_chunks][6] restriction partials
   float* rc;             // [ncp] restricted residual Z^T r (zero in the padding)
   int* cnt;              // [n_sub] chunks of each subdomain done (reset by the last)
