@@ -334,7 +334,7 @@ def run_c4b(args):
     def step():
         ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
         return ctx.solve_multi_device(f.data_ptr(), u.data_ptr(), rtol=RTOL, inner_rtol=args.delta,
-                                      preconditioner=L.PRECOND_COARSE, coarse_nodes=(args.coarse_nodes or 2000) // 4)
+                                      preconditioner=L.PRECOND_COARSE, coarse_nodes=(args.coarse_nodes or 2000) // 2)
     msj, (infoj, relj, itsj) = timer(step_jacobi, args.warmup, args.steps)
     uj = u.clone()
     ms, (info, rel, its) = timer(step, args.warmup, args.steps)
