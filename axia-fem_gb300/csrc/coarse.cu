@@ -1177,6 +1177,7 @@ int build_operator(axia_ctx* ctx, CoarseState* S) {
   }
   S->items_fresh = false;
   const int nblk = (int)S->blk.size();
+  if (nblk > 65535) return set_error(ctx, AXIA_ERR_TOO_LARGE, "coarse space: more than 65535 meshes");
   AXIA_CUDA(ctx, cudaMemsetAsync(S->a64, 0, (size_t)S->blk_elems * sizeof(double), ctx->stream));
   k_run_sum<<<grid_for(ctx, (int64_t)S->n_runs * 32, 256), 256, 0, ctx->stream>>>(
       S->n_runs, n_sub, S->run_key, S->run_off, S->run_cnt, S->perm, S->vals, S->tmat, S->a64, S->d_blk,

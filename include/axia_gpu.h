@@ -118,7 +118,7 @@ typedef struct axia_solve_opts {
   int32_t preconditioner;  /* axia_preconditioner (0 = Jacobi) */
   int32_t coarse_nodes;    /* AXIA_PRECOND_COARSE: nodes per subdomain (0 = about 53,000 matrix node
                               blocks per subdomain: 2000 nodes for C3D8, ~950 for C3D20; at most 682
-                              subdomains) */
+                              subdomains per system, in a multi-mesh solve per mesh) */
 } axia_solve_opts;
 
 typedef struct axia_solve_info {
