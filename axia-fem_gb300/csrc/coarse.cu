@@ -1257,6 +1257,7 @@ int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out, bool per_me
     S = new CoarseState();
     S->nodes_target = nodes_target;
     S->per_mesh = per_mesh;
+    ++ctx->coarse_gen;
     ctx->coarse = S;
     const int st = build_space(ctx, S);
     if (st) {

@@ -368,7 +368,8 @@ struct axia_ctx {
   unsigned char* d_mouts = nullptr;   // PcgOut[n_meshes]
   int multi_grid = 0, multi_lanes = 0, multi_vec = 0;
   bool multi_coarse = false;          // groups planned for the two-level kernel
-  const void* graph_coarse = nullptr; // coarse inverse the captured graph reads (null: diagonal only)
+  int64_t graph_coarse = -1;    // coarse space the captured graph reads (its coarse_gen; -1: diagonal only)
+  int64_t coarse_gen = 0;       // coarse spaces built so far (a new space gets new device arrays)
   int tuned_lanes = 0, tuned_vec = 0;  // node-block layout chosen by axia_gpu_autotune (0: none)
   void* multi_graph = nullptr;        // cudaGraphExec_t
   const double* graph_f = nullptr;

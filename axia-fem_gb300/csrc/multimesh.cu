@@ -134,7 +134,7 @@ int capture_graph(axia_ctx* ctx, const double* d_f, double* d_u, double rtol, do
   ctx->graph_rtol = rtol;
   ctx->graph_delta = delta;
   ctx->graph_max_iter = max_iter;
-  ctx->graph_coarse = coarse ? (const void*)coarse->minv : nullptr;
+  ctx->graph_coarse = coarse ? ctx->coarse_gen : -1;
   return AXIA_OK;
 }
 
@@ -190,7 +190,9 @@ int solve_multi_device(axia_ctx* ctx, const double* d_f, double* d_u, const axia
     for (int k = 0; k < nm; ++k) biggest = std::max<int64_t>(biggest, 3 * (ctx->mesh_node0[k + 1] - ctx->mesh_node0[k]));
     max_iter = std::max<long long>(4 * biggest, 200);
   }
-  const void* coarse_key = coarse ? (const void*)cargs.minv : nullptr;
+  // the space's generation, not an address: a rebuilt space may reuse some
+  // released blocks of the pool and not others
+  const int64_t coarse_key = coarse ? ctx->coarse_gen : -1;
   if (!ctx->multi_graph || ctx->graph_f != d_f || ctx->graph_u != d_u || ctx->graph_rtol != opts->rtol ||
       ctx->graph_delta != delta || ctx->graph_max_iter != max_iter || ctx->graph_coarse != coarse_key)
     AXIA_TRY(capture_graph(ctx, d_f, d_u, opts->rtol, delta, max_iter, coarse ? &cargs : nullptr));

@@ -155,3 +155,23 @@ def test_multi_mesh_with_per_mesh_coarse_spaces(gpu_ctx):
     gpu_ctx.assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
     u3, _, _, _ = gpu_ctx.solve_multi(2.0 * f, rtol=1e-10, preconditioner=_lib.PRECOND_COARSE, coarse_nodes=60)
     assert np.linalg.norm(u3 - 2.0 * u) <= 1e-8 * np.linalg.norm(u3)
+
+
+def test_multi_mesh_context_switches_between_block_layouts(gpu_ctx):
+    """The multi-mesh solve keeps one block of the coarse inverse per mesh; a
+    solve of the same context as one system keeps one block for all meshes.
+    Alternating the two rebuilds the space each time; both give the same
+    solution (to the solver tolerance) and repeats are bitwise equal."""
+    cubes = meshgen.cube_family(count=4, lo=4, hi=9, seed=11)
+    gpu_ctx.setup_multi(cubes).assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+    f = np.concatenate([c.cload for c in cubes])
+    kw = dict(preconditioner=_lib.PRECOND_COARSE, coarse_nodes=40)
+    um, _, _, _ = gpu_ctx.solve_multi(f, rtol=1e-11, **kw)
+    n_sub_multi, _ = gpu_ctx.coarse_size()
+    us, info = gpu_ctx.solve(f, rtol=1e-11, precision=_lib.PREC_MIXED, refine_mode=_lib.REFINE_RELIABLE,
+                             matrix_format=_lib.FORMAT_BSR3, **kw)
+    assert info.iters > 0
+    assert _rel(us, um) < 1e-8
+    um2, _, _, _ = gpu_ctx.solve_multi(f, rtol=1e-11, **kw)
+    assert np.array_equal(um, um2)
+    assert gpu_ctx.coarse_size()[0] == n_sub_multi
