@@ -40,6 +40,7 @@ namespace {
 constexpr int GJ_T = 64;          // Gauss-Jordan tile
 constexpr int GJ_THREADS = 256;   // 16 x 16 threads, 4 x 4 outputs each
 constexpr int ROW_SLOTS = 8;      // subdomains accumulated per pass over a node row
+constexpr int GJ_GROUPS = 32;     // at most this many coarse blocks are inverted side by side
 
 // One diagonal block of the coarse matrix: the unknowns [u0, u0 + n) of the
 // subdomains s0 .. s0 + n / 6 - 1, padded to p (a multiple of GJ_T), stored
@@ -84,7 +85,8 @@ struct CoarseState {
   double* a64 = nullptr;         // [blk_elems]
   float* a32 = nullptr;          // [blk_elems] inverted in place
   double* scale = nullptr;       // [ncp] per unknown
-  float* piv = nullptr;          // [2][GJ_T][GJ_T]
+  float* piv = nullptr;          // [GJ_GROUPS][2][GJ_T][GJ_T]
+  GridBarrier* gj_bar = nullptr; // [GJ_GROUPS]
   float* part = nullptr;         // [n_chunks][6]
   float* rc = nullptr;           // [ncp]
   int* cnt = nullptr;            // [n_sub]
@@ -111,6 +113,7 @@ struct CoarseState {
     dev_release(ctx, a32);
     dev_release(ctx, scale);
     dev_release(ctx, piv);
+    dev_release(ctx, gj_bar);
     dev_release(ctx, part_m);
     dev_release(ctx, rc_m);
     dev_release(ctx, yc_m);
@@ -521,6 +524,7 @@ struct GjArgs {
   GridBarrier* bar;
   DevStatus* st;
   unsigned long long limit_ns;
+  int rank, nb;      // this block's rank in its group of nb blocks (at least 2)
 };
 
 // operand tiles: sa[q][r] = X[r][q] (transposed), sb[q][c] = Y[q][c]
@@ -651,7 +655,7 @@ __device__ __forceinline__ bool gj_invert_block(GjArgs P) {
   for (int k = 0; k < nt; ++k) {
     // 1. block 0 stores P_(k-1) into its tile (and inverts tile (0, 0) at
     //    k = 0); the other blocks write step k-1's column panel
-    if (blockIdx.x == 0) {
+    if (P.rank == 0) {
       if (k > 0) gj_store_global(piv(k - 1), tile(k - 1, k - 1), ld);
       if (k == 0) {
         float a[4][4];
@@ -661,11 +665,11 @@ __device__ __forceinline__ bool gj_invert_block(GjArgs P) {
         __syncthreads();
       }
     } else if (k > 0) {
-      gj_column_panel(P, k - 1, blockIdx.x - 1, gridDim.x - 1);
+      gj_column_panel(P, k - 1, P.rank - 1, P.nb - 1);
     }
-    if (!grid_sync(P.bar, P.st, P.limit_ns)) return false;
+    if (!group_sync(P.bar, P.st, P.limit_ns, P.nb)) return false;
     // 2. row panel: A_kj <- P_k A_kj
-    for (int j = blockIdx.x; j < nt; j += gridDim.x) {
+    for (int j = P.rank; j < nt; j += P.nb) {
       if (j == k) continue;
       __syncthreads();
       gj_load_t(sa, piv(k), GJ_T);
@@ -675,13 +679,13 @@ __device__ __forceinline__ bool gj_invert_block(GjArgs P) {
       gj_mul(sa, sb, o);
       gj_store_regs(o, tile(k, j), ld);
     }
-    if (!grid_sync(P.bar, P.st, P.limit_ns)) return false;
+    if (!group_sync(P.bar, P.st, P.limit_ns, P.nb)) return false;
     // 3. trailing tiles j <= i (i, j != k): A_ij -= A_ik R_j, mirrored into
     //    A_ji; block 0 takes tile (k+1, k+1) alone and inverts it
     const int m = nt - 1, ntiles = m * (m + 1) / 2;
-    const bool ahead = k + 1 < nt && gridDim.x > 1;
+    const bool ahead = k + 1 < nt && P.nb > 1;
     const int tdiag = ahead ? k * (k + 1) / 2 + k : -1;  // (k+1, k+1) in the compressed numbering
-    if (ahead && blockIdx.x == 0) {
+    if (ahead && P.rank == 0) {
       __syncthreads();
       gj_load_t(sa, tile(k + 1, k), ld);
       gj_load(sb, tile(k, k + 1), ld);
@@ -701,8 +705,8 @@ __device__ __forceinline__ bool gj_invert_block(GjArgs P) {
       gj_invert_regs(a, &sa[0][0], &sb[0][0], P.st, (k + 1) * GJ_T);
       gj_store_regs(a, piv(k + 1), GJ_T);
     }
-    const int first = ahead ? (int)blockIdx.x - 1 : (int)blockIdx.x;
-    const int stride = ahead ? (int)gridDim.x - 1 : (int)gridDim.x;
+    const int first = ahead ? P.rank - 1 : P.rank;
+    const int stride = ahead ? P.nb - 1 : P.nb;
     for (int t = first; first >= 0 && t < ntiles; t += stride) {
       if (t == tdiag) continue;
       int i = (int)((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
@@ -737,24 +741,32 @@ __device__ __forceinline__ bool gj_invert_block(GjArgs P) {
               make_float4(sg * v[0][c], sg * v[1][c], sg * v[2][c], sg * v[3][c]);
       }
     }
-    if (!grid_sync(P.bar, P.st, P.limit_ns)) return false;
+    if (!group_sync(P.bar, P.st, P.limit_ns, P.nb)) return false;
   }
   // the last step's P and column panel
   const int k = nt - 1;
-  if (blockIdx.x == 0) {
+  if (P.rank == 0) {
     gj_store_global(piv(k), tile(k, k), ld);
   } else {
-    gj_column_panel(P, k, blockIdx.x - 1, gridDim.x - 1);
+    gj_column_panel(P, k, P.rank - 1, P.nb - 1);
   }
   return true;
 }
 
-// The diagonal blocks of the coarse matrix one after the other (one cooperative
-// launch; the pivot buffers are reused, hence the barrier between blocks).
-__global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P, const CoarseBlk* blk, int nblk) {
-  for (int b = 0; b < nblk; ++b) {
-    if (b > 0 && !grid_sync(P.bar, P.st, P.limit_ns)) return;
-    GjArgs Q = P;
+// The diagonal blocks of the coarse matrix in one cooperative launch: the
+// blocks are split into ngroups groups (block b to group b mod ngroups, the
+// launch's blocks likewise by blockIdx mod ngroups); each group inverts its
+// blocks one after another with its own barrier and pivot buffers (reused,
+// hence the barrier between blocks).  Groups never wait on one another.
+__global__ void __launch_bounds__(GJ_THREADS) k_gj_inverse(GjArgs P, const CoarseBlk* blk, int nblk, int ngroups) {
+  const int g = (int)(blockIdx.x % (unsigned)ngroups);
+  GjArgs Q = P;
+  Q.rank = (int)(blockIdx.x / (unsigned)ngroups);
+  Q.nb = ((int)gridDim.x - g + ngroups - 1) / ngroups;
+  Q.bar = P.bar + g;
+  Q.piv = P.piv + (size_t)g * 2 * GJ_T * GJ_T;
+  for (int b = g; b < nblk; b += ngroups) {
+    if (b != g && !group_sync(Q.bar, Q.st, Q.limit_ns, Q.nb)) return;
     Q.A = P.A + blk[b].off;
     Q.n = blk[b].p;
     if (!gj_invert_block(Q)) return;
@@ -1121,7 +1133,8 @@ int build_item_structure(axia_ctx* ctx, CoarseState* S) {
     if ((st = dev_alloc(ctx, &S->a64, (size_t)S->blk_elems))) break;
     if ((st = dev_alloc(ctx, &S->a32, (size_t)S->blk_elems))) break;
     if ((st = dev_alloc(ctx, &S->scale, ncp))) break;
-    if ((st = dev_alloc(ctx, &S->piv, (size_t)2 * GJ_T * GJ_T))) break;
+    if ((st = dev_alloc(ctx, &S->piv, (size_t)GJ_GROUPS * 2 * GJ_T * GJ_T))) break;
+    if ((st = dev_alloc(ctx, &S->gj_bar, (size_t)GJ_GROUPS))) break;
     S->items_fresh = true;  // the values of this pass belong to the current K
   } while (false);
   if (d_temp) cudaFree(d_temp);
@@ -1197,11 +1210,18 @@ int build_operator(axia_ctx* ctx, CoarseState* S) {
     AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_inverse, GJ_THREADS, 0));
     if (per_sm < 1) return set_error(ctx, AXIA_ERR_CUDA, "coarse space: inverse kernel does not fit");
     const int nt = S->max_p / GJ_T;
-    const int grid = std::max(2, std::min(std::min(per_sm, 2) * ctx->sm_count, std::max(2, nt * (nt - 1) / 2)));
-    AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
-    GjArgs P{S->a32, S->max_p, S->piv, ctx->d_bar, ctx->d_status, 2000000000ull};
+    const int full = std::min(per_sm, 2) * ctx->sm_count;
+    int grid = std::max(2, std::min(full, std::max(2, nt * (nt - 1) / 2)));
+    // several blocks: groups of at least 16 launch blocks invert them side by side
+    int ngroups = 1;
+    if (nblk > 1) {
+      grid = std::max(2, full);
+      ngroups = std::max(1, std::min(std::min(nblk, GJ_GROUPS), grid / 16));
+    }
+    AXIA_CUDA(ctx, cudaMemsetAsync(S->gj_bar, 0, sizeof(GridBarrier) * GJ_GROUPS, ctx->stream));
+    GjArgs P{S->a32, S->max_p, S->piv, S->gj_bar, ctx->d_status, 2000000000ull, 0, grid};
     const CoarseBlk* dblk = S->d_blk;
-    void* params[] = {&P, &dblk, (void*)&nblk};
+    void* params[] = {&P, &dblk, (void*)&nblk, &ngroups};
     AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_gj_inverse, dim3(grid), dim3(GJ_THREADS), params, 0,
                                                ctx->stream));
     ctx->launches++;
