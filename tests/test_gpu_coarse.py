@@ -175,3 +175,24 @@ def test_multi_mesh_context_switches_between_block_layouts(gpu_ctx):
     um2, _, _, _ = gpu_ctx.solve_multi(f, rtol=1e-11, **kw)
     assert np.array_equal(um, um2)
     assert gpu_ctx.coarse_size()[0] == n_sub_multi
+
+
+def test_many_meshes_share_inversion_groups(gpu_ctx):
+    """More meshes than inversion groups (at most 19 of 16 CTAs each on 152
+    SMs): groups invert several coarse blocks in turn.  Every mesh against its
+    direct solve, repeat bitwise equal."""
+    cubes = meshgen.cube_family(count=40, lo=2, hi=6, seed=17)
+    gpu_ctx.setup_multi(cubes).assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+    f = np.concatenate([c.cload for c in cubes])
+    kw = dict(preconditioner=_lib.PRECOND_COARSE, coarse_nodes=40)
+    u, info, rel, its = gpu_ctx.solve_multi(f, rtol=1e-11, **kw)
+    n_sub, _ = gpu_ctx.coarse_size()
+    assert n_sub >= len(cubes)
+    node0 = gpu_ctx.node0
+    for k, c in enumerate(cubes):
+        uk = u[3 * node0[k]:3 * node0[k + 1]]
+        ref = O.solve_static(c, solver=O.SOLVER_CHOLESKY)
+        # a cube that drew no loaded surface node has u = 0 exactly
+        assert np.linalg.norm(uk - ref.u) <= 1e-8 * np.linalg.norm(ref.u), k
+    u2, _, _, its2 = gpu_ctx.solve_multi(f, rtol=1e-11, **kw)
+    assert np.array_equal(u, u2) and np.array_equal(its, its2)
