@@ -1253,15 +1253,18 @@ void coarse_release(axia_ctx* ctx) {
 // The coarse space of the current mesh (built on first use, or when the
 // requested subdomain size changes) and its operator for the current
 // assembly (rebuilt after every assembly).
-// Default subdomain size: about 53,000 node blocks of the matrix per
-// subdomain -- 2000 nodes for C3D8 (27 blocks per node row), about 950 for
-// C3D20 (about 55).  Measured: C3D20 50^3 took 350 iterations with 216
-// subdomains of 2000 nodes and 271 with 512 of about 1000 (127 instead of
-// 147 ms per step); the C3D8 100^3 headline keeps its 512.
+// Default subdomain size: about 512 subdomains (8^3 for a cube; the dense
+// inverse then costs about 4 ms), but no fewer than about 13,500 matrix node
+// blocks per subdomain -- 500 nodes for C3D8 (27 blocks per node row), about
+// 250 for C3D20 (about 55).  Measured per step: C3D20 50^3 350 iterations
+// and 147 ms with 216 subdomains, 271 and 127 ms with 512; SIMP C3D8
+// 100x50x50 236 iterations and 31.1 ms with 125 subdomains, 167 and 26.9 ms
+// with 512; the C3D8 100^3 headline keeps its 512.
 static int default_nodes_target(const axia_ctx* ctx) {
   if (ctx->n_adj <= 0 || ctx->n_nodes <= 0) return 2000;
-  const double v = (double)ctx->n_nodes * 53000.0 / (double)ctx->n_adj;
-  return (int)std::min(1.0e6, std::max(64.0, v));
+  const double floor_nodes = 500.0 * 27.0 * (double)ctx->n_nodes / (double)ctx->n_adj;
+  const double v = std::max(floor_nodes, (double)ctx->n_nodes / 512.0);
+  return (int)std::min(1.0e6, std::max(16.0, v));
 }
 
 int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out, bool per_mesh) {

@@ -33,8 +33,8 @@
 // part of the solver's argument pack).
 
 // Builds (or reuses) the coarse space of the current mesh and its operator
-// for the current assembly (coarse.cu); nodes_target <= 0: about 53,000
-// node blocks per subdomain (2000 nodes for C3D8).
+// for the current assembly (coarse.cu); nodes_target <= 0: about 512
+// subdomains, at least about 13,500 node blocks each (500 nodes for C3D8).
 // per_mesh (multi-mesh solve): a block of the coarse inverse per mesh, so
 // every mesh may have as many subdomains as one mesh alone.
 int coarse_prepare(axia_ctx* ctx, int nodes_target, CoarseArgs* out, bool per_mesh = false);

@@ -448,8 +448,8 @@ def main():
     ap.add_argument("--lanes32csr", type=int, default=0)
     ap.add_argument("--delta", type=float, default=0.01, help="reliable-update residual reduction")
     ap.add_argument("--coarse-nodes", type=int, default=0,
-                    help="nodes per subdomain of the coarse space (0: the library default, about 53,000 "
-                         "matrix node blocks per subdomain)")
+                    help="nodes per subdomain of the coarse space (0: the library default, about 512 "
+                         "subdomains of at least ~13,500 matrix node blocks)")
     ap.add_argument("--only", choices=["mixed", "coarse", "fp64", "spmv", "batch"], default=None,
                     help="run one solve (or SpMV sweep) once and exit: the profiling entry")
     ap.add_argument("--max-iter", type=int, default=0, help="with --only: cap the CG iterations")

@@ -116,9 +116,9 @@ typedef struct axia_solve_opts {
   int32_t matrix_format;   /* axia_matrix_format */
   int32_t spmv_vec;        /* node-block form: blocks per lane load (1, 2, 4; 0 = automatic) */
   int32_t preconditioner;  /* axia_preconditioner (0 = Jacobi) */
-  int32_t coarse_nodes;    /* AXIA_PRECOND_COARSE: nodes per subdomain (0 = about 53,000 matrix node
-                              blocks per subdomain: 2000 nodes for C3D8, ~950 for C3D20; at most 682
-                              subdomains per system, in a multi-mesh solve per mesh) */
+  int32_t coarse_nodes;    /* AXIA_PRECOND_COARSE: nodes per subdomain (0 = about 512 subdomains, but
+                              at least ~13,500 matrix node blocks each: 500 nodes for C3D8; at most
+                              682 subdomains per system, in a multi-mesh solve per mesh) */
 } axia_solve_opts;
 
 typedef struct axia_solve_info {
