@@ -352,43 +352,41 @@ __device__ __forceinline__ void coarse_restrict_m(const CoarseArgs& C, const flo
   }
 }
 
-// Y = M R_c; per column r_c . y into partials[(slot0 + col) * G + block]
+// Y = M R_c; per column r_c . y into partials[(slot0 + col) * G + block].
+// Tasks of 16 rows go to the blocks in turn; a thread owns one (row, load
+// case): the warp of a row streams that row of M once (broadcast loads) and
+// reads R_c row by row (coalesced, shared by the block's warps through L1).
+// The per-column sums run over the block's tasks and rows in a fixed order.
 __device__ __forceinline__ void coarse_solve_m(const CoarseArgs& C, int gwarp, int nwarps, int lane, double* partials,
                                                int slot0) {
-  __shared__ float s_cc[PCG_THREADS / 32][NR];
-  const int warp = threadIdx.x >> 5;
-  s_cc[warp][lane] = 0.f;
-  __syncwarp();
-  const int ntask = C.nc * LPG;
-  for (int t = gwarp; t < ntask; t += nwarps) {
-    const int i = t / LPG, cq = t - i * LPG;
-    const float* mrow = C.minv + (size_t)i * C.ldm;
-    float acc[CPL] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 4
-    for (int j = lane; j < C.nc; j += 32) {
-      const float mv = __ldg(mrow + j);
-      float rv[CPL];
-      ld4(C.rc_m + (size_t)j * NR + CPL * cq, rv);
-#pragma unroll
-      for (int c = 0; c < CPL; ++c) acc[c] = fmaf(mv, rv[c], acc[c]);
+  constexpr int TR = PCG_THREADS / NR;  // rows per task
+  __shared__ float s_prod[PCG_THREADS];
+  __shared__ float s_cc[NR];
+  const int r = threadIdx.x / NR, c = threadIdx.x % NR;
+  if (threadIdx.x < NR) s_cc[threadIdx.x] = 0.f;
+  const int ntask = (C.nc + TR - 1) / TR;
+  for (int task = blockIdx.x; task < ntask; task += gridDim.x) {
+    const int i = task * TR + r;
+    float prod = 0.f;
+    if (i < C.nc) {
+      const float* mrow = C.minv + (size_t)i * C.ldm;
+      const float* rcol = C.rc_m + c;
+      float y = 0.f;
+#pragma unroll 8
+      for (int j = 0; j < C.nc; ++j) y = fmaf(__ldg(mrow + j), rcol[(size_t)j * NR], y);
+      C.yc_m[(size_t)i * NR + c] = y;
+      prod = rcol[(size_t)i * NR] * y;
     }
-#pragma unroll
-    for (int c = 0; c < CPL; ++c) acc[c] = warp_sum(acc[c]);
-    if (lane == 0) {
-      st4(C.yc_m + (size_t)i * NR + CPL * cq, acc);
-      float rv[CPL];
-      ld4(C.rc_m + (size_t)i * NR + CPL * cq, rv);
-#pragma unroll
-      for (int c = 0; c < CPL; ++c) s_cc[warp][CPL * cq + c] = fmaf(rv[c], acc[c], s_cc[warp][CPL * cq + c]);
+    s_prod[threadIdx.x] = prod;
+    __syncthreads();
+    if (threadIdx.x < NR) {
+      float sum = s_cc[threadIdx.x];
+      for (int q = 0; q < TR; ++q) sum += s_prod[q * NR + threadIdx.x];
+      s_cc[threadIdx.x] = sum;
     }
-    __syncwarp();
+    __syncthreads();
   }
-  __syncthreads();
-  if (threadIdx.x < NR) {
-    double sum = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += s_cc[w][threadIdx.x];
-    partials[(size_t)(slot0 + threadIdx.x) * gridDim.x + blockIdx.x] = sum;
-  }
+  if (threadIdx.x < NR) partials[(size_t)(slot0 + threadIdx.x) * gridDim.x + blockIdx.x] = (double)s_cc[threadIdx.x];
 }
 
 // coarse part of z at DOF row `row`, columns c0..c0+3
