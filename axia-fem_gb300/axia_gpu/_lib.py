@@ -1,8 +1,8 @@
 """ctypes binding of libaxia_gpu.so (declarations in include/axia_gpu.h).
 
-This is the binding a host of the C ABI writes; the Rust-side equivalent is in
-INTEGRATION.md.  Loading fails loudly when the library is missing: there is no
-CPU fallback behind this module.
+This is the binding a host of the C ABI writes (a Rust host declares the same
+functions in an extern "C" block).  Loading fails loudly when the library is
+missing: there is no CPU fallback behind this module.
 """
 from __future__ import annotations
 

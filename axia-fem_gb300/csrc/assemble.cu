@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "element.cuh"
 
@@ -217,9 +219,13 @@ struct DevTables {
   int* blk = nullptr;
 };
 
-// hex8, hex20 (27 gp), hex20r (8 gp), tet4, tet10, hex8r (1 gp), wedge6, wedge15 -- by device id
-DevTables g_tab[8];
-int g_tab_device[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+// hex8, hex20 (27 gp), hex20r (8 gp), tet4, tet10, hex8r (1 gp), wedge6,
+// wedge15: one set per device, uploaded on first use under a mutex (contexts
+// on different devices may be driven from different threads) and kept until
+// the process exits.
+constexpr int kTabDevices = 64, kTabKinds = 8;
+DevTables g_tab[kTabDevices][kTabKinds];
+std::mutex g_tab_mutex;
 
 int table_index(int nn, int ng) {
   if (nn == 8 && ng == 1) return 5;
@@ -230,24 +236,42 @@ int table_index(int nn, int ng) {
   return nn == 8 ? 0 : (ng == 27 ? 1 : 2);
 }
 
+void free_tables(DevTables& d) {
+  cudaFree(d.dn);
+  cudaFree(d.w);
+  cudaFree(d.e0);
+  cudaFree(d.e1);
+  cudaFree(d.blk);
+  d = DevTables{};
+}
+
+template <typename T>
+cudaError_t upload(T** dst, const std::vector<T>& src) {
+  cudaError_t e = cudaMalloc(dst, src.size() * sizeof(T));
+  if (e == cudaSuccess) e = cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return e;
+}
+
 int ensure_tables(axia_ctx* ctx, int nn, int ng, ElemTables* out) {
-  int ti = table_index(nn, ng);
-  if (g_tab_device[ti] != ctx->device) {
-    HostTables h = make_tables(nn, ng);
-    DevTables& d = g_tab[ti];
-    AXIA_CUDA(ctx, cudaMalloc(&d.dn, h.dn.size() * sizeof(double)));
-    AXIA_CUDA(ctx, cudaMalloc(&d.w, h.w.size() * sizeof(double)));
-    AXIA_CUDA(ctx, cudaMalloc(&d.e0, h.e0.size() * sizeof(int)));
-    AXIA_CUDA(ctx, cudaMalloc(&d.e1, h.e1.size() * sizeof(int)));
-    AXIA_CUDA(ctx, cudaMalloc(&d.blk, h.blk.size() * sizeof(int)));
-    AXIA_CUDA(ctx, cudaMemcpy(d.dn, h.dn.data(), h.dn.size() * sizeof(double), cudaMemcpyHostToDevice));
-    AXIA_CUDA(ctx, cudaMemcpy(d.w, h.w.data(), h.w.size() * sizeof(double), cudaMemcpyHostToDevice));
-    AXIA_CUDA(ctx, cudaMemcpy(d.e0, h.e0.data(), h.e0.size() * sizeof(int), cudaMemcpyHostToDevice));
-    AXIA_CUDA(ctx, cudaMemcpy(d.e1, h.e1.data(), h.e1.size() * sizeof(int), cudaMemcpyHostToDevice));
-    AXIA_CUDA(ctx, cudaMemcpy(d.blk, h.blk.data(), h.blk.size() * sizeof(int), cudaMemcpyHostToDevice));
-    g_tab_device[ti] = ctx->device;
+  const int ti = table_index(nn, ng);
+  if (ctx->device < 0 || ctx->device >= kTabDevices)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "device index out of range for the element tables");
+  std::lock_guard<std::mutex> lock(g_tab_mutex);
+  DevTables& d = g_tab[ctx->device][ti];
+  if (!d.blk) {  // blk is uploaded last: set only when the whole set is on the device
+    const HostTables h = make_tables(nn, ng);
+    DevTables t;
+    cudaError_t e = upload(&t.dn, h.dn);
+    if (e == cudaSuccess) e = upload(&t.w, h.w);
+    if (e == cudaSuccess) e = upload(&t.e0, h.e0);
+    if (e == cudaSuccess) e = upload(&t.e1, h.e1);
+    if (e == cudaSuccess) e = upload(&t.blk, h.blk);
+    if (e != cudaSuccess) {
+      free_tables(t);
+      return set_error(ctx, AXIA_ERR_CUDA, std::string("element table upload: ") + cudaGetErrorString(e));
+    }
+    d = t;
   }
-  const DevTables& d = g_tab[ti];
   out->dn = d.dn;
   out->w = d.w;
   out->e0 = d.e0;

@@ -15,7 +15,9 @@
 // device current) and caches; that first call should come before any stream
 // capture.  Every call reuses the array: the status word is cleared at the
 // start of each call, and calls that overlap on the GPU would race (calls in
-// one process are serialized by a host mutex).
+// one process are serialized by a host mutex).  The cached address and tables
+// belong to the CUDA context that was current at the first call: calls after
+// cudaDeviceReset (or any teardown of the primary context) are not supported.
 #include <mutex>
 
 #include "element.cuh"
@@ -184,7 +186,11 @@ extern "C" AXIA_API int32_t axia_gpu_element_ke_noalloc(int32_t nn, int32_t redu
                                                         const double* xyz, const double* e, double nu, double* ke,
                                                         double* vol, int64_t* bad_elem) {
   if (bad_elem) *bad_elem = -1;
+  // C3D8, C3D20 and C3D20R only: the C3D8R / C3D8I arms (reduced = 1 / 2 with
+  // nn = 8) need the hourglass and condensation kernels of the context path,
+  // and any other `reduced` would silently pick a different element.
   if (nn != 8 && nn != 20) return AXIA_ERR_INVALID_ARG;
+  if ((nn == 8 && reduced != 0) || (nn == 20 && reduced != 0 && reduced != 1)) return AXIA_ERR_INVALID_ARG;
   const int64_t max_elem = nn == 8 ? kMaxElemHex8 : kMaxElemHex20;
   if (n_elem < 0) return AXIA_ERR_INVALID_ARG;
   if (n_elem > max_elem) return AXIA_ERR_TOO_LARGE;

@@ -170,14 +170,18 @@ AXIA_API int32_t axia_gpu_element_ke(axia_ctx* ctx, int32_t nn, int32_t reduced,
  * not call cudaMalloc -- hosts whose device memory belongs to another
  * allocator or to a budget they may not exceed, and latency-critical loops
  * where an allocation's implicit device synchronization is not acceptable.
- * Same arguments, results and error codes as axia_gpu_element_ke (host
- * buffers in and out), on the current CUDA device.  Limit: n_elem <= 2048
- * for nn = 8 and <= 512 for nn = 20 (AXIA_ERR_TOO_LARGE above).  Its device
- * memory is one fixed 16 MiB array per device, held until the process exits;
- * the first call on a device looks up that array's address and uploads the
- * element tables, so make it before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race (calls within one process are
- * serialized). */
+ * The arguments, results and error codes of axia_gpu_element_ke (host
+ * buffers in and out), on the current CUDA device, for three element kinds
+ * only: C3D8 (nn = 8, reduced = 0), C3D20 (nn = 20, reduced = 0) and C3D20R
+ * (nn = 20, reduced = 1).  Every other nn, and nn = 8 with reduced != 0
+ * (C3D8R / C3D8I) or nn = 20 with reduced other than 0 / 1, returns
+ * AXIA_ERR_INVALID_ARG.  Limit: n_elem <= 2048 for nn = 8 and <= 512 for
+ * nn = 20 (AXIA_ERR_TOO_LARGE above).  Its device memory is one fixed 16 MiB
+ * array per device, held until the process exits; the first call on a device
+ * looks up that array's address and uploads the element tables, so make it
+ * before any stream capture; calls after cudaDeviceReset are not supported.
+ * Calls share the array: calls that overlap on the GPU race (calls within one
+ * process are serialized). */
 AXIA_API int32_t axia_gpu_element_ke_noalloc(int32_t nn, int32_t reduced, int64_t n_elem, const double* xyz,
                                              const double* e, double nu, double* ke, double* vol,
                                              int64_t* bad_elem);

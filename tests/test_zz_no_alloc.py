@@ -73,3 +73,13 @@ def test_noalloc_limits_and_errors(ctx):
     # the status word is cleared on the next call
     st, ke, vol, bad = _noalloc(_elements(8, 10, 5), 1.0, 0.3)
     assert st == _lib.OK and bad == -1
+
+
+@pytest.mark.parametrize("nn,reduced", [(8, 1), (8, 2), (20, 2), (20, -1), (4, 0), (10, 0), (6, 0), (15, 0)])
+def test_noalloc_rejects_unsupported_kinds(ctx, nn, reduced):
+    """Only C3D8, C3D20 and C3D20R: C3D8R / C3D8I and the other kinds are refused, not
+    answered with another element's stiffness."""
+    xyz = np.zeros((3, nn, 3))
+    st, ke, vol, bad = _noalloc(xyz, 1.0, 0.3, reduced)
+    assert st == _lib.ERR_INVALID_ARG and bad == -1
+    assert not ke.any()
