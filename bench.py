@@ -38,7 +38,7 @@ sys.path.insert(0, os.path.join(ROOT, "axia-fem_gb300"))
 
 METRIC = "MDOF/s static solve, mixed vs FP64 PCG at rel err ≤1e-8; SpMV HBM GB/s"
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
-CPU_SAMPLE_N = 30          # edge count of the CPU-baseline sample block
+CPU_SAMPLE_N = 50          # edge count of the CPU-baseline sample block (also timed on the GPU)
 RTOL = 1e-10
 
 
@@ -162,7 +162,8 @@ def recover_bytes(n_elem, nn, n_nodes):
 def cpu_baseline(n=CPU_SAMPLE_N, threads=1):
     """The CPU restatement of the reference's *STATIC path (oracle/) on a
     bounded sample: the same block, loads and BCs at n^3, full path
-    (element loop -> triplets -> reduce -> CSR -> PCG to rtol 1e-10)."""
+    (element loop -> triplets -> reduce -> CSR -> Jacobi PCG to rtol 1e-10;
+    the PCG's vector work over `threads` OpenMP threads)."""
     from axia_gpu import meshgen
     from oracle import oracle as O
     m = meshgen.block_c3d8_pressure(n=n)
@@ -173,7 +174,41 @@ def cpu_baseline(n=CPU_SAMPLE_N, threads=1):
     return {"value": r.n_free / dt / 1e6, "unit": "MDOF/s", "cores": threads, "kind": "port",
             "sample": f"C3D8 {n}^3 block, same loads/BCs, full path to rtol {RTOL:g} "
                       f"({r.n_free} free DOFs, {r.iters} PCG iterations, {dt:.2f} s)",
-            "seconds": dt, "iters": r.iters}
+            "seconds": dt, "iters": r.iters, "n_free": r.n_free,
+            "phases_s": {"element_loop": r.t_assembly, "reduce": r.t_reduce, "csr_from_triplets": r.t_csr,
+                         "pcg": r.t_solve}}
+
+
+def oracle_residuals(model, sols, f, group=4):
+    """||(K_oracle u - f)_free|| / ||f_free|| of each solution, with the oracle's own
+    element stiffness applied element by element over all host threads (no K
+    stored, no code shared with the library): the full-size accuracy check.
+    sols: {name: u[ndof]} (one load f) or {name: U[k][ndof]} (f is [k][ndof]);
+    vectors go through the element loop `group` at a time."""
+    import numpy as np
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    names, vecs, loads = [], [], []
+    for name, u in sols.items():
+        u = np.asarray(u)
+        if u.ndim == 1:
+            names.append(name)
+            vecs.append(u)
+            loads.append(f)
+        else:
+            for k in range(u.shape[0]):
+                names.append(name)
+                vecs.append(u[k])
+                loads.append(f[k])
+    res = []
+    for k in range(0, len(vecs), group):
+        res.extend(O.relative_residual(model, np.stack(vecs[k:k + group]), np.stack(loads[k:k + group])))
+    out = {}
+    for name, r in zip(names, res):
+        out[name] = max(out.get(name, 0.0), float(r))
+    return {"rel_residual_free": out, "seconds": time.perf_counter() - t0, "threads": os.cpu_count() or 1,
+            "what": "||(K u - f)_free|| / ||f_free|| with K the oracle's element stiffness (restated "
+                    "hex8/hex20_stiffness), applied element by element on the host; max over load cases"}
 
 
 class Timer:
@@ -218,6 +253,61 @@ def _line(args, workload, value, ms, extra):
     print(json.dumps(out))
 
 
+def same_sample_leg(args, local, n=CPU_SAMPLE_N):
+    """The GPU on the CPU baseline's own sample (the n^3 block): the reference's
+    algorithm (FP64 CSR Jacobi-PCG) and the headline path (mixed, two-level),
+    each as assemble + solve on resident inputs, and the headline path through
+    the C ABI with pinned host buffers (setup + assemble + solve + copy back)."""
+    import numpy as np
+    import torch
+    from axia_gpu import GpuContext, _lib as L, meshgen
+    model = meshgen.block_c3d8_pressure(n=n)
+    ctx = GpuContext(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    timer = Timer(torch, stream)
+    ctx.setup(model)
+    f_host = ctx.load_vector(model)
+    f_dev = torch.from_numpy(f_host).to(f"cuda:{local}")
+    u64, uco = torch.empty_like(f_dev), torch.empty_like(f_dev)
+    coarse_kw = dict(precision=L.PREC_MIXED, refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta,
+                     matrix_format=L.FORMAT_BSR3, preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
+
+    def step64():
+        ctx.assemble_ex(L.ASM_CSR64)
+        return ctx.solve_device(f_dev.data_ptr(), u64.data_ptr(), rtol=RTOL, precision=L.PREC_FP64)
+
+    def stepco():
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        return ctx.solve_device(f_dev.data_ptr(), uco.data_ptr(), rtol=RTOL, **coarse_kw)
+    ms64, i64 = timer(step64, args.warmup, args.steps)
+    msco, ico = timer(stepco, args.warmup, args.steps)
+    f_pin = torch.empty(f_host.shape, dtype=torch.float64, pin_memory=True).numpy()
+    f_pin[...] = f_host
+    u_pin = torch.empty(f_host.shape, dtype=torch.float64, pin_memory=True).numpy()
+    ctx.set_stream(None)
+    ts = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.setup(model)
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        ctx.solve(f_pin, out=u_pin, rtol=RTOL, **coarse_kw)
+        if k >= args.warmup:
+            ts.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * sum(ts) / len(ts)
+    nf = ctx.n_free
+    u64h = u64.cpu().numpy()
+    out = {"workload": f"C3D8 block {n}^3 (the CPU baseline's sample), same loads/BCs", "n_free": nf,
+           "fp64_jacobi": {"value": nf / (ms64 * 1e-3) / 1e6, "ms_per_step": ms64, "iters": i64.iters,
+                           "algorithm": "FP64 CSR Jacobi-PCG (the reference's)"},
+           "mixed_coarse": {"value": nf / (msco * 1e-3) / 1e6, "ms_per_step": msco, "iters": ico.iters,
+                            "rel_err_vs_fp64": float(np.linalg.norm(uco.cpu().numpy() - u64h) / np.linalg.norm(u64h))},
+           "mixed_coarse_e2e": {"value": nf / (e2e_ms * 1e-3) / 1e6, "ms_per_step": e2e_ms}}
+    ctx.close()
+    return out
+
+
 def run_c3(args):
     """C3D20 50^3 block, base clamped, random top traction: mixed (FP32 node-block
     inner CG, FP64 reliable updates) vs FP64 CSR PCG, both to rtol 1e-10."""
@@ -252,6 +342,8 @@ def run_c3(args):
     msco, ico = timer(stepco, args.warmup, args.steps)
     rel = float(torch.linalg.norm(umx - u64) / torch.linalg.norm(u64))
     relco = float(torch.linalg.norm(uco - u64) / torch.linalg.norm(u64))
+    oracle_check = oracle_residuals(m, {"fp64": u64.cpu().numpy(), "mixed": umx.cpu().numpy(),
+                                        "mixed_coarse": uco.cpu().numpy()}, f.cpu().numpy())
     nf = ctx.n_free
     n_sub, n_coarse = ctx.coarse_size()
     _line(args, f"C3D20 block {n}^3, 27-point Gauss, E=70000 nu=0.33, base clamped, top traction N(0,1)",
@@ -268,7 +360,8 @@ def run_c3(args):
            "mixed": {"ms_per_step": msmx, "inner_iters": imx.iters, "reliable_updates": imx.outer_iters,
                      "ms_assemble": imx.ms_assemble, "true_rel_residual": imx.true_residual / imx.bnorm,
                      "rel_err_vs_fp64": rel},
-           "speedup_mixed_vs_fp64": ms64 / msco, "speedup_mixed_jacobi_vs_fp64": ms64 / msmx})
+           "speedup_mixed_vs_fp64": ms64 / msco, "speedup_mixed_jacobi_vs_fp64": ms64 / msmx,
+           "oracle_check": oracle_check})
 
 
 def run_c4a(args):
@@ -303,6 +396,8 @@ def run_c4a(args):
                                 preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
     ms1, i1 = timer(single, 1, 2)
     err = float(torch.linalg.norm(U[0] - u1) / torch.linalg.norm(u1))
+    oracle_check = oracle_residuals(m, {"batched_coarse": U.cpu().numpy(), "batched_jacobi": Uj.cpu().numpy()},
+                                    m.cload_batch)
     nf = ctx.n_free
     _line(args, f"C3D8 block {n}^3, x=0 clamped, 32 load cases (5% of surface nodes, N(0,1))",
           32 * nf / (ms * 1e-3) / 1e6, ms,
@@ -314,7 +409,7 @@ def run_c4a(args):
            "batched_jacobi": {"ms_per_step": msj, "iters": infoj.iters, "reliable_updates": infoj.outer_iters,
                               "max_rel_residual": float(relj.max()), "ms_kernel": infoj.ms_pcg_kernel},
            "single_case": {"ms": ms1, "iters": i1.iters, "rel_err_batched_vs_single": err},
-           "speedup_vs_32_single_solves": 32 * ms1 / ms})
+           "speedup_vs_32_single_solves": 32 * ms1 / ms, "oracle_check": oracle_check})
 
 
 def run_c4b(args):
@@ -340,6 +435,15 @@ def run_c4b(args):
     ms, (info, rel, its) = timer(step, args.warmup, args.steps)
     err_j = float(torch.linalg.norm(u - uj) / torch.linalg.norm(uj))
     n_sub, n_coarse = ctx.coarse_size()
+    uh = u.cpu().numpy()
+    t0 = time.perf_counter()
+    worst = 0.0
+    for k, c in enumerate(cubes):
+        chk = oracle_residuals(c, {"u": uh[3 * ctx.node0[k]:3 * ctx.node0[k + 1]]}, c.cload)
+        worst = max(worst, chk["rel_residual_free"]["u"])
+    oracle_check = {"rel_residual_free": {"multi_coarse_worst_mesh": worst}, "seconds": time.perf_counter() - t0,
+                    "what": "per mesh ||(K u - f)_free|| / ||f_free|| with the oracle's element stiffness; "
+                            "the worst of the 64 meshes"}
     nf = ctx.n_free
     _line(args, "64 C3D8 cubes, edge counts U{10..40} (seeded), x=0 clamped, random surface loads",
           nf / (ms * 1e-3) / 1e6, ms,
@@ -349,7 +453,8 @@ def run_c4b(args):
            "multi": {"max_iters": int(its.max()), "min_iters": int(its.min()), "max_rel_residual": float(rel.max()),
                      "ms_kernel": info.ms_pcg_kernel, "ms_assemble": info.ms_assemble,
                      "rel_err_vs_diagonal": err_j, "coarse_unknowns": n_coarse},
-           "multi_diagonal": {"ms_per_step": msj, "max_iters": int(itsj.max()), "ms_kernel": infoj.ms_pcg_kernel}})
+           "multi_diagonal": {"ms_per_step": msj, "max_iters": int(itsj.max()), "ms_kernel": infoj.ms_pcg_kernel},
+           "oracle_check": oracle_check})
 
 
 def run_c5(args):
@@ -395,6 +500,7 @@ def run_c5(args):
         worst_direct = max(worst_direct, abs((cp - cm) / (2 * h) - g[k]) / abs(g[k]))
     m.e_elem = m.e0 * m.rho ** m.pexp
     g_cpu = O.compliance_grad(m, m.rho, m.pexp, m.e0, u)
+    oracle_check = oracle_residuals(m, {"forward_fp64": u64, "forward_mixed_coarse": u}, f)
     nf = ctx.n_free
     _line(args, "SIMP beam 100x50x50 C3D8, E=rho^3, rho~U[0.3,1], tip load", nf / t_fwd / 1e6, t_fwd * 1e3,
           {"dtype": "f32+f64", "config": {"workload": "C3D8 100x50x50 SIMP", "n_free": nf, "elements": m.n_elem,
@@ -406,7 +512,8 @@ def run_c5(args):
            "backward_ms": t_bwd * 1e3,
            "gradient_vs_cpu_analytic_max_rel": float(np.abs(g - g_cpu).max() / np.abs(g_cpu).max()),
            "fd_20_elements": {"h": h, "max_rel_err_exact_difference": worst_exact,
-                              "max_rel_err_direct_difference": worst_direct}})
+                              "max_rel_err_direct_difference": worst_direct},
+           "oracle_check": oracle_check})
 
 
 def run_reference(args):
@@ -665,6 +772,10 @@ def main():
              "rel_err_mixed_csr": float(np.linalg.norm(umc.cpu().numpy() - uth) / np.linalg.norm(uth)),
              "rel_err_mixed_coarse": float(np.linalg.norm(uco.cpu().numpy() - uth) / np.linalg.norm(uth))}
 
+    # full-size residual of every solution under the oracle's own stiffness (host, untimed)
+    oracle_check = oracle_residuals(model, {"fp64": u64h, "mixed": umx.cpu().numpy(), "mixed_csr": umc.cpu().numpy(),
+                                            "mixed_coarse": uco.cpu().numpy(), "fp64_rtol_1e-12": uth}, f_host)
+
     last64, lastmx, lastmc, lastco = inf64[-1], infmx[-1], infmc[-1], infco[-1]
     mdofs_co = n / (msco * 1e-3) / 1e6 * world
     mdofs = n / (msmx * 1e-3) / 1e6 * world
@@ -727,11 +838,25 @@ def main():
         e2e = {"value": n / e2e_s / 1e6 * world, "unit": "MDOF/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
 
+    same = None
+    if rank == 0 and not args.no_cpu:
+        same = same_sample_leg(args, local)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(CPU_SAMPLE_N, 1)
-        cpu.pop("seconds", None)
-        cpu.pop("iters", None)
+        cpu = cpu_baseline(CPU_SAMPLE_N, os.cpu_count() or 1)
+        cpu_iters, cpu_s = cpu.pop("iters"), cpu.pop("seconds")
+        cpu.pop("n_free")
+        if same is not None:
+            same["cpu"] = {"value": cpu["value"], "iters": cpu_iters, "seconds": cpu_s, "threads": cpu["cores"],
+                           "phases_s": cpu.pop("phases_s")}
+            same["gpu_over_cpu_same_algorithm"] = same["fp64_jacobi"]["value"] / cpu["value"]
+            same["gpu_over_cpu_headline"] = same["mixed_coarse"]["value"] / cpu["value"]
+            same["gpu_over_cpu_headline_e2e"] = same["mixed_coarse_e2e"]["value"] / cpu["value"]
+            same["jacobi_iterations"] = {f"{CPU_SAMPLE_N}^3 (CPU)": cpu_iters,
+                                         f"{CPU_SAMPLE_N}^3 (GPU FP64)": same["fp64_jacobi"]["iters"],
+                                         f"{args.n}^3 (GPU FP64)": inf64[-1]["iters"]}
+        else:
+            cpu.pop("phases_s", None)
 
     if rank != 0:
         if dist is not None:
@@ -794,6 +919,8 @@ def main():
         "roofline_mixed_csr_pcg": {"bound": "hbm", "achieved": achmc, "peak": hbm, "unit": "GB/s",
                                    "frac": achmc / hbm, "kernel": "pcg_reliable_kernel (CSR FP32 + FP64 updates)",
                                    "ms_per_launch": kmc_ms, "bytes_per_launch": bytesmc},
+        "oracle_check": oracle_check,
+        "same_sample": same,
         "gpu_launches": int(la64 + lamx + lamc + laco),
         "clocks": clocks,
         "e2e": e2e,

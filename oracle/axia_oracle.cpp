@@ -1808,6 +1808,68 @@ int or_reactions(int64_t n_nodes, const double* coords, int nn, int reduced, int
   return OK;
 }
 
+// K u_k - f_k for nvec vectors at once (u, f, rf: [nvec][3 n_nodes]) with the
+// element stiffness of the restated element_ke, the reactions of
+// analysis.rs:1027-1035 without triplets: element by element, Ke computed once
+// per element and applied to every vector.  nthreads > 1 splits the element
+// loop into nthreads contiguous ranges with their own accumulators, added in
+// range order (the result depends on nthreads only through that order).
+// Used as a residual check of solutions computed elsewhere: no K is stored,
+// so it reaches meshes whose triplet lists would not fit in host memory.
+int or_residual_multi(int64_t n_nodes, const double* coords, int nn, int reduced, int64_t n_elem,
+                      const int32_t* conn, const double* e_elem, double nu, int64_t nvec, const double* u,
+                      const double* f, double* rf, int nthreads, int64_t* bad) {
+  const int m = 3 * nn;
+  const int64_t ndof = 3 * n_nodes;
+  if (nthreads < 1) nthreads = 1;
+  std::vector<std::vector<double>> acc(nthreads);
+  std::vector<int64_t> first_bad(nthreads, -1);
+  std::vector<int> first_st(nthreads, OK);
+#pragma omp parallel num_threads(nthreads)
+  {
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    const int64_t e0 = n_elem * t / nt, e1 = n_elem * (t + 1) / nt;
+    std::vector<double>& ku = acc[t];
+    ku.assign((size_t)nvec * ndof, 0.0);
+    std::vector<double> ke((size_t)m * m);
+    double xyz[60], vol;
+    for (int64_t e = e0; e < e1; ++e) {
+      const int32_t* c = conn + e * nn;
+      for (int a = 0; a < nn; ++a)
+        for (int q = 0; q < 3; ++q) xyz[3 * a + q] = coords[3 * (int64_t)c[a] + q];
+      const int st = element_ke(nn, xyz, e_elem[e], nu, reduced, ke.data(), &vol);
+      if (st) {
+        first_bad[t] = e;
+        first_st[t] = st;
+        break;
+      }
+      for (int64_t k = 0; k < nvec; ++k) {
+        const double* uk = u + k * ndof;
+        double* yk = ku.data() + k * ndof;
+        for (int i = 0; i < m; ++i) {
+          double s = 0.0;
+          for (int j = 0; j < m; ++j) s += ke[(size_t)i * m + j] * uk[3 * (int64_t)c[j / 3] + j % 3];
+          yk[3 * (int64_t)c[i / 3] + i % 3] += s;
+        }
+      }
+    }
+  }
+  for (int t = 0; t < nthreads; ++t)
+    if (first_st[t]) {
+      *bad = first_bad[t];
+      return first_st[t];
+    }
+  const int64_t tot = nvec * ndof;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+  for (int64_t d = 0; d < tot; ++d) {
+    double s = 0.0;
+    for (int t = 0; t < nthreads; ++t)
+      if (!acc[t].empty()) s += acc[t][d];
+    rf[d] = s - f[d];
+  }
+  return OK;
+}
+
 // ||K x - b|| <= 1e-8 max(||b||, 1) + 1e-10 (sparse_native.rs:1572-1578)
 int or_residual_ok(double residual, double bnorm) {
   return std::isfinite(residual) && residual <= 1e-8 * std::max(bnorm, 1.0) + 1e-10;

@@ -65,6 +65,8 @@ def lib():
         L.or_solve_kff.argtypes = [C.c_int64, C.c_int64, _i64, _i64, _d, _d, C.c_int, C.c_double,
                                    C.c_int64, C.c_int, _d, _d]
         L.or_residual_ok.argtypes = [C.c_double, C.c_double]
+        L.or_residual_multi.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int64, _i32, _d, C.c_double,
+                                        C.c_int64, _d, _d, _d, C.c_int, C.POINTER(C.c_int64)]
         L.or_nodal_stress.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int64, _i32, _d, C.c_double, _d, _d,
                                       C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]
         L.or_reactions.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int64, _i32, _d, C.c_double, _d, _d, _d,
@@ -255,6 +257,45 @@ def reactions(model, u_full, f_full):
     if st:
         raise OracleError(st, f"reactions element {bad.value}")
     return rf
+
+
+def residual_multi(model, u, f, nthreads=None):
+    """K u - f for one vector (u[ndof]) or several (u[k][ndof], f the same shape or
+    one f for all) with the oracle's own element stiffness, element by element
+    (no K stored), the element loop split over nthreads (default: all cores)."""
+    u = np.ascontiguousarray(u, np.float64)
+    one = u.ndim == 1
+    U = u.reshape(1, -1) if one else u
+    F = np.ascontiguousarray(np.broadcast_to(f, U.shape), np.float64)
+    out = np.zeros_like(U)
+    nt = int(nthreads or os.cpu_count() or 1)
+    bad = C.c_int64(-1)
+    st = lib().or_residual_multi(model.n_nodes, np.ascontiguousarray(model.coords).ravel(), model.nn,
+                                 int(model.reduced), model.n_elem,
+                                 np.ascontiguousarray(model.conn, dtype=np.int32).ravel(),
+                                 np.ascontiguousarray(model.e_elem, np.float64), float(model.nu), U.shape[0],
+                                 U.ravel(), F.ravel(), out.ravel(), nt, C.byref(bad))
+    if st:
+        raise OracleError(st, f"residual element {bad.value}")
+    return out[0] if one else out
+
+
+def free_mask(model):
+    """True on the DOFs no boundary condition prescribes (the model's SPCs only)."""
+    m = np.ones(model.ndof, bool)
+    m[np.asarray(model.bc_dof, np.int64)] = False
+    return m
+
+
+def relative_residual(model, u, f, nthreads=None):
+    """||(K u - f)_free|| / ||f_free|| per vector with the oracle's K: the residual of a
+    solution computed elsewhere under the oracle's own assembly (prescribed values zero)."""
+    r = residual_multi(model, u, f, nthreads)
+    m = free_mask(model)
+    F = np.broadcast_to(f, np.shape(u))
+    if r.ndim == 1:
+        return float(np.linalg.norm(r[m]) / np.linalg.norm(F[m]))
+    return np.linalg.norm(r[:, m], axis=1) / np.linalg.norm(F[:, m], axis=1)
 
 
 def residual_ok(residual, bnorm):

@@ -276,3 +276,22 @@ def test_wedge_face_pressure_resultant(nn):
         np.testing.assert_allclose(fe, 2.0 * np.array(vec), atol=1e-13)
     with pytest.raises(O.OracleError):
         O.face_pressure(xyz, 6, 1.0)
+
+
+@pytest.mark.parametrize("name,model", [("c3d8", meshgen.block_c3d8_pressure(n=6)),
+                                        ("c3d20", meshgen.block_c3d20_traction(n=3)),
+                                        ("simp", meshgen.simp_beam(nx=6, ny=3, nz=3))])
+def test_residual_multi_matches_reactions_and_solutions(name, model):
+    """The element-by-element residual K u - f (several vectors, threads) equals
+    the serial reactions over the triplets, and is ~0 on the free DOFs of the
+    oracle's own direct solution."""
+    f = O.load_vector(model)
+    rng = np.random.default_rng(3)
+    U = rng.standard_normal((3, model.ndof))
+    R = O.residual_multi(model, U, f, nthreads=4)
+    for k in range(3):
+        ref = O.reactions(model, U[k], f)
+        assert np.abs(R[k] - ref).max() <= 1e-12 * np.abs(ref).max(), (name, k)
+    assert np.array_equal(O.residual_multi(model, U[1], f, nthreads=1), O.residual_multi(model, U[1], f, 1))
+    r = O.solve_static(model, solver=O.SOLVER_CHOLESKY, f=f)
+    assert O.relative_residual(model, r.u, f, 3) <= 1e-12
