@@ -92,6 +92,7 @@ SIGNATURES = [
     ("axia_gpu_set_stream", C.c_int32, [_P, _P]),
     ("axia_gpu_kernel_launches", C.c_int64, [_P]),
     ("axia_gpu_check_wait_limit", C.c_int32, [_P, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    ("axia_gpu_fma_rate", C.c_int32, [_P, C.c_int32, C.POINTER(C.c_double)]),
     ("axia_gpu_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32]),
     ("axia_gpu_bsr_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32, C.c_int32]),
     ("axia_gpu_node_blocks", C.c_int64, [_P]),

@@ -193,6 +193,12 @@ class GpuContext:
                     "check_wait_limit")
         return int(st.value), float(ms.value)
 
+    def fma_rate(self, precision=L.PREC_FP64) -> float:
+        """Measured FMA throughput of the device in TFLOP/s (FP64 or FP32)."""
+        t = C.c_double(0.0)
+        self._check(self.lib.axia_gpu_fma_rate(self.h, int(precision), C.byref(t)), "fma_rate")
+        return float(t.value)
+
     def spmv_device(self, precision, x_dev_ptr, y_dev_ptr, lanes=0):
         self._check(self.lib.axia_gpu_spmv_device(self.h, int(precision), C.c_void_p(x_dev_ptr),
                                                   C.c_void_p(y_dev_ptr), int(lanes)), "spmv")

@@ -131,3 +131,62 @@ int device_exclusive_scan(axia_ctx* ctx, const int64_t* d_in, int64_t* d_out, in
   dev_free(d_tot_scan);
   return AXIA_OK;
 }
+
+// ---------------------------------------------------------------------------
+// FMA throughput probe: every thread runs NCH independent chains of
+// a = fma(a, m, c) (2 flops each), the grid fills every SM; the rate is the
+// flops over the kernel's CUDA-event time (best of three launches).  It gives
+// the FP64 (and FP32) denominators of the element kernel's roofline.
+// ---------------------------------------------------------------------------
+template <typename T, int NCH>
+__global__ void __launch_bounds__(256) k_fma_rate(int iters, T m, T c, T* sink) {
+  T a[NCH];
+#pragma unroll
+  for (int k = 0; k < NCH; ++k) a[k] = T(threadIdx.x + k) * T(1e-3);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < NCH; ++k) a[k] = fma(a[k], m, c);
+  }
+  T s = T(0);
+#pragma unroll
+  for (int k = 0; k < NCH; ++k) s += a[k];
+  if (s == T(-1.0)) sink[blockIdx.x] = s;  // never true for these inputs; keeps the chains live
+}
+
+template <typename T, int NCH>
+static int fma_rate(axia_ctx* ctx, int iters, double* tflops) {
+  auto kern = k_fma_rate<T, NCH>;
+  int per_sm = 0;
+  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+  const int grid = std::max(1, per_sm) * ctx->sm_count;
+  T* sink = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &sink, (size_t)grid));
+  cudaEvent_t a, b;
+  AXIA_CUDA(ctx, cudaEventCreate(&a));
+  AXIA_CUDA(ctx, cudaEventCreate(&b));
+  float best = 0.f;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(a, ctx->stream);
+    kern<<<grid, 256, 0, ctx->stream>>>(iters, T(0.9999999), T(1e-7), sink);
+    cudaEventRecord(b, ctx->stream);
+    ctx->launches++;
+    AXIA_CUDA(ctx, cudaEventSynchronize(b));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;  // the first launch warms up
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  dev_free(sink);
+  AXIA_CUDA(ctx, cudaGetLastError());
+  const double flops = 2.0 * NCH * (double)iters * (double)grid * 256.0;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return AXIA_OK;
+}
+
+extern "C" AXIA_API int32_t axia_gpu_fma_rate(axia_ctx* ctx, int32_t precision, double* tflops) {
+  if (!ctx || !tflops) return AXIA_ERR_INVALID_ARG;
+  AXIA_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (precision == AXIA_PREC_FP64) return fma_rate<double, 8>(ctx, 2048, tflops);
+  return fma_rate<float, 16>(ctx, 16384, tflops);
+}

@@ -244,6 +244,13 @@ AXIA_API int64_t axia_gpu_kernel_launches(const axia_ctx* ctx);
  * AXIA_OK unless the call itself failed. */
 AXIA_API int32_t axia_gpu_check_wait_limit(axia_ctx* ctx, int64_t limit_us, int32_t* status, double* elapsed_ms);
 
+/* Measured FMA throughput of the context's device (no reference counterpart;
+ * the denominator of the FP64-bound element kernel's roofline): every thread
+ * of a full grid runs independent chains of fused multiply-adds, timed with
+ * CUDA events (best of three after one warm-up launch).  precision
+ * AXIA_PREC_FP64: double; anything else: float.  *tflops = 2 x FMAs / time. */
+AXIA_API int32_t axia_gpu_fma_rate(axia_ctx* ctx, int32_t precision, double* tflops);
+
 /* y = K_ff x on device vectors of n_free entries: FP64 (double x, y) with
  * precision AXIA_PREC_FP64, FP32 (float x, y, the FP32 copy of K_ff) with
  * AXIA_PREC_MIXED.  lanes: CSR lanes per row (0 = automatic).  The matrix
