@@ -43,8 +43,10 @@ ASM_CSR64 = 1
 ASM_CSR32 = 2
 ASM_BSR64 = 4
 ASM_BSR32 = 8
+ASM_SYM32 = 16
 FORMAT_CSR = 0
 FORMAT_BSR3 = 1
+FORMAT_BSR3_SYM = 2
 PRECOND_JACOBI = 0
 PRECOND_COARSE = 1
 
@@ -95,6 +97,8 @@ SIGNATURES = [
     ("axia_gpu_fma_rate", C.c_int32, [_P, C.c_int32, C.POINTER(C.c_double)]),
     ("axia_gpu_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32]),
     ("axia_gpu_bsr_spmv_device", C.c_int32, [_P, C.c_int32, _P, _P, C.c_int32, C.c_int32]),
+    ("axia_gpu_sym_spmv_device", C.c_int32, [_P, _P, _P, C.c_int32]),
+    ("axia_gpu_sym_blocks", C.c_int64, [_P, C.POINTER(C.c_int64)]),
     ("axia_gpu_node_blocks", C.c_int64, [_P]),
     ("axia_gpu_coarse_size", C.c_int32, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("axia_gpu_setup_multi", C.c_int32, [_P, C.c_int32, C.POINTER(Mesh), _P, _P, _P]),

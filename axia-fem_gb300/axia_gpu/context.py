@@ -207,6 +207,17 @@ class GpuContext:
         self._check(self.lib.axia_gpu_bsr_spmv_device(self.h, int(precision), C.c_void_p(x_dev_ptr),
                                                       C.c_void_p(y_dev_ptr), int(lanes), int(vec)), "bsr_spmv")
 
+    def sym_spmv_device(self, x_dev_ptr, y_dev_ptr, lanes=0):
+        """y = K x (FP32) with the matrix in symmetric storage (AXIA_ASM_SYM32)."""
+        self._check(self.lib.axia_gpu_sym_spmv_device(self.h, C.c_void_p(x_dev_ptr), C.c_void_p(y_dev_ptr),
+                                                      int(lanes)), "sym_spmv")
+
+    def sym_blocks(self):
+        """(stored upper blocks incl. padding, lower-list entries) of the symmetric form."""
+        nl = C.c_int64(0)
+        nu = int(self.lib.axia_gpu_sym_blocks(self.h, C.byref(nl)))
+        return nu, int(nl.value)
+
     def solve(self, f_full, out=None, **kw):
         """u for the load vector f_full (host arrays; out: a float64 array of the same
         size to write u into, e.g. in pinned memory)."""

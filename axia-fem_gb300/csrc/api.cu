@@ -11,6 +11,7 @@ int symbolic_setup(axia_ctx* ctx, int64_t n_bc, const int64_t* d_bc_dof, const d
 int numeric_assemble(axia_ctx* ctx, int flags);
 int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_opts* opts, axia_solve_info* info);
 int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req, int vec_req);
+int sym_spmv_device(axia_ctx* ctx, const float* x, float* y, int lanes_req);
 int element_energy(axia_ctx* ctx, const double* d_u, const double* d_v, double* d_s);
 int simp_modulus(axia_ctx* ctx, const double* d_rho, double pexp, double e0);
 int simp_gradient(axia_ctx* ctx, const double* d_rho, const double* d_s, double pexp, double e0, double* d_g);
@@ -103,6 +104,12 @@ void free_mesh_state(axia_ctx* ctx) {
   ctx->nbq = 0;
   dev_release(ctx, ctx->d_bval64);
   dev_release(ctx, ctx->d_bval32);
+  dev_release(ctx, ctx->d_uptr);
+  dev_release(ctx, ctx->d_uval);
+  dev_release(ctx, ctx->d_lptr);
+  dev_release(ctx, ctx->d_low);
+  ctx->nbu = ctx->nbl = 0;
+  ctx->have_sym32 = false;
   dev_release(ctx, ctx->d_bdinv64);
   dev_release(ctx, ctx->d_bdinv32);
   dev_release(ctx, ctx->d_bf);
@@ -338,7 +345,7 @@ int32_t axia_gpu_assemble_ex(axia_ctx* ctx, int32_t flags) {
   if (!ctx) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   if (!ctx->d_rowptr || !ctx->d_conn) return set_error(ctx, AXIA_ERR_STATE, "assemble before setup");
-  if (flags <= 0 || flags > 15) return set_error(ctx, AXIA_ERR_INVALID_ARG, "assemble: unknown matrix forms");
+  if (flags <= 0 || flags > 31) return set_error(ctx, AXIA_ERR_INVALID_ARG, "assemble: unknown matrix forms");
   EventTimer t(ctx->stream);
   int st = numeric_assemble(ctx, flags);
   ctx->ms_assemble = t.stop_ms();
@@ -364,12 +371,13 @@ static int32_t solve_common(axia_ctx* ctx, const double* d_f, double* d_u, const
   }
   if (!(o.rtol > 0.0)) o.rtol = 1e-8;
   if (o.preconditioner != AXIA_PRECOND_JACOBI &&
-      (o.preconditioner != AXIA_PRECOND_COARSE || o.matrix_format != AXIA_FORMAT_BSR3 ||
+      (o.preconditioner != AXIA_PRECOND_COARSE ||
+       (o.matrix_format != AXIA_FORMAT_BSR3 && o.matrix_format != AXIA_FORMAT_BSR3_SYM) ||
        o.precision != AXIA_PREC_MIXED))
     return set_error(ctx, AXIA_ERR_INVALID_ARG, "the coarse preconditioner needs the mixed node-block solve");
   EventTimer t(ctx->stream);
   int st = AXIA_OK;
-  if (ctx->n_free > 0 && o.matrix_format == AXIA_FORMAT_BSR3) {
+  if (ctx->n_free > 0 && (o.matrix_format == AXIA_FORMAT_BSR3 || o.matrix_format == AXIA_FORMAT_BSR3_SYM)) {
     st = bsr_solve(ctx, d_f, d_u, &o, info);
     info->ms_solve = t.stop_ms();
     fill_info_sizes(ctx, info);
@@ -600,6 +608,19 @@ int32_t axia_gpu_bsr_spmv_device(axia_ctx* ctx, int32_t precision, const void* x
   return bsr_spmv_device(ctx, precision == AXIA_PREC_MIXED, x_dev, y_dev, lanes, vec);
 }
 
+int32_t axia_gpu_sym_spmv_device(axia_ctx* ctx, const float* x_dev, float* y_dev, int32_t lanes) {
+  if (!ctx || !x_dev || !y_dev) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  if (!ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "spmv before assemble");
+  return sym_spmv_device(ctx, x_dev, y_dev, lanes);
+}
+
+int64_t axia_gpu_sym_blocks(const axia_ctx* ctx, int64_t* lower_entries) {
+  if (!ctx) return -1;
+  if (lower_entries) *lower_entries = ctx->nbl;
+  return ctx->nbu;
+}
+
 int64_t axia_gpu_node_blocks(const axia_ctx* ctx) { return ctx ? ctx->n_adj : -1; }
 
 int32_t axia_gpu_element_energy(axia_ctx* ctx, const double* u_full, const double* v_full, double* s) {
@@ -642,8 +663,9 @@ int32_t axia_gpu_compliance_forward(axia_ctx* ctx, const double* rho, double pen
     o.rtol = 1e-10;
   }
   const bool mixed = o.precision == AXIA_PREC_MIXED;
-  int flags = o.matrix_format == AXIA_FORMAT_BSR3 ? (AXIA_ASM_BSR64 | (mixed ? AXIA_ASM_BSR32 : 0))
-                                                  : (AXIA_ASM_CSR64 | (mixed ? AXIA_ASM_CSR32 : 0));
+  int flags = o.matrix_format == AXIA_FORMAT_BSR3       ? (AXIA_ASM_BSR64 | (mixed ? AXIA_ASM_BSR32 : 0))
+              : o.matrix_format == AXIA_FORMAT_BSR3_SYM ? (AXIA_ASM_BSR64 | AXIA_ASM_SYM32)
+                                                        : (AXIA_ASM_CSR64 | (mixed ? AXIA_ASM_CSR32 : 0));
   AXIA_TRY(axia_gpu_assemble_ex(ctx, flags));
   AXIA_TRY(axia_gpu_solve(ctx, f_full, u_full, &o, info));
   AXIA_TRY(device_dot(ctx, ctx->d_f, ctx->d_u, ctx->ndof, compliance));

@@ -584,6 +584,66 @@ __global__ void k_fill_columns(int64_t n_nodes, const int64_t* adj_ptr, const in
 }
 
 // ---------------------------------------------------------------------------
+// Symmetric node-block form (AXIA_ASM_SYM32): structure from the sorted node
+// adjacency.  Row a keeps its blocks b >= a (the adjacency's tail, starting at
+// the diagonal) as upper blocks, padded to an even count, and lists its
+// neighbours b < a with the position of K_ba among row b's upper blocks.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int lower_bound_i32(const int32_t* v, int n, int key) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (v[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_sym_counts(int64_t n_nodes, const int64_t* adj_ptr, const int32_t* adj, int64_t* ucnt,
+                             int64_t* lcnt) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a <= n_nodes; a += (int64_t)gridDim.x * blockDim.x) {
+    if (a == n_nodes) {
+      ucnt[a] = lcnt[a] = 0;
+      continue;
+    }
+    const int64_t s0 = adj_ptr[a];
+    const int len = (int)(adj_ptr[a + 1] - s0);
+    const int first = lower_bound_i32(adj + s0, len, (int)a);
+    ucnt[a] = (len - first + 1) & ~1;
+    lcnt[a] = first;
+  }
+}
+
+__global__ void k_sym_lower(int64_t n_nodes, const int64_t* adj_ptr, const int32_t* adj, const int64_t* uptr,
+                            const int64_t* lptr, int2* low) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n_nodes; a += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s0 = adj_ptr[a], l0 = lptr[a];
+    const int nl = (int)(lptr[a + 1] - l0);
+    for (int k = 0; k < nl; ++k) {
+      const int b = adj[s0 + k];  // b < a: the sorted adjacency's head
+      const int64_t t0 = adj_ptr[b];
+      const int blen = (int)(adj_ptr[b + 1] - t0);
+      const int first_b = lower_bound_i32(adj + t0, blen, b);
+      const int at = lower_bound_i32(adj + t0, blen, (int)a);
+      low[l0 + k] = make_int2(b, (int)(uptr[b] + (at - first_b)));
+    }
+  }
+}
+
+// pad blocks of the upper rows: zero values, the row's own node as column
+__global__ void k_sym_pad(int64_t n_nodes, const int64_t* adj_ptr, const int32_t* adj, const int64_t* uptr,
+                          float* uval) {
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n_nodes; a += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s0 = adj_ptr[a];
+    const int len = (int)(adj_ptr[a + 1] - s0);
+    const int nu = len - lower_bound_i32(adj + s0, len, (int)a);
+    for (int64_t k = uptr[a] + nu; k < uptr[a + 1]; ++k) {
+      for (int c = 0; c < 9; ++c) uval[10 * k + c] = 0.f;
+      uval[10 * k + 9] = __int_as_float((int)a);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Numeric gather: warp per node, contributions of incident elements summed in
 // ascending element order into a shared-memory block row, then written as up
 // to three CSR rows of K_ff (free columns) and K_fp u0 (prescribed columns).
@@ -616,6 +676,8 @@ struct GatherArgs {
   float* bdinv32;
   const int32_t* qptr;  // padded node-block row starts
   int64_t nb;           // padded block count (plane stride)
+  float* uval;          // symmetric FP32 form [nbu][10] (null: not assembled)
+  const int32_t* uptr;  // its upper-block row starts
 };
 
 // incident elements whose column slots are looked up at once (x nodes per
@@ -718,7 +780,26 @@ __global__ void k_gather(GatherArgs g) {
         if (lane == 0) g.kfu0[r] = kf;
       }
     }
-    if (g.bval64 || g.bval32) {
+    if (g.uval) {
+      // symmetric form: the blocks b >= a of the row (sorted adjacency tail), 9 values + column
+      const int first_up = lower_bound_i32(s_adj, nadj, (int)a);
+      const int nu = nadj - first_up;
+      const int64_t u0 = g.uptr[a];
+      for (int t = lane; t < 10 * nu; t += 32) {
+        const int k = t / 10, c = t - 10 * k, s = first_up + k;
+        const int b = s_adj[s];
+        float v;
+        if (c < 9) {
+          const int i = c / 3, j = c % 3;
+          const bool fi = g.ind_of[3 * a + i] >= 0, fj = g.ind_of[3 * (int64_t)b + j] >= 0;
+          v = (fi && fj) ? (float)acc[s * 9 + c] : ((b == a && i == j) ? 1.f : 0.f);
+        } else {
+          v = __int_as_float(b);
+        }
+        g.uval[10 * (u0 + k) + c] = v;
+      }
+    }
+    if (g.bval64 || g.bval32 || g.uval) {
       // node-block form: free-free entries of K, a unit diagonal on prescribed DOFs
       for (int t = lane; t < 9 * nadj; t += 32) {
         const int ij = t / nadj, s = t - ij * nadj;
@@ -979,10 +1060,54 @@ int symbolic_setup(axia_ctx* ctx, int64_t n_bc, const int64_t* d_bc_dof, const d
   return AXIA_OK;
 }
 
+// Structure of the symmetric FP32 node-block form, built on first use per mesh:
+// upper-block row starts (even counts), pad blocks, lower lists.
+static int ensure_sym_structure(axia_ctx* ctx) {
+  if (ctx->d_uval) return AXIA_OK;
+  cudaStream_t s = ctx->stream;
+  const int64_t n_nodes = ctx->n_nodes;
+  int64_t *d_ucnt = nullptr, *d_lcnt = nullptr, *d_uptr64 = nullptr, *d_lptr64 = nullptr;
+  AXIA_TRY(dev_alloc(ctx, &d_ucnt, n_nodes + 1));
+  AXIA_TRY(dev_alloc(ctx, &d_lcnt, n_nodes + 1));
+  AXIA_TRY(dev_alloc(ctx, &d_uptr64, n_nodes + 1));
+  AXIA_TRY(dev_alloc(ctx, &d_lptr64, n_nodes + 1));
+  k_sym_counts<<<grid_for(n_nodes + 1, 256, ctx->sm_count), 256, 0, s>>>(n_nodes, ctx->d_adj_ptr, ctx->d_adj, d_ucnt,
+                                                                        d_lcnt);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  int64_t nbu = 0, nbl = 0;
+  AXIA_TRY(device_exclusive_scan(ctx, d_ucnt, d_uptr64, n_nodes + 1, &nbu));
+  AXIA_TRY(device_exclusive_scan(ctx, d_lcnt, d_lptr64, n_nodes + 1, &nbl));
+  if (nbu >= (int64_t)INT32_MAX / 10 || nbl >= (int64_t)INT32_MAX)
+    return set_error(ctx, AXIA_ERR_TOO_LARGE, "symmetric node-block form exceeds 32-bit positions");
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_uptr, n_nodes + 1));
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_lptr, n_nodes + 1));
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_uval, (size_t)std::max<int64_t>(10 * nbu, 20)));
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_low, (size_t)std::max<int64_t>(nbl, 1)));
+  k_to_i32<<<grid_for(n_nodes + 1, 256, ctx->sm_count), 256, 0, s>>>(n_nodes + 1, d_uptr64, ctx->d_uptr);
+  k_to_i32<<<grid_for(n_nodes + 1, 256, ctx->sm_count), 256, 0, s>>>(n_nodes + 1, d_lptr64, ctx->d_lptr);
+  k_sym_lower<<<grid_for(n_nodes, 128, ctx->sm_count), 128, 0, s>>>(n_nodes, ctx->d_adj_ptr, ctx->d_adj, d_uptr64,
+                                                                    d_lptr64, ctx->d_low);
+  k_sym_pad<<<grid_for(n_nodes, 256, ctx->sm_count), 256, 0, s>>>(n_nodes, ctx->d_adj_ptr, ctx->d_adj, d_uptr64,
+                                                                  ctx->d_uval);
+  ctx->launches += 4;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  AXIA_CUDA(ctx, cudaStreamSynchronize(s));
+  dev_release(ctx, d_ucnt);
+  dev_release(ctx, d_lcnt);
+  dev_release(ctx, d_uptr64);
+  dev_release(ctx, d_lptr64);
+  ctx->nbu = nbu;
+  ctx->nbl = nbl;
+  return AXIA_OK;
+}
+
 int numeric_assemble(axia_ctx* ctx, int flags) {
   cudaStream_t s = ctx->stream;
   const bool csr64 = flags & AXIA_ASM_CSR64, csr32 = flags & AXIA_ASM_CSR32;
   const bool bsr64 = flags & AXIA_ASM_BSR64, bsr32 = flags & AXIA_ASM_BSR32;
+  const bool sym32 = flags & AXIA_ASM_SYM32;
+  if (sym32) AXIA_TRY(ensure_sym_structure(ctx));
   const int64_t kesz = (int64_t)9 * ctx->nn * ctx->nn;
   if (ctx->ke_elems < (size_t)(ctx->n_elem * kesz)) {
     AXIA_TRY(dev_alloc(ctx, &ctx->d_ke, (size_t)(ctx->n_elem * kesz)));
@@ -1017,8 +1142,8 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
     AXIA_TRY(dev_alloc(ctx, &ctx->d_bval32, (size_t)(9 * ctx->nbq)));
     AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bval32, 0, (size_t)(9 * ctx->nbq) * sizeof(float), s));
   }
-  if ((bsr64 || bsr32) && !ctx->d_bdinv64) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv64, (size_t)ctx->ndof));
-  if (bsr32 && !ctx->d_bdinv32) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv32, (size_t)ctx->ndof));
+  if ((bsr64 || bsr32 || sym32) && !ctx->d_bdinv64) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv64, (size_t)ctx->ndof));
+  if ((bsr32 || sym32) && !ctx->d_bdinv32) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv32, (size_t)ctx->ndof));
   AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_kfu0, 0, ctx->n_free * sizeof(double), s));
   GatherArgs g{};
   g.n_nodes = ctx->n_nodes;
@@ -1043,15 +1168,17 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   g.kfu0 = ctx->d_kfu0;
   g.bval64 = bsr64 ? ctx->d_bval64 : nullptr;
   g.bval32 = bsr32 ? ctx->d_bval32 : nullptr;
-  g.bdinv64 = (bsr64 || bsr32) ? ctx->d_bdinv64 : nullptr;
-  g.bdinv32 = bsr32 ? ctx->d_bdinv32 : nullptr;
+  g.bdinv64 = (bsr64 || bsr32 || sym32) ? ctx->d_bdinv64 : nullptr;
+  g.bdinv32 = (bsr32 || sym32) ? ctx->d_bdinv32 : nullptr;
   g.qptr = ctx->d_qptr;
   g.nb = ctx->nbq;
+  g.uval = sym32 ? ctx->d_uval : nullptr;
+  g.uptr = ctx->d_uptr;
   AXIA_TRY(run_gather(ctx, g));
   AXIA_CUDA(ctx, cudaStreamSynchronize(s));
   DevStatus hs;
   AXIA_TRY(read_dev_status(ctx, &hs));
-  ctx->have_csr64 = ctx->have32 = ctx->have_bsr64 = ctx->have_bsr32 = false;
+  ctx->have_csr64 = ctx->have32 = ctx->have_bsr64 = ctx->have_bsr32 = ctx->have_sym32 = false;
   ctx->assembled = false;
   if (hs.first_error != ~0ull) {
     int code = (int)(hs.first_error & 0xff);
@@ -1066,6 +1193,7 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   ctx->have32 = csr32;
   ctx->have_bsr64 = bsr64;
   ctx->have_bsr32 = bsr32;
+  ctx->have_sym32 = sym32;
   ctx->assembled = true;
   ctx->assemble_gen++;
   return AXIA_OK;

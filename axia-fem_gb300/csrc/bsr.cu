@@ -131,6 +131,77 @@ __global__ void __launch_bounds__(PCG_THREADS) bsr_spmv_kernel(BsrMat<V> M, cons
   }
 }
 
+// Block row a of the symmetric form with L lanes:
+//   (y0, y1, y2) = sum_{b >= a} K_ab x_b + sum_{b < a} K_ba^T x_b.
+// Upper blocks go two at a time (20 floats: five aligned float4 loads, kept in
+// L2 for the later rows that read them transposed); a lower block is one
+// 40-byte read (five float2) at the position its row b stored it, normally
+// still in L2 because row b was streamed a few thousand rows earlier.  The
+// first two lower entries of each lane are fetched before the upper loop so
+// their index loads overlap it.  Fixed order: bitwise reproducible.
+template <int L>
+__device__ __forceinline__ void sym_row(int a, int sl, const SymMat& S, const float* x, float& y0, float& y1,
+                                        float& y2) {
+  y0 = y1 = y2 = 0.f;
+  if (a < S.n_nodes) {
+    const int l0 = __ldg(S.lptr + a), l1 = __ldg(S.lptr + a + 1);
+    int2 pre[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int e = l0 + sl + k * L;
+      pre[k] = e < l1 ? __ldcs(S.low + e) : make_int2(-1, 0);
+    }
+    const int u0 = __ldg(S.uptr + a), u1 = __ldg(S.uptr + a + 1);
+    for (int s = u0 + 2 * sl; s < u1; s += 2 * L) {
+      const float4* p = reinterpret_cast<const float4*>(S.uval + 10LL * s);
+      const float4 q0 = __ldcg(p), q1 = __ldcg(p + 1), q2 = __ldcg(p + 2), q3 = __ldcg(p + 3), q4 = __ldcg(p + 4);
+      const int c0 = __float_as_int(q2.y), c1 = __float_as_int(q4.w);
+      const float a0 = x[3 * c0], a1 = x[3 * c0 + 1], a2 = x[3 * c0 + 2];
+      const float b0 = x[3 * c1], b1 = x[3 * c1 + 1], b2 = x[3 * c1 + 2];
+      y0 = fmaf(q0.x, a0, fmaf(q0.y, a1, fmaf(q0.z, a2, y0)));
+      y1 = fmaf(q0.w, a0, fmaf(q1.x, a1, fmaf(q1.y, a2, y1)));
+      y2 = fmaf(q1.z, a0, fmaf(q1.w, a1, fmaf(q2.x, a2, y2)));
+      y0 = fmaf(q2.z, b0, fmaf(q2.w, b1, fmaf(q3.x, b2, y0)));
+      y1 = fmaf(q3.y, b0, fmaf(q3.z, b1, fmaf(q3.w, b2, y1)));
+      y2 = fmaf(q4.x, b0, fmaf(q4.y, b1, fmaf(q4.z, b2, y2)));
+    }
+    auto lower = [&](int2 bt) {
+      const float2* p = reinterpret_cast<const float2*>(S.uval + 10LL * bt.y);
+      const float2 v0 = __ldcg(p), v1 = __ldcg(p + 1), v2 = __ldcg(p + 2), v3 = __ldcg(p + 3), v4 = __ldcg(p + 4);
+      const float b0 = x[3 * bt.x], b1 = x[3 * bt.x + 1], b2 = x[3 * bt.x + 2];
+      // K_ba = [v0.x v0.y v1.x; v1.y v2.x v2.y; v3.x v3.y v4.x], y += K_ba^T x_b
+      y0 = fmaf(v0.x, b0, fmaf(v1.y, b1, fmaf(v3.x, b2, y0)));
+      y1 = fmaf(v0.y, b0, fmaf(v2.x, b1, fmaf(v3.y, b2, y1)));
+      y2 = fmaf(v1.x, b0, fmaf(v2.y, b1, fmaf(v4.x, b2, y2)));
+    };
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+      if (pre[k].x >= 0) lower(pre[k]);
+    for (int e = l0 + sl + 2 * L; e < l1; e += L) lower(__ldcs(S.low + e));
+  }
+  y0 = group_sum<L>(y0);
+  y1 = group_sum<L>(y1);
+  y2 = group_sum<L>(y2);
+}
+
+template <int L>
+__global__ void __launch_bounds__(PCG_THREADS) sym_spmv_kernel(SymMat S, const float* x, float* y) {
+  constexpr int RPW = 32 / L;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  const int gwarp = tid >> 5, nwarps = nth >> 5;
+  const int lane = threadIdx.x & 31, sl = lane % L, grp = lane / L;
+  for (int base = gwarp * RPW; base < S.n_nodes; base += nwarps * RPW) {
+    const int a = base + grp;
+    float y0, y1, y2;
+    sym_row<L>(a, sl, S, x, y0, y1, y2);
+    if (a < S.n_nodes && sl == 0) {
+      y[3 * a] = y0;
+      y[3 * a + 1] = y1;
+      y[3 * a + 2] = y2;
+    }
+  }
+}
+
 template <typename V>
 struct BsrPcgArgs {
   BsrMat<V> M;
@@ -268,7 +339,7 @@ __device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const Coar
   return true;
 }
 
-template <int L32, int V32, int L64, int V64, bool COARSE = false>
+template <int L32, int V32, int L64, int V64, bool COARSE = false, bool SYM = false>
 __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const CoarseArgs& C, const SolveRange& R) {
   const int n0 = R.node0, n1 = R.node1;
   const int i0 = 3 * n0;
@@ -325,7 +396,13 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
       for (int base = n0 + gwarp * RPW; base < n1; base += nwarps * RPW) {
         const int a = base + grp;
         float y0, y1, y2;
-        bsr_row<float, float, V32, L32>(a, sl, M32, P.p32, y0, y1, y2);
+        if constexpr (SYM) {
+          SymMat S = P.S32;
+          S.n_nodes = n1;
+          sym_row<L32>(a, sl, S, P.p32, y0, y1, y2);
+        } else {
+          bsr_row<float, float, V32, L32>(a, sl, M32, P.p32, y0, y1, y2);
+        }
         if (a < n1 && sl == 0) {
           P.q32[3 * a] = y0;
           P.q32[3 * a + 1] = y1;
@@ -446,10 +523,10 @@ __host__ __device__ constexpr int rel_v64() { return V32 >= 4 ? 2 : 1; }
 template <int V32>
 __host__ __device__ constexpr int rel_min_blocks() { return V32 >= 4 ? 2 : 3; }
 
-template <int L32, int V32, bool COARSE = false>
+template <int L32, int V32, bool COARSE = false, bool SYM = false>
 __global__ void __launch_bounds__(PCG_THREADS, rel_min_blocks<V32>()) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
-  const SolveRange R{0, P.M32.n_nodes, blockIdx.x, gridDim.x, P.partials, P.totals, P.bar, P.out};
-  reliable_body<L32, V32, kL64, rel_v64<V32>(), COARSE>(P, P.C, R);
+  const SolveRange R{0, P.M64.n_nodes, blockIdx.x, gridDim.x, P.partials, P.totals, P.bar, P.out};
+  reliable_body<L32, V32, kL64, rel_v64<V32>(), COARSE, SYM>(P, P.C, R);
 }
 
 // Independent systems on disjoint node ranges of one node-block matrix (the
@@ -579,6 +656,18 @@ static BsrMat<V> bsr_mat(const axia_ctx* ctx, const V* val) {
   return BsrMat<V>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, val, (long long)ctx->nbq};
 }
 
+static SymMat sym_mat(const axia_ctx* ctx) {
+  return SymMat{(int)ctx->n_nodes, ctx->d_uptr, ctx->d_uval, ctx->d_lptr, ctx->d_low};
+}
+
+// Lanes per block row of the symmetric form: about one upper pair or lower
+// block per lane and step.
+static int sym_lanes(const axia_ctx* ctx, int requested) {
+  if (requested == 4 || requested == 8 || requested == 16) return requested;
+  const double work = ctx->n_nodes ? (0.5 * (double)ctx->nbu + (double)ctx->nbl) / (double)ctx->n_nodes : 1.0;
+  return work <= 12 ? 4 : (work <= 28 ? 8 : 16);
+}
+
 static int ensure_full_buffers(axia_ctx* ctx, bool mixed) {
   const size_t nd = (size_t)ctx->ndof;
   if (ctx->full_capacity < nd || (mixed && !ctx->d_xf32)) {
@@ -620,15 +709,24 @@ static int launch_bsr_pcg(axia_ctx* ctx, BsrPcgArgs<V>& P, int lanes) {
   }
 }
 
-template <int L32, int V32, bool COARSE>
+template <int L32, int V32, bool COARSE, bool SYM = false>
 static int launch_bsr_rel_t(axia_ctx* ctx, BsrReliableArgs& P) {
-  auto kern = pcg_bsr_reliable_kernel<L32, V32, COARSE>;
+  auto kern = pcg_bsr_reliable_kernel<L32, V32, COARSE, SYM>;
   int grid = 0;
   AXIA_TRY(coop_grid(ctx, (const void*)kern, P.nd, &grid));
   void* params[] = {&P};
   AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params, 0, ctx->stream));
   ctx->launches++;
   return AXIA_OK;
+}
+
+// The symmetric form: lanes per block row only (V32 = 4 keeps the register
+// budget of two blocks per SM).
+static int launch_sym_rel(axia_ctx* ctx, BsrReliableArgs& P, int lanes) {
+  const bool c = P.C.n_sub > 0;
+  if (lanes == 4) return c ? launch_bsr_rel_t<4, 4, true, true>(ctx, P) : launch_bsr_rel_t<4, 4, false, true>(ctx, P);
+  if (lanes == 16) return c ? launch_bsr_rel_t<16, 4, true, true>(ctx, P) : launch_bsr_rel_t<16, 4, false, true>(ctx, P);
+  return c ? launch_bsr_rel_t<8, 4, true, true>(ctx, P) : launch_bsr_rel_t<8, 4, false, true>(ctx, P);
 }
 
 static int launch_bsr_rel(axia_ctx* ctx, BsrReliableArgs& P, RowLayout r) {
@@ -697,7 +795,8 @@ int launch_full_reconstruct(axia_ctx* ctx, double* d_u) {
 int prepare_full_buffers(axia_ctx* ctx) { return ensure_full_buffers(ctx, true); }
 
 BsrReliableArgs make_reliable_args(axia_ctx* ctx, double rtol, double delta, long long max_iter) {
-  return BsrReliableArgs{bsr_mat<float>(ctx, ctx->d_bval32), bsr_mat<double>(ctx, ctx->d_bval64), (int)ctx->ndof,
+  return BsrReliableArgs{bsr_mat<float>(ctx, ctx->d_bval32), sym_mat(ctx), bsr_mat<double>(ctx, ctx->d_bval64),
+                         (int)ctx->ndof,
                          ctx->d_bdinv32, ctx->d_bf, ctx->d_xf, ctx->d_xf32, ctx->d_rf32, ctx->d_pf32, ctx->d_qf32,
                          ctx->d_zf32, ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status,
                          (PcgOut*)ctx->d_out, rtol, delta, max_iter, 2000000000ull};
@@ -718,8 +817,12 @@ static double bsr_residual(axia_ctx* ctx, const double* b, const double* x) {
 
 // Solve on the node-block form: rhs from d_f (full), solution into d_u (full).
 int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_opts* opts, axia_solve_info* info) {
+  const bool sym = opts->matrix_format == AXIA_FORMAT_BSR3_SYM;
   const bool mixed = opts->precision == AXIA_PREC_MIXED;
-  if (!ctx->have_bsr64 || (mixed && !ctx->have_bsr32))
+  if (sym && (!mixed || !ctx->have_bsr64 || !ctx->have_sym32))
+    return set_error(ctx, AXIA_ERR_STATE,
+                     "the symmetric node-block solve is mixed precision on AXIA_ASM_BSR64 | AXIA_ASM_SYM32");
+  if (!sym && (!ctx->have_bsr64 || (mixed && !ctx->have_bsr32)))
     return set_error(ctx, AXIA_ERR_STATE, "node-block solve needs axia_gpu_assemble_ex with the BSR flags");
   if (opts->preconditioner != AXIA_PRECOND_JACOBI && (opts->preconditioner != AXIA_PRECOND_COARSE || !mixed))
     return set_error(ctx, AXIA_ERR_INVALID_ARG, "the coarse preconditioner needs the mixed node-block solve");
@@ -742,7 +845,7 @@ int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_op
     AXIA_TRY(timed_launch(ctx, info, [&] { return launch_bsr_pcg<double>(ctx, P, lanes); }));
   } else {
     const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.1;
-    BsrReliableArgs P{bsr_mat<float>(ctx, ctx->d_bval32), bsr_mat<double>(ctx, ctx->d_bval64), (int)nd,
+    BsrReliableArgs P{bsr_mat<float>(ctx, ctx->d_bval32), sym_mat(ctx), bsr_mat<double>(ctx, ctx->d_bval64), (int)nd,
                       ctx->d_bdinv32, ctx->d_bf, ctx->d_xf, ctx->d_xf32, ctx->d_rf32, ctx->d_pf32, ctx->d_qf32,
                       ctx->d_zf32, ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (PcgOut*)ctx->d_out, opts->rtol,
                       delta, max_iter, limit_ns};
@@ -751,7 +854,10 @@ int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_op
       AXIA_TRY(reset_dev_status(ctx));
       AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
     }
-    AXIA_TRY(timed_launch(ctx, info, [&] { return launch_bsr_rel(ctx, P, lay); }));
+    if (sym)
+      AXIA_TRY(timed_launch(ctx, info, [&] { return launch_sym_rel(ctx, P, sym_lanes(ctx, opts->spmv_lanes)); }));
+    else
+      AXIA_TRY(timed_launch(ctx, info, [&] { return launch_bsr_rel(ctx, P, lay); }));
   }
   AXIA_TRY(read_out(ctx, &o));
   info->iters = o.iters;
@@ -785,6 +891,20 @@ int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_
           <<<grid_max, PCG_THREADS, 0, ctx->stream>>>(M, (const double*)x, (double*)y);
       return 0;
     });
+  }
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  return AXIA_OK;
+}
+
+int sym_spmv_device(axia_ctx* ctx, const float* x, float* y, int lanes_req) {
+  if (!ctx->have_sym32) return set_error(ctx, AXIA_ERR_STATE, "symmetric node-block matrix not assembled");
+  const int grid = ctx->sm_count * 4;
+  const SymMat S = sym_mat(ctx);
+  switch (sym_lanes(ctx, lanes_req)) {
+    case 4: sym_spmv_kernel<4><<<grid, PCG_THREADS, 0, ctx->stream>>>(S, x, y); break;
+    case 16: sym_spmv_kernel<16><<<grid, PCG_THREADS, 0, ctx->stream>>>(S, x, y); break;
+    default: sym_spmv_kernel<8><<<grid, PCG_THREADS, 0, ctx->stream>>>(S, x, y); break;
   }
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());

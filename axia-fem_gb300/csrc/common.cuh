@@ -322,6 +322,19 @@ struct axia_ctx {
   float* d_bdinv32 = nullptr;      // [ndof]
   bool have_bsr64 = false, have_bsr32 = false;
 
+  // symmetric node-block form of the FP32 matrix (AXIA_ASM_SYM32): every block
+  // K_ab with b >= a stored once, in row a, as 10 floats (the 9 values row-major
+  // and the block column as int bits); rows padded to an even block count (pad:
+  // zero values, column = the row's node) so two blocks are five aligned float4.
+  // The blocks with b < a are read through row a's lower list: (b, position of
+  // K_ba in row b), K_ab = K_ba^T.
+  int32_t* d_uptr = nullptr;       // [n_nodes+1] upper-block row starts (even)
+  float* d_uval = nullptr;         // [nbu][10]
+  int32_t* d_lptr = nullptr;       // [n_nodes+1] lower-list row starts
+  int2* d_low = nullptr;           // [nbl] (b, position)
+  int64_t nbu = 0, nbl = 0;
+  bool have_sym32 = false;
+
   // element stiffness scratch
   double* d_ke = nullptr;
   size_t ke_elems = 0;

@@ -92,6 +92,17 @@ struct BsrMat {
   long long nb;
 };
 
+// Symmetric FP32 node-block form (axia_ctx::d_uval ...): upper blocks of row a
+// at [uptr[a], uptr[a+1]) as 10 floats each (9 values, column bits), lower
+// neighbours of row a at [lptr[a], lptr[a+1]) as (b, position of K_ba).
+struct SymMat {
+  int n_nodes;
+  const int* uptr;
+  const float* uval;
+  const int* lptr;
+  const int2* low;
+};
+
 // one system of a multi-mesh solve: its block rows and its blocks
 struct MeshGroup {
   int node0, node1;   // block rows [node0, node1)
@@ -133,6 +144,7 @@ struct CoarseArgs {
 
 struct BsrReliableArgs {
   BsrMat<float> M32;
+  SymMat S32;        // the FP32 matrix in symmetric storage (kernels instantiated with SYM)
   BsrMat<double> M64;
   int nd;
   const float* dinv32;

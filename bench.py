@@ -141,6 +141,21 @@ def bsr_pcg_iter_bytes(nblocks, n_nodes, vbytes):
     return (9 * vbytes + 4) * nblocks + 4 * (n_nodes + 1) + 2 * vbytes * nd + 11 * vbytes * nd
 
 
+def sym_spmv_bytes(nbu, nbl, n_nodes):
+    """Algorithmic bytes of y = K x in the symmetric node-block form: each stored
+    block (9 FP32 values + int32 column, pad blocks included) once, one
+    (row, position) pair per lower entry, both row-pointer arrays, x and y once
+    (the transposed re-reads of stored blocks are not counted: they are the
+    same bytes)."""
+    return 40 * nbu + 8 * nbl + 8 * (n_nodes + 1) + 2 * 4 * 3 * n_nodes
+
+
+def sym_pcg_iter_bytes(nbu, nbl, n_nodes):
+    """One CG iteration with the symmetric FP32 matrix (full-DOF vectors)."""
+    nd = 3 * n_nodes
+    return 40 * nbu + 8 * nbl + 8 * (n_nodes + 1) + 2 * 4 * nd + 11 * 4 * nd
+
+
 def coarse_iter_bytes(n_nodes, n_coarse):
     """Extra algorithmic bytes of one two-level CG iteration: the per-node
     subdomain geometry (16 B) and node order (4 B) once, the dense coarse
@@ -678,8 +693,10 @@ def main():
     mixed_csr_kw = dict(precision=L.PREC_MIXED, refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta,
                         spmv_lanes=args.lanes32csr, matrix_format=L.FORMAT_CSR)
     coarse_kw = dict(mixed_kw, preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
+    sym_kw = dict(coarse_kw, matrix_format=L.FORMAT_BSR3_SYM, spmv_lanes=0)
     umc = torch.empty_like(f_dev)
     uco = torch.empty_like(f_dev)
+    ucs = torch.empty_like(f_dev)
     # layout of the FP32 inner loop, picked by the library's autotuner (untimed)
     ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
     tuned = {"lanes": None, "vec": None}
@@ -691,6 +708,7 @@ def main():
         msmx, infmx, lamx = timed(L.ASM_BSR64 | L.ASM_BSR32, mixed_kw, umx)
         msmc, infmc, lamc = timed(L.ASM_CSR64 | L.ASM_CSR32, mixed_csr_kw, umc)
         msco, infco, laco = timed(L.ASM_BSR64 | L.ASM_BSR32, coarse_kw, uco)
+        mscs, infcs, lacs = timed(L.ASM_BSR64 | L.ASM_SYM32, sym_kw, ucs)
     clocks = clk.summary()
     n_sub, n_coarse = ctx.coarse_size()
 
@@ -707,14 +725,19 @@ def main():
     xf32 = xf64.float()
     yf32 = torch.empty_like(xf32)
     nblocks = ctx.n_blocks()
+    nbu, nbl = ctx.sym_blocks()
     cases = (("csr_fp64", ctx.spmv_device, L.PREC_FP64, x64, y64, spmv_bytes(nnz, n, 8), args.lanes64),
              ("csr_fp32", ctx.spmv_device, L.PREC_MIXED, x32, y32, spmv_bytes(nnz, n, 4), args.lanes32csr),
              ("bsr_fp64", ctx.bsr_spmv_device, L.PREC_FP64, xf64, yf64, bsr_spmv_bytes(nblocks, model.n_nodes, 8), 0),
              ("bsr_fp32", ctx.bsr_spmv_device, L.PREC_MIXED, xf32, yf32, bsr_spmv_bytes(nblocks, model.n_nodes, 4),
-              args.lanes32))
+              args.lanes32),
+             ("sym_fp32", lambda prec, x, y, lanes: ctx.sym_spmv_device(x, y, lanes), L.PREC_MIXED, xf32, yf32,
+              sym_spmv_bytes(nbu, nbl, model.n_nodes), 0))
     for name, fn, prec, x, y, nbytes, lanes in cases:
         if name.startswith("csr"):
             ctx.assemble_ex(L.ASM_CSR64 | L.ASM_CSR32)
+        elif name.startswith("sym"):
+            ctx.assemble_ex(L.ASM_BSR64 | L.ASM_SYM32)
         else:
             ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
         with torch.cuda.stream(stream):
@@ -760,6 +783,7 @@ def main():
     rel_mx = float(np.linalg.norm(umx.cpu().numpy() - u64h) / np.linalg.norm(u64h))
     rel_mc = float(np.linalg.norm(umc.cpu().numpy() - u64h) / np.linalg.norm(u64h))
     rel_co = float(np.linalg.norm(uco.cpu().numpy() - u64h) / np.linalg.norm(u64h))
+    rel_cs = float(np.linalg.norm(ucs.cpu().numpy() - u64h) / np.linalg.norm(u64h))
     ctx.assemble_ex(L.ASM_CSR64)
     utight = torch.empty_like(f_dev)
     with torch.cuda.stream(stream):
@@ -770,13 +794,21 @@ def main():
              "rel_err_fp64": float(np.linalg.norm(u64h - uth) / np.linalg.norm(uth)),
              "rel_err_mixed": float(np.linalg.norm(umx.cpu().numpy() - uth) / np.linalg.norm(uth)),
              "rel_err_mixed_csr": float(np.linalg.norm(umc.cpu().numpy() - uth) / np.linalg.norm(uth)),
-             "rel_err_mixed_coarse": float(np.linalg.norm(uco.cpu().numpy() - uth) / np.linalg.norm(uth))}
+             "rel_err_mixed_coarse": float(np.linalg.norm(uco.cpu().numpy() - uth) / np.linalg.norm(uth)),
+             "rel_err_mixed_coarse_sym": float(np.linalg.norm(ucs.cpu().numpy() - uth) / np.linalg.norm(uth))}
 
     # full-size residual of every solution under the oracle's own stiffness (host, untimed)
     oracle_check = oracle_residuals(model, {"fp64": u64h, "mixed": umx.cpu().numpy(), "mixed_csr": umc.cpu().numpy(),
-                                            "mixed_coarse": uco.cpu().numpy(), "fp64_rtol_1e-12": uth}, f_host)
+                                            "mixed_coarse": uco.cpu().numpy(), "mixed_coarse_sym": ucs.cpu().numpy(),
+                                            "fp64_rtol_1e-12": uth}, f_host)
 
-    last64, lastmx, lastmc, lastco = inf64[-1], infmx[-1], infmc[-1], infco[-1]
+    last64, lastmx, lastmc, lastco, lastcs = inf64[-1], infmx[-1], infmc[-1], infco[-1], infcs[-1]
+    itcs = statistics.mean(i["iters"] for i in infcs)
+    kcs_ms = statistics.mean(i["ms_pcg_kernel"] for i in infcs)
+    updcs = statistics.mean(i["outer_iters"] for i in infcs)
+    bytescs = ((sym_pcg_iter_bytes(nbu, nbl, model.n_nodes) + coarse_iter_bytes(model.n_nodes, n_coarse)) * itcs +
+               bsr_spmv_bytes(nblocks, model.n_nodes, 8) * updcs)
+    achcs = bytescs / (kcs_ms * 1e-3) / 1e9
     mdofs_co = n / (msco * 1e-3) / 1e6 * world
     mdofs = n / (msmx * 1e-3) / 1e6 * world
     mdofs64 = n / (ms64 * 1e-3) / 1e6 * world
@@ -882,6 +914,14 @@ def main():
                          "ms_pcg_kernel": lastco["ms_pcg_kernel"],
                          "ms_coarse_setup": lastco["ms_solve"] - lastco["ms_pcg_kernel"],
                          "true_rel_residual": lastco["true_residual"] / lastco["bnorm"], "rel_err_vs_fp64": rel_co},
+        "mixed_coarse_sym": {"value": n / (mscs * 1e-3) / 1e6 * world, "ms_per_step": mscs,
+                             "inner_iters": lastcs["iters"], "reliable_updates": lastcs["outer_iters"],
+                             "format": "FP32 symmetric node blocks (upper blocks stored once) + FP64 node blocks",
+                             "ms_assemble": lastcs["ms_assemble"], "ms_solve": lastcs["ms_solve"],
+                             "ms_pcg_kernel": lastcs["ms_pcg_kernel"],
+                             "true_rel_residual": lastcs["true_residual"] / lastcs["bnorm"], "rel_err_vs_fp64": rel_cs,
+                             "roofline": {"achieved": achcs, "frac": achcs / hbm, "bytes_per_launch": bytescs,
+                                          "ms_per_launch": kcs_ms}},
         "mixed": {"value": mdofs, "ms_per_step": msmx, "inner_iters": lastmx["iters"],
                   "reliable_updates": lastmx["outer_iters"], "format": "3x3 node blocks, int32 block columns",
                   "ms_assemble": lastmx["ms_assemble"], "ms_solve": lastmx["ms_solve"],
@@ -921,7 +961,7 @@ def main():
                                    "ms_per_launch": kmc_ms, "bytes_per_launch": bytesmc},
         "oracle_check": oracle_check,
         "same_sample": same,
-        "gpu_launches": int(la64 + lamx + lamc + laco),
+        "gpu_launches": int(la64 + lamx + lamc + laco + lacs),
         "clocks": clocks,
         "e2e": e2e,
         "cpu_baseline": cpu,

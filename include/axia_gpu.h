@@ -68,12 +68,16 @@ typedef enum axia_assemble_flags {
   AXIA_ASM_CSR64 = 1,   /* K_ff in CSR, FP64 values (the reference's Csr, linalg.rs:3-8) */
   AXIA_ASM_CSR32 = 2,   /* FP32 copy of the CSR values */
   AXIA_ASM_BSR64 = 4,   /* full-DOF node-block (3x3) form, FP64 */
-  AXIA_ASM_BSR32 = 8    /* full-DOF node-block (3x3) form, FP32 */
+  AXIA_ASM_BSR32 = 8,   /* full-DOF node-block (3x3) form, FP32 */
+  AXIA_ASM_SYM32 = 16   /* the FP32 node-block form in symmetric storage: each block K_ab, b >= a,
+                           stored once (about half the bytes of AXIA_ASM_BSR32) */
 } axia_assemble_flags;
 
 typedef enum axia_matrix_format {
   AXIA_FORMAT_CSR = 0,  /* solve on K_ff in CSR */
-  AXIA_FORMAT_BSR3 = 1  /* solve on the node-block form (prescribed DOFs as unit rows) */
+  AXIA_FORMAT_BSR3 = 1,     /* solve on the node-block form (prescribed DOFs as unit rows) */
+  AXIA_FORMAT_BSR3_SYM = 2  /* the same, mixed precision, with the FP32 inner matrix in symmetric
+                               storage (AXIA_ASM_SYM32 + AXIA_ASM_BSR64); single system only */
 } axia_matrix_format;
 
 typedef enum axia_refine_mode {
@@ -263,6 +267,17 @@ AXIA_API int32_t axia_gpu_spmv_device(axia_ctx* ctx, int32_t precision, const vo
  * and blocks per lane load (vec) as in axia_solve_opts, 0 = automatic. */
 AXIA_API int32_t axia_gpu_bsr_spmv_device(axia_ctx* ctx, int32_t precision, const void* x_dev, void* y_dev,
                                           int32_t lanes, int32_t vec);
+
+/* y = K x with the FP32 matrix in symmetric storage (AXIA_ASM_SYM32; float x,
+ * y of 3*n_nodes entries): each row adds its stored blocks K_ab (b >= a) and
+ * the transposes of the blocks K_ba (b < a) that the earlier rows store.
+ * lanes per block row: 4, 8, 16 or 0 (automatic).  No reference counterpart
+ * (the reference stores K in full CSR, linalg.rs:3-8); same product. */
+AXIA_API int32_t axia_gpu_sym_spmv_device(axia_ctx* ctx, const float* x_dev, float* y_dev, int32_t lanes);
+
+/* Stored blocks of the symmetric form (pad blocks included; -1 without a
+ * context) and, in *lower_entries, its lower-list entries. */
+AXIA_API int64_t axia_gpu_sym_blocks(const axia_ctx* ctx, int64_t* lower_entries);
 
 /* Number of 3x3 node blocks of the node-block form (node adjacency entries). */
 AXIA_API int64_t axia_gpu_node_blocks(const axia_ctx* ctx);
