@@ -113,6 +113,8 @@ SIGNATURES = [
                                             C.POINTER(SolveInfo)]),
     ("axia_gpu_autotune", C.c_int32, [_P, C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_double)]),
+    ("axia_gpu_autotune_batched", C.c_int32, [_P, C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                              C.POINTER(C.c_double)]),
     ("axia_dofmap_build", C.c_int32, [C.c_int64, C.c_int64, _P, _P, C.c_int64, _P, _P, _P, _P, _P,
                                       C.POINTER(C.c_void_p)]),
     ("axia_dofmap_n_ind", C.c_int64, [_P]),

@@ -315,6 +315,15 @@ class GpuContext:
         self._check(self.lib.axia_gpu_autotune(self.h, path, C.byref(lanes), C.byref(vec), C.byref(us)), "autotune")
         return lanes.value, vec.value, us.value
 
+    def autotune_batched(self, cache_path=None):
+        """Time the tiles of the batched load-case kernel on the assembled mesh and keep the
+        fastest for later batched solves; returns (cases_per_lane, blocks_per_step, us_per_iter)."""
+        tc, tu, us = C.c_int32(), C.c_int32(), C.c_double()
+        path = None if cache_path is None else os.fsencode(cache_path)
+        self._check(self.lib.axia_gpu_autotune_batched(self.h, path, C.byref(tc), C.byref(tu), C.byref(us)),
+                    "autotune_batched")
+        return tc.value, tu.value, us.value
+
     def solve_kff(self, n, trips, rhs, **kw):
         """solve_kff on the GPU (linalg.rs:311 with PCG): trips = (i, j, v) arrays in the
         caller's order; returns (x, info).  Replaces any mesh set up on the context."""

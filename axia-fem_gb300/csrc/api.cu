@@ -29,6 +29,7 @@ int true_residual(axia_ctx* ctx, double* out);
 int prepare_solve(axia_ctx* ctx, bool mixed);
 int spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req);
 int bsr_autotune(axia_ctx* ctx, const char* cache_path, int* lanes_out, int* vec_out, double* us_out);
+int batch_autotune(axia_ctx* ctx, const char* cache_path, int* tc_out, int* tu_out, double* us_out);
 int64_t dofmap_n_full(const axia_dofmap* m);
 int raw_system_from_triplets(axia_ctx* ctx, int64_t n, int64_t nt, const int64_t* h_i, const int64_t* h_j,
                              const double* h_v, bool fp32);
@@ -541,6 +542,19 @@ int32_t axia_gpu_autotune(axia_ctx* ctx, const char* cache_path, int32_t* lanes,
   AXIA_TRY(bsr_autotune(ctx, cache_path, &l, &v, us_per_iter));
   *lanes = l;
   *vec = v;
+  return AXIA_OK;
+}
+
+int32_t axia_gpu_autotune_batched(axia_ctx* ctx, const char* cache_path, int32_t* cases_per_lane,
+                                  int32_t* blocks_per_step, double* us_per_iter) {
+  if (!ctx || !cases_per_lane || !blocks_per_step) return AXIA_ERR_INVALID_ARG;
+  AXIA_TRY(use_device(ctx));
+  int tc = 0, tu = 0;
+  double us = 0.0;
+  AXIA_TRY(batch_autotune(ctx, cache_path, &tc, &tu, &us));
+  *cases_per_lane = tc;
+  *blocks_per_step = tu;
+  if (us_per_iter) *us_per_iter = us;
   return AXIA_OK;
 }
 

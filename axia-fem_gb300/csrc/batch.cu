@@ -12,6 +12,9 @@
 // A converged column is frozen (alpha = beta = 0).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
 
 #include "coarse.cuh"
 
@@ -46,48 +49,12 @@ __device__ __forceinline__ void st4(double* p, const double v[4]) {
   *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
 }
 
-// Y[3a+i][4cl..4cl+3] for block row a; valid in the lanes of group 0 after the call.
-template <typename V>
-__device__ __forceinline__ void bsr_row_multi(int a, int lane, const BsrMatM<V>& M, const V* X, V y[3][CPL]) {
-  const int cl = lane % LPG, grp = lane / LPG;
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int c = 0; c < CPL; ++c) y[i][c] = V(0);
-  const int beg = __ldg(M.adj_ptr + a), end = __ldg(M.adj_ptr + a + 1);
-  // the next block's column is loaded one step ahead, so a step waits for one
-  // memory round trip (values and vector rows) instead of two in a row
-  int b = beg + grp < end ? ld_stream(M.adj + beg + grp) : 0;
-  for (int s = beg + grp; s < end; s += 32 / LPG) {
-    const int b_next = s + 32 / LPG < end ? ld_stream(M.adj + s + 32 / LPG) : 0;
-    V v[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) v[k] = ld_stream(M.val + (long long)k * M.nb + s);
-    V x[3][CPL];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) ld4(X + (size_t)(3 * b + j) * NR + CPL * cl, x[j]);
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int c = 0; c < CPL; ++c)
-        y[i][c] = fma(v[3 * i], x[0][c], fma(v[3 * i + 1], x[1][c], fma(v[3 * i + 2], x[2][c], y[i][c])));
-    b = b_next;
-  }
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int c = 0; c < CPL; ++c) {
-      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 8);
-      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 16);
-    }
-}
-
 // Rows of at most STAGE_B blocks (C3D8 rows have up to 27) are staged: while a
 // warp computes one block row, the matrix values and block columns of its
 // next row are copied to shared memory asynchronously (cp.async, 4 bytes per
 // lane and array), so a step of the row loop waits only for the vector rows
 // (mostly L1 / L2 hits), not for the matrix stream from DRAM.  Longer rows
-// take bsr_row_multi.
+// read their values from the matrix planes.
 constexpr int STAGE_B = 28;
 struct RowStage {
   float v[9][STAGE_B];
@@ -119,35 +86,87 @@ __device__ __forceinline__ void stage_row(int a, int lane, const BsrMatM<float>&
   cp_async_commit();
 }
 
-// bsr_row_multi for a staged row (len <= STAGE_B blocks, copies complete).
-__device__ __forceinline__ void bsr_row_multi_staged(int len, int lane, const RowStage* st, const float* X,
-                                                     float y[3][CPL]) {
-  const int cl = lane % LPG, grp = lane / LPG;
+// ---------------------------------------------------------------------------
+// Tiled row product for the FP32 SpMV, the shape picked by the batch
+// autotuner: TC load cases per lane (1, 2 or 4: a group of 32 / TC lanes
+// covers the 32 cases, a warp holds TC groups that take interleaved blocks of
+// the row) and TU blocks per group and step, whose vector rows (3 x TC floats
+// per lane and block) are all requested before any is used, so a lane keeps
+// 3 TU loads in flight instead of waiting for one block at a time.  The
+// result for cases TC cl .. TC cl + TC - 1 is valid in the lanes of group 0
+// (lane < 32 / TC) after the call.
+// ---------------------------------------------------------------------------
+template <int TC>
+__device__ __forceinline__ void ldc(const float* p, float (&v)[TC]) {
+  if constexpr (TC == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+  } else if constexpr (TC == 2) {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    v[0] = t.x, v[1] = t.y;
+  } else {
+    v[0] = *p;
+  }
+}
+
+template <int TC>
+__device__ __forceinline__ void stc(float* p, const float (&v)[TC]) {
+  if constexpr (TC == 4)
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  else if constexpr (TC == 2)
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+  else
+    *p = v[0];
+}
+
+// values of block s: from the row's staging (staged) or the matrix planes
+template <int TC, int TU, bool STAGED>
+__device__ __forceinline__ void row_tile(int a, int len, int lane, const RowStage* st, const BsrMatM<float>& M,
+                                         const float* X, float (&y)[3][TC]) {
+  constexpr int LG = NR / TC, G = 32 / LG;
+  const int cl = lane % LG, grp = lane / LG;
+  const int beg = STAGED ? 0 : __ldg(M.adj_ptr + a);
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int c = 0; c < CPL; ++c) y[i][c] = 0.f;
-  for (int s = grp; s < len; s += 32 / LPG) {
-    const int b = st->adj[s];
-    float x[3][CPL];
+    for (int c = 0; c < TC; ++c) y[i][c] = 0.f;
+  for (int s0 = grp; s0 < len; s0 += G * TU) {
+    float x[TU][3][TC];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) ld4(X + (size_t)(3 * b + j) * NR + CPL * cl, x[j]);
-    float v[9];
+    for (int u = 0; u < TU; ++u) {
+      const int s = s0 + u * G;
+      if (s < len) {
+        const int b = STAGED ? st->adj[s] : ld_stream(M.adj + beg + s);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) v[k] = st->v[k][s];
+        for (int j = 0; j < 3; ++j) ldc<TC>(X + (size_t)(3 * b + j) * NR + TC * cl, x[u][j]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+          for (int c = 0; c < TC; ++c) x[u][j][c] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < TU; ++u) {
+      const int s = s0 + u * G;
+      if (s < len) {
+        float v[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) v[k] = STAGED ? st->v[k][s] : ld_stream(M.val + (long long)k * M.nb + beg + s);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int c = 0; c < TC; ++c)
+            y[i][c] = fmaf(v[3 * i], x[u][0][c], fmaf(v[3 * i + 1], x[u][1][c], fmaf(v[3 * i + 2], x[u][2][c], y[i][c])));
+      }
+    }
+  }
+#pragma unroll
+  for (int o = LG; o < 32; o <<= 1)
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int c = 0; c < CPL; ++c)
-        y[i][c] = fmaf(v[3 * i], x[0][c], fmaf(v[3 * i + 1], x[1][c], fmaf(v[3 * i + 2], x[2][c], y[i][c])));
-  }
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int c = 0; c < CPL; ++c) {
-      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 8);
-      y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], 16);
-    }
+      for (int c = 0; c < TC; ++c) y[i][c] += __shfl_xor_sync(0xffffffffu, y[i][c], o);
 }
 
 // Y[3a+i][4 cl + 2 h + c], c = 0, 1: two of the lane's four load cases in FP64.
@@ -189,21 +208,23 @@ __device__ __forceinline__ void bsr_row_multi_half(int a, int lane, const BsrMat
 }
 
 // Per-column partial sums of this block: v[c] is this thread's contribution
-// to column 4*(tid%8)+c.  Written to partials[(slot0 + col) * G + block].
-template <typename A>
-__device__ __forceinline__ void block_partials_cols(const A v[CPL], double* partials, int slot0) {
+// to column TC*(tid % (32/TC))+c (TC = 4: the float4 layout of the vector
+// phases).  Written to partials[(slot0 + col) * G + block].
+template <typename A, int TC = CPL>
+__device__ __forceinline__ void block_partials_cols(const A (&v)[TC], double* partials, int slot0) {
+  constexpr int LG = NR / TC;
   __shared__ double s_cols[32][NR];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  double t[CPL];
+  double t[TC];
 #pragma unroll
-  for (int c = 0; c < CPL; ++c) {
+  for (int c = 0; c < TC; ++c) {
     t[c] = (double)v[c];
-    t[c] += __shfl_xor_sync(0xffffffffu, t[c], 8);
-    t[c] += __shfl_xor_sync(0xffffffffu, t[c], 16);
-  }
-  if (lane < LPG) {
 #pragma unroll
-    for (int c = 0; c < CPL; ++c) s_cols[warp][CPL * lane + c] = t[c];
+    for (int o = LG; o < 32; o <<= 1) t[c] += __shfl_xor_sync(0xffffffffu, t[c], o);
+  }
+  if (lane < LG) {
+#pragma unroll
+    for (int c = 0; c < TC; ++c) s_cols[warp][TC * lane + c] = t[c];
   }
   __syncthreads();
   if (threadIdx.x < NR) {
@@ -420,7 +441,7 @@ __device__ __forceinline__ bool coarse_step_m(const MultiArgs& P, int gwarp, int
   return grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, SL_A, NR);
 }
 
-template <bool COARSE>
+template <bool COARSE, int TC, int TU>
 __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs P) {
   extern __shared__ RowStage s_stage[];  // STAGE_BYTES
   __shared__ double s_rz[NR], s_bnorm[NR], s_rmax[NR], s_res[NR];
@@ -494,7 +515,9 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
     if (!any) break;
     iters = it + 1;
     // Q = K P (FP32) and per-column p.q
-    float pq_p[CPL] = {0, 0, 0, 0};
+    float pq_p[TC];
+#pragma unroll
+    for (int c = 0; c < TC; ++c) pq_p[c] = 0.f;
     RowStage* const stg = s_stage + 2 * (threadIdx.x >> 5);
     stage_row(gwarp, lane, P.M32, stg);
     int kb = 0;
@@ -502,28 +525,28 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
       stage_row(a + nwarps, lane, P.M32, stg + (kb ^ 1));
       cp_async_wait<1>();  // this row's copies (all but the group just opened)
       __syncwarp();
-      float y[3][CPL];
+      float y[3][TC];
       const int len = __ldg(P.M32.adj_ptr + a + 1) - __ldg(P.M32.adj_ptr + a);
       if (len <= STAGE_B)
-        bsr_row_multi_staged(len, lane, stg + kb, P.P32, y);
+        row_tile<TC, TU, true>(a, len, lane, stg + kb, P.M32, P.P32, y);
       else
-        bsr_row_multi<float>(a, lane, P.M32, P.P32, y);
+        row_tile<TC, TU, false>(a, len, lane, stg + kb, P.M32, P.P32, y);
       __syncwarp();  // every lane is done with stg[kb] before it is refilled
-      if (lane < LPG) {
+      if (lane < NR / TC) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const size_t off = (size_t)(3 * a + i) * NR + CPL * lane;
-          st4(P.Q32 + off, y[i]);
-          float p[CPL];
-          ld4(P.P32 + off, p);
+          const size_t off = (size_t)(3 * a + i) * NR + TC * lane;
+          float p[TC];
+          ldc<TC>(P.P32 + off, p);
+          stc<TC>(P.Q32 + off, y[i]);
 #pragma unroll
-          for (int c = 0; c < CPL; ++c) pq_p[c] = fmaf(p[c], y[i][c], pq_p[c]);
+          for (int c = 0; c < TC; ++c) pq_p[c] = fmaf(p[c], y[i][c], pq_p[c]);
         }
       }
     }
     cp_async_wait<0>();  // the last (empty or unused) group
-    // lanes 0..7 hold column quads 0..7 of their warp: same mapping as tid % 8
-    block_partials_cols<float>(pq_p, P.partials, SL_A);
+    // lanes 0 .. 32/TC - 1 hold the columns TC lane .. TC lane + TC - 1 of their warp
+    block_partials_cols<float, TC>(pq_p, P.partials, SL_A);
     if (!grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, SL_A, NR)) return;
     if (threadIdx.x < NR) {
       const int c = threadIdx.x;
@@ -698,15 +721,35 @@ __global__ void k_batch_out(int64_t nd, int nrhs, const int32_t* ind_of, const d
   }
 }
 
-}  // namespace
+// Tile shapes the batched kernel is instantiated for: (load cases per lane,
+// blocks per group and step).
+struct BatchTile {
+  int tc, tu;
+};
+// ((4, 2) is left out: it spills about 100 bytes of registers with the coarse space.)
+constexpr BatchTile kBatchTiles[] = {{4, 1}, {2, 2}, {2, 4}, {1, 4}, {1, 8}};
+constexpr BatchTile kBatchDefault = {2, 4};
 
-// Solves nrhs load cases (F, U: [nrhs][nd] device arrays) 32 at a time.
-int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const axia_solve_opts* opts,
-                axia_solve_info* info, double* rel_res) {
-  if (!ctx->have_bsr64 || !ctx->have_bsr32)
-    return set_error(ctx, AXIA_ERR_STATE, "batched solve needs the node-block forms (AXIA_ASM_BSR64 | AXIA_ASM_BSR32)");
-  const int64_t nd = ctx->ndof;
-  const size_t blk = (size_t)nd * NR;
+template <bool COARSE>
+const void* batch_kernel(BatchTile t) {
+  switch (t.tc * 100 + t.tu) {
+    case 401: return (const void*)pcg_bsr_multi_kernel<COARSE, 4, 1>;
+    case 202: return (const void*)pcg_bsr_multi_kernel<COARSE, 2, 2>;
+    case 204: return (const void*)pcg_bsr_multi_kernel<COARSE, 2, 4>;
+    case 104: return (const void*)pcg_bsr_multi_kernel<COARSE, 1, 4>;
+    case 108: return (const void*)pcg_bsr_multi_kernel<COARSE, 1, 8>;
+    default: return nullptr;
+  }
+}
+
+bool valid_tile(int tc, int tu) {
+  for (const BatchTile& t : kBatchTiles)
+    if (t.tc == tc && t.tu == tu) return true;
+  return false;
+}
+
+int ensure_batch_buffers(axia_ctx* ctx) {
+  const size_t blk = (size_t)ctx->ndof * NR;
   if (ctx->batch_capacity < blk) {
     AXIA_TRY(dev_alloc(ctx, &ctx->d_mB, blk));
     AXIA_TRY(dev_alloc(ctx, &ctx->d_mX, blk));
@@ -721,6 +764,161 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
     AXIA_TRY(dev_alloc(ctx, &o, 1));
     ctx->d_mout = o;
   }
+  return AXIA_OK;
+}
+
+// Grid of the cooperative launch of kern (its occupancy with the staging buffers).
+int batch_grid(axia_ctx* ctx, const void* kern, int* grid) {
+  // static + staging shared memory is above the 48 KB a block gets without opting in
+  AXIA_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STAGE_BYTES));
+  AXIA_TRY(coop_grid(ctx, kern, (int)std::min<int64_t>(ctx->ndof, INT32_MAX), grid, STAGE_BYTES));
+  if ((size_t)*grid * 2 * NR > ctx->partial_slots) *grid = (int)(ctx->partial_slots / (2 * NR));
+  return AXIA_OK;
+}
+
+MultiArgs multi_args(axia_ctx* ctx, double rtol, double delta, long long max_iter, const CoarseArgs& cargs) {
+  return MultiArgs{BsrMatM<float>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval32, (long long)ctx->nbq},
+                   BsrMatM<double>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq},
+                   (int)ctx->ndof, ctx->d_bdinv32, ctx->d_mB, ctx->d_mX, ctx->d_mX32, ctx->d_mR32, ctx->d_mP32,
+                   ctx->d_mQ32, ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (MultiOut*)ctx->d_mout,
+                   rtol, delta, max_iter, 2000000000ull, cargs};
+}
+
+int launch_batch(axia_ctx* ctx, const void* kern, int grid, MultiArgs& P) {
+  void* params[] = {&P};
+  AXIA_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(PCG_THREADS), params, STAGE_BYTES, ctx->stream));
+  ctx->launches++;
+  return AXIA_OK;
+}
+
+// B[d][c] = (1 + c / 32) on free DOFs: the autotuner's load (every column busy)
+__global__ void k_batch_tune_rhs(int64_t nd, const int32_t* ind_of, double* B) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nd * NR; t += (int64_t)gridDim.x * blockDim.x)
+    B[t] = ind_of[t / NR] >= 0 ? 1.0 + (double)(t % NR) / NR : 0.0;
+}
+
+std::string batch_tune_key(const axia_ctx* ctx) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, ctx->device);
+  const double rb = ctx->n_nodes ? (double)ctx->nbq / (double)ctx->n_nodes : 0.0;
+  int bucket = 0;
+  for (int64_t n = ctx->n_nodes; n > 1; n >>= 1) ++bucket;
+  std::string name(prop.name);
+  for (char& c : name)
+    if (c == '"' || c == '\\') c = '_';
+  return name + "|batch32|nn=" + std::to_string(ctx->nn) + "|r=" + std::to_string(ctx->reduced) +
+         "|rowblocks=" + std::to_string((int)std::lround(rb)) + "|log2nodes=" + std::to_string(bucket);
+}
+
+bool batch_cache_lookup(const char* path, const std::string& key, int* tc, int* tu) {
+  FILE* fh = path ? std::fopen(path, "r") : nullptr;
+  if (!fh) return false;
+  char line[1024];
+  const std::string want = "\"key\": \"" + key + "\"";
+  bool found = false;
+  while (std::fgets(line, sizeof(line), fh)) {
+    const std::string l(line);
+    if (l.find(want) == std::string::npos) continue;
+    const size_t pc = l.find("\"cases_per_lane\": "), pu = l.find("\"blocks_per_step\": ");
+    if (pc == std::string::npos || pu == std::string::npos) continue;
+    *tc = std::atoi(l.c_str() + pc + 18);
+    *tu = std::atoi(l.c_str() + pu + 19);
+    found = true;  // the last matching line wins
+  }
+  std::fclose(fh);
+  return found;
+}
+
+}  // namespace
+
+// Autotuner of the batched kernel's tile: every instantiated (cases per lane,
+// blocks per step) pair runs 30 CG iterations of the 32-case solve (diagonal
+// preconditioner, a load on every free DOF of every case), timed with CUDA
+// events on the context's stream (best of two); the fastest per iteration is
+// kept for later batched solves and appended to the JSON-lines cache.
+int batch_autotune(axia_ctx* ctx, const char* cache_path, int* tc_out, int* tu_out, double* us_out) {
+  if (!ctx->have_bsr64 || !ctx->have_bsr32)
+    return set_error(ctx, AXIA_ERR_STATE, "batch autotune needs the node-block forms (AXIA_ASM_BSR64 | AXIA_ASM_BSR32)");
+  const std::string key = batch_tune_key(ctx);
+  int tc = 0, tu = 0;
+  if (batch_cache_lookup(cache_path, key, &tc, &tu) && valid_tile(tc, tu)) {
+    ctx->tuned_btc = tc;
+    ctx->tuned_btu = tu;
+    *tc_out = tc;
+    *tu_out = tu;
+    if (us_out) *us_out = 0.0;
+    return AXIA_OK;
+  }
+  AXIA_TRY(ensure_batch_buffers(ctx));
+  k_batch_tune_rhs<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(ctx->ndof, ctx->d_ind_of, ctx->d_mB);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  const long long iters = 30;
+  double best = 1e300;
+  BatchTile pick = kBatchDefault;
+  cudaEvent_t a = nullptr, b = nullptr;
+  int st = AXIA_OK;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
+    st = set_error(ctx, AXIA_ERR_CUDA, "batch autotune events");
+  for (const BatchTile& t : kBatchTiles) {
+    if (st != AXIA_OK) break;
+    const void* kern = batch_kernel<false>(t);
+    int grid = 0;
+    if ((st = batch_grid(ctx, kern, &grid)) != AXIA_OK) break;
+    float best_t = 1e30f;
+    for (int rep = 0; rep < 2 && st == AXIA_OK; ++rep) {
+      if ((st = reset_dev_status(ctx)) != AXIA_OK) break;
+      cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream);
+      MultiArgs P = multi_args(ctx, 1e-30, 1e-30, iters, CoarseArgs{});
+      cudaEventRecord(a, ctx->stream);
+      if ((st = launch_batch(ctx, kern, grid, P)) != AXIA_OK) break;
+      cudaEventRecord(b, ctx->stream);
+      MultiOut o;
+      if (cudaMemcpyAsync(&o, ctx->d_mout, sizeof(MultiOut), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+          cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        st = set_error(ctx, AXIA_ERR_CUDA, "batch autotune launch");
+        break;
+      }
+      DevStatus hs;
+      if ((st = read_dev_status(ctx, &hs)) != AXIA_OK) break;
+      if (hs.timeout) {
+        st = set_error(ctx, AXIA_ERR_TIMEOUT, "a grid barrier of the batched PCG ran past its limit");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      best_t = std::min(best_t, ms / (float)std::max<long long>(o.iters, 1));
+    }
+    if (st == AXIA_OK && best_t < best) {
+      best = best_t;
+      pick = t;
+    }
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (st != AXIA_OK) return st;
+  ctx->tuned_btc = pick.tc;
+  ctx->tuned_btu = pick.tu;
+  *tc_out = pick.tc;
+  *tu_out = pick.tu;
+  if (us_out) *us_out = best * 1e3;
+  if (cache_path) {
+    if (FILE* fh = std::fopen(cache_path, "a")) {
+      std::fprintf(fh, "{\"key\": \"%s\", \"cases_per_lane\": %d, \"blocks_per_step\": %d, \"us_per_iter\": %.3f}\n",
+                   key.c_str(), pick.tc, pick.tu, best * 1e3);
+      std::fclose(fh);
+    }
+  }
+  return AXIA_OK;
+}
+
+// Solves nrhs load cases (F, U: [nrhs][nd] device arrays) 32 at a time.
+int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const axia_solve_opts* opts,
+                axia_solve_info* info, double* rel_res) {
+  if (!ctx->have_bsr64 || !ctx->have_bsr32)
+    return set_error(ctx, AXIA_ERR_STATE, "batched solve needs the node-block forms (AXIA_ASM_BSR64 | AXIA_ASM_BSR32)");
+  const int64_t nd = ctx->ndof;
+  AXIA_TRY(ensure_batch_buffers(ctx));
   if (opts->preconditioner != AXIA_PRECOND_JACOBI && opts->preconditioner != AXIA_PRECOND_COARSE)
     return set_error(ctx, AXIA_ERR_INVALID_ARG, "batched load cases: unknown preconditioner");
   const bool coarse = opts->preconditioner == AXIA_PRECOND_COARSE;
@@ -728,12 +926,11 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
   if (coarse) AXIA_TRY(coarse_prepare_batched(ctx, opts->coarse_nodes, &cargs));
   const long long max_iter = opts->max_iter > 0 ? opts->max_iter : std::max<long long>(4LL * ctx->n_free, 200);
   const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.01;
-  auto kern = coarse ? pcg_bsr_multi_kernel<true> : pcg_bsr_multi_kernel<false>;
+  const BatchTile tile = valid_tile(ctx->tuned_btc, ctx->tuned_btu) ? BatchTile{ctx->tuned_btc, ctx->tuned_btu}
+                                                                     : kBatchDefault;
+  const void* kern = coarse ? batch_kernel<true>(tile) : batch_kernel<false>(tile);
   int grid = 0;
-  // static + staging shared memory is above the 48 KB a block gets without opting in
-  AXIA_CUDA(ctx, cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STAGE_BYTES));
-  AXIA_TRY(coop_grid(ctx, (const void*)kern, (int)std::min<int64_t>(nd, INT32_MAX), &grid, STAGE_BYTES));
-  if ((size_t)grid * 2 * NR > ctx->partial_slots) grid = (int)(ctx->partial_slots / (2 * NR));
+  AXIA_TRY(batch_grid(ctx, kern, &grid));
   info->iters = 0;
   info->outer_iters = 0;
   double worst = 0.0;
@@ -744,18 +941,8 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
                                                            ctx->d_mB);
     ctx->launches++;
     AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
-    MultiArgs P{BsrMatM<float>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval32, (long long)ctx->nbq},
-                BsrMatM<double>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq},
-                (int)nd, ctx->d_bdinv32, ctx->d_mB, ctx->d_mX, ctx->d_mX32, ctx->d_mR32, ctx->d_mP32, ctx->d_mQ32,
-                ctx->d_partials, ctx->d_totals, ctx->d_bar, ctx->d_status, (MultiOut*)ctx->d_mout, opts->rtol, delta,
-                max_iter, 2000000000ull, cargs};
-    AXIA_TRY(timed_launch(ctx, info, [&]() -> int {
-      void* params[] = {&P};
-      AXIA_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(PCG_THREADS), params,
-                                                 STAGE_BYTES, ctx->stream));
-      ctx->launches++;
-      return AXIA_OK;
-    }));
+    MultiArgs P = multi_args(ctx, opts->rtol, delta, max_iter, cargs);
+    AXIA_TRY(timed_launch(ctx, info, [&]() -> int { return launch_batch(ctx, kern, grid, P); }));
     MultiOut o;
     AXIA_CUDA(ctx, cudaMemcpyAsync(&o, ctx->d_mout, sizeof(MultiOut), cudaMemcpyDeviceToHost, ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -167,7 +167,7 @@ __device__ __forceinline__ void sym_row(int a, int sl, const SymMat& S, const fl
     }
     auto lower = [&](int2 bt) {
       const float2* p = reinterpret_cast<const float2*>(S.uval + 10LL * bt.y);
-      const float2 v0 = __ldcg(p), v1 = __ldcg(p + 1), v2 = __ldcg(p + 2), v3 = __ldcg(p + 3), v4 = __ldcg(p + 4);
+      const float2 v0 = __ldg(p), v1 = __ldg(p + 1), v2 = __ldg(p + 2), v3 = __ldg(p + 3), v4 = __ldg(p + 4);
       const float b0 = x[3 * bt.x], b1 = x[3 * bt.x + 1], b2 = x[3 * bt.x + 2];
       // K_ba = [v0.x v0.y v1.x; v1.y v2.x v2.y; v3.x v3.y v4.x], y += K_ba^T x_b
       y0 = fmaf(v0.x, b0, fmaf(v1.y, b1, fmaf(v3.x, b2, y0)));

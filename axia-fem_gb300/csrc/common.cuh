@@ -384,6 +384,7 @@ struct axia_ctx {
   int64_t graph_coarse = -1;    // coarse space the captured graph reads (its coarse_gen; -1: diagonal only)
   int64_t coarse_gen = 0;       // coarse spaces built so far (a new space gets new device arrays)
   int tuned_lanes = 0, tuned_vec = 0;  // node-block layout chosen by axia_gpu_autotune (0: none)
+  int tuned_btc = 0, tuned_btu = 0;    // batched-kernel tile chosen by axia_gpu_autotune_batched (0: none)
   void* multi_graph = nullptr;        // cudaGraphExec_t
   const double* graph_f = nullptr;
   double* graph_u = nullptr;

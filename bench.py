@@ -164,6 +164,25 @@ def coarse_iter_bytes(n_nodes, n_coarse):
     return 20 * n_nodes + 4 * n_coarse * ncp
 
 
+def batch_iter_bytes(nblocks, n_nodes, n_coarse, nrhs=32):
+    """One iteration of the 32-case kernel: the FP32 node-block matrix once
+    (values + block columns, unpadded), the block-row pointers, 13 passes over
+    [3 n_nodes][32] FP32 vectors (SpMV: P gathered once, Q written, P read for
+    p.q; update: X, R read+written, P, Q read; search direction: R read, P
+    read+written) and, with a coarse space, its per-iteration bytes."""
+    b = (9 * 4 + 4) * nblocks + 4 * (n_nodes + 1) + 13 * 4 * nrhs * 3 * n_nodes
+    if n_coarse:
+        b += coarse_iter_bytes(n_nodes, n_coarse)
+    return b
+
+
+def batch_update_bytes(nblocks, n_nodes, nrhs=32):
+    """One FP64 reliable update of the 32-case kernel: X += X32 (X read+written,
+    X32 read+written), the FP64 matrix once, X gathered once, B read, R32 written."""
+    nd = 3 * n_nodes
+    return (9 * 8 + 4) * nblocks + 4 * (n_nodes + 1) + nrhs * nd * (8 + 8 + 4 + 4 + 8 + 8 + 4)
+
+
 def recover_bytes(n_elem, nn, n_nodes):
     """Algorithmic bytes of stress recovery + reactions: per element the
     connectivity twice, E once, 9 doubles per (element, node) written and read
@@ -388,6 +407,9 @@ def run_c4a(args):
     ctx.setup(m)
     F = torch.from_numpy(m.cload_batch).to(f"cuda:{local}")
     U = torch.empty_like(F)
+    # tile of the batched kernel, picked by the library's autotuner (untimed)
+    ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+    btc, btu, bus = ctx.autotune_batched()
 
     def step_jacobi():
         ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
@@ -411,6 +433,15 @@ def run_c4a(args):
                                 preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
     ms1, i1 = timer(single, 1, 2)
     err = float(torch.linalg.norm(U[0] - u1) / torch.linalg.norm(u1))
+    pk, pk_kind = peaks()
+    nblocks = ctx.n_blocks()
+    bbytes = batch_iter_bytes(nblocks, m.n_nodes, n_coarse) * info.iters + \
+        batch_update_bytes(nblocks, m.n_nodes) * info.outer_iters
+    bach = bbytes / (info.ms_pcg_kernel * 1e-3) / 1e9
+    broof = {"bound": "hbm", "achieved": bach, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": bach / pk["hbm_gbs"],
+             "bytes_per_launch": bbytes, "ms_per_launch": info.ms_pcg_kernel,
+             "us_per_iteration": 1e3 * info.ms_pcg_kernel / max(info.iters, 1),
+             "kernel": "pcg_bsr_multi_kernel (32 load cases, two-level)", "peak_source": f"{pk_kind} hbm_gbs"}
     oracle_check = oracle_residuals(m, {"batched_coarse": U.cpu().numpy(), "batched_jacobi": Uj.cpu().numpy()},
                                     m.cload_batch)
     nf = ctx.n_free
@@ -418,6 +449,8 @@ def run_c4a(args):
           32 * nf / (ms * 1e-3) / 1e6, ms,
           {"dtype": "f32+f64", "config": {"workload": f"C3D8 {n}^3 x 32 load cases", "n_free": nf, "rhs": 32,
                                           "preconditioner": f"diagonal + coarse space ({n_sub} subdomains)"},
+           "tile": {"cases_per_lane": btc, "blocks_per_step": btu, "us_per_iter_tuning": bus},
+           "roofline": broof,
            "batched": {"iters": info.iters, "reliable_updates": info.outer_iters, "max_rel_residual": float(rel.max()),
                        "ms_kernel": info.ms_pcg_kernel, "coarse_unknowns": n_coarse,
                        "rel_err_vs_jacobi_batched": err_j},
@@ -633,13 +666,15 @@ def main():
 
     if args.only:
         if args.only == "spmv":
-            ctx.assemble_ex(L.ASM_CSR64 | L.ASM_CSR32 | L.ASM_BSR64 | L.ASM_BSR32)
+            ctx.assemble_ex(L.ASM_CSR64 | L.ASM_CSR32 | L.ASM_BSR64 | L.ASM_BSR32 | L.ASM_SYM32)
             nd = 3 * model.n_nodes
             xf32 = torch.rand(nd, device=f"cuda:{local}")
             yf32 = torch.empty_like(xf32)
             with torch.cuda.stream(stream):
                 for _ in range(5):
                     ctx.bsr_spmv_device(L.PREC_MIXED, xf32.data_ptr(), yf32.data_ptr(), args.lanes32)
+                for _ in range(5):
+                    ctx.sym_spmv_device(xf32.data_ptr(), yf32.data_ptr(), 0)
         else:
             mixed = args.only in ("mixed", "coarse")
             ctx.assemble_ex((L.ASM_BSR64 | L.ASM_BSR32) if mixed else L.ASM_CSR64)

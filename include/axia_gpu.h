@@ -403,6 +403,19 @@ AXIA_API int32_t axia_gpu_solve_csr(axia_ctx* ctx, int64_t n, const int64_t* ind
 AXIA_API int32_t axia_gpu_autotune(axia_ctx* ctx, const char* cache_path, int32_t* lanes, int32_t* vec,
                                    double* us_per_iter);
 
+/* Picks the tile of the batched load-case kernel (axia_gpu_solve_batched):
+ * load cases per lane (1, 2 or 4; a group of 32 / cases lanes covers the 32
+ * cases and a warp runs that many groups over interleaved blocks of a row)
+ * and blocks per group and step (their vector rows are all requested before
+ * the first is used).  Each instantiated pair runs 30 CG iterations of the
+ * 32-case solve on the assembled mesh, timed with CUDA events; the fastest
+ * per iteration is used by later batched solves.  cache_path and
+ * us_per_iter as in axia_gpu_autotune (one JSON line per choice).  Needs
+ * axia_gpu_assemble_ex(AXIA_ASM_BSR64 | AXIA_ASM_BSR32).  No reference
+ * counterpart. */
+AXIA_API int32_t axia_gpu_autotune_batched(axia_ctx* ctx, const char* cache_path, int32_t* cases_per_lane,
+                                           int32_t* blocks_per_step, double* us_per_iter);
+
 /* ---- DOF map with multi-point constraints (constraint.rs:8-136) ---------- */
 typedef struct axia_dofmap axia_dofmap;
 

@@ -51,3 +51,48 @@ def test_autotune_needs_node_block_forms(gpu_ctx):
     with pytest.raises(_lib.AxiaError) as e:
         gpu_ctx.autotune()
     assert e.value.code == _lib.ERR_STATE
+
+
+BATCH_TILES = {(4, 1), (2, 2), (2, 4), (1, 4), (1, 8)}
+
+
+def test_batch_autotune_every_tile_solves(gpu_ctx, tmp_path):
+    """axia_gpu_autotune_batched picks one of the instantiated tiles of the
+    32-case kernel by timing; every tile (forced through a cache entry) gives
+    the direct solution of every case to 1e-8 at rtol 1e-10, with and without
+    the coarse space."""
+    m = meshgen.block_c3d8_multiload(n=12, nrhs=32)
+    F = m.cload_batch
+    gpu_ctx.setup(m).assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+    cache = tmp_path / "batch.jsonl"
+    tc, tu, us = gpu_ctx.autotune_batched(str(cache))
+    assert (tc, tu) in BATCH_TILES and us > 0
+    lines = cache.read_text().splitlines()
+    assert len(lines) == 1 and json.loads(lines[0])["cases_per_lane"] == tc
+    r = O.solve_static(m, solver=O.SOLVER_PCG, tol=1e-6, keep_csr=True, f=F[0])
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    lu = spla.splu(sp.csr_matrix((r.data, r.indices, r.indptr), shape=(r.n_free, r.n_free)).tocsc())
+    free = m.free_mask()
+    ref = np.zeros_like(F)
+    for c in range(F.shape[0]):
+        ref[c][free] = lu.solve(F[c][free])
+    entry = json.loads(lines[0])
+    for tile in sorted(BATCH_TILES):
+        entry["cases_per_lane"], entry["blocks_per_step"] = tile
+        cache.write_text(json.dumps(entry) + "\n")
+        assert gpu_ctx.autotune_batched(str(cache)) == (tile[0], tile[1], 0.0)
+        for pre in (dict(), dict(preconditioner=_lib.PRECOND_COARSE, coarse_nodes=200)):
+            U, info, rel = gpu_ctx.solve_batched(F, rtol=1e-10, **pre)
+            assert np.all(rel <= 1e-10 * 1.0001), (tile, pre)
+            err = np.linalg.norm(U - ref, axis=1) / np.linalg.norm(ref, axis=1)
+            assert err.max() < 1e-8, (tile, pre, err.max())
+
+
+def test_batch_autotune_needs_node_block_forms(gpu_ctx):
+    m = meshgen.cantilever_c3d8()
+    gpu_ctx.setup(m)
+    gpu_ctx.assemble(_lib.PREC_FP64)
+    with pytest.raises(_lib.AxiaError) as e:
+        gpu_ctx.autotune_batched()
+    assert e.value.code == _lib.ERR_STATE
