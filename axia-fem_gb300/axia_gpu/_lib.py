@@ -47,6 +47,8 @@ ASM_SYM32 = 16
 FORMAT_CSR = 0
 FORMAT_BSR3 = 1
 FORMAT_BSR3_SYM = 2
+KRYLOV_PER_CASE = 0
+KRYLOV_BLOCK = 1
 PRECOND_JACOBI = 0
 PRECOND_COARSE = 1
 
@@ -61,7 +63,8 @@ class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_iter", C.c_int64), ("precision", C.c_int32),
                 ("refine_mode", C.c_int32), ("inner_rtol", C.c_double), ("max_outer", C.c_int32),
                 ("spmv_lanes", C.c_int32), ("matrix_format", C.c_int32), ("spmv_vec", C.c_int32),
-                ("preconditioner", C.c_int32), ("coarse_nodes", C.c_int32)]
+                ("preconditioner", C.c_int32), ("coarse_nodes", C.c_int32), ("krylov", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class SolveInfo(C.Structure):

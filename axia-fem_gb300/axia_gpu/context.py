@@ -163,9 +163,9 @@ class GpuContext:
     @staticmethod
     def opts(rtol=1e-8, max_iter=0, precision=L.PREC_FP64, refine_mode=L.REFINE_RESTART, inner_rtol=1e-3,
              max_outer=50, spmv_lanes=0, matrix_format=L.FORMAT_CSR, spmv_vec=0, preconditioner=0,
-             coarse_nodes=0):
+             coarse_nodes=0, krylov=L.KRYLOV_PER_CASE):
         return L.SolveOpts(rtol, max_iter, precision, refine_mode, inner_rtol, max_outer, spmv_lanes,
-                           matrix_format, spmv_vec, preconditioner, coarse_nodes)
+                           matrix_format, spmv_vec, preconditioner, coarse_nodes, krylov, 0)
 
     def set_stream(self, stream_handle: int | None):
         """Issue the context's work on a caller's cudaStream_t (None: own stream)."""

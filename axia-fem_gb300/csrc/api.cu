@@ -17,6 +17,8 @@ int simp_modulus(axia_ctx* ctx, const double* d_rho, double pexp, double e0);
 int simp_gradient(axia_ctx* ctx, const double* d_rho, const double* d_s, double pexp, double e0, double* d_g);
 int device_dot(axia_ctx* ctx, const double* a, const double* b, int64_t n, double* out);
 void multimesh_release(axia_ctx* ctx);
+int batch_block_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const axia_solve_opts* opts,
+                      axia_solve_info* info, double* rel_res);
 int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const axia_solve_opts* opts,
                 axia_solve_info* info, double* rel_res);
 int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args);
@@ -130,6 +132,11 @@ void free_mesh_state(axia_ctx* ctx) {
   dev_release(ctx, ctx->d_mR32);
   dev_release(ctx, ctx->d_mP32);
   dev_release(ctx, ctx->d_mQ32);
+  dev_release(ctx, ctx->d_mZ32);
+  dev_release(ctx, ctx->d_bpart);
+  dev_release(ctx, ctx->d_bgram);
+  dev_release(ctx, ctx->d_bsmall);
+  ctx->bpart_capacity = 0;
   if (ctx->d_mout) cudaFree(ctx->d_mout);
   ctx->d_mout = nullptr;
   ctx->batch_capacity = 0;
@@ -712,7 +719,8 @@ static int32_t batched_common(axia_ctx* ctx, int32_t nrhs, const double* d_F, do
   if (opts) o = *opts;
   if (!(o.rtol > 0.0)) o.rtol = 1e-8;
   EventTimer t(ctx->stream);
-  int st = batch_solve(ctx, nrhs, d_F, d_U, &o, info, rel_res);
+  int st = o.krylov == AXIA_KRYLOV_BLOCK ? batch_block_solve(ctx, nrhs, d_F, d_U, &o, info, rel_res)
+                                        : batch_solve(ctx, nrhs, d_F, d_U, &o, info, rel_res);
   info->ms_solve = t.stop_ms();
   fill_info_sizes(ctx, info);
   info->status = st;

@@ -721,6 +721,341 @@ __global__ void k_batch_out(int64_t nd, int nrhs, const int32_t* ind_of, const d
   }
 }
 
+// ---------------------------------------------------------------------------
+// Block PCG of the 32 load cases (AXIA_BATCH_BLOCK): one Krylov block for all
+// cases instead of 32 recurrences.  The breakdown-free form of block CG
+// (O'Leary's method with the search block orthonormalized every iteration
+// and dependent directions dropped, as in Ji and Li's breakdown-free block
+// CG):
+//   Q = K P,  Gm = P^T Q,  alpha = Gm^-1 (P^T R),  X += P alpha,  R -= Q alpha,
+//   Z = M R,  beta = -Gm^-1 (Q^T Z),  W = Z + P beta,  P = W T  with  P^T P = I
+// (T from the Cholesky factor of the scaled W^T W; a direction whose scaled
+// pivot falls below 1e-6 is dropped: its column of P is zero).  The 32 x 32
+// Gram matrices are reduced in FP64 in a fixed order; alpha, beta and T are
+// computed in FP64 and applied to the FP32 blocks.  A load case whose FP64
+// residual meets the tolerance is frozen (its alpha column and its column of
+// W are zero).  FP64 reliable updates as in the recurrence-per-case kernel.
+// No reference counterpart: the reference solves load cases one at a time
+// (solver/src/linalg.rs:199-259); the solutions are the same.
+// ---------------------------------------------------------------------------
+constexpr int BT = 256;             // threads of the block-PCG kernels
+constexpr int GRAM_ROWS = 64;       // rows staged per Gram tile
+constexpr int NG_MAX = 3;           // Gram products per pass
+
+// Q = K P on [nd][32] blocks: warp per block row, two cases per lane, four
+// blocks per group and step
+__global__ void __launch_bounds__(BT) k_blk_spmm(BsrMatM<float> M, const float* P, float* Q) {
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (blockIdx.x * BT + threadIdx.x) >> 5, nwarps = (gridDim.x * BT) >> 5;
+  for (int a = gwarp; a < M.n_nodes; a += nwarps) {
+    const int len = __ldg(M.adj_ptr + a + 1) - __ldg(M.adj_ptr + a);
+    float y[3][2];
+    row_tile<2, 4, false>(a, len, lane, nullptr, M, P, y);
+    if (lane < 16) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) stc<2>(Q + (size_t)(3 * a + i) * NR + 2 * lane, y[i]);
+    }
+  }
+}
+
+// Gram products G_g = A^T B_g (g < ng) over the rows of [nd][32] blocks; a block
+// takes tiles of GRAM_ROWS rows in turn (staged in shared memory), thread t owns
+// entries (t / 8, 4 (t % 8) .. + 3) of each product, sums a tile in FP32 and
+// the tiles in FP64, and writes its 32 x 32 partials to part[block][g].
+__global__ void __launch_bounds__(BT) k_blk_gram(int64_t nd, const float* A, const float* B0, const float* B1,
+                                                 const float* B2, int ng, double* part) {
+  __shared__ __align__(16) float sA[GRAM_ROWS][NR];
+  __shared__ __align__(16) float sB[NG_MAX][GRAM_ROWS][NR];
+  const float* Bs[NG_MAX] = {B0, B1, B2};
+  const int i = threadIdx.x >> 3, j4 = 4 * (threadIdx.x & 7);
+  double acc[NG_MAX][4] = {};
+  const int64_t ntile = (nd + GRAM_ROWS - 1) / GRAM_ROWS;
+  for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int64_t r0 = tile * GRAM_ROWS;
+    const int rows = nd - r0 < GRAM_ROWS ? (int)(nd - r0) : GRAM_ROWS;
+    __syncthreads();
+    for (int t = threadIdx.x; t < GRAM_ROWS * NR / 4; t += BT) {
+      const int r = t / (NR / 4), c = 4 * (t % (NR / 4));
+      const bool ok = r < rows;
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      *reinterpret_cast<float4*>(&sA[r][c]) = ok ? __ldcs(reinterpret_cast<const float4*>(A + (r0 + r) * NR + c)) : z;
+#pragma unroll
+      for (int g = 0; g < NG_MAX; ++g)
+        if (g < ng)
+          *reinterpret_cast<float4*>(&sB[g][r][c]) =
+              ok ? __ldcs(reinterpret_cast<const float4*>(Bs[g] + (r0 + r) * NR + c)) : z;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int g = 0; g < NG_MAX; ++g) {
+      if (g >= ng) break;
+      float s[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+      for (int r = 0; r < GRAM_ROWS; ++r) {
+        const float a = sA[r][i];
+        const float4 b = *reinterpret_cast<const float4*>(&sB[g][r][j4]);
+        s[0] = fmaf(a, b.x, s[0]);
+        s[1] = fmaf(a, b.y, s[1]);
+        s[2] = fmaf(a, b.z, s[2]);
+        s[3] = fmaf(a, b.w, s[3]);
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[g][c] += (double)s[c];
+    }
+  }
+#pragma unroll
+  for (int g = 0; g < NG_MAX; ++g)
+    if (g < ng)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) part[((size_t)blockIdx.x * NG_MAX + g) * NR * NR + i * NR + j4 + c] = acc[g][c];
+}
+
+// out[e] = sum over blocks b of part[b][src + e], e < n_entries (part rows of
+// NG_MAX * 1024 doubles): 16 threads per entry take every 16th block and
+// their sums are added in a fixed pattern, so the result is reproducible
+__global__ void __launch_bounds__(BT) k_blk_finalize(int nblk, int src, int n_entries, const double* part,
+                                                     double* out) {
+  const int t = blockIdx.x * BT + threadIdx.x;
+  const int e = t >> 4, k = t & 15;
+  double s = 0.0;
+  if (e < n_entries)
+    for (int b = k; b < nblk; b += 16) s += __ldcg(part + (size_t)b * NG_MAX * NR * NR + src + e);
+#pragma unroll
+  for (int o = 1; o < 16; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (e < n_entries && k == 0) out[e] = s;
+}
+
+// Out = (acc ? Out : 0) + sgn In M over the rows (M 32 x 32 FP32); columns
+// whose bit of `zero_cols` is set come out zero.  With `norms`, each block
+// also writes the sums of squares of its output rows per column to
+// part[block][3][..] (the fourth slot of the Gram partials).
+__global__ void __launch_bounds__(BT, 4) k_blk_mm(int64_t nd, const float* In, const float* Mx, float sgn, int acc,
+                                               unsigned zero_cols, float* Out, double* norm_part) {
+  __shared__ __align__(16) float sM[NR][NR];
+  __shared__ double sN[BT / 8][NR];
+  for (int t = threadIdx.x; t < NR * NR; t += BT) sM[t / NR][t % NR] = Mx[t];
+  __syncthreads();
+  const int j4 = 4 * (threadIdx.x & 7);
+  double nrm[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int64_t r = (int64_t)blockIdx.x * (BT / 8) + (threadIdx.x >> 3); r < nd; r += (int64_t)gridDim.x * (BT / 8)) {
+    const float4* in = reinterpret_cast<const float4*>(In + r * NR);
+    float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+    for (int q = 0; q < 8; ++q) {
+      const float4 v = in[q];
+      const float vk[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4 m = *reinterpret_cast<const float4*>(&sM[4 * q + u][j4]);
+        o[0] = fmaf(vk[u], m.x, o[0]);
+        o[1] = fmaf(vk[u], m.y, o[1]);
+        o[2] = fmaf(vk[u], m.z, o[2]);
+        o[3] = fmaf(vk[u], m.w, o[3]);
+      }
+    }
+    float4* out = reinterpret_cast<float4*>(Out + r * NR + j4);
+    const float4 prev = acc ? *out : make_float4(0.f, 0.f, 0.f, 0.f);
+    float res[4] = {fmaf(sgn, o[0], prev.x), fmaf(sgn, o[1], prev.y), fmaf(sgn, o[2], prev.z), fmaf(sgn, o[3], prev.w)};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      if ((zero_cols >> (j4 + c)) & 1u) res[c] = 0.f;
+      nrm[c] = fma((double)res[c], (double)res[c], nrm[c]);
+    }
+    *out = make_float4(res[0], res[1], res[2], res[3]);
+  }
+  if (norm_part) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) sN[threadIdx.x >> 3][j4 + c] = nrm[c];
+    __syncthreads();
+    if (threadIdx.x < NR) {
+      double s = 0.0;
+      for (int w = 0; w < BT / 8; ++w) s += sN[w][threadIdx.x];
+      norm_part[((size_t)blockIdx.x * NG_MAX) * NR * NR + threadIdx.x] = s;
+    }
+  }
+}
+
+// z = D^-1 r (+ the coarse part Z_c y) on [nd][32] blocks, float4 per thread
+template <bool COARSE>
+__global__ void __launch_bounds__(BT) k_blk_precond(int64_t nd, const float* dinv, const float* R, CoarseArgs C,
+                                                    float* Z) {
+  const int64_t nq = nd * LPG;
+  for (int64_t q = blockIdx.x * (int64_t)BT + threadIdx.x; q < nq; q += (int64_t)gridDim.x * BT) {
+    const int64_t row = q / LPG;
+    float r[CPL], zc[CPL] = {0.f, 0.f, 0.f, 0.f};
+    ld4(R + q * CPL, r);
+    if constexpr (COARSE) coarse_prolong_m(C, row, CPL * (int)(q % LPG), zc);
+    const float di = dinv[row];
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) zc[c] = fmaf(r[c], di, zc[c]);
+    st4(Z + q * CPL, zc);
+  }
+}
+
+__global__ void __launch_bounds__(BT) k_blk_restrict(CoarseArgs C, const float* R) {
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (blockIdx.x * BT + threadIdx.x) >> 5, nwarps = (gridDim.x * BT) >> 5;
+  coarse_restrict_m(C, R, gwarp, nwarps, lane);
+}
+
+__global__ void __launch_bounds__(PCG_THREADS) k_blk_coarse_solve(CoarseArgs C, double* scratch) {
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (blockIdx.x * PCG_THREADS + threadIdx.x) >> 5, nwarps = (gridDim.x * PCG_THREADS) >> 5;
+  coarse_solve_m(C, gwarp, nwarps, lane, scratch, 0);
+}
+
+// X += X32 (FP64), X32 = 0
+__global__ void __launch_bounds__(BT) k_blk_xadd(int64_t n, double* X, float* X32) {
+  for (int64_t t = blockIdx.x * (int64_t)BT + threadIdx.x; t < n; t += (int64_t)gridDim.x * BT) {
+    X[t] += (double)X32[t];
+    X32[t] = 0.f;
+  }
+}
+
+// R = B - K X in FP64 (lane = load case), R32 = (float) R, per-case sums of
+// squares of R to part[block][3][..]
+__global__ void __launch_bounds__(BT) k_blk_residual64(BsrMatM<double> M, const double* X, const double* B, float* R32,
+                                                       double* norm_part) {
+  __shared__ double sN[BT / 32][NR];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gwarp = (blockIdx.x * BT + threadIdx.x) >> 5, nwarps = (gridDim.x * BT) >> 5;
+  double nrm = 0.0;
+  for (int a = gwarp; a < M.n_nodes; a += nwarps) {
+    const int beg = __ldg(M.adj_ptr + a), end = __ldg(M.adj_ptr + a + 1);
+    double y0 = 0.0, y1 = 0.0, y2 = 0.0;
+    for (int s = beg; s < end; s += 4) {
+      double x[4][3], v[4][9];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int su = s + u < end ? s + u : beg;
+        const int b = ld_stream(M.adj + su);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) x[u][j] = s + u < end ? X[(size_t)(3 * b + j) * NR + lane] : 0.0;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) v[u][k] = ld_stream(M.val + (long long)k * M.nb + su);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        y0 = fma(v[u][0], x[u][0], fma(v[u][1], x[u][1], fma(v[u][2], x[u][2], y0)));
+        y1 = fma(v[u][3], x[u][0], fma(v[u][4], x[u][1], fma(v[u][5], x[u][2], y1)));
+        y2 = fma(v[u][6], x[u][0], fma(v[u][7], x[u][1], fma(v[u][8], x[u][2], y2)));
+      }
+    }
+    const double y[3] = {y0, y1, y2};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const size_t off = (size_t)(3 * a + i) * NR + lane;
+      const double r = B[off] - y[i];
+      nrm = fma(r, r, nrm);
+      R32[off] = (float)r;
+    }
+  }
+  sN[warp][lane] = nrm;
+  __syncthreads();
+  if (threadIdx.x < NR) {
+    double s = 0.0;
+    for (int w = 0; w < BT / 32; ++w) s += sN[w][threadIdx.x];
+    norm_part[((size_t)blockIdx.x * NG_MAX) * NR * NR + threadIdx.x] = s;
+  }
+}
+
+// The small dense steps (one warp, FP64, lane = column):
+//   mode 0 (alpha): G = Gram 0 (P^T Q, kept as Gm), S = Gram 1 (P^T R):
+//           alpha = Gm^-1 S, zero in the columns of `frozen`
+//   mode 1 (beta):  Gm (kept), S = Gram 1 (Q^T Z): beta = -Gm^-1 S
+//   mode 2 (orth):  G = Gram 2 (W^T W): T = D L^-T for D G D = L L^T,
+//           D = diag(G)^-1/2; a scaled pivot below 1e-6 (or a zero column)
+//           drops that direction (its column of T is zero)
+// gram: [4][32][32] (Gm, S, WtW, norms); small: [3][32][32] FP32 alpha, beta, T.
+// Gm's factor is recomputed each time (a 32 x 32 Cholesky is a few microseconds).
+__global__ void __launch_bounds__(32) k_blk_small(int mode, unsigned frozen, const double* gram, float* small) {
+  __shared__ double L[NR][NR + 1];
+  __shared__ double S[NR][NR + 1];
+  __shared__ double dsc[NR];
+  __shared__ int drop[NR];
+  const int lane = threadIdx.x;
+  const double* G = gram + (mode == 2 ? 2 : 0) * NR * NR;
+  // scaling (orth) or none
+  const double gd = G[lane * NR + lane];
+  if (mode == 2) {
+    dsc[lane] = gd > 1e-300 ? 1.0 / sqrt(gd) : 0.0;
+  } else {
+    dsc[lane] = 1.0;
+  }
+  __syncwarp();
+  for (int i = 0; i < NR; ++i) L[i][lane] = G[i * NR + lane] * dsc[i] * dsc[lane];
+  if (mode != 2)
+    for (int i = 0; i < NR; ++i) S[i][lane] = gram[NR * NR + i * NR + lane];
+  __syncwarp();
+  // Cholesky L L^T of the (scaled) matrix, in place in the lower triangle
+  double dmax = 0.0;
+  for (int i = 0; i < NR; ++i) dmax = fmax(dmax, L[i][i]);
+  const double thr = mode == 2 ? 1e-6 : 1e-12 * dmax;
+  for (int k = 0; k < NR; ++k) {
+    const double piv = L[k][k];
+    const bool dr = !(piv > thr) || (mode == 2 && dsc[k] == 0.0);
+    __syncwarp();
+    if (lane == 0) drop[k] = dr;
+    if (lane > k) L[lane][k] = dr ? 0.0 : L[lane][k] / sqrt(piv);
+    __syncwarp();
+    if (lane == k) L[k][k] = dr ? 1.0 : sqrt(piv);
+    __syncwarp();
+    if (lane > k)
+      for (int j = k + 1; j <= lane; ++j) L[lane][j] -= L[lane][k] * L[j][k];
+    __syncwarp();
+  }
+  if (mode == 2) {
+    // T = D L^-T: column c of L^-T solves L^T t = e_c (upper triangular back substitution)
+    double t[NR];
+    for (int i = NR - 1; i >= 0; --i) {
+      double v = i == lane ? 1.0 : 0.0;
+      for (int j = i + 1; j < NR; ++j) v -= L[j][i] * t[j];
+      t[i] = (i <= lane) ? v / L[i][i] : 0.0;
+    }
+    for (int i = 0; i < NR; ++i)
+      small[2 * NR * NR + i * NR + lane] = (drop[lane] || drop[i]) ? 0.f : (float)(dsc[i] * t[i]);
+    return;
+  }
+  // X = Gm^-1 S column by column (lane = column of S), dropped directions zero
+  double y[NR];
+  for (int i = 0; i < NR; ++i) {
+    double v = S[i][lane];
+    for (int j = 0; j < i; ++j) v -= L[i][j] * y[j];
+    y[i] = drop[i] ? 0.0 : v / L[i][i];
+  }
+  for (int i = NR - 1; i >= 0; --i) {
+    double v = y[i];
+    for (int j = i + 1; j < NR; ++j) v -= L[j][i] * y[j];
+    y[i] = drop[i] ? 0.0 : v / L[i][i];
+  }
+  const bool fz = (frozen >> lane) & 1u;
+  for (int i = 0; i < NR; ++i) {
+    const double v = mode == 0 ? (fz ? 0.0 : y[i]) : -y[i];
+    small[mode * NR * NR + i * NR + lane] = (float)v;
+  }
+}
+
+// R32 = (float) B, X = 0, X32 = 0, per-case sums of squares of B to part[block][0][..]
+__global__ void __launch_bounds__(BT) k_blk_init(int64_t n, const double* B, double* X, float* X32, float* R32,
+                                                 double* norm_part) {
+  __shared__ double sN[BT / 32][NR];
+  double nrm = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)BT + threadIdx.x; t < n; t += (int64_t)gridDim.x * BT) {
+    const double b = B[t];
+    X[t] = 0.0;
+    X32[t] = 0.f;
+    R32[t] = (float)b;
+    nrm = fma(b, b, nrm);  // this thread's case: t % 32 = lane
+  }
+  sN[threadIdx.x >> 5][threadIdx.x & 31] = nrm;
+  __syncthreads();
+  if (threadIdx.x < NR) {
+    double s = 0.0;
+    for (int w = 0; w < BT / 32; ++w) s += sN[w][threadIdx.x];
+    norm_part[((size_t)blockIdx.x * NG_MAX) * NR * NR + threadIdx.x] = s;
+  }
+}
+
 // Tile shapes the batched kernel is instantiated for: (load cases per lane,
 // blocks per group and step).
 struct BatchTile {
@@ -909,6 +1244,225 @@ int batch_autotune(axia_ctx* ctx, const char* cache_path, int* tc_out, int* tu_o
       std::fclose(fh);
     }
   }
+  return AXIA_OK;
+}
+
+namespace {
+
+int ensure_block_buffers(axia_ctx* ctx, int grid) {
+  AXIA_TRY(ensure_batch_buffers(ctx));
+  if (!ctx->d_mZ32) AXIA_TRY(dev_alloc(ctx, &ctx->d_mZ32, (size_t)ctx->ndof * NR));
+  const size_t need = (size_t)grid * NG_MAX * NR * NR;
+  if (ctx->bpart_capacity < need) {
+    dev_free(ctx->d_bpart);
+    ctx->d_bpart = nullptr;
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_bpart, need));
+    ctx->bpart_capacity = need;
+  }
+  if (!ctx->d_bgram) AXIA_TRY(dev_alloc(ctx, &ctx->d_bgram, (size_t)4 * NR * NR));
+  if (!ctx->d_bsmall) AXIA_TRY(dev_alloc(ctx, &ctx->d_bsmall, (size_t)3 * NR * NR));
+  return AXIA_OK;
+}
+
+// The launches of one block-PCG solve of 32 cases on ctx->stream.
+struct BlockRun {
+  axia_ctx* ctx;
+  int64_t nd;
+  int g_row, g_gram, g_mm;
+  CoarseArgs C;
+  bool coarse;
+  cudaStream_t s;
+  double* part() const { return ctx->d_bpart; }
+  double* gram(int k) const { return ctx->d_bgram + (size_t)k * NR * NR; }
+  float* small(int k) const { return ctx->d_bsmall + (size_t)k * NR * NR; }
+  BsrMatM<float> m32() const {
+    return BsrMatM<float>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval32, (long long)ctx->nbq};
+  }
+  BsrMatM<double> m64() const {
+    return BsrMatM<double>{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq};
+  }
+  void count(int n) { ctx->launches += n; }
+  // Gram products A^T B_g into gram slots dst .. dst + ng - 1
+  void gram_pass(const float* A, const float* B0, const float* B1, int ng, int dst) {
+    k_blk_gram<<<g_gram, BT, 0, s>>>(nd * 1, A, B0, B1, nullptr, ng, part());
+    const int ne = ng * NR * NR;
+    k_blk_finalize<<<(ne * 16 + BT - 1) / BT, BT, 0, s>>>(g_gram, 0, ne, part(), gram(dst));
+    count(2);
+  }
+  // the per-case sums of squares written by the last norm kernel (grid nblk) -> gram slot 3
+  void norms(int nblk) {
+    k_blk_finalize<<<(NR * 16 + BT - 1) / BT, BT, 0, s>>>(nblk, 0, NR, part(), gram(3));
+    count(1);
+  }
+  void mm(const float* In, const float* Mx, float sgn, int acc, unsigned zero_cols, float* Out, bool with_norms) {
+    k_blk_mm<<<g_mm, BT, 0, s>>>(nd, In, Mx, sgn, acc, zero_cols, Out, with_norms ? part() : nullptr);
+    count(1);
+  }
+  void small_step(int mode, unsigned frozen) {
+    k_blk_small<<<1, 32, 0, s>>>(mode, frozen, ctx->d_bgram, ctx->d_bsmall);
+    count(1);
+  }
+  // Z = M R (diagonal, plus the coarse part)
+  void precond(const float* R, float* Z) {
+    if (coarse) {
+      k_blk_restrict<<<g_row, BT, 0, s>>>(C, R);
+      k_blk_coarse_solve<<<ctx->sm_count * 2, PCG_THREADS, 0, s>>>(C, part());
+      k_blk_precond<true><<<g_row, BT, 0, s>>>(nd, ctx->d_bdinv32, R, C, Z);
+      count(3);
+    } else {
+      k_blk_precond<false><<<g_row, BT, 0, s>>>(nd, ctx->d_bdinv32, R, C, Z);
+      count(1);
+    }
+  }
+  // W = Z (+ P beta), frozen columns zero; T from W^T W; P = W T.  The first
+  // time P holds nothing yet: W = Z + 0 (Z beta with the zeroed beta).
+  void new_directions(unsigned frozen, bool first) {
+    mm(first ? ctx->d_mZ32 : ctx->d_mP32, small(1), first ? 0.f : 1.f, 1, frozen, ctx->d_mZ32, false);
+    gram_pass(ctx->d_mZ32, ctx->d_mZ32, nullptr, 1, 2);
+    small_step(2, frozen);
+    mm(ctx->d_mZ32, small(2), 1.f, 0, 0u, ctx->d_mP32, false);
+  }
+};
+
+int read_norms(axia_ctx* ctx, double* h) {
+  AXIA_CUDA(ctx, cudaMemcpyAsync(h, ctx->d_bgram + 3 * NR * NR, NR * sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return AXIA_OK;
+}
+
+}  // namespace
+
+// Block PCG over the load cases (AXIA_KRYLOV_BLOCK), 32 at a time: the launch
+// sequence of the breakdown-free block recurrence above, with the per-case
+// residual norms read back after every iteration to decide on reliable
+// updates, convergence and frozen cases.
+int batch_block_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const axia_solve_opts* opts,
+                      axia_solve_info* info, double* rel_res) {
+  if (!ctx->have_bsr64 || !ctx->have_bsr32)
+    return set_error(ctx, AXIA_ERR_STATE, "batched solve needs the node-block forms (AXIA_ASM_BSR64 | AXIA_ASM_BSR32)");
+  if (opts->preconditioner != AXIA_PRECOND_JACOBI && opts->preconditioner != AXIA_PRECOND_COARSE)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "batched load cases: unknown preconditioner");
+  BlockRun B{};
+  B.ctx = ctx;
+  B.nd = ctx->ndof;
+  B.s = ctx->stream;
+  B.g_row = ctx->sm_count * 8;
+  B.g_gram = ctx->sm_count * 4;
+  B.g_mm = ctx->sm_count * 4;
+  B.coarse = opts->preconditioner == AXIA_PRECOND_COARSE;
+  AXIA_TRY(ensure_block_buffers(ctx, std::max(B.g_gram, std::max(B.g_mm, B.g_row))));
+  if (B.coarse) AXIA_TRY(coarse_prepare_batched(ctx, opts->coarse_nodes, &B.C));
+  const long long max_iter = opts->max_iter > 0 ? opts->max_iter : std::max<long long>(4LL * ctx->n_free, 200);
+  const double delta = opts->inner_rtol > 0 && opts->inner_rtol < 1 ? opts->inner_rtol : 0.01;
+  const double tol = opts->rtol;
+  info->iters = 0;
+  info->outer_iters = 0;
+  double worst = 0.0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  AXIA_CUDA(ctx, cudaEventCreate(&ev0));
+  AXIA_CUDA(ctx, cudaEventCreate(&ev1));
+  int st = AXIA_OK;
+  const int64_t n = B.nd * NR;
+  for (int c0 = 0; c0 < nrhs && st == AXIA_OK; c0 += NR) {
+    const int nc = std::min(NR, nrhs - c0);
+    k_batch_rhs<<<ctx->sm_count * 8, 256, 0, B.s>>>(B.nd, nc, ctx->d_ind_of, d_F + (int64_t)c0 * B.nd, ctx->d_kfu0,
+                                                   ctx->d_mB);
+    cudaEventRecord(ev0, B.s);
+    k_blk_init<<<B.g_row, BT, 0, B.s>>>(n, ctx->d_mB, ctx->d_mX, ctx->d_mX32, ctx->d_mR32, B.part());
+    B.count(2);
+    B.norms(B.g_row);
+    double h[NR], bnorm[NR], rmax[NR], res[NR];
+    if ((st = read_norms(ctx, h)) != AXIA_OK) break;
+    unsigned frozen = 0u;
+    for (int c = 0; c < NR; ++c) {
+      bnorm[c] = std::sqrt(h[c]);
+      rmax[c] = res[c] = bnorm[c];
+      if (!(bnorm[c] >= 1e-30)) {
+        frozen |= 1u << c;
+        res[c] = 0.0;
+      }
+    }
+    long long iters = 0;
+    int updates = 0;
+    if (frozen != 0xffffffffu) {
+      AXIA_CUDA(ctx, cudaMemsetAsync(B.small(1), 0, NR * NR * sizeof(float), B.s));
+      B.precond(ctx->d_mR32, ctx->d_mZ32);
+      B.new_directions(frozen, true);
+    }
+    for (long long it = 0; frozen != 0xffffffffu && it < max_iter; ++it) {
+      iters = it + 1;
+      // Q = K P; Gm = P^T Q, S = P^T R; alpha = Gm^-1 S; X += P alpha, R -= Q alpha
+      k_blk_spmm<<<B.g_row, BT, 0, B.s>>>(B.m32(), ctx->d_mP32, ctx->d_mQ32);
+      B.count(1);
+      B.gram_pass(ctx->d_mP32, ctx->d_mQ32, ctx->d_mR32, 2, 0);
+      B.small_step(0, frozen);
+      B.mm(ctx->d_mP32, B.small(0), 1.f, 1, 0u, ctx->d_mX32, false);
+      B.mm(ctx->d_mQ32, B.small(0), -1.f, 1, 0u, ctx->d_mR32, true);
+      B.norms(B.g_mm);
+      if ((st = read_norms(ctx, h)) != AXIA_OK) break;
+      bool all_dropped = true, candidate = false;
+      for (int c = 0; c < NR; ++c) {
+        if ((frozen >> c) & 1u) continue;
+        const double rn = std::sqrt(h[c]);
+        if (!std::isfinite(rn)) candidate = true;
+        if (rn > delta * rmax[c]) all_dropped = false;
+        if (rn <= tol * bnorm[c]) candidate = true;
+      }
+      if (all_dropped || candidate) {
+        // reliable update: X += X32, R = B - K X in FP64 for every case
+        k_blk_xadd<<<B.g_row, BT, 0, B.s>>>(n, ctx->d_mX, ctx->d_mX32);
+        k_blk_residual64<<<B.g_row, BT, 0, B.s>>>(B.m64(), ctx->d_mX, ctx->d_mB, ctx->d_mR32, B.part());
+        B.count(2);
+        B.norms(B.g_row);
+        if ((st = read_norms(ctx, h)) != AXIA_OK) break;
+        ++updates;
+        for (int c = 0; c < NR; ++c) {
+          if ((frozen >> c) & 1u) continue;
+          const double rn = std::sqrt(h[c]);
+          if (!std::isfinite(rn)) {
+            st = set_error(ctx, AXIA_ERR_NONFINITE, "block CG: non-finite residual");
+            break;
+          }
+          res[c] = rmax[c] = rn;
+          if (rn <= tol * bnorm[c]) frozen |= 1u << c;
+        }
+        if (st != AXIA_OK || frozen == 0xffffffffu) break;
+      }
+      // Z = M R; beta = -Gm^-1 (Q^T Z); W = Z + P beta; P = orth(W)
+      B.precond(ctx->d_mR32, ctx->d_mZ32);
+      B.gram_pass(ctx->d_mQ32, ctx->d_mZ32, nullptr, 1, 1);
+      B.small_step(1, frozen);
+      B.new_directions(frozen, false);
+    }
+    cudaEventRecord(ev1, B.s);
+    AXIA_CUDA(ctx, cudaEventSynchronize(ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    info->ms_pcg_kernel += ms;
+    info->pcg_launches += 1;
+    if (st != AXIA_OK) break;
+    info->iters = std::max<int64_t>(info->iters, iters);
+    info->outer_iters += updates;
+    for (int c = 0; c < nc; ++c) {
+      const double rr = bnorm[c] > 0 ? res[c] / bnorm[c] : 0.0;
+      if (rel_res) rel_res[c0 + c] = rr;
+      worst = std::max(worst, rr);
+    }
+    if (frozen != 0xffffffffu) {
+      st = set_error(ctx, AXIA_ERR_NOT_CONVERGED, "block CG did not converge in " + std::to_string(iters) + " iterations");
+      break;
+    }
+    k_batch_out<<<ctx->sm_count * 8, 256, 0, B.s>>>(B.nd, nc, ctx->d_ind_of, ctx->d_u0, ctx->d_mX,
+                                                   d_U + (int64_t)c0 * B.nd);
+    ctx->launches++;
+    if (cudaGetLastError() != cudaSuccess) st = set_error(ctx, AXIA_ERR_CUDA, "block CG launch");
+  }
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  if (st != AXIA_OK) return st;
+  info->residual = worst;
+  info->bnorm = 1.0;
   return AXIA_OK;
 }
 

@@ -369,6 +369,12 @@ struct axia_ctx {
   float *d_mX32 = nullptr, *d_mR32 = nullptr, *d_mP32 = nullptr, *d_mQ32 = nullptr;
   void* d_mout = nullptr;
   size_t batch_capacity = 0;
+  // block PCG of the load cases: W / Z block, Gram partials and results, small matrices
+  float* d_mZ32 = nullptr;
+  double* d_bpart = nullptr;    // [grid][3][32][32] per-block Gram partials
+  double* d_bgram = nullptr;    // [4][32][32]: P^T Q, second Gram, W^T W, column norms
+  float* d_bsmall = nullptr;    // [3][32][32]: alpha, beta, T (FP32 copies applied to the blocks)
+  size_t bpart_capacity = 0;
 
   // multi-mesh solve: node ranges per mesh, CTA groups, captured graph
   std::vector<int64_t> mesh_node0;    // [n_meshes+1] first node of each mesh

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AXIA_GPU_ABI_VERSION 1
+#define AXIA_GPU_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define AXIA_API __attribute__((visibility("default")))
@@ -109,6 +109,12 @@ typedef enum axia_preconditioner {
                                solution is the same, the iteration count drops */
 } axia_preconditioner;
 
+typedef enum axia_krylov {
+  AXIA_KRYLOV_PER_CASE = 0,  /* batched solves: one CG recurrence per load case (linalg.rs:199-259 each) */
+  AXIA_KRYLOV_BLOCK = 1      /* batched solves: one block Krylov space for the 32 cases of a launch
+                                (breakdown-free block PCG); same solutions, fewer iterations */
+} axia_krylov;
+
 typedef struct axia_solve_opts {
   double rtol;             /* stop when ||r||_2 <= rtol ||b||_2 (reference: 1e-8, linalg.rs:363) */
   int64_t max_iter;        /* <= 0: max(4 n, 200) as linalg.rs:376 */
@@ -123,6 +129,8 @@ typedef struct axia_solve_opts {
   int32_t coarse_nodes;    /* AXIA_PRECOND_COARSE: nodes per subdomain (0 = about 512 subdomains, but
                               at least ~13,500 matrix node blocks each: 500 nodes for C3D8; at most
                               682 subdomains per system, in a multi-mesh solve per mesh) */
+  int32_t krylov;          /* axia_krylov: batched load cases only (0 = one recurrence per case) */
+  int32_t reserved;        /* zero */
 } axia_solve_opts;
 
 typedef struct axia_solve_info {

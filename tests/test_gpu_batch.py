@@ -64,3 +64,30 @@ def test_batched_prescribed_values(gpu_ctx):
         ref = O.solve_static(m, solver=O.SOLVER_CHOLESKY, f=F[c])
         assert np.linalg.norm(U[c] - ref.u) / np.linalg.norm(ref.u) < 1e-8, c
         assert np.allclose(U[c][3 * tip + 2], -0.01)
+
+
+@pytest.mark.parametrize("pre", [dict(), dict(preconditioner=_lib.PRECOND_COARSE, coarse_nodes=150)],
+                         ids=["jacobi", "coarse"])
+def test_block_pcg_matches_direct_with_fewer_iterations(gpu_ctx, pre):
+    """One block Krylov space for the 32 cases of a launch (AXIA_KRYLOV_BLOCK):
+    every case (two launches: 40 cases, one of them without load) equals its
+    direct solve to 1e-8 at rtol 1e-10, with fewer iterations than the 32
+    separate recurrences, and a repeated solve gives the same bits."""
+    m = meshgen.block_c3d8_multiload(n=10, nrhs=40)
+    F = m.cload_batch.copy()
+    F[5] = 0.0
+    gpu_ctx.setup(m).assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+    U, info, rel = gpu_ctx.solve_batched(F, rtol=1e-10, krylov=_lib.KRYLOV_BLOCK, **pre)
+    assert np.all(rel <= 1e-10 * 1.0001)
+    ref = _direct_all(m, F)
+    for c in range(F.shape[0]):
+        if c == 5:
+            assert np.all(U[c] == 0.0)
+            continue
+        err = np.linalg.norm(U[c] - ref[c]) / np.linalg.norm(ref[c])
+        assert err < 1e-8, (c, err)
+    U1, i1, _ = gpu_ctx.solve_batched(F[:32], rtol=1e-10, **pre)
+    Ub, ib, _ = gpu_ctx.solve_batched(F[:32], rtol=1e-10, krylov=_lib.KRYLOV_BLOCK, **pre)
+    assert ib.iters < i1.iters, (ib.iters, i1.iters)
+    U2, _, _ = gpu_ctx.solve_batched(F, rtol=1e-10, krylov=_lib.KRYLOV_BLOCK, **pre)
+    assert np.array_equal(U, U2)

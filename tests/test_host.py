@@ -28,13 +28,13 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, name), name
     bound = {n for n, _, _ in _lib.SIGNATURES}
     assert set(declared) == bound, set(declared) ^ bound
-    assert lib.axia_gpu_abi_version() == 1
+    assert lib.axia_gpu_abi_version() == 2
 
 
 def test_struct_layouts_match_header():
     # field order and sizes of the ABI structs (x86-64 and aarch64 share them)
     assert ctypes.sizeof(_lib.Mesh) == 8 * 3 + 4 * 2 + 8 * 4
-    assert ctypes.sizeof(_lib.SolveOpts) == 8 + 8 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 4 + 4
+    assert ctypes.sizeof(_lib.SolveOpts) == 8 + 8 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 4 + 4 + 4 + 4
     assert ctypes.sizeof(_lib.SolveInfo) == 8 * 4 + 8 * 7 + 8 + 8 + 4 + 4
 
 
