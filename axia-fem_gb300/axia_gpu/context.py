@@ -171,6 +171,12 @@ class GpuContext:
         """Issue the context's work on a caller's cudaStream_t (None: own stream)."""
         self._check(self.lib.axia_gpu_set_stream(self.h, C.c_void_p(stream_handle or 0)), "set_stream")
 
+    def assemble_times(self):
+        """(element kernel ms, gather ms) of the last numeric assembly (CUDA events)."""
+        a, b = C.c_double(0.0), C.c_double(0.0)
+        self._check(self.lib.axia_gpu_assemble_times(self.h, C.byref(a), C.byref(b)), "assemble_times")
+        return a.value, b.value
+
     def n_blocks(self) -> int:
         """3x3 node blocks of the node-block form."""
         return int(self.lib.axia_gpu_node_blocks(self.h))

@@ -644,6 +644,13 @@ int64_t axia_gpu_sym_blocks(const axia_ctx* ctx, int64_t* lower_entries) {
 
 int64_t axia_gpu_node_blocks(const axia_ctx* ctx) { return ctx ? ctx->n_adj : -1; }
 
+int32_t axia_gpu_assemble_times(const axia_ctx* ctx, double* ms_element, double* ms_gather) {
+  if (!ctx || !ms_element || !ms_gather) return AXIA_ERR_INVALID_ARG;
+  *ms_element = ctx->ms_element;
+  *ms_gather = ctx->ms_gather;
+  return AXIA_OK;
+}
+
 int32_t axia_gpu_element_energy(axia_ctx* ctx, const double* u_full, const double* v_full, double* s) {
   if (!ctx || !u_full || !v_full || !s) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));

@@ -681,20 +681,31 @@ struct GatherArgs {
 };
 
 // incident elements whose column slots are looked up at once (x nodes per
-// element <= GATHER_SLOTS), and the Ke values per lane of one element's row block
+// element <= GATHER_SLOTS); their row blocks (3 x 3nn doubles each, at most
+// GATHER_STAGE doubles for a batch) are staged in shared memory together
 constexpr int GATHER_SLOTS = 64;
-constexpr int GATHER_VPL = 6;  // ceil(3 * 60 / 32): C3D20
+constexpr int GATHER_STAGE = 576;  // batch x 9 nn <= 64 / nn x 9 nn
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_wait_all() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
 
 __global__ void k_gather(GatherArgs g) {
   extern __shared__ __align__(16) unsigned char s_gather[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   const int nn = g.nn, ndof_e = 3 * nn, ke_size = ndof_e * ndof_e;
-  const int per = 3 * ndof_e, nv = (per + 31) / 32;
+  const int per = 3 * ndof_e;
   const int batch = max(1, GATHER_SLOTS / nn);
   unsigned char* base = s_gather + (size_t)warp * g.warp_stride;
-  double* acc = (double*)base;                                   // [max_adj][9]
-  int32_t* s_adj = (int32_t*)(base + (size_t)g.max_adj * 72);    // [max_adj]
+  double* stg = (double*)base;                                   // [GATHER_STAGE]
+  double* acc = stg + GATHER_STAGE;                              // [max_adj][9]
+  int32_t* s_adj = (int32_t*)(acc + (size_t)g.max_adj * 9);      // [max_adj]
   int32_t* s_slot = s_adj + g.max_adj;                           // [GATHER_SLOTS]
   int32_t* s_code = s_slot + GATHER_SLOTS;                       // [GATHER_SLOTS]
   for (int64_t a = (int64_t)blockIdx.x * wpb + warp; a < g.n_nodes; a += (int64_t)gridDim.x * wpb) {
@@ -719,32 +730,21 @@ __global__ void k_gather(GatherArgs g) {
         s_slot[t] = lo;
       }
       __syncwarp();
-      // element by element in ascending element order, the next element's
-      // row block loaded while the current one is summed
-      double cur[GATHER_VPL], nxt[GATHER_VPL];
-      auto load = [&](int j, double* v) {
+      // the batch's row blocks into shared memory with every copy in flight at
+      // once, then summed element by element in ascending element order
+      for (int j = 0; j < nbat; ++j) {
         const int32_t code = s_code[j];
         const double* rowblk = g.ke + (int64_t)(code >> 5) * ke_size + (int64_t)(3 * (code & 31)) * ndof_e;
-#pragma unroll
-        for (int m = 0; m < GATHER_VPL; ++m) {
-          const int t = lane + 32 * m;
-          v[m] = (m < nv && t < per) ? __ldcs(rowblk + t) : 0.0;
-        }
-      };
-      load(0, cur);
+        for (int t = lane; t < per; t += 32) cp_async8(stg + j * per + t, rowblk + t);
+      }
+      cp_async_commit_wait_all();
+      __syncwarp();
       for (int j = 0; j < nbat; ++j) {
-        if (j + 1 < nbat) load(j + 1, nxt);
-#pragma unroll
-        for (int m = 0; m < GATHER_VPL; ++m) {
-          const int t = lane + 32 * m;
-          if (m < nv && t < per) {
-            const int i = t / ndof_e, c = t - i * ndof_e;
-            acc[s_slot[j * nn + c / 3] * 9 + i * 3 + (c % 3)] += cur[m];
-          }
+        for (int t = lane; t < per; t += 32) {
+          const int i = t / ndof_e, c = t - i * ndof_e;
+          acc[s_slot[j * nn + c / 3] * 9 + i * 3 + (c % 3)] += stg[j * per + t];
         }
         __syncwarp();
-#pragma unroll
-        for (int m = 0; m < GATHER_VPL; ++m) cur[m] = nxt[m];
       }
     }
     // K_ff in CSR, and K_fp u0 -- skipped for a node-block-only assembly
@@ -829,7 +829,8 @@ __global__ void k_gather(GatherArgs g) {
 }
 
 int run_gather(axia_ctx* ctx, GatherArgs args) {
-  size_t per_warp = (size_t)args.max_adj * 9 * sizeof(double) + (size_t)(args.max_adj + 2 * GATHER_SLOTS) * 4;
+  size_t per_warp = (size_t)(GATHER_STAGE + args.max_adj * 9) * sizeof(double) +
+                    (size_t)(args.max_adj + 2 * GATHER_SLOTS) * 4;
   per_warp = (per_warp + 15) & ~(size_t)15;
   if (per_warp > 200 * 1024) return set_error(ctx, AXIA_ERR_TOO_LARGE, "node adjacency too large for the gather");
   int warps = 8;
@@ -1114,6 +1115,16 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
     ctx->ke_elems = (size_t)(ctx->n_elem * kesz);
   }
   AXIA_TRY(reset_dev_status(ctx));
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  for (auto& e : ev) AXIA_CUDA(ctx, cudaEventCreate(&e));
+  struct EvGuard {
+    cudaEvent_t* e;
+    ~EvGuard() {
+      for (int k = 0; k < 3; ++k)
+        if (e[k]) cudaEventDestroy(e[k]);
+    }
+  } ev_guard{ev};
+  cudaEventRecord(ev[0], s);
   ElemArgs ea{};
   ea.n_elem = ctx->n_elem;
   ea.conn = ctx->d_conn;
@@ -1127,6 +1138,7 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   ea.vol_out = nullptr;
   ea.status = ctx->d_status;
   AXIA_TRY(run_element_ke(ctx, ctx->nn, ctx->reduced, ea));
+  cudaEventRecord(ev[1], s);
   if (csr64 && !ctx->d_val) AXIA_TRY(dev_alloc(ctx, &ctx->d_val, ctx->nnz));
   if (csr32 && !ctx->d_val32) AXIA_TRY(dev_alloc(ctx, &ctx->d_val32, ctx->nnz));
   if (!ctx->d_diag) AXIA_TRY(dev_alloc(ctx, &ctx->d_diag, ctx->n_free));
@@ -1174,8 +1186,18 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   g.nb = ctx->nbq;
   g.uval = sym32 ? ctx->d_uval : nullptr;
   g.uptr = ctx->d_uptr;
+  // the gather's interval also holds the first-use allocations and clears above
+  // (none after the first assembly of a mesh)
   AXIA_TRY(run_gather(ctx, g));
+  cudaEventRecord(ev[2], s);
   AXIA_CUDA(ctx, cudaStreamSynchronize(s));
+  {
+    float m1 = 0.f, m2 = 0.f;
+    cudaEventElapsedTime(&m1, ev[0], ev[1]);
+    cudaEventElapsedTime(&m2, ev[1], ev[2]);
+    ctx->ms_element = m1;
+    ctx->ms_gather = m2;
+  }
   DevStatus hs;
   AXIA_TRY(read_dev_status(ctx, &hs));
   ctx->have_csr64 = ctx->have32 = ctx->have_bsr64 = ctx->have_bsr32 = ctx->have_sym32 = false;

@@ -375,28 +375,42 @@ __device__ __forceinline__ void coarse_restrict_m(const CoarseArgs& C, const flo
 
 // Y = M R_c; per column r_c . y into partials[(slot0 + col) * G + block].
 // Tasks of 16 rows go to the blocks in turn; a thread owns one (row, load
-// case): the warp of a row streams that row of M once (broadcast loads) and
-// reads R_c row by row (coalesced, shared by the block's warps through L1).
-// The per-column sums run over the block's tasks and rows in a fixed order.
+// case): the warp of a row streams that row of M once (broadcast loads), and
+// R_c passes through shared memory in tiles of 64 rows shared by the block's
+// 16 warps (one L2 read of each tile per task instead of a dependent L2
+// round trip per row of R_c).  The per-column sums run over the block's
+// tasks and rows in a fixed order.
 __device__ __forceinline__ void coarse_solve_m(const CoarseArgs& C, int gwarp, int nwarps, int lane, double* partials,
                                                int slot0) {
   constexpr int TR = PCG_THREADS / NR;  // rows per task
+  constexpr int TJ = 64;                // rows of R_c per shared-memory tile
   __shared__ float s_prod[PCG_THREADS];
   __shared__ float s_cc[NR];
+  __shared__ __align__(16) float s_rc[TJ][NR];
   const int r = threadIdx.x / NR, c = threadIdx.x % NR;
   if (threadIdx.x < NR) s_cc[threadIdx.x] = 0.f;
   const int ntask = (C.nc + TR - 1) / TR;
   for (int task = blockIdx.x; task < ntask; task += gridDim.x) {
     const int i = task * TR + r;
+    const float* mrow = C.minv + (size_t)min(i, C.nc - 1) * C.ldm;
+    float y = 0.f;
+    for (int j0 = 0; j0 < C.nc; j0 += TJ) {
+      const int nj = min(TJ, C.nc - j0);
+      __syncthreads();
+      for (int t = threadIdx.x; t < TJ * NR / 4; t += PCG_THREADS) {
+        const int jj = t / (NR / 4), cc = 4 * (t % (NR / 4));
+        *reinterpret_cast<float4*>(&s_rc[jj][cc]) =
+            jj < nj ? __ldcg(reinterpret_cast<const float4*>(C.rc_m + (size_t)(j0 + jj) * NR + cc))
+                    : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      __syncthreads();
+#pragma unroll 16
+      for (int jj = 0; jj < nj; ++jj) y = fmaf(__ldg(mrow + j0 + jj), s_rc[jj][c], y);
+    }
     float prod = 0.f;
     if (i < C.nc) {
-      const float* mrow = C.minv + (size_t)i * C.ldm;
-      const float* rcol = C.rc_m + c;
-      float y = 0.f;
-#pragma unroll 8
-      for (int j = 0; j < C.nc; ++j) y = fmaf(__ldg(mrow + j), rcol[(size_t)j * NR], y);
       C.yc_m[(size_t)i * NR + c] = y;
-      prod = rcol[(size_t)i * NR] * y;
+      prod = __ldcg(C.rc_m + (size_t)i * NR + c) * y;
     }
     s_prod[threadIdx.x] = prod;
     __syncthreads();
@@ -959,80 +973,78 @@ __global__ void __launch_bounds__(BT) k_blk_residual64(BsrMatM<double> M, const 
   }
 }
 
-// The small dense steps (one warp, FP64, lane = column):
+// The small dense steps (one block of 32 x 32 threads, FP64, thread (r, c)
+// owns entry (r, c); every elimination step is one synchronised parallel
+// update, so a step costs a barrier instead of a serial loop):
 //   mode 0 (alpha): G = Gram 0 (P^T Q, kept as Gm), S = Gram 1 (P^T R):
 //           alpha = Gm^-1 S, zero in the columns of `frozen`
 //   mode 1 (beta):  Gm (kept), S = Gram 1 (Q^T Z): beta = -Gm^-1 S
 //   mode 2 (orth):  G = Gram 2 (W^T W): T = D L^-T for D G D = L L^T,
 //           D = diag(G)^-1/2; a scaled pivot below 1e-6 (or a zero column)
-//           drops that direction (its column of T is zero)
+//           drops that direction (its row and column of T are zero)
 // gram: [4][32][32] (Gm, S, WtW, norms); small: [3][32][32] FP32 alpha, beta, T.
 // Gm's factor is recomputed each time (a 32 x 32 Cholesky is a few microseconds).
-__global__ void __launch_bounds__(32) k_blk_small(int mode, unsigned frozen, const double* gram, float* small) {
+__global__ void __launch_bounds__(NR * NR) k_blk_small(int mode, unsigned frozen, const double* gram, float* small) {
   __shared__ double L[NR][NR + 1];
   __shared__ double S[NR][NR + 1];
   __shared__ double dsc[NR];
   __shared__ int drop[NR];
-  const int lane = threadIdx.x;
+  __shared__ double s_thr;
+  const int r = threadIdx.x / NR, c = threadIdx.x % NR;
   const double* G = gram + (mode == 2 ? 2 : 0) * NR * NR;
-  // scaling (orth) or none
-  const double gd = G[lane * NR + lane];
-  if (mode == 2) {
-    dsc[lane] = gd > 1e-300 ? 1.0 / sqrt(gd) : 0.0;
-  } else {
-    dsc[lane] = 1.0;
+  if (r == 0) {
+    const double gd = G[c * NR + c];
+    dsc[c] = mode != 2 ? 1.0 : (gd > 1e-300 ? 1.0 / sqrt(gd) : 0.0);
   }
-  __syncwarp();
-  for (int i = 0; i < NR; ++i) L[i][lane] = G[i * NR + lane] * dsc[i] * dsc[lane];
-  if (mode != 2)
-    for (int i = 0; i < NR; ++i) S[i][lane] = gram[NR * NR + i * NR + lane];
-  __syncwarp();
-  // Cholesky L L^T of the (scaled) matrix, in place in the lower triangle
-  double dmax = 0.0;
-  for (int i = 0; i < NR; ++i) dmax = fmax(dmax, L[i][i]);
-  const double thr = mode == 2 ? 1e-6 : 1e-12 * dmax;
+  __syncthreads();
+  L[r][c] = G[r * NR + c] * dsc[r] * dsc[c];
+  S[r][c] = mode == 2 ? (r == c ? 1.0 : 0.0) : gram[NR * NR + r * NR + c];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double dmax = 0.0;
+    for (int i = 0; i < NR; ++i) dmax = fmax(dmax, L[i][i]);
+    s_thr = mode == 2 ? 1e-6 : 1e-12 * dmax;
+  }
+  __syncthreads();
+  // right-looking Cholesky L L^T in the lower triangle; a dropped pivot gets a
+  // unit diagonal and a zero column, so it drops out of the later steps
   for (int k = 0; k < NR; ++k) {
-    const double piv = L[k][k];
-    const bool dr = !(piv > thr) || (mode == 2 && dsc[k] == 0.0);
-    __syncwarp();
-    if (lane == 0) drop[k] = dr;
-    if (lane > k) L[lane][k] = dr ? 0.0 : L[lane][k] / sqrt(piv);
-    __syncwarp();
-    if (lane == k) L[k][k] = dr ? 1.0 : sqrt(piv);
-    __syncwarp();
-    if (lane > k)
-      for (int j = k + 1; j <= lane; ++j) L[lane][j] -= L[lane][k] * L[j][k];
-    __syncwarp();
-  }
-  if (mode == 2) {
-    // T = D L^-T: column c of L^-T solves L^T t = e_c (upper triangular back substitution)
-    double t[NR];
-    for (int i = NR - 1; i >= 0; --i) {
-      double v = i == lane ? 1.0 : 0.0;
-      for (int j = i + 1; j < NR; ++j) v -= L[j][i] * t[j];
-      t[i] = (i <= lane) ? v / L[i][i] : 0.0;
+    if (threadIdx.x == 0) {
+      const double piv = L[k][k];
+      const int dr = !(piv > s_thr) || (mode == 2 && dsc[k] == 0.0);
+      drop[k] = dr;
+      L[k][k] = dr ? 1.0 : sqrt(piv);
     }
-    for (int i = 0; i < NR; ++i)
-      small[2 * NR * NR + i * NR + lane] = (drop[lane] || drop[i]) ? 0.f : (float)(dsc[i] * t[i]);
-    return;
+    __syncthreads();
+    if (c == 0 && r > k) L[r][k] = drop[k] ? 0.0 : L[r][k] / L[k][k];
+    __syncthreads();
+    if (r > k && c > k && c <= r) L[r][c] -= L[r][k] * L[c][k];
+    __syncthreads();
   }
-  // X = Gm^-1 S column by column (lane = column of S), dropped directions zero
-  double y[NR];
-  for (int i = 0; i < NR; ++i) {
-    double v = S[i][lane];
-    for (int j = 0; j < i; ++j) v -= L[i][j] * y[j];
-    y[i] = drop[i] ? 0.0 : v / L[i][i];
+  if (mode != 2) {
+    // forward substitution L y = S (every column c of S at once)
+    for (int i = 0; i < NR; ++i) {
+      if (r == i) S[i][c] = drop[i] ? 0.0 : S[i][c] / L[i][i];
+      __syncthreads();
+      if (r > i) S[r][c] -= L[r][i] * S[i][c];
+      __syncthreads();
+    }
   }
+  // backward substitution L^T x = y (mode 2: x = L^-T from S = I)
   for (int i = NR - 1; i >= 0; --i) {
-    double v = y[i];
-    for (int j = i + 1; j < NR; ++j) v -= L[j][i] * y[j];
-    y[i] = drop[i] ? 0.0 : v / L[i][i];
+    if (r == i) S[i][c] = drop[i] ? 0.0 : S[i][c] / L[i][i];
+    __syncthreads();
+    if (r < i) S[r][c] -= L[i][r] * S[i][c];
+    __syncthreads();
   }
-  const bool fz = (frozen >> lane) & 1u;
-  for (int i = 0; i < NR; ++i) {
-    const double v = mode == 0 ? (fz ? 0.0 : y[i]) : -y[i];
-    small[mode * NR * NR + i * NR + lane] = (float)v;
-  }
+  double v;
+  if (mode == 2)
+    v = (drop[r] || drop[c]) ? 0.0 : dsc[r] * S[r][c];
+  else if (mode == 0)
+    v = ((frozen >> c) & 1u) ? 0.0 : S[r][c];
+  else
+    v = -S[r][c];
+  small[mode * NR * NR + r * NR + c] = (float)v;
 }
 
 // R32 = (float) B, X = 0, X32 = 0, per-case sums of squares of B to part[block][0][..]
@@ -1299,7 +1311,7 @@ struct BlockRun {
     count(1);
   }
   void small_step(int mode, unsigned frozen) {
-    k_blk_small<<<1, 32, 0, s>>>(mode, frozen, ctx->d_bgram, ctx->d_bsmall);
+    k_blk_small<<<1, NR * NR, 0, s>>>(mode, frozen, ctx->d_bgram, ctx->d_bsmall);
     count(1);
   }
   // Z = M R (diagonal, plus the coarse part)

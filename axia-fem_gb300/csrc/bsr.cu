@@ -339,9 +339,7 @@ __device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const Coar
   return true;
 }
 
-// NODES: the single-system kernel, whose coarse space may restrict in node
-// order (C.n_nchunks > 0); the multi-mesh groups restrict by subdomain chunks.
-template <int L32, int V32, int L64, int V64, bool COARSE = false, bool SYM = false, bool NODES = false>
+template <int L32, int V32, int L64, int V64, bool COARSE = false, bool SYM = false>
 __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const CoarseArgs& C, const SolveRange& R) {
   const int n0 = R.node0, n1 = R.node1;
   const int i0 = 3 * n0;
@@ -381,10 +379,7 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
   if constexpr (COARSE) {
     if (!converged) {  // p = D^-1 b + Z M Z^T b
       float rz_c = 0.f;
-      if (NODES && C.n_nchunks > 0)
-        coarse_restrict_nodes(C, n1, P.r32, gwarp, nwarps, lane);
-      else
-        coarse_restrict(C, P.r32, gwarp, nwarps, lane);
+      coarse_restrict(C, P.r32, gwarp, nwarps, lane);
       if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
       if (!coarse_step(P, C, R, gwarp, nwarps, lane, &rz_c)) return;
       rz += rz_c;
@@ -429,11 +424,7 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
     const float alpha = rz / pq;
     float rr_p = 0.f, rzn_p = 0.f;
     if constexpr (COARSE) {
-      if (NODES && C.n_nchunks > 0)
-        coarse_update_restrict_nodes(C, n1, alpha, P.x32, P.p32, P.q32, P.r32, P.dinv32, gwarp, nwarps, lane, rr_p,
-                                     rzn_p);
-      else
-        coarse_update_restrict(C, alpha, P.x32, P.p32, P.q32, P.r32, P.dinv32, gwarp, nwarps, lane, rr_p, rzn_p);
+      coarse_update_restrict(C, alpha, P.x32, P.p32, P.q32, P.r32, P.dinv32, gwarp, nwarps, lane, rr_p, rzn_p);
     } else {
       for (int i = i0 + tid; i < nd; i += nth) {
         P.x32[i] = fmaf(alpha, P.p32[i], P.x32[i]);
@@ -495,10 +486,7 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
         break;
       }
       if constexpr (COARSE) {  // r was replaced: restrict it again
-        if (NODES && C.n_nchunks > 0)
-          coarse_restrict_nodes(C, n1, P.r32, gwarp, nwarps, lane);
-        else
-          coarse_restrict(C, P.r32, gwarp, nwarps, lane);
+        coarse_restrict(C, P.r32, gwarp, nwarps, lane);
         if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
       }
     }
@@ -538,7 +526,7 @@ __host__ __device__ constexpr int rel_min_blocks() { return V32 >= 4 ? 2 : 3; }
 template <int L32, int V32, bool COARSE = false, bool SYM = false>
 __global__ void __launch_bounds__(PCG_THREADS, rel_min_blocks<V32>()) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
   const SolveRange R{0, P.M64.n_nodes, blockIdx.x, gridDim.x, P.partials, P.totals, P.bar, P.out};
-  reliable_body<L32, V32, kL64, rel_v64<V32>(), COARSE, SYM, true>(P, P.C, R);
+  reliable_body<L32, V32, kL64, rel_v64<V32>(), COARSE, SYM>(P, P.C, R);
 }
 
 // Independent systems on disjoint node ranges of one node-block matrix (the

@@ -94,18 +94,7 @@ struct CoarseState {
   float* rc_m = nullptr;         // [ncp][32]
   float* yc_m = nullptr;         // [ncp][32]
   float* yc = nullptr;           // [ncp]
-  // node-order restriction of a single system (CoarseArgs::n_nchunks ...)
-  int* run_base = nullptr;       // [n_nchunks + 1]
-  int* slot_ptr = nullptr;       // [n_sub + 1]
-  int* slot_list = nullptr;      // [n_slots]
-  float* npart = nullptr;        // [n_slots][6]
-  int* ncnt = nullptr;           // [n_sub]
   void release(axia_ctx* ctx) {
-    dev_release(ctx, run_base);
-    dev_release(ctx, slot_ptr);
-    dev_release(ctx, slot_list);
-    dev_release(ctx, npart);
-    dev_release(ctx, ncnt);
     dev_release(ctx, sub_node);
     dev_release(ctx, chunk);
     dev_release(ctx, chunk_ptr);
@@ -1050,41 +1039,6 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     if ((st = dev_alloc(ctx, &S->minv, (size_t)S->blk_elems))) break;
     AXIA_CUDA(ctx, cudaMemsetAsync(S->yc, 0, A.ncp * sizeof(float), ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    // node-order restriction (one system): the runs of equal subdomain within
-    // every 32-node warp chunk, and each subdomain's slots in ascending order
-    A.n_nchunks = 0;
-    if (nm == 1 && n > 0) {
-      std::vector<int> hsub((size_t)n);
-      if ((st = copy_to_host(ctx, hsub.data(), d_sub, (size_t)n))) break;
-      const int nch = (int)((n + 31) / 32);
-      std::vector<int> run_base((size_t)nch + 1, 0), slot_sub;
-      for (int j = 0; j < nch; ++j) {
-        run_base[j] = (int)slot_sub.size();
-        for (int64_t a = 32LL * j; a < std::min<int64_t>(32LL * j + 32, n); ++a)
-          if (a == 32LL * j || hsub[a] != hsub[a - 1]) slot_sub.push_back(hsub[a]);
-      }
-      run_base[nch] = (int)slot_sub.size();
-      std::vector<int> slot_ptr((size_t)n_sub + 1, 0), slot_list(slot_sub.size());
-      for (int I : slot_sub) slot_ptr[I + 1]++;
-      for (int I = 0; I < n_sub; ++I) slot_ptr[I + 1] += slot_ptr[I];
-      std::vector<int> fill(slot_ptr.begin(), slot_ptr.end() - 1);
-      for (size_t k = 0; k < slot_sub.size(); ++k) slot_list[fill[slot_sub[k]]++] = (int)k;
-      if ((st = dev_alloc(ctx, &S->run_base, run_base.size()))) break;
-      if ((st = copy_to_device(ctx, S->run_base, run_base.data(), run_base.size()))) break;
-      if ((st = dev_alloc(ctx, &S->slot_ptr, slot_ptr.size()))) break;
-      if ((st = copy_to_device(ctx, S->slot_ptr, slot_ptr.data(), slot_ptr.size()))) break;
-      if ((st = dev_alloc(ctx, &S->slot_list, std::max<size_t>(slot_list.size(), 1)))) break;
-      if ((st = copy_to_device(ctx, S->slot_list, slot_list.data(), slot_list.size()))) break;
-      if ((st = dev_alloc(ctx, &S->npart, std::max<size_t>(6 * slot_sub.size(), 6)))) break;
-      if ((st = dev_alloc(ctx, &S->ncnt, (size_t)n_sub))) break;
-      AXIA_CUDA(ctx, cudaMemsetAsync(S->ncnt, 0, n_sub * sizeof(int), ctx->stream));
-      A.n_nchunks = nch;
-      A.run_base = S->run_base;
-      A.slot_ptr = S->slot_ptr;
-      A.slot_list = S->slot_list;
-      A.npart = S->npart;
-      A.ncnt = S->ncnt;
-    }
     A.sub_node = S->sub_node;
     A.chunk = S->chunk;
     A.chunk_ptr = S->chunk_ptr;

@@ -128,110 +128,6 @@ __device__ __forceinline__ void coarse_update_restrict(const CoarseArgs& C, floa
   }
 }
 
-// Node-order restriction: lane l of the warp holds node 32 j + l of chunk j
-// with its subdomain `sub` (0xffffffff past the system) and Z_a^T r_a in v.
-// A segmented inclusive scan over the lanes (fixed shuffle pattern) sums each
-// run of consecutive nodes of one subdomain; the run's last lane stores it in
-// the run's slot; the warp that brings a subdomain's last run sums its slots
-// in slot order (every lane a fixed stride, then a warp sum) into r_c and
-// re-arms the counter.  Same bits whichever warp finishes a subdomain.
-__device__ __forceinline__ void coarse_runs_finish(const CoarseArgs& C, int j, unsigned sub, float (&v)[6],
-                                                   int lane) {
-  const unsigned full = 0xffffffffu, le = full >> (31 - lane);
-  const unsigned prev = __shfl_up_sync(full, sub, 1), next = __shfl_down_sync(full, sub, 1);
-  const bool head = lane == 0 || prev != sub;
-  const unsigned heads = __ballot_sync(full, head);
-  const int start = 31 - __clz(heads & le);
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    float t[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) t[k] = __shfl_up_sync(full, v[k], d);
-    if (lane - d >= start)
-#pragma unroll
-      for (int k = 0; k < 6; ++k) v[k] += t[k];
-  }
-  const bool tail = (lane == 31 || next != sub) && sub != 0xffffffffu;
-  if (tail) {
-    const int slot = __ldg(C.run_base + j) + __popc(heads & le) - 1;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) C.npart[6 * slot + k] = v[k];
-  }
-  __threadfence();
-  __syncwarp();
-  int last = 0;
-  if (tail) last = atomicAdd(C.ncnt + sub, 1) == __ldg(C.slot_ptr + sub + 1) - __ldg(C.slot_ptr + sub) - 1;
-  unsigned lasts = __ballot_sync(full, last);
-  while (lasts) {
-    const int src = __ffs(lasts) - 1;
-    lasts &= lasts - 1;
-    const unsigned I = __shfl_sync(full, sub, src);
-    __threadfence();
-    const int s0 = __ldg(C.slot_ptr + I), s1 = __ldg(C.slot_ptr + I + 1);
-    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int s = s0 + lane; s < s1; s += 32) {
-      const int sl = __ldg(C.slot_list + s);
-#pragma unroll
-      for (int k = 0; k < 6; ++k) acc[k] += __ldcg(C.npart + 6 * sl + k);
-    }
-#pragma unroll
-    for (int k = 0; k < 6; ++k) acc[k] = warp_sum(acc[k]);
-    if (lane < 6) {
-      const float x = lane == 0 ? acc[0] : lane == 1 ? acc[1] : lane == 2 ? acc[2] : lane == 3 ? acc[3] : lane == 4 ? acc[4] : acc[5];
-      C.rc[6 * I + lane] = x;
-    }
-    if (lane == 0) atomicExch(C.ncnt + I, 0);
-  }
-}
-
-// r_c = Z^T r, nodes in order (after an FP64 residual replaced r, and at the start)
-__device__ __forceinline__ void coarse_restrict_nodes(const CoarseArgs& C, int n1, const float* r, int gwarp,
-                                                      int nwarps, int lane) {
-  for (int j = gwarp; j < C.n_nchunks; j += nwarps) {
-    const int a = 32 * j + lane;
-    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    unsigned sub = 0xffffffffu;
-    if (a < n1) {
-      const float4 g = __ldg(C.geo + a);
-      const unsigned m = geo_bits(g);
-      sub = m >> 3;
-      zt_add(g, (m & 1u) ? r[3 * a] : 0.f, (m & 2u) ? r[3 * a + 1] : 0.f, (m & 4u) ? r[3 * a + 2] : 0.f, v);
-    }
-    coarse_runs_finish(C, j, sub, v, lane);
-  }
-}
-
-// The CG update x += alpha p, r -= alpha q in node order (coalesced), with the
-// partial sums of r.r and r.D^-1 r and the node-order restriction of the new r.
-__device__ __forceinline__ void coarse_update_restrict_nodes(const CoarseArgs& C, int n1, float alpha, float* x,
-                                                             const float* p, const float* q, float* r,
-                                                             const float* dinv, int gwarp, int nwarps, int lane,
-                                                             float& rr_p, float& rz_p) {
-  for (int j = gwarp; j < C.n_nchunks; j += nwarps) {
-    const int a = 32 * j + lane;
-    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    unsigned sub = 0xffffffffu;
-    if (a < n1) {
-      const float4 g = __ldg(C.geo + a);
-      const unsigned m = geo_bits(g);
-      sub = m >> 3;
-      float rv[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const int i = 3 * a + d;
-        x[i] = fmaf(alpha, p[i], x[i]);
-        const float ri = fmaf(-alpha, q[i], r[i]);
-        r[i] = ri;
-        rr_p = fmaf(ri, ri, rr_p);
-        rz_p = fmaf(ri, ri * dinv[i], rz_p);
-        rv[d] = ((m >> d) & 1u) ? ri : 0.f;
-      }
-      zt_add(g, rv[0], rv[1], rv[2], v);
-    }
-    coarse_runs_finish(C, j, sub, v, lane);
-  }
-}
-
 // The block's part of r_c into shared memory (zero past its unknowns), then
 // rows of y = M r_c over the warps of the group.  Returns this thread's share
 // of r_c . y (nonzero on lane 0 of warps that own rows).

@@ -412,6 +412,7 @@ struct axia_ctx {
   int64_t assemble_gen = 0;     // numeric assemblies so far (the operator follows K)
 
   double ms_setup = 0.0, ms_assemble = 0.0;
+  double ms_element = 0.0, ms_gather = 0.0;  // kernel times of the last numeric assembly (CUDA events)
   int64_t last_bad = -1;
 
   // device blocks of a released mesh state, kept for the next setup of the

@@ -116,7 +116,7 @@ struct MeshGroup {
 constexpr int GROUP_SLOTS = 4;  // partial-sum slots per group: S_PQ, S_RR, S_RZ, S_RC
 
 constexpr int COARSE_MAX = 4096;    // coarse unknowns (6 per subdomain, padded to 64)
-constexpr int COARSE_CHUNK = 256;   // nodes per restriction chunk
+constexpr int COARSE_CHUNK = 64;    // nodes per restriction chunk (a few per warp: every warp busy)
 constexpr int S_RC = 3;             // partial-sum slot of r_c . y
 
 struct CoarseArgs {
@@ -140,16 +140,6 @@ struct CoarseArgs {
   float* part_m;
   float* rc_m;
   float* yc_m;
-  // node-order restriction of a single system (0 chunks: not built): warp
-  // chunk j = nodes [32 j, 32 j + 32); its runs of nodes of one subdomain get
-  // the slots run_base[j] ..; subdomain I sums the slots slot_list[slot_ptr[I]
-  // .. slot_ptr[I+1]) (ascending) once its last run has arrived (ncnt)
-  int n_nchunks;
-  const int* run_base;   // [n_nchunks + 1]
-  const int* slot_ptr;   // [n_sub + 1]
-  const int* slot_list;  // [n_slots]
-  float* npart;          // [n_slots][6]
-  int* ncnt;             // [n_sub]
 };
 
 struct BsrReliableArgs {

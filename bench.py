@@ -183,6 +183,28 @@ def batch_update_bytes(nblocks, n_nodes, nrhs=32):
     return (9 * 8 + 4) * nblocks + 4 * (n_nodes + 1) + nrhs * nd * (8 + 8 + 4 + 4 + 8 + 8 + 4)
 
 
+def element_fp64_flops(nn, ng):
+    """FP64 operations of element_ke_kernel per element (FMA = 2): per Gauss point
+    J (9 nn FMA), the cofactors (9 MUL + 9 FMA), det J and w / det J (2 FMA,
+    2 MUL/DIV), c_a = adj(J)^T dN_a (3 nn x (1 MUL + 2 FMA)) and h_a = (w / det J) c_a
+    (3 nn MUL); A_ab over the NE upper-triangle entries (NE FMA per Gauss point);
+    K_ab from A (NE MUL + NE FMA, 3 FMA per node pair for the trace term) and
+    the traces (2 ADD per node pair)."""
+    ne = 9 * nn * (nn - 1) // 2 + 6 * nn
+    nb = nn * (nn + 1) // 2
+    fma = ng * (9 * nn + 9 + 2 + 6 * nn) + ne * ng + ne + 3 * nb
+    other = ng * (9 + 2 + 3 * nn + 3 * nn) + ne + 2 * nb
+    return 2 * fma + other
+
+
+def gather_bytes(n_elem, nn, nblocks, n_nodes):
+    """Algorithmic bytes of the gather into the node-block forms (FP64 + FP32):
+    each (element, node) reads its 3 rows of Ke (9 nn doubles) and its element
+    code, the node's adjacency and incidence; the 9 value planes are written in
+    FP64 and FP32 and the inverse diagonals (FP64, FP32) once."""
+    return n_elem * nn * (9 * nn * 8 + 4 + 4 * nn) + nblocks * (4 + 9 * 12) + 3 * n_nodes * 12 + 16 * n_nodes
+
+
 def recover_bytes(n_elem, nn, n_nodes):
     """Algorithmic bytes of stress recovery + reactions: per element the
     connectivity twice, E once, 9 doubles per (element, node) written and read
@@ -813,6 +835,29 @@ def main():
     for v in spmv.values():
         v["frac_of_hbm"] = v["gbs"] / hbm
 
+    # assembly phases (CUDA events inside the library): the FP64-pipe-bound element
+    # kernel against the measured FP64 FMA rate, the gather against HBM
+    asm_t = []
+    for _ in range(4):
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        asm_t.append(ctx.assemble_times())
+    ms_el = statistics.median(a[0] for a in asm_t[1:])
+    ms_ga = statistics.median(a[1] for a in asm_t[1:])
+    fp64_peak = ctx.fma_rate(L.PREC_FP64)
+    fp32_peak = ctx.fma_rate(L.PREC_MIXED)
+    el_flops = element_fp64_flops(model.nn, 8) * model.n_elem
+    ga_bytes = gather_bytes(model.n_elem, model.nn, nblocks, model.n_nodes)
+    assembly = {"ms_element": ms_el, "ms_gather": ms_ga,
+                "element": {"kernel": "element_ke_kernel<8,8,8>", "bound": "fp64 pipe",
+                            "fp64_flops": el_flops, "achieved_tflops": el_flops / (ms_el * 1e-3) / 1e12,
+                            "peak_tflops": fp64_peak, "frac": el_flops / (ms_el * 1e-3) / 1e12 / fp64_peak,
+                            "peak_source": "axia_gpu_fma_rate (FP64 FMA chains on every SM, CUDA events)",
+                            "canonical_flops_per_element": 32872},
+                "gather": {"kernel": "k_gather", "bound": "hbm", "bytes": ga_bytes,
+                           "achieved_gbs": ga_bytes / (ms_ga * 1e-3) / 1e9,
+                           "frac": ga_bytes / (ms_ga * 1e-3) / 1e9 / hbm},
+                "fp32_fma_tflops_measured": fp32_peak}
+
     # post-solve recovery of the mixed solution: nodal stress, strain, von Mises,
     # element means and reactions K u - f (two kernels)
     nn_ = model.n_nodes
@@ -1013,6 +1058,7 @@ def main():
         "roofline_mixed_csr_pcg": {"bound": "hbm", "achieved": achmc, "peak": hbm, "unit": "GB/s",
                                    "frac": achmc / hbm, "kernel": "pcg_reliable_kernel (CSR FP32 + FP64 updates)",
                                    "ms_per_launch": kmc_ms, "bytes_per_launch": bytesmc},
+        "assembly": assembly,
         "oracle_check": oracle_check,
         "same_sample": same,
         "gpu_launches": int(la64 + lamx + lamc + laco + lacs),

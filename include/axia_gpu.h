@@ -287,6 +287,11 @@ AXIA_API int32_t axia_gpu_sym_spmv_device(axia_ctx* ctx, const float* x_dev, flo
  * context) and, in *lower_entries, its lower-list entries. */
 AXIA_API int64_t axia_gpu_sym_blocks(const axia_ctx* ctx, int64_t* lower_entries);
 
+/* Device times (CUDA events, milliseconds) of the last numeric assembly's two
+ * phases: the element stiffness kernels and the gather into the matrix forms
+ * (with Dirichlet elimination).  No reference counterpart. */
+AXIA_API int32_t axia_gpu_assemble_times(const axia_ctx* ctx, double* ms_element, double* ms_gather);
+
 /* Number of 3x3 node blocks of the node-block form (node adjacency entries). */
 AXIA_API int64_t axia_gpu_node_blocks(const axia_ctx* ctx);
 
