@@ -681,31 +681,20 @@ struct GatherArgs {
 };
 
 // incident elements whose column slots are looked up at once (x nodes per
-// element <= GATHER_SLOTS); their row blocks (3 x 3nn doubles each, at most
-// GATHER_STAGE doubles for a batch) are staged in shared memory together
+// element <= GATHER_SLOTS), and the Ke values per lane of one element's row block
 constexpr int GATHER_SLOTS = 64;
-constexpr int GATHER_STAGE = 576;  // batch x 9 nn <= 64 / nn x 9 nn
-
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit_wait_all() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
-  asm volatile("cp.async.wait_group 0;" ::: "memory");
-}
+constexpr int GATHER_VPL = 6;  // ceil(3 * 60 / 32): C3D20
 
 __global__ void k_gather(GatherArgs g) {
   extern __shared__ __align__(16) unsigned char s_gather[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   const int nn = g.nn, ndof_e = 3 * nn, ke_size = ndof_e * ndof_e;
-  const int per = 3 * ndof_e;
+  const int per = 3 * ndof_e, nv = (per + 31) / 32;
   const int batch = max(1, GATHER_SLOTS / nn);
   unsigned char* base = s_gather + (size_t)warp * g.warp_stride;
-  double* stg = (double*)base;                                   // [GATHER_STAGE]
-  double* acc = stg + GATHER_STAGE;                              // [max_adj][9]
-  int32_t* s_adj = (int32_t*)(acc + (size_t)g.max_adj * 9);      // [max_adj]
+  double* acc = (double*)base;                                   // [max_adj][9]
+  int32_t* s_adj = (int32_t*)(base + (size_t)g.max_adj * 72);    // [max_adj]
   int32_t* s_slot = s_adj + g.max_adj;                           // [GATHER_SLOTS]
   int32_t* s_code = s_slot + GATHER_SLOTS;                       // [GATHER_SLOTS]
   for (int64_t a = (int64_t)blockIdx.x * wpb + warp; a < g.n_nodes; a += (int64_t)gridDim.x * wpb) {
@@ -730,21 +719,32 @@ __global__ void k_gather(GatherArgs g) {
         s_slot[t] = lo;
       }
       __syncwarp();
-      // the batch's row blocks into shared memory with every copy in flight at
-      // once, then summed element by element in ascending element order
-      for (int j = 0; j < nbat; ++j) {
+      // element by element in ascending element order, the next element's
+      // row block loaded while the current one is summed
+      double cur[GATHER_VPL], nxt[GATHER_VPL];
+      auto load = [&](int j, double* v) {
         const int32_t code = s_code[j];
         const double* rowblk = g.ke + (int64_t)(code >> 5) * ke_size + (int64_t)(3 * (code & 31)) * ndof_e;
-        for (int t = lane; t < per; t += 32) cp_async8(stg + j * per + t, rowblk + t);
-      }
-      cp_async_commit_wait_all();
-      __syncwarp();
+#pragma unroll
+        for (int m = 0; m < GATHER_VPL; ++m) {
+          const int t = lane + 32 * m;
+          v[m] = (m < nv && t < per) ? __ldcs(rowblk + t) : 0.0;
+        }
+      };
+      load(0, cur);
       for (int j = 0; j < nbat; ++j) {
-        for (int t = lane; t < per; t += 32) {
-          const int i = t / ndof_e, c = t - i * ndof_e;
-          acc[s_slot[j * nn + c / 3] * 9 + i * 3 + (c % 3)] += stg[j * per + t];
+        if (j + 1 < nbat) load(j + 1, nxt);
+#pragma unroll
+        for (int m = 0; m < GATHER_VPL; ++m) {
+          const int t = lane + 32 * m;
+          if (m < nv && t < per) {
+            const int i = t / ndof_e, c = t - i * ndof_e;
+            acc[s_slot[j * nn + c / 3] * 9 + i * 3 + (c % 3)] += cur[m];
+          }
         }
         __syncwarp();
+#pragma unroll
+        for (int m = 0; m < GATHER_VPL; ++m) cur[m] = nxt[m];
       }
     }
     // K_ff in CSR, and K_fp u0 -- skipped for a node-block-only assembly
@@ -829,8 +829,7 @@ __global__ void k_gather(GatherArgs g) {
 }
 
 int run_gather(axia_ctx* ctx, GatherArgs args) {
-  size_t per_warp = (size_t)(GATHER_STAGE + args.max_adj * 9) * sizeof(double) +
-                    (size_t)(args.max_adj + 2 * GATHER_SLOTS) * 4;
+  size_t per_warp = (size_t)args.max_adj * 9 * sizeof(double) + (size_t)(args.max_adj + 2 * GATHER_SLOTS) * 4;
   per_warp = (per_warp + 15) & ~(size_t)15;
   if (per_warp > 200 * 1024) return set_error(ctx, AXIA_ERR_TOO_LARGE, "node adjacency too large for the gather");
   int warps = 8;

@@ -116,7 +116,7 @@ struct MeshGroup {
 constexpr int GROUP_SLOTS = 4;  // partial-sum slots per group: S_PQ, S_RR, S_RZ, S_RC
 
 constexpr int COARSE_MAX = 4096;    // coarse unknowns (6 per subdomain, padded to 64)
-constexpr int COARSE_CHUNK = 64;    // nodes per restriction chunk (a few per warp: every warp busy)
+constexpr int COARSE_CHUNK = 256;   // nodes per restriction chunk
 constexpr int S_RC = 3;             // partial-sum slot of r_c . y
 
 struct CoarseArgs {
