@@ -328,11 +328,10 @@ struct SolveRange {
 
 // The coarse solve of the two-level preconditioner, r_c complete:
 // y = M r_c, and r_c . y reduced over the group.
-template <bool PARTIALS>
 __device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const CoarseArgs& C, const SolveRange& R,
                                             int gwarp, int nwarps, int lane, float* rz_c) {
   __shared__ __align__(16) float s_rc[COARSE_MAX];
-  const float acc = coarse_solve<PARTIALS>(C, s_rc, gwarp, nwarps, lane);
+  const float acc = coarse_solve(C, s_rc, gwarp, nwarps, lane);
   block_partials<float>(acc, 0.f, 1, R.partials, S_RC, S_RC, R.nblk, R.rank);
   double red[REDUCE_MAX_NV];
   if (!group_reduce_sync(R.bar, P.st, P.limit_ns, R.partials, R.totals, S_RC, 1, R.nblk, red)) return false;
@@ -340,10 +339,7 @@ __device__ __forceinline__ bool coarse_step(const BsrReliableArgs& P, const Coar
   return true;
 }
 
-// PARTIALS (single system): the restriction leaves chunk partials and every
-// block sums r_c from them in the coarse step; the multi-mesh groups finish
-// each subdomain in the restriction (their r_c rows are per mesh).
-template <int L32, int V32, int L64, int V64, bool COARSE = false, bool SYM = false, bool PARTIALS = false>
+template <int L32, int V32, int L64, int V64, bool COARSE = false, bool SYM = false>
 __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const CoarseArgs& C, const SolveRange& R) {
   const int n0 = R.node0, n1 = R.node1;
   const int i0 = 3 * n0;
@@ -383,9 +379,9 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
   if constexpr (COARSE) {
     if (!converged) {  // p = D^-1 b + Z M Z^T b
       float rz_c = 0.f;
-      coarse_restrict<PARTIALS>(C, P.r32, gwarp, nwarps, lane);
+      coarse_restrict(C, P.r32, gwarp, nwarps, lane);
       if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
-      if (!coarse_step<PARTIALS>(P, C, R, gwarp, nwarps, lane, &rz_c)) return;
+      if (!coarse_step(P, C, R, gwarp, nwarps, lane, &rz_c)) return;
       rz += rz_c;
       coarse_update_p(C, n0, n1, tid, nth, 0.f, P.r32, P.dinv32, P.p32, true);
       if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
@@ -428,8 +424,7 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
     const float alpha = rz / pq;
     float rr_p = 0.f, rzn_p = 0.f;
     if constexpr (COARSE) {
-      coarse_update_restrict<PARTIALS>(C, alpha, P.x32, P.p32, P.q32, P.r32, P.dinv32, gwarp, nwarps, lane, rr_p,
-                                       rzn_p);
+      coarse_update_restrict(C, alpha, P.x32, P.p32, P.q32, P.r32, P.dinv32, gwarp, nwarps, lane, rr_p, rzn_p);
     } else {
       for (int i = i0 + tid; i < nd; i += nth) {
         P.x32[i] = fmaf(alpha, P.p32[i], P.x32[i]);
@@ -491,13 +486,13 @@ __device__ __forceinline__ void reliable_body(const BsrReliableArgs& P, const Co
         break;
       }
       if constexpr (COARSE) {  // r was replaced: restrict it again
-        coarse_restrict<PARTIALS>(C, P.r32, gwarp, nwarps, lane);
+        coarse_restrict(C, P.r32, gwarp, nwarps, lane);
         if (!group_sync(R.bar, P.st, P.limit_ns, R.nblk)) return;
       }
     }
     if constexpr (COARSE) {
       float rz_c = 0.f;
-      if (!coarse_step<PARTIALS>(P, C, R, gwarp, nwarps, lane, &rz_c)) return;
+      if (!coarse_step(P, C, R, gwarp, nwarps, lane, &rz_c)) return;
       rzn += rz_c;
     }
     const float beta = rzn / rz;
@@ -531,7 +526,7 @@ __host__ __device__ constexpr int rel_min_blocks() { return V32 >= 4 ? 2 : 3; }
 template <int L32, int V32, bool COARSE = false, bool SYM = false>
 __global__ void __launch_bounds__(PCG_THREADS, rel_min_blocks<V32>()) pcg_bsr_reliable_kernel(BsrReliableArgs P) {
   const SolveRange R{0, P.M64.n_nodes, blockIdx.x, gridDim.x, P.partials, P.totals, P.bar, P.out};
-  reliable_body<L32, V32, kL64, rel_v64<V32>(), COARSE, SYM, true>(P, P.C, R);
+  reliable_body<L32, V32, kL64, rel_v64<V32>(), COARSE, SYM>(P, P.C, R);
 }
 
 // Independent systems on disjoint node ranges of one node-block matrix (the

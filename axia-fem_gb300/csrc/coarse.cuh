@@ -81,21 +81,7 @@ __device__ __forceinline__ void coarse_chunk_finish(const CoarseArgs& C, int c, 
   }
 }
 
-// Chunk c's six sums into part[c] and nothing else: the single-system kernel
-// forms r_c from the chunk partials after the phase's grid barrier (every
-// block sums them itself), so the update phase needs no fence and no counter.
-__device__ __forceinline__ void coarse_chunk_store(const CoarseArgs& C, int c, float (&v)[6], int lane) {
-#pragma unroll
-  for (int k = 0; k < 6; ++k) v[k] = warp_sum(v[k]);
-  if (lane < 6) {
-    const float x = lane == 0 ? v[0] : lane == 1 ? v[1] : lane == 2 ? v[2] : lane == 3 ? v[3] : lane == 4 ? v[4] : v[5];
-    C.part[6 * c + lane] = x;
-  }
-}
-
-// r_c = Z^T r over the chunks (after an FP64 residual replaced r, and at the start);
-// PARTIALS: chunk partials only (see coarse_chunk_store)
-template <bool PARTIALS = false>
+// r_c = Z^T r over the chunks (after an FP64 residual replaced r, and at the start)
 __device__ __forceinline__ void coarse_restrict(const CoarseArgs& C, const float* r, int gwarp, int nwarps,
                                                 int lane) {
   for (int c = C.chunk_lo + gwarp; c < C.chunk_hi; c += nwarps) {
@@ -108,16 +94,12 @@ __device__ __forceinline__ void coarse_restrict(const CoarseArgs& C, const float
       const unsigned m = geo_bits(g);
       zt_add(g, (m & 1u) ? r[3 * a] : 0.f, (m & 2u) ? r[3 * a + 1] : 0.f, (m & 4u) ? r[3 * a + 2] : 0.f, v);
     }
-    if (PARTIALS)
-      coarse_chunk_store(C, c, v, lane);
-    else
-      coarse_chunk_finish(C, c, ch.x, v, lane);
+    coarse_chunk_finish(C, c, ch.x, v, lane);
   }
 }
 
 // The CG update x += alpha p, r -= alpha q node by node in subdomain order,
 // with the partial sums of r.r and r.D^-1 r and the restriction of the new r.
-template <bool PARTIALS = false>
 __device__ __forceinline__ void coarse_update_restrict(const CoarseArgs& C, float alpha, float* x, const float* p,
                                                        const float* q, float* r, const float* dinv, int gwarp,
                                                        int nwarps, int lane, float& rr_p, float& rz_p) {
@@ -142,31 +124,15 @@ __device__ __forceinline__ void coarse_update_restrict(const CoarseArgs& C, floa
       }
       zt_add(g, rv[0], rv[1], rv[2], v);
     }
-    if (PARTIALS)
-      coarse_chunk_store(C, c, v, lane);
-    else
-      coarse_chunk_finish(C, c, ch.x, v, lane);
+    coarse_chunk_finish(C, c, ch.x, v, lane);
   }
 }
 
 // The block's part of r_c into shared memory (zero past its unknowns), then
 // rows of y = M r_c over the warps of the group.  Returns this thread's share
 // of r_c . y (nonzero on lane 0 of warps that own rows).
-// PARTIALS: r_c is summed here from the chunk partials (chunks of a subdomain
-// in ascending order, the order coarse_chunk_finish uses).
-template <bool PARTIALS = false>
 __device__ __forceinline__ float coarse_solve(const CoarseArgs& C, float* s_rc, int gwarp, int nwarps, int lane) {
-  if (PARTIALS) {
-    for (int u = threadIdx.x; u < C.ldm; u += blockDim.x) {
-      float v = 0.f;
-      if (u < C.nc) {
-        const int I = u / 6, k = u - 6 * I;
-        const int c0 = __ldg(C.chunk_ptr + I), c1 = __ldg(C.chunk_ptr + I + 1);
-        v = ldcg_sum(C.part + 6 * c0 + k, 6, c1 - c0);
-      }
-      s_rc[u] = v;
-    }
-  } else if (C.col0 == 0 && C.row0 == 0 && C.row1 == C.nc && C.ldm <= C.ncp) {  // the whole matrix: r_c is zero past nc
+  if (C.col0 == 0 && C.row0 == 0 && C.row1 == C.nc && C.ldm <= C.ncp) {  // the whole matrix: r_c is zero past nc
     for (int t = threadIdx.x; t < (C.ldm >> 2); t += blockDim.x)
       reinterpret_cast<float4*>(s_rc)[t] = __ldcg(reinterpret_cast<const float4*>(C.rc) + t);
   } else {

@@ -184,16 +184,17 @@ def batch_update_bytes(nblocks, n_nodes, nrhs=32):
 
 
 def element_fp64_flops(nn, ng):
-    """FP64 operations of element_ke_kernel per element (FMA = 2): per Gauss point
-    J (9 nn FMA), the cofactors (9 MUL + 9 FMA), det J and w / det J (2 FMA,
-    2 MUL/DIV), c_a = adj(J)^T dN_a (3 nn x (1 MUL + 2 FMA)) and h_a = (w / det J) c_a
-    (3 nn MUL); A_ab over the NE upper-triangle entries (NE FMA per Gauss point);
-    K_ab from A (NE MUL + NE FMA, 3 FMA per node pair for the trace term) and
-    the traces (2 ADD per node pair)."""
+    """FP64 operations of element_ke_kernel per element (FMA = 2 flops): per Gauss
+    point 15 nn + 19 FMA (J, cofactors, det J, c_a) and 6 nn + 19 MUL (cofactors,
+    c_a, h_a = (w / det J) c_a, w / det J); NE FMA per Gauss point for A_ab over
+    the NE upper-triangle entries; NE MUL + NE FMA for K_ab from A and 3 FMA per
+    node pair for the trace term; 2 ADD per node pair for the traces.  For C3D8
+    that is 3920 FMA + 836 MUL + 72 ADD, the DFMA / DMUL / DADD counts ncu reads
+    for the kernel (8,748 flop)."""
     ne = 9 * nn * (nn - 1) // 2 + 6 * nn
     nb = nn * (nn + 1) // 2
-    fma = ng * (9 * nn + 9 + 2 + 6 * nn) + ne * ng + ne + 3 * nb
-    other = ng * (9 + 2 + 3 * nn + 3 * nn) + ne + 2 * nb
+    fma = ng * (15 * nn + 19) + ne * ng + ne + 3 * nb
+    other = ng * (6 * nn + 19) + ne + 2 * nb
     return 2 * fma + other
 
 
@@ -665,7 +666,7 @@ def main():
     ap.add_argument("--coarse-nodes", type=int, default=0,
                     help="nodes per subdomain of the coarse space (0: the library default, about 512 "
                          "subdomains of at least ~13,500 matrix node blocks)")
-    ap.add_argument("--only", choices=["mixed", "coarse", "fp64", "spmv", "batch"], default=None,
+    ap.add_argument("--only", choices=["mixed", "coarse", "fp64", "spmv", "batch", "assemble"], default=None,
                     help="run one solve (or SpMV sweep) once and exit: the profiling entry")
     ap.add_argument("--max-iter", type=int, default=0, help="with --only: cap the CG iterations")
     ap.add_argument("--krylov", choices=["per-case", "block"], default="per-case",
@@ -729,6 +730,14 @@ def main():
     umx = torch.empty_like(f_dev)
 
     if args.only:
+        if args.only == "assemble":
+            # numeric assembly only (element kernel + gather into both node-block forms), three times
+            for _ in range(3):
+                ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+            el, ga = ctx.assemble_times()
+            print(json.dumps({"only": "assemble", "ms_element": el, "ms_gather": ga, "n_elem": model.n_elem}))
+            torch.cuda.synchronize()
+            return
         if args.only == "spmv":
             ctx.assemble_ex(L.ASM_CSR64 | L.ASM_CSR32 | L.ASM_BSR64 | L.ASM_BSR32 | L.ASM_SYM32)
             nd = 3 * model.n_nodes
