@@ -670,7 +670,9 @@ def main():
                     help="run one solve (or SpMV sweep) once and exit: the profiling entry")
     ap.add_argument("--max-iter", type=int, default=0, help="with --only: cap the CG iterations")
     ap.add_argument("--krylov", choices=["per-case", "block"], default="per-case",
-                    help="with --only batch: one recurrence per load case, or the block PCG (two-level)")
+                    help="with --only batch: one recurrence per load case, or the block PCG")
+    ap.add_argument("--precond", choices=["jacobi", "coarse"], default="jacobi",
+                    help="with --only batch: the diagonal or the two-level preconditioner")
     ap.add_argument("--workload", choices=["c2", "c3", "c4a", "c4b", "c5"], default="c2",
                     help="c2 (default): the 100^3 C3D8 block; others: the remaining configurations")
     args = ap.parse_args()
@@ -707,9 +709,10 @@ def main():
         U = torch.empty_like(F)
         try:
             kry = L.KRYLOV_BLOCK if args.krylov == "block" else L.KRYLOV_PER_CASE
-            pre = L.PRECOND_COARSE if args.coarse_nodes >= 0 and args.krylov == "block" else 0
+            pre = L.PRECOND_COARSE if args.precond == "coarse" else L.PRECOND_JACOBI
             info, rel = ctx.solve_batched_device(32, F.data_ptr(), U.data_ptr(), rtol=RTOL, inner_rtol=args.delta,
-                                                 max_iter=args.max_iter, krylov=kry, preconditioner=pre)
+                                                 max_iter=args.max_iter, krylov=kry, preconditioner=pre,
+                                                 coarse_nodes=args.coarse_nodes)
             print(json.dumps({"only": "batch", "iters": info.iters, "ms_kernel": info.ms_pcg_kernel}))
         except Exception as e:  # a capped iteration count ends as NOT_CONVERGED
             print(json.dumps({"only": "batch", "status": str(e)[:120]}))
