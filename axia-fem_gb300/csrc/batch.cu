@@ -375,38 +375,64 @@ __device__ __forceinline__ void coarse_restrict_m(const CoarseArgs& C, const flo
 
 // Y = M R_c; per column r_c . y into partials[(slot0 + col) * G + block].
 // Tasks of 16 rows go to the blocks in turn; a thread owns one (row, load
-// case): the warp of a row streams that row of M once (broadcast loads), and
-// R_c passes through shared memory in tiles of 64 rows shared by the block's
-// 16 warps (one L2 read of each tile per task instead of a dependent L2
-// round trip per row of R_c).  The per-column sums run over the block's
-// tasks and rows in a fixed order.
-__device__ __forceinline__ void coarse_solve_m(const CoarseArgs& C, int gwarp, int nwarps, int lane, double* partials,
-                                               int slot0) {
-  constexpr int TR = PCG_THREADS / NR;  // rows per task
-  constexpr int TJ = 64;                // rows of R_c per shared-memory tile
+// case).  The task walks the columns of M in tiles of 64: the tile of R_c
+// (64 x 32, contiguous) and the 16 x 64 tile of M are copied into a 3-stage
+// shared-memory ring with cp.async, two tiles ahead of the one being summed,
+// so a task keeps ~24 KB in flight instead of waiting one memory round trip
+// per tile.  `ring` is COARSE_RING_FLOATS of 16-byte aligned shared memory.
+// The per-column sums run over the block's tasks and rows in a fixed order.
+constexpr int CS_TJ = 64;                          // columns of M per tile
+constexpr int CS_TR = PCG_THREADS / NR;            // rows per task (16)
+constexpr int CS_STAGE = CS_TJ * NR + CS_TR * CS_TJ;  // floats per stage: R_c tile + M tile
+constexpr int COARSE_RING_FLOATS = 3 * CS_STAGE;
+
+// dynamic shared memory of the 32-case kernel: the row staging of the SpMV
+// phase and the coarse solve's ring take turns in it
+constexpr size_t DYN_BYTES =
+    STAGE_BYTES > COARSE_RING_FLOATS * sizeof(float) ? STAGE_BYTES : COARSE_RING_FLOATS * sizeof(float);
+
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void coarse_solve_m(const CoarseArgs& C, float* ring, double* partials, int slot0) {
   __shared__ float s_prod[PCG_THREADS];
   __shared__ float s_cc[NR];
-  __shared__ __align__(16) float s_rc[TJ][NR];
   const int r = threadIdx.x / NR, c = threadIdx.x % NR;
   if (threadIdx.x < NR) s_cc[threadIdx.x] = 0.f;
-  const int ntask = (C.nc + TR - 1) / TR;
+  const int ntask = (C.nc + CS_TR - 1) / CS_TR;
+  const int nt = C.ldm / CS_TJ;  // tiles per row of M (ldm is a multiple of 64; zero past nc)
   for (int task = blockIdx.x; task < ntask; task += gridDim.x) {
-    const int i = task * TR + r;
-    const float* mrow = C.minv + (size_t)min(i, C.nc - 1) * C.ldm;
-    float y = 0.f;
-    for (int j0 = 0; j0 < C.nc; j0 += TJ) {
-      const int nj = min(TJ, C.nc - j0);
-      __syncthreads();
-      for (int t = threadIdx.x; t < TJ * NR / 4; t += PCG_THREADS) {
-        const int jj = t / (NR / 4), cc = 4 * (t % (NR / 4));
-        *reinterpret_cast<float4*>(&s_rc[jj][cc]) =
-            jj < nj ? __ldcg(reinterpret_cast<const float4*>(C.rc_m + (size_t)(j0 + jj) * NR + cc))
-                    : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int i0 = task * CS_TR;
+    // thread t copies 16 bytes of the R_c tile and (t < 256) 16 bytes of the M tile
+    auto issue = [&](int t) {
+      if (t < nt) {
+        float* st = ring + (t % 3) * CS_STAGE;
+        const int jj = threadIdx.x >> 3, cc = 4 * (threadIdx.x & 7);
+        cp_async16(st + jj * NR + cc, C.rc_m + (size_t)(t * CS_TJ + jj) * NR + cc);
+        if (threadIdx.x < CS_TR * CS_TJ / 4) {
+          const int rr = threadIdx.x >> 4, kk = 4 * (threadIdx.x & 15);
+          cp_async16(st + CS_TJ * NR + rr * CS_TJ + kk, C.minv + (size_t)(i0 + rr) * C.ldm + t * CS_TJ + kk);
+        }
       }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    __syncthreads();  // the ring is free (the previous task's readers are done)
+    issue(0);
+    issue(1);
+    float y = 0.f;
+    for (int t = 0; t < nt; ++t) {
+      asm volatile("cp.async.wait_group 1;" ::: "memory");  // tile t has landed
       __syncthreads();
-#pragma unroll 16
-      for (int jj = 0; jj < nj; ++jj) y = fmaf(__ldg(mrow + j0 + jj), s_rc[jj][c], y);
+      issue(t + 2);  // into the stage tile t - 1 used; every thread is past it
+      const float* st = ring + (t % 3) * CS_STAGE;
+      const float* mt = st + CS_TJ * NR + r * CS_TJ;
+#pragma unroll 8
+      for (int jj = 0; jj < CS_TJ; ++jj) y = fmaf(mt[jj], st[jj * NR + c], y);
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    const int i = i0 + r;
     float prod = 0.f;
     if (i < C.nc) {
       C.yc_m[(size_t)i * NR + c] = y;
@@ -416,11 +442,11 @@ __device__ __forceinline__ void coarse_solve_m(const CoarseArgs& C, int gwarp, i
     __syncthreads();
     if (threadIdx.x < NR) {
       float sum = s_cc[threadIdx.x];
-      for (int q = 0; q < TR; ++q) sum += s_prod[q * NR + threadIdx.x];
+      for (int q = 0; q < CS_TR; ++q) sum += s_prod[q * NR + threadIdx.x];
       s_cc[threadIdx.x] = sum;
     }
-    __syncthreads();
   }
+  __syncthreads();
   if (threadIdx.x < NR) partials[(size_t)(slot0 + threadIdx.x) * gridDim.x + blockIdx.x] = (double)s_cc[threadIdx.x];
 }
 
@@ -448,16 +474,17 @@ __device__ __forceinline__ void coarse_prolong_m(const CoarseArgs& C, long long 
 
 // the coarse half of the preconditioner for the current R32: restriction,
 // barrier, Y = M R_c and the per-column r . Z y reduced into totals[SL_A..]
-__device__ __forceinline__ bool coarse_step_m(const MultiArgs& P, int gwarp, int nwarps, int lane) {
+__device__ __forceinline__ bool coarse_step_m(const MultiArgs& P, int gwarp, int nwarps, int lane, float* ring) {
   coarse_restrict_m(P.C, P.R32, gwarp, nwarps, lane);
   if (!grid_sync(P.bar, P.st, P.limit_ns)) return false;
-  coarse_solve_m(P.C, gwarp, nwarps, lane, P.partials, SL_A);
+  coarse_solve_m(P.C, ring, P.partials, SL_A);
   return grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, SL_A, NR);
 }
 
 template <bool COARSE, int TC, int TU>
 __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs P) {
-  extern __shared__ RowStage s_stage[];  // STAGE_BYTES
+  extern __shared__ __align__(16) RowStage s_stage[];  // DYN_BYTES: row staging, or the coarse solve's ring
+  float* const ring = reinterpret_cast<float*>(s_stage);
   __shared__ double s_rz[NR], s_bnorm[NR], s_rmax[NR], s_res[NR];
   __shared__ float s_alpha[NR], s_beta[NR];
   __shared__ int s_active[NR], s_flag;
@@ -509,7 +536,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
   }
   __syncthreads();
   if constexpr (COARSE) {  // P = D^-1 B + Z M Z^T B
-    if (!coarse_step_m(P, gwarp, nwarps, lane)) return;
+    if (!coarse_step_m(P, gwarp, nwarps, lane, ring)) return;
     if (threadIdx.x < NR) s_rz[threadIdx.x] += __ldcg(P.totals + SL_A + threadIdx.x);
     for (long long q = tid; q < nq; q += nth) {
       float p[CPL], zc[CPL];
@@ -671,7 +698,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
       __syncthreads();
     }
     if constexpr (COARSE) {
-      if (!coarse_step_m(P, gwarp, nwarps, lane)) return;
+      if (!coarse_step_m(P, gwarp, nwarps, lane, ring)) return;
     }
     if (threadIdx.x < NR) {
       const int c = threadIdx.x;
@@ -913,9 +940,8 @@ __global__ void __launch_bounds__(BT) k_blk_restrict(CoarseArgs C, const float* 
 }
 
 __global__ void __launch_bounds__(PCG_THREADS) k_blk_coarse_solve(CoarseArgs C, double* scratch) {
-  const int lane = threadIdx.x & 31;
-  const int gwarp = (blockIdx.x * PCG_THREADS + threadIdx.x) >> 5, nwarps = (gridDim.x * PCG_THREADS) >> 5;
-  coarse_solve_m(C, gwarp, nwarps, lane, scratch, 0);
+  extern __shared__ __align__(16) float s_ring[];  // COARSE_RING_FLOATS
+  coarse_solve_m(C, s_ring, scratch, 0);
 }
 
 // X += X32 (FP64), X32 = 0
@@ -1117,8 +1143,8 @@ int ensure_batch_buffers(axia_ctx* ctx) {
 // Grid of the cooperative launch of kern (its occupancy with the staging buffers).
 int batch_grid(axia_ctx* ctx, const void* kern, int* grid) {
   // static + staging shared memory is above the 48 KB a block gets without opting in
-  AXIA_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STAGE_BYTES));
-  AXIA_TRY(coop_grid(ctx, kern, (int)std::min<int64_t>(ctx->ndof, INT32_MAX), grid, STAGE_BYTES));
+  AXIA_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DYN_BYTES));
+  AXIA_TRY(coop_grid(ctx, kern, (int)std::min<int64_t>(ctx->ndof, INT32_MAX), grid, DYN_BYTES));
   if ((size_t)*grid * 2 * NR > ctx->partial_slots) *grid = (int)(ctx->partial_slots / (2 * NR));
   return AXIA_OK;
 }
@@ -1133,7 +1159,7 @@ MultiArgs multi_args(axia_ctx* ctx, double rtol, double delta, long long max_ite
 
 int launch_batch(axia_ctx* ctx, const void* kern, int grid, MultiArgs& P) {
   void* params[] = {&P};
-  AXIA_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(PCG_THREADS), params, STAGE_BYTES, ctx->stream));
+  AXIA_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(PCG_THREADS), params, DYN_BYTES, ctx->stream));
   ctx->launches++;
   return AXIA_OK;
 }
@@ -1318,7 +1344,7 @@ struct BlockRun {
   void precond(const float* R, float* Z) {
     if (coarse) {
       k_blk_restrict<<<g_row, BT, 0, s>>>(C, R);
-      k_blk_coarse_solve<<<ctx->sm_count * 2, PCG_THREADS, 0, s>>>(C, part());
+      k_blk_coarse_solve<<<ctx->sm_count * 2, PCG_THREADS, COARSE_RING_FLOATS * sizeof(float), s>>>(C, part());
       k_blk_precond<true><<<g_row, BT, 0, s>>>(nd, ctx->d_bdinv32, R, C, Z);
       count(3);
     } else {
