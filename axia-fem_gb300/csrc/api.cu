@@ -9,6 +9,7 @@
 
 int symbolic_setup(axia_ctx* ctx, int64_t n_bc, const int64_t* d_bc_dof, const double* d_bc_val);
 int numeric_assemble(axia_ctx* ctx, int flags);
+int ensure_csr_columns(axia_ctx* ctx);
 int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_opts* opts, axia_solve_info* info);
 int bsr_spmv_device(axia_ctx* ctx, bool fp32, const void* x, void* y, int lanes_req, int vec_req);
 int sym_spmv_device(axia_ctx* ctx, const float* x, float* y, int lanes_req);
@@ -788,7 +789,11 @@ int32_t axia_gpu_export_system(const axia_ctx* ctx_c, int32_t* rowptr, int32_t* 
   AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the copies below run on the legacy stream
   const int64_t n = ctx->n_free, nnz = ctx->nnz;
   if (rowptr) AXIA_CUDA(ctx, cudaMemcpy(rowptr, ctx->d_rowptr, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost));
-  if (col) AXIA_CUDA(ctx, cudaMemcpy(col, ctx->d_col, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (col) {
+    AXIA_TRY(ensure_csr_columns(ctx));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    AXIA_CUDA(ctx, cudaMemcpy(col, ctx->d_col, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  }
   if ((val || diag || kfu0) && !ctx->assembled) return set_error(ctx, AXIA_ERR_STATE, "export of values before assemble");
   if (val && !ctx->have_csr64) return set_error(ctx, AXIA_ERR_STATE, "export of CSR values needs AXIA_ASM_CSR64");
   if (val) AXIA_CUDA(ctx, cudaMemcpy(val, ctx->d_val, nnz * sizeof(double), cudaMemcpyDeviceToHost));

@@ -1008,10 +1008,8 @@ int symbolic_setup(axia_ctx* ctx, int64_t n_bc, const int64_t* d_bc_dof, const d
   AXIA_TRY(dev_alloc(ctx, &ctx->d_rowptr, n_free + 1));
   k_to_i32<<<grid_for(n_free + 1, 256, ctx->sm_count), 256, 0, s>>>(n_free + 1, d_rptr, ctx->d_rowptr);
   ctx->launches++;
-  AXIA_TRY(dev_alloc(ctx, &ctx->d_col, nnz));
-  k_fill_columns<<<grid_for(n_nodes, 8, ctx->sm_count), 256, 0, s>>>(n_nodes, d_adj_ptr, ctx->d_adj, ctx->d_adj_off,
-                                                                     ctx->d_ind_of, ctx->d_rowptr, ctx->d_col);
-  ctx->launches++;
+  // the column indices of K_ff (nnz int32) are filled on first use by a CSR
+  // assembly or export (ensure_csr_columns): the node-block solves never read them
   AXIA_CUDA(ctx, cudaGetLastError());
   AXIA_CUDA(ctx, cudaStreamSynchronize(s));
   AXIA_TRY(read_dev_status(ctx, &hs));
@@ -1102,12 +1100,25 @@ static int ensure_sym_structure(axia_ctx* ctx) {
   return AXIA_OK;
 }
 
+// Column indices of K_ff in CSR, built once per mesh when a CSR form is first
+// assembled or exported (warp per node from the node adjacency and the DOF map).
+int ensure_csr_columns(axia_ctx* ctx) {
+  if (ctx->d_col || ctx->nnz == 0) return AXIA_OK;
+  AXIA_TRY(dev_alloc(ctx, &ctx->d_col, (size_t)ctx->nnz));
+  k_fill_columns<<<grid_for(ctx->n_nodes, 8, ctx->sm_count), 256, 0, ctx->stream>>>(
+      ctx->n_nodes, ctx->d_adj_ptr, ctx->d_adj, ctx->d_adj_off, ctx->d_ind_of, ctx->d_rowptr, ctx->d_col);
+  ctx->launches++;
+  AXIA_CUDA(ctx, cudaGetLastError());
+  return AXIA_OK;
+}
+
 int numeric_assemble(axia_ctx* ctx, int flags) {
   cudaStream_t s = ctx->stream;
   const bool csr64 = flags & AXIA_ASM_CSR64, csr32 = flags & AXIA_ASM_CSR32;
   const bool bsr64 = flags & AXIA_ASM_BSR64, bsr32 = flags & AXIA_ASM_BSR32;
   const bool sym32 = flags & AXIA_ASM_SYM32;
   if (sym32) AXIA_TRY(ensure_sym_structure(ctx));
+  if (csr64 || csr32) AXIA_TRY(ensure_csr_columns(ctx));
   const int64_t kesz = (int64_t)9 * ctx->nn * ctx->nn;
   if (ctx->ke_elems < (size_t)(ctx->n_elem * kesz)) {
     AXIA_TRY(dev_alloc(ctx, &ctx->d_ke, (size_t)(ctx->n_elem * kesz)));

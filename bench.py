@@ -989,20 +989,27 @@ def main():
         d2h = u_pin.nbytes
         ctx.set_stream(None)
         mixed_kw["spmv_lanes"] = args.lanes32
-        ts = []
+        ts, phases = [], []
         for k in range(args.warmup + args.steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            ctx.setup(pm)
+            ctx.setup(pm)  # every call of the C ABI returns after its device work
+            t1 = time.perf_counter()
             ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+            t2 = time.perf_counter()
             u, info = ctx.solve(f_pin, out=u_pin, rtol=RTOL, **coarse_kw)
-            dt = time.perf_counter() - t0
+            t3 = time.perf_counter()
             if k >= args.warmup:
-                ts.append(dt)
+                ts.append(t3 - t0)
+                phases.append((t1 - t0, t2 - t1, t3 - t2))
         e2e_s = sum(ts) / len(ts)
         e2e_s = replicas.max_over_ranks(e2e_s, dist, f"cuda:{local}")
         e2e = {"value": n / e2e_s / 1e6 * world, "unit": "MDOF/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+               "phases_ms": {"setup (mesh upload + symbolic)": 1e3 * statistics.median(p[0] for p in phases),
+                             "assemble": 1e3 * statistics.median(p[1] for p in phases),
+                             "solve (f upload, coarse operator, CG, u copy back)":
+                                 1e3 * statistics.median(p[2] for p in phases)}}
 
     same = None
     if rank == 0 and not args.no_cpu:
