@@ -49,6 +49,8 @@ FORMAT_BSR3 = 1
 FORMAT_BSR3_SYM = 2
 KRYLOV_PER_CASE = 0
 KRYLOV_BLOCK = 1
+ELEMENT_DWORD = 0
+ELEMENT_FP64 = 1
 PRECOND_JACOBI = 0
 PRECOND_COARSE = 1
 
@@ -104,6 +106,7 @@ SIGNATURES = [
     ("axia_gpu_sym_blocks", C.c_int64, [_P, C.POINTER(C.c_int64)]),
     ("axia_gpu_node_blocks", C.c_int64, [_P]),
     ("axia_gpu_assemble_times", C.c_int32, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("axia_gpu_set_element_arith", C.c_int32, [_P, C.c_int32]),
     ("axia_gpu_coarse_size", C.c_int32, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("axia_gpu_setup_multi", C.c_int32, [_P, C.c_int32, C.POINTER(Mesh), _P, _P, _P]),
     ("axia_gpu_solve_multi", C.c_int32, [_P, _P, _P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), _P, _P]),

@@ -177,6 +177,12 @@ class GpuContext:
         self._check(self.lib.axia_gpu_assemble_times(self.h, C.byref(a), C.byref(b)), "assemble_times")
         return a.value, b.value
 
+    def set_element_arith(self, arith):
+        """C3D8 / C3D20(R) element stiffness arithmetic: _lib.ELEMENT_DWORD (FP32-pair
+        double words, default) or _lib.ELEMENT_FP64."""
+        self._check(self.lib.axia_gpu_set_element_arith(self.h, int(arith)), "set_element_arith")
+        return self
+
     def n_blocks(self) -> int:
         """3x3 node blocks of the node-block form."""
         return int(self.lib.axia_gpu_node_blocks(self.h))

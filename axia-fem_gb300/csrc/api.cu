@@ -652,6 +652,14 @@ int32_t axia_gpu_assemble_times(const axia_ctx* ctx, double* ms_element, double*
   return AXIA_OK;
 }
 
+int32_t axia_gpu_set_element_arith(axia_ctx* ctx, int32_t arith) {
+  if (!ctx) return AXIA_ERR_INVALID_ARG;
+  if (arith != AXIA_ELEMENT_DWORD && arith != AXIA_ELEMENT_FP64)
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "element arithmetic must be AXIA_ELEMENT_DWORD or AXIA_ELEMENT_FP64");
+  ctx->element_fp64 = arith == AXIA_ELEMENT_FP64;
+  return AXIA_OK;
+}
+
 int32_t axia_gpu_element_energy(axia_ctx* ctx, const double* u_full, const double* v_full, double* s) {
   if (!ctx || !u_full || !v_full || !s) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));

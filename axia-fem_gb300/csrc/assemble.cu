@@ -21,7 +21,7 @@
 #include <mutex>
 #include <string>
 
-#include "element.cuh"
+#include "element_dw.cuh"
 
 // ---------------------------------------------------------------------------
 // Element tables: dN/dxi at the Gauss points (hex8_shape elem.rs:158-171,
@@ -280,12 +280,20 @@ int ensure_tables(axia_ctx* ctx, int nn, int ng, ElemTables* out) {
   return AXIA_OK;
 }
 
-template <int NN, int NG, int WARPS>
+// DW: the double-word Gauss loop (element_dw.cuh) instead of the FP64 one
+template <int NN, int NG, int WARPS, bool DW = false>
 int launch_element_ke(axia_ctx* ctx, const ElemArgs& args) {
   ElemTables tab;
   AXIA_TRY(ensure_tables(ctx, NN, NG, &tab));
-  size_t smem = element_smem_bytes<NN, NG>(WARPS);
-  auto kern = element_ke_kernel<NN, NG, WARPS>;
+  size_t smem;
+  void (*kern)(ElemArgs, ElemTables);
+  if constexpr (DW) {
+    smem = element_dw_smem_bytes<NN, NG>(WARPS);
+    kern = element_ke_dw_kernel<NN, NG, WARPS>;
+  } else {
+    smem = element_smem_bytes<NN, NG>(WARPS);
+    kern = element_ke_kernel<NN, NG, WARPS>;
+  }
   AXIA_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARPS * 32, smem));
@@ -314,6 +322,14 @@ int element_tables_for(axia_ctx* ctx, int nn, int ng, const double** dn, const d
 int run_hex8r_hourglass(axia_ctx* ctx, const ElemArgs& args);
 int run_hex8i_condense(axia_ctx* ctx, const ElemArgs& args, const double* dn_tab);
 
+// true when run_element_ke runs the double-word kernel for this kind: C3D8.
+// C3D20 / C3D20R keep the FP64 loop: their double-word form (1,830 entries
+// per element, 4 warps per SM by shared memory) measured slower than the
+// FP64 one, 23.3 against 22.2 ms for the 50^3 block.
+bool element_uses_dw(const axia_ctx* ctx, int nn, int reduced) {
+  return !ctx->element_fp64 && nn == 8 && reduced == 0;
+}
+
 // nn = 8: reduced 1 = C3D8R (centre point + hourglass), 2 = C3D8I (incompatible modes)
 int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args) {
   if (args.n_elem == 0) return AXIA_OK;
@@ -327,7 +343,8 @@ int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args) {
     AXIA_TRY(ensure_tables(ctx, 8, 8, &tab));
     return run_hex8i_condense(ctx, args, tab.dn);
   }
-  if (nn == 8) return launch_element_ke<8, 8, 8>(ctx, args);
+  const bool dw = element_uses_dw(ctx, nn, reduced);
+  if (nn == 8) return dw ? launch_element_ke<8, 8, 8, true>(ctx, args) : launch_element_ke<8, 8, 8>(ctx, args);
   if (nn == 20 && !reduced) return launch_element_ke<20, 27, 4>(ctx, args);
   if (nn == 20 && reduced) return launch_element_ke<20, 8, 4>(ctx, args);
   if (nn == 4) return launch_element_ke<4, 1, 8>(ctx, args);
@@ -678,6 +695,7 @@ struct GatherArgs {
   int64_t nb;           // padded block count (plane stride)
   float* uval;          // symmetric FP32 form [nbu][10] (null: not assembled)
   const int32_t* uptr;  // its upper-block row starts
+  int ke_dw;            // ke holds double words (element_ke_dw_kernel): sums in double words
 };
 
 // incident elements whose column slots are looked up at once (x nodes per
@@ -685,15 +703,32 @@ struct GatherArgs {
 constexpr int GATHER_SLOTS = 64;
 constexpr int GATHER_VPL = 6;  // ceil(3 * 60 / 32): C3D20
 
+// DWK: the Ke scratch holds double words; each K entry is then summed in a
+// compensated double-word accumulator (dword.cuh) on the FP32 pipe and
+// rounded once to FP64 (and to FP32 for the FP32 forms), instead of one FP64
+// add per element contribution.
+// NNT: nodes per element when fixed at compile time (8, 20), 0 for g.nn.
+template <bool DWK, int NNT>
 __global__ void k_gather(GatherArgs g) {
   extern __shared__ __align__(16) unsigned char s_gather[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
-  const int nn = g.nn, ndof_e = 3 * nn, ke_size = ndof_e * ndof_e;
+  const int nn = NNT ? NNT : g.nn, ndof_e = 3 * nn, ke_size = ndof_e * ndof_e;
   const int per = 3 * ndof_e, nv = (per + 31) / 32;
   const int batch = max(1, GATHER_SLOTS / nn);
+  // the lane's values of an element's row block: element node c / 3 and the
+  // entry i * 3 + c % 3 of the 3 x 3 block they add to (fixed per lane)
+  int v_node[GATHER_VPL], v_ent[GATHER_VPL];
+#pragma unroll
+  for (int m = 0; m < GATHER_VPL; ++m) {
+    const int t = lane + 32 * m;
+    const int i = t / ndof_e, c = t - i * ndof_e;
+    v_node[m] = c / 3;
+    v_ent[m] = i * 3 + c % 3;
+  }
   unsigned char* base = s_gather + (size_t)warp * g.warp_stride;
   double* acc = (double*)base;                                   // [max_adj][9]
+  dw_acc* acw = (dw_acc*)base;                                   // the same, DWK
   int32_t* s_adj = (int32_t*)(base + (size_t)g.max_adj * 72);    // [max_adj]
   int32_t* s_slot = s_adj + g.max_adj;                           // [GATHER_SLOTS]
   int32_t* s_code = s_slot + GATHER_SLOTS;                       // [GATHER_SLOTS]
@@ -738,8 +773,15 @@ __global__ void k_gather(GatherArgs g) {
         for (int m = 0; m < GATHER_VPL; ++m) {
           const int t = lane + 32 * m;
           if (m < nv && t < per) {
-            const int i = t / ndof_e, c = t - i * ndof_e;
-            acc[s_slot[j * nn + c / 3] * 9 + i * 3 + (c % 3)] += cur[m];
+            const int idx = s_slot[j * nn + v_node[m]] * 9 + v_ent[m];
+            if constexpr (DWK) {
+              const long long bits = __double_as_longlong(cur[m]);
+              dw_acc q = acw[idx];
+              dw_add(q, dw{__int_as_float((int)bits), __int_as_float((int)(bits >> 32))});
+              acw[idx] = q;
+            } else {
+              acc[idx] += cur[m];
+            }
           }
         }
         __syncwarp();
@@ -747,6 +789,17 @@ __global__ void k_gather(GatherArgs g) {
         for (int m = 0; m < GATHER_VPL; ++m) cur[m] = nxt[m];
       }
     }
+    // the summed entry idx in FP64 and FP32
+    auto kval = [&](int idx, double& v64, float& v32) {
+      if constexpr (DWK) {
+        const dw v = dw_value(acw[idx]);
+        v64 = dw_to_double(v);
+        v32 = v.h;
+      } else {
+        v64 = acc[idx];
+        v32 = (float)v64;
+      }
+    };
     // K_ff in CSR, and K_fp u0 -- skipped for a node-block-only assembly
     // without prescribed values (the diagonal is then written below)
     const bool csr_pass = g.val || g.val32 || g.any_u0;
@@ -758,12 +811,14 @@ __global__ void k_gather(GatherArgs g) {
       for (int t = lane; t < 3 * nadj; t += 32) {
         const int s = t / 3, j = t % 3;
         const int b = s_adj[s];
-        const double v = acc[s * 9 + i * 3 + j];
+        double v;
+        float v32;
+        kval(s * 9 + i * 3 + j, v, v32);
         const int c = g.ind_of[3 * (int64_t)b + j];
         if (c >= 0) {
           const int64_t pos = rs + g.adj_off[s0 + s] + (c - first_free(g.ind_of, b));
           if (g.val) g.val[pos] = v;
-          if (g.val32) g.val32[pos] = (float)v;
+          if (g.val32) g.val32[pos] = v32;
           if (c == r) {
             g.diag[r] = v;
             const double di = fabs(v) > 1e-30 ? 1.0 / v : 1.0;  // linalg.rs:218-219 guard
@@ -792,7 +847,10 @@ __global__ void k_gather(GatherArgs g) {
         if (c < 9) {
           const int i = c / 3, j = c % 3;
           const bool fi = g.ind_of[3 * a + i] >= 0, fj = g.ind_of[3 * (int64_t)b + j] >= 0;
-          v = (fi && fj) ? (float)acc[s * 9 + c] : ((b == a && i == j) ? 1.f : 0.f);
+          double v64;
+          float v32;
+          kval(s * 9 + c, v64, v32);
+          v = (fi && fj) ? v32 : ((b == a && i == j) ? 1.f : 0.f);
         } else {
           v = __int_as_float(b);
         }
@@ -800,27 +858,50 @@ __global__ void k_gather(GatherArgs g) {
       }
     }
     if (g.bval64 || g.bval32 || g.uval) {
-      // node-block form: free-free entries of K, a unit diagonal on prescribed DOFs
-      for (int t = lane; t < 9 * nadj; t += 32) {
-        const int ij = t / nadj, s = t - ij * nadj;
-        const int i = ij / 3, j = ij % 3;
+      // node-block form: free-free entries of K, a unit diagonal on prescribed
+      // DOFs; lanes take the row's blocks s, each all 9 entries (for every
+      // entry the lanes write consecutive blocks of one value plane)
+      bool fi[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) fi[i] = g.ind_of[3 * a + i] >= 0;
+      const int64_t q0 = g.qptr[a];
+      for (int s = lane; s < nadj; s += 32) {
         const int b = s_adj[s];
-        const bool fi = g.ind_of[3 * a + i] >= 0, fj = g.ind_of[3 * (int64_t)b + j] >= 0;
-        const bool dg = (b == a) && (i == j);
-        const double v = (fi && fj) ? acc[s * 9 + ij] : (dg ? 1.0 : 0.0);
-        const int64_t pos = (int64_t)ij * g.nb + g.qptr[a] + s;
-        if (g.bval64) g.bval64[pos] = v;
-        if (g.bval32) g.bval32[pos] = (float)v;
-        if (dg) {
-          const double di = fi ? (fabs(v) > 1e-30 ? 1.0 / v : 1.0) : 1.0;
-          if (g.bdinv64) g.bdinv64[3 * a + i] = di;
-          if (g.bdinv32) g.bdinv32[3 * a + i] = (float)di;
-          if (!csr_pass && fi) {  // the K_ff diagonal the CSR pass would have written
-            const int r = g.ind_of[3 * a + i];
-            g.diag[r] = v;
-            g.dinv[r] = di;
-            if (g.dinv32) g.dinv32[r] = (float)di;
+        bool fj[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) fj[j] = g.ind_of[3 * (int64_t)b + j] >= 0;
+#pragma unroll
+        for (int ij = 0; ij < 9; ++ij) {
+          const int i = ij / 3, j = ij % 3;
+          double v;
+          float v32;
+          kval(s * 9 + ij, v, v32);
+          if (!(fi[i] && fj[j])) {
+            const bool dg = (b == a) && (i == j);
+            v = dg ? 1.0 : 0.0;
+            v32 = dg ? 1.f : 0.f;
           }
+          const int64_t pos = (int64_t)ij * g.nb + q0 + s;
+          if (g.bval64) g.bval64[pos] = v;
+          if (g.bval32) g.bval32[pos] = v32;
+        }
+      }
+      // 1 / diagonal, one division per lane on lanes 0..2 (linalg.rs:218-219 guard)
+      if (lane < 3) {
+        const int i = lane;
+        const int self = lower_bound_i32(s_adj, nadj, (int)a);
+        double v;
+        float v32;
+        kval(self * 9 + 4 * i, v, v32);
+        const bool f = g.ind_of[3 * a + i] >= 0;
+        const double di = f ? (fabs(v) > 1e-30 ? 1.0 / v : 1.0) : 1.0;
+        if (g.bdinv64) g.bdinv64[3 * a + i] = di;
+        if (g.bdinv32) g.bdinv32[3 * a + i] = (float)di;
+        if (!csr_pass && f) {  // the K_ff diagonal the CSR pass would have written
+          const int r = g.ind_of[3 * a + i];
+          g.diag[r] = v;
+          g.dinv[r] = di;
+          if (g.dinv32) g.dinv32[r] = (float)di;
         }
       }
     }
@@ -837,13 +918,20 @@ int run_gather(axia_ctx* ctx, GatherArgs args) {
   args.warp_stride = (int)per_warp;
   size_t stride = per_warp;
   size_t smem = stride * warps;
-  AXIA_CUDA(ctx, cudaFuncSetAttribute(k_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  void (*kern)(GatherArgs);
+  if (args.nn == 8)
+    kern = args.ke_dw ? k_gather<true, 8> : k_gather<false, 8>;
+  else if (args.nn == 20)
+    kern = args.ke_dw ? k_gather<true, 20> : k_gather<false, 20>;
+  else
+    kern = args.ke_dw ? k_gather<true, 0> : k_gather<false, 0>;
+  AXIA_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather, warps * 32, smem));
+  AXIA_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
   if (per_sm < 1) per_sm = 1;
   int64_t need = (args.n_nodes + warps - 1) / warps;
   int64_t grid = std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)per_sm * ctx->sm_count));
-  k_gather<<<(unsigned)grid, warps * 32, smem, ctx->stream>>>(args);
+  kern<<<(unsigned)grid, warps * 32, smem, ctx->stream>>>(args);
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());
   return AXIA_OK;
@@ -1147,6 +1235,8 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   ea.ke_out = ctx->d_ke;
   ea.vol_out = nullptr;
   ea.status = ctx->d_status;
+  ea.ke_dw = element_uses_dw(ctx, ctx->nn, ctx->reduced) ? 1 : 0;
+  ctx->ke_dw = ea.ke_dw != 0;
   AXIA_TRY(run_element_ke(ctx, ctx->nn, ctx->reduced, ea));
   cudaEventRecord(ev[1], s);
   if (csr64 && !ctx->d_val) AXIA_TRY(dev_alloc(ctx, &ctx->d_val, ctx->nnz));
@@ -1196,6 +1286,7 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   g.nb = ctx->nbq;
   g.uval = sym32 ? ctx->d_uval : nullptr;
   g.uptr = ctx->d_uptr;
+  g.ke_dw = ctx->ke_dw ? 1 : 0;
   // the gather's interval also holds the first-use allocations and clears above
   // (none after the first assembly of a mesh)
   AXIA_TRY(run_gather(ctx, g));

@@ -338,6 +338,7 @@ struct axia_ctx {
   // element stiffness scratch
   double* d_ke = nullptr;
   size_t ke_elems = 0;
+  bool ke_dw = false;           // d_ke holds double words (h, l) rather than FP64 (the last assembly)
 
   // solver vectors
   double* d_f = nullptr;        // [ndof]
@@ -413,6 +414,9 @@ struct axia_ctx {
 
   double ms_setup = 0.0, ms_assemble = 0.0;
   double ms_element = 0.0, ms_gather = 0.0;  // kernel times of the last numeric assembly (CUDA events)
+  // element stiffness arithmetic of C3D8 / C3D20 / C3D20R: double words on the
+  // FP32 pipe (default) or the FP64 Gauss loop (axia_gpu_set_element_arith)
+  bool element_fp64 = false;
   int64_t last_bad = -1;
 
   // device blocks of a released mesh state, kept for the next setup of the

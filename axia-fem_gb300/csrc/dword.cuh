@@ -1,0 +1,189 @@
+// dword.cuh -- double-word arithmetic: a value held as an unevaluated sum of
+// two FP32 numbers h + l (|l| <= ulp(h) / 2 once normalised), computed on
+// the FP32 pipe.
+//
+// GB300 executes FP64 at about 1/75 of its FP32 rate (measured: 1.05 against
+// 78 TFLOP/s), so FP64-accurate work that is compute bound runs faster as
+// error-free transformations of FP32 operations:
+//   * TwoSum (Knuth, TAOCP vol. 2, 4.2.2): s + e = a + b exactly, 6 adds;
+//   * TwoProduct with a fused multiply-add (the FMA form of Dekker's 1971
+//     product): p + e = a * b exactly, 2 operations;
+//   * compensated dot products (Ogita, Rump and Oishi, "Accurate sum and dot
+//     product", SIAM J. Sci. Comput. 26, 2005, algorithm Dot2), extended to
+//     double-word inputs by the two cross products a.h b.l + a.l b.h (the
+//     dropped a.l b.l is below 2^-48 |a b|): the result is as accurate as if
+//     computed in twice the FP32 precision and rounded, error about
+//     n^2 2^-48 sum |a_i b_i| in the worst case, ~2^-48 in practice.
+// Double-word values carry 48 significant bits against FP64's 53; the FP32
+// exponent range bounds them (|x| < 3.4e38; parts below 1.2e-38 lose
+// precision gradually), which every stiffness and geometry value here
+// respects by many orders of magnitude.
+//
+// Every operation is an explicit round-to-nearest intrinsic on the device so
+// the compiler cannot contract or reorder the transformations; host builds
+// (the tests' emulation) compile with -ffp-contract=off.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#ifdef __CUDACC__
+#define DW_FN __host__ __device__ __forceinline__
+#else
+#define DW_FN inline
+#endif
+
+struct alignas(8) dw {
+  float h, l;
+};
+
+namespace dwop {
+
+DW_FN float add(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+DW_FN float sub(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+DW_FN float mul(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+DW_FN float fma(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return std::fmaf(a, b, c);
+#endif
+}
+DW_FN float div(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdiv_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+
+// s + e = a + b exactly
+DW_FN void two_sum(float a, float b, float& s, float& e) {
+  s = add(a, b);
+  const float bb = sub(s, a);
+  e = add(sub(a, sub(s, bb)), sub(b, bb));
+}
+
+// s + e = a + b exactly, provided |a| >= |b| or a == 0
+DW_FN void fast_two_sum(float a, float b, float& s, float& e) {
+  s = add(a, b);
+  e = sub(b, sub(s, a));
+}
+
+// p + e = a * b exactly (barring underflow)
+DW_FN void two_prod(float a, float b, float& p, float& e) {
+  p = mul(a, b);
+  e = fma(a, b, -p);
+}
+
+}  // namespace dwop
+
+DW_FN dw dw_neg(dw a) { return dw{-a.h, -a.l}; }
+
+// An FP32 number as the FP64 number of the same value: normal numbers by
+// re-encoding their bits (exponent rebased by 1023 - 127, significand
+// shifted into place), zero, subnormals, inf and NaN by the conversion.
+DW_FN double f32_to_f64_exact(float f) {
+  uint32_t u;
+#ifdef __CUDA_ARCH__
+  u = __float_as_uint(f);
+#else
+  std::memcpy(&u, &f, 4);
+#endif
+  const uint32_t mag = u & 0x7fffffffu;
+  if (mag - 0x00800000u >= 0x7f000000u) return (double)f;  // not a normal number
+  const uint32_t hi = (u & 0x80000000u) | ((mag >> 3) + ((1023u - 127u) << 20));
+  const uint32_t lo = mag << 29;
+#ifdef __CUDA_ARCH__
+  return __hiloint2double((int)hi, (int)lo);
+#else
+  const uint64_t bits = ((uint64_t)hi << 32) | lo;
+  double d;
+  std::memcpy(&d, &bits, 8);
+  return d;
+#endif
+}
+
+// FP64 -> double word: h = fl32(x), l = fl32(x - h); x - h is exact in FP64.
+DW_FN dw dw_from_double(double x) {
+  const float h = (float)x;
+  return dw{h, (float)(x - f32_to_f64_exact(h))};
+}
+
+// Double word -> FP64: one FP64 add of two exactly re-encoded parts.
+DW_FN double dw_to_double(dw a) { return f32_to_f64_exact(a.h) + f32_to_f64_exact(a.l); }
+
+// a * b for double words (Dekker's product with the cross terms), normalised
+DW_FN dw dw_mul(dw a, dw b) {
+  float p, e;
+  dwop::two_prod(a.h, b.h, p, e);
+  e = dwop::fma(a.l, b.h, dwop::fma(a.h, b.l, e));
+  dw r;
+  dwop::fast_two_sum(p, e, r.h, r.l);
+  return r;
+}
+
+// a / b for double words: FP32 quotient, one correction from the remainder
+DW_FN dw dw_div(dw a, dw b) {
+  const float q1 = dwop::div(a.h, b.h);
+  float p, e;
+  dwop::two_prod(q1, b.h, p, e);
+  // a - q1 b = (a.h - p) - e + a.l - q1 b.l; a.h - p is exact (Sterbenz)
+  float r = dwop::sub(a.h, p);
+  r = dwop::sub(r, e);
+  r = dwop::add(r, a.l);
+  r = dwop::fma(-q1, b.l, r);
+  const float q2 = dwop::div(r, b.h);
+  dw q;
+  dwop::fast_two_sum(q1, q2, q.h, q.l);
+  return q;
+}
+
+// Compensated accumulator (Dot2): running FP32 sum s, every rounding error
+// and low-order part collected in c.
+struct dw_acc {
+  float s = 0.f, c = 0.f;
+};
+
+// acc += a * b
+DW_FN void dw_fma(dw_acc& acc, dw a, dw b) {
+  float p, e, s, t;
+  dwop::two_prod(a.h, b.h, p, e);
+  e = dwop::fma(a.l, b.h, dwop::fma(a.h, b.l, e));
+  dwop::two_sum(acc.s, p, s, t);
+  acc.s = s;
+  acc.c = dwop::add(acc.c, dwop::add(t, e));
+}
+
+// acc += a
+DW_FN void dw_add(dw_acc& acc, dw a) {
+  float s, t;
+  dwop::two_sum(acc.s, a.h, s, t);
+  acc.s = s;
+  acc.c = dwop::add(acc.c, dwop::add(t, a.l));
+}
+
+DW_FN dw dw_value(const dw_acc& acc) {
+  dw r;
+  dwop::two_sum(acc.s, acc.c, r.h, r.l);
+  return r;
+}

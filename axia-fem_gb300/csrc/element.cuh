@@ -65,6 +65,7 @@ struct ElemArgs {
   double* ke_out;        // [n_elem][KE]
   double* vol_out;       // [n_elem] or null
   DevStatus* status;
+  int ke_dw;             // double-word kernel only: Ke entries as FP32 pairs (h, l) instead of FP64
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {

@@ -9,8 +9,8 @@
 // Its device memory is one file-scope __device__ array (kScratchBytes, held by
 // every GPU that loads the library until the process exits): the element
 // tables, the status word and the staging of coordinates, moduli, Ke and
-// volumes.  The element kernel is the same element_ke_kernel the context path
-// runs.  Host code only ever passes the array's device address, which the
+// volumes.  The element kernels are the ones the context path runs by default
+// (double words for C3D8, the FP64 loop for C3D20 / C3D20R).  Host code only ever passes the array's device address, which the
 // first call on each device looks up with cudaGetSymbolAddress (with that
 // device current) and caches; that first call should come before any stream
 // capture.  Every call reuses the array: the status word is cleared at the
@@ -20,7 +20,7 @@
 // cudaDeviceReset (or any teardown of the primary context) are not supported.
 #include <mutex>
 
-#include "element.cuh"
+#include "element_dw.cuh"
 
 namespace {
 
@@ -165,8 +165,16 @@ int launch(unsigned char* base, int kind, const ElemArgs& args) {
   tab.e0 = reinterpret_cast<const int*>(t + v.off_e0);
   tab.e1 = reinterpret_cast<const int*>(t + v.off_e1);
   tab.blk = reinterpret_cast<const int*>(t + v.off_blk);
-  const size_t smem = element_smem_bytes<NN, NG>(WARPS);
-  auto kern = element_ke_kernel<NN, NG, WARPS>;
+  // the context path's default kernels: double words for C3D8, FP64 for C3D20(R)
+  size_t smem;
+  void (*kern)(ElemArgs, ElemTables);
+  if constexpr (NN == 8) {
+    smem = element_dw_smem_bytes<NN, NG>(WARPS);
+    kern = element_ke_dw_kernel<NN, NG, WARPS>;
+  } else {
+    smem = element_smem_bytes<NN, NG>(WARPS);
+    kern = element_ke_kernel<NN, NG, WARPS>;
+  }
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return AXIA_ERR_CUDA;
   int device = 0, sms = 0, per_sm = 0;

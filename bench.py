@@ -330,9 +330,12 @@ def same_sample_leg(args, local, n=CPU_SAMPLE_N):
     coarse_kw = dict(precision=L.PREC_MIXED, refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta,
                      matrix_format=L.FORMAT_BSR3, preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
 
-    def step64():
+    def step64():  # the reference's algorithm throughout (FP64 element stiffness too)
+        ctx.set_element_arith(L.ELEMENT_FP64)
         ctx.assemble_ex(L.ASM_CSR64)
-        return ctx.solve_device(f_dev.data_ptr(), u64.data_ptr(), rtol=RTOL, precision=L.PREC_FP64)
+        info = ctx.solve_device(f_dev.data_ptr(), u64.data_ptr(), rtol=RTOL, precision=L.PREC_FP64)
+        ctx.set_element_arith(L.ELEMENT_DWORD)
+        return info
 
     def stepco():
         ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
@@ -580,10 +583,12 @@ def run_c5(args):
     # node-block solve with the two-level preconditioner, both to rtol 1e-12
     fwd = dict(rtol=1e-12, precision=L.PREC_MIXED, refine_mode=L.REFINE_RELIABLE, inner_rtol=args.delta,
                matrix_format=L.FORMAT_BSR3, preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
+    ctx.set_element_arith(L.ELEMENT_FP64)  # the reference's algorithm throughout
     ctx.compliance_forward(m.rho, m.pexp, m.e0, f, rtol=1e-12)  # warm-up
     t0 = time.perf_counter()
     u64, c64, info64 = ctx.compliance_forward(m.rho, m.pexp, m.e0, f, rtol=1e-12)
     t_fwd64 = time.perf_counter() - t0
+    ctx.set_element_arith(L.ELEMENT_DWORD)
     ctx.compliance_forward(m.rho, m.pexp, m.e0, f, **fwd)  # warm-up
     t0 = time.perf_counter()
     u, c, info = ctx.compliance_forward(m.rho, m.pexp, m.e0, f, **fwd)
@@ -774,7 +779,8 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    def timed(asm_flags, solve_kw, u_dev):
+    def timed(asm_flags, solve_kw, u_dev, arith=L.ELEMENT_DWORD):
+        ctx.set_element_arith(arith)
         infos = []
         times = []
         for k in range(args.warmup + args.steps):
@@ -794,6 +800,7 @@ def main():
                 infos.append(info.as_dict())
         barrier()
         launches = ctx.kernel_launches() - l0
+        ctx.set_element_arith(L.ELEMENT_DWORD)
         ms = sum(times) / len(times)
         ms = replicas.max_over_ranks(ms, dist, f"cuda:{local}")
         return ms, infos, launches
@@ -815,7 +822,8 @@ def main():
         lanes_t, vec_t, us_t = ctx.autotune()
         tuned = {"lanes": lanes_t, "vec": vec_t, "us_per_iter": us_t}
     with ClockSampler(local) as clk:
-        ms64, inf64, la64 = timed(L.ASM_CSR64, fp64_kw, u64)
+        # the reference's algorithm throughout: FP64 element stiffness and assembly sums
+        ms64, inf64, la64 = timed(L.ASM_CSR64, fp64_kw, u64, L.ELEMENT_FP64)
         msmx, infmx, lamx = timed(L.ASM_BSR64 | L.ASM_BSR32, mixed_kw, umx)
         msmc, infmc, lamc = timed(L.ASM_CSR64 | L.ASM_CSR32, mixed_csr_kw, umc)
         msco, infco, laco = timed(L.ASM_BSR64 | L.ASM_BSR32, coarse_kw, uco)
@@ -870,27 +878,42 @@ def main():
     for v in spmv.values():
         v["frac_of_hbm"] = v["gbs"] / hbm
 
-    # assembly phases (CUDA events inside the library): the FP64-pipe-bound element
-    # kernel against the measured FP64 FMA rate, the gather against HBM
-    asm_t = []
-    for _ in range(4):
-        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
-        asm_t.append(ctx.assemble_times())
-    ms_el = statistics.median(a[0] for a in asm_t[1:])
-    ms_ga = statistics.median(a[1] for a in asm_t[1:])
+    # assembly phases (CUDA events inside the library), in both element
+    # arithmetics: double words on the FP32 pipe (the default; issue bound) and
+    # FP64 (the reference's; FP64-pipe bound), each against the measured FP64 FMA
+    # rate in FP64-equivalent flops, the gathers against HBM
+    def asm_times(arith):
+        ctx.set_element_arith(arith)
+        t = []
+        for _ in range(4):
+            ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+            t.append(ctx.assemble_times())
+        ctx.set_element_arith(L.ELEMENT_DWORD)
+        return statistics.median(a[0] for a in t[1:]), statistics.median(a[1] for a in t[1:])
+    ms_el64, ms_ga64 = asm_times(L.ELEMENT_FP64)
+    ms_el, ms_ga = asm_times(L.ELEMENT_DWORD)
+    ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
     fp64_peak = ctx.fma_rate(L.PREC_FP64)
     fp32_peak = ctx.fma_rate(L.PREC_MIXED)
     el_flops = element_fp64_flops(model.nn, 8) * model.n_elem
     ga_bytes = gather_bytes(model.n_elem, model.nn, nblocks, model.n_nodes)
     assembly = {"ms_element": ms_el, "ms_gather": ms_ga,
-                "element": {"kernel": "element_ke_kernel<8,8,8>", "bound": "fp64 pipe",
-                            "fp64_flops": el_flops, "achieved_tflops": el_flops / (ms_el * 1e-3) / 1e12,
-                            "peak_tflops": fp64_peak, "frac": el_flops / (ms_el * 1e-3) / 1e12 / fp64_peak,
-                            "peak_source": "axia_gpu_fma_rate (FP64 FMA chains on every SM, CUDA events)",
+                "element": {"kernel": "element_ke_dw_kernel<8,8,8>",
+                            "arith": "double words (FP32 pairs, 48 significant bits) on the FP32 pipe",
+                            "bound": "instruction issue (about 3,700 warp instructions per element)",
+                            "fp64_equivalent_flops": el_flops,
+                            "fp64_equivalent_tflops": el_flops / (ms_el * 1e-3) / 1e12,
+                            "x_fp64_fma_peak": el_flops / (ms_el * 1e-3) / 1e12 / fp64_peak,
                             "canonical_flops_per_element": 32872},
-                "gather": {"kernel": "k_gather", "bound": "hbm", "bytes": ga_bytes,
+                "element_fp64": {"kernel": "element_ke_kernel<8,8,8>", "bound": "fp64 pipe", "ms": ms_el64,
+                                 "achieved_tflops": el_flops / (ms_el64 * 1e-3) / 1e12, "peak_tflops": fp64_peak,
+                                 "frac": el_flops / (ms_el64 * 1e-3) / 1e12 / fp64_peak,
+                                 "peak_source": "axia_gpu_fma_rate (FP64 FMA chains on every SM, CUDA events)"},
+                "gather": {"kernel": "k_gather<true,8> (double-word sums)", "bound": "hbm", "bytes": ga_bytes,
                            "achieved_gbs": ga_bytes / (ms_ga * 1e-3) / 1e9,
                            "frac": ga_bytes / (ms_ga * 1e-3) / 1e9 / hbm},
+                "gather_fp64": {"kernel": "k_gather<false,8> (FP64 sums)", "ms": ms_ga64,
+                                "frac": ga_bytes / (ms_ga64 * 1e-3) / 1e9 / hbm},
                 "fp32_fma_tflops_measured": fp32_peak}
 
     # post-solve recovery of the mixed solution: nodal stress, strain, von Mises,
@@ -918,11 +941,13 @@ def main():
     rel_mc = float(np.linalg.norm(umc.cpu().numpy() - u64h) / np.linalg.norm(u64h))
     rel_co = float(np.linalg.norm(uco.cpu().numpy() - u64h) / np.linalg.norm(u64h))
     rel_cs = float(np.linalg.norm(ucs.cpu().numpy() - u64h) / np.linalg.norm(u64h))
+    ctx.set_element_arith(L.ELEMENT_FP64)
     ctx.assemble_ex(L.ASM_CSR64)
     utight = torch.empty_like(f_dev)
     with torch.cuda.stream(stream):
         itight = ctx.solve_device(f_dev.data_ptr(), utight.data_ptr(), rtol=1e-12, precision=L.PREC_FP64)
     torch.cuda.synchronize()
+    ctx.set_element_arith(L.ELEMENT_DWORD)
     uth = utight.cpu().numpy()
     tight = {"rtol": 1e-12, "iters": itight.iters, "true_rel_residual": itight.true_residual / itight.bnorm,
              "rel_err_fp64": float(np.linalg.norm(u64h - uth) / np.linalg.norm(uth)),

@@ -120,3 +120,21 @@ def test_setup_rejects_bad_input(gpu_ctx):
     assert e.value.code == _lib.ERR_NEG_JACOBIAN
     # the context is still usable
     gpu_ctx.setup(m).assemble()
+
+
+@pytest.mark.parametrize("name,model", _models()[1:4], ids=[n for n, _ in _models()[1:4]])
+def test_kff_fp64_element_arith_matches_oracle(gpu_ctx, name, model):
+    """The FP64 element arithmetic (AXIA_ELEMENT_FP64) assembles the same K_ff
+    within the same tolerance as the default double-word form."""
+    ref = O.solve_static(model, solver=O.SOLVER_PCG, tol=1e-6, keep_csr=True)
+    gpu_ctx.set_element_arith(_lib.ELEMENT_FP64)
+    try:
+        gpu_ctx.setup(model).assemble()
+        rp, col, val, diag, kfu0 = gpu_ctx.export_system()
+    finally:
+        gpu_ctx.set_element_arith(_lib.ELEMENT_DWORD)
+    import scipy.sparse as sp
+    n = ref.n_free
+    A = sp.csr_matrix((val, col, rp), shape=(n, n))
+    R = sp.csr_matrix((ref.data, ref.indices, ref.indptr), shape=(n, n))
+    assert abs(A - R).max() <= VTOL * np.abs(ref.data).max(), name

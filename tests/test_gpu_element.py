@@ -89,3 +89,53 @@ def test_element_ke_empty_and_large_batch(gpu_ctx):
     for k in (0, 1234, 4999):
         ref, _ = O.element_ke(xyz[k], 1.0, 0.25)
         assert np.abs(ke[k] - ref).max() <= TOL * np.abs(ref).max()
+
+
+def _placed_elems(nn, count, seed, offset, size, amp):
+    """Elements of edge ~size, corners/midsides moved by up to amp*size, placed up to offset from the origin."""
+    rng = np.random.default_rng(seed)
+    base = (meshgen.HEX20_XI[:nn].astype(float) + 1) / 2
+    out = np.empty((count, nn, 3))
+    for k in range(count):
+        scale = size * rng.uniform(0.5, 2.0, 3)
+        out[k] = base * scale + rng.uniform(-amp, amp, (nn, 3)) * scale.min() + rng.uniform(-offset, offset, 3)
+    return out
+
+
+@pytest.mark.parametrize("arith", [_lib.ELEMENT_DWORD, _lib.ELEMENT_FP64])
+@pytest.mark.parametrize("nn,reduced", [(8, False), (20, False), (20, True)])
+def test_element_arith_matches_oracle_across_sizes_and_offsets(gpu_ctx, arith, nn, reduced):
+    """Both element arithmetics against the oracle at 1e-12 of max|Ke|: element
+    edges from 1e-3 to 1e3, placed up to 100 edges from the origin.  The
+    double-word form works on coordinates relative to the element's first node,
+    scaled by a power of two, so size and placement cost it no accuracy."""
+    gpu_ctx.set_element_arith(arith)
+    try:
+        for size, offset in ((1e-3, 0.0), (1.0, 100.0), (1e3, 5e3), (0.05, 2.0)):
+            xyz = _placed_elems(nn, 24, seed=nn + 7 * reduced, offset=offset, size=size, amp=0.08)
+            e = np.random.default_rng(5).uniform(1e3, 2e11, xyz.shape[0])
+            ke, vol = gpu_ctx.element_ke(xyz, e, 0.3, reduced=reduced)
+            for k in range(xyz.shape[0]):
+                ref, rvol = O.element_ke(xyz[k], e[k], 0.3, reduced=reduced)
+                assert np.abs(ke[k] - ref).max() <= TOL * np.abs(ref).max(), (size, offset, k)
+                assert abs(vol[k] - rvol) <= 1e-12 * rvol, (size, offset, k)
+    finally:
+        gpu_ctx.set_element_arith(_lib.ELEMENT_DWORD)
+
+
+def test_element_dword_close_to_fp64(gpu_ctx):
+    """The double-word Ke differs from the FP64 kernel's by a few 1e-14 of max|Ke|
+    on moderately distorted elements, and the two assemble the same K structure."""
+    xyz = _rand_elems(8, 500, seed=31)
+    ke_dw, vol_dw = gpu_ctx.element_ke(xyz, 2e5, 0.3)
+    gpu_ctx.set_element_arith(_lib.ELEMENT_FP64)
+    try:
+        ke64, vol64 = gpu_ctx.element_ke(xyz, 2e5, 0.3)
+    finally:
+        gpu_ctx.set_element_arith(_lib.ELEMENT_DWORD)
+    worst = max(np.abs(ke_dw[k] - ke64[k]).max() / np.abs(ke64[k]).max() for k in range(xyz.shape[0]))
+    assert worst <= 1e-13, worst
+    assert np.abs(vol_dw - vol64).max() <= 1e-13 * np.abs(vol64).max()
+    with pytest.raises(_lib.AxiaError) as e:
+        gpu_ctx.set_element_arith(2)
+    assert e.value.code == _lib.ERR_INVALID_ARG
