@@ -44,6 +44,7 @@ ASM_CSR32 = 2
 ASM_BSR64 = 4
 ASM_BSR32 = 8
 ASM_SYM32 = 16
+ASM_BSR32LO = 32
 FORMAT_CSR = 0
 FORMAT_BSR3 = 1
 FORMAT_BSR3_SYM = 2

@@ -108,6 +108,8 @@ void free_mesh_state(axia_ctx* ctx) {
   ctx->nbq = 0;
   dev_release(ctx, ctx->d_bval64);
   dev_release(ctx, ctx->d_bval32);
+  dev_release(ctx, ctx->d_bval32lo);
+  ctx->have_bsr32lo = false;
   dev_release(ctx, ctx->d_uptr);
   dev_release(ctx, ctx->d_uval);
   dev_release(ctx, ctx->d_lptr);
@@ -147,7 +149,7 @@ void free_mesh_state(axia_ctx* ctx) {
   dev_release(ctx, ctx->d_rec);
   ctx->have_forward = false;
   ctx->vec_capacity = 0;
-  ctx->assembled = ctx->have32 = ctx->have_csr64 = ctx->have_bsr64 = ctx->have_bsr32 = false;
+  ctx->assembled = ctx->have32 = ctx->have_csr64 = ctx->have_bsr64 = ctx->have_bsr32 = ctx->have_bsr32lo = false;
   ctx->n_free = ctx->nnz = 0;
 }
 
@@ -354,7 +356,9 @@ int32_t axia_gpu_assemble_ex(axia_ctx* ctx, int32_t flags) {
   if (!ctx) return AXIA_ERR_INVALID_ARG;
   AXIA_TRY(use_device(ctx));
   if (!ctx->d_rowptr || !ctx->d_conn) return set_error(ctx, AXIA_ERR_STATE, "assemble before setup");
-  if (flags <= 0 || flags > 31) return set_error(ctx, AXIA_ERR_INVALID_ARG, "assemble: unknown matrix forms");
+  if (flags <= 0 || flags > 63) return set_error(ctx, AXIA_ERR_INVALID_ARG, "assemble: unknown matrix forms");
+  if ((flags & AXIA_ASM_BSR32LO) && !(flags & AXIA_ASM_BSR32))
+    return set_error(ctx, AXIA_ERR_INVALID_ARG, "assemble: AXIA_ASM_BSR32LO needs AXIA_ASM_BSR32");
   EventTimer t(ctx->stream);
   int st = numeric_assemble(ctx, flags);
   ctx->ms_assemble = t.stop_ms();

@@ -689,6 +689,7 @@ struct GatherArgs {
   double* kfu0;
   double* bval64;     // node-block values [9][nb] (null: not assembled)
   float* bval32;
+  float* bval32lo;    // fl32(K64 - K32) [9][nb] (null: not assembled)
   double* bdinv64;    // full-DOF 1/diag, 1 on prescribed DOFs
   float* bdinv32;
   const int32_t* qptr;  // padded node-block row starts
@@ -789,16 +790,22 @@ __global__ void k_gather(GatherArgs g) {
         for (int m = 0; m < GATHER_VPL; ++m) cur[m] = nxt[m];
       }
     }
-    // the summed entry idx in FP64 and FP32
-    auto kval = [&](int idx, double& v64, float& v32) {
+    // the summed entry idx in FP64, in FP32 and the FP32 low part fl32(v64 - v32)
+    auto kval3 = [&](int idx, double& v64, float& v32, float& lo) {
       if constexpr (DWK) {
         const dw v = dw_value(acw[idx]);
         v64 = dw_to_double(v);
         v32 = v.h;
+        lo = v.l;
       } else {
         v64 = acc[idx];
         v32 = (float)v64;
+        lo = g.bval32lo ? (float)(v64 - f32_to_f64_exact(v32)) : 0.f;
       }
+    };
+    auto kval = [&](int idx, double& v64, float& v32) {
+      float lo;
+      kval3(idx, v64, v32, lo);
     };
     // K_ff in CSR, and K_fp u0 -- skipped for a node-block-only assembly
     // without prescribed values (the diagonal is then written below)
@@ -874,16 +881,18 @@ __global__ void k_gather(GatherArgs g) {
         for (int ij = 0; ij < 9; ++ij) {
           const int i = ij / 3, j = ij % 3;
           double v;
-          float v32;
-          kval(s * 9 + ij, v, v32);
+          float v32, lo;
+          kval3(s * 9 + ij, v, v32, lo);
           if (!(fi[i] && fj[j])) {
             const bool dg = (b == a) && (i == j);
             v = dg ? 1.0 : 0.0;
             v32 = dg ? 1.f : 0.f;
+            lo = 0.f;
           }
           const int64_t pos = (int64_t)ij * g.nb + q0 + s;
           if (g.bval64) g.bval64[pos] = v;
           if (g.bval32) g.bval32[pos] = v32;
+          if (g.bval32lo) g.bval32lo[pos] = lo;
         }
       }
       // 1 / diagonal, one division per lane on lanes 0..2 (linalg.rs:218-219 guard)
@@ -1205,6 +1214,7 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   const bool csr64 = flags & AXIA_ASM_CSR64, csr32 = flags & AXIA_ASM_CSR32;
   const bool bsr64 = flags & AXIA_ASM_BSR64, bsr32 = flags & AXIA_ASM_BSR32;
   const bool sym32 = flags & AXIA_ASM_SYM32;
+  const bool bsr32lo = bsr32 && (flags & AXIA_ASM_BSR32LO);
   if (sym32) AXIA_TRY(ensure_sym_structure(ctx));
   if (csr64 || csr32) AXIA_TRY(ensure_csr_columns(ctx));
   const int64_t kesz = (int64_t)9 * ctx->nn * ctx->nn;
@@ -1254,6 +1264,10 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
     AXIA_TRY(dev_alloc(ctx, &ctx->d_bval32, (size_t)(9 * ctx->nbq)));
     AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bval32, 0, (size_t)(9 * ctx->nbq) * sizeof(float), s));
   }
+  if (bsr32lo && !ctx->d_bval32lo) {
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_bval32lo, (size_t)(9 * ctx->nbq)));
+    AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bval32lo, 0, (size_t)(9 * ctx->nbq) * sizeof(float), s));
+  }
   if ((bsr64 || bsr32 || sym32) && !ctx->d_bdinv64) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv64, (size_t)ctx->ndof));
   if ((bsr32 || sym32) && !ctx->d_bdinv32) AXIA_TRY(dev_alloc(ctx, &ctx->d_bdinv32, (size_t)ctx->ndof));
   AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_kfu0, 0, ctx->n_free * sizeof(double), s));
@@ -1280,6 +1294,7 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   g.kfu0 = ctx->d_kfu0;
   g.bval64 = bsr64 ? ctx->d_bval64 : nullptr;
   g.bval32 = bsr32 ? ctx->d_bval32 : nullptr;
+  g.bval32lo = bsr32lo ? ctx->d_bval32lo : nullptr;
   g.bdinv64 = (bsr64 || bsr32 || sym32) ? ctx->d_bdinv64 : nullptr;
   g.bdinv32 = (bsr32 || sym32) ? ctx->d_bdinv32 : nullptr;
   g.qptr = ctx->d_qptr;
@@ -1301,7 +1316,7 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   }
   DevStatus hs;
   AXIA_TRY(read_dev_status(ctx, &hs));
-  ctx->have_csr64 = ctx->have32 = ctx->have_bsr64 = ctx->have_bsr32 = ctx->have_sym32 = false;
+  ctx->have_csr64 = ctx->have32 = ctx->have_bsr64 = ctx->have_bsr32 = ctx->have_sym32 = ctx->have_bsr32lo = false;
   ctx->assembled = false;
   if (hs.first_error != ~0ull) {
     int code = (int)(hs.first_error & 0xff);
@@ -1316,6 +1331,7 @@ int numeric_assemble(axia_ctx* ctx, int flags) {
   ctx->have32 = csr32;
   ctx->have_bsr64 = bsr64;
   ctx->have_bsr32 = bsr32;
+  ctx->have_bsr32lo = bsr32lo;
   ctx->have_sym32 = sym32;
   ctx->assembled = true;
   ctx->assemble_gen++;

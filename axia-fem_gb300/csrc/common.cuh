@@ -321,6 +321,8 @@ struct axia_ctx {
   double* d_bdinv64 = nullptr;     // [ndof]
   float* d_bdinv32 = nullptr;      // [ndof]
   bool have_bsr64 = false, have_bsr32 = false;
+  float* d_bval32lo = nullptr;     // [9][nbq] fl32(K64 - K32) (AXIA_ASM_BSR32LO)
+  bool have_bsr32lo = false;
 
   // symmetric node-block form of the FP32 matrix (AXIA_ASM_SYM32): every block
   // K_ab with b >= a stored once, in row a, as 10 floats (the 9 values row-major

@@ -44,45 +44,6 @@ constexpr size_t element_dw_smem_bytes(int warps) {
   return (size_t)(ElemDwTraits<NN, NG>::TAB + warps * ElemTraits<NN, NG>::WARP_DOUBLES) * sizeof(double);
 }
 
-// 2^e as an FP64 number, e in [-1022, 1023]
-__device__ __forceinline__ double pow2(int e) {
-  return __longlong_as_double((long long)(1023 + e) << 52);
-}
-
-// x 2^-k as a double word from the bits of x with integer operations only:
-// h = its leading 24 significant bits, l = the next 24 (both truncated, so
-// |x 2^-k - h - l| < 2^-47 |x 2^-k|).  Zero, subnormal, non-finite and
-// out-of-range values (|x 2^-k| outside [2^-74, 2^127)) go through the FP64
-// conversion.
-__device__ __forceinline__ dw dw_split_scaled(double x, int k) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7ff) - k;  // biased exponent of x 2^-k
-  if ((unsigned)(e - 949) > (unsigned)(1150 - 949) || ((b >> 52) & 0x7ff) == 0 || ((b >> 52) & 0x7ff) == 0x7ff)
-    return dw_from_double(x * pow2(-k));
-  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-  const unsigned long long m = b & 0xfffffffffffffull;
-  const float h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29));
-  const unsigned r = (unsigned)(m & 0x1fffffffu);  // value r 2^(e - 1075)
-  float l = 0.f;
-  if (r) {
-    const int p = 31 - __clz(r);                   // top bit of r, 0..28
-    const unsigned frac = p >= 23 ? (r >> (p - 23)) & 0x7fffffu : (r << (23 - p)) & 0x7fffffu;
-    l = __uint_as_float(sign | ((unsigned)(p + e - 948) << 23) | frac);
-  }
-  return dw{h, l};
-}
-
-// a 2^k for a double word, |k| <= 100 (exact: a power-of-two product of each part)
-__device__ __forceinline__ dw dw_scale(dw a, int k) {
-  const float s = __uint_as_float((unsigned)(127 + k) << 23);
-  return dw{__fmul_rn(a.h, s), __fmul_rn(a.l, s)};
-}
-
-// FP64 finiteness and positivity from the bits (no FP64 instruction)
-__device__ __forceinline__ bool finite_bits(double x) {
-  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
-}
-
 // Three blocks of 8 warps per SM (their shared memory fits three).
 template <int NN, int NG, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 3)
