@@ -903,14 +903,24 @@ __global__ void k_gather(GatherArgs g) {
         float v32;
         kval(self * 9 + 4 * i, v, v32);
         const bool f = g.ind_of[3 * a + i] >= 0;
-        const double di = f ? (fabs(v) > 1e-30 ? 1.0 / v : 1.0) : 1.0;
+        double di;
+        float di32;
+        if constexpr (DWK) {  // 1 / d in double words (48 bits) on the FP32 pipe
+          const dw d = dw_value(acw[self * 9 + 4 * i]);
+          const dw q = f && fabsf(d.h) > 1e-30f ? dw_div(dw{1.f, 0.f}, d) : dw{1.f, 0.f};
+          di = dw_to_double(q);
+          di32 = q.h;
+        } else {
+          di = f ? (fabs(v) > 1e-30 ? 1.0 / v : 1.0) : 1.0;
+          di32 = (float)di;
+        }
         if (g.bdinv64) g.bdinv64[3 * a + i] = di;
-        if (g.bdinv32) g.bdinv32[3 * a + i] = (float)di;
+        if (g.bdinv32) g.bdinv32[3 * a + i] = di32;
         if (!csr_pass && f) {  // the K_ff diagonal the CSR pass would have written
           const int r = g.ind_of[3 * a + i];
           g.diag[r] = v;
           g.dinv[r] = di;
-          if (g.dinv32) g.dinv32[r] = (float)di;
+          if (g.dinv32) g.dinv32[r] = di32;
         }
       }
     }
