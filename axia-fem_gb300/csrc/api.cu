@@ -132,6 +132,11 @@ void free_mesh_state(axia_ctx* ctx) {
   dev_release(ctx, ctx->d_mB);
   dev_release(ctx, ctx->d_mX);
   dev_release(ctx, ctx->d_mX32);
+  dev_release(ctx, ctx->d_mXh);
+  dev_release(ctx, ctx->d_mXl);
+  ctx->seg_capacity = 0;
+  if (ctx->d_mstate) cudaFree(ctx->d_mstate);
+  ctx->d_mstate = nullptr;
   dev_release(ctx, ctx->d_mR32);
   dev_release(ctx, ctx->d_mP32);
   dev_release(ctx, ctx->d_mQ32);

@@ -17,6 +17,7 @@
 #include <string>
 
 #include "coarse.cuh"
+#include "dword.cuh"
 
 namespace {
 
@@ -278,6 +279,18 @@ struct MultiOut {
   long long col_iters[NR];
 };
 
+// The per-case state of pcg_bsr_multi_kernel between launches when it runs
+// in segments (MultiArgs::split): the kernel stops at each reliable update,
+// the update runs as its own launches, and the kernel resumes from here.
+struct BatchState {
+  long long it, iters;
+  int updates;
+  int phase;  // 1: stopped for a reliable update, 0: finished
+  double rz[NR], bnorm[NR], rmax[NR], res[NR], rrec[NR];
+  int active[NR];
+  long long citers[NR];
+};
+
 struct MultiArgs {
   BsrMatM<float> M32;
   BsrMatM<double> M64;
@@ -299,6 +312,9 @@ struct MultiArgs {
   long long max_iter;
   unsigned long long limit_ns;
   CoarseArgs C;         // two-level preconditioner (n_sub = 0: Jacobi only)
+  BatchState* state = nullptr;
+  int split = 0;        // stop at every reliable update (state saved, phase 1)
+  int resume = 0;       // start from state, after an update whose |r|^2 and r.D^-1 r are in totals
 };
 
 constexpr int SL_A = 0, SL_B = NR;  // two banks of NR slots
@@ -487,7 +503,8 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
   float* const ring = reinterpret_cast<float*>(s_stage);
   __shared__ double s_rz[NR], s_bnorm[NR], s_rmax[NR], s_res[NR];
   __shared__ float s_alpha[NR], s_beta[NR];
-  __shared__ int s_active[NR], s_flag;
+  __shared__ int s_active[NR], s_flag, s_restart[NR];
+  __shared__ double s_rrec[NR];  // recurrence |r| of each case when the last update was triggered
   __shared__ long long s_citers[NR];
   const int nd = P.nd, n_nodes = P.M32.n_nodes;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
@@ -495,8 +512,79 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
   const int gwarp = tid >> 5, nwarps = nth >> 5;
   const int cq = tid % LPG;            // this thread's column quad in the vector phases
   const long long nq = (long long)nd * LPG;  // float4 chunks of an [nd][NR] vector
+  // the bookkeeping after a reliable update whose |r|^2 (slots SL_A) is in
+  // totals.  A case whose true residual came back more than twice its
+  // recurrence residual restarts its search direction (beta = 0): the
+  // replaced residual no longer fits the old directions, and carrying them on
+  // let the FP32 recurrence of an ill-conditioned case wander instead of
+  // converging.
+  auto after_update = [&](int& updates) {
+    ++updates;
+    if (threadIdx.x < NR) {
+      const int c = threadIdx.x;
+      const double rn = sqrt(__ldcg(P.totals + SL_A + c));
+      s_restart[c] = 0;
+      if (s_active[c]) {
+        s_restart[c] = rn > 2.0 * s_rrec[c];
+        s_res[c] = rn;
+        s_rmax[c] = rn;
+        if (rn <= P.tol * s_bnorm[c]) s_active[c] = 0;  // converged
+      }
+    }
+    __syncthreads();
+  };
+  // the end of an iteration: the coarse correction of r, beta, p = z + beta p
+  auto iteration_tail = [&]() -> bool {
+    if constexpr (COARSE) {
+      if (!coarse_step_m(P, gwarp, nwarps, lane, ring)) return false;
+    }
+    if (threadIdx.x < NR) {
+      const int c = threadIdx.x;
+      double rzn = __ldcg(P.totals + SL_B + c);
+      if constexpr (COARSE) rzn += __ldcg(P.totals + SL_A + c);
+      s_beta[c] = s_active[c] && !s_restart[c] ? (float)(rzn / s_rz[c]) : 0.f;
+      s_restart[c] = 0;
+      s_rz[c] = rzn;
+    }
+    __syncthreads();
+    for (long long q = tid; q < nq; q += nth) {
+      const long long row = q / LPG;
+      const int c0 = CPL * (int)(q % LPG);
+      float p[CPL], r[CPL], zc[CPL] = {0.f, 0.f, 0.f, 0.f};
+      ld4(P.P32 + q * CPL, p);
+      ld4(P.R32 + q * CPL, r);
+      if constexpr (COARSE) coarse_prolong_m(P.C, row, c0, zc);
+      const float di = P.dinv32[row];
+#pragma unroll
+      for (int c = 0; c < CPL; ++c)
+        p[c] = s_active[c0 + c] ? fmaf(s_beta[c0 + c], p[c], fmaf(r[c], di, zc[c])) : 0.f;
+      st4(P.P32 + q * CPL, p);
+    }
+    return grid_sync(P.bar, P.st, P.limit_ns);
+  };
+  long long it0 = 0, iters0 = 0;
+  int updates0 = 0;
+  if (P.resume) {  // the rest of the iteration that stopped for the update
+    if (threadIdx.x < NR) {
+      const int c = threadIdx.x;
+      s_rz[c] = P.state->rz[c];
+      s_bnorm[c] = P.state->bnorm[c];
+      s_rmax[c] = P.state->rmax[c];
+      s_res[c] = P.state->res[c];
+      s_active[c] = P.state->active[c];
+      s_citers[c] = P.state->citers[c];
+      s_rrec[c] = P.state->rrec[c];
+      s_restart[c] = 0;
+    }
+    it0 = P.state->it + 1;
+    iters0 = P.state->iters;
+    updates0 = P.state->updates;
+    __syncthreads();
+    after_update(updates0);
+    if (!iteration_tail()) return;
+  }
   // init: x = 0, r32 = b, p = z = r32 / diag, per-column r.z and b.b
-  {
+  if (!P.resume) {
     float rz_p[CPL] = {0, 0, 0, 0};
     double bb_p[CPL] = {0, 0, 0, 0};
     for (long long q = tid; q < nq; q += nth) {
@@ -523,6 +611,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
     __syncthreads();
     block_partials_cols<float>(rz_p, P.partials, SL_B);
   }
+  if (!P.resume) {
   if (!grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, 0, 2 * NR)) return;
   if (threadIdx.x < NR) {
     const int c = threadIdx.x;
@@ -532,6 +621,8 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
     s_res[c] = s_bnorm[c];
     s_active[c] = s_bnorm[c] >= 1e-30;
     s_citers[c] = 0;
+    s_restart[c] = 0;
+    s_rrec[c] = s_bnorm[c];
     if (!s_active[c]) s_res[c] = 0.0;
   }
   __syncthreads();
@@ -548,9 +639,10 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
     }
     if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
   }
-  long long iters = 0;
-  int updates = 0, status = AXIA_OK;
-  for (long long it = 0; it < P.max_iter; ++it) {
+  }
+  long long iters = iters0;
+  int updates = updates0, status = AXIA_OK;
+  for (long long it = it0; it < P.max_iter; ++it) {
     int any = 0;
     for (int c = 0; c < NR; ++c) any |= s_active[c];
     if (!any) break;
@@ -636,6 +728,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
         if (!s_active[c]) continue;
         seen = 1;
         const double rn = sqrt(__ldcg(P.totals + SL_A + c));
+        s_rrec[c] = rn;
         if (!isfinite(rn)) candidate = 1;
         if (rn > P.delta * s_rmax[c]) all_dropped = 0;
         if (rn <= P.tol * s_bnorm[c]) candidate = 1;
@@ -643,6 +736,27 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
       s_flag = seen && (all_dropped || candidate);
     }
     __syncthreads();
+    if (s_flag && P.split) {  // the update runs as its own launches; resume from the state
+      if (blockIdx.x == 0) {
+        if (threadIdx.x < NR) {
+          const int c = threadIdx.x;
+          P.state->rz[c] = s_rz[c];
+          P.state->bnorm[c] = s_bnorm[c];
+          P.state->rmax[c] = s_rmax[c];
+          P.state->res[c] = s_res[c];
+          P.state->active[c] = s_active[c];
+          P.state->citers[c] = s_citers[c];
+          P.state->rrec[c] = s_rrec[c];
+        }
+        if (threadIdx.x == 0) {
+          P.state->it = it;
+          P.state->iters = iters;
+          P.state->updates = updates;
+          P.state->phase = 1;
+        }
+      }
+      return;
+    }
     if (s_flag) {
       // reliable update for all columns: x += x32, r = b - K x (FP64), r32 = r
       for (long long q = tid; q < nq; q += nth) {
@@ -685,43 +799,9 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
       __syncthreads();
       block_partials_cols<float>(rz2, P.partials, SL_B);
       if (!grid_reduce_sync_wide(P.bar, P.st, P.limit_ns, P.partials, P.totals, 0, 2 * NR)) return;
-      ++updates;
-      if (threadIdx.x < NR) {
-        const int c = threadIdx.x;
-        const double rn = sqrt(__ldcg(P.totals + SL_A + c));
-        if (s_active[c]) {
-          s_res[c] = rn;
-          s_rmax[c] = rn;
-          if (rn <= P.tol * s_bnorm[c]) s_active[c] = 0;  // converged
-        }
-      }
-      __syncthreads();
+      after_update(updates);
     }
-    if constexpr (COARSE) {
-      if (!coarse_step_m(P, gwarp, nwarps, lane, ring)) return;
-    }
-    if (threadIdx.x < NR) {
-      const int c = threadIdx.x;
-      double rzn = __ldcg(P.totals + SL_B + c);
-      if constexpr (COARSE) rzn += __ldcg(P.totals + SL_A + c);
-      s_beta[c] = s_active[c] ? (float)(rzn / s_rz[c]) : 0.f;
-      s_rz[c] = rzn;
-    }
-    __syncthreads();
-    for (long long q = tid; q < nq; q += nth) {
-      const long long row = q / LPG;
-      const int c0 = CPL * (int)(q % LPG);
-      float p[CPL], r[CPL], zc[CPL] = {0.f, 0.f, 0.f, 0.f};
-      ld4(P.P32 + q * CPL, p);
-      ld4(P.R32 + q * CPL, r);
-      if constexpr (COARSE) coarse_prolong_m(P.C, row, c0, zc);
-      const float di = P.dinv32[row];
-#pragma unroll
-      for (int c = 0; c < CPL; ++c)
-        p[c] = s_active[c0 + c] ? fmaf(s_beta[c0 + c], p[c], fmaf(r[c], di, zc[c])) : 0.f;
-      st4(P.P32 + q * CPL, p);
-    }
-    if (!grid_sync(P.bar, P.st, P.limit_ns)) return;
+    if (!iteration_tail()) return;
   }
   int any_active = 0, broke = 0;
   for (int c = 0; c < NR; ++c) {
@@ -739,8 +819,175 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
       P.out->iters = iters;
       P.out->updates = updates;
       P.out->status = status;
+      if (P.state) P.state->phase = 0;
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Reliable update of the segmented batched solve, as its own launches:
+// X += X32 (and X as double words), then R = B - K X with one warp per node
+// row and lane c = load case c, then the per-case sums in a fixed order.
+// The residual is computed in double words from the FP32 matrix and its low
+// parts (K32 + K32lo holds K to 48 bits; FP32-pipe work instead of 9 FP64
+// multiply-adds per block and case), or in FP64 from the FP64 matrix.
+// ---------------------------------------------------------------------------
+__global__ void k_batch_fold(long long n, double* X, float* X32, float* Xh, float* Xl, int split_dw) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const double x = X[t] + (double)X32[t];
+    X[t] = x;
+    X32[t] = 0.f;
+    if (split_dw) {
+      const dw xs = dw_split_scaled(x, 0);
+      Xh[t] = xs.h;
+      Xl[t] = xs.l;
+    }
+  }
+}
+
+template <bool DW>
+__global__ void __launch_bounds__(256) k_batch_resid(BsrMatM<float> M32, const float* __restrict__ lo32,
+                                                    BsrMatM<double> M64, const double* __restrict__ B,
+                                                    const double* __restrict__ X, const float* __restrict__ Xh,
+                                                    const float* __restrict__ Xl, const float* __restrict__ dinv32,
+                                                    float* R32, double* part, unsigned cases) {
+  __shared__ double s_rr[8][NR], s_rz[8][NR];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const bool on = (cases >> lane) & 1u;  // the cases (lanes) this pass computes
+  const int n = M32.n_nodes;
+  const long long nb = M32.nb;
+  double rr = 0.0, rz = 0.0;
+  for (int a = blockIdx.x * 8 + w; on && a < n; a += gridDim.x * 8) {
+    const int beg = __ldg(M32.adj_ptr + a), end = __ldg(M32.adj_ptr + a + 1);
+    double y[3];
+    if constexpr (DW) {
+      dw_acc acc[3];
+      for (int s = beg; s < end; ++s) {
+        const int b = __ldg(M32.adj + s);
+        dw xv[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const size_t o = (size_t)(3 * b + j) * NR + lane;
+          xv[j] = dw{Xh[o], Xl[o]};
+        }
+#pragma unroll
+        for (int p = 0; p < 9; ++p)
+          dw_fma(acc[p / 3], dw{__ldg(M32.val + p * nb + s), __ldg(lo32 + p * nb + s)}, xv[p % 3]);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) y[i] = dw_to_double(dw_value(acc[i]));
+    } else {
+      y[0] = y[1] = y[2] = 0.0;
+      for (int s = beg; s < end; ++s) {
+        const int b = __ldg(M64.adj + s);
+        double xv[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) xv[j] = X[(size_t)(3 * b + j) * NR + lane];
+#pragma unroll
+        for (int p = 0; p < 9; ++p) y[p / 3] = fma(__ldg(M64.val + p * nb + s), xv[p % 3], y[p / 3]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const size_t o = (size_t)(3 * a + i) * NR + lane;
+      const double r = B[o] - y[i];
+      rr = fma(r, r, rr);
+      const float r32 = (float)r;
+      R32[o] = r32;
+      rz += (double)(r32 * (r32 * __ldg(dinv32 + 3 * a + i)));
+    }
+  }
+  s_rr[w][lane] = rr;
+  s_rz[w][lane] = rz;
+  __syncthreads();
+  if (w == 0 && on) {  // the other cases keep the partials of an earlier pass
+    double a = 0.0, b = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      a += s_rr[k][lane];
+      b += s_rz[k][lane];
+    }
+    part[(size_t)lane * gridDim.x + blockIdx.x] = a;
+    part[(size_t)(NR + lane) * gridDim.x + blockIdx.x] = b;
+  }
+}
+
+// The FP64 residual for a few cases only: KP lanes per node row (the cases
+// list[0 .. n-1] on lanes 0 .. n-1 of each group, KP the power of two >= n),
+// 32 / KP rows per warp, so the FP64 work follows the number of cases (the
+// FP64 pipe charges a warp instruction in full whatever its active lanes).
+// Partials of the listed cases only; the others keep an earlier pass's.
+struct CaseList {
+  int n;
+  int c[NR];
+};
+
+template <int KP>
+__global__ void __launch_bounds__(256) k_batch_resid64_cases(BsrMatM<double> M64, const double* __restrict__ B,
+                                                            const double* __restrict__ X,
+                                                            const float* __restrict__ dinv32, float* R32,
+                                                            double* part, CaseList list) {
+  __shared__ double s_rr[8][32], s_rz[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int sub = lane % KP, grp = lane / KP;
+  constexpr int RPW = 32 / KP;
+  const bool on = sub < list.n;
+  const int c = on ? list.c[sub] : 0;
+  const int n = M64.n_nodes;
+  const long long nb = M64.nb;
+  double rr = 0.0, rz = 0.0;
+  for (int base = (blockIdx.x * 8 + w) * RPW; base < n; base += gridDim.x * 8 * RPW) {
+    const int a = base + grp;
+    if (!on || a >= n) continue;
+    const int beg = __ldg(M64.adj_ptr + a), end = __ldg(M64.adj_ptr + a + 1);
+    double y[3] = {0.0, 0.0, 0.0};
+    for (int s = beg; s < end; ++s) {
+      const int b = __ldg(M64.adj + s);
+      double xv[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) xv[j] = X[(size_t)(3 * b + j) * NR + c];
+#pragma unroll
+      for (int p = 0; p < 9; ++p) y[p / 3] = fma(__ldg(M64.val + p * nb + s), xv[p % 3], y[p / 3]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const size_t o = (size_t)(3 * a + i) * NR + c;
+      const double r = B[o] - y[i];
+      rr = fma(r, r, rr);
+      const float r32 = (float)r;
+      R32[o] = r32;
+      rz += (double)(r32 * (r32 * __ldg(dinv32 + 3 * a + i)));
+    }
+  }
+  // the warp's rows of one case: lanes sub, sub + KP, ... (fixed order)
+#pragma unroll
+  for (int o = KP; o < 32; o <<= 1) {
+    rr += __shfl_xor_sync(0xffffffffu, rr, o);
+    rz += __shfl_xor_sync(0xffffffffu, rz, o);
+  }
+  s_rr[w][lane] = rr;
+  s_rz[w][lane] = rz;
+  __syncthreads();
+  if (w == 0 && lane < list.n) {
+    double a = 0.0, b = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      a += s_rr[k][lane];
+      b += s_rz[k][lane];
+    }
+    part[(size_t)list.c[lane] * gridDim.x + blockIdx.x] = a;
+    part[(size_t)(NR + list.c[lane]) * gridDim.x + blockIdx.x] = b;
+  }
+}
+
+// totals[k] = sum over the g blocks of part[k][.], ascending block order (one warp per slot)
+__global__ void k_batch_resid_sum(const double* part, int g, double* totals) {
+  const int lane = threadIdx.x & 31, k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (k >= 2 * NR) return;
+  double a = 0.0;
+  for (int b = lane; b < g; b += 32) a += part[(size_t)k * g + b];
+  a = warp_sum(a);
+  if (lane == 0) totals[k] = a;
 }
 
 // B[d][c] = f_c[d] - K_fp u0 (free d), 0 (prescribed d); columns >= nrhs zero
@@ -1505,6 +1752,112 @@ int batch_block_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, c
 }
 
 // Solves nrhs load cases (F, U: [nrhs][nd] device arrays) 32 at a time.
+int ensure_segment_buffers(axia_ctx* ctx) {
+  const size_t blk = (size_t)ctx->ndof * NR;
+  if (ctx->seg_capacity < blk) {
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_mXh, blk));
+    AXIA_TRY(dev_alloc(ctx, &ctx->d_mXl, blk));
+    ctx->seg_capacity = blk;
+  }
+  if (!ctx->d_mstate) {
+    BatchState* st = nullptr;
+    AXIA_CUDA(ctx, cudaMalloc(&st, sizeof(BatchState)));
+    ctx->d_mstate = st;
+  }
+  return AXIA_OK;
+}
+
+// The batched kernel in segments: it stops at each reliable update (phase 1);
+// X is folded and R = B - K X computed in double words, then in FP64 for the
+// cases whose double-word residual meets its tolerance (the FP64 one decides
+// convergence) or has not dropped below half of its previous update's.  If the two residuals of a case then differ by more than 10 %,
+// the double-word error floor (about 2^-47 sum |K| |X|) is reached and the
+// updates are FP64 from then on.  Then the kernel resumes (phase 0 when it
+// finishes).
+int run_segmented(axia_ctx* ctx, const void* kern, int grid, MultiArgs& P) {
+  const int64_t nd = ctx->ndof;
+  const long long n = (long long)nd * NR;
+  const int g_res = (int)std::min<int64_t>((ctx->n_nodes + 7) / 8, (int64_t)ctx->sm_count * 8);
+  if ((size_t)g_res * 2 * NR > ctx->partial_slots) return set_error(ctx, AXIA_ERR_TOO_LARGE, "partials area too small");
+  const BsrMatM<float> M32{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval32, (long long)ctx->nbq};
+  const BsrMatM<double> M64{(int)ctx->n_nodes, ctx->d_qptr, ctx->d_qadj, ctx->d_bval64, (long long)ctx->nbq};
+  BatchState hs;
+  bool fp64_only = false;
+  P.resume = 0;
+  for (int seg = 0; seg < 100000; ++seg) {
+    const int phase_unset = -1;
+    AXIA_CUDA(ctx, cudaMemcpyAsync(&P.state->phase, &phase_unset, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
+    AXIA_TRY(launch_batch(ctx, kern, grid, P));
+    AXIA_CUDA(ctx, cudaMemcpyAsync(&hs, P.state, sizeof(BatchState), cudaMemcpyDeviceToHost, ctx->stream));
+    AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (hs.phase != 1) return AXIA_OK;  // finished, or stopped early (status / barrier limit)
+    auto residual = [&](bool dwr, unsigned cases) -> int {
+      if (dwr)
+        k_batch_resid<true><<<g_res, 256, 0, ctx->stream>>>(M32, ctx->d_bval32lo, M64, ctx->d_mB, ctx->d_mX,
+                                                             ctx->d_mXh, ctx->d_mXl, ctx->d_bdinv32, ctx->d_mR32,
+                                                             ctx->d_partials, cases);
+      else
+        k_batch_resid<false><<<g_res, 256, 0, ctx->stream>>>(M32, ctx->d_bval32lo, M64, ctx->d_mB, ctx->d_mX,
+                                                              ctx->d_mXh, ctx->d_mXl, ctx->d_bdinv32, ctx->d_mR32,
+                                                              ctx->d_partials, cases);
+      k_batch_resid_sum<<<2, NR * 32, 0, ctx->stream>>>(ctx->d_partials, g_res, ctx->d_totals);
+      ctx->launches += 2;
+      AXIA_CUDA(ctx, cudaGetLastError());
+      return AXIA_OK;
+    };
+    k_batch_fold<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(n, ctx->d_mX, ctx->d_mX32, ctx->d_mXh, ctx->d_mXl,
+                                                            fp64_only ? 0 : 1);
+    ctx->launches++;
+    AXIA_TRY(residual(!fp64_only, ~0u));
+    if (!fp64_only) {
+      double tot[NR];
+      AXIA_CUDA(ctx, cudaMemcpyAsync(tot, ctx->d_totals, sizeof(tot), cudaMemcpyDeviceToHost, ctx->stream));
+      AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      // the cases whose double-word residual meets tol or stalled: FP64 for them
+      unsigned check = 0;
+      for (int c = 0; c < NR; ++c) {
+        if (!hs.active[c]) continue;
+        const double rn = std::sqrt(tot[c]);
+        if (rn <= P.tol * hs.bnorm[c] || !(rn <= 0.5 * hs.rmax[c])) check |= 1u << c;
+      }
+      if (check) {
+        double t64[NR];
+        CaseList list{};
+        for (int c = 0; c < NR; ++c)
+          if ((check >> c) & 1u) list.c[list.n++] = c;
+        int kp = 1;
+        while (kp < list.n) kp <<= 1;
+        auto sub = [&](auto kern) {
+          kern<<<g_res, 256, 0, ctx->stream>>>(M64, ctx->d_mB, ctx->d_mX, ctx->d_bdinv32, ctx->d_mR32,
+                                               ctx->d_partials, list);
+        };
+        switch (kp) {
+          case 1: sub(k_batch_resid64_cases<1>); break;
+          case 2: sub(k_batch_resid64_cases<2>); break;
+          case 4: sub(k_batch_resid64_cases<4>); break;
+          case 8: sub(k_batch_resid64_cases<8>); break;
+          case 16: sub(k_batch_resid64_cases<16>); break;
+          default: sub(k_batch_resid64_cases<32>); break;
+        }
+        k_batch_resid_sum<<<2, NR * 32, 0, ctx->stream>>>(ctx->d_partials, g_res, ctx->d_totals);
+        ctx->launches += 2;
+        AXIA_CUDA(ctx, cudaGetLastError());
+        AXIA_CUDA(ctx, cudaMemcpyAsync(t64, ctx->d_totals, sizeof(t64), cudaMemcpyDeviceToHost, ctx->stream));
+        AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        // double-word and FP64 residuals apart by more than 10 %: the floor is reached
+        for (int c = 0; c < NR; ++c) {
+          if (!((check >> c) & 1u)) continue;
+          const double a = std::sqrt(tot[c]), b = std::sqrt(t64[c]);
+          if (!(std::fabs(a - b) <= 0.1 * b)) fp64_only = true;
+        }
+      }
+    }
+    P.resume = 1;
+  }
+  return set_error(ctx, AXIA_ERR_NOT_CONVERGED, "batched CG: too many segments");
+}
+
 int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const axia_solve_opts* opts,
                 axia_solve_info* info, double* rel_res) {
   if (!ctx->have_bsr64 || !ctx->have_bsr32)
@@ -1523,6 +1876,10 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
   const void* kern = coarse ? batch_kernel<true>(tile) : batch_kernel<false>(tile);
   int grid = 0;
   AXIA_TRY(batch_grid(ctx, kern, &grid));
+  // with the FP32 low parts assembled the reliable updates run in double words
+  // between segments of the kernel
+  const bool split = ctx->have_bsr32lo;
+  if (split) AXIA_TRY(ensure_segment_buffers(ctx));
   info->iters = 0;
   info->outer_iters = 0;
   double worst = 0.0;
@@ -1534,7 +1891,13 @@ int batch_solve(axia_ctx* ctx, int nrhs, const double* d_F, double* d_U, const a
     ctx->launches++;
     AXIA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBarrier), ctx->stream));
     MultiArgs P = multi_args(ctx, opts->rtol, delta, max_iter, cargs);
-    AXIA_TRY(timed_launch(ctx, info, [&]() -> int { return launch_batch(ctx, kern, grid, P); }));
+    if (split) {
+      P.state = static_cast<BatchState*>(ctx->d_mstate);
+      P.split = 1;
+      AXIA_TRY(timed_launch(ctx, info, [&]() -> int { return run_segmented(ctx, kern, grid, P); }));
+    } else {
+      AXIA_TRY(timed_launch(ctx, info, [&]() -> int { return launch_batch(ctx, kern, grid, P); }));
+    }
     MultiOut o;
     AXIA_CUDA(ctx, cudaMemcpyAsync(&o, ctx->d_mout, sizeof(MultiOut), cudaMemcpyDeviceToHost, ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -868,7 +868,9 @@ int bsr_solve(axia_ctx* ctx, const double* d_f, double* d_u, const axia_solve_op
   k_reconstruct_full<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(nd, ctx->d_ind_of, ctx->d_u0, ctx->d_xf, d_u);
   ctx->launches++;
   AXIA_CUDA(ctx, cudaGetLastError());
-  info->true_residual = bsr_residual(ctx, ctx->d_bf, ctx->d_xf);
+  // the mixed kernels end on an FP64 residual b - K x of the returned x (every
+  // convergence test is a reliable update's); the FP64 CG's is a recurrence
+  info->true_residual = mixed ? o.residual : bsr_residual(ctx, ctx->d_bf, ctx->d_xf);
   return AXIA_OK;
 }
 

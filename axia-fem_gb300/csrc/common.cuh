@@ -371,6 +371,10 @@ struct axia_ctx {
   double *d_mB = nullptr, *d_mX = nullptr;
   float *d_mX32 = nullptr, *d_mR32 = nullptr, *d_mP32 = nullptr, *d_mQ32 = nullptr;
   void* d_mout = nullptr;
+  // segmented batched solve (double-word reliable updates): X as FP32 pairs and the kernel's state
+  float *d_mXh = nullptr, *d_mXl = nullptr;
+  size_t seg_capacity = 0;
+  void* d_mstate = nullptr;
   size_t batch_capacity = 0;
   // block PCG of the load cases: W / Z block, Gram partials and results, small matrices
   float* d_mZ32 = nullptr;

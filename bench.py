@@ -437,12 +437,15 @@ def run_c4a(args):
     ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
     btc, btu, bus = ctx.autotune_batched()
 
+    # the FP32 low parts: reliable updates in double words between kernel segments
+    LO = L.ASM_BSR64 | L.ASM_BSR32 | L.ASM_BSR32LO
+
     def step_jacobi():
-        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        ctx.assemble_ex(LO)
         return ctx.solve_batched_device(32, F.data_ptr(), Uj.data_ptr(), rtol=RTOL, inner_rtol=args.delta)
 
     def step():
-        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        ctx.assemble_ex(LO)
         return ctx.solve_batched_device(32, F.data_ptr(), U.data_ptr(), rtol=RTOL, inner_rtol=args.delta,
                                         preconditioner=L.PRECOND_COARSE, coarse_nodes=args.coarse_nodes)
     Uj = torch.empty_like(F)
@@ -671,6 +674,8 @@ def main():
     ap.add_argument("--coarse-nodes", type=int, default=0,
                     help="nodes per subdomain of the coarse space (0: the library default, about 512 "
                          "subdomains of at least ~13,500 matrix node blocks)")
+    ap.add_argument("--fp64-updates", action="store_true",
+                    help="--only batch: FP64 reliable updates inside the kernel (no FP32 low parts)")
     ap.add_argument("--only", choices=["mixed", "coarse", "fp64", "spmv", "batch", "assemble"], default=None,
                     help="run one solve (or SpMV sweep) once and exit: the profiling entry")
     ap.add_argument("--max-iter", type=int, default=0, help="with --only: cap the CG iterations")
@@ -709,7 +714,7 @@ def main():
         m = meshgen.block_c3d8_multiload(n=args.n, nrhs=32)
         ctx = GpuContext(local)
         ctx.setup(m)
-        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
+        ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32 | (0 if args.fp64_updates else L.ASM_BSR32LO))
         F = torch.from_numpy(m.cload_batch).to(f"cuda:{local}")
         U = torch.empty_like(F)
         try:
@@ -718,7 +723,7 @@ def main():
             info, rel = ctx.solve_batched_device(32, F.data_ptr(), U.data_ptr(), rtol=RTOL, inner_rtol=args.delta,
                                                  max_iter=args.max_iter, krylov=kry, preconditioner=pre,
                                                  coarse_nodes=args.coarse_nodes)
-            print(json.dumps({"only": "batch", "iters": info.iters, "ms_kernel": info.ms_pcg_kernel}))
+            print(json.dumps({"only": "batch", "iters": info.iters, "updates": info.outer_iters, "ms_kernel": info.ms_pcg_kernel, "max_rel": float(max(rel))}))
         except Exception as e:  # a capped iteration count ends as NOT_CONVERGED
             print(json.dumps({"only": "batch", "status": str(e)[:120]}))
         torch.cuda.synchronize()

@@ -72,9 +72,9 @@ typedef enum axia_assemble_flags {
   AXIA_ASM_SYM32 = 16,  /* the FP32 node-block form in symmetric storage: each block K_ab, b >= a,
                            stored once (about half the bytes of AXIA_ASM_BSR32) */
   AXIA_ASM_BSR32LO = 32 /* with AXIA_ASM_BSR32: the FP32 low parts K64 - K32 of the node-block
-                           values, so K32 + K32lo holds K to 48 bits; the mixed node-block solves
-                           then compute their reliable updates b - K x in double-word arithmetic
-                           on the FP32 pipe and confirm convergence with one FP64 residual */
+                           values, so K32 + K32lo holds K to 48 bits; axia_gpu_solve_batched then
+                           computes its reliable updates B - K X in double-word arithmetic on the
+                           FP32 pipe and confirms convergence with an FP64 residual */
 } axia_assemble_flags;
 
 typedef enum axia_matrix_format {

@@ -91,3 +91,56 @@ def test_block_pcg_matches_direct_with_fewer_iterations(gpu_ctx, pre):
     assert ib.iters < i1.iters, (ib.iters, i1.iters)
     U2, _, _ = gpu_ctx.solve_batched(F, rtol=1e-10, krylov=_lib.KRYLOV_BLOCK, **pre)
     assert np.array_equal(U, U2)
+
+
+LO = _lib.ASM_BSR64 | _lib.ASM_BSR32 | _lib.ASM_BSR32LO
+
+
+@pytest.mark.parametrize("pre", [dict(), dict(preconditioner=_lib.PRECOND_COARSE, coarse_nodes=150)],
+                         ids=["jacobi", "coarse"])
+def test_batched_double_word_updates_match_direct(gpu_ctx, pre):
+    """With the FP32 low parts assembled (AXIA_ASM_BSR32LO) the batched solve
+    runs in segments and computes its reliable updates R = B - K X in double
+    words (FP32 pairs) between them; a case whose double-word residual meets
+    its tolerance is confirmed by an FP64 residual.  Every case equals its
+    direct solve to 1e-8 at rtol 1e-10, the per-case residual reported is at
+    most rtol, the solution matches the FP64-update solve, and a repeated solve
+    gives the same bits."""
+    m = meshgen.block_c3d8_multiload(n=10, nrhs=40)
+    F = m.cload_batch.copy()
+    F[5] = 0.0
+    gpu_ctx.setup(m).assemble_ex(LO)
+    U, info, rel = gpu_ctx.solve_batched(F, rtol=1e-10, **pre)
+    U2, info2, rel2 = gpu_ctx.solve_batched(F, rtol=1e-10, **pre)
+    assert np.all(rel <= 1e-10 * 1.0001) and info.outer_iters > 0
+    assert np.array_equal(U, U2) and np.array_equal(rel, rel2)
+    ref = _direct_all(m, F)
+    for c in range(F.shape[0]):
+        if c == 5:
+            assert np.all(U[c] == 0.0)
+            continue
+        assert np.linalg.norm(U[c] - ref[c]) <= 1e-8 * np.linalg.norm(ref[c]), c
+    gpu_ctx.assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+    U64, info64, rel64 = gpu_ctx.solve_batched(F, rtol=1e-10, **pre)
+    assert np.linalg.norm(U - U64) <= 1e-8 * np.linalg.norm(U64)
+
+
+def test_batched_double_word_updates_tight_and_ill_conditioned(gpu_ctx):
+    """rtol 1e-12, and a slender cantilever whose double-word residual floor
+    (about 2^-47 sum |K| |X|) lies above its tolerance: the solve switches to
+    FP64 updates and still meets rtol on the FP64 residual."""
+    m = meshgen.block_c3d8_multiload(n=8, nrhs=8)
+    gpu_ctx.setup(m).assemble_ex(LO)
+    U, info, rel = gpu_ctx.solve_batched(m.cload_batch, rtol=1e-12)
+    assert np.all(rel <= 1e-12 * 1.0001)
+    ref = _direct_all(m, m.cload_batch)
+    for c in range(8):
+        assert np.linalg.norm(U[c] - ref[c]) <= 1e-9 * np.linalg.norm(ref[c]), c
+    cm = meshgen.cantilever_c3d8()
+    F = np.stack([cm.cload * s for s in (1.0, -0.5, 2.0)])
+    gpu_ctx.setup(cm).assemble_ex(LO)
+    U, info, rel = gpu_ctx.solve_batched(F, rtol=1e-10)
+    assert np.all(rel <= 1e-10 * 1.0001)
+    for c in range(3):
+        r = O.solve_static(cm, solver=O.SOLVER_CHOLESKY, f=F[c])
+        assert np.linalg.norm(U[c] - r.u) <= 1e-8 * np.linalg.norm(r.u), c
