@@ -99,9 +99,13 @@ DW_FN void two_prod(float a, float b, float& p, float& e) {
 
 DW_FN dw dw_neg(dw a) { return dw{-a.h, -a.l}; }
 
-// An FP32 number as the FP64 number of the same value: normal numbers by
-// re-encoding their bits (exponent rebased by 1023 - 127, significand
-// shifted into place), zero, subnormals, inf and NaN by the conversion.
+// An FP32 number as the FP64 number of the same value, by re-encoding its
+// bits with integer operations only (no conversion instruction, which runs on
+// the FP64 pipe; a branch to one for the rare classes is if-converted by the
+// compiler and then executes on every call): normal numbers rebase the
+// exponent by 1023 - 127 and shift the significand into place, subnormals are
+// normalised from the position of their top bit, zero keeps its sign, and
+// inf / NaN keep the payload.
 DW_FN double f32_to_f64_exact(float f) {
   uint32_t u;
 #ifdef __CUDA_ARCH__
@@ -109,10 +113,25 @@ DW_FN double f32_to_f64_exact(float f) {
 #else
   std::memcpy(&u, &f, 4);
 #endif
-  const uint32_t mag = u & 0x7fffffffu;
-  if (mag - 0x00800000u >= 0x7f000000u) return (double)f;  // not a normal number
-  const uint32_t hi = (u & 0x80000000u) | ((mag >> 3) + ((1023u - 127u) << 20));
-  const uint32_t lo = mag << 29;
+  const uint32_t sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  uint32_t hi = sign | ((e + (1023u - 127u)) << 20) | (m >> 3), lo = m << 29;  // normal
+  if (e == 0xffu) hi = sign | 0x7ff00000u | (m >> 3);                          // inf, NaN
+  if (e == 0) {
+    if (m == 0) {  // zero
+      hi = sign;
+      lo = 0;
+    } else {       // subnormal: m 2^-149 with its top bit at p
+#ifdef __CUDA_ARCH__
+      const int p = 31 - __clz((int)m);
+#else
+      int p = 31;
+      while (!((m >> p) & 1u)) --p;
+#endif
+      const uint64_t frac = ((uint64_t)m << (52 - p)) & 0xfffffffffffffull;
+      hi = sign | ((uint32_t)(p + 874) << 20) | (uint32_t)(frac >> 32);
+      lo = (uint32_t)frac;
+    }
+  }
 #ifdef __CUDA_ARCH__
   return __hiloint2double((int)hi, (int)lo);
 #else
@@ -208,14 +227,19 @@ __device__ __forceinline__ double pow2(int e) {
 
 // x 2^-k as a double word from the bits of x with integer operations only:
 // h = its leading 24 significant bits, l = the next 24 (both truncated, so
-// |x 2^-k - h - l| < 2^-47 |x 2^-k|).  Zero, subnormal, non-finite and
-// out-of-range values (|x 2^-k| outside [2^-74, 2^127)) go through the FP64
-// conversion.
+// |x 2^-k - h - l| < 2^-47 |x 2^-k|); zero keeps its sign.  Subnormal,
+// non-finite and out-of-range values (|x 2^-k| outside [2^-74, 2^127)) go
+// through the FP64 conversion.
+// the rare classes of dw_split_scaled, out of line so that the FP64
+// instructions of this path are not executed speculatively on the common one
+static __device__ __noinline__ dw dw_split_scaled_slow(double x, int k) { return dw_from_double(x * pow2(-k)); }
+
 __device__ __forceinline__ dw dw_split_scaled(double x, int k) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  if ((b << 1) == 0) return dw{__uint_as_float((unsigned)(b >> 32)), 0.f};  // +-0
   const int e = (int)((b >> 52) & 0x7ff) - k;  // biased exponent of x 2^-k
   if ((unsigned)(e - 949) > (unsigned)(1150 - 949) || ((b >> 52) & 0x7ff) == 0 || ((b >> 52) & 0x7ff) == 0x7ff)
-    return dw_from_double(x * pow2(-k));
+    return dw_split_scaled_slow(x, k);
   const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
   const unsigned long long m = b & 0xfffffffffffffull;
   const float h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29));
