@@ -834,7 +834,7 @@ __global__ void __launch_bounds__(PCG_THREADS, 2) pcg_bsr_multi_kernel(MultiArgs
 // ---------------------------------------------------------------------------
 __global__ void k_batch_fold(long long n, double* X, float* X32, float* Xh, float* Xl, int split_dw) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const double x = X[t] + (double)X32[t];
+    const double x = X[t] + f32_to_f64_exact(X32[t]);  // no conversion instruction (FP64 pipe)
     X[t] = x;
     X32[t] = 0.f;
     if (split_dw) {
