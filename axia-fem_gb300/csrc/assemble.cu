@@ -287,7 +287,10 @@ int launch_element_ke(axia_ctx* ctx, const ElemArgs& args) {
   AXIA_TRY(ensure_tables(ctx, NN, NG, &tab));
   size_t smem;
   void (*kern)(ElemArgs, ElemTables);
-  if constexpr (DW) {
+  if constexpr (DW && NN == 20) {
+    smem = element_dw_pair_smem_bytes<NN, NG>(WARPS);
+    kern = element_ke_dw_pair_kernel<NN, NG, WARPS>;
+  } else if constexpr (DW) {
     smem = element_dw_smem_bytes<NN, NG>(WARPS);
     kern = element_ke_dw_kernel<NN, NG, WARPS>;
   } else {
@@ -322,12 +325,10 @@ int element_tables_for(axia_ctx* ctx, int nn, int ng, const double** dn, const d
 int run_hex8r_hourglass(axia_ctx* ctx, const ElemArgs& args);
 int run_hex8i_condense(axia_ctx* ctx, const ElemArgs& args, const double* dn_tab);
 
-// true when run_element_ke runs the double-word kernel for this kind: C3D8.
-// C3D20 / C3D20R keep the FP64 loop: their double-word form (1,830 entries
-// per element, 4 warps per SM by shared memory) measured slower than the
-// FP64 one, 23.3 against 22.2 ms for the 50^3 block.
+// true when run_element_ke runs a double-word kernel for this kind: C3D8
+// (element_ke_dw_kernel), C3D20 and C3D20R (element_ke_dw_pair_kernel).
 bool element_uses_dw(const axia_ctx* ctx, int nn, int reduced) {
-  return !ctx->element_fp64 && nn == 8 && reduced == 0;
+  return !ctx->element_fp64 && ((nn == 8 && reduced == 0) || nn == 20);
 }
 
 // nn = 8: reduced 1 = C3D8R (centre point + hourglass), 2 = C3D8I (incompatible modes)
@@ -345,8 +346,10 @@ int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args) {
   }
   const bool dw = element_uses_dw(ctx, nn, reduced);
   if (nn == 8) return dw ? launch_element_ke<8, 8, 8, true>(ctx, args) : launch_element_ke<8, 8, 8>(ctx, args);
-  if (nn == 20 && !reduced) return launch_element_ke<20, 27, 4>(ctx, args);
-  if (nn == 20 && reduced) return launch_element_ke<20, 8, 4>(ctx, args);
+  if (nn == 20 && !reduced)
+    return dw ? launch_element_ke<20, 27, 7, true>(ctx, args) : launch_element_ke<20, 27, 4>(ctx, args);
+  if (nn == 20 && reduced)
+    return dw ? launch_element_ke<20, 8, 8, true>(ctx, args) : launch_element_ke<20, 8, 4>(ctx, args);
   if (nn == 4) return launch_element_ke<4, 1, 8>(ctx, args);
   if (nn == 10) return launch_element_ke<10, 4, 8>(ctx, args);
   if (nn == 6) return launch_element_ke<6, 6, 8>(ctx, args);

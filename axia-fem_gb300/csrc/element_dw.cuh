@@ -1,5 +1,7 @@
-// element_dw.cuh -- C3D8 element stiffness with the Gauss loop on the FP32
-// pipe in double-word arithmetic (dword.cuh), one warp per element.
+// element_dw.cuh -- C3D8, C3D20 and C3D20R element stiffness with the Gauss
+// loop on the FP32 pipe in double-word arithmetic (dword.cuh), one warp per
+// element: element_ke_dw_kernel (C3D8, lanes own Ke entries) and
+// element_ke_dw_pair_kernel (20 nodes, lanes own 3x3 node blocks).
 //
 // The same restatement as element_ke_kernel (element.cuh; the reference's
 // hex8_stiffness, solver/src/elem.rs:194-219): Ke = sum_gp w det(J) B^T D B
@@ -268,4 +270,236 @@ element_ke_dw_kernel(ElemArgs args, ElemTables tab) {
   }
   if (lane == 0) bulk_wait_all();
   __syncwarp();
+}
+
+// C3D20 / C3D20R in double words, one warp per element, each lane owning
+// whole 3x3 node blocks: A_ab = sum_g h_a c_b^T for node pairs a <= b (210
+// for 20 nodes, 7 rounds of 32 lanes), from which the lane forms K_ab =
+// lam A_ab + mu A_ab^T + mu tr(A_ab) I in registers and stores K_ab and its
+// mirror K_ba straight to global memory.  Against the per-entry ownership of
+// element_ke_dw_kernel (which at 1,830 entries and 27 Gauss points had shared
+// memory for 4 warps per SM and measured slower than the FP64 loop) this
+// needs no A, trace or entry tables in shared memory, and each Gauss point
+// costs a lane 6 shared loads (h_a, c_b) for 9 multiply-adds instead of 2 per
+// multiply-add.  The Jacobians share c's space (they are dead before c is
+// formed).  On a diagonal pair (a == a) the entries i <= j are formed and
+// mirrored, so Ke is exactly symmetric like the other kernels' output.
+template <int NN, int NG>
+struct ElemDwPairTraits {
+  using T = ElemTraits<NN, NG>;
+  static constexpr int NR = (T::NB + 31) / 32;  // rounds of node pairs per lane
+  static constexpr int TAB = T::R2(NG * NN * 3 + NG + 2);
+  static constexpr int OFF_X = 0;
+  static constexpr int OFF_G = OFF_X + T::R2(T::NDOF);
+  static constexpr int OFF_S = OFF_G + T::R2(NG * 9);
+  static constexpr int OFF_C = OFF_S + T::R2(NG);
+  static constexpr int OFF_H = OFF_C + T::R2(NG * T::NDOF);
+  static constexpr int WARP_UNITS = OFF_H + T::R2(NG * T::NDOF);  // 8-byte units per warp
+  static_assert(NG * 9 <= NG * T::NDOF, "the Jacobians fit in c's space");
+};
+
+template <int NN, int NG>
+constexpr size_t element_dw_pair_smem_bytes(int warps) {
+  using D = ElemDwPairTraits<NN, NG>;
+  return (size_t)(D::TAB + warps * D::WARP_UNITS) * sizeof(double);
+}
+
+template <int NN, int NG, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+element_ke_dw_pair_kernel(ElemArgs args, ElemTables tab) {
+  using T = ElemTraits<NN, NG>;
+  using D = ElemDwPairTraits<NN, NG>;
+  extern __shared__ __align__(16) double smem[];
+  dw* s_dnw = reinterpret_cast<dw*>(smem);  // [NG*NN*3]
+  dw* s_w = s_dnw + NG * NN * 3;            // [NG]
+  dw* s_cm = s_w + NG;                      // [2]: c_lam, c_mu
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* W = smem + D::TAB + warp * D::WARP_UNITS;
+  dw* Xw = reinterpret_cast<dw*>(W + D::OFF_X);
+  dw* G = reinterpret_cast<dw*>(W + D::OFF_G);
+  dw* S = reinterpret_cast<dw*>(W + D::OFF_S);
+  dw* C = reinterpret_cast<dw*>(W + D::OFF_C);
+  dw* H = reinterpret_cast<dw*>(W + D::OFF_H);
+  dw* J = C;
+  for (int t = threadIdx.x; t < NG * NN * 3; t += blockDim.x) s_dnw[t] = dw_from_double(tab.dn[t]);
+  for (int t = threadIdx.x; t < NG; t += blockDim.x) s_w[t] = dw_from_double(tab.w[t]);
+  if (threadIdx.x == 0) {
+    s_cm[0] = dw_from_double(args.c_lam);
+    s_cm[1] = dw_from_double(args.c_mu);
+  }
+  __syncthreads();
+
+  const int64_t warps_total = (int64_t)gridDim.x * WARPS;
+  for (int64_t e = (int64_t)blockIdx.x * WARPS + warp; e < args.n_elem; e += warps_total) {
+    // 1. coordinates relative to node 0; 2^k above the largest difference
+    constexpr int PER = (T::NDOF + 31) / 32;
+    double dif[PER];
+    int emax = 0;
+#pragma unroll
+    for (int s = 0; s < PER; ++s) {
+      const int t = lane + 32 * s;
+      dif[s] = 0.0;
+      if (t < T::NDOF) {
+        double v, r;
+        if (args.conn) {
+          const int node = __ldg(args.conn + e * NN + t / 3);
+          const int node0 = __ldg(args.conn + e * NN);
+          v = __ldg(args.coords + 3 * (int64_t)node + (t % 3));
+          r = __ldg(args.coords + 3 * (int64_t)node0 + (t % 3));
+        } else {
+          v = __ldg(args.xyz + e * T::NDOF + t);
+          r = __ldg(args.xyz + e * T::NDOF + (t % 3));
+        }
+        if (!finite_bits(v)) record_error(args.status, e, AXIA_ERR_NONFINITE);
+        dif[s] = v - r;
+        const int be = (int)((__double_as_longlong(dif[s]) >> 52) & 0x7ff);
+        emax = max(emax, be == 0x7ff ? 0 : be);
+      }
+    }
+    emax = __reduce_max_sync(0xffffffffu, emax);
+    const int k = emax == 0 ? 0 : min(max(emax - 1022, -1000), 1000);
+    const double E = args.e_elem ? __ldg(args.e_elem + e) : args.e_const;
+#pragma unroll
+    for (int s = 0; s < PER; ++s) {
+      const int t = lane + 32 * s;
+      if (t < T::NDOF) Xw[t] = dw_split_scaled(dif[s], k);
+    }
+    __syncwarp();  // also: the previous element's c / h (J's space) are read
+    // 2. J[g][q][p] = sum_a dN_a/dxi_p x_a,q (quadratic.rs:122-146 via elem.rs:175-181)
+    for (int t = lane; t < NG * 9; t += 32) {
+      const int g = t / 9, q = (t % 9) / 3, p = t % 3;
+      const dw* dn = s_dnw + g * NN * 3;
+      dw_acc s;
+#pragma unroll 4
+      for (int a = 0; a < NN; ++a) dw_fma(s, dn[3 * a + p], Xw[3 * a + q]);
+      J[t] = dw_value(s);
+    }
+    __syncwarp();
+    // 3. cofactor matrix b[i][j] (invert3 before the 1/det scaling, elem.rs:18-26)
+    for (int t = lane; t < NG * 9; t += 32) {
+      const int g = t / 9, i = (t % 9) / 3, j = t % 3;
+      const dw* a = J + 9 * g;
+      const int j1 = (j + 1) % 3, j2 = (j + 2) % 3, i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+      dw_acc s;
+      dw_fma(s, a[3 * j1 + i1], a[3 * j2 + i2]);
+      dw_fma(s, dw_neg(a[3 * j1 + i2]), a[3 * j2 + i1]);
+      G[t] = dw_value(s);
+    }
+    __syncwarp();
+    double vol_part = 0.0;
+    for (int g = lane; g < NG; g += 32) {
+      const dw* a = J + 9 * g;
+      const dw* b = G + 9 * g;
+      dw_acc s;
+      dw_fma(s, a[0], b[0]);
+      dw_fma(s, a[1], b[3]);
+      dw_fma(s, a[2], b[6]);
+      const dw det_s = dw_value(s);
+      double det = dw_to_double(det_s);
+      if (k >= -340 && k <= 340) {
+        det *= pow2(3 * k);
+      } else {
+        const double p2k = pow2(k);
+        det = det * p2k * p2k * p2k;
+      }
+      if (!(fabs(det) >= 1e-18)) {
+        record_error(args.status, e, isfinite(det) ? AXIA_ERR_SINGULAR_JACOBIAN : AXIA_ERR_NONFINITE);
+        S[g] = s_w[g];
+      } else {
+        if (det <= 0.0) record_error(args.status, e, AXIA_ERR_NEG_JACOBIAN);
+        S[g] = dw_div(s_w[g], det_s);
+      }
+      vol_part += tab.w[g] * det;
+    }
+    if (!(__double_as_longlong(E) > 0 && __double_as_longlong(E) <= 0x7ff0000000000000ll)) {  // !(E > 0)
+      if (lane == 0) record_error(args.status, e, AXIA_ERR_MATERIAL);
+    }
+    if (args.vol_out) {
+      vol_part = warp_sum(vol_part);
+      if (lane == 0) args.vol_out[e] = vol_part;
+    }
+    __syncwarp();  // J is read; c overwrites it
+    // 4. c_a[i] = sum_p b[p][i] dN_a/dxi_p and h = (w/det) c at every Gauss point
+    for (int t = lane; t < NG * T::NDOF; t += 32) {
+      const int g = t / T::NDOF, r = t % T::NDOF, a = r / 3, i = r % 3;
+      const dw* b = G + 9 * g;
+      const dw* dn = s_dnw + (g * NN + a) * 3;
+      dw_acc s;
+      dw_fma(s, b[i], dn[0]);
+      dw_fma(s, b[3 + i], dn[1]);
+      dw_fma(s, b[6 + i], dn[2]);
+      const dw c = dw_value(s);
+      C[t] = c;
+      H[t] = dw_mul(S[g], c);
+    }
+    // lam and mu carry the 2^k of the scaled coordinates
+    dw lam, mu;
+    if (k >= -100 && k <= 100) {
+      const dw Ew = dw_split_scaled(E, 0);
+      lam = dw_scale(dw_mul(Ew, s_cm[0]), k);
+      mu = dw_scale(dw_mul(Ew, s_cm[1]), k);
+    } else {
+      lam = dw_from_double(E * args.c_lam * pow2(k));
+      mu = dw_from_double(E * args.c_mu * pow2(k));
+    }
+    __syncwarp();
+    // 5. node pairs p = lane + 32 r, a <= b in row order of the upper triangle
+    double* const ke = args.ke_out + e * T::KE;
+#pragma unroll 1
+    for (int r = 0; r < D::NR; ++r) {
+      const int p = lane + 32 * r;
+      int a = 0, rem = p < T::NB ? p : 0;
+      while (rem >= NN - a) {
+        rem -= NN - a;
+        ++a;
+      }
+      const int b = a + rem;
+      const dw* ha = H + 3 * a;
+      const dw* cb = C + 3 * b;
+      dw_acc acc[9];
+#pragma unroll 9
+      for (int g = 0; g < NG; ++g) {
+        dw hv[3], cv[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          hv[i] = ha[g * T::NDOF + i];
+          cv[i] = cb[g * T::NDOF + i];
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) dw_fma(acc[3 * i + j], hv[i], cv[j]);
+      }
+      if (p >= T::NB) continue;
+      dw av[9];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) av[t] = dw_value(acc[t]);
+      dw_acc ts;
+      dw_add(ts, av[0]);
+      dw_add(ts, av[4]);
+      dw_add(ts, av[8]);
+      const dw tr = dw_value(ts);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          if (a == b && i > j) continue;
+          dw_acc s;
+          dw_fma(s, lam, av[3 * i + j]);
+          dw_fma(s, mu, av[3 * j + i]);
+          if (i == j) dw_fma(s, mu, tr);
+          const dw v = dw_value(s);
+          const int row = 3 * a + i, col = 3 * b + j;
+          if (args.ke_dw) {
+            dw* kw = reinterpret_cast<dw*>(ke);
+            kw[row * T::NDOF + col] = v;
+            kw[col * T::NDOF + row] = v;
+          } else {
+            const double vd = dw_to_double(v);
+            ke[row * T::NDOF + col] = vd;
+            ke[col * T::NDOF + row] = vd;
+          }
+        }
+    }
+  }
 }

@@ -165,15 +165,16 @@ int launch(unsigned char* base, int kind, const ElemArgs& args) {
   tab.e0 = reinterpret_cast<const int*>(t + v.off_e0);
   tab.e1 = reinterpret_cast<const int*>(t + v.off_e1);
   tab.blk = reinterpret_cast<const int*>(t + v.off_blk);
-  // the context path's default kernels: double words for C3D8, FP64 for C3D20(R)
+  // the context path's default kernels: double words for C3D8 (per-entry
+  // lanes) and for C3D20(R) (node-pair lanes)
   size_t smem;
   void (*kern)(ElemArgs, ElemTables);
   if constexpr (NN == 8) {
     smem = element_dw_smem_bytes<NN, NG>(WARPS);
     kern = element_ke_dw_kernel<NN, NG, WARPS>;
   } else {
-    smem = element_smem_bytes<NN, NG>(WARPS);
-    kern = element_ke_kernel<NN, NG, WARPS>;
+    smem = element_dw_pair_smem_bytes<NN, NG>(WARPS);
+    kern = element_ke_dw_pair_kernel<NN, NG, WARPS>;
   }
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return AXIA_ERR_CUDA;
@@ -247,9 +248,9 @@ extern "C" AXIA_API int32_t axia_gpu_element_ke_noalloc(int32_t nn, int32_t redu
   if (nn == 8)
     st = launch<8, 8, 8>(base, 0, a);
   else if (!reduced)
-    st = launch<20, 27, 4>(base, 1, a);
+    st = launch<20, 27, 7>(base, 1, a);
   else
-    st = launch<20, 8, 4>(base, 2, a);
+    st = launch<20, 8, 8>(base, 2, a);
   if (st != AXIA_OK) return st;
   DevStatus hs;
   if (cudaMemcpy(ke, d_ke, sizeof(double) * n_elem * kesz, cudaMemcpyDeviceToHost) != cudaSuccess ||

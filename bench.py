@@ -380,9 +380,12 @@ def run_c3(args):
     f = torch.from_numpy(ctx.load_vector(m)).to(f"cuda:{local}")
     u64, umx = torch.empty_like(f), torch.empty_like(f)
 
-    def step64():
+    def step64():  # the reference's algorithm throughout (FP64 element stiffness too)
+        ctx.set_element_arith(L.ELEMENT_FP64)
         ctx.assemble_ex(L.ASM_CSR64)
-        return ctx.solve_device(f.data_ptr(), u64.data_ptr(), rtol=RTOL, spmv_lanes=args.lanes64)
+        info = ctx.solve_device(f.data_ptr(), u64.data_ptr(), rtol=RTOL, spmv_lanes=args.lanes64)
+        ctx.set_element_arith(L.ELEMENT_DWORD)
+        return info
 
     def stepmx():
         ctx.assemble_ex(L.ASM_BSR64 | L.ASM_BSR32)
@@ -691,7 +694,7 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    if args.workload != "c2":
+    if args.workload != "c2" and not (args.only == "assemble" and args.workload == "c3"):
         {"c3": run_c3, "c4a": run_c4a, "c4b": run_c4b, "c5": run_c5}[args.workload](args)
         return
 
@@ -729,7 +732,10 @@ def main():
         torch.cuda.synchronize()
         return
 
-    model = meshgen.block_c3d8_pressure(n=args.n)
+    if args.only == "assemble" and args.workload == "c3":
+        model = meshgen.block_c3d20_traction(n=args.n)  # the profiling entry of the C3D20 assembly
+    else:
+        model = meshgen.block_c3d8_pressure(n=args.n)
     ctx = GpuContext(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)

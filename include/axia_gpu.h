@@ -296,16 +296,17 @@ AXIA_API int64_t axia_gpu_sym_blocks(const axia_ctx* ctx, int64_t* lower_entries
  * (with Dirichlet elimination).  No reference counterpart. */
 AXIA_API int32_t axia_gpu_assemble_times(const axia_ctx* ctx, double* ms_element, double* ms_gather);
 
-/* Arithmetic of the C3D8 element stiffness, for axia_gpu_element_ke and
- * every later assembly on this context: AXIA_ELEMENT_DWORD (default) runs the
- * Gauss loop on the FP32 pipe in double-word arithmetic (pairs of FP32
- * numbers with error-free transformations, 48 significant bits; Ke within
- * about 3e-14 of max|Ke| of the exact element stiffness) and the assembly
- * sums the element contributions in double words too; AXIA_ELEMENT_FP64 runs
- * both in FP64 as the reference does (hex8_stiffness elem.rs:194-219,
- * analysis.rs:651-668).  GB300 executes FP64 at about 1/75 of its FP32 rate,
- * which bounds the FP64 form.  The other element kinds always use FP64 (the
- * C3D20 double-word form measured slower than its FP64 form).
+/* Arithmetic of the C3D8, C3D20 and C3D20R element stiffness, for
+ * axia_gpu_element_ke and every later assembly on this context:
+ * AXIA_ELEMENT_DWORD (default) runs the Gauss loop on the FP32 pipe in
+ * double-word arithmetic (pairs of FP32 numbers with error-free
+ * transformations, 48 significant bits; Ke within about 3e-14 of max|Ke| of
+ * the exact element stiffness) and the assembly sums the element
+ * contributions in double words too; AXIA_ELEMENT_FP64 runs both in FP64 as
+ * the reference does (hex8_stiffness elem.rs:194-219, hex20_stiffness
+ * quadratic.rs:122-146, analysis.rs:651-668).  GB300 executes FP64 at about
+ * 1/75 of its FP32 rate, which bounds the FP64 form.  The other element kinds
+ * (C3D4, C3D10, C3D6, C3D15, C3D8R, C3D8I) always use FP64.
  * axia_gpu_element_ke_noalloc uses the default. */
 enum axia_element_arith { AXIA_ELEMENT_DWORD = 0, AXIA_ELEMENT_FP64 = 1 };
 AXIA_API int32_t axia_gpu_set_element_arith(axia_ctx* ctx, int32_t arith);

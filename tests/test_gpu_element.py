@@ -123,18 +123,21 @@ def test_element_arith_matches_oracle_across_sizes_and_offsets(gpu_ctx, arith, n
         gpu_ctx.set_element_arith(_lib.ELEMENT_DWORD)
 
 
-def test_element_dword_close_to_fp64(gpu_ctx):
-    """The double-word Ke differs from the FP64 kernel's by a few 1e-14 of max|Ke|
-    on moderately distorted elements, and the two assemble the same K structure."""
-    xyz = _rand_elems(8, 500, seed=31)
-    ke_dw, vol_dw = gpu_ctx.element_ke(xyz, 2e5, 0.3)
+@pytest.mark.parametrize("nn,reduced", [(8, False), (20, False), (20, True)])
+def test_element_dword_close_to_fp64(gpu_ctx, nn, reduced):
+    """The double-word Ke (node-pair kernel for C3D20 / C3D20R) differs from the
+    FP64 kernel's by a few 1e-14 of max|Ke| on moderately distorted elements,
+    and is exactly symmetric like it."""
+    xyz = _rand_elems(nn, 500, seed=31 + nn + reduced)
+    ke_dw, vol_dw = gpu_ctx.element_ke(xyz, 2e5, 0.3, reduced=reduced)
     gpu_ctx.set_element_arith(_lib.ELEMENT_FP64)
     try:
-        ke64, vol64 = gpu_ctx.element_ke(xyz, 2e5, 0.3)
+        ke64, vol64 = gpu_ctx.element_ke(xyz, 2e5, 0.3, reduced=reduced)
     finally:
         gpu_ctx.set_element_arith(_lib.ELEMENT_DWORD)
     worst = max(np.abs(ke_dw[k] - ke64[k]).max() / np.abs(ke64[k]).max() for k in range(xyz.shape[0]))
     assert worst <= 1e-13, worst
+    assert all(np.array_equal(ke_dw[k], ke_dw[k].T) for k in range(xyz.shape[0]))
     assert np.abs(vol_dw - vol64).max() <= 1e-13 * np.abs(vol64).max()
     with pytest.raises(_lib.AxiaError) as e:
         gpu_ctx.set_element_arith(2)
