@@ -211,10 +211,17 @@ __device__ __forceinline__ void bsr_row_multi_half(int a, int lane, const BsrMat
 // Per-column partial sums of this block: v[c] is this thread's contribution
 // to column TC*(tid % (32/TC))+c (TC = 4: the float4 layout of the vector
 // phases).  Written to partials[(slot0 + col) * G + block].
+// one scratch for every instantiation of block_partials_cols (a __shared__
+// array inside the template is allocated once per instantiation: 8 KB each)
+__device__ __forceinline__ double (*cols_scratch())[NR] {
+  __shared__ double s_cols[PCG_THREADS / 32][NR];
+  return s_cols;
+}
+
 template <typename A, int TC = CPL>
 __device__ __forceinline__ void block_partials_cols(const A (&v)[TC], double* partials, int slot0) {
   constexpr int LG = NR / TC;
-  __shared__ double s_cols[32][NR];
+  double (*s_cols)[NR] = cols_scratch();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   double t[TC];
 #pragma unroll

@@ -144,3 +144,19 @@ def test_batched_double_word_updates_tight_and_ill_conditioned(gpu_ctx):
     for c in range(3):
         r = O.solve_static(cm, solver=O.SOLVER_CHOLESKY, f=F[c])
         assert np.linalg.norm(U[c] - r.u) <= 1e-8 * np.linalg.norm(r.u), c
+
+
+def test_batched_c3d20_matches_direct(gpu_ctx):
+    """C3D20 rows (up to 81 node blocks, longer than the SpMV's staged rows of
+    28 blocks) against direct solves, three load cases."""
+    m = meshgen.block_c3d20_traction(n=3)
+    gpu_ctx.setup(m).assemble_ex(_lib.ASM_BSR64 | _lib.ASM_BSR32)
+    f = gpu_ctx.load_vector(m)
+    rng = np.random.default_rng(11)
+    F = np.stack([f, -0.5 * f, f * rng.uniform(0.5, 2.0, f.shape)])
+    U, info, rel = gpu_ctx.solve_batched(F, rtol=1e-10)
+    assert np.all(rel <= 1e-10 * 1.0001)
+    ref = _direct_all(m, F)
+    for c in range(F.shape[0]):
+        err = np.linalg.norm(U[c] - ref[c]) / np.linalg.norm(ref[c])
+        assert err < 1e-8, (c, err)
