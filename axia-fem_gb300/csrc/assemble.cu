@@ -347,7 +347,7 @@ int run_element_ke(axia_ctx* ctx, int nn, int reduced, const ElemArgs& args) {
   const bool dw = element_uses_dw(ctx, nn, reduced);
   if (nn == 8) return dw ? launch_element_ke<8, 8, 8, true>(ctx, args) : launch_element_ke<8, 8, 8>(ctx, args);
   if (nn == 20 && !reduced)
-    return dw ? launch_element_ke<20, 27, 7, true>(ctx, args) : launch_element_ke<20, 27, 4>(ctx, args);
+    return dw ? launch_element_ke<20, 27, 14, true>(ctx, args) : launch_element_ke<20, 27, 4>(ctx, args);
   if (nn == 20 && reduced)
     return dw ? launch_element_ke<20, 8, 8, true>(ctx, args) : launch_element_ke<20, 8, 4>(ctx, args);
   if (nn == 4) return launch_element_ke<4, 1, 8>(ctx, args);

@@ -280,10 +280,13 @@ element_ke_dw_kernel(ElemArgs args, ElemTables tab) {
 // element_ke_dw_kernel (which at 1,830 entries and 27 Gauss points had shared
 // memory for 4 warps per SM and measured slower than the FP64 loop) this
 // needs no A, trace or entry tables in shared memory, and each Gauss point
-// costs a lane 6 shared loads (h_a, c_b) for 9 multiply-adds instead of 2 per
-// multiply-add.  The Jacobians share c's space (they are dead before c is
-// formed).  On a diagonal pair (a == a) the entries i <= j are formed and
-// mirrored, so Ke is exactly symmetric like the other kernels' output.
+// costs a lane 7 shared loads (c_a, c_b, w/det) for 9 multiply-adds instead
+// of 2 per multiply-add.  h_a = (w/det) c_a is formed by the lane (3
+// double-word products per Gauss point, the same values a stored h would
+// hold), so only c is kept per Gauss point: 15.6 KB per warp, 14 warps per
+// SM.  The Jacobians share c's space (they are dead before c is formed).  On
+// a diagonal pair (a == b) the entries i <= j are formed and mirrored, so Ke
+// is exactly symmetric like the other kernels' output.
 template <int NN, int NG>
 struct ElemDwPairTraits {
   using T = ElemTraits<NN, NG>;
@@ -293,8 +296,7 @@ struct ElemDwPairTraits {
   static constexpr int OFF_G = OFF_X + T::R2(T::NDOF);
   static constexpr int OFF_S = OFF_G + T::R2(NG * 9);
   static constexpr int OFF_C = OFF_S + T::R2(NG);
-  static constexpr int OFF_H = OFF_C + T::R2(NG * T::NDOF);
-  static constexpr int WARP_UNITS = OFF_H + T::R2(NG * T::NDOF);  // 8-byte units per warp
+  static constexpr int WARP_UNITS = OFF_C + T::R2(NG * T::NDOF);  // 8-byte units per warp
   static_assert(NG * 9 <= NG * T::NDOF, "the Jacobians fit in c's space");
 };
 
@@ -319,7 +321,6 @@ element_ke_dw_pair_kernel(ElemArgs args, ElemTables tab) {
   dw* G = reinterpret_cast<dw*>(W + D::OFF_G);
   dw* S = reinterpret_cast<dw*>(W + D::OFF_S);
   dw* C = reinterpret_cast<dw*>(W + D::OFF_C);
-  dw* H = reinterpret_cast<dw*>(W + D::OFF_H);
   dw* J = C;
   for (int t = threadIdx.x; t < NG * NN * 3; t += blockDim.x) s_dnw[t] = dw_from_double(tab.dn[t]);
   for (int t = threadIdx.x; t < NG; t += blockDim.x) s_w[t] = dw_from_double(tab.w[t]);
@@ -419,7 +420,7 @@ element_ke_dw_pair_kernel(ElemArgs args, ElemTables tab) {
       if (lane == 0) args.vol_out[e] = vol_part;
     }
     __syncwarp();  // J is read; c overwrites it
-    // 4. c_a[i] = sum_p b[p][i] dN_a/dxi_p and h = (w/det) c at every Gauss point
+    // 4. c_a[i] = sum_p b[p][i] dN_a/dxi_p at every Gauss point
     for (int t = lane; t < NG * T::NDOF; t += 32) {
       const int g = t / T::NDOF, r = t % T::NDOF, a = r / 3, i = r % 3;
       const dw* b = G + 9 * g;
@@ -428,9 +429,7 @@ element_ke_dw_pair_kernel(ElemArgs args, ElemTables tab) {
       dw_fma(s, b[i], dn[0]);
       dw_fma(s, b[3 + i], dn[1]);
       dw_fma(s, b[6 + i], dn[2]);
-      const dw c = dw_value(s);
-      C[t] = c;
-      H[t] = dw_mul(S[g], c);
+      C[t] = dw_value(s);
     }
     // lam and mu carry the 2^k of the scaled coordinates
     dw lam, mu;
@@ -443,7 +442,8 @@ element_ke_dw_pair_kernel(ElemArgs args, ElemTables tab) {
       mu = dw_from_double(E * args.c_mu * pow2(k));
     }
     __syncwarp();
-    // 5. node pairs p = lane + 32 r, a <= b in row order of the upper triangle
+    // 5. node pairs p = lane + 32 r, a <= b in row order of the upper triangle:
+    // A_ab = sum_g h_a c_b^T
     double* const ke = args.ke_out + e * T::KE;
 #pragma unroll 1
     for (int r = 0; r < D::NR; ++r) {
@@ -454,15 +454,16 @@ element_ke_dw_pair_kernel(ElemArgs args, ElemTables tab) {
         ++a;
       }
       const int b = a + rem;
-      const dw* ha = H + 3 * a;
+      const dw* ca = C + 3 * a;
       const dw* cb = C + 3 * b;
       dw_acc acc[9];
 #pragma unroll 9
       for (int g = 0; g < NG; ++g) {
         dw hv[3], cv[3];
+        const dw sg = S[g];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          hv[i] = ha[g * T::NDOF + i];
+          hv[i] = dw_mul(sg, ca[g * T::NDOF + i]);  // h_a = (w / det) c_a
           cv[i] = cb[g * T::NDOF + i];
         }
 #pragma unroll

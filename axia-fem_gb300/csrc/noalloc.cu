@@ -248,7 +248,7 @@ extern "C" AXIA_API int32_t axia_gpu_element_ke_noalloc(int32_t nn, int32_t redu
   if (nn == 8)
     st = launch<8, 8, 8>(base, 0, a);
   else if (!reduced)
-    st = launch<20, 27, 7>(base, 1, a);
+    st = launch<20, 27, 14>(base, 1, a);
   else
     st = launch<20, 8, 8>(base, 2, a);
   if (st != AXIA_OK) return st;
