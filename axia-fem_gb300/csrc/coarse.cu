@@ -904,7 +904,7 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     std::vector<double> hb((size_t)6 * bb_grid);
     const int cst = copy_to_host(ctx, hb.data(), d_bb, hb.size());
     if (cst) {
-      dev_free(d_bb);
+      dev_release(ctx, d_bb);
       return cst;
     }
     double lo[3] = {hb[0], hb[1], hb[2]}, hi[3] = {hb[3], hb[4], hb[5]};
@@ -939,14 +939,14 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     cell_base[k + 1] = cell_base[k] + g.nx * g.ny * g.nz;
     if (k == 0) S->h = h;
   }
-  dev_free(d_bb);
+  dev_release(ctx, d_bb);
   const int ncell = cell_base[nm];
   if (!S->per_mesh && ncell > max_boxes + nm)
     return set_error(ctx, AXIA_ERR_TOO_LARGE, "coarse space: more than " + std::to_string(max_boxes) + " subdomains");
   int *d_cell = nullptr, *d_count = nullptr, *d_sub = nullptr, *d_iota = nullptr, *d_cellsub = nullptr;
   int* d_sub_sorted = nullptr;
   double *d_centre = nullptr, *d_inv_h = nullptr;
-  void* d_temp = nullptr;
+  unsigned char* d_temp = nullptr;  // cub scratch (pooled)
   int st = AXIA_OK;
   do {
     if ((st = dev_alloc(ctx, &d_cell, (size_t)n))) break;
@@ -1034,7 +1034,7 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     while ((1 << bits) < n_sub && bits < 30) ++bits;
     cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, d_sub, d_sub_sorted, d_iota, S->sub_node, (int)n, 0, bits,
                                     ctx->stream);
-    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(temp_bytes, 16)));
+    if ((st = dev_alloc(ctx, &d_temp, std::max<size_t>(temp_bytes, 16)))) break;
     AXIA_CUDA(ctx, cub::DeviceRadixSort::SortPairs(d_temp, temp_bytes, d_sub, d_sub_sorted, d_iota, S->sub_node,
                                                    (int)n, 0, bits, ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1075,15 +1075,15 @@ int build_space(axia_ctx* ctx, CoarseState* S) {
     A.cnt = S->cnt;
     A.yc = S->yc;
   } while (false);
-  if (d_temp) cudaFree(d_temp);
-  dev_free(d_cell);
-  dev_free(d_count);
-  dev_free(d_sub);
-  dev_free(d_iota);
-  dev_free(d_cellsub);
-  dev_free(d_sub_sorted);
-  dev_free(d_centre);
-  dev_free(d_inv_h);
+  dev_release(ctx, d_temp);
+  dev_release(ctx, d_cell);
+  dev_release(ctx, d_count);
+  dev_release(ctx, d_sub);
+  dev_release(ctx, d_iota);
+  dev_release(ctx, d_cellsub);
+  dev_release(ctx, d_sub_sorted);
+  dev_release(ctx, d_centre);
+  dev_release(ctx, d_inv_h);
   return st;
 }
 
@@ -1112,7 +1112,7 @@ int build_item_structure(axia_ctx* ctx, CoarseState* S) {
   const int n = (int)ctx->n_nodes, n_sub = A.n_sub;
   int *d_cnt = nullptr, *d_iota = nullptr, *d_nruns = nullptr;
   unsigned* d_keys_sorted = nullptr;
-  void* d_temp = nullptr;
+  unsigned char* d_temp = nullptr;  // cub scratch (pooled)
   int st = AXIA_OK;
   do {
     if ((st = reset_dev_status(ctx))) break;
@@ -1125,11 +1125,10 @@ int build_item_structure(axia_ctx* ctx, CoarseState* S) {
     if ((st = read_status(ctx, "a node row touches more than 32 subdomains (raise coarse_nodes)"))) break;
     size_t tb = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, tb, d_cnt, S->off, n + 1, ctx->stream);
-    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
+    if ((st = dev_alloc(ctx, &d_temp, std::max<size_t>(tb, 16)))) break;
     AXIA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(d_temp, tb, d_cnt, S->off, n + 1, ctx->stream));
     if ((st = copy_to_host(ctx, &S->n_items, S->off + n, 1))) break;
-    cudaFree(d_temp);
-    d_temp = nullptr;
+    dev_release(ctx, d_temp);
     const int ni = std::max(S->n_items, 1);
     if ((st = dev_alloc(ctx, &S->keys, (size_t)ni))) break;
     if ((st = dev_alloc(ctx, &d_keys_sorted, (size_t)ni))) break;
@@ -1144,26 +1143,24 @@ int build_item_structure(axia_ctx* ctx, CoarseState* S) {
     while ((1ull << bits) < (unsigned long long)n_sub * n_sub && bits < 32) ++bits;
     cub::DeviceRadixSort::SortPairs(nullptr, tb, S->keys, d_keys_sorted, d_iota, S->perm, S->n_items, 0, bits,
                                     ctx->stream);
-    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
+    if ((st = dev_alloc(ctx, &d_temp, std::max<size_t>(tb, 16)))) break;
     AXIA_CUDA(ctx, cub::DeviceRadixSort::SortPairs(d_temp, tb, S->keys, d_keys_sorted, d_iota, S->perm, S->n_items,
                                                    0, bits, ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    cudaFree(d_temp);
-    d_temp = nullptr;
+    dev_release(ctx, d_temp);
     if ((st = dev_alloc(ctx, &S->run_key, (size_t)ni))) break;
     if ((st = dev_alloc(ctx, &S->run_cnt, (size_t)ni))) break;
     if ((st = dev_alloc(ctx, &S->run_off, (size_t)ni))) break;
     if ((st = dev_alloc(ctx, &d_nruns, 1))) break;
     cub::DeviceRunLengthEncode::Encode(nullptr, tb, d_keys_sorted, S->run_key, S->run_cnt, d_nruns, S->n_items,
                                        ctx->stream);
-    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
+    if ((st = dev_alloc(ctx, &d_temp, std::max<size_t>(tb, 16)))) break;
     AXIA_CUDA(ctx, cub::DeviceRunLengthEncode::Encode(d_temp, tb, d_keys_sorted, S->run_key, S->run_cnt, d_nruns,
                                                       S->n_items, ctx->stream));
     if ((st = copy_to_host(ctx, &S->n_runs, d_nruns, 1))) break;
-    cudaFree(d_temp);
-    d_temp = nullptr;
+    dev_release(ctx, d_temp);
     cub::DeviceScan::ExclusiveSum(nullptr, tb, S->run_cnt, S->run_off, S->n_runs, ctx->stream);
-    AXIA_CUDA(ctx, cudaMalloc(&d_temp, std::max<size_t>(tb, 16)));
+    if ((st = dev_alloc(ctx, &d_temp, std::max<size_t>(tb, 16)))) break;
     AXIA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(d_temp, tb, S->run_cnt, S->run_off, S->n_runs, ctx->stream));
     AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     const size_t ncp = (size_t)A.ncp;
@@ -1174,11 +1171,11 @@ int build_item_structure(axia_ctx* ctx, CoarseState* S) {
     if ((st = dev_alloc(ctx, &S->gj_bar, (size_t)GJ_GROUPS))) break;
     S->items_fresh = true;  // the values of this pass belong to the current K
   } while (false);
-  if (d_temp) cudaFree(d_temp);
-  dev_free(d_cnt);
-  dev_free(d_iota);
-  dev_free(d_nruns);
-  dev_free(d_keys_sorted);
+  dev_release(ctx, d_temp);
+  dev_release(ctx, d_cnt);
+  dev_release(ctx, d_iota);
+  dev_release(ctx, d_nruns);
+  dev_release(ctx, d_keys_sorted);
   return st;
 }
 

@@ -127,8 +127,8 @@ int device_exclusive_scan(axia_ctx* ctx, const int64_t* d_in, int64_t* d_out, in
   AXIA_CUDA(ctx, cudaMemcpyAsync(&last_out, d_out + (n - 1), sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
   AXIA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   *total = last_out + last_in;
-  dev_free(d_tot);
-  dev_free(d_tot_scan);
+  dev_release(ctx, d_tot);
+  dev_release(ctx, d_tot_scan);
   return AXIA_OK;
 }
 
@@ -177,7 +177,7 @@ static int fma_rate(axia_ctx* ctx, int iters, double* tflops) {
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  dev_free(sink);
+  dev_release(ctx, sink);
   AXIA_CUDA(ctx, cudaGetLastError());
   const double flops = 2.0 * NCH * (double)iters * (double)grid * 256.0;
   *tflops = flops / (best * 1e-3) / 1e12;
