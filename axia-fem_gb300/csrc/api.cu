@@ -278,10 +278,11 @@ int32_t axia_gpu_element_ke(axia_ctx* ctx, int32_t nn, int32_t reduced, int64_t 
                                     std::to_string(code) + ")");
     }
   } while (0);
-  dev_free(d_xyz);
-  dev_free(d_e);
-  dev_free(d_ke);
-  dev_free(d_vol);
+  cudaStreamSynchronize(ctx->stream);  // (error paths) before the blocks return to the pool
+  dev_release(ctx, d_xyz);
+  dev_release(ctx, d_e);
+  dev_release(ctx, d_ke);
+  dev_release(ctx, d_vol);
   return st;
 }
 
@@ -533,7 +534,8 @@ int32_t axia_gpu_solve_reduced(axia_ctx* ctx, const axia_dofmap* map, int64_t n_
                             cudaSuccess ||
                         cudaStreamSynchronize(ctx->stream) != cudaSuccess))
     st = set_error(ctx, AXIA_ERR_CUDA, "copy of u");
-  dev_free(du);
+  cudaStreamSynchronize(ctx->stream);
+  dev_release(ctx, du);
   S.release();
   return st;
 }
@@ -686,8 +688,9 @@ int32_t axia_gpu_element_energy(axia_ctx* ctx, const double* u_full, const doubl
                                        ctx->stream) != cudaSuccess ||
                         cudaStreamSynchronize(ctx->stream) != cudaSuccess))
     st = set_error(ctx, AXIA_ERR_CUDA, "copy of element energies");
-  dev_free(du);
-  dev_free(dv);
+  cudaStreamSynchronize(ctx->stream);
+  dev_release(ctx, du);
+  dev_release(ctx, dv);
   return st;
 }
 
@@ -785,8 +788,9 @@ int32_t axia_gpu_solve_batched(axia_ctx* ctx, int32_t nrhs, const double* F, dou
         cudaStreamSynchronize(ctx->stream) != cudaSuccess)
       st = set_error(ctx, AXIA_ERR_CUDA, "copy of batched solutions");
   }
-  dev_free(dF);
-  dev_free(dU);
+  cudaStreamSynchronize(ctx->stream);
+  dev_release(ctx, dF);
+  dev_release(ctx, dU);
   return st;
 }
 

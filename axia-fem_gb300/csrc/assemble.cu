@@ -1153,8 +1153,8 @@ int symbolic_setup(axia_ctx* ctx, int64_t n_bc, const int64_t* d_bc_dof, const d
     dev_release(ctx, d_qptr64);
   }
   // keep the 64-bit pointers for the gather
-  dev_free(ctx->d_ne_ptr);
-  dev_free(ctx->d_adj_ptr);
+  dev_release(ctx, ctx->d_ne_ptr);
+  dev_release(ctx, ctx->d_adj_ptr);
   ctx->d_ne_ptr = d_ne_ptr;
   ctx->d_adj_ptr = d_adj_ptr;
   dev_release(ctx, d_cnt);

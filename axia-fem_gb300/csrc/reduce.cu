@@ -159,17 +159,18 @@ int reduce_system(axia_ctx* ctx, const axia_dofmap* map, int64_t nt, const int64
   Runs Rk, Rr;
   int st = AXIA_OK;
   auto done = [&](int code) {
-    dev_free(di);
-    dev_free(dj);
-    dev_free(dv);
-    dev_free(df);
-    dev_free(cnt);
-    dev_free(off);
-    dev_free(val_ff);
-    dev_free(val_rhs);
-    dev_free(key_ff);
-    dev_free(key_rhs);
-    dev_free(dcount);
+    cudaStreamSynchronize(ctx->stream);  // the temporaries return to the pool idle
+    dev_release(ctx, di);
+    dev_release(ctx, dj);
+    dev_release(ctx, dv);
+    dev_release(ctx, df);
+    dev_release(ctx, cnt);
+    dev_release(ctx, off);
+    dev_release(ctx, val_ff);
+    dev_release(ctx, val_rhs);
+    dev_release(ctx, key_ff);
+    dev_release(ctx, key_rhs);
+    dev_release(ctx, dcount);
     Rk.release();
     Rr.release();
     return code;

@@ -204,8 +204,9 @@ int sort_runs(axia_ctx* ctx, const uint64_t* dk, const double* dv, int64_t nt, i
     k_run_heads<<<grid_for(ctx, nv), 256, 0, ctx->stream>>>(nv, out->key, pos, out->head);
     ctx->launches++;
   }
-  dev_free(flag);
-  dev_free(pos);
+  cudaStreamSynchronize(ctx->stream);  // the temporaries return to the pool idle
+  dev_release(ctx, flag);
+  dev_release(ctx, pos);
   if (st == AXIA_OK && cudaGetLastError() != cudaSuccess) st = set_error(ctx, AXIA_ERR_CUDA, "run kernels");
   return st;
 }
@@ -255,11 +256,12 @@ int raw_system_from_triplets(axia_ctx* ctx, int64_t n, int64_t nt, const int64_t
   Runs R;
   int st = AXIA_OK;
   auto done = [&](int code) {
-    dev_free(di);
-    dev_free(dj);
-    dev_free(dv);
-    dev_free(dk);
-    dev_free(dcount);
+    cudaStreamSynchronize(ctx->stream);  // the temporaries return to the pool idle
+    dev_release(ctx, di);
+    dev_release(ctx, dj);
+    dev_release(ctx, dv);
+    dev_release(ctx, dk);
+    dev_release(ctx, dcount);
     R.release();
     return code;
   };
@@ -326,7 +328,7 @@ int raw_system_from_csr(axia_ctx* ctx, int64_t n, const int64_t* h_indptr, const
   }
   if (st == AXIA_OK) st = finish_raw(ctx, n, nnz, fp32);
   cudaStreamSynchronize(ctx->stream);
-  dev_free(dp);
-  dev_free(dc);
+  dev_release(ctx, dp);
+  dev_release(ctx, dc);
   return st;
 }
