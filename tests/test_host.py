@@ -31,6 +31,32 @@ def test_library_exports_every_declared_symbol():
     assert lib.axia_gpu_abi_version() == 2
 
 
+def test_entry_points_reject_null_handles():
+    """Every entry point that takes a context (or a DOF map) returns
+    AXIA_ERR_INVALID_ARG, -1 for the size getters, for a null handle without
+    touching the device; destroy / free accept null."""
+    lib = _lib.load()
+    defaults = {ctypes.c_int32: 1, ctypes.c_int64: 1, ctypes.c_double: 0.3}
+    checked = 0
+    for name, res, args in _lib.SIGNATURES:
+        if not args or args[0] is not ctypes.c_void_p or name in ("axia_gpu_create",):
+            continue
+        if not (name.startswith("axia_gpu_") or name.startswith("axia_dofmap_")):
+            continue
+        call = [defaults.get(a) for a in args]
+        r = getattr(lib, name)(*call)
+        if res is None:
+            assert r is None, name
+        elif res is ctypes.c_char_p:
+            assert r, name
+        elif res is ctypes.c_int64:
+            assert r == -1, (name, r)
+        else:
+            assert r == _lib.ERR_INVALID_ARG, (name, r)
+        checked += 1
+    assert checked >= 40
+
+
 def test_struct_layouts_match_header():
     # field order and sizes of the ABI structs (x86-64 and aarch64 share them)
     assert ctypes.sizeof(_lib.Mesh) == 8 * 3 + 4 * 2 + 8 * 4
